@@ -1,0 +1,380 @@
+"""Benchmark of the GB300 BT-MZ / SP-MZ ADI time step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload bt-c|sp-c|bt-b|sp-a]
+
+A step is one time step of the node loop -- exch_qbc over all zones, then adi
+(compute_rhs, x/y/z line solves, add) over all zones -- on the workload's
+resident state.  The default workload is BT-MZ on the 480x320x28 grid split
+16x16 into geometrically growing zones (area ratio 20.8, 256 zones, dt 1e-4):
+the largest configuration, run batched (one launch per phase for all zones),
+with FP32 line solves refined against an FP64 residual, replayed as one CUDA
+graph per step.  Inputs are seeded synthetic manufactured solutions.
+
+`value` is Mgridpt-steps/s with the state resident in HBM (1.7 GB, far larger
+than the 129 MB L2, so no flush is needed); `e2e` is the same metric through
+the C ABI with the reference-layout arrays in page-locked host memory, copied
+in and out every step.  With N > 1 GPUs each rank runs an independent replica
+(the path's only exchange is on-device between zones of one GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "npbapps.jl_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    # name: (kind, class geometry, description)
+    "bt-c": ("BT", "C", "BT-MZ 480x320x28, 16x16 geometric zones (area ratio 20.8), dt 1e-4"),
+    "sp-c": ("SP", "C", "SP-MZ 480x320x28, 16x16 equal zones (30x20x28), dt 6.7e-4"),
+    "bt-b": ("BT", "B", "BT-MZ 304x208x17, 8x8 geometric zones (area ratio 20.05), dt 3e-4"),
+    "sp-a": ("SP", "A", "SP-MZ 128x128x16, 4x4 equal zones (32x32x16), dt 1.5e-3"),
+}
+SEED = 20261203
+# Algorithmic HBM bytes per grid point of each phase (FP64 state, line-solve
+# scratch kept out of the count): compute_rhs reads u and forcing and writes
+# rhs; each sweep reads u and rhs and writes rhs.
+BYTES_PER_POINT = {"rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+def geometry(npbmz, kind, cls):
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
+    k = npbmz.KINDS[kind]
+    nx, ny, nz, nbr = npbmz.zone_setup(k, gx, gy, gz, xz, yz, ratio)
+    return npbmz.Geometry(k, nx, ny, nz, nbr, gx, gy, gz, xz, yz), dt
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_steps(p, torch, stream, steps, warmup, dist=None):
+    p.step(warmup)
+    stream.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    p.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    return e0.elapsed_time(e1)
+
+
+def phase_times(p, npbmz, torch, stream, reps=3):
+    """Per-phase launch times (CUDA events on the launching stream)."""
+    names = ["exch", "rhs", "x", "y", "z"]
+    ph = [npbmz.PHASE_EXCH, npbmz.PHASE_RHS, npbmz.PHASE_XSOLVE, npbmz.PHASE_YSOLVE, npbmz.PHASE_ZSOLVE]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(ph) + 1)]
+    tot = np.zeros(len(ph))
+    for r in range(reps + 1):
+        ev[0].record(stream)
+        for i, x in enumerate(ph):
+            p.phase(x, -1)
+            ev[i + 1].record(stream)
+        stream.synchronize()
+        if r > 0:
+            tot += [ev[i].elapsed_time(ev[i + 1]) for i in range(len(ph))]
+    return dict(zip(names, (tot / reps).tolist()))
+
+
+def cpu_baseline(kind, cls, ce, target_s=15.0):
+    """The oracle (CPU restatement of the reference path) on the host cores,
+    OpenMP over zones like the reference's Threads.@threads: a bounded sample
+    of the same workload."""
+    from oracle import oracle
+
+    import npbmz
+
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
+    k = npbmz.KINDS[kind]
+    nx, ny, nz, nbr = oracle.zone_setup(k, gx, gy, gz, xz, yz, ratio)
+    pts = int(np.sum(nx.astype(np.int64) * ny * nz))
+    o = oracle.Oracle(k, nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, ce)
+    t0 = time.perf_counter()
+    o.step(1)
+    t1 = time.perf_counter() - t0
+    n = max(1, min(50, int(target_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.step(n)
+    t = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": pts * n / t / 1e6, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n} full time steps of the {kind}-MZ class {cls} grid ({pts} points, all zones) after 1 untimed step"}
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    import npbmz
+
+    kind, cls, desc = WORKLOADS[args.workload]
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
+    from oracle import oracle
+
+    k = npbmz.KINDS[kind]
+    nx, ny, nz, nbr = oracle.zone_setup(k, gx, gy, gz, xz, yz, ratio)
+    ce, _ = npbmz.seeded_coefficients(SEED, nx, ny, nz, gx, gy, gz, xz, yz)
+    pts = int(np.sum(nx.astype(np.int64) * ny * nz))
+    o = oracle.Oracle(k, nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, ce)
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    t = time.perf_counter() - t0
+    value = pts * args.steps / t / 1e6
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {
+        "impl": "reference", "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "points": pts, "zones": len(nx), "variant": "reference CPU path (oracle port), FP64"},
+        "cpu_baseline": {"value": value, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full time steps after {args.warmup} warm-up steps"},
+        "e2e": {"value": value, "unit": "Mgridpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    import npbmz
+
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+        dist = tdist
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    kind, cls, desc = WORKLOADS[args.workload]
+    g, dt = geometry(npbmz, kind, cls)
+    pts = g.points
+    ce, escale = npbmz.seeded_coefficients(SEED, g.nx, g.ny, g.nz, g.gx, g.gy, g.gz, g.x_zones, g.y_zones)
+    flags = {"mixed-graph": npbmz.MIXED | npbmz.GRAPH, "fp64-graph": npbmz.GRAPH,
+             "mixed": npbmz.MIXED, "fp64": 0}[args.variant]
+
+    def make(fl):
+        p = npbmz.Problem(g, dt, fl)
+        p.set_stream(stream.cuda_stream)
+        p.setup(ce)
+        return p
+
+    p = make(flags)
+    if args.autotune:
+        p.autotune()
+        p.setup(ce)
+    with ClockSampler(local) as clk:
+        ms = time_steps(p, torch, stream, args.steps, args.warmup, dist)
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = pts * world * args.steps / (ms_max * 1e-3) / 1e6
+    launches = p.launches_per_step * args.steps
+
+    extra = {}
+    if rank == 0 and args.quick:
+        ph = phase_times(p, npbmz, torch, stream)
+        extra["phase_ms"] = ph
+    elif rank == 0:
+        # per-phase launch times of the timed variant -> dominant kernel roofline
+        ph = phase_times(p, npbmz, torch, stream)
+        top = max((k for k in ph if k != "exch"), key=lambda k: ph[k])
+        pk = peaks()
+        hbm = float(pk.get("hbm_gbs", 6800.0))
+        achieved = BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
+        traffic = None
+        tfile = ROOT / "profiles" / "ncu_traffic.json"
+        if tfile.exists():
+            try:
+                tr = json.loads(tfile.read_text()).get(args.workload, {}).get(args.variant, {}).get(top)
+                traffic = tr
+            except Exception:
+                traffic = None
+        fp64 = npbmz.fp64_peak_gflops()
+        extra["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "traffic": traffic,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
+                             "bytes_per_point": BYTES_PER_POINT[top], "launch_ms": ph[top]}
+        extra["phase_ms"] = ph
+        extra["fp64_peak_gflops_measured"] = fp64
+        # variants (fewer steps each)
+        var = {}
+        nv = max(3, min(args.steps, 10))
+        for name, fl in (("fp64_batched", 0), ("fp64_exact_batched", npbmz.EXACT),
+                         ("mixed_batched", npbmz.MIXED), ("mixed_batched_graph", npbmz.MIXED | npbmz.GRAPH),
+                         ("fp64_batched_graph", npbmz.GRAPH), ("fp64_perzone", npbmz.PERZONE)):
+            q = make(fl)
+            steps_v = 2 if fl & npbmz.PERZONE else nv
+            mv = time_steps(q, torch, stream, steps_v, 1)
+            var[name] = pts * steps_v / (mv * 1e-3) / 1e6
+            q.close()
+        extra["variants_mgridpt_steps_per_s"] = var
+        # accuracy of the timed variant against the plain FP64 GPU path (which
+        # the parity tests hold to the oracle) over the measured number of steps
+        nacc = args.warmup + args.steps
+        a = make(0)
+        a.step(nacc)
+        xa = np.concatenate(a.verify())
+        a.close()
+        b = make(flags)
+        b.step(nacc)
+        xb = np.concatenate(b.verify())
+        b.close()
+        extra["accuracy"] = {"steps": nacc, "max_rel_err_final_norms_vs_fp64": float(np.max(np.abs(xb - xa) / np.abs(xa)))}
+        # e2e through the C ABI: reference-layout u in page-locked host memory,
+        # uploaded and downloaded every step
+        sizes = [npbmz.ref_elems(g.kind, npbmz.U, int(g.nx[z]), int(g.ny[z]), int(g.nz[z])) for z in range(g.nzones)]
+        host = torch.empty(int(sum(sizes)), dtype=torch.float64, pin_memory=True)
+        q = make(flags)
+        q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, host.data_ptr(), False)
+        ptr = host.data_ptr()
+        for _ in range(args.warmup):
+            q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, True, sync=False)
+            q.step(1)
+            q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, False, sync=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, True, sync=False)
+            q.step(1)
+            q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, False, sync=True)
+        te = time.perf_counter() - t0
+        q.close()
+        moved = 5 * 8 * pts
+        extra["e2e"] = {"value": pts * world * args.steps / te / 1e6, "unit": "Mgridpt-steps/s",
+                        "h2d_bytes_per_step": moved, "d2h_bytes_per_step": moved,
+                        "path": "npbmz_upload_async/npbmz_step/npbmz_download(zone=-1, NPBMZ_LAYOUT_REF) on page-locked "
+                                "reference-layout u (interior points read/written in place by one kernel each way)"}
+        if not args.no_cpu_baseline:
+            extra["cpu_baseline"] = cpu_baseline(kind, cls, ce)
+    if rank == 0:
+        line = {
+            "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if flags & npbmz.MIXED else "f64",
+            "data": "synthetic",
+            "config": {"workload": desc, "points_per_gpu": pts, "zones": g.nzones, "variant": args.variant,
+                       "batched": True, "cuda_graph": bool(flags & npbmz.GRAPH),
+                       "line_solves": "fp32 + fp64-residual refinement" if flags & npbmz.MIXED else "fp64",
+                       "seed": SEED, "energy_row_scale": 2 ** escale,
+                       "l2": "state 1.7 GB >> 129 MB L2; no flush needed", "parallelism": f"replicas x{world}"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    p.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bt-c", choices=sorted(WORKLOADS))
+    ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed", "fp64"])
+    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the timed variant and its phase times (for profiler runs)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,179 @@
+/* npbmz.h -- C ABI of libnpbmz_gpu.so, the GB300 (sm_103a) ADI time step of
+ * the NPBApps.jl BT-MZ and SP-MZ solvers.
+ *
+ * The reference has no plugin API: its seam is the pair of Julia calls in the
+ * node time loop, exch_qbc(...) then adi(iz, ...) per zone
+ * (src/BT/bt-node.jl:286-395, src/SP/sp-node.jl:258-397).  Each entry point
+ * below names the reference function it replaces.  Every call returns an int
+ * status (0 = success, negative = error; npbmz_last_error() gives the text);
+ * no C++ exception crosses the ABI.  A handle is not re-entrant: calls on one
+ * handle must come from one thread at a time.  All device work of a handle is
+ * issued on the handle's stream (npbmz_set_stream), asynchronously unless the
+ * entry point says otherwise.
+ *
+ * Field arrays exchanged with the host use one of two layouts:
+ *   NPBMZ_LAYOUT_DENSE  per zone, [m][k][j][i] with m = 0..4, k < nz, j < ny,
+ *                       i < nx (i fastest), nx*ny*nz*5 doubles;
+ *   NPBMZ_LAYOUT_REF    the reference's own OffsetArray memory for one zone
+ *                       (ncells = 1), column-major, pointer to the first
+ *                       element of the parent array:
+ *                         BT u       [1:5, -2:IMAX+1, -2:JMAX+1, -2:KMAX+1]  (src/BT/bt_data.jl:143-144)
+ *                         BT rhs     [1:5, -1:IMAX-1, -1:JMAX-1, -1:KMAX-1]  (src/BT/bt_data.jl:148-149)
+ *                         BT forcing [1:5,  0:IMAX-1,  0:JMAX-1,  0:KMAX-1]  (src/BT/bt_data.jl:138-139)
+ *                         SP u       [-2:IMAXP+1, -2:JMAXP+1, -2:KMAX+1, 1:5] (src/SP/sp_data.jl:115-116)
+ *                         SP rhs, forcing [0:IMAXP-1, 0:JMAXP-1, 0:KMAX-1, 1:5] (src/SP/sp_data.jl:160-166)
+ *                       with IMAX = nx+1, JMAX = ny+1, KMAX = nz+1,
+ *                       IMAXP = 2*(IMAX/2)+1, JMAXP = 2*(JMAX/2)+1.
+ *                       Only the points 0..n-1 of each axis are read or
+ *                       written; the halo is left untouched.
+ */
+#ifndef NPBMZ_H
+#define NPBMZ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct npbmz_handle npbmz_t;
+
+/* problem kinds */
+#define NPBMZ_BT 0
+#define NPBMZ_SP 1
+
+/* variant flags (npbmz_create) */
+#define NPBMZ_EXACT   0x1  /* FP64 kernels built without FMA contraction, in the
+                              reference's operation order: bit-for-bit the
+                              reference's arithmetic */
+#define NPBMZ_MIXED   0x2  /* line solves in FP32 on the FP64 rhs, refined once
+                              against an FP64 residual of the line operator
+                              (compute_rhs, add, exch_qbc and the norms stay
+                              FP64) */
+#define NPBMZ_PERZONE 0x4  /* one launch per zone per phase, the reference's
+                              per-zone adi order; default is all zones batched
+                              in one launch per phase */
+#define NPBMZ_GRAPH   0x8  /* npbmz_step replays one captured CUDA graph per step */
+#define NPBMZ_PERSIST 0x10 /* line solves run as persistent kernels (one CTA set
+                              per SM pulling zone x line work items) */
+#define NPBMZ_FP32_NOREFINE 0x20 /* FP32 line solves without the refinement
+                              pass (the error of plain FP32 solves, for
+                              comparison); implies NPBMZ_MIXED */
+
+/* field selectors */
+#define NPBMZ_U       0
+#define NPBMZ_RHS     1
+#define NPBMZ_FORCING 2
+
+/* host layouts */
+#define NPBMZ_LAYOUT_DENSE 0
+#define NPBMZ_LAYOUT_REF   1
+
+/* single phases (npbmz_phase) */
+#define NPBMZ_PHASE_RHS     0  /* compute_rhs, plus txinvr for SP */
+#define NPBMZ_PHASE_XSOLVE  1  /* x sweep (+ ninvr for SP) */
+#define NPBMZ_PHASE_YSOLVE  2  /* y sweep (+ pinvr for SP) */
+#define NPBMZ_PHASE_ZSOLVE  3  /* z sweep (+ tzetar for SP), without add */
+#define NPBMZ_PHASE_ADD     4  /* u += rhs on the interior */
+#define NPBMZ_PHASE_EXCH    5  /* exch_qbc over all zones */
+#define NPBMZ_PHASE_RHSONLY 6  /* compute_rhs only (SP: no txinvr) */
+
+/* Zone geometry of src/BT/zone_setup.jl:1-77 (SP: src/SP/zone_setup.jl:1-78).
+ * nx, ny, nz receive x_zones*y_zones sizes (zone number (i-1)+(j-1)*x_zones);
+ * nbr receives 4 ints per zone: west, east, south, north (0-based). */
+int npbmz_zone_setup(int kind, int gx, int gy, int gz, int x_zones, int y_zones, double ratio, int* nx, int* ny,
+                     int* nz, int* nbr);
+
+/* Seeded manufactured-solution coefficients, written row-major [5][13] into
+ * ce.  Every coefficient is drawn U(0.5, 2.0) from a SplitMix64 stream seeded
+ * with `seed`; the energy row is then multiplied by the smallest power of two
+ * 2^e (e >= 0) such that rho > 0 and rhoE - |rho v|^2/(2 rho) >= 0.25 rhoE
+ * hold for the exact solution and for the transfinite interpolation of its
+ * face values at every grid coordinate the zones of this geometry use
+ * (i*dnxm1 for i < max nx, and so on).  Returns e (>= 0) or a negative error.
+ * No counterpart in the reference, whose ce table is fixed
+ * (src/BT/set_constants.jl:47-51). */
+int npbmz_seeded_coefficients(uint64_t seed, int nzones, const int* nx, const int* ny, const int* nz, int gx, int gy,
+                              int gz, int x_zones, int y_zones, double* ce);
+
+/* Create a handle on the current CUDA device and allocate every device buffer
+ * it will use.  params = {dt, gx, gy, gz, x_zones, y_zones}: set_constants
+ * (src/BT/set_constants.jl:53-130) is evaluated from them.  nbr as written by
+ * npbmz_zone_setup.  Replaces alloc_field_space + set_constants
+ * (src/BT/bt_data.jl:106, src/BT/bt-node.jl:63-93). */
+int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* nz, const int* nbr,
+                 const double* params, int variant_flags, npbmz_t** out);
+
+/* Device-side initialize + exact_rhs for all zones from the 5x13
+ * coefficient table ce (row-major [5][13]); also records the exact solution
+ * for the error norm.  Replaces initialize, lhsinit and exact_rhs
+ * (src/BT/initialize.jl:6,229; src/BT/exact_rhs.jl:5; SP counterparts). */
+int npbmz_setup(npbmz_t* h, const double* ce);
+
+/* Host <-> device transfer of one field of one zone (zone >= 0), or of all
+ * zones (zone = -1: the host buffer holds every zone's array back to back in
+ * zone order).  The host buffer is read/written before the call returns. */
+int npbmz_upload(npbmz_t* h, int zone, int field, int layout, const double* host);
+int npbmz_download(npbmz_t* h, int zone, int field, int layout, double* host);
+
+/* Asynchronous variants: the host buffer must stay valid (and, for full
+ * overlap, be page-locked) until the stream has passed the copy. */
+int npbmz_upload_async(npbmz_t* h, int zone, int field, int layout, const double* host);
+int npbmz_download_async(npbmz_t* h, int zone, int field, int layout, double* host);
+
+/* exch_qbc: copy every zone's interior boundary planes into its periodic
+ * neighbours' ghost planes on the device.  Replaces exch_qbc
+ * (src/BT/exchange_qbc.jl:1-122, src/SP/exchange_qbc.jl:1-122). */
+int npbmz_exch_qbc(npbmz_t* h);
+
+/* adi: one ADI step (compute_rhs, x/y/z solves, add) for one zone, or for all
+ * zones (zone = -1, batched).  Replaces adi (src/BT/adi.jl:5-251,
+ * src/SP/adi.jl:6-258). */
+int npbmz_adi(npbmz_t* h, int zone);
+
+/* nsteps time steps of exch_qbc + adi(all zones), the body of the node time
+ * loop (src/BT/bt-node.jl:280-395).  norms (nullable, host) receives 10
+ * doubles per step: xcr[5] (sum over zones of rhs_norm/dt of that step's
+ * compute_rhs) then xce[5] (sum over zones of error_norm after the step).
+ * Synchronous when norms != NULL. */
+int npbmz_step(npbmz_t* h, int nsteps, double* norms);
+
+/* The node part of verify (src/BT/verify.jl:411-505): error_norm of u, then
+ * compute_rhs without an exchange, rhs_norm; sums over zones.  Synchronous. */
+int npbmz_verify(npbmz_t* h, double* xcr, double* xce);
+
+/* One phase (NPBMZ_PHASE_*) for one zone or all zones (zone = -1). */
+int npbmz_phase(npbmz_t* h, int phase, int zone);
+
+/* Use `stream` (a cudaStream_t, NULL = the legacy default stream) for all
+ * later work of the handle. */
+int npbmz_set_stream(npbmz_t* h, void* stream);
+int npbmz_synchronize(npbmz_t* h);
+
+/* Autotune the launch shapes (threads per block and work-item size per
+ * phase and zone-size bucket) by timing candidates on the handle's own data.
+ * Leaves u, rhs and forcing as they were.  Synchronous. */
+int npbmz_autotune(npbmz_t* h);
+
+/* Measured FP64 FMA throughput of the current device in GFLOP/s (an FMA
+ * counts 2 flops): the denominator of the FP64 roofline of the step kernels.
+ * No counterpart in the reference. */
+int npbmz_fp64_peak(double* gflops);
+
+/* Query: number of kernel launches npbmz_step issues per step, device bytes
+ * held by the handle, and (info, n) a small summary string. */
+int npbmz_launches_per_step(npbmz_t* h);
+int64_t npbmz_device_bytes(npbmz_t* h);
+int npbmz_describe(npbmz_t* h, char* buf, size_t n);
+
+/* Error text of the last failing call on h (h may be NULL for create). */
+const char* npbmz_last_error(npbmz_t* h);
+
+/* Free every device buffer and the handle. */
+int npbmz_destroy(npbmz_t* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NPBMZ_H */

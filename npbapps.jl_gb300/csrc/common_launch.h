@@ -1,0 +1,21 @@
+// common_launch.h -- host launchers of common_kernels.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "npbmz_internal.cuh"
+
+namespace npbmz {
+void launch_initialize(const Fields& F, const Consts& K, const double* ce, const Work* work, int nwork, double* uex,
+                       cudaStream_t s);
+void launch_exact_rhs(const Fields& F, const Consts& K, const double* ce, const Work* work, int nwork, double* forcing,
+                      cudaStream_t s);
+void launch_exch_qbc(const Fields& F, const int* nbr_dev, int zone_lo, int nz_count, int max_face, cudaStream_t s);
+void launch_err_partials(const Fields& F, const Work* work, int nwork, double* partials, cudaStream_t s);
+void launch_norm_finish(const ZoneDev* zones, const double* partials, const int* zblk, int nzones, double scale,
+                        double* out, cudaStream_t s);
+void launch_convert(const Fields& F, double* planes, double* stage, const int64_t* soff, int64_t sub, int zone_lo,
+                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s);
+void launch_fill(double* a, int64_t n, double v, cudaStream_t s);
+int probe_fp64(double* gflops);
+}  // namespace npbmz

@@ -1,0 +1,932 @@
+// npbmz_api.cu -- the C ABI of libnpbmz_gpu.so (declared in include/npbmz.h):
+// handle, HBM buffers, zone x point / zone x line work lists, phase
+// orchestration, CUDA-graph capture of a step, norms and the autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/npbmz.h"
+#include "common_launch.h"
+#include "npbmz_internal.cuh"
+#include "step_launch.h"
+
+using namespace npbmz;
+
+namespace {
+
+constexpr int PTS_TPB = 128;   // points per CTA of the point kernels (power of two)
+
+std::string g_create_error;
+
+Consts make_consts(double dt, int gx, int gy, int gz, int xz, int yz) {
+  // set_constants, src/BT/set_constants.jl:1-130 (SP: the same file body)
+  Consts k;
+  std::memset(&k, 0, sizeof(k));
+  k.c1 = 1.4e0; k.c2 = 0.4e0; k.c3 = 0.1e0; k.c4 = 1.0e0; k.c5 = 1.4e0;
+  k.bt = std::sqrt(0.5e0);
+  k.c1c2 = k.c1 * k.c2; k.c1c5 = k.c1 * k.c5; k.c3c4 = k.c3 * k.c4; k.c1345 = k.c1c5 * k.c3c4;
+  k.conz1 = (1.0e0 - k.c1c5);
+  k.dx1 = k.dx2 = k.dx3 = k.dx4 = k.dx5 = 0.75e0;
+  k.dy1 = k.dy2 = k.dy3 = k.dy4 = k.dy5 = 0.75e0;
+  k.dz1 = k.dz2 = k.dz3 = k.dz4 = k.dz5 = 1.0e0;
+  k.dxmax = std::max(k.dx3, k.dx4); k.dymax = std::max(k.dy2, k.dy4); k.dzmax = std::max(k.dz2, k.dz3);
+  k.dssp = 0.25e0 * std::max(k.dx1, std::max(k.dy1, k.dz1));
+  k.c2iv = 2.5e0; k.con43 = 4.0e0 / 3.0e0; k.con16 = 1.0e0 / 6.0e0;
+  k.dt = dt;
+  k.dnxm1 = 1.0e0 / ((double)(gx - 1) / (double)xz);
+  k.dnym1 = 1.0e0 / ((double)(gy - 1) / (double)yz);
+  k.dnzm1 = 1.0e0 / (double)(gz - 1);
+  k.tx1 = 1.0e0 / (k.dnxm1 * k.dnxm1); k.tx2 = 1.0e0 / (2.0e0 * k.dnxm1); k.tx3 = 1.0e0 / k.dnxm1;
+  k.ty1 = 1.0e0 / (k.dnym1 * k.dnym1); k.ty2 = 1.0e0 / (2.0e0 * k.dnym1); k.ty3 = 1.0e0 / k.dnym1;
+  k.tz1 = 1.0e0 / (k.dnzm1 * k.dnzm1); k.tz2 = 1.0e0 / (2.0e0 * k.dnzm1); k.tz3 = 1.0e0 / k.dnzm1;
+  k.dttx1 = dt * k.tx1; k.dttx2 = dt * k.tx2; k.dtty1 = dt * k.ty1; k.dtty2 = dt * k.ty2;
+  k.dttz1 = dt * k.tz1; k.dttz2 = dt * k.tz2;
+  k.c2dttx1 = 2.0e0 * k.dttx1; k.c2dtty1 = 2.0e0 * k.dtty1; k.c2dttz1 = 2.0e0 * k.dttz1;
+  const double dtdssp = dt * k.dssp;
+  k.comz1 = dtdssp; k.comz4 = 4.0e0 * dtdssp; k.comz5 = 5.0e0 * dtdssp; k.comz6 = 6.0e0 * dtdssp;
+  const double c3c4tx3 = k.c3c4 * k.tx3, c3c4ty3 = k.c3c4 * k.ty3, c3c4tz3 = k.c3c4 * k.tz3;
+  k.dx1tx1 = k.dx1 * k.tx1; k.dx2tx1 = k.dx2 * k.tx1; k.dx3tx1 = k.dx3 * k.tx1; k.dx4tx1 = k.dx4 * k.tx1; k.dx5tx1 = k.dx5 * k.tx1;
+  k.dy1ty1 = k.dy1 * k.ty1; k.dy2ty1 = k.dy2 * k.ty1; k.dy3ty1 = k.dy3 * k.ty1; k.dy4ty1 = k.dy4 * k.ty1; k.dy5ty1 = k.dy5 * k.ty1;
+  k.dz1tz1 = k.dz1 * k.tz1; k.dz2tz1 = k.dz2 * k.tz1; k.dz3tz1 = k.dz3 * k.tz1; k.dz4tz1 = k.dz4 * k.tz1; k.dz5tz1 = k.dz5 * k.tz1;
+  k.xxcon1 = c3c4tx3 * k.con43 * k.tx3; k.xxcon2 = c3c4tx3 * k.tx3; k.xxcon3 = c3c4tx3 * k.conz1 * k.tx3;
+  k.xxcon4 = c3c4tx3 * k.con16 * k.tx3; k.xxcon5 = c3c4tx3 * k.c1c5 * k.tx3;
+  k.yycon1 = c3c4ty3 * k.con43 * k.ty3; k.yycon2 = c3c4ty3 * k.ty3; k.yycon3 = c3c4ty3 * k.conz1 * k.ty3;
+  k.yycon4 = c3c4ty3 * k.con16 * k.ty3; k.yycon5 = c3c4ty3 * k.c1c5 * k.ty3;
+  k.zzcon1 = c3c4tz3 * k.con43 * k.tz3; k.zzcon2 = c3c4tz3 * k.tz3; k.zzcon3 = c3c4tz3 * k.conz1 * k.tz3;
+  k.zzcon4 = c3c4tz3 * k.con16 * k.tz3; k.zzcon5 = c3c4tz3 * k.c1c5 * k.tz3;
+  return k;
+}
+
+// A contiguous slice of a work list: items [lo, hi) belong to one zone.
+struct Range {
+  int lo = 0, hi = 0;
+};
+
+}  // namespace
+
+struct npbmz_handle {
+  int kind = 0, nzones = 0, flags = 0;
+  Consts K;
+  std::vector<ZoneDev> zh;
+  std::vector<int> nbr;
+  int64_t NP = 0;
+  int max_face = 0, max_np = 0;
+  // device buffers
+  ZoneDev* zones_d = nullptr;
+  int* nbr_d = nullptr;
+  double* u = nullptr;
+  double* rhs = nullptr;
+  double* forcing = nullptr;
+  double* prim = nullptr;
+  double* uex = nullptr;
+  double* xw = nullptr;      // first-pass line solution of the refined mixed solve
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  double* part_rhs = nullptr;
+  double* part_err = nullptr;
+  double* norms_d = nullptr;
+  int norms_cap = 0;
+  double* stage = nullptr;
+  size_t stage_elems = 0;
+  int64_t* soff_d[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  std::vector<int64_t> soff_h[2][3];   // per layout, field: zone offsets (+ total at [nzones])
+  // work lists
+  Work* wpts_d = nullptr;
+  int nwpts = 0;
+  std::vector<Range> pts_range;   // per zone
+  int* zblk_pts_d = nullptr;      // [2*nzones] CTA ranges of each zone (point list)
+  Work* wline_d[3] = {nullptr, nullptr, nullptr};
+  int nwline[3] = {0, 0, 0};
+  std::vector<Range> line_range[3];
+  int tpb_line[3] = {64, 64, 64};
+  int64_t nlines[3] = {0, 0, 0};
+  // execution
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  cudaStream_t aux_stream = nullptr;   // graph replay when the handle's stream is the legacy one
+  cudaEvent_t fence[2] = {nullptr, nullptr};
+  int launches_per_step = 0;
+  int64_t device_bytes = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(npbmz_t* h, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  else g_create_error = buf;
+  return -1;
+}
+
+#define CK(h, call)                                                                               \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail((h), "%s failed: %s", #call, cudaGetErrorString(e_));      \
+  } while (0)
+
+#define CKL(h)                                                                                    \
+  do {                                                                                            \
+    cudaError_t e_ = cudaGetLastError();                                                          \
+    if (e_ != cudaSuccess) return fail((h), "kernel launch failed: %s", cudaGetErrorString(e_));  \
+  } while (0)
+
+template <typename T>
+int dalloc(npbmz_t* h, T** p, size_t count) {
+  size_t bytes = count * sizeof(T);
+  if (bytes == 0) bytes = sizeof(T);
+  CK(h, cudaMalloc((void**)p, bytes));
+  h->device_bytes += (int64_t)bytes;
+  return 0;
+}
+
+Fields fields(const npbmz_t* h) {
+  Fields F;
+  F.u = h->u;
+  F.rhs = h->rhs;
+  F.forcing = h->forcing;
+  F.prim = h->prim;
+  F.uex = h->uex;
+  F.zones = h->zones_d;
+  F.NP = h->NP;
+  return F;
+}
+
+bool use_exact(const npbmz_t* h) { return (h->flags & NPBMZ_EXACT) != 0; }
+bool use_fp32(const npbmz_t* h) { return (h->flags & (NPBMZ_MIXED | NPBMZ_FP32_NOREFINE)) != 0; }
+
+// Reference-layout element count of one zone's array (see include/npbmz.h).
+int64_t ref_elems(int kind, int field, const ZoneDev& z) {
+  const int64_t IMAX = z.nx + 1, JMAX = z.ny + 1, KMAX = z.nz + 1;
+  if (kind == NPBMZ_BT) {
+    if (field == NPBMZ_U) return 5 * (IMAX + 4) * (JMAX + 4) * (KMAX + 4);
+    if (field == NPBMZ_RHS) return 5 * (IMAX + 1) * (JMAX + 1) * (KMAX + 1);
+    return 5 * IMAX * JMAX * KMAX;
+  }
+  const int64_t IMAXP = (IMAX / 2) * 2 + 1, JMAXP = (JMAX / 2) * 2 + 1;
+  if (field == NPBMZ_U) return 5 * (IMAXP + 4) * (JMAXP + 4) * (KMAX + 4);
+  return 5 * IMAXP * JMAXP * KMAX;
+}
+
+int build_work_lists(npbmz_t* h) {
+  const int nz = h->nzones;
+  // zones in decreasing size: the longest work first, each zone contiguous
+  std::vector<int> order(nz);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const ZoneDev &A = h->zh[a], &B = h->zh[b];
+    return (int64_t)A.nx * A.ny * A.nz > (int64_t)B.nx * B.ny * B.nz;
+  });
+  std::vector<Work> w;
+  h->pts_range.assign(nz, Range());
+  for (int z : order) {
+    const int np = h->zh[z].nx * h->zh[z].ny * h->zh[z].nz;
+    h->pts_range[z].lo = (int)w.size();
+    for (int f = 0; f < np; f += PTS_TPB) w.push_back(Work{z, f});
+    h->pts_range[z].hi = (int)w.size();
+  }
+  h->nwpts = (int)w.size();
+  if (dalloc(h, &h->wpts_d, w.size())) return -1;
+  CK(h, cudaMemcpy(h->wpts_d, w.data(), w.size() * sizeof(Work), cudaMemcpyHostToDevice));
+  std::vector<int> zb(2 * nz);
+  for (int z = 0; z < nz; ++z) { zb[2 * z] = h->pts_range[z].lo; zb[2 * z + 1] = h->pts_range[z].hi; }
+  if (dalloc(h, &h->zblk_pts_d, zb.size())) return -1;
+  CK(h, cudaMemcpy(h->zblk_pts_d, zb.data(), zb.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (dalloc(h, &h->part_rhs, (size_t)h->nwpts * 5)) return -1;
+  if (dalloc(h, &h->part_err, (size_t)h->nwpts * 5)) return -1;
+  return 0;
+}
+
+int build_line_lists(npbmz_t* h) {
+  const int nz = h->nzones;
+  for (int dir = 0; dir < 3; ++dir) {
+    if (h->wline_d[dir]) { cudaFree(h->wline_d[dir]); h->wline_d[dir] = nullptr; }
+    std::vector<int> order(nz);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return zone_line_len(h->zh[a], dir) > zone_line_len(h->zh[b], dir);
+    });
+    const int tpb = h->tpb_line[dir];
+    std::vector<Work> w;
+    h->line_range[dir].assign(nz, Range());
+    for (int z : order) {
+      const int nl = zone_lines(h->zh[z], dir);
+      h->line_range[dir][z].lo = (int)w.size();
+      for (int f = 0; f < nl; f += tpb) w.push_back(Work{z, f});
+      h->line_range[dir][z].hi = (int)w.size();
+    }
+    h->nwline[dir] = (int)w.size();
+    CK(h, cudaMalloc((void**)&h->wline_d[dir], std::max<size_t>(1, w.size()) * sizeof(Work)));
+    CK(h, cudaMemcpy(h->wline_d[dir], w.data(), w.size() * sizeof(Work), cudaMemcpyHostToDevice));
+  }
+  return 0;
+}
+
+// ---- phases ---------------------------------------------------------------
+int phase_prim(npbmz_t* h, int zone) {
+  const Fields F = fields(h);
+  int64_t lo = 0, hi = h->NP;
+  if (zone >= 0) {
+    lo = h->zh[zone].off;
+    hi = lo + (int64_t)h->zh[zone].nx * h->zh[zone].ny * h->zh[zone].nz;
+  }
+  const bool sp = h->kind == NPBMZ_SP;
+  if (use_exact(h)) exact::launch_prim(sp, F, h->K, lo, hi, h->stream);
+  else fast::launch_prim(sp, F, h->K, lo, hi, h->stream);
+  CKL(h);
+  return 0;
+}
+
+int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
+  const Fields F = fields(h);
+  int lo = 0, hi = h->nwpts;
+  if (zone >= 0) { lo = h->pts_range[zone].lo; hi = h->pts_range[zone].hi; }
+  if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wpts_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
+  else fast::launch_rhs(tx, norm, F, h->K, h->wpts_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
+  CKL(h);
+  return 0;
+}
+
+int phase_solve(npbmz_t* h, int dir, int zone, int add_u) {
+  const Fields F = fields(h);
+  int lo = 0, hi = h->nwline[dir];
+  if (zone >= 0) { lo = h->line_range[dir][zone].lo; hi = h->line_range[dir][zone].hi; }
+  const bool sp = h->kind == NPBMZ_SP;
+  if (use_exact(h))
+    exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch,
+                        h->nlines[dir], add_u, nullptr, h->stream);
+  else
+    fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : 2), dir, F, h->K,
+                       h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch, h->nlines[dir], add_u, h->xw,
+                       h->stream);
+  CKL(h);
+  return 0;
+}
+
+int phase_add(npbmz_t* h, int zone) {
+  const Fields F = fields(h);
+  int lo = 0, hi = h->nwpts;
+  if (zone >= 0) { lo = h->pts_range[zone].lo; hi = h->pts_range[zone].hi; }
+  if (use_exact(h)) exact::launch_add(F, h->wpts_d + lo, hi - lo, h->stream);
+  else fast::launch_add(F, h->wpts_d + lo, hi - lo, h->stream);
+  CKL(h);
+  return 0;
+}
+
+int phase_exch(npbmz_t* h) {
+  if (h->nzones < 2) return 0;  // the reference skips exch_qbc for one zone (bt-node.jl:286)
+  launch_exch_qbc(fields(h), h->nbr_d, 0, h->nzones, h->max_face, h->stream);
+  CKL(h);
+  return 0;
+}
+
+// adi for one zone or all zones (batched); norm: rhs partials for this step.
+int run_adi(npbmz_t* h, int zone, bool norm) {
+  const bool sp = h->kind == NPBMZ_SP;
+  if (zone < 0 && (h->flags & NPBMZ_PERZONE)) {
+    for (int z = 0; z < h->nzones; ++z)
+      if (run_adi(h, z, norm)) return -1;
+    return 0;
+  }
+  if (phase_prim(h, zone)) return -1;
+  if (phase_rhs(h, zone, sp, norm)) return -1;
+  if (phase_solve(h, 0, zone, 0)) return -1;
+  if (phase_solve(h, 1, zone, 0)) return -1;
+  if (phase_solve(h, 2, zone, 1)) return -1;  // add fused into the z sweep
+  return 0;
+}
+
+int finish_norms(npbmz_t* h, double* out_rhs, double* out_err) {
+  if (out_rhs) launch_norm_finish(h->zones_d, h->part_rhs, h->zblk_pts_d, h->nzones, 1.0 / h->K.dt, out_rhs, h->stream);
+  if (out_err) launch_norm_finish(h->zones_d, h->part_err, h->zblk_pts_d, h->nzones, 1.0, out_err, h->stream);
+  CKL(h);
+  return 0;
+}
+
+int err_partials(npbmz_t* h) {
+  launch_err_partials(fields(h), h->wpts_d, h->nwpts, h->part_err, h->stream);
+  CKL(h);
+  return 0;
+}
+
+int one_step(npbmz_t* h, bool norm, double* norm_slot) {
+  if (phase_exch(h)) return -1;
+  if (run_adi(h, -1, norm)) return -1;
+  if (norm) {
+    if (err_partials(h)) return -1;
+    if (finish_norms(h, norm_slot, norm_slot + 5)) return -1;
+  }
+  return 0;
+}
+
+void drop_graph(npbmz_t* h) {
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  h->graph_exec = nullptr;
+}
+
+int capture_step_graph(npbmz_t* h) {
+  drop_graph(h);
+  // Capture is not allowed on the legacy default stream: capture and replay
+  // on an owned stream, fenced against the caller's stream by events.
+  cudaStream_t cs = h->stream;
+  if (cs == nullptr) {
+    if (!h->aux_stream) CK(h, cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+    if (!h->fence[0]) {
+      CK(h, cudaEventCreateWithFlags(&h->fence[0], cudaEventDisableTiming));
+      CK(h, cudaEventCreateWithFlags(&h->fence[1], cudaEventDisableTiming));
+    }
+    cs = h->aux_stream;
+  }
+  cudaGraph_t g = nullptr;
+  cudaStream_t saved = h->stream;
+  h->stream = cs;
+  CK(h, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  int rc = one_step(h, false, nullptr);
+  cudaError_t e = cudaStreamEndCapture(cs, &g);
+  h->stream = saved;
+  if (rc) { if (g) cudaGraphDestroy(g); return -1; }
+  if (e != cudaSuccess) return fail(h, "stream capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(h, "graph instantiate failed: %s", cudaGetErrorString(e));
+  h->graph_stream = h->stream;
+  return 0;
+}
+
+int replay_graph(npbmz_t* h, int nsteps) {
+  if (h->stream != nullptr) {
+    for (int s = 0; s < nsteps; ++s) CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
+    return 0;
+  }
+  CK(h, cudaEventRecord(h->fence[0], nullptr));
+  CK(h, cudaStreamWaitEvent(h->aux_stream, h->fence[0], 0));
+  for (int s = 0; s < nsteps; ++s) CK(h, cudaGraphLaunch(h->graph_exec, h->aux_stream));
+  CK(h, cudaEventRecord(h->fence[1], h->aux_stream));
+  CK(h, cudaStreamWaitEvent(nullptr, h->fence[1], 0));
+  return 0;
+}
+
+int count_launches(npbmz_t* h) {
+  const int adi = 5;  // prim, rhs, x, y, z
+  int n = (h->nzones > 1 ? 1 : 0) + ((h->flags & NPBMZ_PERZONE) ? adi * h->nzones : adi);
+  return n;
+}
+
+int ensure_stage(npbmz_t* h, size_t elems) {
+  if (elems <= h->stage_elems) return 0;
+  if (h->stage) { cudaFree(h->stage); h->device_bytes -= (int64_t)(h->stage_elems * sizeof(double)); }
+  h->stage = nullptr;
+  h->stage_elems = 0;
+  if (dalloc(h, &h->stage, elems)) return -1;
+  h->stage_elems = elems;
+  return 0;
+}
+
+double* field_ptr(npbmz_t* h, int field) {
+  return field == NPBMZ_U ? h->u : field == NPBMZ_RHS ? h->rhs : h->forcing;
+}
+
+// Reference-array geometry of one zone: extents (fastest first, elements)
+// and the position of point (0,0,0) inside the halo.
+struct RefBox {
+  int64_t di, dj, dk;
+  int oi, oj, ok;
+};
+
+RefBox ref_box(int kind, int field, const ZoneDev& z) {
+  const int64_t IMAX = z.nx + 1, JMAX = z.ny + 1, KMAX = z.nz + 1;
+  if (kind == NPBMZ_BT) {
+    if (field == NPBMZ_U) return {IMAX + 4, JMAX + 4, KMAX + 4, 2, 2, 2};
+    if (field == NPBMZ_RHS) return {IMAX + 1, JMAX + 1, KMAX + 1, 1, 1, 1};
+    return {IMAX, JMAX, KMAX, 0, 0, 0};
+  }
+  const int64_t IMAXP = (IMAX / 2) * 2 + 1, JMAXP = (JMAX / 2) * 2 + 1;
+  if (field == NPBMZ_U) return {IMAXP + 4, JMAXP + 4, KMAX + 4, 2, 2, 2};
+  return {IMAXP, JMAXP, KMAX, 0, 0, 0};
+}
+
+// Copy the interior box of one zone's reference array between host memory
+// and the compact staging order (BT: [k][j][i][m], SP: [m][k][j][i]); the
+// halo of the host array is neither read nor written.
+int ref_box_copy(npbmz_t* h, int zone, int field, double* host_zone, double* stage_zone, cudaMemcpyKind kind) {
+  const ZoneDev& z = h->zh[zone];
+  const RefBox b = ref_box(h->kind, field, z);
+  const int vars = h->kind == NPBMZ_BT ? 1 : 5;
+  const size_t w = h->kind == NPBMZ_BT ? 5 : 1;  // doubles per i step in the host array
+  const int64_t np = (int64_t)z.nx * z.ny * z.nz;
+  for (int m = 0; m < vars; ++m) {
+    double* hz = host_zone + (h->kind == NPBMZ_BT ? 0 : (int64_t)m * b.di * b.dj * b.dk);
+    double* sz = stage_zone + (h->kind == NPBMZ_BT ? 0 : m * np);
+    cudaMemcpy3DParms p;
+    std::memset(&p, 0, sizeof(p));
+    cudaPitchedPtr hp = make_cudaPitchedPtr(hz, w * b.di * sizeof(double), w * b.di, b.dj);
+    cudaPitchedPtr sp = make_cudaPitchedPtr(sz, w * z.nx * sizeof(double), w * z.nx, z.ny);
+    const cudaPos hpos = make_cudaPos(w * b.oi * sizeof(double), b.oj, b.ok);
+    if (kind == cudaMemcpyHostToDevice) { p.srcPtr = hp; p.srcPos = hpos; p.dstPtr = sp; }
+    else { p.srcPtr = sp; p.dstPtr = hp; p.dstPos = hpos; }
+    p.extent = make_cudaExtent(w * z.nx * sizeof(double), z.ny, z.nz);
+    p.kind = kind;
+    CK(h, cudaMemcpy3DAsync(&p, h->stream));
+  }
+  return 0;
+}
+
+int transfer(npbmz_t* h, int zone, int field, int layout, void* host, int dir, bool sync) {
+  if (!h) return fail(nullptr, "null handle");
+  if (field < 0 || field > 2) return fail(h, "bad field %d", field);
+  if (layout != NPBMZ_LAYOUT_DENSE && layout != NPBMZ_LAYOUT_REF) return fail(h, "bad layout %d", layout);
+  if (zone < -1 || zone >= h->nzones) return fail(h, "bad zone %d", zone);
+  if (!host) return fail(h, "null host buffer");
+  const std::vector<int64_t>& so = h->soff_h[layout][field];
+  const int zlo = zone < 0 ? 0 : zone, zn = zone < 0 ? h->nzones : 1;
+  const int64_t first = so[zlo], count = so[zlo + zn] - first;
+  double* planes = field_ptr(h, field);
+  const Fields F = fields(h);
+  // Page-locked (mapped) host memory: one kernel reads / writes it directly.
+  cudaPointerAttributes attr;
+  std::memset(&attr, 0, sizeof(attr));
+  if (cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+    launch_convert(F, planes, reinterpret_cast<double*>(attr.devicePointer), h->soff_d[layout][field], first, zlo, zn,
+                   h->max_np, h->kind, field, layout, dir, h->stream);
+    CKL(h);
+  } else {
+    cudaGetLastError();  // cudaPointerGetAttributes on pageable memory is not an error to keep
+    if (ensure_stage(h, (size_t)so[h->nzones])) return -1;
+    if (dir == 0) {
+      CK(h, cudaMemcpyAsync(h->stage + first, host, count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+      launch_convert(F, planes, h->stage, h->soff_d[layout][field], 0, zlo, zn, h->max_np, h->kind, field, layout, 0,
+                     h->stream);
+      CKL(h);
+    } else if (layout == NPBMZ_LAYOUT_DENSE) {
+      launch_convert(F, planes, h->stage, h->soff_d[layout][field], 0, zlo, zn, h->max_np, h->kind, field, layout, 1,
+                     h->stream);
+      CKL(h);
+      CK(h, cudaMemcpyAsync(host, h->stage + first, count * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+      // compact staging (dense offsets), then the interior box of each zone
+      const std::vector<int64_t>& sd = h->soff_h[NPBMZ_LAYOUT_DENSE][field];
+      launch_convert(F, planes, h->stage, h->soff_d[NPBMZ_LAYOUT_DENSE][field], 0, zlo, zn, h->max_np, h->kind, field,
+                     2, 1, h->stream);
+      CKL(h);
+      double* hb = reinterpret_cast<double*>(host);
+      for (int z = zlo; z < zlo + zn; ++z)
+        if (ref_box_copy(h, z, field, hb + (so[z] - first), h->stage + sd[z], cudaMemcpyDeviceToHost)) return -1;
+    }
+  }
+  if (sync) CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+// ---- seeded coefficients ----------------------------------------------------
+uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+void exact_host(double xi, double eta, double zeta, const double* ce, double out[5]) {
+  for (int m = 0; m < 5; ++m) {
+    const double* c = ce + 13 * m;
+    out[m] = c[0] + xi * (c[1] + xi * (c[4] + xi * (c[7] + xi * c[10]))) +
+             eta * (c[2] + eta * (c[5] + eta * (c[8] + eta * c[11]))) +
+             zeta * (c[3] + zeta * (c[6] + zeta * (c[9] + zeta * c[12])));
+  }
+}
+
+bool state_ok(const double u[5], double margin) {
+  if (!(u[0] > 0.0)) return false;
+  const double ke = 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0];
+  return u[4] - ke >= margin * u[4] && u[4] > 0.0;
+}
+
+}  // namespace
+
+// =============================== C ABI ======================================
+extern "C" {
+
+int npbmz_zone_setup(int kind, int gx, int gy, int gz, int xz, int yz, double ratio, int* nx, int* ny, int* nz,
+                     int* nbr) {
+  if (xz < 1 || yz < 1 || gx < 3 || gy < 3 || gz < 3 || !nx || !ny || !nz || !nbr) return -1;
+  std::vector<long> x_end(xz), y_end(yz), x_start(xz), y_start(yz), x_size(xz), y_size(yz);
+  const bool stretch = std::fabs(ratio - 1.0e0) > 1.0e-10 && (kind == NPBMZ_SP || (xz > 1 && yz > 1));
+  if (stretch) {
+    // geometric zone widths, src/BT/zone_setup.jl:5-22
+    const double x_r = std::exp(std::log(ratio) / (xz - 1));
+    const double y_r = std::exp(std::log(ratio) / (yz - 1));
+    const double x_smallest = (double)gx * (x_r - 1.0e0) / (std::pow(x_r, xz) - 1.0e0);
+    const double y_smallest = (double)gy * (y_r - 1.0e0) / (std::pow(y_r, yz) - 1.0e0);
+    for (int i = 1; i <= xz; ++i)
+      x_end[i - 1] = (long)std::trunc(x_smallest * (std::pow(x_r, i) - 1.0e0) / (x_r - 1.0e0) + 0.45e0);
+    for (int j = 1; j <= yz; ++j)
+      y_end[j - 1] = (long)std::trunc(y_smallest * (std::pow(y_r, j) - 1.0e0) / (y_r - 1.0e0) + 0.45e0);
+  } else {
+    for (int i = 1; i <= xz; ++i) x_end[i - 1] = (long)((double)(i * gx) / (double)xz);
+    for (int j = 1; j <= yz; ++j) y_end[j - 1] = (long)((double)(j * gy) / (double)yz);
+  }
+  x_start[0] = 1;
+  for (int i = 0; i < xz; ++i) {
+    if (i != xz - 1) x_start[i + 1] = x_end[i] + 1;
+    x_size[i] = x_end[i] - x_start[i] + 1;
+  }
+  y_start[0] = 1;
+  for (int j = 0; j < yz; ++j) {
+    if (j != yz - 1) y_start[j + 1] = y_end[j] + 1;
+    y_size[j] = y_end[j] - y_start[j] + 1;
+  }
+  for (int j = 1; j <= yz; ++j)
+    for (int i = 1; i <= xz; ++i) {
+      const int zn = (i - 1) + (j - 1) * xz;
+      nx[zn] = (int)x_size[i - 1];
+      ny[zn] = (int)y_size[j - 1];
+      nz[zn] = gz;
+      nbr[4 * zn + 0] = (i - 2 + xz) % xz + (j - 1) * xz;
+      nbr[4 * zn + 1] = i % xz + (j - 1) * xz;
+      nbr[4 * zn + 2] = (i - 1) + ((j - 2 + yz) % yz) * xz;
+      nbr[4 * zn + 3] = (i - 1) + (j % yz) * xz;
+    }
+  return 0;
+}
+
+int npbmz_seeded_coefficients(uint64_t seed, int nzones, const int* nx, const int* ny, const int* nz, int gx, int gy,
+                              int gz, int xz, int yz, double* ce) {
+  if (!nx || !ny || !nz || !ce || nzones < 1) return -1;
+  uint64_t s = seed;
+  for (int e = 0; e < 65; ++e) {
+    const double r = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
+    ce[e] = 0.5 + 1.5 * r;
+  }
+  const Consts K = make_consts(1.0, gx, gy, gz, xz, yz);
+  int mx = 0, my = 0, mz = 0;
+  for (int z = 0; z < nzones; ++z) { mx = std::max(mx, nx[z]); my = std::max(my, ny[z]); mz = std::max(mz, nz[z]); }
+  const double margin = 0.25;
+  for (int e = 0; e < 40; ++e) {
+    bool ok = true;
+    double st[5], P1[2][5], P2[2][5], P3[2][5], ui[5];
+    for (int k = 0; k < mz && ok; ++k)
+      for (int j = 0; j < my && ok; ++j)
+        for (int i = 0; i < mx && ok; ++i) {
+          const double xi = (double)i * K.dnxm1, eta = (double)j * K.dnym1, zeta = (double)k * K.dnzm1;
+          exact_host(xi, eta, zeta, ce, st);
+          if (!state_ok(st, margin)) { ok = false; break; }
+          exact_host(0.0, eta, zeta, ce, P1[0]); exact_host(1.0, eta, zeta, ce, P1[1]);
+          exact_host(xi, 0.0, zeta, ce, P2[0]); exact_host(xi, 1.0, zeta, ce, P2[1]);
+          exact_host(xi, eta, 0.0, ce, P3[0]); exact_host(xi, eta, 1.0, ce, P3[1]);
+          for (int m = 0; m < 5; ++m) {
+            const double Pxi = xi * P1[1][m] + (1.0 - xi) * P1[0][m];
+            const double Peta = eta * P2[1][m] + (1.0 - eta) * P2[0][m];
+            const double Pzeta = zeta * P3[1][m] + (1.0 - zeta) * P3[0][m];
+            ui[m] = Pxi + Peta + Pzeta - Pxi * Peta - Pxi * Pzeta - Peta * Pzeta + Pxi * Peta * Pzeta;
+          }
+          if (!state_ok(ui, margin)) ok = false;
+          for (int f = 0; f < 2 && ok; ++f)
+            if (!state_ok(P1[f], margin) || !state_ok(P2[f], margin) || !state_ok(P3[f], margin)) ok = false;
+        }
+    if (ok) return e;
+    for (int n = 0; n < 13; ++n) ce[4 * 13 + n] *= 2.0;
+  }
+  return -2;
+}
+
+int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* nz, const int* nbr,
+                 const double* params, int variant_flags, npbmz_t** out) {
+  if (!out) return fail(nullptr, "out is null");
+  *out = nullptr;
+  if (kind != NPBMZ_BT && kind != NPBMZ_SP) return fail(nullptr, "kind must be NPBMZ_BT or NPBMZ_SP");
+  if (nzones < 1 || !nx || !ny || !nz || !nbr || !params) return fail(nullptr, "bad geometry arguments");
+  if ((variant_flags & NPBMZ_EXACT) && (variant_flags & (NPBMZ_MIXED | NPBMZ_FP32_NOREFINE)))
+    return fail(nullptr, "NPBMZ_EXACT and the FP32 line-solve variants are exclusive");
+  for (int z = 0; z < nzones; ++z) {
+    // src/BT/make_set.jl:100-105 aborts on a cell size <= 2
+    if (nx[z] < 3 || ny[z] < 3 || nz[z] < 3) return fail(nullptr, "zone %d: size %dx%dx%d, minimum is 3", z, nx[z], ny[z], nz[z]);
+    if ((int64_t)nx[z] * ny[z] * nz[z] > (1 << 30)) return fail(nullptr, "zone %d too large", z);
+    for (int f = 0; f < 4; ++f)
+      if (nbr[4 * z + f] < 0 || nbr[4 * z + f] >= nzones) return fail(nullptr, "zone %d: bad neighbour", z);
+  }
+  for (int z = 0; z < nzones; ++z) {
+    const int w = nbr[4 * z], e = nbr[4 * z + 1], s = nbr[4 * z + 2], n = nbr[4 * z + 3];
+    if (ny[w] != ny[z] || nz[w] != nz[z] || ny[e] != ny[z] || nz[e] != nz[z] || nx[s] != nx[z] || nz[s] != nz[z] ||
+        nx[n] != nx[z] || nz[n] != nz[z])
+      return fail(nullptr, "zone %d: neighbour face sizes do not match", z);
+  }
+  npbmz_t* h = new npbmz_t();
+  h->kind = kind;
+  h->nzones = nzones;
+  h->flags = variant_flags;
+  h->K = make_consts(params[0], (int)params[1], (int)params[2], (int)params[3], (int)params[4], (int)params[5]);
+  h->nbr.assign(nbr, nbr + 4 * nzones);
+  h->zh.resize(nzones);
+  int64_t off = 0, lines[3] = {0, 0, 0};
+  int64_t scratch_elems = 0;
+  for (int z = 0; z < nzones; ++z) {
+    ZoneDev& d = h->zh[z];
+    d.nx = nx[z]; d.ny = ny[z]; d.nz = nz[z]; d.pad = 0;
+    d.off = off;
+    const int64_t np = (int64_t)d.nx * d.ny * d.nz;
+    off += (np + 31) / 32 * 32;
+    for (int dir = 0; dir < 3; ++dir) {
+      d.lineoff[dir] = lines[dir];
+      lines[dir] += zone_lines(d, dir);
+    }
+    h->max_np = std::max<int>(h->max_np, (int)np);
+    h->max_face = std::max(h->max_face, 5 * std::max(d.nx, d.ny) * d.nz);
+  }
+  h->NP = std::max<int64_t>(off, 32);
+  for (int dir = 0; dir < 3; ++dir) {
+    h->nlines[dir] = lines[dir];
+    int maxlen = 0;
+    for (int z = 0; z < nzones; ++z) maxlen = std::max(maxlen, zone_line_len(h->zh[z], dir));
+    scratch_elems = std::max<int64_t>(scratch_elems, (int64_t)maxlen * lines[dir]);
+  }
+  // line scratch: BT keeps 25 values per point (C'), SP 6 (l4, l5 of 3 systems)
+  const int per = kind == NPBMZ_BT ? 25 : 6;
+  if (variant_flags & NPBMZ_FP32_NOREFINE) variant_flags |= NPBMZ_MIXED;
+  h->flags = variant_flags;
+  const size_t esz = (variant_flags & NPBMZ_MIXED) ? sizeof(float) : sizeof(double);
+  h->scratch_bytes = (size_t)scratch_elems * per * esz;
+
+  int rc = 0;
+  rc |= dalloc(h, &h->zones_d, nzones);
+  rc |= dalloc(h, &h->nbr_d, 4 * (size_t)nzones);
+  rc |= dalloc(h, &h->u, 5 * (size_t)h->NP);
+  rc |= dalloc(h, &h->rhs, 5 * (size_t)h->NP);
+  rc |= dalloc(h, &h->forcing, 5 * (size_t)h->NP);
+  rc |= dalloc(h, &h->prim, (size_t)PR_COUNT * h->NP);
+  rc |= dalloc(h, &h->uex, 5 * (size_t)h->NP);
+  if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
+  if (!rc) {
+    if (cudaMalloc(&h->scratch, std::max<size_t>(h->scratch_bytes, 16)) != cudaSuccess) rc = fail(h, "scratch alloc failed");
+    else h->device_bytes += (int64_t)h->scratch_bytes;
+  }
+  if (!rc && cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(ZoneDev), cudaMemcpyHostToDevice) != cudaSuccess) rc = -1;
+  if (!rc && cudaMemcpy(h->nbr_d, nbr, 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) rc = -1;
+  if (!rc) rc = build_work_lists(h);
+  if (!rc) rc = build_line_lists(h);
+  // staging offsets per layout and field
+  for (int layout = 0; layout < 2 && !rc; ++layout)
+    for (int field = 0; field < 3 && !rc; ++field) {
+      std::vector<int64_t>& so = h->soff_h[layout][field];
+      so.assign(nzones + 1, 0);
+      for (int z = 0; z < nzones; ++z) {
+        const ZoneDev& d = h->zh[z];
+        const int64_t n = layout == NPBMZ_LAYOUT_DENSE ? 5 * (int64_t)d.nx * d.ny * d.nz : ref_elems(kind, field, d);
+        so[z + 1] = so[z] + n;
+      }
+      rc = dalloc(h, &h->soff_d[layout][field], (size_t)nzones + 1);
+      if (!rc && cudaMemcpy(h->soff_d[layout][field], so.data(), so.size() * sizeof(int64_t), cudaMemcpyHostToDevice) !=
+                     cudaSuccess)
+        rc = -1;
+    }
+  if (!rc) {
+    // fields start defined: u = (1, 0, 0, 0, 1) on padding keeps the
+    // primitive kernel finite there; rhs and forcing zero.
+    const Fields F = fields(h);
+    (void)F;
+    for (int m = 0; m < 5; ++m) launch_fill(h->u + m * h->NP, h->NP, (m == 0 || m == 4) ? 1.0 : 0.0, nullptr);
+    if (cudaMemset(h->rhs, 0, 5 * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
+    if (cudaMemset(h->forcing, 0, 5 * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
+    if (cudaMemset(h->prim, 0, PR_COUNT * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
+    if (cudaMemset(h->uex, 0, 5 * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
+    if (cudaDeviceSynchronize() != cudaSuccess) rc = -1;
+  }
+  if (rc) {
+    const std::string msg = h->err.empty() ? std::string("device allocation or copy failed: ") +
+                                                 cudaGetErrorString(cudaGetLastError())
+                                           : h->err;
+    npbmz_destroy(h);
+    return fail(nullptr, "%s", msg.c_str());
+  }
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess) { h->stream = s; h->own_stream = true; }
+  h->launches_per_step = count_launches(h);
+  *out = h;
+  return 0;
+}
+
+int npbmz_setup(npbmz_t* h, const double* ce) {
+  if (!h || !ce) return fail(h, "null argument");
+  const Fields F = fields(h);
+  launch_initialize(F, h->K, ce, h->wpts_d, h->nwpts, h->uex, h->stream);
+  CKL(h);
+  launch_exact_rhs(F, h->K, ce, h->wpts_d, h->nwpts, h->forcing, h->stream);
+  CKL(h);
+  // rhs starts as the forcing (its boundary values are never rewritten)
+  CK(h, cudaMemcpyAsync(h->rhs, h->forcing, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int npbmz_upload(npbmz_t* h, int zone, int field, int layout, const double* host) {
+  return transfer(h, zone, field, layout, const_cast<double*>(host), 0, true);
+}
+int npbmz_download(npbmz_t* h, int zone, int field, int layout, double* host) {
+  return transfer(h, zone, field, layout, host, 1, true);
+}
+int npbmz_upload_async(npbmz_t* h, int zone, int field, int layout, const double* host) {
+  return transfer(h, zone, field, layout, const_cast<double*>(host), 0, false);
+}
+int npbmz_download_async(npbmz_t* h, int zone, int field, int layout, double* host) {
+  return transfer(h, zone, field, layout, host, 1, false);
+}
+
+int npbmz_exch_qbc(npbmz_t* h) {
+  if (!h) return fail(nullptr, "null handle");
+  return phase_exch(h);
+}
+
+int npbmz_adi(npbmz_t* h, int zone) {
+  if (!h) return fail(nullptr, "null handle");
+  if (zone < -1 || zone >= h->nzones) return fail(h, "bad zone %d", zone);
+  return run_adi(h, zone, false);
+}
+
+int npbmz_step(npbmz_t* h, int nsteps, double* norms) {
+  if (!h) return fail(nullptr, "null handle");
+  if (nsteps < 0) return fail(h, "nsteps < 0");
+  if (norms) {
+    if (nsteps > h->norms_cap) {
+      if (h->norms_d) { cudaFree(h->norms_d); h->device_bytes -= (int64_t)h->norms_cap * 10 * sizeof(double); }
+      h->norms_d = nullptr;
+      h->norms_cap = 0;
+      if (dalloc(h, &h->norms_d, 10 * (size_t)std::max(nsteps, 1))) return -1;
+      h->norms_cap = std::max(nsteps, 1);
+    }
+    for (int s = 0; s < nsteps; ++s)
+      if (one_step(h, true, h->norms_d + 10 * s)) return -1;
+    CK(h, cudaMemcpyAsync(norms, h->norms_d, 10 * sizeof(double) * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return 0;
+  }
+  if (h->flags & NPBMZ_GRAPH) {
+    if (!h->graph_exec || h->graph_stream != h->stream)
+      if (capture_step_graph(h)) return -1;
+    return replay_graph(h, nsteps);
+  }
+  for (int s = 0; s < nsteps; ++s)
+    if (one_step(h, false, nullptr)) return -1;
+  return 0;
+}
+
+int npbmz_verify(npbmz_t* h, double* xcr, double* xce) {
+  if (!h || !xcr || !xce) return fail(h, "null argument");
+  if (!h->norms_d) {
+    if (dalloc(h, &h->norms_d, 10)) return -1;
+    h->norms_cap = 1;
+  }
+  if (err_partials(h)) return -1;
+  if (finish_norms(h, nullptr, h->norms_d + 5)) return -1;
+  if (phase_prim(h, -1)) return -1;
+  if (phase_rhs(h, -1, false, true)) return -1;
+  if (finish_norms(h, h->norms_d, nullptr)) return -1;
+  double buf[10];
+  CK(h, cudaMemcpyAsync(buf, h->norms_d, sizeof(buf), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < 5; ++m) { xcr[m] = buf[m]; xce[m] = buf[5 + m]; }
+  return 0;
+}
+
+int npbmz_phase(npbmz_t* h, int phase, int zone) {
+  if (!h) return fail(nullptr, "null handle");
+  if (zone < -1 || zone >= h->nzones) return fail(h, "bad zone %d", zone);
+  const bool sp = h->kind == NPBMZ_SP;
+  switch (phase) {
+    case NPBMZ_PHASE_RHS:
+      if (phase_prim(h, zone)) return -1;
+      return phase_rhs(h, zone, sp, false);
+    case NPBMZ_PHASE_RHSONLY:
+      if (phase_prim(h, zone)) return -1;
+      return phase_rhs(h, zone, false, false);
+    case NPBMZ_PHASE_XSOLVE: return phase_solve(h, 0, zone, 0);
+    case NPBMZ_PHASE_YSOLVE: return phase_solve(h, 1, zone, 0);
+    case NPBMZ_PHASE_ZSOLVE: return phase_solve(h, 2, zone, 0);
+    case NPBMZ_PHASE_ADD: return phase_add(h, zone);
+    case NPBMZ_PHASE_EXCH: return phase_exch(h);
+    default: return fail(h, "bad phase %d", phase);
+  }
+}
+
+int npbmz_set_stream(npbmz_t* h, void* stream) {
+  if (!h) return fail(nullptr, "null handle");
+  if (h->own_stream && h->stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
+  h->own_stream = false;
+  h->stream = reinterpret_cast<cudaStream_t>(stream);
+  drop_graph(h);
+  return 0;
+}
+
+int npbmz_synchronize(npbmz_t* h) {
+  if (!h) return fail(nullptr, "null handle");
+  CK(h, cudaStreamSynchronize(h->stream));
+  CK(h, cudaGetLastError());
+  return 0;
+}
+
+int npbmz_autotune(npbmz_t* h) {
+  if (!h) return fail(nullptr, "null handle");
+  // Candidate lines per CTA for each sweep direction; timed on a snapshot of
+  // u so that the handle's state is unchanged afterwards.
+  const int cand[] = {32, 64, 128};
+  double* usave = nullptr;
+  CK(h, cudaMalloc(&usave, 5 * h->NP * sizeof(double)));
+  double* rsave = nullptr;
+  if (cudaMalloc(&rsave, 5 * h->NP * sizeof(double)) != cudaSuccess) { cudaFree(usave); return fail(h, "autotune alloc"); }
+  cudaMemcpyAsync(usave, h->u, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(rsave, h->rhs, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = 0;
+  // prim + rhs once so that the solves read defined data
+  rc |= phase_prim(h, -1);
+  rc |= phase_rhs(h, -1, h->kind == NPBMZ_SP, false);
+  for (int dir = 0; dir < 3 && !rc; ++dir) {
+    float best = 1e30f;
+    int best_tpb = h->tpb_line[dir];
+    for (int c : cand) {
+      h->tpb_line[dir] = c;
+      if (build_line_lists(h)) { rc = -1; break; }
+      // warm-up, then 3 timed repetitions (the solve rewrites rhs in place;
+      // restore it between repetitions)
+      float tot = 0.f;
+      for (int rep = 0; rep < 4 && !rc; ++rep) {
+        cudaMemcpyAsync(h->rhs, rsave, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+        cudaEventRecord(e0, h->stream);
+        rc |= phase_solve(h, dir, -1, 0);
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) tot += ms;
+      }
+      if (tot < best) { best = tot; best_tpb = c; }
+    }
+    h->tpb_line[dir] = best_tpb;
+  }
+  if (!rc) rc = build_line_lists(h);
+  cudaMemcpyAsync(h->u, usave, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(h->rhs, rsave, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  cudaStreamSynchronize(h->stream);
+  cudaFree(usave);
+  cudaFree(rsave);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  drop_graph(h);
+  return rc ? -1 : 0;
+}
+
+int npbmz_fp64_peak(double* gflops) {
+  if (!gflops) return -1;
+  return probe_fp64(gflops);
+}
+
+int npbmz_launches_per_step(npbmz_t* h) { return h ? h->launches_per_step : -1; }
+int64_t npbmz_device_bytes(npbmz_t* h) { return h ? h->device_bytes : -1; }
+
+int npbmz_describe(npbmz_t* h, char* buf, size_t n) {
+  if (!h || !buf || n == 0) return -1;
+  snprintf(buf, n, "{\"kind\":\"%s\",\"zones\":%d,\"points\":%lld,\"flags\":%d,\"tpb_line\":[%d,%d,%d],"
+                   "\"launches_per_step\":%d,\"device_bytes\":%lld}",
+           h->kind == NPBMZ_BT ? "BT" : "SP", h->nzones, (long long)h->NP, h->flags, h->tpb_line[0], h->tpb_line[1],
+           h->tpb_line[2], h->launches_per_step, (long long)h->device_bytes);
+  return 0;
+}
+
+const char* npbmz_last_error(npbmz_t* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int npbmz_destroy(npbmz_t* h) {
+  if (!h) return 0;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graph(h);
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->scratch, h->part_rhs,
+                  h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wline_d[0], h->wline_d[1],
+                  h->wline_d[2]};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  for (int l = 0; l < 2; ++l)
+    for (int f = 0; f < 3; ++f)
+      if (h->soff_d[l][f]) cudaFree(h->soff_d[l][f]);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  if (h->aux_stream) { cudaStreamSynchronize(h->aux_stream); cudaStreamDestroy(h->aux_stream); }
+  for (cudaEvent_t e : h->fence)
+    if (e) cudaEventDestroy(e);
+  delete h;
+  return 0;
+}
+
+}  // extern "C"

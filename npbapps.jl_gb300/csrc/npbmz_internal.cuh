@@ -1,0 +1,101 @@
+// npbmz_internal.cuh -- device-side data layout and constants shared by the
+// kernels of libnpbmz_gpu.so.
+//
+// HBM layout: every field is variable-major structure-of-arrays over the
+// points of ALL zones: field[m * NP + zone.off + (k * ny + j) * nx + i].
+// Zone offsets are multiples of 32 points (256 B), NP is the padded total.
+// Each zone stores its points 0..n-1 on every axis (0 and n-1 are the ghost /
+// physical-boundary planes); the reference's 2-deep OffsetArray halo is not
+// stored because no value computed there reaches u, rhs or a norm.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace npbmz {
+
+// set_constants (src/BT/set_constants.jl:1-130), evaluated on the host.
+struct Consts {
+  double dt, dnxm1, dnym1, dnzm1;
+  double c1, c2, c3, c4, c5, bt, c1c2, c1c5, c3c4, c1345, conz1, con43, con16, c2iv, dssp;
+  double dx1, dx2, dx3, dx4, dx5, dy1, dy2, dy3, dy4, dy5, dz1, dz2, dz3, dz4, dz5, dxmax, dymax, dzmax;
+  double tx1, tx2, tx3, ty1, ty2, ty3, tz1, tz2, tz3;
+  double dttx1, dttx2, dtty1, dtty2, dttz1, dttz2, c2dttx1, c2dtty1, c2dttz1;
+  double comz1, comz4, comz5, comz6;
+  double dx1tx1, dx2tx1, dx3tx1, dx4tx1, dx5tx1;
+  double dy1ty1, dy2ty1, dy3ty1, dy4ty1, dy5ty1;
+  double dz1tz1, dz2tz1, dz3tz1, dz4tz1, dz5tz1;
+  double xxcon1, xxcon2, xxcon3, xxcon4, xxcon5;
+  double yycon1, yycon2, yycon3, yycon4, yycon5;
+  double zzcon1, zzcon2, zzcon3, zzcon4, zzcon5;
+};
+
+struct ZoneDev {
+  int nx, ny, nz, pad;
+  int64_t off;          // first point of the zone in every field plane
+  int64_t lineoff[3];   // first global line index of the zone, per sweep direction
+};
+
+// One work item = one CTA's share: `first` is the first point (point lists)
+// or the first line (line lists) of zone `zone` that the CTA handles.
+struct Work {
+  int zone;
+  int first;
+};
+
+// Primitive-variable planes written by the primitive kernel.
+enum { PR_RHOI = 0, PR_US, PR_VS, PR_WS, PR_QS, PR_SQUARE, PR_SPEED, PR_AINV, PR_COUNT };
+
+struct Fields {
+  double* u;        // [5][NP]
+  double* rhs;      // [5][NP]
+  const double* forcing;  // [5][NP]
+  double* prim;     // [PR_COUNT][NP]
+  const double* uex;      // [5][NP] exact solution (error norm)
+  const ZoneDev* zones;
+  int64_t NP;
+};
+
+// Lines per sweep direction of a zone (interior transverse indices only).
+__host__ __device__ inline int zone_lines(const ZoneDev& z, int dir) {
+  return dir == 0 ? (z.ny - 2) * (z.nz - 2) : (dir == 1 ? (z.nx - 2) * (z.nz - 2) : (z.nx - 2) * (z.ny - 2));
+}
+
+__host__ __device__ inline int zone_line_len(const ZoneDev& z, int dir) {
+  return dir == 0 ? z.nx : (dir == 1 ? z.ny : z.nz);
+}
+
+// First point and point stride of line `line` of zone z in direction dir.
+__host__ __device__ inline void line_geometry(const ZoneDev& z, int dir, int line, int64_t& base, int64_t& stride) {
+  if (dir == 0) {
+    int j = 1 + line % (z.ny - 2), k = 1 + line / (z.ny - 2);
+    base = z.off + ((int64_t)k * z.ny + j) * z.nx;
+    stride = 1;
+  } else if (dir == 1) {
+    int i = 1 + line % (z.nx - 2), k = 1 + line / (z.nx - 2);
+    base = z.off + (int64_t)k * z.ny * z.nx + i;
+    stride = z.nx;
+  } else {
+    int i = 1 + line % (z.nx - 2), j = 1 + line / (z.nx - 2);
+    base = z.off + (int64_t)j * z.nx + i;
+    stride = (int64_t)z.nx * z.ny;
+  }
+}
+
+// Deterministic CTA sum of 5 values per thread (fixed tree shape); the result
+// is valid in thread 0.  scratch must hold 5 * blockDim.x doubles.
+__device__ inline void block_sum5(double v[5], double* scratch) {
+  const int t = threadIdx.x, n = blockDim.x;
+  for (int m = 0; m < 5; ++m) scratch[m * n + t] = v[m];
+  __syncthreads();
+  for (int s = n / 2; s > 0; s >>= 1) {
+    if (t < s)
+      for (int m = 0; m < 5; ++m) scratch[m * n + t] = scratch[m * n + t] + scratch[m * n + t + s];
+    __syncthreads();
+  }
+  if (t == 0)
+    for (int m = 0; m < 5; ++m) v[m] = scratch[m * n];
+  __syncthreads();
+}
+
+}  // namespace npbmz

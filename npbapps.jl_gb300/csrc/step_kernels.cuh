@@ -1,0 +1,1233 @@
+// step_kernels.cuh -- the time-step kernels: primitive variables,
+// compute_rhs (+ txinvr for SP), the BT block-tridiagonal and SP scalar
+// pentadiagonal line solves (with ninvr / pinvr / tzetar and add fused into
+// their back substitution), and their host-side launchers.
+//
+// This file is compiled twice, into namespace NPBMZ_NS:
+//   exact  with -fmad=false: FP64 in the reference's operation order, no FMA
+//          contraction -- bit-for-bit the reference's arithmetic;
+//   fast   with -fmad=true : the same FP64 code with FMA contraction, plus the
+//          FP32 line-solve (mixed precision) instantiations.
+// Every expression keeps the reference's operand order and parenthesisation
+// (reference files cited at each kernel).
+#pragma once
+
+#include "npbmz_internal.cuh"
+
+#ifndef NPBMZ_NS
+#error "NPBMZ_NS must name the variant namespace"
+#endif
+
+namespace npbmz {
+namespace NPBMZ_NS {
+
+// ============================================================================
+// Primitive variables (src/BT/rhs.jl:62-77, src/SP/rhs.jl:62-89), one thread
+// per point of the padded plane (padding points compute garbage nobody reads).
+// ============================================================================
+template <bool SP>
+__global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, int64_t hi) {
+  const int64_t NP = F.NP;
+  for (int64_t p = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < hi; p += (int64_t)gridDim.x * blockDim.x) {
+    const double u1 = F.u[p], u2 = F.u[NP + p], u3 = F.u[2 * NP + p], u4 = F.u[3 * NP + p];
+    const double rho_inv = 1.0e0 / u1;
+    const double square = 0.5e0 * (u2 * u2 + u3 * u3 + u4 * u4) * rho_inv;
+    F.prim[PR_RHOI * NP + p] = rho_inv;
+    F.prim[PR_US * NP + p] = u2 * rho_inv;
+    F.prim[PR_VS * NP + p] = u3 * rho_inv;
+    F.prim[PR_WS * NP + p] = u4 * rho_inv;
+    F.prim[PR_SQUARE * NP + p] = square;
+    F.prim[PR_QS * NP + p] = square * rho_inv;
+    if (SP) {
+      const double u5 = F.u[4 * NP + p];
+      double aux = K.c1c2 * rho_inv * (u5 - square);
+      aux = sqrt(aux);
+      F.prim[PR_SPEED * NP + p] = aux;
+      F.prim[PR_AINV * NP + p] = 1.0e0 / aux;
+    }
+  }
+}
+
+// ============================================================================
+// compute_rhs (src/BT/rhs.jl:4-460; SP src/SP/rhs.jl:3-452 -- the flux and
+// dissipation statements are identical) and, when TX (the SP step), txinvr
+// (src/SP/txinvr.jl:5-56).  One thread per zone point; boundary points copy
+// the forcing, as the reference's `rhs = forcing` over the whole cell does.
+// Per element the order of updates is the reference's: forcing, xi flux, xi
+// dissipation, eta flux, eta dissipation, zeta flux, zeta dissipation, *dt.
+// NORM: also accumulate this CTA's sum of rhs^2 (interior, before txinvr)
+// into partials[blockIdx.x][5] (each CTA covers points of one zone).
+// ============================================================================
+
+// Fourth-order dissipation term at position q of an axis of n points
+// (1 <= q <= n-2): the start / middle / end stencils of the reference,
+// applied in the reference's order when n is so small that they overlap.
+__device__ __forceinline__ void dissip(double& r, int q, int n, double dssp, double um2, double um1, double u0,
+                                       double up1, double up2) {
+  if (q == 1) r -= dssp * (5.0e0 * u0 - 4.0e0 * up1 + up2);
+  if (q == 2) r -= dssp * (-4.0e0 * um1 + 6.0e0 * u0 - 4.0e0 * up1 + up2);
+  if (q >= 3 && q <= n - 4) r -= dssp * (um2 - 4.0e0 * um1 + 6.0 * u0 - 4.0e0 * up1 + up2);
+  if (q == n - 3) r -= dssp * (um2 - 4.0e0 * um1 + 6.0e0 * u0 - 4.0e0 * up1);
+  if (q == n - 2) r -= dssp * (um2 - 4.0e0 * um1 + 5.0e0 * u0);
+}
+
+// Safe neighbour load along an axis: positions outside 0..n-1 are never used
+// by dissip() (their stencil weight is absent), so they read the centre.
+__device__ __forceinline__ double ld_axis(const double* __restrict__ a, int64_t p, int64_t st, int q, int d, int n) {
+  const int qq = q + d;
+  return (qq >= 0 && qq < n) ? a[p + d * st] : a[p];
+}
+
+template <bool TX, bool NORM>
+__global__ void __launch_bounds__(128) k_rhs(Fields F, Consts K, const Work* __restrict__ work,
+                                             double* __restrict__ partials) {
+  __shared__ double red[5 * 128];
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int64_t NP = F.NP;
+  const int np = Z.nx * Z.ny * Z.nz;
+  const int q = w.first + threadIdx.x;
+  double sq[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (q < np) {
+    const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
+    const int64_t p = Z.off + q;
+    const bool interior = i > 0 && i < Z.nx - 1 && j > 0 && j < Z.ny - 1 && k > 0 && k < Z.nz - 1;
+    if (!interior) {
+      for (int m = 0; m < 5; ++m) F.rhs[m * NP + p] = F.forcing[m * NP + p];
+    } else {
+      const double* __restrict__ u = F.u;
+      const double* __restrict__ pr = F.prim;
+      const double* us = pr + PR_US * NP;
+      const double* vs = pr + PR_VS * NP;
+      const double* ws = pr + PR_WS * NP;
+      const double* qs = pr + PR_QS * NP;
+      const double* sqr = pr + PR_SQUARE * NP;
+      const double* ri = pr + PR_RHOI * NP;
+      double r[5];
+      for (int m = 0; m < 5; ++m) r[m] = F.forcing[m * NP + p];
+      const int64_t sx = 1, sy = Z.nx, sz = (int64_t)Z.nx * Z.ny;
+      const double c1 = K.c1, c2 = K.c2, con43 = K.con43, dssp = K.dssp;
+      // ---------------- xi direction ----------------
+      {
+        const int64_t a = p + sx, b = p - sx;
+        const double uijk = us[p], up1 = us[a], um1 = us[b];
+        r[0] += K.dx1tx1 * (u[a] - 2.0e0 * u[p] + u[b]) - K.tx2 * (u[NP + a] - u[NP + b]);
+        r[1] += K.dx2tx1 * (u[NP + a] - 2.0e0 * u[NP + p] + u[NP + b]) + K.xxcon2 * con43 * (up1 - 2.0e0 * uijk + um1) -
+                K.tx2 * (u[NP + a] * up1 - u[NP + b] * um1 + (u[4 * NP + a] - sqr[a] - u[4 * NP + b] + sqr[b]) * c2);
+        r[2] += K.dx3tx1 * (u[2 * NP + a] - 2.0e0 * u[2 * NP + p] + u[2 * NP + b]) +
+                K.xxcon2 * (vs[a] - 2.0e0 * vs[p] + vs[b]) - K.tx2 * (u[2 * NP + a] * up1 - u[2 * NP + b] * um1);
+        r[3] += K.dx4tx1 * (u[3 * NP + a] - 2.0e0 * u[3 * NP + p] + u[3 * NP + b]) +
+                K.xxcon2 * (ws[a] - 2.0e0 * ws[p] + ws[b]) - K.tx2 * (u[3 * NP + a] * up1 - u[3 * NP + b] * um1);
+        r[4] += K.dx5tx1 * (u[4 * NP + a] - 2.0e0 * u[4 * NP + p] + u[4 * NP + b]) +
+                K.xxcon3 * (qs[a] - 2.0e0 * qs[p] + qs[b]) + K.xxcon4 * (up1 * up1 - 2.0e0 * uijk * uijk + um1 * um1) +
+                K.xxcon5 * (u[4 * NP + a] * ri[a] - 2.0e0 * u[4 * NP + p] * ri[p] + u[4 * NP + b] * ri[b]) -
+                K.tx2 * ((c1 * u[4 * NP + a] - c2 * sqr[a]) * up1 - (c1 * u[4 * NP + b] - c2 * sqr[b]) * um1);
+        for (int m = 0; m < 5; ++m) {
+          const double* um = u + m * NP;
+          dissip(r[m], i, Z.nx, dssp, ld_axis(um, p, sx, i, -2, Z.nx), um[p - sx], um[p], um[p + sx],
+                 ld_axis(um, p, sx, i, 2, Z.nx));
+        }
+      }
+      // ---------------- eta direction ----------------
+      {
+        const int64_t a = p + sy, b = p - sy;
+        const double vijk = vs[p], vp1 = vs[a], vm1 = vs[b];
+        r[0] += K.dy1ty1 * (u[a] - 2.0e0 * u[p] + u[b]) - K.ty2 * (u[2 * NP + a] - u[2 * NP + b]);
+        r[1] += K.dy2ty1 * (u[NP + a] - 2.0e0 * u[NP + p] + u[NP + b]) + K.yycon2 * (us[a] - 2.0e0 * us[p] + us[b]) -
+                K.ty2 * (u[NP + a] * vp1 - u[NP + b] * vm1);
+        r[2] += K.dy3ty1 * (u[2 * NP + a] - 2.0e0 * u[2 * NP + p] + u[2 * NP + b]) +
+                K.yycon2 * con43 * (vp1 - 2.0e0 * vijk + vm1) -
+                K.ty2 * (u[2 * NP + a] * vp1 - u[2 * NP + b] * vm1 + (u[4 * NP + a] - sqr[a] - u[4 * NP + b] + sqr[b]) * c2);
+        r[3] += K.dy4ty1 * (u[3 * NP + a] - 2.0e0 * u[3 * NP + p] + u[3 * NP + b]) +
+                K.yycon2 * (ws[a] - 2.0e0 * ws[p] + ws[b]) - K.ty2 * (u[3 * NP + a] * vp1 - u[3 * NP + b] * vm1);
+        r[4] += K.dy5ty1 * (u[4 * NP + a] - 2.0e0 * u[4 * NP + p] + u[4 * NP + b]) +
+                K.yycon3 * (qs[a] - 2.0e0 * qs[p] + qs[b]) + K.yycon4 * (vp1 * vp1 - 2.0e0 * vijk * vijk + vm1 * vm1) +
+                K.yycon5 * (u[4 * NP + a] * ri[a] - 2.0e0 * u[4 * NP + p] * ri[p] + u[4 * NP + b] * ri[b]) -
+                K.ty2 * ((c1 * u[4 * NP + a] - c2 * sqr[a]) * vp1 - (c1 * u[4 * NP + b] - c2 * sqr[b]) * vm1);
+        for (int m = 0; m < 5; ++m) {
+          const double* um = u + m * NP;
+          dissip(r[m], j, Z.ny, dssp, ld_axis(um, p, sy, j, -2, Z.ny), um[p - sy], um[p], um[p + sy],
+                 ld_axis(um, p, sy, j, 2, Z.ny));
+        }
+      }
+      // ---------------- zeta direction ----------------
+      {
+        const int64_t a = p + sz, b = p - sz;
+        const double wijk = ws[p], wp1 = ws[a], wm1 = ws[b];
+        r[0] += K.dz1tz1 * (u[a] - 2.0e0 * u[p] + u[b]) - K.tz2 * (u[3 * NP + a] - u[3 * NP + b]);
+        r[1] += K.dz2tz1 * (u[NP + a] - 2.0e0 * u[NP + p] + u[NP + b]) + K.zzcon2 * (us[a] - 2.0e0 * us[p] + us[b]) -
+                K.tz2 * (u[NP + a] * wp1 - u[NP + b] * wm1);
+        r[2] += K.dz3tz1 * (u[2 * NP + a] - 2.0e0 * u[2 * NP + p] + u[2 * NP + b]) +
+                K.zzcon2 * (vs[a] - 2.0e0 * vs[p] + vs[b]) - K.tz2 * (u[2 * NP + a] * wp1 - u[2 * NP + b] * wm1);
+        r[3] += K.dz4tz1 * (u[3 * NP + a] - 2.0e0 * u[3 * NP + p] + u[3 * NP + b]) +
+                K.zzcon2 * con43 * (wp1 - 2.0e0 * wijk + wm1) -
+                K.tz2 * (u[3 * NP + a] * wp1 - u[3 * NP + b] * wm1 + (u[4 * NP + a] - sqr[a] - u[4 * NP + b] + sqr[b]) * c2);
+        r[4] += K.dz5tz1 * (u[4 * NP + a] - 2.0e0 * u[4 * NP + p] + u[4 * NP + b]) +
+                K.zzcon3 * (qs[a] - 2.0e0 * qs[p] + qs[b]) + K.zzcon4 * (wp1 * wp1 - 2.0e0 * wijk * wijk + wm1 * wm1) +
+                K.zzcon5 * (u[4 * NP + a] * ri[a] - 2.0e0 * u[4 * NP + p] * ri[p] + u[4 * NP + b] * ri[b]) -
+                K.tz2 * ((c1 * u[4 * NP + a] - c2 * sqr[a]) * wp1 - (c1 * u[4 * NP + b] - c2 * sqr[b]) * wm1);
+        for (int m = 0; m < 5; ++m) {
+          const double* um = u + m * NP;
+          dissip(r[m], k, Z.nz, dssp, ld_axis(um, p, sz, k, -2, Z.nz), um[p - sz], um[p], um[p + sz],
+                 ld_axis(um, p, sz, k, 2, Z.nz));
+        }
+      }
+      for (int m = 0; m < 5; ++m) r[m] *= K.dt;
+      if (NORM)
+        for (int m = 0; m < 5; ++m) sq[m] = r[m] * r[m];
+      if (TX) {
+        // txinvr (src/SP/txinvr.jl:28-49)
+        const double ru1 = ri[p], uu = us[p], vv = vs[p], ww = ws[p], ac = pr[PR_SPEED * NP + p];
+        const double ac2inv = 1.0 / (ac * ac);
+        const double r1 = r[0], r2 = r[1], r3 = r[2], r4 = r[3], r5 = r[4];
+        const double t1 = K.c2 * ac2inv * (qs[p] * r1 - uu * r2 - vv * r3 - ww * r4 + r5);
+        const double t2 = K.bt * ru1 * (uu * r1 - r2);
+        const double t3 = (K.bt * ru1 * ac) * t1;
+        r[0] = r1 - t1;
+        r[1] = -ru1 * (ww * r1 - r4);
+        r[2] = ru1 * (vv * r1 - r3);
+        r[3] = -t2 + t3;
+        r[4] = t2 + t3;
+      }
+      for (int m = 0; m < 5; ++m) F.rhs[m * NP + p] = r[m];
+    }
+  }
+  if (NORM) {
+    block_sum5(sq, red);
+    if (threadIdx.x == 0)
+      for (int m = 0; m < 5; ++m) partials[blockIdx.x * 5 + m] = sq[m];
+  }
+}
+
+// ============================================================================
+// BT block-tridiagonal line solve, one thread per line.
+// Reference: x_solve_cell / y_solve_cell / z_solve_cell and the back
+// substitutions (src/BT/x_solve.jl:444-488,501-1746, src/BT/y_solve.jl:443-820,
+// src/BT/z_solve.jl:438-864) with matvec_sub, matmul_sub2, binvcrhs, binvrhs
+// (src/BT/solve_subs.jl:4-37,333-460,468-862).
+//
+// The Jacobians fjac/njac have structural zeros; terms with a structural
+// zero factor are skipped.  That is exact: in the reference such a term
+// contributes +-0, and x - (+-0) == x for every nonzero x.  The boundary
+// steps (binvcrhs at point 0 with B = I, C = 0; binvrhs at point n-1 with
+// A = 0, B = I; back substitution at point 0 with C = 0) are exact no-ops in
+// the reference and are skipped for the same reason.
+// C'_p (the 5x5 block left by binvcrhs) goes to the line scratch
+// lhsc[(p*25 + e) * nlt + global_line] (coalesced across the CTA's lines);
+// the forward-eliminated rhs goes back into rhs in place.
+// ============================================================================
+
+// Structural nonzeros of fjac / njac per sweep direction.
+template <int DIR>
+__host__ __device__ constexpr bool fnz(int a, int b) {
+  return DIR == 0 ? (a == 0 ? b == 1 : a == 1 ? true : a == 2 ? (b <= 2) : a == 3 ? (b == 0 || b == 1 || b == 3) : true)
+       : DIR == 1 ? (a == 0 ? b == 2 : a == 1 ? (b <= 2) : a == 2 ? true : a == 3 ? (b == 0 || b == 2 || b == 3) : true)
+                  : (a == 0 ? b == 3 : a == 1 ? (b == 0 || b == 1 || b == 3) : a == 2 ? (b == 0 || b == 2 || b == 3) : true);
+}
+__host__ __device__ constexpr bool nnz(int a, int b) {
+  return a == 0 ? false : a == 4 ? true : (b == 0 || b == a);
+}
+template <int DIR>
+__host__ __device__ constexpr bool anz(int a, int b) { return fnz<DIR>(a, b) || nnz(a, b) || a == b; }
+__host__ __device__ constexpr bool bnz(int a, int b) { return nnz(a, b) || a == b; }
+
+// fjac / njac at one point (src/BT/x_solve.jl:536-609, y_solve.jl:543-613,
+// z_solve.jl:537-618); only structural nonzeros are written.
+template <int DIR, typename T>
+__device__ __forceinline__ void bt_jac(const Consts& K, T tmp1, T u2, T u3, T u4, T u5, T q, T f[5][5], T n[5][5]) {
+  const T c1 = (T)K.c1, c2 = (T)K.c2, c3c4 = (T)K.c3c4, c1345 = (T)K.c1345, con43 = (T)K.con43;
+  const T tmp2 = tmp1 * tmp1;
+  const T tmp3 = tmp1 * tmp2;
+  if (DIR == 0) {
+    f[0][1] = (T)1.0;
+    f[1][0] = -(u2 * tmp2 * u2) + c2 * q;
+    f[1][1] = ((T)2.0 - c2) * (u2 * tmp1);
+    f[1][2] = -c2 * (u3 * tmp1);
+    f[1][3] = -c2 * (u4 * tmp1);
+    f[1][4] = c2;
+    f[2][0] = -(u2 * u3) * tmp2;
+    f[2][1] = u3 * tmp1;
+    f[2][2] = u2 * tmp1;
+    f[3][0] = -(u2 * u4) * tmp2;
+    f[3][1] = u4 * tmp1;
+    f[3][3] = u2 * tmp1;
+    f[4][0] = (c2 * (T)2.0 * q - c1 * (u5 * tmp1)) * (u2 * tmp1);
+    f[4][1] = c1 * u5 * tmp1 - c2 * (u2 * u2 * tmp2 + q);
+    f[4][2] = -c2 * (u3 * u2) * tmp2;
+    f[4][3] = -c2 * (u4 * u2) * tmp2;
+    f[4][4] = c1 * (u2 * tmp1);
+    n[1][0] = -con43 * c3c4 * tmp2 * u2;
+    n[1][1] = con43 * c3c4 * tmp1;
+    n[2][0] = -c3c4 * tmp2 * u3;
+    n[2][2] = c3c4 * tmp1;
+    n[3][0] = -c3c4 * tmp2 * u4;
+    n[3][3] = c3c4 * tmp1;
+    n[4][0] = -(con43 * c3c4 - c1345) * tmp3 * (u2 * u2) - (c3c4 - c1345) * tmp3 * (u3 * u3) -
+              (c3c4 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5;
+    n[4][1] = (con43 * c3c4 - c1345) * tmp2 * u2;
+    n[4][2] = (c3c4 - c1345) * tmp2 * u3;
+    n[4][3] = (c3c4 - c1345) * tmp2 * u4;
+    n[4][4] = (c1345) * tmp1;
+  } else if (DIR == 1) {
+    f[0][2] = (T)1.0;
+    f[1][0] = -(u2 * u3) * tmp2;
+    f[1][1] = u3 * tmp1;
+    f[1][2] = u2 * tmp1;
+    f[2][0] = -(u3 * u3 * tmp2) + c2 * q;
+    f[2][1] = -c2 * u2 * tmp1;
+    f[2][2] = ((T)2.0 - c2) * u3 * tmp1;
+    f[2][3] = -c2 * u4 * tmp1;
+    f[2][4] = c2;
+    f[3][0] = -(u3 * u4) * tmp2;
+    f[3][2] = u4 * tmp1;
+    f[3][3] = u3 * tmp1;
+    f[4][0] = (c2 * (T)2.0 * q - c1 * u5 * tmp1) * u3 * tmp1;
+    f[4][1] = -c2 * u2 * u3 * tmp2;
+    f[4][2] = c1 * u5 * tmp1 - c2 * (q + u3 * u3 * tmp2);
+    f[4][3] = -c2 * (u3 * u4) * tmp2;
+    f[4][4] = c1 * u3 * tmp1;
+    n[1][0] = -c3c4 * tmp2 * u2;
+    n[1][1] = c3c4 * tmp1;
+    n[2][0] = -con43 * c3c4 * tmp2 * u3;
+    n[2][2] = con43 * c3c4 * tmp1;
+    n[3][0] = -c3c4 * tmp2 * u4;
+    n[3][3] = c3c4 * tmp1;
+    n[4][0] = -(c3c4 - c1345) * tmp3 * (u2 * u2) - (con43 * c3c4 - c1345) * tmp3 * (u3 * u3) -
+              (c3c4 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5;
+    n[4][1] = (c3c4 - c1345) * tmp2 * u2;
+    n[4][2] = (con43 * c3c4 - c1345) * tmp2 * u3;
+    n[4][3] = (c3c4 - c1345) * tmp2 * u4;
+    n[4][4] = (c1345) * tmp1;
+  } else {
+    const T c3 = (T)K.c3, c4 = (T)K.c4;
+    f[0][3] = (T)1.0;
+    f[1][0] = -(u2 * u4) * tmp2;
+    f[1][1] = u4 * tmp1;
+    f[1][3] = u2 * tmp1;
+    f[2][0] = -(u3 * u4) * tmp2;
+    f[2][2] = u4 * tmp1;
+    f[2][3] = u3 * tmp1;
+    f[3][0] = -(u4 * u4 * tmp2) + c2 * q;
+    f[3][1] = -c2 * u2 * tmp1;
+    f[3][2] = -c2 * u3 * tmp1;
+    f[3][3] = ((T)2.0 - c2) * u4 * tmp1;
+    f[3][4] = c2;
+    f[4][0] = (c2 * (T)2.0 * q - c1 * (u5 * tmp1)) * (u4 * tmp1);
+    f[4][1] = -c2 * (u2 * u4) * tmp2;
+    f[4][2] = -c2 * (u3 * u4) * tmp2;
+    f[4][3] = c1 * (u5 * tmp1) - c2 * (q + u4 * u4 * tmp2);
+    f[4][4] = c1 * u4 * tmp1;
+    n[1][0] = -c3c4 * tmp2 * u2;
+    n[1][1] = c3c4 * tmp1;
+    n[2][0] = -c3c4 * tmp2 * u3;
+    n[2][2] = c3c4 * tmp1;
+    n[3][0] = -con43 * c3c4 * tmp2 * u4;
+    n[3][3] = con43 * c3 * c4 * tmp1;
+    n[4][0] = -(c3c4 - c1345) * tmp3 * (u2 * u2) - (c3c4 - c1345) * tmp3 * (u3 * u3) -
+              (con43 * c3c4 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5;
+    n[4][1] = (c3c4 - c1345) * tmp2 * u2;
+    n[4][2] = (c3c4 - c1345) * tmp2 * u3;
+    n[4][3] = (con43 * c3c4 - c1345) * tmp2 * u4;
+    n[4][4] = (c1345) * tmp1;
+  }
+}
+
+// lhsa at the point after the Jacobian point: -tmp2*f - tmp1*n - tmp1*d (diag).
+template <int DIR, typename T>
+__device__ __forceinline__ void bt_asm_a(const T f[5][5], const T n[5][5], T tmp1, T tmp2, const T dd[5], T A[5][5]) {
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      if (!anz<DIR>(a, b)) continue;
+      T t;
+      bool have = false;
+      if (fnz<DIR>(a, b)) { t = -tmp2 * f[a][b]; have = true; }
+      if (nnz(a, b)) { t = have ? t - tmp1 * n[a][b] : -(tmp1 * n[a][b]); have = true; }
+      if (a == b) { t = have ? t - tmp1 * dd[a] : -(tmp1 * dd[a]); }
+      A[a][b] = t;
+    }
+}
+
+// lhsc at the point before the Jacobian point: tmp2*f - tmp1*n - tmp1*d (diag).
+template <int DIR, typename T>
+__device__ __forceinline__ void bt_asm_c(const T f[5][5], const T n[5][5], T tmp1, T tmp2, const T dd[5], T C[5][5]) {
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      T t = (T)0.0;
+      bool have = false;
+      if (fnz<DIR>(a, b)) { t = tmp2 * f[a][b]; have = true; }
+      if (nnz(a, b)) { t = have ? t - tmp1 * n[a][b] : -(tmp1 * n[a][b]); have = true; }
+      if (a == b) { t = have ? t - tmp1 * dd[a] : -(tmp1 * dd[a]); }
+      C[a][b] = t;
+    }
+}
+
+// lhsb at the Jacobian point: 1 + tmp1*2*n + tmp1*2*d (diag), tmp1*2*n off-diag.
+template <typename T>
+__device__ __forceinline__ void bt_asm_b(const T n[5][5], T tmp1, const T dd[5], T B[5][5]) {
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      if (!bnz(a, b)) continue;
+      if (a == b) {
+        T t = (T)1.0;
+        if (nnz(a, b)) t = t + tmp1 * (T)2.0 * n[a][b];
+        B[a][b] = t + tmp1 * (T)2.0 * dd[a];
+      } else {
+        B[a][b] = tmp1 * (T)2.0 * n[a][b];
+      }
+    }
+}
+
+// binvcrhs (src/BT/solve_subs.jl:468-723): Gauss-Jordan on B, no pivoting,
+// applied to C and r.
+template <typename T>
+__device__ __forceinline__ void binvcrhs(T B[5][5], T C[5][5], T r[5]) {
+#pragma unroll
+  for (int p = 0; p < 5; ++p) {
+    const T pivot = (T)1.0 / B[p][p];
+#pragma unroll
+    for (int c = p + 1; c < 5; ++c) B[p][c] *= pivot;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) C[p][c] *= pivot;
+    r[p] *= pivot;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      if (q == p) continue;
+      const T coeff = B[q][p];
+#pragma unroll
+      for (int c = p + 1; c < 5; ++c) B[q][c] -= coeff * B[p][c];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) C[q][c] -= coeff * C[p][c];
+      r[q] -= coeff * r[p];
+    }
+  }
+}
+
+template <int DIR, typename T>
+__device__ __forceinline__ void bt_load_point(const Fields& F, int64_t pt, T& ri, T& u2, T& u3, T& u4, T& u5, T& q) {
+  const int64_t NP = F.NP;
+  ri = (T)F.prim[PR_RHOI * NP + pt];
+  q = (T)F.prim[PR_QS * NP + pt];
+  u2 = (T)F.u[NP + pt];
+  u3 = (T)F.u[2 * NP + pt];
+  u4 = (T)F.u[3 * NP + pt];
+  u5 = (T)F.u[4 * NP + pt];
+}
+
+// out: where the forward-eliminated rhs and the solution go (rhs itself for
+// the in-place solve; a separate buffer when a refinement pass follows).
+template <int DIR, typename T>
+__global__ void __launch_bounds__(128) k_bt_solve(Fields F, Consts K, const Work* __restrict__ work,
+                                                  T* __restrict__ lhsc, int64_t nlt, int add_u,
+                                                  double* __restrict__ out) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  double* __restrict__ rhs = F.rhs;
+
+  const T tmp1 = (T)(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
+  const T tmp2 = (T)(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  T dd[5];
+  if (DIR == 0) { dd[0] = (T)K.dx1; dd[1] = (T)K.dx2; dd[2] = (T)K.dx3; dd[3] = (T)K.dx4; dd[4] = (T)K.dx5; }
+  else if (DIR == 1) { dd[0] = (T)K.dy1; dd[1] = (T)K.dy2; dd[2] = (T)K.dy3; dd[3] = (T)K.dy4; dd[4] = (T)K.dy5; }
+  else { dd[0] = (T)K.dz1; dd[1] = (T)K.dz2; dd[2] = (T)K.dz3; dd[3] = (T)K.dz4; dd[4] = (T)K.dz5; }
+
+  T rp[5];          // r' at p-1
+  T Cp[5][5];       // C' at p-1
+  T Acur[5][5];     // lhsa at p   (structural nonzeros only)
+  T Anext[5][5];    // lhsa at p+1
+  T Bcur[5][5];     // lhsb at p   (structural nonzeros only)
+  T f[5][5], nj[5][5];
+  T ri, u2, u3, u4, u5, q;
+
+#pragma unroll
+  for (int m = 0; m < 5; ++m) rp[m] = (T)rhs[m * NP + base];
+  // Jacobian at point 0 -> lhsa at 1; at point 1 -> lhsb at 1 and lhsa at 2.
+  bt_load_point<DIR, T>(F, base, ri, u2, u3, u4, u5, q);
+  bt_jac<DIR, T>(K, ri, u2, u3, u4, u5, q, f, nj);
+  bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Acur);
+  bt_load_point<DIR, T>(F, base + st, ri, u2, u3, u4, u5, q);
+  bt_jac<DIR, T>(K, ri, u2, u3, u4, u5, q, f, nj);
+  bt_asm_b<T>(nj, tmp1, dd, Bcur);
+  if (n - 2 >= 2) bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Anext);
+
+  for (int p = 1; p <= n - 2; ++p) {
+    const int64_t pt = base + p * st;
+    T r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) r[m] = (T)rhs[m * NP + pt];
+    // matvec_sub(lhsa_p, r'_{p-1}, r_p): the row sum is formed first.
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      T s;
+      bool have = false;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        if (!anz<DIR>(m, c)) continue;
+        s = have ? s + Acur[m][c] * rp[c] : Acur[m][c] * rp[c];
+        have = true;
+      }
+      r[m] -= s;
+    }
+    // lhsb_p (full) = lhsb_p - lhsa_p * C'_{p-1}, one term at a time; C'_0 = 0.
+    T B[5][5];
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) {
+        T t = bnz(a, b) ? Bcur[a][b] : (T)0.0;
+        bool have = bnz(a, b);
+        if (p > 1) {
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            if (!anz<DIR>(a, c)) continue;
+            t = have ? t - Acur[a][c] * Cp[c][b] : -(Acur[a][c] * Cp[c][b]);
+            have = true;
+          }
+        }
+        B[a][b] = t;
+      }
+    // Jacobian at p+1 -> lhsc_p, lhsb_{p+1}, lhsa_{p+2}
+    bt_load_point<DIR, T>(F, pt + st, ri, u2, u3, u4, u5, q);
+    bt_jac<DIR, T>(K, ri, u2, u3, u4, u5, q, f, nj);
+    T C[5][5];
+    bt_asm_c<DIR, T>(f, nj, tmp1, tmp2, dd, C);
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b)
+        if (anz<DIR>(a, b)) Acur[a][b] = Anext[a][b];
+    if (p + 1 <= n - 2) bt_asm_b<T>(nj, tmp1, dd, Bcur);
+    if (p + 2 <= n - 2) bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Anext);
+    binvcrhs<T>(B, C, r);
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) {
+        Cp[a][b] = C[a][b];
+        lhsc[((int64_t)p * 25 + a * 5 + b) * nlt + gl] = C[a][b];
+      }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      rp[m] = r[m];
+      out[m * NP + pt] = (double)r[m];
+    }
+  }
+  // back substitution: r_p -= C'_p r_{p+1}, one term at a time; the boundary
+  // value r_{n-1} is unchanged by the forward sweep.
+  T rn[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) rn[m] = (T)rhs[m * NP + base + (n - 1) * st];
+  if (out != rhs) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      out[m * NP + base] = rhs[m * NP + base];
+      out[m * NP + base + (n - 1) * st] = rhs[m * NP + base + (n - 1) * st];
+    }
+  }
+  for (int p = n - 2; p >= 1; --p) {
+    const int64_t pt = base + p * st;
+    T r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) r[m] = (p == n - 2) ? rp[m] : (T)out[m * NP + pt];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) r[m] -= lhsc[((int64_t)p * 25 + m * 5 + c) * nlt + gl] * rn[c];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double v = (double)r[m];
+      out[m * NP + pt] = v;
+      if (add_u) F.u[m * NP + pt] += v;
+      rn[m] = r[m];
+    }
+  }
+}
+
+// ============================================================================
+// Refinement pass of the mixed-precision BT sweep.  x0 (in xw) is the FP32
+// solution of T x = b (b = rhs).  This pass forms the residual
+// r = b - T x0 in FP64 and solves T d = r in FP32; the result x0 + d goes to
+// rhs (and, after the z sweep, into u).  With F_q = fjac_q x_q and
+// N_q = njac_q x_q, row p of T applied to x is
+//   x_p + tmp2 (F_{p+1} - F_{p-1}) - tmp1 (N_{p-1} - 2 N_p + N_{p+1})
+//       - tmp1 D (x_{p-1} - 2 x_p + x_{p+1})
+// (lhsa/lhsb/lhsc of src/BT/x_solve.jl:613-708 applied to x), so the FP64
+// work is one Jacobian evaluation and two sparse 5x5 products per point.
+// Boundary rows are identity rows whose residual is exactly zero.
+// ============================================================================
+template <int DIR>
+__device__ __forceinline__ void bt_jx(const double f[5][5], const double n[5][5], const double x[5], double Fx[5],
+                                      double Nx[5]) {
+#pragma unroll
+  for (int a = 0; a < 5; ++a) {
+    double sf = 0.0, sn = 0.0;
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      if (fnz<DIR>(a, b)) sf += f[a][b] * x[b];
+      if (nnz(a, b)) sn += n[a][b] * x[b];
+    }
+    Fx[a] = sf;
+    Nx[a] = sn;
+  }
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) k_bt_refine(Fields F, Consts K, const Work* __restrict__ work,
+                                                   float* __restrict__ lhsc, int64_t nlt, int add_u,
+                                                   const double* __restrict__ xw) {
+  using T = float;
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  double* __restrict__ rhs = F.rhs;
+
+  const double t1d = DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1;
+  const double t2d = DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2;
+  const T tmp1 = (T)t1d, tmp2 = (T)t2d;
+  double ddd[5];
+  if (DIR == 0) { ddd[0] = K.dx1; ddd[1] = K.dx2; ddd[2] = K.dx3; ddd[3] = K.dx4; ddd[4] = K.dx5; }
+  else if (DIR == 1) { ddd[0] = K.dy1; ddd[1] = K.dy2; ddd[2] = K.dy3; ddd[3] = K.dy4; ddd[4] = K.dy5; }
+  else { ddd[0] = K.dz1; ddd[1] = K.dz2; ddd[2] = K.dz3; ddd[3] = K.dz4; ddd[4] = K.dz5; }
+  T dd[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) dd[m] = (T)ddd[m];
+
+  double fd[5][5], nd[5][5];
+  T f[5][5], nj[5][5];
+  double xm[5], x0[5], xp[5];       // x0 at p-1, p, p+1
+  double Fm[5], F0[5], Fp[5], Nm[5], N0[5], Np[5];
+  T rp[5], Cp[5][5], Acur[5][5], Anext[5][5], Bcur[5][5];
+
+  auto jac_at = [&](int64_t pt, double x[5], double Fx[5], double Nx[5]) {
+    const double ri = F.prim[PR_RHOI * NP + pt], q = F.prim[PR_QS * NP + pt];
+    bt_jac<DIR, double>(K, ri, F.u[NP + pt], F.u[2 * NP + pt], F.u[3 * NP + pt], F.u[4 * NP + pt], q, fd, nd);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) x[m] = xw[m * NP + pt];
+    bt_jx<DIR>(fd, nd, x, Fx, Nx);
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) {
+        if (fnz<DIR>(a, b)) f[a][b] = (T)fd[a][b];
+        if (nnz(a, b)) nj[a][b] = (T)nd[a][b];
+      }
+  };
+
+  jac_at(base, xm, Fm, Nm);
+  bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Acur);
+  jac_at(base + st, x0, F0, N0);
+  bt_asm_b<T>(nj, tmp1, dd, Bcur);
+  if (n - 2 >= 2) bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Anext);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) rp[m] = (T)0.0;  // the boundary residual is exactly zero
+
+  for (int p = 1; p <= n - 2; ++p) {
+    const int64_t pt = base + p * st;
+    jac_at(pt + st, xp, Fp, Np);
+    T r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double tx = x0[m] + t2d * (Fp[m] - Fm[m]) - t1d * (Nm[m] - 2.0 * N0[m] + Np[m]) -
+                        t1d * ddd[m] * (xm[m] - 2.0 * x0[m] + xp[m]);
+      r[m] = (T)(rhs[m * NP + pt] - tx);
+    }
+    if (p > 1) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        T s = (T)0.0;
+#pragma unroll
+        for (int c = 0; c < 5; ++c)
+          if (anz<DIR>(m, c)) s += Acur[m][c] * rp[c];
+        r[m] -= s;
+      }
+    }
+    T B[5][5];
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) {
+        T t = bnz(a, b) ? Bcur[a][b] : (T)0.0;
+        if (p > 1) {
+#pragma unroll
+          for (int c = 0; c < 5; ++c)
+            if (anz<DIR>(a, c)) t -= Acur[a][c] * Cp[c][b];
+        }
+        B[a][b] = t;
+      }
+    T C[5][5];
+    bt_asm_c<DIR, T>(f, nj, tmp1, tmp2, dd, C);
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b)
+        if (anz<DIR>(a, b)) Acur[a][b] = Anext[a][b];
+    if (p + 1 <= n - 2) bt_asm_b<T>(nj, tmp1, dd, Bcur);
+    if (p + 2 <= n - 2) bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Anext);
+    binvcrhs<T>(B, C, r);
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) {
+        Cp[a][b] = C[a][b];
+        lhsc[((int64_t)p * 25 + a * 5 + b) * nlt + gl] = C[a][b];
+      }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      rp[m] = r[m];
+      rhs[m * NP + pt] = (double)r[m];   // b_p is no longer needed
+      xm[m] = x0[m]; x0[m] = xp[m];
+      Fm[m] = F0[m]; F0[m] = Fp[m];
+      Nm[m] = N0[m]; N0[m] = Np[m];
+    }
+  }
+  // back substitution of the correction, then x = x0 + d
+  T dn[5] = {(T)0.0, (T)0.0, (T)0.0, (T)0.0, (T)0.0};
+  for (int p = n - 2; p >= 1; --p) {
+    const int64_t pt = base + p * st;
+    T d[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) d[m] = (p == n - 2) ? rp[m] : (T)rhs[m * NP + pt];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) d[m] -= lhsc[((int64_t)p * 25 + m * 5 + c) * nlt + gl] * dn[c];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double v = xw[m * NP + pt] + (double)d[m];
+      rhs[m * NP + pt] = v;
+      if (add_u) F.u[m * NP + pt] += v;
+      dn[m] = d[m];
+    }
+  }
+}
+
+// ============================================================================
+// SP scalar pentadiagonal line solve, one thread per line.
+// lhsx / lhsy / lhsz assembly (src/SP/lhsx.jl:27-111, lhsy.jl, lhsz.jl), the
+// Thomas forward elimination and back substitution (src/SP/x_solve.jl:203-313,
+// 456-512; y_solve.jl, z_solve.jl), then ninvr / pinvr / tzetar
+// (src/SP/ninvr.jl:19-32, pinvr.jl:20-33, tzetar.jl:27-52) and, after the z
+// sweep, add (src/SP/add.jl:14-23).  Rows 0 and n-1 are the identity rows
+// lhsinit leaves in the persistent lhs (src/SP/initialize.jl:235-256); they go
+// through the same elimination as in the reference.  The bands l4, l5 of each
+// of the 3 systems are kept for the back substitution in
+// scr[(p*6 + b) * nlt + global_line].
+// ============================================================================
+struct SpBands {
+  double l[3][5];
+};
+
+template <int DIR, typename T>
+__device__ __forceinline__ void sp_assemble(const Consts& K, int q, int n, const double cv[3], const double rhon[3],
+                                            const double spd[3], T L[3][5]) {
+  if (q == 0 || q == n - 1) {
+#pragma unroll
+    for (int s = 0; s < 3; ++s) { L[s][0] = (T)0.0; L[s][1] = (T)0.0; L[s][2] = (T)1.0; L[s][3] = (T)0.0; L[s][4] = (T)0.0; }
+    return;
+  }
+  const double dtt1 = DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1;
+  const double dtt2 = DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2;
+  const double c2dtt1 = DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1;
+  double L1 = 0.0e0;
+  double L2 = -dtt2 * cv[0] - dtt1 * rhon[0];
+  double L3 = 1.0e0 + c2dtt1 * rhon[1];
+  double L4 = dtt2 * cv[2] - dtt1 * rhon[2];
+  double L5 = 0.0e0;
+  if (q == 1) { L3 += K.comz5; L4 -= K.comz4; L5 += K.comz1; }
+  if (q == 2) { L2 -= K.comz4; L3 += K.comz6; L4 -= K.comz4; L5 += K.comz1; }
+  if (q >= 3 && q <= n - 4) { L1 += K.comz1; L2 -= K.comz4; L3 += K.comz6; L4 -= K.comz4; L5 += K.comz1; }
+  if (q == n - 3) { L1 += K.comz1; L2 -= K.comz4; L3 += K.comz6; L4 -= K.comz4; }
+  if (q == n - 2) { L1 += K.comz1; L2 -= K.comz4; L3 += K.comz5; }
+  L[0][0] = (T)L1; L[0][1] = (T)L2; L[0][2] = (T)L3; L[0][3] = (T)L4; L[0][4] = (T)L5;
+  L[1][0] = (T)L1; L[1][1] = (T)(L2 - dtt2 * spd[0]); L[1][2] = (T)L3; L[1][3] = (T)(L4 + dtt2 * spd[2]); L[1][4] = (T)L5;
+  L[2][0] = (T)L1; L[2][1] = (T)(L2 + dtt2 * spd[0]); L[2][2] = (T)L3; L[2][3] = (T)(L4 - dtt2 * spd[2]); L[2][4] = (T)L5;
+}
+
+template <int DIR>
+__device__ __forceinline__ void sp_geom(const Fields& F, const Consts& K, int64_t pt, double& cv, double& rhon,
+                                        double& spd) {
+  const int64_t NP = F.NP;
+  const double ru1 = K.c3c4 * F.prim[PR_RHOI * NP + pt];
+  cv = F.prim[(DIR == 0 ? PR_US : DIR == 1 ? PR_VS : PR_WS) * NP + pt];
+  const double da = DIR == 0 ? K.dx2 : DIR == 1 ? K.dy3 : K.dz4;
+  const double db = DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5;
+  const double dm = DIR == 0 ? K.dxmax : DIR == 1 ? K.dymax : K.dzmax;
+  const double dc = DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1;
+  rhon = fmax(fmax(fmax(da + K.con43 * ru1, db + K.c1c5 * ru1), dm + ru1), dc);
+  spd = F.prim[PR_SPEED * NP + pt];
+}
+
+// system s covers rhs components [s==0 ? 0..2 : s==1 ? 3 : 4]
+#define SP_M0(s) ((s) == 0 ? 0 : (s) + 2)
+#define SP_M1(s) ((s) == 0 ? 2 : (s) + 2)
+
+// out / transform: the in-place solve writes the transformed solution into
+// rhs (out == rhs, transform = 1); the first pass of the refined solve writes
+// the untransformed solution of the interior points to a separate buffer.
+template <int DIR, typename T>
+__global__ void __launch_bounds__(128) k_sp_solve(Fields F, Consts K, const Work* __restrict__ work,
+                                                  T* __restrict__ scr, int64_t nlt, int add_u,
+                                                  double* __restrict__ out, int transform) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  double* __restrict__ rhs = F.rhs;
+
+  // geometry window for assembling row q: values at q-1, q, q+1
+  double gcv[4], grh[4], gsp[4];   // values at rows a-1 .. a+2 of a sliding window
+  T cur3[3], cur4[3], cur5[3];     // row p   (l3, l4, l5), modified
+  T nx2[3], nx3[3], nx4[3], nx5[3];  // row p+1 (l2..l5), modified
+  T rr[3][5];                       // rhs rows p, p+1, p+2
+
+  // rows 0 and 1: assemble
+  {
+    T L0[3][5], L1[3][5];
+    double cv[3], rh[3], sp[3];
+    // row 0 is an identity row; its geometry is not needed.
+    sp_assemble<DIR, T>(K, 0, n, cv, rh, sp, L0);
+    sp_geom<DIR>(F, K, base, gcv[0], grh[0], gsp[0]);
+    sp_geom<DIR>(F, K, base + st, gcv[1], grh[1], gsp[1]);
+    sp_geom<DIR>(F, K, base + 2 * st, gcv[2], grh[2], gsp[2]);
+    cv[0] = gcv[0]; cv[1] = gcv[1]; cv[2] = gcv[2];
+    rh[0] = grh[0]; rh[1] = grh[1]; rh[2] = grh[2];
+    sp[0] = gsp[0]; sp[1] = gsp[1]; sp[2] = gsp[2];
+    sp_assemble<DIR, T>(K, 1, n, cv, rh, sp, L1);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      cur3[s] = L0[s][2]; cur4[s] = L0[s][3]; cur5[s] = L0[s][4];
+      nx2[s] = L1[s][1]; nx3[s] = L1[s][2]; nx4[s] = L1[s][3]; nx5[s] = L1[s][4];
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      rr[0][m] = (T)rhs[m * NP + base];
+      rr[1][m] = (T)rhs[m * NP + base + st];
+    }
+  }
+  // window gcv[0..2] now holds rows 0,1,2.
+  for (int p = 0; p <= n - 3; ++p) {
+    // assemble row p+2 (needs geometry at p+1, p+2, p+3)
+    T L2[3][5];
+    {
+      double cv[3], rh[3], sp[3];
+      const int q = p + 2;
+      if (q + 1 <= n - 1) sp_geom<DIR>(F, K, base + (int64_t)(q + 1) * st, gcv[3], grh[3], gsp[3]);
+      cv[0] = gcv[1]; cv[1] = gcv[2]; cv[2] = gcv[3];
+      rh[0] = grh[1]; rh[1] = grh[2]; rh[2] = grh[3];
+      sp[0] = gsp[1]; sp[1] = gsp[2]; sp[2] = gsp[3];
+      sp_assemble<DIR, T>(K, q, n, cv, rh, sp, L2);
+      gcv[0] = gcv[1]; gcv[1] = gcv[2]; gcv[2] = gcv[3];
+      grh[0] = grh[1]; grh[1] = grh[2]; grh[2] = grh[3];
+      gsp[0] = gsp[1]; gsp[1] = gsp[2]; gsp[2] = gsp[3];
+    }
+    const int64_t pt2 = base + (int64_t)(p + 2) * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) rr[2][m] = (T)rhs[m * NP + pt2];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const T fac1 = (T)1.0 / cur3[s];
+      cur4[s] *= fac1;
+      cur5[s] *= fac1;
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
+      nx3[s] -= nx2[s] * cur4[s];
+      nx4[s] -= nx2[s] * cur5[s];
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
+      T n2 = L2[s][1], n3 = L2[s][2];
+      n2 -= L2[s][0] * cur4[s];
+      n3 -= L2[s][0] * cur5[s];
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[2][m] -= L2[s][0] * rr[0][m];
+      scr[((int64_t)p * 6 + 2 * s) * nlt + gl] = cur4[s];
+      scr[((int64_t)p * 6 + 2 * s + 1) * nlt + gl] = cur5[s];
+      // shift the window: row p+1 becomes current, row p+2 next
+      cur3[s] = nx3[s]; cur4[s] = nx4[s]; cur5[s] = nx5[s];
+      nx2[s] = n2; nx3[s] = n3; nx4[s] = L2[s][3]; nx5[s] = L2[s][4];
+    }
+    const int64_t pt = base + (int64_t)p * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (p > 0) out[m * NP + pt] = (double)rr[0][m];
+      rr[0][m] = rr[1][m];
+      rr[1][m] = rr[2][m];
+    }
+  }
+  // last two rows: p = n-2 (current), n-1 (next)
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const T fac1 = (T)1.0 / cur3[s];
+    cur4[s] *= fac1;
+    cur5[s] *= fac1;
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
+    nx3[s] -= nx2[s] * cur4[s];
+    nx4[s] -= nx2[s] * cur5[s];
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
+    const T fac2 = (T)1.0 / nx3[s];
+    nx4[s] *= fac2;
+    nx5[s] *= fac2;
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] *= fac2;
+  }
+  // back substitution; rr[0] = row n-2, rr[1] = row n-1 (the boundary row,
+  // numerically unchanged).  b1 = r_{p+1}, b2 = r_{p+2} before transforms.
+  T b1[5], b2[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) b2[m] = rr[1][m];
+  {
+    const int p = n - 2;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int s = m < 3 ? 0 : m - 2;
+      b1[m] = rr[0][m] - cur4[s] * b2[m];
+    }
+    (void)p;
+  }
+  // Emit row n-2, then rows n-3 .. 1.
+  auto emit = [&](int p, const T v[5]) {
+    const int64_t pt = base + (int64_t)p * st;
+    double r1 = (double)v[0], r2 = (double)v[1], r3 = (double)v[2], r4 = (double)v[3], r5 = (double)v[4];
+    if (!transform) {
+      out[pt] = r1; out[NP + pt] = r2; out[2 * NP + pt] = r3; out[3 * NP + pt] = r4; out[4 * NP + pt] = r5;
+      return;
+    }
+    double o[5];
+    if (DIR == 0) {  // ninvr
+      const double t1 = K.bt * r3;
+      const double t2 = 0.5e0 * (r4 + r5);
+      o[0] = -r2; o[1] = r1; o[2] = K.bt * (r4 - r5); o[3] = -t1 + t2; o[4] = t1 + t2;
+    } else if (DIR == 1) {  // pinvr
+      const double t1 = K.bt * r1;
+      const double t2 = 0.5e0 * (r4 + r5);
+      o[0] = K.bt * (r4 - r5); o[1] = -r3; o[2] = r2; o[3] = -t1 + t2; o[4] = t1 + t2;
+    } else {  // tzetar
+      const double xvel = F.prim[PR_US * NP + pt], yvel = F.prim[PR_VS * NP + pt], zvel = F.prim[PR_WS * NP + pt];
+      const double ac = F.prim[PR_SPEED * NP + pt], acinv = F.prim[PR_AINV * NP + pt];
+      const double ac2u = ac * ac;
+      const double uzik1 = F.u[pt];
+      const double btuz = K.bt * uzik1;
+      const double t1 = btuz * acinv * (r4 + r5);
+      const double t2 = r3 + t1;
+      const double t3 = btuz * (r4 - r5);
+      o[0] = t2;
+      o[1] = -uzik1 * r2 + xvel * t2;
+      o[2] = uzik1 * r1 + yvel * t2;
+      o[3] = zvel * t2 + t3;
+      o[4] = uzik1 * (-xvel * r2 + yvel * r1) + F.prim[PR_QS * NP + pt] * t2 + K.c2iv * ac2u * t1 + zvel * t3;
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      rhs[m * NP + pt] = o[m];
+      if (add_u) F.u[m * NP + pt] += o[m];
+    }
+  };
+  // row n-2's transform must read u before row n-2 is updated; emit updates
+  // only its own point, so the order below is safe.
+  emit(n - 2, b1);
+  for (int p = n - 3; p >= 1; --p) {
+    const int64_t pt = base + (int64_t)p * st;
+    T r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int s = m < 3 ? 0 : m - 2;
+      const T l4 = scr[((int64_t)p * 6 + 2 * s) * nlt + gl];
+      const T l5 = scr[((int64_t)p * 6 + 2 * s + 1) * nlt + gl];
+      r[m] = (T)out[m * NP + pt];
+      r[m] -= l4 * b1[m] + l5 * b2[m];
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) { b2[m] = b1[m]; b1[m] = r[m]; }
+    emit(p, r);
+  }
+}
+
+// ============================================================================
+// Refinement pass of the mixed-precision SP sweep: residual r = b - L x0 of
+// each scalar pentadiagonal system in FP64 (bands of lhsx/lhsy/lhsz
+// assembled in FP64), FP32 Thomas solve of L d = r, x = x0 + d, then the
+// sweep's transform (ninvr / pinvr / tzetar) and, after the z sweep, add.
+// x0 comes from xw on interior points; boundary rows are identity rows, so
+// x0 there is b itself and the residual is zero.
+// ============================================================================
+template <int DIR>
+__device__ __forceinline__ void sp_transform(const Fields& F, const Consts& K, int64_t pt, const double v[5],
+                                             double o[5]) {
+  const int64_t NP = F.NP;
+  const double r1 = v[0], r2 = v[1], r3 = v[2], r4 = v[3], r5 = v[4];
+  if (DIR == 0) {
+    const double t1 = K.bt * r3;
+    const double t2 = 0.5e0 * (r4 + r5);
+    o[0] = -r2; o[1] = r1; o[2] = K.bt * (r4 - r5); o[3] = -t1 + t2; o[4] = t1 + t2;
+  } else if (DIR == 1) {
+    const double t1 = K.bt * r1;
+    const double t2 = 0.5e0 * (r4 + r5);
+    o[0] = K.bt * (r4 - r5); o[1] = -r3; o[2] = r2; o[3] = -t1 + t2; o[4] = t1 + t2;
+  } else {
+    const double xvel = F.prim[PR_US * NP + pt], yvel = F.prim[PR_VS * NP + pt], zvel = F.prim[PR_WS * NP + pt];
+    const double ac = F.prim[PR_SPEED * NP + pt], acinv = F.prim[PR_AINV * NP + pt];
+    const double ac2u = ac * ac;
+    const double uzik1 = F.u[pt];
+    const double btuz = K.bt * uzik1;
+    const double t1 = btuz * acinv * (r4 + r5);
+    const double t2 = r3 + t1;
+    const double t3 = btuz * (r4 - r5);
+    o[0] = t2;
+    o[1] = -uzik1 * r2 + xvel * t2;
+    o[2] = uzik1 * r1 + yvel * t2;
+    o[3] = zvel * t2 + t3;
+    o[4] = uzik1 * (-xvel * r2 + yvel * r1) + F.prim[PR_QS * NP + pt] * t2 + K.c2iv * ac2u * t1 + zvel * t3;
+  }
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) k_sp_refine(Fields F, Consts K, const Work* __restrict__ work,
+                                                   float* __restrict__ scr, int64_t nlt, int add_u,
+                                                   const double* __restrict__ xw) {
+  using T = float;
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  double* __restrict__ rhs = F.rhs;
+
+  auto xat = [&](int q, int m) -> double {
+    const int64_t pt = base + (int64_t)q * st;
+    return (q == 0 || q == n - 1) ? rhs[m * NP + pt] : xw[m * NP + pt];
+  };
+  // FP64 bands of row q and the residual r_q = b_q - L x0 (zero on boundary rows)
+  auto row = [&](int q, T L[3][5], T r[5]) {
+    double Ld[3][5];
+    double cv[3], rh[3], sp[3];
+    if (q > 0 && q < n - 1) {
+      for (int d = 0; d < 3; ++d) sp_geom<DIR>(F, K, base + (int64_t)(q - 1 + d) * st, cv[d], rh[d], sp[d]);
+    }
+    sp_assemble<DIR, double>(K, q, n, cv, rh, sp, Ld);
+#pragma unroll
+    for (int s = 0; s < 3; ++s)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) L[s][b] = (T)Ld[s][b];
+    if (q == 0 || q == n - 1) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) r[m] = (T)0.0;
+      return;
+    }
+    const int64_t pt = base + (int64_t)q * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int s = m < 3 ? 0 : m - 2;
+      double t = 0.0;
+#pragma unroll
+      for (int d = -2; d <= 2; ++d) {
+        const int qq = q + d;
+        if (qq < 0 || qq > n - 1) continue;
+        t += Ld[s][d + 2] * xat(qq, m);
+      }
+      r[m] = (T)(rhs[m * NP + pt] - t);
+    }
+  };
+
+  T cur3[3], cur4[3], cur5[3];
+  T nx2[3], nx3[3], nx4[3], nx5[3];
+  T rr[3][5];
+  {
+    T L0[3][5], L1[3][5];
+    row(0, L0, rr[0]);
+    row(1, L1, rr[1]);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      cur3[s] = L0[s][2]; cur4[s] = L0[s][3]; cur5[s] = L0[s][4];
+      nx2[s] = L1[s][1]; nx3[s] = L1[s][2]; nx4[s] = L1[s][3]; nx5[s] = L1[s][4];
+    }
+  }
+  for (int p = 0; p <= n - 3; ++p) {
+    T L2[3][5];
+    row(p + 2, L2, rr[2]);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const T fac1 = (T)1.0 / cur3[s];
+      cur4[s] *= fac1;
+      cur5[s] *= fac1;
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
+      nx3[s] -= nx2[s] * cur4[s];
+      nx4[s] -= nx2[s] * cur5[s];
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
+      T n2 = L2[s][1], n3 = L2[s][2];
+      n2 -= L2[s][0] * cur4[s];
+      n3 -= L2[s][0] * cur5[s];
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[2][m] -= L2[s][0] * rr[0][m];
+      scr[((int64_t)p * 6 + 2 * s) * nlt + gl] = cur4[s];
+      scr[((int64_t)p * 6 + 2 * s + 1) * nlt + gl] = cur5[s];
+      cur3[s] = nx3[s]; cur4[s] = nx4[s]; cur5[s] = nx5[s];
+      nx2[s] = n2; nx3[s] = n3; nx4[s] = L2[s][3]; nx5[s] = L2[s][4];
+    }
+    const int64_t pt = base + (int64_t)p * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (p > 0) rhs[m * NP + pt] = (double)rr[0][m];   // b_p is no longer needed
+      rr[0][m] = rr[1][m];
+      rr[1][m] = rr[2][m];
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const T fac1 = (T)1.0 / cur3[s];
+    cur4[s] *= fac1;
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
+  }
+  T b1[5], b2[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    b2[m] = (T)0.0;  // correction on the boundary row
+    const int s = m < 3 ? 0 : m - 2;
+    b1[m] = rr[0][m] - cur4[s] * b2[m];
+  }
+  auto emit = [&](int p, const T d[5]) {
+    const int64_t pt = base + (int64_t)p * st;
+    double v[5], o[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) v[m] = xw[m * NP + pt] + (double)d[m];
+    sp_transform<DIR>(F, K, pt, v, o);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      rhs[m * NP + pt] = o[m];
+      if (add_u) F.u[m * NP + pt] += o[m];
+    }
+  };
+  emit(n - 2, b1);
+  for (int p = n - 3; p >= 1; --p) {
+    const int64_t pt = base + (int64_t)p * st;
+    T r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int s = m < 3 ? 0 : m - 2;
+      const T l4 = scr[((int64_t)p * 6 + 2 * s) * nlt + gl];
+      const T l5 = scr[((int64_t)p * 6 + 2 * s + 1) * nlt + gl];
+      r[m] = (T)rhs[m * NP + pt];
+      r[m] -= l4 * b1[m] + l5 * b2[m];
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) { b2[m] = b1[m]; b1[m] = r[m]; }
+    emit(p, r);
+  }
+}
+
+// ============================================================================
+// add (src/BT/add.jl:5-24, src/SP/add.jl:6-26) as a separate phase.
+// ============================================================================
+__global__ void __launch_bounds__(128) k_add(Fields F, const Work* __restrict__ work) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int q = w.first + threadIdx.x;
+  if (q >= Z.nx * Z.ny * Z.nz) return;
+  const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
+  if (i == 0 || i == Z.nx - 1 || j == 0 || j == Z.ny - 1 || k == 0 || k == Z.nz - 1) return;
+  const int64_t p = Z.off + q;
+  for (int m = 0; m < 5; ++m) F.u[m * F.NP + p] += F.rhs[m * F.NP + p];
+}
+
+// ============================================================================
+// host-side launchers (declared in step_launch.h)
+// ============================================================================
+void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s) {
+  if (hi <= lo) return;
+  int64_t g = (hi - lo + 255) / 256;
+  const int grid = (int)(g > 8192 ? 8192 : g);
+  if (sp) k_prim<true><<<grid, 256, 0, s>>>(F, K, lo, hi);
+  else k_prim<false><<<grid, 256, 0, s>>>(F, K, lo, hi);
+}
+
+void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork, double* partials,
+                cudaStream_t s) {
+  if (nwork <= 0) return;
+  if (tx) {
+    if (norm) k_rhs<true, true><<<nwork, 128, 0, s>>>(F, K, work, partials);
+    else k_rhs<true, false><<<nwork, 128, 0, s>>>(F, K, work, partials);
+  } else {
+    if (norm) k_rhs<false, true><<<nwork, 128, 0, s>>>(F, K, work, partials);
+    else k_rhs<false, false><<<nwork, 128, 0, s>>>(F, K, work, partials);
+  }
+}
+
+template <typename T>
+static void launch_solve_t(bool sp, int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb,
+                           void* scratch, int64_t nlt, int add_u, double* out, int transform, cudaStream_t s) {
+  T* scr = reinterpret_cast<T*>(scratch);
+  if (sp) {
+    if (dir == 0) k_sp_solve<0, T><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, out, transform);
+    else if (dir == 1) k_sp_solve<1, T><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, out, transform);
+    else k_sp_solve<2, T><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, out, transform);
+  } else {
+    if (dir == 0) k_bt_solve<0, T><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, out);
+    else if (dir == 1) k_bt_solve<1, T><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, out);
+    else k_bt_solve<2, T><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, out);
+  }
+}
+
+// mode 0: FP64 in place; 1: FP32 in place; 2: FP32 + FP64-residual
+// refinement (xw: a [5][NP] buffer for the first solution).
+void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb,
+                  void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s) {
+  if (nwork <= 0) return;
+#if NPBMZ_HAS_FP32
+  if (mode == 1) { launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s); return; }
+  if (mode == 2) {
+    launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, 0, xw, 0, s);
+    float* scr = reinterpret_cast<float*>(scratch);
+    if (sp) {
+      if (dir == 0) k_sp_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+      else if (dir == 1) k_sp_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+      else k_sp_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+    } else {
+      if (dir == 0) k_bt_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+      else if (dir == 1) k_bt_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+      else k_bt_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+    }
+    return;
+  }
+#else
+  (void)xw;
+#endif
+  (void)mode;
+  launch_solve_t<double>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s);
+}
+
+void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s) {
+  if (nwork > 0) k_add<<<nwork, 128, 0, s>>>(F, work);
+}
+
+}  // namespace NPBMZ_NS
+}  // namespace npbmz

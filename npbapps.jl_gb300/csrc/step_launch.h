@@ -1,0 +1,22 @@
+// step_launch.h -- host launchers of the time-step kernels, one set per build
+// variant (exact: -fmad=false, fast: -fmad=true).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "npbmz_internal.cuh"
+
+namespace npbmz {
+#define NPBMZ_DECLARE_LAUNCHERS(NS)                                                                                  \
+  namespace NS {                                                                                                     \
+  void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s);                                   \
+  void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork,                 \
+                  double* partials, cudaStream_t s);                                                                 \
+  void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork,       \
+                    int tpb, void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s);                     \
+  void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s);                                     \
+  }
+NPBMZ_DECLARE_LAUNCHERS(exact)
+NPBMZ_DECLARE_LAUNCHERS(fast)
+#undef NPBMZ_DECLARE_LAUNCHERS
+}  // namespace npbmz

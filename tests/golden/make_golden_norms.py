@@ -29,7 +29,7 @@ def parse(path):
         if cls is None:
             continue
         m = re.search(r"dtref\s*=\s*([0-9.eE+-]+)", code)
-        if m:
+        if m and "dt" not in out[cls]:
             out[cls]["dt"] = float(m.group(1))
         m = re.search(r"niterref\s*=\s*(\d+)", code)
         if m and "niter" not in out[cls]:

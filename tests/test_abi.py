@@ -1,0 +1,82 @@
+"""The C ABI library builds for sm_103a, loads, and exports every entry point
+include/npbmz.h declares; host-side helpers that need no GPU."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import npbmz
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "npbmz.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(npbmz_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_the_exported_list():
+    assert sorted(npbmz.EXPORTS) == declared_functions()
+
+
+def test_library_exports_every_declared_symbol(npbmz_mod):
+    L = npbmz_mod.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+
+
+def test_library_is_built_for_sm_103a():
+    from npbmz import build
+
+    assert "arch=compute_103a,code=sm_103a" in build.ARCH
+
+
+@pytest.mark.parametrize("kind,cls", [("BT", c) for c in "SWABC"] + [("SP", c) for c in "SWABC"])
+def test_zone_setup_matches_oracle(npbmz_mod, oracle_mod, kind, cls):
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
+    k = npbmz.KINDS[kind]
+    a = npbmz.zone_setup(k, gx, gy, gz, xz, yz, ratio)
+    b = oracle_mod.zone_setup(k, gx, gy, gz, xz, yz, ratio)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    nx, ny, nz, nbr = a
+    assert int(np.sum(nx[:xz])) == gx and int(np.sum(ny[::xz])) == gy
+
+
+def test_bt_class_b_zone_widths():
+    """The geometric widths of BT class B (= BASELINE config 2's grid)."""
+    nx, ny, nz, nbr = npbmz.zone_setup(npbmz.BT, 304, 208, 17, 8, 8, 4.5)
+    assert nx[:8].tolist() == [16, 20, 24, 30, 38, 47, 57, 72]
+    assert ny[::8].tolist() == [11, 13, 17, 21, 26, 31, 40, 49]
+    area = nx * ny
+    assert 20.0 < area.max() / area.min() < 20.1
+
+
+def test_periodic_neighbours():
+    nx, ny, nz, nbr = npbmz.zone_setup(npbmz.BT, 24, 24, 6, 2, 2, 3.0)
+    # zone 0 = (i=1,j=1): west/east are zone 1, south/north are zone 2
+    assert nbr[:4].tolist() == [1, 1, 2, 2]
+    nx2, ny2, nz2, nbr2 = npbmz.zones_from_widths([8, 16], [10, 14], 6)
+    assert nbr2.tolist() == nbr.tolist()
+    assert nx2.tolist() == [8, 16, 8, 16] and ny2.tolist() == [10, 10, 14, 14]
+
+
+@pytest.mark.parametrize("seed", [0, 1, 7, 12345])
+def test_seeded_coefficients_positivity_rule(npbmz_mod, seed):
+    nx, ny, nz, nbr = npbmz.zone_setup(npbmz.BT, 304, 208, 17, 8, 8, 4.5)
+    ce, e = npbmz.seeded_coefficients(seed, nx, ny, nz, 304, 208, 17, 8, 8)
+    assert e >= 0
+    assert np.all(ce[:4] >= 0.5) and np.all(ce[:4] < 2.0)
+    assert np.all(ce[4] >= 0.5 * 2 ** e) and np.all(ce[4] < 2.0 * 2 ** e)
+    ce2, e2 = npbmz.seeded_coefficients(seed, nx, ny, nz, 304, 208, 17, 8, 8)
+    np.testing.assert_array_equal(ce, ce2)
+
+
+def test_ref_layout_sizes():
+    # BT u carries the 2-deep halo on i, j, k; SP pads i, j to odd extents
+    assert npbmz.ref_elems(npbmz.BT, npbmz.U, 8, 10, 6) == 5 * 13 * 15 * 11
+    assert npbmz.ref_elems(npbmz.BT, npbmz.RHS, 8, 10, 6) == 5 * 10 * 12 * 8
+    assert npbmz.ref_elems(npbmz.BT, npbmz.FORCING, 8, 10, 6) == 5 * 9 * 11 * 7
+    assert npbmz.ref_elems(npbmz.SP, npbmz.U, 12, 12, 6) == 5 * 17 * 17 * 11
+    assert npbmz.ref_elems(npbmz.SP, npbmz.RHS, 12, 12, 6) == 5 * 13 * 13 * 7
