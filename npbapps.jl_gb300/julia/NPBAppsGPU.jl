@@ -1,0 +1,113 @@
+# NPBAppsGPU.jl -- Julia binding of libnpbmz_gpu.so (include/npbmz.h) for the
+# NPBApps.jl BT-MZ / SP-MZ node time loop.
+#
+# The reference's loop (src/BT/bt-node.jl:280-395, src/SP/sp-node.jl:252-397)
+# calls exch_qbc(Val(ncells), ...) over all zones and then adi(iz, ...) per zone
+# under Threads.@threads.  With this module the loop keeps its shape:
+#
+#     gpu = NPBAppsGPU.Problem(NPBAppsGPU.BT, nx, ny, nz, nbr, dt, gx, gy, gz, x_zones, y_zones)
+#     NPBAppsGPU.setup!(gpu, ce)            # initialize + exact_rhs on the GPU
+#     for STEP = 1:niter
+#         NPBAppsGPU.exch_qbc!(gpu)          # replaces exch_qbc(...)
+#         NPBAppsGPU.adi!(gpu)               # replaces the @threads adi(iz, ...) loop
+#     end
+#     xcr, xce = NPBAppsGPU.verify(gpu)      # replaces verify's node part
+#
+# or, where the Julia arrays must stay the source of truth each step,
+# upload!/download! move one zone's OffsetArray (reference memory layout, halo
+# untouched) in and out around the calls.  Every call checks the returned
+# status and throws with npbmz_last_error's text; there is no CPU fallback.
+module NPBAppsGPU
+
+const libnpbmz = get(ENV, "NPBMZ_LIB", joinpath(@__DIR__, "..", "npbmz", "_build", "libnpbmz_gpu.so"))
+
+const BT = Cint(0)
+const SP = Cint(1)
+const EXACT = Cint(0x1)
+const MIXED = Cint(0x2)
+const PERZONE = Cint(0x4)
+const GRAPH = Cint(0x8)
+const U = Cint(0)
+const RHS = Cint(1)
+const FORCING = Cint(2)
+const LAYOUT_DENSE = Cint(0)
+const LAYOUT_REF = Cint(1)
+
+mutable struct Problem
+    handle::Ptr{Cvoid}
+    kind::Cint
+    nzones::Int
+    function Problem(kind, nx::Vector{<:Integer}, ny, nz, nbr, dt, gx, gy, gz, x_zones, y_zones; flags = Cint(0))
+        n = length(nx)
+        # nbr: 4 per zone (west, east, south, north), 0-based zone numbers
+        params = Cdouble[dt, gx, gy, gz, x_zones, y_zones]
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:npbmz_create, libnpbmz), Cint,
+                   (Cint, Cint, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cdouble}, Cint, Ptr{Ptr{Cvoid}}),
+                   kind, n, Cint.(nx), Cint.(ny), Cint.(nz), Cint.(nbr), params, flags, out)
+        rc == 0 || error("npbmz_create: " * unsafe_string(ccall((:npbmz_last_error, libnpbmz), Cstring, (Ptr{Cvoid},), C_NULL)))
+        p = new(out[], Cint(kind), n)
+        finalizer(p) do q
+            q.handle != C_NULL && ccall((:npbmz_destroy, libnpbmz), Cint, (Ptr{Cvoid},), q.handle)
+            q.handle = C_NULL
+        end
+        return p
+    end
+end
+
+check(p::Problem, rc, what) =
+    rc == 0 || error(what * ": " * unsafe_string(ccall((:npbmz_last_error, libnpbmz), Cstring, (Ptr{Cvoid},), p.handle)))
+
+"""Zone geometry of zone_setup (src/BT/zone_setup.jl); 0-based neighbours."""
+function zone_setup(kind, gx, gy, gz, x_zones, y_zones, ratio)
+    n = x_zones * y_zones
+    nx = zeros(Cint, n); ny = zeros(Cint, n); nz = zeros(Cint, n); nbr = zeros(Cint, 4n)
+    rc = ccall((:npbmz_zone_setup, libnpbmz), Cint,
+               (Cint, Cint, Cint, Cint, Cint, Cint, Cdouble, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}),
+               kind, gx, gy, gz, x_zones, y_zones, ratio, nx, ny, nz, nbr)
+    rc == 0 || error("npbmz_zone_setup failed")
+    return nx, ny, nz, nbr
+end
+
+"""initialize + exact_rhs on the GPU; ce is the reference's 5x13 table (set_constants.jl:47-51)."""
+function setup!(p::Problem, ce::AbstractMatrix{Float64})
+    c = Matrix{Float64}(permutedims(ce))      # the C side reads row-major [5][13]
+    check(p, ccall((:npbmz_setup, libnpbmz), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.handle, c), "npbmz_setup")
+end
+
+"""Replaces exch_qbc(Val(ncells), ...) (src/BT/exchange_qbc.jl:1-122)."""
+exch_qbc!(p::Problem) = check(p, ccall((:npbmz_exch_qbc, libnpbmz), Cint, (Ptr{Cvoid},), p.handle), "npbmz_exch_qbc")
+
+"""Replaces adi(iz, ...) (src/BT/adi.jl:5-251): zone iz (1-based), or all zones batched."""
+adi!(p::Problem, iz::Integer = 0) =
+    check(p, ccall((:npbmz_adi, libnpbmz), Cint, (Ptr{Cvoid}, Cint), p.handle, iz - 1), "npbmz_adi")
+
+"""niter steps of exch_qbc + adi; returns the per-step (xcr, xce) norms when norms = true."""
+function step!(p::Problem, niter::Integer; norms = false)
+    if norms
+        out = zeros(Cdouble, 10, niter)
+        check(p, ccall((:npbmz_step, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}), p.handle, niter, out), "npbmz_step")
+        return out
+    end
+    check(p, ccall((:npbmz_step, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}), p.handle, niter, C_NULL), "npbmz_step")
+    return nothing
+end
+
+"""verify's node part (src/BT/verify.jl:411-505): (xcr, xce) summed over zones."""
+function verify(p::Problem)
+    xcr = zeros(Cdouble, 5); xce = zeros(Cdouble, 5)
+    check(p, ccall((:npbmz_verify, libnpbmz), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}), p.handle, xcr, xce), "npbmz_verify")
+    return xcr, xce
+end
+
+"""Upload one zone's array in the reference's own OffsetArray memory
+(u[z], rhs[z] or forcing[z] of bt_data.jl / sp_data.jl): pass the OffsetArray."""
+upload!(p::Problem, zone::Integer, field, a) =
+    check(p, ccall((:npbmz_upload, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
+                   p.handle, zone - 1, field, LAYOUT_REF, parent(a)), "npbmz_upload")
+
+download!(p::Problem, zone::Integer, field, a) =
+    check(p, ccall((:npbmz_download, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
+                   p.handle, zone - 1, field, LAYOUT_REF, parent(a)), "npbmz_download")
+
+end # module
