@@ -167,7 +167,26 @@ int npbmz_launches_per_step(npbmz_t* h);
 int64_t npbmz_device_bytes(npbmz_t* h);
 int npbmz_describe(npbmz_t* h, char* buf, size_t n);
 
-/* Error text of the last failing call on h (h may be NULL for create). */
+/* The FP64 BT x sweep of one zone (compute the primitive variables from u,
+ * then x_solve, as NPBMZ_PHASE_XSOLVE of a handle created without NPBMZ_EXACT
+ * does) for callers that cannot allocate device memory when they need it --
+ * a host runtime whose own pool or garbage collector owns all device memory,
+ * or a loop that cannot afford the device-wide synchronisation of cudaFree.
+ * No counterpart in the reference.  u and rhs are device pointers in the dense
+ * per-zone layout [m][k][j][i] of an nx*ny*nz zone; rhs is solved in place.
+ * params = {dt, gx, gy, gz, x_zones, y_zones} as for npbmz_create.  All
+ * working memory comes from one 16 MiB device array built into the library
+ * (held by every GPU that loads it until the process exits); a zone needing
+ * more (8*nx*ny*nz + 25*nx*(ny-2)*(nz-2) doubles) is rejected with -2.  The
+ * call allocates nothing.  Its first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  Calls
+ * share the array: calls whose kernels may overlap on the GPU race and must
+ * be serialised by the caller.  Errors: npbmz_last_error(NULL). */
+int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* params, const double* u, double* rhs,
+                            void* stream);
+
+/* Error text of the last failing call on h (h may be NULL for create and for
+ * npbmz_bt_xsolve_noalloc). */
 const char* npbmz_last_error(npbmz_t* h);
 
 /* Free every device buffer and the handle. */

@@ -515,6 +515,11 @@ bool state_ok(const double u[5], double margin) {
 
 }  // namespace
 
+namespace npbmz {
+// Error text for calls without a handle, reported by npbmz_last_error(NULL).
+void set_global_error(const char* msg) { g_create_error = msg; }
+}  // namespace npbmz
+
 // =============================== C ABI ======================================
 extern "C" {
 

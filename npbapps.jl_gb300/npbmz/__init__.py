@@ -43,6 +43,7 @@ EXPORTS = [
     "npbmz_download", "npbmz_upload_async", "npbmz_download_async", "npbmz_exch_qbc", "npbmz_adi", "npbmz_step",
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
+    "npbmz_bt_xsolve_noalloc",
 ]
 
 # Problem classes (src/BT/classes.jl:15-24, src/SP/classes.jl:16-25):
@@ -127,6 +128,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_last_error.argtypes = [vp]
     L.npbmz_last_error.restype = ctypes.c_char_p
     L.npbmz_destroy.argtypes = [vp]
+    L.npbmz_bt_xsolve_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, vp, vp, vp]
     _lib = L
     return L
 

@@ -1,10 +1,11 @@
 """Build libnpbmz_gpu.so (sm_103a) in-tree with nvcc.
 
-The four translation units compile in parallel:
+The translation units compile in parallel:
   common_kernels.cu  -fmad=false  set-up, exch_qbc, norms, layout conversion
   step_exact.cu      -fmad=false  FP64 step kernels in the reference's order
   step_fast.cu       -fmad=true   FP64 (FMA) and FP32 line-solve kernels
   npbmz_api.cu                    the C ABI (include/npbmz.h)
+  noalloc.cu         -fmad=true   the x sweep over a file-scope device array
 and are linked into npbapps.jl_gb300/npbmz/_build/libnpbmz_gpu.so.
 """
 import os
@@ -27,6 +28,7 @@ UNITS = {
     "step_exact.cu": ["-fmad=false"],
     "step_fast.cu": ["-fmad=true"],
     "npbmz_api.cu": [],
+    "noalloc.cu": ["-fmad=true"],
 }
 
 
