@@ -48,15 +48,18 @@ typedef struct npbmz_handle npbmz_t;
                               reference's operation order: bit-for-bit the
                               reference's arithmetic */
 #define NPBMZ_MIXED   0x2  /* line solves in FP32 on the FP64 rhs, refined once
-                              against an FP64 residual of the line operator
-                              (compute_rhs, add, exch_qbc and the norms stay
-                              FP64) */
+                              against a residual of the line operator formed in
+                              double-float (BT) or FP64 (SP); compute_rhs, add,
+                              exch_qbc and the norms stay FP64 */
 #define NPBMZ_PERZONE 0x4  /* one launch per zone per phase, the reference's
                               per-zone adi order; default is all zones batched
                               in one launch per phase */
 #define NPBMZ_GRAPH   0x8  /* npbmz_step replays one captured CUDA graph per step */
 #define NPBMZ_PERSIST 0x10 /* line solves run as persistent kernels (one CTA set
                               per SM pulling zone x line work items) */
+#define NPBMZ_REFINE_FP64 0x40 /* with NPBMZ_MIXED on BT: the refinement residual
+                              in FP64 instead of double-float (FP32 pairs,
+                              about 48 bits) */
 #define NPBMZ_FP32_NOREFINE 0x20 /* FP32 line solves without the refinement
                               pass (the error of plain FP32 solves, for
                               comparison); implies NPBMZ_MIXED */

@@ -158,6 +158,7 @@ extern "C" int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* par
   F.uex = nullptr;
   F.zones = sym->zone;
   F.NP = np;
+  F.primf = nullptr;
   const npbmz::Consts K = noalloc_consts(params);
   npbmz::noalloc::launch_prim(false, F, K, 0, np, s);
   npbmz::noalloc::launch_solve(false, 0, 0, F, K, sym->work, nwork, NOALLOC_TPB, sym->scratch + prim_doubles, lines, 0,

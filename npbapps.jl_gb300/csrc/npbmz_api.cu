@@ -87,6 +87,7 @@ struct npbmz_handle {
   double* prim = nullptr;
   double* uex = nullptr;
   double* xw = nullptr;      // first-pass line solution of the refined mixed solve
+  float* primf = nullptr;    // FP32 state copies for the mixed line solves
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
   double* part_rhs = nullptr;
@@ -102,6 +103,11 @@ struct npbmz_handle {
   int nwpts = 0;
   std::vector<Range> pts_range;   // per zone
   int* zblk_pts_d = nullptr;      // [2*nzones] CTA ranges of each zone (point list)
+  Work* wint_d = nullptr;         // interior-point list (compute_rhs)
+  int nwint = 0;
+  std::vector<Range> int_range;
+  int* zblk_int_d = nullptr;
+  bool bnd_dirty = true;          // boundary rhs must be reset to the forcing
   Work* wline_d[3] = {nullptr, nullptr, nullptr};
   int nwline[3] = {0, 0, 0};
   std::vector<Range> line_range[3];
@@ -162,6 +168,7 @@ Fields fields(const npbmz_t* h) {
   F.uex = h->uex;
   F.zones = h->zones_d;
   F.NP = h->NP;
+  F.primf = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE) ? h->primf : nullptr;
   return F;
 }
 
@@ -205,8 +212,35 @@ int build_work_lists(npbmz_t* h) {
   for (int z = 0; z < nz; ++z) { zb[2 * z] = h->pts_range[z].lo; zb[2 * z + 1] = h->pts_range[z].hi; }
   if (dalloc(h, &h->zblk_pts_d, zb.size())) return -1;
   CK(h, cudaMemcpy(h->zblk_pts_d, zb.data(), zb.size() * sizeof(int), cudaMemcpyHostToDevice));
-  if (dalloc(h, &h->part_rhs, (size_t)h->nwpts * 5)) return -1;
+  // interior points (compute_rhs and the residual norm)
+  std::vector<Work> wi;
+  h->int_range.assign(nz, Range());
+  for (int z : order) {
+    const ZoneDev& d = h->zh[z];
+    const int ni = (d.nx - 2) * (d.ny - 2) * (d.nz - 2);
+    h->int_range[z].lo = (int)wi.size();
+    for (int f = 0; f < ni; f += PTS_TPB) wi.push_back(Work{z, f});
+    h->int_range[z].hi = (int)wi.size();
+  }
+  h->nwint = (int)wi.size();
+  if (dalloc(h, &h->wint_d, wi.size())) return -1;
+  CK(h, cudaMemcpy(h->wint_d, wi.data(), wi.size() * sizeof(Work), cudaMemcpyHostToDevice));
+  std::vector<int> zi(2 * nz);
+  for (int z = 0; z < nz; ++z) { zi[2 * z] = h->int_range[z].lo; zi[2 * z + 1] = h->int_range[z].hi; }
+  if (dalloc(h, &h->zblk_int_d, zi.size())) return -1;
+  CK(h, cudaMemcpy(h->zblk_int_d, zi.data(), zi.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (dalloc(h, &h->part_rhs, (size_t)h->nwint * 5)) return -1;
   if (dalloc(h, &h->part_err, (size_t)h->nwpts * 5)) return -1;
+  return 0;
+}
+
+// The boundary points of rhs hold the forcing (compute_rhs sets rhs = forcing
+// on the whole cell, src/BT/rhs.jl:85-93, and no solve rewrites them); the
+// rhs kernel only visits interior points, so reset them after an upload.
+int flush_boundary(npbmz_t* h) {
+  if (!h->bnd_dirty) return 0;
+  CK(h, cudaMemcpyAsync(h->rhs, h->forcing, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  h->bnd_dirty = false;
   return 0;
 }
 
@@ -251,11 +285,12 @@ int phase_prim(npbmz_t* h, int zone) {
 }
 
 int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
+  if (flush_boundary(h)) return -1;
   const Fields F = fields(h);
-  int lo = 0, hi = h->nwpts;
-  if (zone >= 0) { lo = h->pts_range[zone].lo; hi = h->pts_range[zone].hi; }
-  if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wpts_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
-  else fast::launch_rhs(tx, norm, F, h->K, h->wpts_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
+  int lo = 0, hi = h->nwint;
+  if (zone >= 0) { lo = h->int_range[zone].lo; hi = h->int_range[zone].hi; }
+  if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
+  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
   CKL(h);
   return 0;
 }
@@ -269,7 +304,7 @@ int phase_solve(npbmz_t* h, int dir, int zone, int add_u) {
     exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch,
                         h->nlines[dir], add_u, nullptr, h->stream);
   else
-    fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : 2), dir, F, h->K,
+    fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : ((h->flags & NPBMZ_REFINE_FP64) ? 3 : 2)), dir, F, h->K,
                        h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch, h->nlines[dir], add_u, h->xw,
                        h->stream);
   CKL(h);
@@ -310,7 +345,7 @@ int run_adi(npbmz_t* h, int zone, bool norm) {
 }
 
 int finish_norms(npbmz_t* h, double* out_rhs, double* out_err) {
-  if (out_rhs) launch_norm_finish(h->zones_d, h->part_rhs, h->zblk_pts_d, h->nzones, 1.0 / h->K.dt, out_rhs, h->stream);
+  if (out_rhs) launch_norm_finish(h->zones_d, h->part_rhs, h->zblk_int_d, h->nzones, 1.0 / h->K.dt, out_rhs, h->stream);
   if (out_err) launch_norm_finish(h->zones_d, h->part_err, h->zblk_pts_d, h->nzones, 1.0, out_err, h->stream);
   CKL(h);
   return 0;
@@ -339,6 +374,7 @@ void drop_graph(npbmz_t* h) {
 
 int capture_step_graph(npbmz_t* h) {
   drop_graph(h);
+  if (flush_boundary(h)) return -1;  // keep the one-off reset out of the graph
   // Capture is not allowed on the legacy default stream: capture and replay
   // on an owned stream, fenced against the caller's stream by events.
   cudaStream_t cs = h->stream;
@@ -450,6 +486,7 @@ int transfer(npbmz_t* h, int zone, int field, int layout, void* host, int dir, b
   if (layout != NPBMZ_LAYOUT_DENSE && layout != NPBMZ_LAYOUT_REF) return fail(h, "bad layout %d", layout);
   if (zone < -1 || zone >= h->nzones) return fail(h, "bad zone %d", zone);
   if (!host) return fail(h, "null host buffer");
+  if (dir == 0 && field != NPBMZ_U) h->bnd_dirty = true;
   const std::vector<int64_t>& so = h->soff_h[layout][field];
   const int zlo = zone < 0 ? 0 : zone, zn = zone < 0 ? h->nzones : 1;
   const int64_t first = so[zlo], count = so[zlo + zn] - first;
@@ -656,8 +693,10 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
     for (int z = 0; z < nzones; ++z) maxlen = std::max(maxlen, zone_line_len(h->zh[z], dir));
     scratch_elems = std::max<int64_t>(scratch_elems, (int64_t)maxlen * lines[dir]);
   }
-  // line scratch: BT keeps 25 values per point (C'), SP 6 (l4, l5 of 3 systems)
-  const int per = kind == NPBMZ_BT ? 25 : 6;
+  // line scratch: BT keeps 25 values per point (C'; 30 with the FP32
+  // forward rhs of the refined mixed solve), SP 6 (l4, l5 of 3 systems)
+  const bool refined = (variant_flags & NPBMZ_MIXED) && !(variant_flags & NPBMZ_FP32_NOREFINE);
+  const int per = kind == NPBMZ_BT ? (refined ? 30 : 25) : (refined ? 11 : 6);
   if (variant_flags & NPBMZ_FP32_NOREFINE) variant_flags |= NPBMZ_MIXED;
   h->flags = variant_flags;
   const size_t esz = (variant_flags & NPBMZ_MIXED) ? sizeof(float) : sizeof(double);
@@ -672,6 +711,7 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   rc |= dalloc(h, &h->prim, (size_t)PR_COUNT * h->NP);
   rc |= dalloc(h, &h->uex, 5 * (size_t)h->NP);
   if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
+  if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? PF_COUNT : PS_COUNT) * h->NP);
   if (!rc) {
     if (cudaMalloc(&h->scratch, std::max<size_t>(h->scratch_bytes, 16)) != cudaSuccess) rc = fail(h, "scratch alloc failed");
     else h->device_bytes += (int64_t)h->scratch_bytes;
@@ -730,6 +770,7 @@ int npbmz_setup(npbmz_t* h, const double* ce) {
   CKL(h);
   // rhs starts as the forcing (its boundary values are never rewritten)
   CK(h, cudaMemcpyAsync(h->rhs, h->forcing, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  h->bnd_dirty = false;
   CK(h, cudaStreamSynchronize(h->stream));
   return 0;
 }
@@ -778,6 +819,7 @@ int npbmz_step(npbmz_t* h, int nsteps, double* norms) {
   if (h->flags & NPBMZ_GRAPH) {
     if (!h->graph_exec || h->graph_stream != h->stream)
       if (capture_step_graph(h)) return -1;
+    if (flush_boundary(h)) return -1;
     return replay_graph(h, nsteps);
   }
   for (int s = 0; s < nsteps; ++s)
@@ -918,8 +960,9 @@ int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->scratch, h->part_rhs,
-                  h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wline_d[0], h->wline_d[1],
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->scratch, h->part_rhs,
+                  h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wint_d, h->zblk_int_d,
+                  h->wline_d[0], h->wline_d[1],
                   h->wline_d[2]};
   for (void* b : bufs)
     if (b) cudaFree(b);

@@ -46,6 +46,13 @@ struct Work {
 // Primitive-variable planes written by the primitive kernel.
 enum { PR_RHOI = 0, PR_US, PR_VS, PR_WS, PR_QS, PR_SQUARE, PR_SPEED, PR_AINV, PR_COUNT };
 
+// FP32 copies of the state read by the FP32 line-solve passes: planes
+// 0..5 hold the rounded values (hi), planes 6..11 the remainders (lo), so
+// that hi + lo carries the FP64 value to about 48 bits (double-float).
+enum { PF_RHOI = 0, PF_QS, PF_U2, PF_U3, PF_U4, PF_U5, PF_HI_COUNT, PF_COUNT = 2 * PF_HI_COUNT };
+// SP: FP32 copies of 1/rho, the three velocities and the speed of sound.
+enum { PS_RHOI = 0, PS_US, PS_VS, PS_WS, PS_SPEED, PS_COUNT };
+
 struct Fields {
   double* u;        // [5][NP]
   double* rhs;      // [5][NP]
@@ -54,6 +61,7 @@ struct Fields {
   const double* uex;      // [5][NP] exact solution (error norm)
   const ZoneDev* zones;
   int64_t NP;
+  float* primf;     // [PF_COUNT][NP] or null
 };
 
 // Lines per sweep direction of a zone (interior transverse indices only).

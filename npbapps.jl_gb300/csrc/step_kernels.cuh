@@ -45,6 +45,21 @@ __global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, in
       F.prim[PR_SPEED * NP + p] = aux;
       F.prim[PR_AINV * NP + p] = 1.0e0 / aux;
     }
+    if (SP && F.primf) {
+      F.primf[PS_RHOI * NP + p] = (float)rho_inv;
+      F.primf[PS_US * NP + p] = (float)(u2 * rho_inv);
+      F.primf[PS_VS * NP + p] = (float)(u3 * rho_inv);
+      F.primf[PS_WS * NP + p] = (float)(u4 * rho_inv);
+      F.primf[PS_SPEED * NP + p] = (float)F.prim[PR_SPEED * NP + p];
+    } else if (F.primf) {
+      const double v[PF_HI_COUNT] = {rho_inv, square * rho_inv, u2, u3, u4, F.u[4 * NP + p]};
+#pragma unroll
+      for (int e = 0; e < PF_HI_COUNT; ++e) {
+        const float hi = __double2float_rn(v[e]);
+        F.primf[e * NP + p] = hi;
+        F.primf[(PF_HI_COUNT + e) * NP + p] = __double2float_rn(v[e] - (double)hi);
+      }
+    }
   }
 }
 
@@ -78,6 +93,33 @@ __device__ __forceinline__ double ld_axis(const double* __restrict__ a, int64_t 
   return (qq >= 0 && qq < n) ? a[p + d * st] : a[p];
 }
 
+// Weighted form of the dissipation stencils at position q of an axis of n
+// points: the sum of the start / middle / end stencils that apply at q.  Used
+// by the FMA build (no lane divergence at zone edges); the exact build keeps
+// dissip() and the reference's operation order.
+__device__ __forceinline__ void dissip_weights(int q, int n, double w[5]) {
+  w[0] = w[1] = w[2] = w[3] = w[4] = 0.0;
+  if (q == 1) { w[2] += 5.0; w[3] -= 4.0; w[4] += 1.0; }
+  if (q == 2) { w[1] -= 4.0; w[2] += 6.0; w[3] -= 4.0; w[4] += 1.0; }
+  if (q >= 3 && q <= n - 4) { w[0] += 1.0; w[1] -= 4.0; w[2] += 6.0; w[3] -= 4.0; w[4] += 1.0; }
+  if (q == n - 3) { w[0] += 1.0; w[1] -= 4.0; w[2] += 6.0; w[3] -= 4.0; }
+  if (q == n - 2) { w[0] += 1.0; w[1] -= 4.0; w[2] += 5.0; }
+}
+
+#if NPBMZ_HAS_FP32
+#define NPBMZ_DISSIP(r, q, n, dssp, um2, um1, u0, up1, up2)                                        \
+  do {                                                                                              \
+    double w_[5];                                                                                   \
+    dissip_weights((q), (n), w_);                                                                   \
+    (r) -= (dssp) * (w_[0] * (um2) + w_[1] * (um1) + w_[2] * (u0) + w_[3] * (up1) + w_[4] * (up2)); \
+  } while (0)
+#else
+#define NPBMZ_DISSIP(r, q, n, dssp, um2, um1, u0, up1, up2) dissip((r), (q), (n), (dssp), (um2), (um1), (u0), (up1), (up2))
+#endif
+
+// One thread per INTERIOR point of a zone (the work list counts interior
+// points only): the boundary rhs equals the forcing and no solve rewrites
+// it, so it is set when the forcing or rhs is set, not every step.
 template <bool TX, bool NORM>
 __global__ void __launch_bounds__(128) k_rhs(Fields F, Consts K, const Work* __restrict__ work,
                                              double* __restrict__ partials) {
@@ -85,16 +127,14 @@ __global__ void __launch_bounds__(128) k_rhs(Fields F, Consts K, const Work* __r
   const Work w = work[blockIdx.x];
   const ZoneDev Z = F.zones[w.zone];
   const int64_t NP = F.NP;
-  const int np = Z.nx * Z.ny * Z.nz;
-  const int q = w.first + threadIdx.x;
+  const int ix = Z.nx - 2, iy = Z.ny - 2;
+  const int ni = ix * iy * (Z.nz - 2);
+  const int t = w.first + threadIdx.x;
   double sq[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  if (q < np) {
-    const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
-    const int64_t p = Z.off + q;
-    const bool interior = i > 0 && i < Z.nx - 1 && j > 0 && j < Z.ny - 1 && k > 0 && k < Z.nz - 1;
-    if (!interior) {
-      for (int m = 0; m < 5; ++m) F.rhs[m * NP + p] = F.forcing[m * NP + p];
-    } else {
+  if (t < ni) {
+    const int i = 1 + t % ix, j = 1 + (t / ix) % iy, k = 1 + t / (ix * iy);
+    const int64_t p = Z.off + ((int64_t)k * Z.ny + j) * Z.nx + i;
+    {
       const double* __restrict__ u = F.u;
       const double* __restrict__ pr = F.prim;
       const double* us = pr + PR_US * NP;
@@ -124,8 +164,8 @@ __global__ void __launch_bounds__(128) k_rhs(Fields F, Consts K, const Work* __r
                 K.tx2 * ((c1 * u[4 * NP + a] - c2 * sqr[a]) * up1 - (c1 * u[4 * NP + b] - c2 * sqr[b]) * um1);
         for (int m = 0; m < 5; ++m) {
           const double* um = u + m * NP;
-          dissip(r[m], i, Z.nx, dssp, ld_axis(um, p, sx, i, -2, Z.nx), um[p - sx], um[p], um[p + sx],
-                 ld_axis(um, p, sx, i, 2, Z.nx));
+          NPBMZ_DISSIP(r[m], i, Z.nx, dssp, ld_axis(um, p, sx, i, -2, Z.nx), um[p - sx], um[p], um[p + sx],
+                       ld_axis(um, p, sx, i, 2, Z.nx));
         }
       }
       // ---------------- eta direction ----------------
@@ -146,8 +186,8 @@ __global__ void __launch_bounds__(128) k_rhs(Fields F, Consts K, const Work* __r
                 K.ty2 * ((c1 * u[4 * NP + a] - c2 * sqr[a]) * vp1 - (c1 * u[4 * NP + b] - c2 * sqr[b]) * vm1);
         for (int m = 0; m < 5; ++m) {
           const double* um = u + m * NP;
-          dissip(r[m], j, Z.ny, dssp, ld_axis(um, p, sy, j, -2, Z.ny), um[p - sy], um[p], um[p + sy],
-                 ld_axis(um, p, sy, j, 2, Z.ny));
+          NPBMZ_DISSIP(r[m], j, Z.ny, dssp, ld_axis(um, p, sy, j, -2, Z.ny), um[p - sy], um[p], um[p + sy],
+                       ld_axis(um, p, sy, j, 2, Z.ny));
         }
       }
       // ---------------- zeta direction ----------------
@@ -168,8 +208,8 @@ __global__ void __launch_bounds__(128) k_rhs(Fields F, Consts K, const Work* __r
                 K.tz2 * ((c1 * u[4 * NP + a] - c2 * sqr[a]) * wp1 - (c1 * u[4 * NP + b] - c2 * sqr[b]) * wm1);
         for (int m = 0; m < 5; ++m) {
           const double* um = u + m * NP;
-          dissip(r[m], k, Z.nz, dssp, ld_axis(um, p, sz, k, -2, Z.nz), um[p - sz], um[p], um[p + sz],
-                 ld_axis(um, p, sz, k, 2, Z.nz));
+          NPBMZ_DISSIP(r[m], k, Z.nz, dssp, ld_axis(um, p, sz, k, -2, Z.nz), um[p - sz], um[p], um[p + sz],
+                       ld_axis(um, p, sz, k, 2, Z.nz));
         }
       }
       for (int m = 0; m < 5; ++m) r[m] *= K.dt;
@@ -556,38 +596,233 @@ __global__ void __launch_bounds__(128) k_bt_solve(Fields F, Consts K, const Work
 }
 
 // ============================================================================
-// Refinement pass of the mixed-precision BT sweep.  x0 (in xw) is the FP32
-// solution of T x = b (b = rhs).  This pass forms the residual
-// r = b - T x0 in FP64 and solves T d = r in FP32; the result x0 + d goes to
-// rhs (and, after the z sweep, into u).  With F_q = fjac_q x_q and
-// N_q = njac_q x_q, row p of T applied to x is
+// Mixed-precision BT sweep (NPBMZ_MIXED): two kernels per sweep direction.
+//
+// Pass 1 (k_bt_mixed_solve): T x0 = b in FP32 from the FP32 state copies,
+// C' and the forward-eliminated rhs kept as FP32 in the line scratch
+// (30 floats per point), x0 written as FP32.
+// Pass 2 (k_bt_refine): the residual r = b - T x0 in FP64, T d = r in FP32,
+// x = x0 + d into rhs (and, after the z sweep, into u).  Row p of T applied
+// to x is, with F_q = fjac_q x_q and N_q = njac_q x_q,
 //   x_p + tmp2 (F_{p+1} - F_{p-1}) - tmp1 (N_{p-1} - 2 N_p + N_{p+1})
 //       - tmp1 D (x_{p-1} - 2 x_p + x_{p+1})
-// (lhsa/lhsb/lhsc of src/BT/x_solve.jl:613-708 applied to x), so the FP64
-// work is one Jacobian evaluation and two sparse 5x5 products per point.
-// Boundary rows are identity rows whose residual is exactly zero.
+// (lhsa/lhsb/lhsc of src/BT/x_solve.jl:613-708 applied to x), and F, N are
+// formed from the velocities directly (bt_jx), so the FP64 work is about
+// 90 operations per point.  Boundary rows are identity rows whose residual
+// is exactly zero, so d = 0 there.
 // ============================================================================
 template <int DIR>
-__device__ __forceinline__ void bt_jx(const double f[5][5], const double n[5][5], const double x[5], double Fx[5],
-                                      double Nx[5]) {
+__device__ __forceinline__ void bt_jx(const Consts& K, double ri, double q, double u2, double u3, double u4, double u5,
+                                      const double x[5], double Fx[5], double Nx[5]) {
+  const double vel[3] = {u2 * ri, u3 * ri, u4 * ri};
+  const double E = u5 * ri;
+  constexpr int a = DIR + 1;  // the momentum component normal to the sweep
+  const double vn = vel[DIR];
+  const double c1 = K.c1, c2 = K.c2;
+  double d[3];
 #pragma unroll
-  for (int a = 0; a < 5; ++a) {
-    double sf = 0.0, sn = 0.0;
+  for (int m = 0; m < 3; ++m) d[m] = x[m + 1] - vel[m] * x[0];
+  double tang = 0.0;
+  Fx[0] = x[a];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    if (m == DIR) continue;
+    Fx[m + 1] = vn * d[m] + vel[m] * x[a];
+    tang += vel[m] * x[m + 1];
+  }
+  Fx[a] = (c2 * q - vn * vn) * x[0] - c2 * tang + (2.0 - c2) * vn * x[a] + c2 * x[4];
+  Fx[4] = (2.0 * c2 * q - c1 * E) * vn * x[0] - c2 * vn * tang + (c1 * E - c2 * (q + vn * vn)) * x[a] + c1 * vn * x[4];
+  const double k43 = K.con43 * K.c3c4, c3c4 = K.c3c4, c1345 = K.c1345;
+  double s4 = c1345 * (x[4] - E * x[0]);
+  Nx[0] = 0.0;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const double cm = (m == DIR) ? k43 : c3c4;
+    Nx[m + 1] = cm * ri * d[m];
+    s4 += (cm - c1345) * vel[m] * d[m];
+  }
+  Nx[4] = ri * s4;
+}
+
+// State of the FP32 block elimination carried from point p to p+1.
+template <int DIR>
+struct BtF32Carry {
+  float Cp[5][5];     // C' at p-1
+  float rp[5];        // forward-eliminated rhs at p-1
+  float Acur[5][5];   // lhsa at p   (structural nonzeros)
+  float Anext[5][5];  // lhsa at p+1
+  float Bcur[5][5];   // lhsb at p   (structural nonzeros)
+};
+
+template <int DIR>
+__device__ __forceinline__ void bt_f32_consts(const Consts& K, float& tmp1, float& tmp2, float dd[5]) {
+  tmp1 = (float)(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
+  tmp2 = (float)(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  if (DIR == 0) { dd[0] = (float)K.dx1; dd[1] = (float)K.dx2; dd[2] = (float)K.dx3; dd[3] = (float)K.dx4; dd[4] = (float)K.dx5; }
+  else if (DIR == 1) { dd[0] = (float)K.dy1; dd[1] = (float)K.dy2; dd[2] = (float)K.dy3; dd[3] = (float)K.dy4; dd[4] = (float)K.dy5; }
+  else { dd[0] = (float)K.dz1; dd[1] = (float)K.dz2; dd[2] = (float)K.dz3; dd[3] = (float)K.dz4; dd[4] = (float)K.dz5; }
+}
+
+// Start of the elimination: Jacobians at points 0 and 1 (FP32 state s0, s1 =
+// ri, u2, u3, u4, u5, q).
+template <int DIR>
+__device__ __forceinline__ void bt_f32_begin(const Consts& K, int n, const float s0[6], const float s1[6],
+                                             BtF32Carry<DIR>& c) {
+  float tmp1, tmp2, dd[5], f[5][5], nj[5][5];
+  bt_f32_consts<DIR>(K, tmp1, tmp2, dd);
+  bt_jac<DIR, float>(K, s0[0], s0[1], s0[2], s0[3], s0[4], s0[5], f, nj);
+  bt_asm_a<DIR, float>(f, nj, tmp1, tmp2, dd, c.Acur);
+  bt_jac<DIR, float>(K, s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], f, nj);
+  bt_asm_b<float>(nj, tmp1, dd, c.Bcur);
+  if (n - 2 >= 2) bt_asm_a<DIR, float>(f, nj, tmp1, tmp2, dd, c.Anext);
+}
+
+// One forward step at point p (1..n-2): r holds the rhs of row p on entry and
+// the eliminated rhs on exit; sn is the FP32 state at p+1.  C'_p and r'_p go
+// to scr[(p*30 + e) * nlt + gl].
+template <int DIR>
+__device__ __forceinline__ void bt_f32_step(const Consts& K, int p, int n, bool skip_first_matvec, float r[5],
+                                            const float sn[6], BtF32Carry<DIR>& c, float* __restrict__ scr,
+                                            int64_t nlt, int64_t gl) {
+  float tmp1, tmp2, dd[5];
+  bt_f32_consts<DIR>(K, tmp1, tmp2, dd);
+  if (p > 1 || !skip_first_matvec) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      float sacc = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc)
+        if (anz<DIR>(m, cc)) sacc += c.Acur[m][cc] * c.rp[cc];
+      r[m] -= sacc;
+    }
+  }
+  float B[5][5];
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
 #pragma unroll
     for (int b = 0; b < 5; ++b) {
-      if (fnz<DIR>(a, b)) sf += f[a][b] * x[b];
-      if (nnz(a, b)) sn += n[a][b] * x[b];
+      float t = bnz(a, b) ? c.Bcur[a][b] : 0.f;
+      if (p > 1) {
+#pragma unroll
+        for (int cc = 0; cc < 5; ++cc)
+          if (anz<DIR>(a, cc)) t -= c.Acur[a][cc] * c.Cp[cc][b];
+      }
+      B[a][b] = t;
     }
-    Fx[a] = sf;
-    Nx[a] = sn;
+  float f[5][5], nj[5][5], C[5][5];
+  bt_jac<DIR, float>(K, sn[0], sn[1], sn[2], sn[3], sn[4], sn[5], f, nj);
+  bt_asm_c<DIR, float>(f, nj, tmp1, tmp2, dd, C);
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
+#pragma unroll
+    for (int b = 0; b < 5; ++b)
+      if (anz<DIR>(a, b)) c.Acur[a][b] = c.Anext[a][b];
+  if (p + 1 <= n - 2) bt_asm_b<float>(nj, tmp1, dd, c.Bcur);
+  if (p + 2 <= n - 2) bt_asm_a<DIR, float>(f, nj, tmp1, tmp2, dd, c.Anext);
+  binvcrhs<float>(B, C, r);
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      c.Cp[a][b] = C[a][b];
+      scr[((int64_t)p * 30 + a * 5 + b) * nlt + gl] = C[a][b];
+    }
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    c.rp[m] = r[m];
+    scr[((int64_t)p * 30 + 25 + m) * nlt + gl] = r[m];
   }
 }
 
+__device__ __forceinline__ void load_state_f32(const Fields& F, int64_t pt, float s[6]) {
+  const int64_t NP = F.NP;
+  s[0] = F.primf[PF_RHOI * NP + pt];
+  s[1] = F.primf[PF_U2 * NP + pt];
+  s[2] = F.primf[PF_U3 * NP + pt];
+  s[3] = F.primf[PF_U4 * NP + pt];
+  s[4] = F.primf[PF_U5 * NP + pt];
+  s[5] = F.primf[PF_QS * NP + pt];
+}
+
+__device__ __forceinline__ void load_state_f64(const Fields& F, int64_t pt, double s[6]) {
+  const int64_t NP = F.NP;
+  s[0] = F.prim[PR_RHOI * NP + pt];
+  s[1] = F.u[NP + pt];
+  s[2] = F.u[2 * NP + pt];
+  s[3] = F.u[3 * NP + pt];
+  s[4] = F.u[4 * NP + pt];
+  s[5] = F.prim[PR_QS * NP + pt];
+}
+
+// Pass 1: T x0 = b in FP32.  Loads of point p+2 and of b_{p+1} are issued one
+// step ahead so that they overlap the elimination of point p.
+template <int DIR>
+__global__ void __launch_bounds__(128) k_bt_mixed_solve(Fields F, Consts K, const Work* __restrict__ work,
+                                                        float* __restrict__ scr, int64_t nlt,
+                                                        float* __restrict__ x0) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  const double* __restrict__ rhs = F.rhs;
+  BtF32Carry<DIR> c;
+  float s0[6], s1[6];
+  load_state_f32(F, base, s0);
+  load_state_f32(F, base + st, s1);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) c.rp[m] = (float)rhs[m * NP + base];
+  bt_f32_begin<DIR>(K, n, s0, s1, c);
+  float sn[6], bn[5];
+  load_state_f32(F, base + 2 * st, sn);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) bn[m] = (float)rhs[m * NP + base + st];
+  for (int p = 1; p <= n - 2; ++p) {
+    float r[5], s[6];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) r[m] = bn[m];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s[e] = sn[e];
+    if (p + 1 <= n - 2) {  // prefetch for the next step
+      load_state_f32(F, base + (int64_t)(p + 2) * st, sn);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) bn[m] = (float)rhs[m * NP + base + (int64_t)(p + 1) * st];
+    }
+    bt_f32_step<DIR>(K, p, n, false, r, s, c, scr, nlt, gl);
+  }
+  float rn[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) rn[m] = (float)rhs[m * NP + base + (n - 1) * st];
+  for (int p = n - 2; p >= 1; --p) {
+    float r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) r[m] = (p == n - 2) ? c.rp[m] : scr[((int64_t)p * 30 + 25 + m) * nlt + gl];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc) r[m] -= scr[((int64_t)p * 30 + m * 5 + cc) * nlt + gl] * rn[cc];
+    const int64_t pt = base + p * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      x0[m * NP + pt] = r[m];
+      rn[m] = r[m];
+    }
+  }
+}
+
+// Pass 2: r = b - T x0 in FP64, T d = r in FP32, x = x0 + d.  The residual
+// rows are accumulated point by point: point q adds
+//   -tmp2 F_q - tmp1 N_q - tmp1 D x_q          to row q+1,
+//   x_q + 2 tmp1 N_q + 2 tmp1 D x_q            to row q,
+//   tmp2 F_q - tmp1 N_q - tmp1 D x_q           to row q-1 (which is then complete).
 template <int DIR>
 __global__ void __launch_bounds__(128) k_bt_refine(Fields F, Consts K, const Work* __restrict__ work,
-                                                   float* __restrict__ lhsc, int64_t nlt, int add_u,
-                                                   const double* __restrict__ xw) {
-  using T = float;
+                                                   float* __restrict__ scr, int64_t nlt, int add_u,
+                                                   const float* __restrict__ x0f) {
   const Work w = work[blockIdx.x];
   const ZoneDev Z = F.zones[w.zone];
   const int line = w.first + threadIdx.x;
@@ -601,117 +836,319 @@ __global__ void __launch_bounds__(128) k_bt_refine(Fields F, Consts K, const Wor
 
   const double t1d = DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1;
   const double t2d = DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2;
-  const T tmp1 = (T)t1d, tmp2 = (T)t2d;
   double ddd[5];
   if (DIR == 0) { ddd[0] = K.dx1; ddd[1] = K.dx2; ddd[2] = K.dx3; ddd[3] = K.dx4; ddd[4] = K.dx5; }
   else if (DIR == 1) { ddd[0] = K.dy1; ddd[1] = K.dy2; ddd[2] = K.dy3; ddd[3] = K.dy4; ddd[4] = K.dy5; }
   else { ddd[0] = K.dz1; ddd[1] = K.dz2; ddd[2] = K.dz3; ddd[3] = K.dz4; ddd[4] = K.dz5; }
-  T dd[5];
-#pragma unroll
-  for (int m = 0; m < 5; ++m) dd[m] = (T)ddd[m];
 
-  double fd[5][5], nd[5][5];
-  T f[5][5], nj[5][5];
-  double xm[5], x0[5], xp[5];       // x0 at p-1, p, p+1
-  double Fm[5], F0[5], Fp[5], Nm[5], N0[5], Np[5];
-  T rp[5], Cp[5][5], Acur[5][5], Anext[5][5], Bcur[5][5];
-
-  auto jac_at = [&](int64_t pt, double x[5], double Fx[5], double Nx[5]) {
-    const double ri = F.prim[PR_RHOI * NP + pt], q = F.prim[PR_QS * NP + pt];
-    bt_jac<DIR, double>(K, ri, F.u[NP + pt], F.u[2 * NP + pt], F.u[3 * NP + pt], F.u[4 * NP + pt], q, fd, nd);
+  // x0 at point q: the FP32 first pass inside, b itself on the boundary.
+  auto load_x = [&](int q, double x[5]) {
+    const int64_t pt = base + (int64_t)q * st;
+    if (q == 0 || q == n - 1) {
 #pragma unroll
-    for (int m = 0; m < 5; ++m) x[m] = xw[m * NP + pt];
-    bt_jx<DIR>(fd, nd, x, Fx, Nx);
+      for (int m = 0; m < 5; ++m) x[m] = rhs[m * NP + pt];
+    } else {
 #pragma unroll
-    for (int a = 0; a < 5; ++a)
-#pragma unroll
-      for (int b = 0; b < 5; ++b) {
-        if (fnz<DIR>(a, b)) f[a][b] = (T)fd[a][b];
-        if (nnz(a, b)) nj[a][b] = (T)nd[a][b];
-      }
+      for (int m = 0; m < 5; ++m) x[m] = (double)x0f[m * NP + pt];
+    }
   };
-
-  jac_at(base, xm, Fm, Nm);
-  bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Acur);
-  jac_at(base + st, x0, F0, N0);
-  bt_asm_b<T>(nj, tmp1, dd, Bcur);
-  if (n - 2 >= 2) bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Anext);
+  double acc_c[5], acc_n[5];   // partial (T x0) of rows p and p+1
+  double xq[5], sq[6];
+  float s0[6], s1[6];
+  // point 0: contributes to row 1 only (row 0 is an identity row)
+  load_x(0, xq);
+  load_state_f64(F, base, sq);
+  {
+    double Fq[5], Nq[5];
+    bt_jx<DIR>(K, sq[0], sq[5], sq[1], sq[2], sq[3], sq[4], xq, Fq, Nq);
 #pragma unroll
-  for (int m = 0; m < 5; ++m) rp[m] = (T)0.0;  // the boundary residual is exactly zero
+    for (int m = 0; m < 5; ++m) acc_c[m] = -t2d * Fq[m] - t1d * Nq[m] - t1d * ddd[m] * xq[m];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s0[e] = (float)sq[e];
+  }
+  // point 1: centre of row 1, left neighbour of row 2
+  load_x(1, xq);
+  load_state_f64(F, base + st, sq);
+  {
+    double Fq[5], Nq[5];
+    bt_jx<DIR>(K, sq[0], sq[5], sq[1], sq[2], sq[3], sq[4], xq, Fq, Nq);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      acc_c[m] += xq[m] + 2.0 * t1d * Nq[m] + 2.0 * t1d * ddd[m] * xq[m];
+      acc_n[m] = -t2d * Fq[m] - t1d * Nq[m] - t1d * ddd[m] * xq[m];
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s1[e] = (float)sq[e];
+  }
+  BtF32Carry<DIR> c;
+#pragma unroll
+  for (int m = 0; m < 5; ++m) c.rp[m] = 0.f;  // the boundary residual is exactly zero
+  bt_f32_begin<DIR>(K, n, s0, s1, c);
+  // prefetch point 2 and b_1
+  double xn[5], sn[6], bn[5];
+  load_x(2, xn);
+  load_state_f64(F, base + 2 * st, sn);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) bn[m] = rhs[m * NP + base + st];
 
   for (int p = 1; p <= n - 2; ++p) {
-    const int64_t pt = base + p * st;
-    jac_at(pt + st, xp, Fp, Np);
-    T r[5];
+    const int64_t pt = base + (int64_t)p * st;
+    double b[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) { xq[m] = xn[m]; b[m] = bn[m]; }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) sq[e] = sn[e];
+    if (p + 1 <= n - 2) {
+      load_x(p + 2, xn);
+      load_state_f64(F, base + (int64_t)(p + 2) * st, sn);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) bn[m] = rhs[m * NP + base + (int64_t)(p + 1) * st];
+    }
+    // point p+1 completes row p
+    double Fq[5], Nq[5];
+    bt_jx<DIR>(K, sq[0], sq[5], sq[1], sq[2], sq[3], sq[4], xq, Fq, Nq);
+    float r[5], s[6];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      const double tx = x0[m] + t2d * (Fp[m] - Fm[m]) - t1d * (Nm[m] - 2.0 * N0[m] + Np[m]) -
-                        t1d * ddd[m] * (xm[m] - 2.0 * x0[m] + xp[m]);
-      r[m] = (T)(rhs[m * NP + pt] - tx);
+      const double tx = acc_c[m] + t2d * Fq[m] - t1d * Nq[m] - t1d * ddd[m] * xq[m];
+      r[m] = (float)(b[m] - tx);
+      acc_c[m] = acc_n[m] + xq[m] + 2.0 * t1d * Nq[m] + 2.0 * t1d * ddd[m] * xq[m];
+      acc_n[m] = -t2d * Fq[m] - t1d * Nq[m] - t1d * ddd[m] * xq[m];
     }
-    if (p > 1) {
 #pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        T s = (T)0.0;
-#pragma unroll
-        for (int c = 0; c < 5; ++c)
-          if (anz<DIR>(m, c)) s += Acur[m][c] * rp[c];
-        r[m] -= s;
-      }
-    }
-    T B[5][5];
-#pragma unroll
-    for (int a = 0; a < 5; ++a)
-#pragma unroll
-      for (int b = 0; b < 5; ++b) {
-        T t = bnz(a, b) ? Bcur[a][b] : (T)0.0;
-        if (p > 1) {
-#pragma unroll
-          for (int c = 0; c < 5; ++c)
-            if (anz<DIR>(a, c)) t -= Acur[a][c] * Cp[c][b];
-        }
-        B[a][b] = t;
-      }
-    T C[5][5];
-    bt_asm_c<DIR, T>(f, nj, tmp1, tmp2, dd, C);
-#pragma unroll
-    for (int a = 0; a < 5; ++a)
-#pragma unroll
-      for (int b = 0; b < 5; ++b)
-        if (anz<DIR>(a, b)) Acur[a][b] = Anext[a][b];
-    if (p + 1 <= n - 2) bt_asm_b<T>(nj, tmp1, dd, Bcur);
-    if (p + 2 <= n - 2) bt_asm_a<DIR, T>(f, nj, tmp1, tmp2, dd, Anext);
-    binvcrhs<T>(B, C, r);
-#pragma unroll
-    for (int a = 0; a < 5; ++a)
-#pragma unroll
-      for (int b = 0; b < 5; ++b) {
-        Cp[a][b] = C[a][b];
-        lhsc[((int64_t)p * 25 + a * 5 + b) * nlt + gl] = C[a][b];
-      }
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      rp[m] = r[m];
-      rhs[m * NP + pt] = (double)r[m];   // b_p is no longer needed
-      xm[m] = x0[m]; x0[m] = xp[m];
-      Fm[m] = F0[m]; F0[m] = Fp[m];
-      Nm[m] = N0[m]; N0[m] = Np[m];
-    }
+    for (int e = 0; e < 6; ++e) s[e] = (float)sq[e];
+    bt_f32_step<DIR>(K, p, n, true, r, s, c, scr, nlt, gl);
+    (void)pt;
   }
-  // back substitution of the correction, then x = x0 + d
-  T dn[5] = {(T)0.0, (T)0.0, (T)0.0, (T)0.0, (T)0.0};
+  // back substitution of the correction d, then x = x0 + d
+  float dn[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   for (int p = n - 2; p >= 1; --p) {
     const int64_t pt = base + p * st;
-    T d[5];
+    float d[5];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) d[m] = (p == n - 2) ? rp[m] : (T)rhs[m * NP + pt];
+    for (int m = 0; m < 5; ++m) d[m] = (p == n - 2) ? c.rp[m] : scr[((int64_t)p * 30 + 25 + m) * nlt + gl];
 #pragma unroll
     for (int m = 0; m < 5; ++m)
 #pragma unroll
-      for (int c = 0; c < 5; ++c) d[m] -= lhsc[((int64_t)p * 25 + m * 5 + c) * nlt + gl] * dn[c];
+      for (int cc = 0; cc < 5; ++cc) d[m] -= scr[((int64_t)p * 30 + m * 5 + cc) * nlt + gl] * dn[cc];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      const double v = xw[m * NP + pt] + (double)d[m];
+      const double v = (double)x0f[m * NP + pt] + (double)d[m];
+      rhs[m * NP + pt] = v;
+      if (add_u) F.u[m * NP + pt] += v;
+      dn[m] = d[m];
+    }
+  }
+}
+
+// ============================================================================
+// Double-float (FP32 pair) arithmetic for the residual of the refinement
+// pass.  GB300 issues FP32 at 64x the FP64 rate; a value hi + lo with
+// |lo| <= ulp(hi)/2 carries about 48 significant bits, enough for the
+// residual r = b - T x0 (its error enters the refined solution at about
+// 1e-14 relative, below the FP32 re-solve's own (eps32 * kappa)^2 term).
+// Error-free transformations (Knuth two-sum, FMA two-product) are written
+// with explicit round-to-nearest intrinsics so no contraction or
+// reassociation can change them.
+// ============================================================================
+struct df64 {
+  float hi, lo;
+};
+
+__device__ __forceinline__ df64 df_quick(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ df64 df_add(df64 a, df64 b) {
+  const df64 s = df_two_sum(a.hi, b.hi);
+  return df_quick(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df64 df_neg(df64 a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df64 df_sub(df64 a, df64 b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_quick(p, e);
+}
+__device__ __forceinline__ df64 df_scale2(df64 a) { return {2.f * a.hi, 2.f * a.lo}; }  // exact
+__device__ __forceinline__ df64 df_from(double d) {
+  const float h = __double2float_rn(d);
+  return {h, __double2float_rn(d - (double)h)};
+}
+
+// F = fjac x and N = njac x in double-float (the formulas of bt_jx).
+template <int DIR>
+__device__ __forceinline__ void bt_jx_df(const df64 c1, const df64 c2, const df64 two_m_c2, const df64 k43,
+                                         const df64 c3c4, const df64 c1345, const df64 k43m, const df64 c3c4m,
+                                         const df64 st[6], const df64 x[5], df64 Fx[5], df64 Nx[5]) {
+  // st = ri, u2, u3, u4, u5, q
+  const df64 ri = st[0], q = st[5];
+  const df64 vel[3] = {df_mul(st[1], ri), df_mul(st[2], ri), df_mul(st[3], ri)};
+  const df64 E = df_mul(st[4], ri);
+  constexpr int a = DIR + 1;
+  const df64 vn = vel[DIR];
+  df64 d[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) d[m] = df_sub(x[m + 1], df_mul(vel[m], x[0]));
+  df64 tang = {0.f, 0.f};
+  Fx[0] = x[a];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    if (m == DIR) continue;
+    Fx[m + 1] = df_add(df_mul(vn, d[m]), df_mul(vel[m], x[a]));
+    tang = df_add(tang, df_mul(vel[m], x[m + 1]));
+  }
+  const df64 c2q = df_mul(c2, q), vn2 = df_mul(vn, vn), c1E = df_mul(c1, E);
+  Fx[a] = df_add(df_add(df_mul(df_sub(c2q, vn2), x[0]), df_neg(df_mul(c2, tang))),
+                 df_add(df_mul(df_mul(two_m_c2, vn), x[a]), df_mul(c2, x[4])));
+  Fx[4] = df_add(df_add(df_mul(df_mul(df_sub(df_scale2(c2q), c1E), vn), x[0]), df_neg(df_mul(df_mul(c2, vn), tang))),
+                 df_add(df_mul(df_sub(c1E, df_mul(c2, df_add(q, vn2))), x[a]), df_mul(df_mul(c1, vn), x[4])));
+  df64 s4 = df_mul(c1345, df_sub(x[4], df_mul(E, x[0])));
+  const df64 k43ri = df_mul(k43, ri), c3c4ri = df_mul(c3c4, ri);
+  Nx[0] = {0.f, 0.f};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    Nx[m + 1] = df_mul(m == DIR ? k43ri : c3c4ri, d[m]);
+    s4 = df_add(s4, df_mul(df_mul(m == DIR ? k43m : c3c4m, vel[m]), d[m]));
+  }
+  Nx[4] = df_mul(ri, s4);
+}
+
+__device__ __forceinline__ void load_state_df(const Fields& F, int64_t pt, df64 s[6]) {
+  const int64_t NP = F.NP;
+  const int order[6] = {PF_RHOI, PF_U2, PF_U3, PF_U4, PF_U5, PF_QS};
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    s[e].hi = F.primf[order[e] * NP + pt];
+    s[e].lo = F.primf[(PF_HI_COUNT + order[e]) * NP + pt];
+  }
+}
+
+// Refinement pass with the residual in double-float.  Point q contributes,
+// with P_q = tmp2 F_q and Q_q = tmp1 (N_q + D x_q),
+//   -P_q - Q_q to row q+1,   x_q + 2 Q_q to row q,   P_q - Q_q to row q-1.
+template <int DIR>
+__global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const Work* __restrict__ work,
+                                                      float* __restrict__ scr, int64_t nlt, int add_u,
+                                                      const float* __restrict__ x0f) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  double* __restrict__ rhs = F.rhs;
+
+  const df64 t1 = df_from(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
+  const df64 t2 = df_from(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  df64 D[5];
+  if (DIR == 0) { D[0] = df_from(K.dx1); D[1] = df_from(K.dx2); D[2] = df_from(K.dx3); D[3] = df_from(K.dx4); D[4] = df_from(K.dx5); }
+  else if (DIR == 1) { D[0] = df_from(K.dy1); D[1] = df_from(K.dy2); D[2] = df_from(K.dy3); D[3] = df_from(K.dy4); D[4] = df_from(K.dy5); }
+  else { D[0] = df_from(K.dz1); D[1] = df_from(K.dz2); D[2] = df_from(K.dz3); D[3] = df_from(K.dz4); D[4] = df_from(K.dz5); }
+  const df64 c1 = df_from(K.c1), c2 = df_from(K.c2), two_m_c2 = df_from(2.0 - K.c2);
+  const double k43d = K.con43 * K.c3c4;
+  const df64 k43 = df_from(k43d), c3c4 = df_from(K.c3c4), c1345 = df_from(K.c1345);
+  const df64 k43m = df_from(k43d - K.c1345), c3c4m = df_from(K.c3c4 - K.c1345);
+
+  auto load_x = [&](int q, df64 x[5]) {
+    const int64_t pt = base + (int64_t)q * st;
+    if (q == 0 || q == n - 1) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) x[m] = df_from(rhs[m * NP + pt]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) x[m] = {x0f[m * NP + pt], 0.f};
+    }
+  };
+  // P and Q of one point
+  auto pq = [&](const df64 s[6], const df64 x[5], df64 P[5], df64 Q[5]) {
+    df64 Fq[5], Nq[5];
+    bt_jx_df<DIR>(c1, c2, two_m_c2, k43, c3c4, c1345, k43m, c3c4m, s, x, Fq, Nq);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      P[m] = df_mul(t2, Fq[m]);
+      Q[m] = df_mul(t1, df_add(Nq[m], df_mul(D[m], x[m])));
+    }
+  };
+  df64 acc_c[5], acc_n[5], xq[5], sq[6], P[5], Q[5];
+  float s0[6], s1[6];
+  load_x(0, xq);
+  load_state_df(F, base, sq);
+  pq(sq, xq, P, Q);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) acc_c[m] = df_neg(df_add(P[m], Q[m]));
+#pragma unroll
+  for (int e = 0; e < 6; ++e) s0[e] = sq[e].hi;
+  load_x(1, xq);
+  load_state_df(F, base + st, sq);
+  pq(sq, xq, P, Q);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    acc_c[m] = df_add(acc_c[m], df_add(xq[m], df_scale2(Q[m])));
+    acc_n[m] = df_neg(df_add(P[m], Q[m]));
+  }
+#pragma unroll
+  for (int e = 0; e < 6; ++e) s1[e] = sq[e].hi;
+  BtF32Carry<DIR> c;
+#pragma unroll
+  for (int m = 0; m < 5; ++m) c.rp[m] = 0.f;
+  // bt_f32_begin takes ri, u2, u3, u4, u5, q in that order (as sq)
+  bt_f32_begin<DIR>(K, n, s0, s1, c);
+  df64 xn[5], sn[6];
+  double bn[5];
+  load_x(2, xn);
+  load_state_df(F, base + 2 * st, sn);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) bn[m] = rhs[m * NP + base + st];
+
+  for (int p = 1; p <= n - 2; ++p) {
+    double b[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) { xq[m] = xn[m]; b[m] = bn[m]; }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) sq[e] = sn[e];
+    if (p + 1 <= n - 2) {
+      load_x(p + 2, xn);
+      load_state_df(F, base + (int64_t)(p + 2) * st, sn);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) bn[m] = rhs[m * NP + base + (int64_t)(p + 1) * st];
+    }
+    pq(sq, xq, P, Q);
+    float r[5], s[6];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const df64 tx = df_add(acc_c[m], df_sub(P[m], Q[m]));
+      r[m] = __double2float_rn((b[m] - (double)tx.hi) - (double)tx.lo);
+      acc_c[m] = df_add(acc_n[m], df_add(xq[m], df_scale2(Q[m])));
+      acc_n[m] = df_neg(df_add(P[m], Q[m]));
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s[e] = sq[e].hi;
+    bt_f32_step<DIR>(K, p, n, true, r, s, c, scr, nlt, gl);
+  }
+  float dn[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int p = n - 2; p >= 1; --p) {
+    const int64_t pt = base + p * st;
+    float d[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) d[m] = (p == n - 2) ? c.rp[m] : scr[((int64_t)p * 30 + 25 + m) * nlt + gl];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc) d[m] -= scr[((int64_t)p * 30 + m * 5 + cc) * nlt + gl] * dn[cc];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double v = (double)x0f[m * NP + pt] + (double)d[m];
       rhs[m * NP + pt] = v;
       if (add_u) F.u[m * NP + pt] += v;
       dn[m] = d[m];
@@ -735,27 +1172,28 @@ struct SpBands {
   double l[3][5];
 };
 
-template <int DIR, typename T>
-__device__ __forceinline__ void sp_assemble(const Consts& K, int q, int n, const double cv[3], const double rhon[3],
-                                            const double spd[3], T L[3][5]) {
+template <int DIR, typename T, typename G>
+__device__ __forceinline__ void sp_assemble(const Consts& K, int q, int n, const G cv[3], const G rhon[3],
+                                            const G spd[3], T L[3][5]) {
   if (q == 0 || q == n - 1) {
 #pragma unroll
     for (int s = 0; s < 3; ++s) { L[s][0] = (T)0.0; L[s][1] = (T)0.0; L[s][2] = (T)1.0; L[s][3] = (T)0.0; L[s][4] = (T)0.0; }
     return;
   }
-  const double dtt1 = DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1;
-  const double dtt2 = DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2;
-  const double c2dtt1 = DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1;
-  double L1 = 0.0e0;
-  double L2 = -dtt2 * cv[0] - dtt1 * rhon[0];
-  double L3 = 1.0e0 + c2dtt1 * rhon[1];
-  double L4 = dtt2 * cv[2] - dtt1 * rhon[2];
-  double L5 = 0.0e0;
-  if (q == 1) { L3 += K.comz5; L4 -= K.comz4; L5 += K.comz1; }
-  if (q == 2) { L2 -= K.comz4; L3 += K.comz6; L4 -= K.comz4; L5 += K.comz1; }
-  if (q >= 3 && q <= n - 4) { L1 += K.comz1; L2 -= K.comz4; L3 += K.comz6; L4 -= K.comz4; L5 += K.comz1; }
-  if (q == n - 3) { L1 += K.comz1; L2 -= K.comz4; L3 += K.comz6; L4 -= K.comz4; }
-  if (q == n - 2) { L1 += K.comz1; L2 -= K.comz4; L3 += K.comz5; }
+  const G dtt1 = (G)(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
+  const G dtt2 = (G)(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  const G c2dtt1 = (G)(DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1);
+  const G comz1 = (G)K.comz1, comz4 = (G)K.comz4, comz5 = (G)K.comz5, comz6 = (G)K.comz6;
+  G L1 = (G)0.0;
+  G L2 = -dtt2 * cv[0] - dtt1 * rhon[0];
+  G L3 = (G)1.0 + c2dtt1 * rhon[1];
+  G L4 = dtt2 * cv[2] - dtt1 * rhon[2];
+  G L5 = (G)0.0;
+  if (q == 1) { L3 += comz5; L4 -= comz4; L5 += comz1; }
+  if (q == 2) { L2 -= comz4; L3 += comz6; L4 -= comz4; L5 += comz1; }
+  if (q >= 3 && q <= n - 4) { L1 += comz1; L2 -= comz4; L3 += comz6; L4 -= comz4; L5 += comz1; }
+  if (q == n - 3) { L1 += comz1; L2 -= comz4; L3 += comz6; L4 -= comz4; }
+  if (q == n - 2) { L1 += comz1; L2 -= comz4; L3 += comz5; }
   L[0][0] = (T)L1; L[0][1] = (T)L2; L[0][2] = (T)L3; L[0][3] = (T)L4; L[0][4] = (T)L5;
   L[1][0] = (T)L1; L[1][1] = (T)(L2 - dtt2 * spd[0]); L[1][2] = (T)L3; L[1][3] = (T)(L4 + dtt2 * spd[2]); L[1][4] = (T)L5;
   L[2][0] = (T)L1; L[2][1] = (T)(L2 + dtt2 * spd[0]); L[2][2] = (T)L3; L[2][3] = (T)(L4 - dtt2 * spd[2]); L[2][4] = (T)L5;
@@ -1004,11 +1442,181 @@ __device__ __forceinline__ void sp_transform(const Fields& F, const Consts& K, i
   }
 }
 
+// Geometry of one point for the SP band assembly, generic in the type.
+template <int DIR, typename G>
+__device__ __forceinline__ void sp_geom_t(G ri, G cvel, G spd_in, const Consts& K, G& cv, G& rhon, G& spd) {
+  const G ru1 = (G)K.c3c4 * ri;
+  cv = cvel;
+  const G da = (G)(DIR == 0 ? K.dx2 : DIR == 1 ? K.dy3 : K.dz4);
+  const G db = (G)(DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5);
+  const G dm = (G)(DIR == 0 ? K.dxmax : DIR == 1 ? K.dymax : K.dzmax);
+  const G dc = (G)(DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1);
+  rhon = fmax(fmax(fmax(da + (G)K.con43 * ru1, db + (G)K.c1c5 * ru1), dm + ru1), dc);
+  spd = spd_in;
+}
+
+// Thomas forward elimination of the three SP systems over one line, in FP32,
+// with rows supplied by row_at(q, L, r) (q = 0..n-1; L[3][5] bands, r[5]).
+// Bands l4, l5 and the eliminated rhs of rows 0..n-3 go to the line scratch
+// scr[(p*11 + e) * nlt + gl]; rows n-2 and n-1 stay in the returned state.
+struct SpF32Tail {
+  float cur4[3];     // l4 of row n-2
+  float r2[5];       // eliminated rhs of row n-2
+  float rlast[5];    // eliminated rhs of row n-1
+};
+
+template <typename RowAt>
+__device__ __forceinline__ void sp_forward_f32(int n, float* __restrict__ scr, int64_t nlt, int64_t gl, RowAt row_at,
+                                               SpF32Tail& tail) {
+  float cur3[3], cur4[3], cur5[3], nx2[3], nx3[3], nx4[3], nx5[3];
+  float rr[3][5];
+  {
+    float L0[3][5], L1[3][5];
+    row_at(0, L0, rr[0]);
+    row_at(1, L1, rr[1]);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      cur3[s] = L0[s][2]; cur4[s] = L0[s][3]; cur5[s] = L0[s][4];
+      nx2[s] = L1[s][1]; nx3[s] = L1[s][2]; nx4[s] = L1[s][3]; nx5[s] = L1[s][4];
+    }
+  }
+  for (int p = 0; p <= n - 3; ++p) {
+    float L2[3][5];
+    row_at(p + 2, L2, rr[2]);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const float fac1 = 1.0f / cur3[s];
+      cur4[s] *= fac1;
+      cur5[s] *= fac1;
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
+      nx3[s] -= nx2[s] * cur4[s];
+      nx4[s] -= nx2[s] * cur5[s];
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
+      float n2 = L2[s][1], n3 = L2[s][2];
+      n2 -= L2[s][0] * cur4[s];
+      n3 -= L2[s][0] * cur5[s];
+#pragma unroll
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[2][m] -= L2[s][0] * rr[0][m];
+      scr[((int64_t)p * 11 + 2 * s) * nlt + gl] = cur4[s];
+      scr[((int64_t)p * 11 + 2 * s + 1) * nlt + gl] = cur5[s];
+      cur3[s] = nx3[s]; cur4[s] = nx4[s]; cur5[s] = nx5[s];
+      nx2[s] = n2; nx3[s] = n3; nx4[s] = L2[s][3]; nx5[s] = L2[s][4];
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      scr[((int64_t)p * 11 + 6 + m) * nlt + gl] = rr[0][m];
+      rr[0][m] = rr[1][m];
+      rr[1][m] = rr[2][m];
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const float fac1 = 1.0f / cur3[s];
+    cur4[s] *= fac1;
+    cur5[s] *= fac1;
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
+    nx3[s] -= nx2[s] * cur4[s];
+    nx4[s] -= nx2[s] * cur5[s];
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
+    const float fac2 = 1.0f / nx3[s];
+#pragma unroll
+    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] *= fac2;
+    tail.cur4[s] = cur4[s];
+  }
+#pragma unroll
+  for (int m = 0; m < 5; ++m) { tail.r2[m] = rr[0][m]; tail.rlast[m] = rr[1][m]; }
+}
+
+// Back substitution of the three systems; emit(p, v[5]) receives rows n-2..1.
+template <typename Emit>
+__device__ __forceinline__ void sp_back_f32(int n, const float* __restrict__ scr, int64_t nlt, int64_t gl,
+                                            const SpF32Tail& tail, Emit emit) {
+  float b1[5], b2[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    const int s = m < 3 ? 0 : m - 2;
+    b2[m] = tail.rlast[m];
+    b1[m] = tail.r2[m] - tail.cur4[s] * b2[m];
+  }
+  emit(n - 2, b1);
+  for (int p = n - 3; p >= 1; --p) {
+    float r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int s = m < 3 ? 0 : m - 2;
+      const float l4 = scr[((int64_t)p * 11 + 2 * s) * nlt + gl];
+      const float l5 = scr[((int64_t)p * 11 + 2 * s + 1) * nlt + gl];
+      r[m] = scr[((int64_t)p * 11 + 6 + m) * nlt + gl] - (l4 * b1[m] + l5 * b2[m]);
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) { b2[m] = b1[m]; b1[m] = r[m]; }
+    emit(p, r);
+  }
+}
+
+// Pass 1 of the mixed SP sweep: all three systems in FP32 from the FP32
+// geometry copies; x0 (untransformed) in FP32.  Geometry of point q+1 is
+// fetched one row ahead.
+template <int DIR>
+__global__ void __launch_bounds__(128) k_sp_mixed_solve(Fields F, Consts K, const Work* __restrict__ work,
+                                                        float* __restrict__ scr, int64_t nlt,
+                                                        float* __restrict__ x0) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  const double* __restrict__ rhs = F.rhs;
+  const float* pf = F.primf;
+  const int PCV = DIR == 0 ? PS_US : DIR == 1 ? PS_VS : PS_WS;
+  // geometry window: values at rows q-1, q, q+1 of the row being assembled
+  float gcv[3], grh[3], gsp[3];
+  auto geom = [&](int q, float& cv, float& rh, float& sp) {
+    const int64_t pt = base + (int64_t)q * st;
+    sp_geom_t<DIR, float>(pf[PS_RHOI * NP + pt], pf[PCV * NP + pt], pf[PS_SPEED * NP + pt], K, cv, rh, sp);
+  };
+  geom(0, gcv[1], grh[1], gsp[1]);
+  geom(1, gcv[2], grh[2], gsp[2]);
+  gcv[0] = gcv[1]; grh[0] = grh[1]; gsp[0] = gsp[1];
+  float ncv = 0.f, nrh = 0.f, nsp = 0.f;
+  if (n > 2) geom(2, ncv, nrh, nsp);
+  auto row_at = [&](int q, float L[3][5], float r[5]) {
+    // window holds q-1, q, q+1 on entry (q+1 from the prefetch)
+    sp_assemble<DIR, float, float>(K, q, n, gcv, grh, gsp, L);
+    const int64_t pt = base + (int64_t)q * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) r[m] = (float)rhs[m * NP + pt];
+    // shift: q, q+1, prefetched q+2
+    gcv[0] = gcv[1]; grh[0] = grh[1]; gsp[0] = gsp[1];
+    gcv[1] = gcv[2]; grh[1] = grh[2]; gsp[1] = gsp[2];
+    gcv[2] = ncv; grh[2] = nrh; gsp[2] = nsp;
+    if (q + 3 <= n - 1) geom(q + 3, ncv, nrh, nsp);
+  };
+  SpF32Tail tail;
+  sp_forward_f32(n, scr, nlt, gl, row_at, tail);
+  sp_back_f32(n, scr, nlt, gl, tail, [&](int p, const float v[5]) {
+    const int64_t pt = base + (int64_t)p * st;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) x0[m * NP + pt] = v[m];
+  });
+}
+
+// Pass 2 of the mixed SP sweep: residual r = b - L x0 of each system in FP64
+// (bands of lhsx/lhsy/lhsz assembled in FP64 from a geometry window), the
+// FP32 Thomas solve of L d = r, x = x0 + d, the sweep's transform and, after
+// the z sweep, add.  x0 is b itself on the boundary rows (identity rows).
 template <int DIR>
 __global__ void __launch_bounds__(128) k_sp_refine(Fields F, Consts K, const Work* __restrict__ work,
                                                    float* __restrict__ scr, int64_t nlt, int add_u,
-                                                   const double* __restrict__ xw) {
-  using T = float;
+                                                   const float* __restrict__ x0f) {
   const Work w = work[blockIdx.x];
   const ZoneDev Z = F.zones[w.zone];
   const int line = w.first + threadIdx.x;
@@ -1019,130 +1627,87 @@ __global__ void __launch_bounds__(128) k_sp_refine(Fields F, Consts K, const Wor
   const int64_t gl = Z.lineoff[DIR] + line;
   const int64_t NP = F.NP;
   double* __restrict__ rhs = F.rhs;
-
-  auto xat = [&](int q, int m) -> double {
+  const int PCV = DIR == 0 ? PR_US : DIR == 1 ? PR_VS : PR_WS;
+  auto geom = [&](int q, double& cv, double& rh, double& sp) {
     const int64_t pt = base + (int64_t)q * st;
-    return (q == 0 || q == n - 1) ? rhs[m * NP + pt] : xw[m * NP + pt];
+    sp_geom_t<DIR, double>(F.prim[PR_RHOI * NP + pt], F.prim[PCV * NP + pt], F.prim[PR_SPEED * NP + pt], K, cv, rh,
+                           sp);
   };
-  // FP64 bands of row q and the residual r_q = b_q - L x0 (zero on boundary rows)
-  auto row = [&](int q, T L[3][5], T r[5]) {
-    double Ld[3][5];
-    double cv[3], rh[3], sp[3];
-    if (q > 0 && q < n - 1) {
-      for (int d = 0; d < 3; ++d) sp_geom<DIR>(F, K, base + (int64_t)(q - 1 + d) * st, cv[d], rh[d], sp[d]);
+  auto load_x = [&](int q, double x[5]) {
+    const int64_t pt = base + (int64_t)q * st;
+    if (q < 0 || q > n - 1) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) x[m] = 0.0;
+    } else if (q == 0 || q == n - 1) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) x[m] = rhs[m * NP + pt];
+    } else {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) x[m] = (double)x0f[m * NP + pt];
     }
-    sp_assemble<DIR, double>(K, q, n, cv, rh, sp, Ld);
+  };
+  // windows for the row being assembled, q: geometry at q-1, q, q+1 and x0 at
+  // q-2 .. q+2
+  double gcv[3], grh[3], gsp[3], ncv = 0.0, nrh = 0.0, nsp = 0.0;
+  double xw[5][5], nxp[5];
+  geom(0, gcv[1], grh[1], gsp[1]);
+  gcv[0] = gcv[1]; grh[0] = grh[1]; gsp[0] = gsp[1];
+  geom(1, gcv[2], grh[2], gsp[2]);
+  if (n > 2) geom(2, ncv, nrh, nsp);
+  load_x(-2, xw[0]);
+  load_x(-1, xw[1]);
+  load_x(0, xw[2]);
+  load_x(1, xw[3]);
+  load_x(2, xw[4]);
+  load_x(3, nxp);
+  auto row_at = [&](int q, float L[3][5], float r[5]) {
+    double Ld[3][5];
+    sp_assemble<DIR, double, double>(K, q, n, gcv, grh, gsp, Ld);
 #pragma unroll
     for (int s = 0; s < 3; ++s)
 #pragma unroll
-      for (int b = 0; b < 5; ++b) L[s][b] = (T)Ld[s][b];
+      for (int b = 0; b < 5; ++b) L[s][b] = (float)Ld[s][b];
     if (q == 0 || q == n - 1) {
 #pragma unroll
-      for (int m = 0; m < 5; ++m) r[m] = (T)0.0;
-      return;
-    }
-    const int64_t pt = base + (int64_t)q * st;
+      for (int m = 0; m < 5; ++m) r[m] = 0.f;
+    } else {
+      const int64_t pt = base + (int64_t)q * st;
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      const int s = m < 3 ? 0 : m - 2;
-      double t = 0.0;
-#pragma unroll
-      for (int d = -2; d <= 2; ++d) {
-        const int qq = q + d;
-        if (qq < 0 || qq > n - 1) continue;
-        t += Ld[s][d + 2] * xat(qq, m);
+      for (int m = 0; m < 5; ++m) {
+        const int s = m < 3 ? 0 : m - 2;
+        const double t = Ld[s][0] * xw[0][m] + Ld[s][1] * xw[1][m] + Ld[s][2] * xw[2][m] + Ld[s][3] * xw[3][m] +
+                         Ld[s][4] * xw[4][m];
+        r[m] = (float)(rhs[m * NP + pt] - t);
       }
-      r[m] = (T)(rhs[m * NP + pt] - t);
     }
+    // advance the windows to row q+1 (values of q+2 / q+3 were fetched one
+    // row earlier; fetch the next ones now)
+    gcv[0] = gcv[1]; grh[0] = grh[1]; gsp[0] = gsp[1];
+    gcv[1] = gcv[2]; grh[1] = grh[2]; gsp[1] = gsp[2];
+    gcv[2] = ncv; grh[2] = nrh; gsp[2] = nsp;
+    if (q + 3 <= n - 1) geom(q + 3, ncv, nrh, nsp);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int m = 0; m < 5; ++m) xw[k][m] = xw[k + 1][m];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) xw[4][m] = nxp[m];
+    load_x(q + 4, nxp);
   };
-
-  T cur3[3], cur4[3], cur5[3];
-  T nx2[3], nx3[3], nx4[3], nx5[3];
-  T rr[3][5];
-  {
-    T L0[3][5], L1[3][5];
-    row(0, L0, rr[0]);
-    row(1, L1, rr[1]);
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      cur3[s] = L0[s][2]; cur4[s] = L0[s][3]; cur5[s] = L0[s][4];
-      nx2[s] = L1[s][1]; nx3[s] = L1[s][2]; nx4[s] = L1[s][3]; nx5[s] = L1[s][4];
-    }
-  }
-  for (int p = 0; p <= n - 3; ++p) {
-    T L2[3][5];
-    row(p + 2, L2, rr[2]);
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const T fac1 = (T)1.0 / cur3[s];
-      cur4[s] *= fac1;
-      cur5[s] *= fac1;
-#pragma unroll
-      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
-      nx3[s] -= nx2[s] * cur4[s];
-      nx4[s] -= nx2[s] * cur5[s];
-#pragma unroll
-      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
-      T n2 = L2[s][1], n3 = L2[s][2];
-      n2 -= L2[s][0] * cur4[s];
-      n3 -= L2[s][0] * cur5[s];
-#pragma unroll
-      for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[2][m] -= L2[s][0] * rr[0][m];
-      scr[((int64_t)p * 6 + 2 * s) * nlt + gl] = cur4[s];
-      scr[((int64_t)p * 6 + 2 * s + 1) * nlt + gl] = cur5[s];
-      cur3[s] = nx3[s]; cur4[s] = nx4[s]; cur5[s] = nx5[s];
-      nx2[s] = n2; nx3[s] = n3; nx4[s] = L2[s][3]; nx5[s] = L2[s][4];
-    }
-    const int64_t pt = base + (int64_t)p * st;
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      if (p > 0) rhs[m * NP + pt] = (double)rr[0][m];   // b_p is no longer needed
-      rr[0][m] = rr[1][m];
-      rr[1][m] = rr[2][m];
-    }
-  }
-#pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    const T fac1 = (T)1.0 / cur3[s];
-    cur4[s] *= fac1;
-#pragma unroll
-    for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[0][m] *= fac1;
-  }
-  T b1[5], b2[5];
-#pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    b2[m] = (T)0.0;  // correction on the boundary row
-    const int s = m < 3 ? 0 : m - 2;
-    b1[m] = rr[0][m] - cur4[s] * b2[m];
-  }
-  auto emit = [&](int p, const T d[5]) {
+  SpF32Tail tail;
+  sp_forward_f32(n, scr, nlt, gl, row_at, tail);
+  sp_back_f32(n, scr, nlt, gl, tail, [&](int p, const float d[5]) {
     const int64_t pt = base + (int64_t)p * st;
     double v[5], o[5];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) v[m] = xw[m * NP + pt] + (double)d[m];
+    for (int m = 0; m < 5; ++m) v[m] = (double)x0f[m * NP + pt] + (double)d[m];
     sp_transform<DIR>(F, K, pt, v, o);
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
       rhs[m * NP + pt] = o[m];
       if (add_u) F.u[m * NP + pt] += o[m];
     }
-  };
-  emit(n - 2, b1);
-  for (int p = n - 3; p >= 1; --p) {
-    const int64_t pt = base + (int64_t)p * st;
-    T r[5];
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      const int s = m < 3 ? 0 : m - 2;
-      const T l4 = scr[((int64_t)p * 6 + 2 * s) * nlt + gl];
-      const T l5 = scr[((int64_t)p * 6 + 2 * s + 1) * nlt + gl];
-      r[m] = (T)rhs[m * NP + pt];
-      r[m] -= l4 * b1[m] + l5 * b2[m];
-    }
-#pragma unroll
-    for (int m = 0; m < 5; ++m) { b2[m] = b1[m]; b1[m] = r[m]; }
-    emit(p, r);
-  }
+  });
 }
 
 // ============================================================================
@@ -1197,24 +1762,44 @@ static void launch_solve_t(bool sp, int dir, const Fields& F, const Consts& K, c
   }
 }
 
-// mode 0: FP64 in place; 1: FP32 in place; 2: FP32 + FP64-residual
-// refinement (xw: a [5][NP] buffer for the first solution).
+// mode 0: FP64 in place; 1: FP32 in place; 2: FP32 + refinement with a
+// double-float residual (BT; SP: FP64 residual); 3: FP32 + refinement with
+// an FP64 residual (xw: a [5][NP] buffer for the first solution).
 void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb,
                   void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s) {
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
   if (mode == 1) { launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s); return; }
-  if (mode == 2) {
-    launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, 0, xw, 0, s);
+  if (mode == 2 || mode == 3) {
+    const bool resid64 = mode == 3;
     float* scr = reinterpret_cast<float*>(scratch);
     if (sp) {
-      if (dir == 0) k_sp_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
-      else if (dir == 1) k_sp_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
-      else k_sp_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+      float* x0 = reinterpret_cast<float*>(xw);
+      if (dir == 0) {
+        k_sp_mixed_solve<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        k_sp_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+      } else if (dir == 1) {
+        k_sp_mixed_solve<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        k_sp_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+      } else {
+        k_sp_mixed_solve<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        k_sp_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+      }
     } else {
-      if (dir == 0) k_bt_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
-      else if (dir == 1) k_bt_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
-      else k_bt_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, xw);
+      float* x0 = reinterpret_cast<float*>(xw);
+      if (dir == 0) {
+        k_bt_mixed_solve<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        if (resid64) k_bt_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+        else k_bt_refine_df<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+      } else if (dir == 1) {
+        k_bt_mixed_solve<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        if (resid64) k_bt_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+        else k_bt_refine_df<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+      } else {
+        k_bt_mixed_solve<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        if (resid64) k_bt_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+        else k_bt_refine_df<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+      }
     }
     return;
   }

@@ -814,8 +814,10 @@ void matmul_sub(const T A[5][5], const T B[5][5], T C[5][5]) {
 template <class T>
 void bt_line(int dir, int n, const double* ul, const double* ri, const double* q, double* rl, double dtt1,
              double dtt2, const double dd[5]) {
-  std::vector<T> fj((size_t)n * 25), nj((size_t)n * 25), la((size_t)n * 25), lb((size_t)n * 25),
-      lc((size_t)n * 25), r((size_t)n * 5);
+  // per-thread line scratch, reused across lines (no allocation per line)
+  static thread_local std::vector<T> fj, nj, la, lb, lc, r;
+  for (auto* v : {&fj, &nj, &la, &lb, &lc}) v->resize((size_t)n * 25);
+  r.resize((size_t)n * 5);
   auto F = [&](int p) { return reinterpret_cast<T(*)[5]>(&fj[(size_t)p * 25]); };
   auto N = [&](int p) { return reinterpret_cast<T(*)[5]>(&nj[(size_t)p * 25]); };
   auto A = [&](int p) { return reinterpret_cast<T(*)[5]>(&la[(size_t)p * 25]); };
@@ -930,8 +932,12 @@ void sp_line(int n, const double* rho_i, const double* cvel, const double* speed
   if (dir == 0) { dtt1 = K.dttx1; dtt2 = K.dttx2; c2dtt1 = K.c2dttx1; da = dx2; db = dx5; dmax_ = dxmax; dc = dx1; }
   else if (dir == 1) { dtt1 = K.dtty1; dtt2 = K.dtty2; c2dtt1 = K.c2dtty1; da = dy3; db = dy5; dmax_ = dymax; dc = dy1; }
   else { dtt1 = K.dttz1; dtt2 = K.dttz2; c2dtt1 = K.c2dttz1; da = dz4; db = dz5; dmax_ = dzmax; dc = dz1; }
-  std::vector<double> rhon(n), cv(n);
-  std::vector<T> L((size_t)n * 15), r((size_t)n * 5);
+  static thread_local std::vector<double> rhon, cv, L64;
+  static thread_local std::vector<T> L, r;
+  rhon.resize(n);
+  cv.resize(n);
+  L.resize((size_t)n * 15);
+  r.resize((size_t)n * 5);
   auto l = [&](int p, int b) -> T& { return L[(size_t)p * 15 + b]; };  // b = 0..14 (bands 1..15)
   for (int p = 0; p < n * 5; ++p) r[p] = (T)rl[p];
   for (int p = 0; p < n; ++p)
@@ -942,7 +948,7 @@ void sp_line(int n, const double* rho_i, const double* cvel, const double* speed
     rhon[p] = std::max(std::max(std::max(da + con43 * ru1, db + c1c5 * ru1), dmax_ + ru1), dc);
   }
   // lhs assembly is FP64 in the reference; it is converted to T afterwards.
-  std::vector<double> L64((size_t)n * 5, 0.0);
+  L64.assign((size_t)n * 5, 0.0);
   auto l64 = [&](int p, int b) -> double& { return L64[(size_t)p * 5 + b]; };
   for (int p = 1; p <= n - 2; ++p) {
     l64(p, 0) = 0.0e0;

@@ -208,9 +208,10 @@ MIXED_REL = 1e-10   # FP32 line solves refined against an FP64 residual
 
 
 @pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 60), ("sp_classS", 100)])
-def test_mixed_precision_within_1e10_of_fp64_oracle(oracle_mod, gname, nsteps):
+@pytest.mark.parametrize("flags", [npbmz.MIXED, npbmz.MIXED | npbmz.REFINE_FP64], ids=["df64-residual", "fp64-residual"])
+def test_mixed_precision_within_1e10_of_fp64_oracle(oracle_mod, gname, nsteps, flags):
     geom, dt, _ = GEOMS[gname]()
-    p, o = make_pair(oracle_mod, geom, dt, npbmz.MIXED, seeded(geom))
+    p, o = make_pair(oracle_mod, geom, dt, flags, seeded(geom))
     ng = p.step(nsteps, norms=True)
     no = o.step(nsteps, norms=True)
     err_u = compare(p, o, npbmz.U, MIXED_REL)
@@ -255,3 +256,46 @@ def test_reference_layout_round_trip_pinned():
         p.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, host.data_ptr(), False)
         np.testing.assert_array_equal(host.numpy()[host.numpy() != -3.0], (h * 1.5)[h != -3.0])
         assert all(np.all(np.isfinite(b)) for b in before)
+
+
+# ---- BASELINE configurations at full size (the oracle runs them on the host cores) ----
+
+def test_config1_sp_class_a_per_step_norms(oracle_mod):
+    """SP-MZ 128x128x16 split 4x4 (32x32x16 zones), dt 1.5e-3, 400 steps: per-step
+    residual and error norms of the FP64 GPU path within 1e-12 of the oracle."""
+    geom, dt, niter = geom_class("SP", "A")
+    p, o = make_pair(oracle_mod, geom, dt, 0, seeded(geom))
+    ng = p.step(niter, norms=True)
+    no = o.step(niter, norms=True)
+    np.testing.assert_allclose(ng, no, rtol=FAST_REL, atol=0)
+    compare(p, o, npbmz.U, FAST_REL)
+
+
+@pytest.mark.parametrize("flags,rel", [(0, FAST_REL), (npbmz.MIXED, MIXED_REL), (npbmz.MIXED | npbmz.GRAPH, MIXED_REL)],
+                         ids=["fp64", "mixed", "mixed-graph"])
+def test_config2_bt_class_b_final_norms(oracle_mod, flags, rel):
+    """BT-MZ 304x208x17 split 8x8 (area ratio 20.05), dt 3e-4, 200 steps, batched:
+    final norms of each variant against the FP64 oracle."""
+    geom, dt, niter = geom_class("BT", "B")
+    p, o = make_pair(oracle_mod, geom, dt, flags, seeded(geom))
+    p.step(niter)
+    o.step(niter)
+    p.synchronize()
+    xg = np.concatenate(p.verify())
+    xo = np.concatenate(o.verify())
+    np.testing.assert_allclose(xg, xo, rtol=rel, atol=0)
+
+
+def test_config2_autotuned_launch_shapes_keep_results(oracle_mod):
+    geom, dt, niter = geom_class("BT", "B")
+    ce = seeded(geom)
+    a = npbmz.Problem(geom, dt, 0)
+    a.setup(ce)
+    a.autotune()
+    a.setup(ce)
+    b = npbmz.Problem(geom, dt, 0)
+    b.setup(ce)
+    a.step(5)
+    b.step(5)
+    for z in range(0, geom.nzones, 7):
+        np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
