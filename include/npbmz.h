@@ -149,6 +149,21 @@ int npbmz_verify(npbmz_t* h, double* xcr, double* xce);
 /* One phase (NPBMZ_PHASE_*) for one zone or all zones (zone = -1). */
 int npbmz_phase(npbmz_t* h, int phase, int zone);
 
+/* Discrete adjoint of nsteps BT-MZ time steps (exch_qbc + adi of all zones,
+ * the loop body of src/BT/bt-node.jl:280-395) from the handle's current u
+ * and forcing, for the terminal objective
+ *     J = 1/2 * sum over every stored point of every zone of (u_N - u_target)^2.
+ * u_target, grad_forcing and grad_u0 are host arrays of the dense layout for
+ * all zones back to back (zone z: [5][nz][ny][nx]).  grad_forcing receives
+ * dJ/dforcing and grad_u0 dJ/du_0 (either may be NULL); J (nullable) the
+ * objective.  The forward pass keeps u every checkpoint_every steps; the
+ * reverse pass recomputes the steps of one checkpoint interval at a time.
+ * u is left as it was on entry; rhs is overwritten.  BT only.  No
+ * counterpart in the reference (its gradient would come from ForwardDiff
+ * dual numbers pushed through the Julia step).  Synchronous. */
+int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_target, double* J,
+                  double* grad_forcing, double* grad_u0);
+
 /* Use `stream` (a cudaStream_t, NULL = the legacy default stream) for all
  * later work of the handle. */
 int npbmz_set_stream(npbmz_t* h, void* stream);

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/npbmz.h"
+#include "adjoint_launch.h"
 #include "common_launch.h"
 #include "npbmz_internal.cuh"
 #include "step_launch.h"
@@ -557,6 +558,157 @@ namespace npbmz {
 void set_global_error(const char* msg) { g_create_error = msg; }
 }  // namespace npbmz
 
+// ---- discrete adjoint of the BT step ----------------------------------------
+namespace {
+
+// Device buffers of one npbmz_adjoint call, freed on every exit path.
+struct AdjointBuffers {
+  std::vector<void*> owned;
+  ~AdjointBuffers() {
+    for (void* p : owned) cudaFree(p);
+  }
+  template <typename T>
+  int get(npbmz_t* h, T** p, size_t count) {
+    *p = nullptr;
+    CK(h, cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
+    owned.push_back(*p);
+    return 0;
+  }
+};
+
+// All zones' planes <-> a host array of the dense layout ([m][k][j][i] per
+// zone, zones back to back), synchronous.
+int dense_io(npbmz_t* h, double* planes, double* host, int dir) {
+  const std::vector<int64_t>& so = h->soff_h[NPBMZ_LAYOUT_DENSE][NPBMZ_U];
+  const int64_t total = so[h->nzones];
+  if (ensure_stage(h, (size_t)total)) return -1;
+  const Fields F = fields(h);
+  const int64_t* soff = h->soff_d[NPBMZ_LAYOUT_DENSE][NPBMZ_U];
+  if (dir == 0) {
+    CK(h, cudaMemcpyAsync(h->stage, host, total * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_convert(F, planes, h->stage, soff, 0, 0, h->nzones, h->max_np, h->kind, NPBMZ_U, 0, 0, h->stream);
+    CKL(h);
+  } else {
+    launch_convert(F, planes, h->stage, soff, 0, 0, h->nzones, h->max_np, h->kind, NPBMZ_U, 0, 1, h->stream);
+    CKL(h);
+    CK(h, cudaMemcpyAsync(host, h->stage, total * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+// Forward step n recomputed from u_n (in h->u): h->u becomes v = exch_qbc(u_n)
+// (the state every Jacobian of the step is taken at), x[d] the solution of
+// sweep d.  The update u_{n+1} = v + x[2] is not applied.
+int adjoint_recompute(npbmz_t* h, double* const x[3]) {
+  const size_t bytes = 5 * (size_t)h->NP * sizeof(double);
+  if (phase_exch(h)) return -1;
+  if (phase_prim(h, -1)) return -1;
+  if (phase_rhs(h, -1, false, false)) return -1;
+  for (int dir = 0; dir < 3; ++dir) {
+    if (phase_solve(h, dir, -1, 0)) return -1;
+    CK(h, cudaMemcpyAsync(x[dir], h->rhs, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  return 0;
+}
+
+// ub <- (d u_{n+1} / d u_n)^T ub and fb += (d u_{n+1} / d forcing)^T ub,
+// after adjoint_recompute of step n.
+int adjoint_back_step(npbmz_t* h, double* const x[3], double* ub, double* vb, double* yb, double* fb, double* scr) {
+  const size_t bytes = 5 * (size_t)h->NP * sizeof(double);
+  const Fields F = fields(h);
+  // add: u_{n+1} = v + x3 on the interior
+  CK(h, cudaMemcpyAsync(vb, ub, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  adj_launch_seed(F, h->wpts_d, h->nwpts, ub, nullptr, yb, nullptr, 1, h->stream);
+  CKL(h);
+  // the sweeps in reverse order
+  for (int dir = 2; dir >= 0; --dir) {
+    adj_launch_solve(dir, F, h->K, h->wline_d[dir], h->nwline[dir], h->tpb_line[dir], yb, x[dir], vb, scr,
+                     h->nlines[dir], h->stream);
+    CKL(h);
+  }
+  // compute_rhs (yb is now the adjoint of rhs)
+  adj_launch_rhs(F, h->K, h->wpts_d, h->nwpts, yb, vb, fb, h->stream);
+  CKL(h);
+  // exch_qbc
+  CK(h, cudaMemcpyAsync(ub, vb, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->nzones > 1) {
+    adj_launch_exch(F, h->nbr_d, h->nzones, h->max_face, vb, ub, h->stream);
+    CKL(h);
+  }
+  return 0;
+}
+
+int adjoint_run(npbmz_t* h, int nsteps, int every, const double* u_target, double* J, double* grad_forcing,
+                double* grad_u0) {
+  const cudaStream_t s = h->stream;
+  const size_t F5 = 5 * (size_t)h->NP, bytes = F5 * sizeof(double);
+  const int nck = (nsteps + every - 1) / every;
+  const int seglen = std::min(every, nsteps);
+  int64_t scr_elems = 0;
+  for (int dir = 0; dir < 3; ++dir) {
+    int maxlen = 0;
+    for (const ZoneDev& z : h->zh) maxlen = std::max(maxlen, zone_line_len(z, dir));
+    scr_elems = std::max<int64_t>(scr_elems, 30 * (int64_t)maxlen * h->nlines[dir]);
+  }
+  AdjointBuffers B;
+  double *ck, *seg, *x[3], *yb, *vb, *ub, *fb, *tgt, *scr, *part;
+  if (B.get(h, &ck, (size_t)nck * F5) || B.get(h, &seg, (size_t)seglen * F5) || B.get(h, &x[0], F5) ||
+      B.get(h, &x[1], F5) || B.get(h, &x[2], F5) || B.get(h, &yb, F5) || B.get(h, &vb, F5) || B.get(h, &ub, F5) ||
+      B.get(h, &fb, F5) || B.get(h, &tgt, F5) || B.get(h, &scr, (size_t)scr_elems) || B.get(h, &part, 5 * (size_t)h->nwpts))
+    return -1;
+  CK(h, cudaMemsetAsync(fb, 0, bytes, s));
+  CK(h, cudaMemsetAsync(tgt, 0, bytes, s));
+  CK(h, cudaMemcpyAsync(ck, h->u, bytes, cudaMemcpyDeviceToDevice, s));
+  int rc = 0;
+  // forward pass, keeping u every `every` steps
+  for (int n = 0; n < nsteps && !rc; ++n) {
+    if (n % every == 0 && n > 0) rc = cudaMemcpyAsync(ck + (size_t)(n / every) * F5, h->u, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess;
+    if (!rc) rc = one_step(h, false, nullptr);
+  }
+  // objective: J = 1/2 sum over every stored point of (u_N - u_target)^2
+  if (!rc) rc = dense_io(h, tgt, const_cast<double*>(u_target), 0);
+  if (!rc) {
+    adj_launch_seed(fields(h), h->wpts_d, h->nwpts, h->u, tgt, ub, part, 0, s);
+    rc = cudaGetLastError() != cudaSuccess;
+  }
+  if (!rc) {
+    std::vector<double> ph(5 * (size_t)h->nwpts);
+    rc = cudaMemcpyAsync(ph.data(), part, ph.size() * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+         cudaStreamSynchronize(s) != cudaSuccess;
+    double sum = 0.0;
+    for (double v : ph) sum += v;
+    if (J) *J = 0.5 * sum;
+  }
+  // reverse pass, one checkpoint segment at a time
+  for (int c = nck - 1; c >= 0 && !rc; --c) {
+    const int n0 = c * every, n1 = std::min(n0 + every, nsteps);
+    rc = cudaMemcpyAsync(h->u, ck + (size_t)c * F5, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess;
+    for (int n = n0; n < n1 && !rc; ++n) {
+      rc = cudaMemcpyAsync(seg + (size_t)(n - n0) * F5, h->u, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess;
+      if (!rc && n + 1 < n1) rc = one_step(h, false, nullptr);
+    }
+    for (int n = n1 - 1; n >= n0 && !rc; --n) {
+      rc = cudaMemcpyAsync(h->u, seg + (size_t)(n - n0) * F5, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess;
+      if (!rc) rc = adjoint_recompute(h, x);
+      if (!rc) rc = adjoint_back_step(h, x, ub, vb, yb, fb, scr);
+    }
+  }
+  if (!rc && grad_forcing) rc = dense_io(h, fb, grad_forcing, 1);
+  if (!rc && grad_u0) rc = dense_io(h, ub, grad_u0, 1);
+  // the handle's state is u_0 again
+  const bool restored = cudaMemcpyAsync(h->u, ck, bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                        cudaStreamSynchronize(s) == cudaSuccess;
+  if (rc) {
+    if (h->err.empty()) h->err = std::string("adjoint failed: ") + cudaGetErrorString(cudaGetLastError());
+    return -1;
+  }
+  if (!restored) return fail(h, "adjoint: restoring u_0 failed: %s", cudaGetErrorString(cudaGetLastError()));
+  return 0;
+}
+
+}  // namespace
+
 // =============================== C ABI ======================================
 extern "C" {
 
@@ -711,7 +863,7 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   rc |= dalloc(h, &h->prim, (size_t)PR_COUNT * h->NP);
   rc |= dalloc(h, &h->uex, 5 * (size_t)h->NP);
   if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
-  if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? PF_COUNT : PS_COUNT) * h->NP);
+  if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? (int)PF_COUNT : (int)PS_COUNT) * h->NP);
   if (!rc) {
     if (cudaMalloc(&h->scratch, std::max<size_t>(h->scratch_bytes, 16)) != cudaSuccess) rc = fail(h, "scratch alloc failed");
     else h->device_bytes += (int64_t)h->scratch_bytes;
@@ -843,6 +995,17 @@ int npbmz_verify(npbmz_t* h, double* xcr, double* xce) {
   CK(h, cudaStreamSynchronize(h->stream));
   for (int m = 0; m < 5; ++m) { xcr[m] = buf[m]; xce[m] = buf[5 + m]; }
   return 0;
+}
+
+int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_target, double* J,
+                  double* grad_forcing, double* grad_u0) {
+  if (!h) return fail(nullptr, "null handle");
+  if (h->kind != NPBMZ_BT) return fail(h, "the discrete adjoint covers BT-MZ only");
+  if (nsteps < 1 || checkpoint_every < 1) return fail(h, "nsteps and checkpoint_every must be >= 1");
+  if (!u_target) return fail(h, "u_target is null");
+  h->err.clear();
+  CK(h, cudaStreamSynchronize(h->stream));
+  return adjoint_run(h, nsteps, checkpoint_every, u_target, J, grad_forcing, grad_u0);
 }
 
 int npbmz_phase(npbmz_t* h, int phase, int zone) {

@@ -1724,6 +1724,7 @@ __global__ void __launch_bounds__(128) k_add(Fields F, const Work* __restrict__ 
   for (int m = 0; m < 5; ++m) F.u[m * F.NP + p] += F.rhs[m * F.NP + p];
 }
 
+#ifndef NPBMZ_NO_LAUNCHERS
 // ============================================================================
 // host-side launchers (declared in step_launch.h)
 // ============================================================================
@@ -1813,6 +1814,8 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
 void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s) {
   if (nwork > 0) k_add<<<nwork, 128, 0, s>>>(F, work);
 }
+
+#endif  // NPBMZ_NO_LAUNCHERS
 
 }  // namespace NPBMZ_NS
 }  // namespace npbmz

@@ -43,7 +43,7 @@ EXPORTS = [
     "npbmz_download", "npbmz_upload_async", "npbmz_download_async", "npbmz_exch_qbc", "npbmz_adi", "npbmz_step",
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
-    "npbmz_bt_xsolve_noalloc",
+    "npbmz_bt_xsolve_noalloc", "npbmz_adjoint",
 ]
 
 # Problem classes (src/BT/classes.jl:15-24, src/SP/classes.jl:16-25):
@@ -129,6 +129,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_last_error.restype = ctypes.c_char_p
     L.npbmz_destroy.argtypes = [vp]
     L.npbmz_bt_xsolve_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, vp, vp, vp]
+    L.npbmz_adjoint.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp]
     _lib = L
     return L
 
@@ -281,6 +282,54 @@ class Problem:
 
     def autotune(self):
         self._check(lib().npbmz_autotune(self._h), "npbmz_autotune")
+
+    def adjoint(self, nsteps: int, u_target, checkpoint_every: int = 10, grad_forcing: bool = True,
+                grad_u0: bool = True):
+        """Discrete adjoint of ``nsteps`` steps for J = 1/2 sum (u_N - u_target)^2
+        over every stored point (BT only).  ``u_target``: one dense array per
+        zone (or the flat concatenation).  Returns (J, dJ/dforcing, dJ/du0),
+        the gradients as lists of per-zone dense arrays (None when not asked
+        for).  u is left as it was."""
+        total = self.dense_total()
+        t = self.flatten(u_target)
+        gf = np.zeros(total) if grad_forcing else None
+        gu = np.zeros(total) if grad_u0 else None
+        J = ctypes.c_double(0.0)
+        self._check(lib().npbmz_adjoint(self._h, nsteps, checkpoint_every, _dp(t), ctypes.byref(J),
+                                        _dp(gf) if gf is not None else None, _dp(gu) if gu is not None else None),
+                    "npbmz_adjoint")
+        return J.value, (self.split(gf) if gf is not None else None), (self.split(gu) if gu is not None else None)
+
+    # -- all zones in the dense layout (zone z: [5][nz][ny][nx], zones back to back) --
+    def dense_total(self) -> int:
+        return int(5 * np.sum(self._nx.astype(np.int64) * self._ny * self._nz))
+
+    def flatten(self, arrays):
+        if isinstance(arrays, np.ndarray) and arrays.ndim == 1:
+            a = np.ascontiguousarray(arrays, np.float64)
+        else:
+            a = np.concatenate([np.ascontiguousarray(x, np.float64).reshape(-1) for x in arrays])
+        if a.size != self.dense_total():
+            raise NpbmzError(f"{a.size} values for {self.dense_total()} dense elements")
+        return a
+
+    def split(self, flat):
+        out, o = [], 0
+        for z in range(self.geom.nzones):
+            shp = self.zone_shape(z)
+            n = int(np.prod(shp))
+            out.append(flat[o:o + n].reshape(shp))
+            o += n
+        return out
+
+    def download_all(self, field: int):
+        out = np.zeros(self.dense_total())
+        self._check(lib().npbmz_download(self._h, -1, field, LAYOUT_DENSE, out.ctypes.data), "npbmz_download")
+        return self.split(out)
+
+    def upload_all(self, field: int, arrays):
+        a = self.flatten(arrays)
+        self._check(lib().npbmz_upload(self._h, -1, field, LAYOUT_DENSE, a.ctypes.data), "npbmz_upload")
 
     # -- data movement -------------------------------------------------------------
     def zone_shape(self, zone):

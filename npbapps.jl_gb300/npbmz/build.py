@@ -6,6 +6,7 @@ The translation units compile in parallel:
   step_fast.cu       -fmad=true   FP64 (FMA) and FP32 line-solve kernels
   npbmz_api.cu                    the C ABI (include/npbmz.h)
   noalloc.cu         -fmad=true   the x sweep over a file-scope device array
+  adjoint.cu         -fmad=true   the discrete adjoint of the BT step
 and are linked into npbapps.jl_gb300/npbmz/_build/libnpbmz_gpu.so.
 """
 import os
@@ -29,6 +30,7 @@ UNITS = {
     "step_fast.cu": ["-fmad=true"],
     "npbmz_api.cu": [],
     "noalloc.cu": ["-fmad=true"],
+    "adjoint.cu": ["-fmad=true"],
 }
 
 

@@ -34,6 +34,12 @@
 // The line solves are templated on the arithmetic type T so that the same
 // restatement also runs with float line solves (the mixed-precision variant's
 // expected behaviour); T = double is the reference path.
+//
+// The state (u, rhs, forcing and the primitive variables) has the scalar type
+// `real`, double here.  oracle/npbmz_tangent.cpp includes this file with a
+// forward-mode dual number as `real` (ORACLE_REAL, ORACLE_BT_ONLY) to push
+// directional derivatives through the same BT statements; the dual's value
+// part then follows exactly the double operations of this file.
 
 #include <algorithm>
 #include <cmath>
@@ -41,7 +47,17 @@
 #include <cstring>
 #include <vector>
 
+#ifndef ORACLE_REAL
+#define ORACLE_REAL double
+#endif
+#ifndef ORACLE_BT_ONLY
+#define ORACLE_BT_ONLY 0
+#endif
+
 namespace {
+
+typedef ORACLE_REAL real;
+inline double value(double x) { return x; }
 
 constexpr int KIND_BT = 0;
 constexpr int KIND_SP = 1;
@@ -114,12 +130,12 @@ void exact_solution(double xi, double eta, double zeta, const double* ce, double
 
 struct Zone {
   int nx, ny, nz;
-  std::vector<double> u, rhs, forcing;                  // [k][j][i][m]
-  std::vector<double> rho_i, us, vs, ws, qs, square, speed, ainv;  // [k][j][i]
+  std::vector<real> u, rhs, forcing;                  // [k][j][i][m]
+  std::vector<real> rho_i, us, vs, ws, qs, square, speed, ainv;  // [k][j][i]
   size_t P(int i, int j, int k) const { return ((size_t)k * ny + j) * nx + i; }
-  double& U(int m, int i, int j, int k) { return u[P(i, j, k) * 5 + m]; }
-  double& R(int m, int i, int j, int k) { return rhs[P(i, j, k) * 5 + m]; }
-  double& F(int m, int i, int j, int k) { return forcing[P(i, j, k) * 5 + m]; }
+  real& U(int m, int i, int j, int k) { return u[P(i, j, k) * 5 + m]; }
+  real& R(int m, int i, int j, int k) { return rhs[P(i, j, k) * 5 + m]; }
+  real& F(int m, int i, int j, int k) { return forcing[P(i, j, k) * 5 + m]; }
 };
 
 struct Problem {
@@ -408,7 +424,7 @@ void exch_qbc(Problem& pb) {
   const int nzn = pb.nzones;
   // All sends are packed before any receive is unpacked (MPI semantics), so
   // snapshot every source plane first.
-  std::vector<std::vector<double>> west_src(nzn), east_src(nzn), south_src(nzn), north_src(nzn);
+  std::vector<std::vector<real>> west_src(nzn), east_src(nzn), south_src(nzn), north_src(nzn);
   for (int zi = 0; zi < nzn; ++zi) {
     Zone& z = pb.zones[zi];
     // plane sent to the east neighbour (its west ghost): i = nx-2
@@ -455,7 +471,7 @@ void compute_rhs(Problem& pb, Zone& z) {
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i) {
         size_t p = z.P(i, j, k);
-        double rho_inv = 1.0e0 / z.U(0, i, j, k);
+        real rho_inv = 1.0e0 / z.U(0, i, j, k);
         z.rho_i[p] = rho_inv;
         z.us[p] = z.U(1, i, j, k) * rho_inv;
         z.vs[p] = z.U(2, i, j, k) * rho_inv;
@@ -464,8 +480,9 @@ void compute_rhs(Problem& pb, Zone& z) {
                                z.U(3, i, j, k) * z.U(3, i, j, k)) * rho_inv;
         z.qs[p] = z.square[p] * rho_inv;
         if (pb.kind == KIND_SP) {
-          double aux = c1c2 * rho_inv * (z.U(4, i, j, k) - z.square[p]);
-          aux = std::sqrt(aux);
+          using std::sqrt;
+          real aux = c1c2 * rho_inv * (z.U(4, i, j, k) - z.square[p]);
+          aux = sqrt(aux);
           z.speed[p] = aux;
           z.ainv[p] = 1.0e0 / aux;
         }
@@ -483,7 +500,7 @@ void compute_rhs(Problem& pb, Zone& z) {
   for (int k = 1; k <= nz - 2; ++k)
     for (int j = 1; j <= ny - 2; ++j)
       for (int i = 1; i <= nx - 2; ++i) {
-        double uijk = us(i, j, k), up1 = us(i + 1, j, k), um1 = us(i - 1, j, k);
+        real uijk = us(i, j, k), up1 = us(i + 1, j, k), um1 = us(i - 1, j, k);
         z.R(0, i, j, k) += K.dx1tx1 * (u.U(0, i + 1, j, k) - 2.0e0 * u.U(0, i, j, k) + u.U(0, i - 1, j, k)) -
                            K.tx2 * (u.U(1, i + 1, j, k) - u.U(1, i - 1, j, k));
         z.R(1, i, j, k) += K.dx2tx1 * (u.U(1, i + 1, j, k) - 2.0e0 * u.U(1, i, j, k) + u.U(1, i - 1, j, k)) +
@@ -536,7 +553,7 @@ void compute_rhs(Problem& pb, Zone& z) {
   for (int k = 1; k <= nz - 2; ++k)
     for (int j = 1; j <= ny - 2; ++j)
       for (int i = 1; i <= nx - 2; ++i) {
-        double vijk = vs(i, j, k), vp1 = vs(i, j + 1, k), vm1 = vs(i, j - 1, k);
+        real vijk = vs(i, j, k), vp1 = vs(i, j + 1, k), vm1 = vs(i, j - 1, k);
         z.R(0, i, j, k) += K.dy1ty1 * (u.U(0, i, j + 1, k) - 2.0e0 * u.U(0, i, j, k) + u.U(0, i, j - 1, k)) -
                            K.ty2 * (u.U(2, i, j + 1, k) - u.U(2, i, j - 1, k));
         z.R(1, i, j, k) += K.dy2ty1 * (u.U(1, i, j + 1, k) - 2.0e0 * u.U(1, i, j, k) + u.U(1, i, j - 1, k)) +
@@ -590,7 +607,7 @@ void compute_rhs(Problem& pb, Zone& z) {
   for (int k = 1; k <= nz - 2; ++k)
     for (int j = 1; j <= ny - 2; ++j)
       for (int i = 1; i <= nx - 2; ++i) {
-        double wijk = ws(i, j, k), wp1 = ws(i, j, k + 1), wm1 = ws(i, j, k - 1);
+        real wijk = ws(i, j, k), wp1 = ws(i, j, k + 1), wm1 = ws(i, j, k - 1);
         z.R(0, i, j, k) += K.dz1tz1 * (u.U(0, i, j, k + 1) - 2.0e0 * u.U(0, i, j, k) + u.U(0, i, j, k - 1)) -
                            K.tz2 * (u.U(3, i, j, k + 1) - u.U(3, i, j, k - 1));
         z.R(1, i, j, k) += K.dz2tz1 * (u.U(1, i, j, k + 1) - 2.0e0 * u.U(1, i, j, k) + u.U(1, i, j, k - 1)) +
@@ -812,7 +829,7 @@ void matmul_sub(const T A[5][5], const T B[5][5], T C[5][5]) {
 // rl: rhs (in/out).  Restates x_solve_cell + x_backsubstitute for one (j,k).
 // dtt1 = dt*t?1, dtt2 = dt*t?2, dd[5] = d?1..d?5 of the direction.
 template <class T>
-void bt_line(int dir, int n, const double* ul, const double* ri, const double* q, double* rl, double dtt1,
+void bt_line(int dir, int n, const real* ul, const real* ri, const real* q, real* rl, double dtt1,
              double dtt2, const double dd[5]) {
   // per-thread line scratch, reused across lines (no allocation per line)
   static thread_local std::vector<T> fj, nj, la, lb, lc, r;
@@ -867,7 +884,7 @@ void bt_line(int dir, int n, const double* ul, const double* ri, const double* q
   for (int p = n - 2; p >= 0; --p)
     for (int m = 0; m < 5; ++m)
       for (int c = 0; c < 5; ++c) r[p * 5 + m] -= C(p)[m][c] * r[(p + 1) * 5 + c];
-  for (int p = 0; p < n * 5; ++p) rl[p] = (double)r[p];
+  for (int p = 0; p < n * 5; ++p) rl[p] = (real)r[p];
 }
 
 template <class T>
@@ -881,7 +898,7 @@ void bt_sweep(Problem& pb, Zone& z, int dir) {
   if (dir == 0) { dd[0] = dx1; dd[1] = dx2; dd[2] = dx3; dd[3] = dx4; dd[4] = dx5; dtt1 = K.dt * K.tx1; dtt2 = K.dt * K.tx2; }
   else if (dir == 1) { dd[0] = dy1; dd[1] = dy2; dd[2] = dy3; dd[3] = dy4; dd[4] = dy5; dtt1 = K.dt * K.ty1; dtt2 = K.dt * K.ty2; }
   else { dd[0] = dz1; dd[1] = dz2; dd[2] = dz3; dd[3] = dz4; dd[4] = dz5; dtt1 = K.dt * K.tz1; dtt2 = K.dt * K.tz2; }
-  std::vector<double> ul(n * 5), ri(n), q(n), rl(n * 5);
+  std::vector<real> ul(n * 5), ri(n), q(n), rl(n * 5);
   for (int b = 1; b <= nb - 2; ++b)
     for (int a = 1; a <= na - 2; ++a) {
       for (int p = 0; p < n; ++p) {
@@ -899,6 +916,7 @@ void bt_sweep(Problem& pb, Zone& z, int dir) {
     }
 }
 
+#if !ORACLE_BT_ONLY
 // ======================= SP scalar pentadiagonal solves ======================
 // txinvr (src/SP/txinvr.jl:5-56)
 void txinvr(Zone& z) {
@@ -1088,6 +1106,8 @@ void sp_sweep(Problem& pb, Zone& z, int dir) {
       }
 }
 
+#endif  // !ORACLE_BT_ONLY
+
 void add(Zone& z) {
   for (int k = 1; k <= z.nz - 2; ++k)
     for (int j = 1; j <= z.ny - 2; ++j)
@@ -1106,6 +1126,9 @@ void adi(Problem& pb, Zone& z, double* xcr = nullptr) {
     double xce_unused[5];
     zone_norms(pb, z, xce_unused, xcr);
   }
+#if ORACLE_BT_ONLY
+  for (int d = 0; d < 3; ++d) bt_sweep<real>(pb, z, d);
+#else
   if (pb.kind == KIND_BT) {
     for (int d = 0; d < 3; ++d) {
       if (pb.solve_float) bt_sweep<float>(pb, z, d); else bt_sweep<double>(pb, z, d);
@@ -1116,6 +1139,7 @@ void adi(Problem& pb, Zone& z, double* xcr = nullptr) {
       if (pb.solve_float) sp_sweep<float>(pb, z, d); else sp_sweep<double>(pb, z, d);
     }
   }
+#endif
   add(z);
 }
 
@@ -1133,7 +1157,7 @@ void zone_norms(Problem& pb, Zone& z, double xce[5], double xcr[5]) {
         double xi = (double)i * K.dnxm1;
         exact_solution(xi, eta, zeta, pb.ce, ue);
         for (int m = 0; m < 5; ++m) {
-          double a = z.U(m, i, j, k) - ue[m];
+          double a = value(z.U(m, i, j, k)) - ue[m];
           rms[m] = rms[m] + a * a;
         }
       }
@@ -1146,7 +1170,7 @@ void zone_norms(Problem& pb, Zone& z, double xce[5], double xcr[5]) {
     for (int j = 1; j <= z.ny - 2; ++j)
       for (int i = 1; i <= z.nx - 2; ++i)
         for (int m = 0; m < 5; ++m) {
-          double a = z.R(m, i, j, k);
+          double a = value(z.R(m, i, j, k));
           rr[m] = rr[m] + a * a;
         }
   for (int m = 0; m < 5; ++m) xcr[m] = std::sqrt(rr[m] / denom);
@@ -1154,6 +1178,7 @@ void zone_norms(Problem& pb, Zone& z, double xce[5], double xcr[5]) {
 
 }  // namespace
 
+#if !ORACLE_BT_ONLY
 // =============================== C ABI ======================================
 extern "C" {
 
@@ -1332,3 +1357,4 @@ int oracle_set(oracle_t* h, int which, int zone, const double* in) {
 }
 
 }  // extern "C"
+#endif  // !ORACLE_BT_ONLY

@@ -2,7 +2,10 @@
 
 The oracle restates the NPBApps.jl BT-MZ/SP-MZ single-rank time step on the
 CPU (oracle/npbmz_oracle.cpp).  Only tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py use it, always as the checker.
+CPU-baseline leg of bench.py use it, always as the checker.  The tangent
+library (oracle/npbmz_tangent.cpp) is the same BT restatement with
+forward-mode dual numbers: the reference directional derivatives against
+which tests check the GPU adjoint.
 """
 import ctypes
 import os
@@ -13,15 +16,58 @@ import numpy as np
 
 _HERE = Path(__file__).resolve().parent
 _LIB_PATH = _HERE / "_build" / "libnpbmz_oracle.so"
+_TAN_PATH = _HERE / "_build" / "libnpbmz_tangent.so"
 _lib = None
+_tan = None
+TANGENT_NDIR = 16
 
 KIND_BT, KIND_SP = 0, 1
 
 
 def build(force=False):
-    if force or not _LIB_PATH.exists() or _LIB_PATH.stat().st_mtime < (_HERE / "npbmz_oracle.cpp").stat().st_mtime:
+    srcs = [_HERE / "npbmz_oracle.cpp", _HERE / "npbmz_tangent.cpp"]
+    newest = max(p.stat().st_mtime for p in srcs)
+    if force or any(not p.exists() or p.stat().st_mtime < newest for p in (_LIB_PATH, _TAN_PATH)):
         subprocess.run(["make", "-s", "-C", str(_HERE)], check=True)
     return _LIB_PATH
+
+
+def tangent_lib():
+    global _tan
+    if _tan is None:
+        build()
+        L = ctypes.CDLL(str(_TAN_PATH))
+        ip = ctypes.POINTER(ctypes.c_int)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.tangent_bt_objective.argtypes = ([ctypes.c_int, ip, ip, ip, ip, ctypes.c_double] + [ctypes.c_int] * 5 +
+                                           [dp, dp, dp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp])
+        _tan = L
+    return _tan
+
+
+def tangent_bt_objective(nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, u0, forcing, u_target, nsteps, du0=None,
+                         dforcing=None):
+    """J = 1/2 sum (u_N - u_target)^2 after nsteps BT-MZ steps and its
+    derivatives along up to 16 directions, by dual numbers through the
+    oracle.  Flat dense arrays (zone z: [5][nz][ny][nx], zones back to back);
+    du0 / dforcing: (ndir, total) or None.  Returns (J, dJ[ndir], u_N)."""
+    nx, ny, nz, nbr = (np.ascontiguousarray(a, np.int32) for a in (nx, ny, nz, nbr))
+    u0, forcing, u_target = (np.ascontiguousarray(a, np.float64) for a in (u0, forcing, u_target))
+    total = u0.size
+    seeds = [a for a in (du0, dforcing) if a is not None]
+    ndir = seeds[0].shape[0] if seeds else 0
+    assert ndir <= TANGENT_NDIR
+    du0 = None if du0 is None else np.ascontiguousarray(du0, np.float64).reshape(ndir, total)
+    dforcing = None if dforcing is None else np.ascontiguousarray(dforcing, np.float64).reshape(ndir, total)
+    J = np.zeros(1)
+    dJ = np.zeros(max(ndir, 1))
+    uN = np.zeros(total)
+    rc = tangent_lib().tangent_bt_objective(len(nx), _ip(nx), _ip(ny), _ip(nz), _ip(nbr), dt, gx, gy, gz, xz, yz,
+                                            _dp(u0), _dp(forcing), _dp(u_target), nsteps, ndir,
+                                            _dp(du0) if du0 is not None else None,
+                                            _dp(dforcing) if dforcing is not None else None, _dp(J), _dp(dJ), _dp(uN))
+    assert rc == 0, rc
+    return float(J[0]), dJ[:ndir], uN
 
 
 def lib():
@@ -93,6 +139,10 @@ class Oracle:
     def phase(self, phase, zone=0):
         rc = lib().oracle_phase(self._h, phase, zone)
         assert rc == 0, rc
+
+    def get_all(self, which):
+        """One field of every zone, flat dense (zones back to back)."""
+        return np.concatenate([self.get(which, z).reshape(-1) for z in range(self.nzones)])
 
     def get(self, which, zone):
         z = zone
