@@ -110,4 +110,52 @@ download!(p::Problem, zone::Integer, field, a) =
     check(p, ccall((:npbmz_download, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
                    p.handle, zone - 1, field, LAYOUT_REF, parent(a)), "npbmz_download")
 
+# ---- all zones at once, dense layout (zone z: [5][nz][ny][nx] row-major, i.e. a
+# Julia Array{Float64}(undef, nx, ny, nz, 5) per zone, zones back to back) ----
+upload_all!(p::Problem, field, x::Vector{Float64}) =
+    check(p, ccall((:npbmz_upload, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
+                   p.handle, -1, field, LAYOUT_DENSE, x), "npbmz_upload")
+
+function download_all(p::Problem, field, n::Integer)
+    x = Vector{Float64}(undef, n)
+    check(p, ccall((:npbmz_download, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
+                   p.handle, -1, field, LAYOUT_DENSE, x), "npbmz_download")
+    return x
+end
+
+"""
+    adjoint(p, nsteps, u_target; checkpoint_every = 10) -> (J, dJ/dforcing, dJ/du0)
+
+Discrete adjoint of `nsteps` BT-MZ steps from the handle's current u and
+forcing for J = 1/2 sum (u_N - u_target)^2 over every stored point
+(npbmz_adjoint).  Dense all-zone vectors; u is left as it was.
+"""
+function adjoint(p::Problem, nsteps::Integer, u_target::Vector{Float64}; checkpoint_every::Integer = 10)
+    n = length(u_target)
+    J = Ref{Cdouble}(0.0)
+    gf = Vector{Float64}(undef, n)
+    gu = Vector{Float64}(undef, n)
+    check(p, ccall((:npbmz_adjoint, libnpbmz), Cint,
+                   (Ptr{Cvoid}, Cint, Cint, Ptr{Cdouble}, Ref{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                   p.handle, nsteps, checkpoint_every, u_target, J, gf, gu), "npbmz_adjoint")
+    return J[], gf, gu
+end
+
+"""
+    terminal_objective(p, forcing, u0, u_target, nsteps) -> J
+
+J = 1/2 sum (u_N - u_target)^2 after `nsteps` steps of exch_qbc + adi from
+(u0, forcing), all dense all-zone vectors.  Differentiable through the rrule
+in NPBAppsGPUChainRules.jl (the hand-written discrete adjoint on the GPU).
+"""
+function terminal_objective(p::Problem, forcing::Vector{Float64}, u0::Vector{Float64}, u_target::Vector{Float64},
+                            nsteps::Integer)
+    upload_all!(p, FORCING, forcing)
+    upload_all!(p, U, u0)
+    step!(p, nsteps)
+    a = download_all(p, U, length(u0)) .- u_target
+    upload_all!(p, U, u0)
+    return 0.5 * sum(abs2, a)
+end
+
 end # module

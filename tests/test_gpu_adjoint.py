@@ -218,3 +218,22 @@ def geom_class_sp():
     niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES["SP"]["S"]
     nx, ny, nz, nbr = npbmz.zone_setup(npbmz.SP, gx, gy, gz, xz, yz, ratio)
     return npbmz.Geometry(npbmz.SP, nx, ny, nz, nbr, gx, gy, gz, xz, yz), dt, niter
+
+
+def test_torch_autograd_function(config3):
+    """TerminalObjective (the torch.autograd counterpart of the Julia rrule)
+    returns the adjoint's J and gradients."""
+    torch = pytest.importorskip("torch")
+    from npbmz.autograd import terminal_objective
+
+    p, target, nsteps = config3
+    u0 = p.flatten(p.download_all(npbmz.U))
+    f0 = p.flatten(p.download_all(npbmz.FORCING))
+    J0, gf, gu = p.adjoint(nsteps, target, checkpoint_every=10)
+    f = torch.tensor(f0, requires_grad=True)
+    u = torch.tensor(u0, requires_grad=True)
+    J = terminal_objective(p, f, u, torch.tensor(p.flatten(target)), nsteps)
+    (2.0 * J).backward()
+    assert float(J) == J0
+    np.testing.assert_array_equal(f.grad.numpy(), 2.0 * p.flatten(gf))
+    np.testing.assert_array_equal(u.grad.numpy(), 2.0 * p.flatten(gu))
