@@ -65,6 +65,35 @@ Consts make_consts(double dt, int gx, int gy, int gz, int xz, int yz) {
   return k;
 }
 
+// Weights of the linear 5-point stencil of compute_rhs per direction and
+// position class (see LinWeights): the second difference d*t1*(1, -2, 1) of
+// x/y/z plus -dssp times the sum of the reference's dissipation stencils that
+// apply at that position (src/BT/rhs.jl:124-160 and its eta/zeta copies).
+// False when the d*t1 factors differ between variables of a direction.
+bool make_lin_weights(const Consts& k, LinWeights& lw) {
+  const double a[3][5] = {{k.dx1tx1, k.dx2tx1, k.dx3tx1, k.dx4tx1, k.dx5tx1},
+                          {k.dy1ty1, k.dy2ty1, k.dy3ty1, k.dy4ty1, k.dy5ty1},
+                          {k.dz1tz1, k.dz2tz1, k.dz3tz1, k.dz4tz1, k.dz5tz1}};
+  static const int stencil[5][5] = {{0, 0, 5, -4, 1},    // q == 1
+                                    {0, -4, 6, -4, 1},   // q == 2
+                                    {1, -4, 6, -4, 1},   // 3 <= q <= n-4
+                                    {1, -4, 6, -4, 0},   // q == n-3
+                                    {1, -4, 5, 0, 0}};   // q == n-2
+  static const double second[5] = {0.0, 1.0, -2.0, 1.0, 0.0};
+  for (int d = 0; d < 3; ++d) {
+    for (int m = 1; m < 5; ++m)
+      if (a[d][m] != a[d][0]) return false;
+    for (int c = 0; c < 32; ++c)
+      for (int o = 0; o < 5; ++o) {
+        int wsum = 0;
+        for (int b = 0; b < 5; ++b)
+          if (c >> b & 1) wsum += stencil[b][o];
+        lw.w[d][c][o] = a[d][0] * second[o] - k.dssp * (double)wsum;
+      }
+  }
+  return true;
+}
+
 // A contiguous slice of a work list: items [lo, hi) belong to one zone.
 struct Range {
   int lo = 0, hi = 0;
@@ -89,6 +118,8 @@ struct npbmz_handle {
   double* uex = nullptr;
   double* xw = nullptr;      // first-pass line solution of the refined mixed solve
   float* primf = nullptr;    // FP32 state copies for the mixed line solves
+  double* flux = nullptr;    // compute_rhs point functions (FMA build)
+  LinWeights lw;             // compute_rhs linear stencil weights (FMA build)
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
   double* part_rhs = nullptr;
@@ -170,6 +201,7 @@ Fields fields(const npbmz_t* h) {
   F.zones = h->zones_d;
   F.NP = h->NP;
   F.primf = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE) ? h->primf : nullptr;
+  F.flux = (h->flags & NPBMZ_EXACT) ? nullptr : h->flux;
   return F;
 }
 
@@ -291,7 +323,7 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
   int lo = 0, hi = h->nwint;
   if (zone >= 0) { lo = h->int_range[zone].lo; hi = h->int_range[zone].hi; }
   if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
-  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
+  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->lw);
   CKL(h);
   return 0;
 }
@@ -864,6 +896,8 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   rc |= dalloc(h, &h->uex, 5 * (size_t)h->NP);
   if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
   if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? (int)PF_COUNT : (int)PS_COUNT) * h->NP);
+  if (!(variant_flags & NPBMZ_EXACT) && make_lin_weights(h->K, h->lw))
+    rc |= dalloc(h, &h->flux, (size_t)PX_COUNT * h->NP);
   if (!rc) {
     if (cudaMalloc(&h->scratch, std::max<size_t>(h->scratch_bytes, 16)) != cudaSuccess) rc = fail(h, "scratch alloc failed");
     else h->device_bytes += (int64_t)h->scratch_bytes;
@@ -1123,7 +1157,7 @@ int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->scratch, h->part_rhs,
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->scratch, h->part_rhs,
                   h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wint_d, h->zblk_int_d,
                   h->wline_d[0], h->wline_d[1],
                   h->wline_d[2]};

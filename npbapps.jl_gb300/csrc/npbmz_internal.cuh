@@ -53,6 +53,19 @@ enum { PF_RHOI = 0, PF_QS, PF_U2, PF_U3, PF_U4, PF_U5, PF_HI_COUNT, PF_COUNT = 2
 // SP: FP32 copies of 1/rho, the three velocities and the speed of sound.
 enum { PS_RHOI = 0, PS_US, PS_VS, PS_WS, PS_SPEED, PS_COUNT };
 
+// Point functions of compute_rhs written by the primitive kernel of the FMA
+// build (one value per point, shared by both neighbours that difference it):
+// the off-diagonal momentum fluxes (u2 u3 / u1 = u3 us = u2 vs, ...), the
+// normal momentum fluxes with the pressure term, the energy fluxes and the
+// viscous energy terms of each direction.
+enum {
+  PX_UV = 0, PX_UW, PX_VW,   // u2*u3/u1, u2*u4/u1, u3*u4/u1
+  PX_XX, PX_YY, PX_ZZ,       // u2*us + c2*(u5 - square), u3*vs + ..., u4*ws + ...
+  PX_EX, PX_EY, PX_EZ,       // (c1*u5 - c2*square) * us / vs / ws
+  PX_WX, PX_WY, PX_WZ,       // con3*qs + con4*vel^2 + con5*u5/u1 with the x / y / z constants
+  PX_COUNT
+};
+
 struct Fields {
   double* u;        // [5][NP]
   double* rhs;      // [5][NP]
@@ -62,6 +75,18 @@ struct Fields {
   const ZoneDev* zones;
   int64_t NP;
   float* primf;     // [PF_COUNT][NP] or null
+  double* flux = nullptr;  // [PX_COUNT][NP] or null (FMA build's compute_rhs)
+};
+
+// The linear part of compute_rhs along one direction -- the second
+// difference d*t1*(u[q-1] - 2u[q] + u[q+1]) of each variable and the
+// fourth-order dissipation -- as one 5-point stencil whose weights depend on
+// the position class of q (bit 0: q == 1, 1: q == 2, 2: 3 <= q <= n-4,
+// 3: q == n-3, 4: q == n-2; several bits when the reference's stencils
+// overlap on a short axis).  Valid when the d*t1 factor is the same for the
+// five variables of a direction, as set_constants makes it.
+struct LinWeights {
+  double w[3][32][5];
 };
 
 // Lines per sweep direction of a zone (interior transverse indices only).

@@ -11,7 +11,7 @@ namespace npbmz {
   namespace NS {                                                                                                     \
   void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s);                                   \
   void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork,                 \
-                  double* partials, cudaStream_t s);                                                                 \
+                  double* partials, cudaStream_t s, const LinWeights* lw = nullptr);                                 \
   void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork,       \
                     int tpb, void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s);                     \
   void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s);                                     \

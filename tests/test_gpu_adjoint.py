@@ -19,10 +19,14 @@ config 3 (max relative error over the 16 directions at h = 1e-6):
   u_0, entries of unit RMS (absolute h; rho ~ 800 and rho E ~ 6e4 in the
       seeded state): 6.4e-7;  scaled by each variable's RMS: 1.1e-4
       (curvature);
-  forcing, scaled by each variable's RMS: 7.2e-7;  unit RMS: 3.6e-6
-      (rounding: the forcing enters through dt).
-So u_0 directions have unit-RMS entries and forcing directions are scaled
-per variable.  The agreement improves to ~1e-8 at the best h of each.
+  forcing, scaled by each variable's RMS: 7.2e-7 .. 1.2e-6 (depending on
+      the rounding of the forward kernels);  unit RMS: 3.6e-6 (rounding).
+The forcing moves u only through dt * forcing (dt = 8e-4, forcing RMS ~ 10
+against u RMS ~ 1e3), so a relative forcing perturbation of 1e-6 changes u_50
+by ~1e-10 relative and its difference quotient sits on the rounding floor of
+the forward run.  So u_0 directions have unit-RMS entries at h = 1e-6, and
+forcing directions are scaled per variable at h = 1e-5 (worst of 16: 4.6e-8;
+J is nearly linear in the forcing, so the O(h^2) term stays below 1e-9).
 
 The gradient is also checked against forward-mode dual numbers pushed
 through the CPU oracle's BT step (oracle/npbmz_tangent.cpp, the stand-in for
@@ -135,10 +139,11 @@ def config3():
     return p, target, nsteps
 
 
-@pytest.mark.parametrize("field", [npbmz.FORCING, npbmz.U], ids=["forcing", "u0"])
-def test_config3_adjoint_matches_central_differences(config3, field):
+@pytest.mark.parametrize("field,h", [(npbmz.FORCING, 1e-5), (npbmz.U, 1e-6)], ids=["forcing", "u0"])
+def test_config3_adjoint_matches_central_differences(config3, field, h):
     p, target, nsteps = config3
-    J, grad, errs = fd_check(p, target, nsteps, 10, field, seed=77)
+    J, grad, errs = fd_check(p, target, nsteps, 10, field, seed=77, h=h)
+    print(f"field {field} h {h:.0e}: worst {max(errs):.2e}, median {np.median(errs):.2e}")
     assert J > 0.0 and np.all(np.isfinite(grad))
     assert max(errs) <= ADJ_REL, f"max rel err {max(errs):.3e} over {NDIR} directions: {errs}"
 

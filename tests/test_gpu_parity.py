@@ -98,6 +98,27 @@ def test_each_phase_is_bit_exact(oracle_mod, gname):
         compare(p, o, npbmz.U, EXACT_REL, [z])
 
 
+@pytest.mark.parametrize("gname", list(GEOMS))
+def test_each_phase_fast_path_within_1e12(oracle_mod, gname):
+    """The FMA build's phases (compute_rhs from the point-function planes and
+    the merged linear stencil, the FMA sweeps) against the oracle, one phase
+    at a time from identical inputs."""
+    geom, dt, _ = GEOMS[gname]()
+    p, o = make_pair(oracle_mod, geom, dt, 0, seeded(geom))
+    p.phase(npbmz.PHASE_EXCH)
+    o.phase(5)
+    for z in range(geom.nzones):
+        p.phase(npbmz.PHASE_RHS, z)
+        o.phase(0, z)
+        compare(p, o, npbmz.RHS, FAST_REL, [z])
+        p.upload(npbmz.RHS, z, o.get(npbmz.RHS, z))
+        for ph in (npbmz.PHASE_XSOLVE, npbmz.PHASE_YSOLVE, npbmz.PHASE_ZSOLVE):
+            p.phase(ph, z)
+            o.phase(ph, z)
+            compare(p, o, npbmz.RHS, FAST_REL, [z])
+            p.upload(npbmz.RHS, z, o.get(npbmz.RHS, z))
+
+
 @pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 20), ("sp_classS", 40)])
 def test_steps_exact_path_bit_exact(oracle_mod, gname, nsteps):
     geom, dt, _ = GEOMS[gname]()
