@@ -119,6 +119,10 @@ struct npbmz_handle {
   double* xw = nullptr;      // first-pass line solution of the refined mixed solve
   float* primf = nullptr;    // FP32 state copies for the mixed line solves
   double* flux = nullptr;    // compute_rhs point functions (FMA build)
+  float* rdf = nullptr;      // double-float rhs handed between the refined FP32 BT sweeps of a step
+  float* pfx = nullptr;      // x-line-major copies for the refined FP32 BT x sweep (see Fields)
+  float* rdx = nullptr;
+  float* x0x = nullptr;
   LinWeights lw;             // compute_rhs linear stencil weights (FMA build)
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -202,6 +206,11 @@ Fields fields(const npbmz_t* h) {
   F.NP = h->NP;
   F.primf = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE) ? h->primf : nullptr;
   F.flux = (h->flags & NPBMZ_EXACT) ? nullptr : h->flux;
+  F.rdf = h->rdf;
+  F.pfx = h->pfx;
+  F.rdx = h->rdx;
+  F.x0x = h->x0x;
+  F.nlx = h->nlines[0];
   return F;
 }
 
@@ -273,6 +282,14 @@ int build_work_lists(npbmz_t* h) {
 int flush_boundary(npbmz_t* h) {
   if (!h->bnd_dirty) return 0;
   CK(h, cudaMemcpyAsync(h->rhs, h->forcing, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  if (h->rdf) {
+    fast::launch_split_df(h->forcing, h->rdf, h->NP, h->stream);
+    CKL(h);
+  }
+  if (h->rdx) {
+    fast::launch_xline_ends(fields(h), h->wline_d[0], h->nwline[0], h->tpb_line[0], h->stream);
+    CKL(h);
+  }
   h->bnd_dirty = false;
   return 0;
 }
@@ -311,8 +328,15 @@ int phase_prim(npbmz_t* h, int zone) {
     hi = lo + (int64_t)h->zh[zone].nx * h->zh[zone].ny * h->zh[zone].nz;
   }
   const bool sp = h->kind == NPBMZ_SP;
-  if (use_exact(h)) exact::launch_prim(sp, F, h->K, lo, hi, h->stream);
-  else fast::launch_prim(sp, F, h->K, lo, hi, h->stream);
+  if (use_exact(h)) {
+    exact::launch_prim(sp, F, h->K, lo, hi, h->stream);
+  } else {
+    // over the point work list: the zone of each point is known, so the
+    // x-line-major state copy can be written too
+    int wlo = 0, whi = h->nwpts;
+    if (zone >= 0) { wlo = h->pts_range[zone].lo; whi = h->pts_range[zone].hi; }
+    fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream);
+  }
   CKL(h);
   return 0;
 }
@@ -328,7 +352,10 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
   return 0;
 }
 
-int phase_solve(npbmz_t* h, int dir, int zone, int add_u) {
+// fused: part of a whole step (run_adi), where the refined FP32 BT sweeps
+// hand their results on as double-float; otherwise each sweep reads and
+// writes rhs in FP64 (single phases, the adjoint's recomputation).
+int phase_solve(npbmz_t* h, int dir, int zone, int add_u, bool fused = false) {
   const Fields F = fields(h);
   int lo = 0, hi = h->nwline[dir];
   if (zone >= 0) { lo = h->line_range[dir][zone].lo; hi = h->line_range[dir][zone].hi; }
@@ -337,7 +364,7 @@ int phase_solve(npbmz_t* h, int dir, int zone, int add_u) {
     exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch,
                         h->nlines[dir], add_u, nullptr, h->stream);
   else
-    fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : ((h->flags & NPBMZ_REFINE_FP64) ? 3 : 2)), dir, F, h->K,
+    fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : ((h->flags & NPBMZ_REFINE_FP64) ? 3 : (fused && h->rdf ? 4 : 2))), dir, F, h->K,
                        h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch, h->nlines[dir], add_u, h->xw,
                        h->stream);
   CKL(h);
@@ -371,9 +398,9 @@ int run_adi(npbmz_t* h, int zone, bool norm) {
   }
   if (phase_prim(h, zone)) return -1;
   if (phase_rhs(h, zone, sp, norm)) return -1;
-  if (phase_solve(h, 0, zone, 0)) return -1;
-  if (phase_solve(h, 1, zone, 0)) return -1;
-  if (phase_solve(h, 2, zone, 1)) return -1;  // add fused into the z sweep
+  if (phase_solve(h, 0, zone, 0, true)) return -1;
+  if (phase_solve(h, 1, zone, 0, true)) return -1;
+  if (phase_solve(h, 2, zone, 1, true)) return -1;  // add fused into the z sweep
   return 0;
 }
 
@@ -896,14 +923,25 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   rc |= dalloc(h, &h->uex, 5 * (size_t)h->NP);
   if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
   if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? (int)PF_COUNT : (int)PS_COUNT) * h->NP);
-  if (!(variant_flags & NPBMZ_EXACT) && make_lin_weights(h->K, h->lw))
+  if (!(variant_flags & NPBMZ_EXACT) && make_lin_weights(h->K, h->lw)) {
     rc |= dalloc(h, &h->flux, (size_t)PX_COUNT * h->NP);
+    if (kind == NPBMZ_BT && refined && !(variant_flags & NPBMZ_REFINE_FP64)) {
+      rc |= dalloc(h, &h->rdf, 10 * (size_t)h->NP);
+      int maxnx = 0;
+      for (int z = 0; z < nzones; ++z) maxnx = std::max(maxnx, nx[z]);
+      const size_t xpts = (size_t)maxnx * (size_t)std::max<int64_t>(lines[0], 1);
+      rc |= dalloc(h, &h->pfx, (size_t)PF_COUNT * xpts);
+      rc |= dalloc(h, &h->rdx, 10 * xpts);
+      rc |= dalloc(h, &h->x0x, 5 * xpts);
+    }
+  }
   if (!rc) {
     if (cudaMalloc(&h->scratch, std::max<size_t>(h->scratch_bytes, 16)) != cudaSuccess) rc = fail(h, "scratch alloc failed");
     else h->device_bytes += (int64_t)h->scratch_bytes;
   }
   if (!rc && cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(ZoneDev), cudaMemcpyHostToDevice) != cudaSuccess) rc = -1;
   if (!rc && cudaMemcpy(h->nbr_d, nbr, 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) rc = -1;
+  if (!rc && h->rdf && fast::configure_kernels()) rc = fail(h, "cudaFuncSetAttribute failed: %s", cudaGetErrorString(cudaGetLastError()));
   if (!rc) rc = build_work_lists(h);
   if (!rc) rc = build_line_lists(h);
   // staging offsets per layout and field
@@ -955,8 +993,8 @@ int npbmz_setup(npbmz_t* h, const double* ce) {
   launch_exact_rhs(F, h->K, ce, h->wpts_d, h->nwpts, h->forcing, h->stream);
   CKL(h);
   // rhs starts as the forcing (its boundary values are never rewritten)
-  CK(h, cudaMemcpyAsync(h->rhs, h->forcing, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-  h->bnd_dirty = false;
+  h->bnd_dirty = true;
+  if (flush_boundary(h)) return -1;
   CK(h, cudaStreamSynchronize(h->stream));
   return 0;
 }
@@ -1157,7 +1195,7 @@ int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->scratch, h->part_rhs,
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->part_rhs,
                   h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wint_d, h->zblk_int_d,
                   h->wline_d[0], h->wline_d[1],
                   h->wline_d[2]};

@@ -76,7 +76,23 @@ struct Fields {
   int64_t NP;
   float* primf;     // [PF_COUNT][NP] or null
   double* flux = nullptr;  // [PX_COUNT][NP] or null (FMA build's compute_rhs)
+  // [10][NP] double-float copy of rhs (planes 0..4 hi, 5..9 lo) that the
+  // refined FP32 BT sweeps of one step hand to each other, or null
+  float* rdf = nullptr;
+  // x-line-major copies for the refined FP32 BT x sweep, so that the lines of
+  // a warp (consecutive j, nx points apart in the zone layout) read adjacent
+  // words: element e of point i of x line g at [(i * E + e) * nlx + g]
+  float* pfx = nullptr;  // E = PF_COUNT: FP32 state hi / lo (primitive kernel)
+  float* rdx = nullptr;  // E = 10: double-float rhs (compute_rhs; line ends: the forcing)
+  float* x0x = nullptr;  // E = 5: first-pass solution
+  int64_t nlx = 0;       // x lines of all zones
 };
+
+// x line through interior point (j, k) of zone z (-1 when j or k is a face).
+__host__ __device__ inline int64_t xline_of(const ZoneDev& z, int j, int k) {
+  if (j < 1 || j > z.ny - 2 || k < 1 || k > z.nz - 2) return -1;
+  return z.lineoff[0] + (j - 1) + (int64_t)(k - 1) * (z.ny - 2);
+}
 
 // The linear part of compute_rhs along one direction -- the second
 // difference d*t1*(u[q-1] - 2u[q] + u[q+1]) of each variable and the

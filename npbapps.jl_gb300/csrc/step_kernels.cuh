@@ -25,10 +25,12 @@ namespace NPBMZ_NS {
 // Primitive variables (src/BT/rhs.jl:62-77, src/SP/rhs.jl:62-89), one thread
 // per point of the padded plane (padding points compute garbage nobody reads).
 // ============================================================================
+// xl: x line through the point and its position on it (FP32 BT sweeps of
+// the FMA build write the x-line-major state copy there), or xl < 0.
 template <bool SP>
-__global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, int64_t hi) {
+__device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int64_t p, int64_t xl, int xi) {
   const int64_t NP = F.NP;
-  for (int64_t p = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < hi; p += (int64_t)gridDim.x * blockDim.x) {
+  {
     const double u1 = F.u[p], u2 = F.u[NP + p], u3 = F.u[2 * NP + p], u4 = F.u[3 * NP + p];
     const double rho_inv = 1.0e0 / u1;
     const double square = 0.5e0 * (u2 * u2 + u3 * u3 + u4 * u4) * rho_inv;
@@ -56,8 +58,13 @@ __global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, in
 #pragma unroll
       for (int e = 0; e < PF_HI_COUNT; ++e) {
         const float hi = __double2float_rn(v[e]);
+        const float lo = __double2float_rn(v[e] - (double)hi);
         F.primf[e * NP + p] = hi;
-        F.primf[(PF_HI_COUNT + e) * NP + p] = __double2float_rn(v[e] - (double)hi);
+        F.primf[(PF_HI_COUNT + e) * NP + p] = lo;
+        if (F.pfx && xl >= 0) {
+          F.pfx[((int64_t)xi * PF_COUNT + e) * F.nlx + xl] = hi;
+          F.pfx[((int64_t)xi * PF_COUNT + PF_HI_COUNT + e) * F.nlx + xl] = lo;
+        }
       }
     }
 #if NPBMZ_HAS_FP32
@@ -85,6 +92,23 @@ __global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, in
     }
 #endif
   }
+}
+
+template <bool SP>
+__global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, int64_t hi) {
+  for (int64_t p = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < hi; p += (int64_t)gridDim.x * blockDim.x)
+    prim_point<SP>(F, K, p, -1, 0);
+}
+
+// Over the point work list (zone known): also the x-line-major state copy.
+template <bool SP>
+__global__ void __launch_bounds__(128) k_prim_w(Fields F, Consts K, const Work* __restrict__ work) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int q = w.first + threadIdx.x;
+  if (q >= Z.nx * Z.ny * Z.nz) return;
+  const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
+  prim_point<SP>(F, K, Z.off + q, xline_of(Z, j, k), i);
 }
 
 // ============================================================================
@@ -372,11 +396,60 @@ __global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, LinWeights
     }
 #pragma unroll
     for (int m = 0; m < 5; ++m) F.rhs[m * NP + p] = r[m];
+    if (F.rdx) {  // b of the x sweep, x-line-major
+      const int64_t xl = xline_of(Z, j, k);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const float hi = __double2float_rn(r[m]);
+        F.rdx[((int64_t)i * 10 + m) * F.nlx + xl] = hi;
+        F.rdx[((int64_t)i * 10 + 5 + m) * F.nlx + xl] = __double2float_rn(r[m] - (double)hi);
+      }
+    } else if (F.rdf) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const float hi = __double2float_rn(r[m]);
+        F.rdf[m * NP + p] = hi;
+        F.rdf[(5 + m) * NP + p] = __double2float_rn(r[m] - (double)hi);
+      }
+    }
   }
   if (NORM) {
     block_sum5(sq, red);
     if (threadIdx.x == 0)
       for (int m = 0; m < 5; ++m) partials[blockIdx.x * 5 + m] = sq[m];
+  }
+}
+
+// The two end points of every x line in the x-line-major double-float rhs
+// copy: the forcing, as rhs holds there (one thread per x line).
+__global__ void __launch_bounds__(128) k_xline_ends(Fields F, const Work* __restrict__ work) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, 0)) return;
+  int64_t base, st;
+  line_geometry(Z, 0, line, base, st);
+  const int64_t gl = Z.lineoff[0] + line;
+  const int ends[2] = {0, Z.nx - 1};
+#pragma unroll
+  for (int e = 0; e < 2; ++e)
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double v = F.forcing[m * F.NP + base + ends[e]];
+      const float hi = __double2float_rn(v);
+      F.rdx[((int64_t)ends[e] * 10 + m) * F.nlx + gl] = hi;
+      F.rdx[((int64_t)ends[e] * 10 + 5 + m) * F.nlx + gl] = __double2float_rn(v - (double)hi);
+    }
+}
+
+// dst (double-float planes 0..4 hi, 5..9 lo) <- src (5 FP64 planes)
+__global__ void __launch_bounds__(256) k_split_df(const double* __restrict__ src, float* __restrict__ dst, int64_t NP) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 5 * NP; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = t / NP, p = t - m * NP;
+    const double v = src[t];
+    const float hi = __double2float_rn(v);
+    dst[m * NP + p] = hi;
+    dst[(5 + m) * NP + p] = __double2float_rn(v - (double)hi);
   }
 }
 #endif  // NPBMZ_HAS_FP32
@@ -898,7 +971,8 @@ __device__ __forceinline__ void load_state_f64(const Fields& F, int64_t pt, doub
 
 // Pass 1: T x0 = b in FP32.  Loads of point p+2 and of b_{p+1} are issued one
 // step ahead so that they overlap the elimination of point p.
-template <int DIR>
+// IN_DF: b comes from the double-float planes F.rdf (hi part), not rhs.
+template <int DIR, bool IN_DF>
 __global__ void __launch_bounds__(128) k_bt_mixed_solve(Fields F, Consts K, const Work* __restrict__ work,
                                                         float* __restrict__ scr, int64_t nlt,
                                                         float* __restrict__ x0) {
@@ -912,17 +986,19 @@ __global__ void __launch_bounds__(128) k_bt_mixed_solve(Fields F, Consts K, cons
   const int64_t gl = Z.lineoff[DIR] + line;
   const int64_t NP = F.NP;
   const double* __restrict__ rhs = F.rhs;
+  const float* __restrict__ bdf = F.rdf;
+  auto bload = [&](int m, int64_t pt) -> float { return IN_DF ? bdf[m * NP + pt] : (float)rhs[m * NP + pt]; };
   BtF32Carry<DIR> c;
   float s0[6], s1[6];
   load_state_f32(F, base, s0);
   load_state_f32(F, base + st, s1);
 #pragma unroll
-  for (int m = 0; m < 5; ++m) c.rp[m] = (float)rhs[m * NP + base];
+  for (int m = 0; m < 5; ++m) c.rp[m] = bload(m, base);
   bt_f32_begin<DIR>(K, n, s0, s1, c);
   float sn[6], bn[5];
   load_state_f32(F, base + 2 * st, sn);
 #pragma unroll
-  for (int m = 0; m < 5; ++m) bn[m] = (float)rhs[m * NP + base + st];
+  for (int m = 0; m < 5; ++m) bn[m] = bload(m, base + st);
   for (int p = 1; p <= n - 2; ++p) {
     float r[5], s[6];
 #pragma unroll
@@ -932,13 +1008,13 @@ __global__ void __launch_bounds__(128) k_bt_mixed_solve(Fields F, Consts K, cons
     if (p + 1 <= n - 2) {  // prefetch for the next step
       load_state_f32(F, base + (int64_t)(p + 2) * st, sn);
 #pragma unroll
-      for (int m = 0; m < 5; ++m) bn[m] = (float)rhs[m * NP + base + (int64_t)(p + 1) * st];
+      for (int m = 0; m < 5; ++m) bn[m] = bload(m, base + (int64_t)(p + 1) * st);
     }
     bt_f32_step<DIR>(K, p, n, false, r, s, c, scr, nlt, gl);
   }
   float rn[5];
 #pragma unroll
-  for (int m = 0; m < 5; ++m) rn[m] = (float)rhs[m * NP + base + (n - 1) * st];
+  for (int m = 0; m < 5; ++m) rn[m] = bload(m, base + (int64_t)(n - 1) * st);
   for (int p = n - 2; p >= 1; --p) {
     float r[5];
 #pragma unroll
@@ -1176,7 +1252,10 @@ __device__ __forceinline__ void load_state_df(const Fields& F, int64_t pt, df64 
 // Refinement pass with the residual in double-float.  Point q contributes,
 // with P_q = tmp2 F_q and Q_q = tmp1 (N_q + D x_q),
 //   -P_q - Q_q to row q+1,   x_q + 2 Q_q to row q,   P_q - Q_q to row q-1.
-template <int DIR>
+// IN_DF: b and the line's end values come from the double-float planes
+// F.rdf; OUT_DF: x goes back to F.rdf as the exact double-float sum x0 + d
+// instead of to rhs in FP64 (the next sweep of the same step reads it so).
+template <int DIR, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const Work* __restrict__ work,
                                                       float* __restrict__ scr, int64_t nlt, int add_u,
                                                       const float* __restrict__ x0f) {
@@ -1190,6 +1269,7 @@ __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const 
   const int64_t gl = Z.lineoff[DIR] + line;
   const int64_t NP = F.NP;
   double* __restrict__ rhs = F.rhs;
+  float* __restrict__ bdf = F.rdf;
 
   const df64 t1 = df_from(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
   const df64 t2 = df_from(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
@@ -1206,7 +1286,7 @@ __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const 
     const int64_t pt = base + (int64_t)q * st;
     if (q == 0 || q == n - 1) {
 #pragma unroll
-      for (int m = 0; m < 5; ++m) x[m] = df_from(rhs[m * NP + pt]);
+      for (int m = 0; m < 5; ++m) x[m] = IN_DF ? df64{bdf[m * NP + pt], bdf[(5 + m) * NP + pt]} : df_from(rhs[m * NP + pt]);
     } else {
 #pragma unroll
       for (int m = 0; m < 5; ++m) x[m] = {x0f[m * NP + pt], 0.f};
@@ -1247,30 +1327,47 @@ __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const 
   // bt_f32_begin takes ri, u2, u3, u4, u5, q in that order (as sq)
   bt_f32_begin<DIR>(K, n, s0, s1, c);
   df64 xn[5], sn[6];
-  double bn[5];
+  // b of the next point: double-float planes (IN_DF) or FP64 rhs
+  df64 bn[5];
+  double bn64[5];
+  auto load_b = [&](int64_t pt) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (IN_DF) bn[m] = df64{bdf[m * NP + pt], bdf[(5 + m) * NP + pt]};
+      else bn64[m] = rhs[m * NP + pt];
+    }
+  };
   load_x(2, xn);
   load_state_df(F, base + 2 * st, sn);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) bn[m] = rhs[m * NP + base + st];
+  load_b(base + st);
 
   for (int p = 1; p <= n - 2; ++p) {
     double b[5];
+    df64 bd[5];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) { xq[m] = xn[m]; b[m] = bn[m]; }
+    for (int m = 0; m < 5; ++m) {
+      xq[m] = xn[m];
+      if (IN_DF) bd[m] = bn[m];
+      else b[m] = bn64[m];
+    }
 #pragma unroll
     for (int e = 0; e < 6; ++e) sq[e] = sn[e];
     if (p + 1 <= n - 2) {
       load_x(p + 2, xn);
       load_state_df(F, base + (int64_t)(p + 2) * st, sn);
-#pragma unroll
-      for (int m = 0; m < 5; ++m) bn[m] = rhs[m * NP + base + (int64_t)(p + 1) * st];
+      load_b(base + (int64_t)(p + 1) * st);
     }
     pq(sq, xq, P, Q);
     float r[5], s[6];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
       const df64 tx = df_add(acc_c[m], df_sub(P[m], Q[m]));
-      r[m] = __double2float_rn((b[m] - (double)tx.hi) - (double)tx.lo);
+      if (IN_DF) {
+        const df64 rr = df_sub(bd[m], tx);
+        r[m] = rr.hi + rr.lo;
+      } else {
+        r[m] = __double2float_rn((b[m] - (double)tx.hi) - (double)tx.lo);
+      }
       acc_c[m] = df_add(acc_n[m], df_add(xq[m], df_scale2(Q[m])));
       acc_n[m] = df_neg(df_add(P[m], Q[m]));
     }
@@ -1290,13 +1387,353 @@ __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const 
       for (int cc = 0; cc < 5; ++cc) d[m] -= scr[((int64_t)p * 30 + m * 5 + cc) * nlt + gl] * dn[cc];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      const double v = (double)x0f[m * NP + pt] + (double)d[m];
-      rhs[m * NP + pt] = v;
-      if (add_u) F.u[m * NP + pt] += v;
+      if (OUT_DF) {
+        const df64 v = df_two_sum(x0f[m * NP + pt], d[m]);
+        bdf[m * NP + pt] = v.hi;
+        bdf[(5 + m) * NP + pt] = v.lo;
+      } else {
+        const double v = (double)x0f[m * NP + pt] + (double)d[m];
+        rhs[m * NP + pt] = v;
+        if (add_u) F.u[m * NP + pt] += v;
+      }
       dn[m] = d[m];
     }
   }
 }
+
+#if NPBMZ_HAS_FP32
+// ============================================================================
+// Software-pipelined refined FP32 BT sweep of a fused step (mode 4).  The
+// two passes above wait on memory once per point: a line advances one point
+// per DRAM round trip, and with 8-12 resident warps per SM nothing hides it.
+// Here each thread streams its own line's data PIPE points ahead with
+// cp.async into a ring of PIPE slots in shared memory (word e of slot s of
+// thread t at ring[(s * W + e) * T + t]: a warp's copies land in consecutive
+// banks), in the forward elimination and in the back substitution alike.
+// The arithmetic is that of k_bt_mixed_solve<DIR, true> and
+// k_bt_refine_df<DIR, true, OUT_DF>.
+// ============================================================================
+constexpr int PIPE = 4;
+
+__device__ __forceinline__ void cpa4(float* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa8(double* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int PL_MIXED_W = 30;   // words per slot, first pass
+constexpr int PL_REFINE_W = 35;  // words per slot, refinement pass
+
+// Dynamic shared memory of the pipelined kernels for tpb threads.
+__host__ __device__ constexpr size_t pl_mixed_smem(int tpb) { return (size_t)PIPE * PL_MIXED_W * tpb * sizeof(float); }
+__host__ __device__ constexpr size_t pl_refine_smem(int tpb, bool out_df) {
+  return (size_t)PIPE * 5 * tpb * sizeof(double) * (out_df ? 0 : 1) + (size_t)PIPE * PL_REFINE_W * tpb * sizeof(float);
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) k_bt_mixed_pl(Fields F, Consts K, const Work* __restrict__ work,
+                                                     float* __restrict__ scr, int64_t nlt, float* __restrict__ x0) {
+  extern __shared__ __align__(16) unsigned char pl_smem[];
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  const int T = blockDim.x;
+  float* my = reinterpret_cast<float*>(pl_smem) + threadIdx.x;
+  auto S = [&](int slot, int e) -> float* { return my + (slot * PL_MIXED_W + e) * T; };
+  const int order[6] = {PF_RHOI, PF_U2, PF_U3, PF_U4, PF_U5, PF_QS};
+  // the x sweep reads its x-line-major copies, y and z the zone layout
+  auto st_at = [&](int q, int plane) -> const float* {
+    return DIR == 0 ? F.pfx + ((int64_t)q * PF_COUNT + plane) * F.nlx + gl : F.primf + plane * NP + base + (int64_t)q * st;
+  };
+  auto b_at = [&](int q, int e) -> const float* {
+    return DIR == 0 ? F.rdx + ((int64_t)q * 10 + e) * F.nlx + gl : F.rdf + e * NP + base + (int64_t)q * st;
+  };
+  auto x0_at = [&](int q, int m) -> float* {
+    return DIR == 0 ? F.x0x + ((int64_t)q * 5 + m) * F.nlx + gl : x0 + m * NP + base + (int64_t)q * st;
+  };
+
+  // forward step p (1..n-2) consumes b_p and the state at p+1
+  auto issue_fwd = [&](int p) {
+    if (p <= n - 2) {
+      const int slot = p % PIPE;
+#pragma unroll
+      for (int e = 0; e < 6; ++e) cpa4(S(slot, e), st_at(p + 1, order[e]));
+#pragma unroll
+      for (int m = 0; m < 5; ++m) cpa4(S(slot, 6 + m), b_at(p, m));
+    }
+    cpa_commit();
+  };
+  BtF32Carry<DIR> c;
+  {
+    float s0[6], s1[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      s0[e] = *st_at(0, order[e]);
+      s1[e] = *st_at(1, order[e]);
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) c.rp[m] = *b_at(0, m);
+    bt_f32_begin<DIR>(K, n, s0, s1, c);
+  }
+#pragma unroll
+  for (int q = 1; q < PIPE; ++q) issue_fwd(q);
+  for (int p = 1; p <= n - 2; ++p) {
+    issue_fwd(p + PIPE - 1);
+    cpa_wait<PIPE - 1>();
+    const int slot = p % PIPE;
+    float r[5], s[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s[e] = *S(slot, e);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) r[m] = *S(slot, 6 + m);
+    bt_f32_step<DIR>(K, p, n, false, r, s, c, scr, nlt, gl);
+  }
+  cpa_wait<0>();
+  // back substitution: step p (n-2 .. 1) consumes C'_p and r'_p
+  auto issue_bwd = [&](int p) {
+    if (p >= 1) {
+      const int slot = (n - 2 - p) % PIPE;
+#pragma unroll
+      for (int e = 0; e < 30; ++e) cpa4(S(slot, e), scr + ((int64_t)p * 30 + e) * nlt + gl);
+    }
+    cpa_commit();
+  };
+  float rn[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) rn[m] = *b_at(n - 1, m);
+#pragma unroll
+  for (int q = 0; q < PIPE - 1; ++q) issue_bwd(n - 2 - q);
+  for (int p = n - 2; p >= 1; --p) {
+    issue_bwd(p - (PIPE - 1));
+    cpa_wait<PIPE - 1>();
+    const int slot = (n - 2 - p) % PIPE;
+    float r[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      float t = *S(slot, 25 + m);
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc) t -= *S(slot, m * 5 + cc) * rn[cc];
+      r[m] = t;
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      *x0_at(p, m) = r[m];
+      rn[m] = r[m];
+    }
+  }
+  cpa_wait<0>();
+}
+
+template <int DIR, bool OUT_DF>
+__global__ void __launch_bounds__(128) k_bt_refine_pl(Fields F, Consts K, const Work* __restrict__ work,
+                                                      float* __restrict__ scr, int64_t nlt, int add_u,
+                                                      const float* __restrict__ x0f) {
+  extern __shared__ __align__(16) unsigned char pl_smem[];
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  const int T = blockDim.x;
+  // the FP64 ring (u, z sweep only) first: 8-byte words
+  double* umy = reinterpret_cast<double*>(pl_smem) + threadIdx.x;
+  float* my = reinterpret_cast<float*>(pl_smem + (OUT_DF ? 0 : (size_t)PIPE * 5 * T * sizeof(double))) + threadIdx.x;
+  auto S = [&](int slot, int e) -> float* { return my + (slot * PL_REFINE_W + e) * T; };
+  auto SU = [&](int slot, int m) -> double* { return umy + (slot * 5 + m) * T; };
+  double* __restrict__ rhs = F.rhs;
+  float* __restrict__ bdf = F.rdf;
+  const int order[6] = {PF_RHOI, PF_U2, PF_U3, PF_U4, PF_U5, PF_QS};
+  // the x sweep reads its x-line-major copies, y and z the zone layout; the
+  // result always goes to the zone layout (the next sweep reads it there)
+  auto st_at = [&](int q, int plane) -> const float* {
+    return DIR == 0 ? F.pfx + ((int64_t)q * PF_COUNT + plane) * F.nlx + gl : F.primf + plane * NP + base + (int64_t)q * st;
+  };
+  auto b_at = [&](int q, int e) -> const float* {
+    return DIR == 0 ? F.rdx + ((int64_t)q * 10 + e) * F.nlx + gl : bdf + e * NP + base + (int64_t)q * st;
+  };
+  auto x0_at = [&](int q, int m) -> const float* {
+    return DIR == 0 ? F.x0x + ((int64_t)q * 5 + m) * F.nlx + gl : x0f + m * NP + base + (int64_t)q * st;
+  };
+
+  const df64 t1 = df_from(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
+  const df64 t2 = df_from(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  df64 D[5];
+  if (DIR == 0) { D[0] = df_from(K.dx1); D[1] = df_from(K.dx2); D[2] = df_from(K.dx3); D[3] = df_from(K.dx4); D[4] = df_from(K.dx5); }
+  else if (DIR == 1) { D[0] = df_from(K.dy1); D[1] = df_from(K.dy2); D[2] = df_from(K.dy3); D[3] = df_from(K.dy4); D[4] = df_from(K.dy5); }
+  else { D[0] = df_from(K.dz1); D[1] = df_from(K.dz2); D[2] = df_from(K.dz3); D[3] = df_from(K.dz4); D[4] = df_from(K.dz5); }
+  const df64 c1 = df_from(K.c1), c2 = df_from(K.c2), two_m_c2 = df_from(2.0 - K.c2);
+  const double k43d = K.con43 * K.c3c4;
+  const df64 k43 = df_from(k43d), c3c4 = df_from(K.c3c4), c1345 = df_from(K.c1345);
+  const df64 k43m = df_from(k43d - K.c1345), c3c4m = df_from(K.c3c4 - K.c1345);
+
+  auto pq = [&](const df64 s[6], const df64 x[5], df64 P[5], df64 Q[5]) {
+    df64 Fq[5], Nq[5];
+    bt_jx_df<DIR>(c1, c2, two_m_c2, k43, c3c4, c1345, k43m, c3c4m, s, x, Fq, Nq);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      P[m] = df_mul(t2, Fq[m]);
+      Q[m] = df_mul(t1, df_add(Nq[m], df_mul(D[m], x[m])));
+    }
+  };
+  auto load_x = [&](int q, df64 x[5]) {  // direct loads (prologue)
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+      x[m] = (q == 0 || q == n - 1) ? df64{*b_at(q, m), *b_at(q, 5 + m)} : df64{*x0_at(q, m), 0.f};
+  };
+  auto load_sdf = [&](int q, df64 s6[6]) {
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s6[e] = df64{*st_at(q, order[e]), *st_at(q, PF_HI_COUNT + order[e])};
+  };
+  // forward step p (1..n-2) consumes x and the state at p+1 and b_p:
+  // words 0..9 x (5 x0 values, or hi/lo of the line's end value), 10..21
+  // state hi/lo, 22..31 b hi/lo
+  auto issue_fwd = [&](int p) {
+    if (p <= n - 2) {
+      const int slot = p % PIPE;
+      if (p + 1 == n - 1) {
+#pragma unroll
+        for (int e = 0; e < 10; ++e) cpa4(S(slot, e), b_at(p + 1, e));
+      } else {
+#pragma unroll
+        for (int m = 0; m < 5; ++m) cpa4(S(slot, m), x0_at(p + 1, m));
+      }
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        cpa4(S(slot, 10 + e), st_at(p + 1, order[e]));
+        cpa4(S(slot, 16 + e), st_at(p + 1, PF_HI_COUNT + order[e]));
+      }
+#pragma unroll
+      for (int e = 0; e < 10; ++e) cpa4(S(slot, 22 + e), b_at(p, e));
+    }
+    cpa_commit();
+  };
+
+  df64 acc_c[5], acc_n[5], xq[5], sq[6], P[5], Q[5];
+  BtF32Carry<DIR> c;
+  {
+    float s0[6], s1[6];
+    load_x(0, xq);
+    load_sdf(0, sq);
+    pq(sq, xq, P, Q);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) acc_c[m] = df_neg(df_add(P[m], Q[m]));
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s0[e] = sq[e].hi;
+    load_x(1, xq);
+    load_sdf(1, sq);
+    pq(sq, xq, P, Q);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      acc_c[m] = df_add(acc_c[m], df_add(xq[m], df_scale2(Q[m])));
+      acc_n[m] = df_neg(df_add(P[m], Q[m]));
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s1[e] = sq[e].hi;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) c.rp[m] = 0.f;
+    bt_f32_begin<DIR>(K, n, s0, s1, c);
+  }
+#pragma unroll
+  for (int q = 1; q < PIPE; ++q) issue_fwd(q);
+  for (int p = 1; p <= n - 2; ++p) {
+    issue_fwd(p + PIPE - 1);
+    cpa_wait<PIPE - 1>();
+    const int slot = p % PIPE;
+    df64 bd[5];
+    if (p + 1 == n - 1) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) xq[m] = df64{*S(slot, m), *S(slot, 5 + m)};
+    } else {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) xq[m] = df64{*S(slot, m), 0.f};
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) sq[e] = df64{*S(slot, 10 + e), *S(slot, 16 + e)};
+#pragma unroll
+    for (int m = 0; m < 5; ++m) bd[m] = df64{*S(slot, 22 + m), *S(slot, 27 + m)};
+    pq(sq, xq, P, Q);
+    float r[5], s[6];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const df64 tx = df_add(acc_c[m], df_sub(P[m], Q[m]));
+      const df64 rr = df_sub(bd[m], tx);
+      r[m] = rr.hi + rr.lo;
+      acc_c[m] = df_add(acc_n[m], df_add(xq[m], df_scale2(Q[m])));
+      acc_n[m] = df_neg(df_add(P[m], Q[m]));
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) s[e] = sq[e].hi;
+    bt_f32_step<DIR>(K, p, n, true, r, s, c, scr, nlt, gl);
+  }
+  cpa_wait<0>();
+  // back substitution: step p (n-2 .. 1) consumes C'_p, r'_p, x0_p (and u_p)
+  auto issue_bwd = [&](int p) {
+    if (p >= 1) {
+      const int slot = (n - 2 - p) % PIPE;
+      const int64_t pt = base + (int64_t)p * st;
+#pragma unroll
+      for (int e = 0; e < 30; ++e) cpa4(S(slot, e), scr + ((int64_t)p * 30 + e) * nlt + gl);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) cpa4(S(slot, 30 + m), x0_at(p, m));
+      if (!OUT_DF && add_u) {
+#pragma unroll
+        for (int m = 0; m < 5; ++m) cpa8(SU(slot, m), F.u + m * NP + pt);
+      }
+    }
+    cpa_commit();
+  };
+  float dn[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int q = 0; q < PIPE - 1; ++q) issue_bwd(n - 2 - q);
+  for (int p = n - 2; p >= 1; --p) {
+    issue_bwd(p - (PIPE - 1));
+    cpa_wait<PIPE - 1>();
+    const int slot = (n - 2 - p) % PIPE;
+    const int64_t pt = base + (int64_t)p * st;
+    float d[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      float t = *S(slot, 25 + m);
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc) t -= *S(slot, m * 5 + cc) * dn[cc];
+      d[m] = t;
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const float xv = *S(slot, 30 + m);
+      if (OUT_DF) {
+        const df64 v = df_two_sum(xv, d[m]);
+        bdf[m * NP + pt] = v.hi;
+        bdf[(5 + m) * NP + pt] = v.lo;
+      } else {
+        const double v = (double)xv + (double)d[m];
+        rhs[m * NP + pt] = v;
+        if (add_u) F.u[m * NP + pt] = *SU(slot, m) + v;
+      }
+      dn[m] = d[m];
+    }
+  }
+  cpa_wait<0>();
+}
+#endif  // NPBMZ_HAS_FP32
 
 // ============================================================================
 // SP scalar pentadiagonal line solve, one thread per line.
@@ -1870,6 +2307,12 @@ __global__ void __launch_bounds__(128) k_add(Fields F, const Work* __restrict__ 
 // ============================================================================
 // host-side launchers (declared in step_launch.h)
 // ============================================================================
+void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s) {
+  if (nwork <= 0) return;
+  if (sp) k_prim_w<true><<<nwork, 128, 0, s>>>(F, K, work);
+  else k_prim_w<false><<<nwork, 128, 0, s>>>(F, K, work);
+}
+
 void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s) {
   if (hi <= lo) return;
   int64_t g = (hi - lo + 255) / 256;
@@ -1925,6 +2368,26 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
   if (mode == 1) { launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s); return; }
+  if (mode == 4 && !sp) {
+    // one fused step: b of the x sweep comes from compute_rhs's double-float
+    // copy, x and y hand their results on as double-float, z writes FP64
+    // rhs (and u)
+    float* scr = reinterpret_cast<float*>(scratch);
+    float* x0 = reinterpret_cast<float*>(xw);
+    const size_t sm_m = pl_mixed_smem(tpb), sm_r = pl_refine_smem(tpb, dir != 2);
+    if (dir == 0) {
+      k_bt_mixed_pl<0><<<nwork, tpb, sm_m, s>>>(F, K, work, scr, nlt, x0);
+      k_bt_refine_pl<0, true><<<nwork, tpb, sm_r, s>>>(F, K, work, scr, nlt, add_u, x0);
+    } else if (dir == 1) {
+      k_bt_mixed_pl<1><<<nwork, tpb, sm_m, s>>>(F, K, work, scr, nlt, x0);
+      k_bt_refine_pl<1, true><<<nwork, tpb, sm_r, s>>>(F, K, work, scr, nlt, add_u, x0);
+    } else {
+      k_bt_mixed_pl<2><<<nwork, tpb, sm_m, s>>>(F, K, work, scr, nlt, x0);
+      k_bt_refine_pl<2, false><<<nwork, tpb, sm_r, s>>>(F, K, work, scr, nlt, add_u, x0);
+    }
+    return;
+  }
+  if (mode == 4) mode = 2;
   if (mode == 2 || mode == 3) {
     const bool resid64 = mode == 3;
     float* scr = reinterpret_cast<float*>(scratch);
@@ -1943,17 +2406,17 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
     } else {
       float* x0 = reinterpret_cast<float*>(xw);
       if (dir == 0) {
-        k_bt_mixed_solve<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        k_bt_mixed_solve<0, false><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
         if (resid64) k_bt_refine<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
-        else k_bt_refine_df<0><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+        else k_bt_refine_df<0, false, false><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
       } else if (dir == 1) {
-        k_bt_mixed_solve<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        k_bt_mixed_solve<1, false><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
         if (resid64) k_bt_refine<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
-        else k_bt_refine_df<1><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+        else k_bt_refine_df<1, false, false><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
       } else {
-        k_bt_mixed_solve<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
+        k_bt_mixed_solve<2, false><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, x0);
         if (resid64) k_bt_refine<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
-        else k_bt_refine_df<2><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
+        else k_bt_refine_df<2, false, false><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, add_u, x0);
       }
     }
     return;
@@ -1964,6 +2427,35 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
   (void)mode;
   launch_solve_t<double>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s);
 }
+
+#if NPBMZ_HAS_FP32
+// Opt the pipelined sweeps into their dynamic shared memory (above 48 KB for
+// 128 threads per CTA); called once per handle, outside any stream capture.
+int configure_kernels() {
+  const int cap = (int)pl_refine_smem(128, false);
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void* f) {
+    const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+    if (r != cudaSuccess) e = r;
+  };
+  set((const void*)k_bt_mixed_pl<0>);
+  set((const void*)k_bt_mixed_pl<1>);
+  set((const void*)k_bt_mixed_pl<2>);
+  set((const void*)k_bt_refine_pl<0, true>);
+  set((const void*)k_bt_refine_pl<1, true>);
+  set((const void*)k_bt_refine_pl<2, false>);
+  return e == cudaSuccess ? 0 : -1;
+}
+
+void launch_xline_ends(const Fields& F, const Work* work, int nwork, int tpb, cudaStream_t s) {
+  if (nwork > 0) k_xline_ends<<<nwork, tpb, 0, s>>>(F, work);
+}
+
+void launch_split_df(const double* src, float* dst, int64_t NP, cudaStream_t s) {
+  int64_t g = (5 * NP + 255) / 256;
+  k_split_df<<<(int)(g > 8192 ? 8192 : g), 256, 0, s>>>(src, dst, NP);
+}
+#endif
 
 void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s) {
   if (nwork > 0) k_add<<<nwork, 128, 0, s>>>(F, work);

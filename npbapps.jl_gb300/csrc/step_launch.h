@@ -10,6 +10,7 @@ namespace npbmz {
 #define NPBMZ_DECLARE_LAUNCHERS(NS)                                                                                  \
   namespace NS {                                                                                                     \
   void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s);                                   \
+  void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s);       \
   void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork,                 \
                   double* partials, cudaStream_t s, const LinWeights* lw = nullptr);                                 \
   void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork,       \
@@ -19,4 +20,12 @@ namespace npbmz {
 NPBMZ_DECLARE_LAUNCHERS(exact)
 NPBMZ_DECLARE_LAUNCHERS(fast)
 #undef NPBMZ_DECLARE_LAUNCHERS
+namespace fast {
+// dst (10 float planes: double-float hi 0..4, lo 5..9) <- src (5 FP64 planes)
+void launch_split_df(const double* src, float* dst, int64_t NP, cudaStream_t s);
+// the forcing at both ends of every x line into Fields::rdx
+void launch_xline_ends(const Fields& F, const Work* work, int nwork, int tpb, cudaStream_t s);
+// dynamic shared memory limits of the pipelined sweeps; 0 on success
+int configure_kernels();
+}  // namespace fast
 }  // namespace npbmz
