@@ -43,10 +43,17 @@ WORKLOADS = {
     "sp-a": ("SP", "A", "SP-MZ 128x128x16, 4x4 equal zones (32x32x16), dt 1.5e-3"),
 }
 SEED = 20261203
-# Algorithmic HBM bytes per grid point of each phase (FP64 state, line-solve
-# scratch kept out of the count): compute_rhs reads u and forcing and writes
-# rhs; each sweep reads u and rhs and writes rhs.
-BYTES_PER_POINT = {"rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
+# Algorithmic HBM bytes per grid point of each phase (the 600 B/pt-step model:
+# FP64 state, intermediates and line-solve scratch kept out of the count):
+# compute_rhs reads u and forcing and writes rhs; each sweep reads u and rhs
+# and writes rhs; the z sweep also updates u (add); the primitive kernel reads u.
+BYTES_PER_POINT = {"prim": 40.0, "rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
+# Kernels of each phase of the batched step (for the per-kernel ncu figures).
+PHASE_KERNELS = {
+    "mixed": {"prim": ["k_prim_w<0>"], "rhs": ["k_rhs_flux<0, 0>"],
+              "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>"], "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
+              "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
+}
 
 
 def env_rank():
@@ -68,7 +75,8 @@ def geometry(npbmz, kind, cls):
 
 
 class ClockSampler:
-    """nvidia-smi samples (200 ms) while the timed region runs."""
+    """nvidia-smi samples (every 20 ms) while the timed region runs; entering
+    waits for the first sample so that sampling covers the region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -83,9 +91,13 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.lines.clear()  # samples from before the region starts
         except Exception:
             self.proc = None
         return self
@@ -141,21 +153,27 @@ def time_steps(p, torch, stream, steps, warmup, dist=None):
     return e0.elapsed_time(e1)
 
 
-def phase_times(p, npbmz, torch, stream, reps=3):
-    """Per-phase launch times (CUDA events on the launching stream)."""
-    names = ["exch", "rhs", "x", "y", "z"]
-    ph = [npbmz.PHASE_EXCH, npbmz.PHASE_RHS, npbmz.PHASE_XSOLVE, npbmz.PHASE_YSOLVE, npbmz.PHASE_ZSOLVE]
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(ph) + 1)]
-    tot = np.zeros(len(ph))
-    for r in range(reps + 1):
-        ev[0].record(stream)
-        for i, x in enumerate(ph):
-            p.phase(x, -1)
-            ev[i + 1].record(stream)
-        stream.synchronize()
-        if r > 0:
-            tot += [ev[i].elapsed_time(ev[i + 1]) for i in range(len(ph))]
-    return dict(zip(names, (tot / reps).tolist()))
+def phase_times(p, nsteps):
+    """Per-phase device time of the batched step -- the kernels the timed
+    steps run -- from CUDA events the library records around each phase on
+    its stream (npbmz_step_profile)."""
+    p.step_profile(1)  # warm
+    return p.step_profile(nsteps)
+
+
+def kernel_metrics(workload, variant):
+    """Per-point ncu figures of the step kernels (profiles/ncu_kernel_metrics.json):
+    from a capture of this workload, else of the BT-B workload (same kernels),
+    per point."""
+    try:
+        allm = json.loads((ROOT / "profiles" / "ncu_kernel_metrics.json").read_text())
+    except Exception:
+        return None, None
+    for w in (workload, "bt-b"):
+        m = allm.get(w, {}).get(variant)
+        if m:
+            return m, w
+    return None, None
 
 
 def cpu_baseline(kind, cls, ce, target_s=15.0):
@@ -259,28 +277,38 @@ def run_gpu(args):
 
     extra = {}
     if rank == 0 and args.quick:
-        ph = phase_times(p, npbmz, torch, stream)
+        ph = phase_times(p, max(3, min(args.steps, 10)))
         extra["phase_ms"] = ph
     elif rank == 0:
-        # per-phase launch times of the timed variant -> dominant kernel roofline
-        ph = phase_times(p, npbmz, torch, stream)
+        # per-phase device times of the timed variant's kernels -> dominant kernel roofline
+        ph = phase_times(p, max(3, min(args.steps, 10)))
         top = max((k for k in ph if k != "exch"), key=lambda k: ph[k])
         pk = peaks()
         hbm = float(pk.get("hbm_gbs", 6800.0))
         achieved = BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
-        traffic = None
-        tfile = ROOT / "profiles" / "ncu_traffic.json"
-        if tfile.exists():
-            try:
-                tr = json.loads(tfile.read_text()).get(args.workload, {}).get(args.variant, {}).get(top)
-                traffic = tr
-            except Exception:
-                traffic = None
         fp64 = npbmz.fp64_peak_gflops()
-        extra["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm, "traffic": traffic,
+        km, km_src = kernel_metrics(args.workload, args.variant)
+        kvar = "mixed" if flags & npbmz.MIXED and kind == "BT" else None
+        knames = PHASE_KERNELS.get(kvar, {}).get(top, []) if kvar else []
+        traffic = None
+        fp64_obj = None
+        if km and knames and all(k in km for k in knames):
+            traffic = sum(km[k]["dram_bytes_per_point"] for k in knames) * pts
+            flops_pt = sum(km[k]["fp64_flops_per_point"] for k in knames)
+            fp64_ach = flops_pt * pts / (ph[top] * 1e-3) / 1e9
+            fp64_obj = {"achieved": fp64_ach, "peak": fp64, "unit": "GFLOP/s", "frac": fp64_ach / fp64,
+                        "flops_per_point": flops_pt,
+                        "pipe_active_ncu": max(km[k]["fp64_pipe_active"] for k in knames),
+                        "peak_source": "npbmz_fp64_peak: FP64 FMA chains on this GPU, measured in this run"}
+        extra["roofline"] = {"bound": "hbm", "kernel": "+".join(knames) if knames else top, "phase": top,
+                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                             "traffic": traffic,
+                             "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum per point, {km_src} "
+                                                "capture (profiles/ncu_kernel_metrics.json), times this workload's points")
+                             if traffic is not None else None,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
-                             "bytes_per_point": BYTES_PER_POINT[top], "launch_ms": ph[top]}
+                             "bytes_per_point": BYTES_PER_POINT[top], "launch_ms": ph[top],
+                             "binding_ceiling": "fp64" if fp64_obj else None, "fp64": fp64_obj}
         extra["phase_ms"] = ph
         extra["fp64_peak_gflops_measured"] = fp64
         # variants (fewer steps each)

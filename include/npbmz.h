@@ -179,6 +179,21 @@ int npbmz_autotune(npbmz_t* h);
  * No counterpart in the reference. */
 int npbmz_fp64_peak(double* gflops);
 
+/* Per-phase device time of the batched step: nsteps steps launched directly
+ * (the kernels npbmz_step and its graph run), with CUDA events around each
+ * phase on the handle's stream; phase_ms[NPBMZ_PROF_COUNT] receives the mean
+ * milliseconds per step of exch_qbc, the primitive kernel, compute_rhs and
+ * the x, y and z sweeps (each sweep: all its kernels).  Advances the state
+ * by nsteps steps.  No counterpart in the reference.  Synchronous. */
+#define NPBMZ_PROF_EXCH 0
+#define NPBMZ_PROF_PRIM 1
+#define NPBMZ_PROF_RHS 2
+#define NPBMZ_PROF_X 3
+#define NPBMZ_PROF_Y 4
+#define NPBMZ_PROF_Z 5
+#define NPBMZ_PROF_COUNT 6
+int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms);
+
 /* Query: number of kernel launches npbmz_step issues per step, device bytes
  * held by the handle, and (info, n) a small summary string. */
 int npbmz_launches_per_step(npbmz_t* h);

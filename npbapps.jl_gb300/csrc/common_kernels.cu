@@ -281,8 +281,13 @@ __global__ void __launch_bounds__(256) k_convert(Fields F, double* __restrict__ 
   const ZoneDev Z = F.zones[zone];
   const int np = Z.nx * Z.ny * Z.nz;
   double* st = stage + (soff[zone] - sub);
+  // BT's reference arrays are variable-fastest (AoS): there consecutive
+  // threads take consecutive variables of a point, so a warp reads or writes
+  // one contiguous run of host memory (over NVLink-C2C for page-locked
+  // buffers) and the device side splits it across the five planes.
+  const bool aos = kind == 0 && layout != 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 5 * np; t += gridDim.x * blockDim.x) {
-    const int m = t / np, q = t % np;
+    const int m = aos ? t % 5 : t / np, q = aos ? t / 5 : t % np;
     const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
     int64_t s;
     if (layout == 0) s = t;

@@ -1051,6 +1051,45 @@ int npbmz_step(npbmz_t* h, int nsteps, double* norms) {
   return 0;
 }
 
+int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms) {
+  if (!h) return fail(nullptr, "null handle");
+  if (nsteps < 1 || !phase_ms) return fail(h, "nsteps must be >= 1 and phase_ms non-null");
+  constexpr int NE = NPBMZ_PROF_COUNT + 1;
+  std::vector<cudaEvent_t> ev((size_t)nsteps * NE, nullptr);
+  int rc = 0;
+  for (auto& e : ev)
+    if (!rc && cudaEventCreate(&e) != cudaSuccess) rc = fail(h, "cudaEventCreate failed");
+  if (!rc && flush_boundary(h)) rc = -1;
+  for (int st = 0; st < nsteps && !rc; ++st) {
+    cudaEvent_t* E = &ev[(size_t)st * NE];
+    rc |= cudaEventRecord(E[0], h->stream) != cudaSuccess;
+    if (!rc) rc = phase_exch(h);
+    rc |= cudaEventRecord(E[1], h->stream) != cudaSuccess;
+    if (!rc) rc = phase_prim(h, -1);
+    rc |= cudaEventRecord(E[2], h->stream) != cudaSuccess;
+    if (!rc) rc = phase_rhs(h, -1, h->kind == NPBMZ_SP, false);
+    rc |= cudaEventRecord(E[3], h->stream) != cudaSuccess;
+    for (int dir = 0; dir < 3 && !rc; ++dir) {
+      rc = phase_solve(h, dir, -1, dir == 2 ? 1 : 0, true);
+      rc |= cudaEventRecord(E[4 + dir], h->stream) != cudaSuccess;
+    }
+  }
+  if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = fail(h, "profiled steps failed: %s", cudaGetErrorString(cudaGetLastError()));
+  if (!rc) {
+    for (int k = 0; k < NPBMZ_PROF_COUNT; ++k) phase_ms[k] = 0.0;
+    for (int st = 0; st < nsteps; ++st)
+      for (int k = 0; k < NPBMZ_PROF_COUNT; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[(size_t)st * NE + k], ev[(size_t)st * NE + k + 1]);
+        phase_ms[k] += ms / nsteps;
+      }
+  }
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  if (rc && h->err.empty()) h->err = "profiled steps failed";
+  return rc ? -1 : 0;
+}
+
 int npbmz_verify(npbmz_t* h, double* xcr, double* xce) {
   if (!h || !xcr || !xce) return fail(h, "null argument");
   if (!h->norms_d) {

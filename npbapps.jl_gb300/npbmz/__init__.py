@@ -43,8 +43,9 @@ EXPORTS = [
     "npbmz_download", "npbmz_upload_async", "npbmz_download_async", "npbmz_exch_qbc", "npbmz_adi", "npbmz_step",
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
-    "npbmz_bt_xsolve_noalloc", "npbmz_adjoint",
+    "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile",
 ]
+PROF_PHASES = ("exch", "prim", "rhs", "x", "y", "z")
 
 # Problem classes (src/BT/classes.jl:15-24, src/SP/classes.jl:16-25):
 # niter, dt, ratio, x_zones, y_zones, gx, gy, gz
@@ -130,6 +131,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_destroy.argtypes = [vp]
     L.npbmz_bt_xsolve_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, vp, vp, vp]
     L.npbmz_adjoint.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp]
+    L.npbmz_step_profile.argtypes = [vp, ctypes.c_int, dp]
     _lib = L
     return L
 
@@ -265,6 +267,13 @@ class Problem:
         out = np.zeros(10 * max(nsteps, 1)) if norms else None
         self._check(lib().npbmz_step(self._h, nsteps, _dp(out) if norms else None), "npbmz_step")
         return out[: 10 * nsteps].reshape(nsteps, 2, 5) if norms else None
+
+    def step_profile(self, nsteps: int = 1):
+        """Mean device milliseconds per step of each phase of the batched step
+        (CUDA events on the handle's stream); advances nsteps steps."""
+        out = np.zeros(len(PROF_PHASES))
+        self._check(lib().npbmz_step_profile(self._h, nsteps, _dp(out)), "npbmz_step_profile")
+        return dict(zip(PROF_PHASES, out.tolist()))
 
     def verify(self):
         xcr, xce = np.zeros(5), np.zeros(5)
