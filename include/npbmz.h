@@ -164,6 +164,17 @@ int npbmz_phase(npbmz_t* h, int phase, int zone);
 int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_target, double* J,
                   double* grad_forcing, double* grad_u0);
 
+/* Zone groups of the step graph (NPBMZ_GRAPH, FMA build), 1..8.  With G > 1
+ * the zones are split into G groups of near-equal size, and the captured
+ * step runs each group's primitive kernel, compute_rhs and sweeps as one
+ * branch.  Each branch starts when the previous group's compute_rhs is done,
+ * so FP64-bound phases of one group run beside the FP32 sweeps of the
+ * previous one.  Results are unchanged (zones are independent within a step
+ * after exch_qbc).  npbmz_create sets 4 groups for NPBMZ_GRAPH handles with
+ * at least 8 zones (not NPBMZ_EXACT or NPBMZ_PERZONE).  No counterpart in the
+ * reference. */
+int npbmz_set_step_groups(npbmz_t* h, int groups);
+
 /* Use `stream` (a cudaStream_t, NULL = the legacy default stream) for all
  * later work of the handle. */
 int npbmz_set_stream(npbmz_t* h, void* stream);

@@ -126,6 +126,9 @@ struct npbmz_handle {
   LinWeights lw;             // compute_rhs linear stencil weights (FMA build)
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
+  // y and z line scratch of the grouped step graph, where sweeps of
+  // different directions (of different zone groups) run at the same time
+  void* scratch_yz[2] = {nullptr, nullptr};
   double* part_rhs = nullptr;
   double* part_err = nullptr;
   double* norms_d = nullptr;
@@ -147,6 +150,14 @@ struct npbmz_handle {
   Work* wline_d[3] = {nullptr, nullptr, nullptr};
   int nwline[3] = {0, 0, 0};
   std::vector<Range> line_range[3];
+  // zone groups of the pipelined step graph: every work list is ordered
+  // group-major, so group g owns one contiguous slice of each list
+  int ngroups = 1;
+  std::vector<int> zone_group;     // per zone
+  std::vector<Range> grp_pts, grp_int, grp_line[3];
+  int cur_group = -1;              // >= 0 while the phases of one group are issued
+  cudaStream_t grp_stream[8] = {};
+  cudaEvent_t grp_ev[2 * 8 + 1] = {};
   int tpb_line[3] = {64, 64, 64};
   int64_t nlines[3] = {0, 0, 0};
   // execution
@@ -230,15 +241,60 @@ int64_t ref_elems(int kind, int field, const ZoneDev& z) {
   return 5 * IMAXP * JMAXP * KMAX;
 }
 
-int build_work_lists(npbmz_t* h) {
+// Zones into ngroups groups of near-equal point counts (largest zone first
+// into the lightest group).
+void assign_zone_groups(npbmz_t* h) {
   const int nz = h->nzones;
-  // zones in decreasing size: the longest work first, each zone contiguous
+  const int G = std::max(1, std::min(h->ngroups, nz));
+  h->ngroups = G;
   std::vector<int> order(nz);
   std::iota(order.begin(), order.end(), 0);
+  auto npts = [&](int z) { return (int64_t)h->zh[z].nx * h->zh[z].ny * h->zh[z].nz; };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return npts(a) > npts(b); });
+  std::vector<int64_t> load(G, 0);
+  h->zone_group.assign(nz, 0);
+  for (int z : order) {
+    const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    h->zone_group[z] = g;
+    load[g] += npts(z);
+  }
+}
+
+// Zones group-major, each group's zones by decreasing key (the longest work
+// first, each zone contiguous).
+template <typename Key>
+std::vector<int> group_order(const npbmz_t* h, Key key) {
+  std::vector<int> order(h->nzones);
+  std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    const ZoneDev &A = h->zh[a], &B = h->zh[b];
-    return (int64_t)A.nx * A.ny * A.nz > (int64_t)B.nx * B.ny * B.nz;
+    if (h->zone_group[a] != h->zone_group[b]) return h->zone_group[a] < h->zone_group[b];
+    return key(a) > key(b);
   });
+  return order;
+}
+
+// Per-group slices [lo, hi) of a work list from its per-zone ranges.
+std::vector<Range> group_ranges(const npbmz_t* h, const std::vector<Range>& zr) {
+  std::vector<Range> gr(h->ngroups);
+  for (int g = 0; g < h->ngroups; ++g) { gr[g].lo = 1 << 30; gr[g].hi = 0; }
+  for (int z = 0; z < h->nzones; ++z) {
+    Range& r = gr[h->zone_group[z]];
+    r.lo = std::min(r.lo, zr[z].lo);
+    r.hi = std::max(r.hi, zr[z].hi);
+  }
+  for (Range& r : gr)
+    if (r.hi < r.lo) r.lo = r.hi = 0;
+  return gr;
+}
+
+int build_work_lists(npbmz_t* h) {
+  const int nz = h->nzones;
+  if ((int)h->zone_group.size() != nz) assign_zone_groups(h);
+  for (void** b : {(void**)&h->wpts_d, (void**)&h->zblk_pts_d, (void**)&h->wint_d, (void**)&h->zblk_int_d,
+                   (void**)&h->part_rhs, (void**)&h->part_err})
+    if (*b) { cudaFree(*b); *b = nullptr; }
+  const std::vector<int> order =
+      group_order(h, [&](int z) { return (int64_t)h->zh[z].nx * h->zh[z].ny * h->zh[z].nz; });
   std::vector<Work> w;
   h->pts_range.assign(nz, Range());
   for (int z : order) {
@@ -273,6 +329,8 @@ int build_work_lists(npbmz_t* h) {
   CK(h, cudaMemcpy(h->zblk_int_d, zi.data(), zi.size() * sizeof(int), cudaMemcpyHostToDevice));
   if (dalloc(h, &h->part_rhs, (size_t)h->nwint * 5)) return -1;
   if (dalloc(h, &h->part_err, (size_t)h->nwpts * 5)) return -1;
+  h->grp_pts = group_ranges(h, h->pts_range);
+  h->grp_int = group_ranges(h, h->int_range);
   return 0;
 }
 
@@ -298,11 +356,7 @@ int build_line_lists(npbmz_t* h) {
   const int nz = h->nzones;
   for (int dir = 0; dir < 3; ++dir) {
     if (h->wline_d[dir]) { cudaFree(h->wline_d[dir]); h->wline_d[dir] = nullptr; }
-    std::vector<int> order(nz);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-      return zone_line_len(h->zh[a], dir) > zone_line_len(h->zh[b], dir);
-    });
+    const std::vector<int> order = group_order(h, [&](int z) { return (int64_t)zone_line_len(h->zh[z], dir); });
     const int tpb = h->tpb_line[dir];
     std::vector<Work> w;
     h->line_range[dir].assign(nz, Range());
@@ -315,6 +369,7 @@ int build_line_lists(npbmz_t* h) {
     h->nwline[dir] = (int)w.size();
     CK(h, cudaMalloc((void**)&h->wline_d[dir], std::max<size_t>(1, w.size()) * sizeof(Work)));
     CK(h, cudaMemcpy(h->wline_d[dir], w.data(), w.size() * sizeof(Work), cudaMemcpyHostToDevice));
+    h->grp_line[dir] = group_ranges(h, h->line_range[dir]);
   }
   return 0;
 }
@@ -335,6 +390,7 @@ int phase_prim(npbmz_t* h, int zone) {
     // x-line-major state copy can be written too
     int wlo = 0, whi = h->nwpts;
     if (zone >= 0) { wlo = h->pts_range[zone].lo; whi = h->pts_range[zone].hi; }
+    else if (h->cur_group >= 0) { wlo = h->grp_pts[h->cur_group].lo; whi = h->grp_pts[h->cur_group].hi; }
     fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream);
   }
   CKL(h);
@@ -346,6 +402,7 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
   const Fields F = fields(h);
   int lo = 0, hi = h->nwint;
   if (zone >= 0) { lo = h->int_range[zone].lo; hi = h->int_range[zone].hi; }
+  else if (h->cur_group >= 0) { lo = h->grp_int[h->cur_group].lo; hi = h->grp_int[h->cur_group].hi; }
   if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
   else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->lw);
   CKL(h);
@@ -355,17 +412,22 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
 // fused: part of a whole step (run_adi), where the refined FP32 BT sweeps
 // hand their results on as double-float; otherwise each sweep reads and
 // writes rhs in FP64 (single phases, the adjoint's recomputation).
+void* line_scratch(npbmz_t* h, int dir) {
+  return (dir > 0 && h->scratch_yz[dir - 1]) ? h->scratch_yz[dir - 1] : h->scratch;
+}
+
 int phase_solve(npbmz_t* h, int dir, int zone, int add_u, bool fused = false) {
   const Fields F = fields(h);
   int lo = 0, hi = h->nwline[dir];
   if (zone >= 0) { lo = h->line_range[dir][zone].lo; hi = h->line_range[dir][zone].hi; }
+  else if (h->cur_group >= 0) { lo = h->grp_line[dir][h->cur_group].lo; hi = h->grp_line[dir][h->cur_group].hi; }
   const bool sp = h->kind == NPBMZ_SP;
   if (use_exact(h))
-    exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch,
+    exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], line_scratch(h, dir),
                         h->nlines[dir], add_u, nullptr, h->stream);
   else
     fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : ((h->flags & NPBMZ_REFINE_FP64) ? 3 : (fused && h->rdf ? 4 : 2))), dir, F, h->K,
-                       h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], h->scratch, h->nlines[dir], add_u, h->xw,
+                       h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], line_scratch(h, dir), h->nlines[dir], add_u, h->xw,
                        h->stream);
   CKL(h);
   return 0;
@@ -432,8 +494,49 @@ void drop_graph(npbmz_t* h) {
   h->graph_exec = nullptr;
 }
 
+// One step as zone-group branches (captured into the step graph): after
+// exch_qbc, group g runs prim, compute_rhs and its three sweeps on its own
+// stream; its primitive kernel waits for group g-1's compute_rhs.  So the
+// FP32 sweeps of group g (FP32 / issue bound) run beside the FP64
+// primitive and compute_rhs kernels of group g+1 (FP64-pipe bound).
+int grouped_step(npbmz_t* h, cudaStream_t cs) {
+  const int G = h->ngroups;
+  const bool sp = h->kind == NPBMZ_SP;
+  if (phase_exch(h)) return -1;
+  cudaEvent_t start = h->grp_ev[2 * G];
+  CK(h, cudaEventRecord(start, cs));
+  int rc = 0;
+  for (int g = 0; g < G && !rc; ++g) {
+    cudaStream_t S = h->grp_stream[g];
+    rc |= cudaStreamWaitEvent(S, start, 0) != cudaSuccess;
+    if (g > 0) rc |= cudaStreamWaitEvent(S, h->grp_ev[2 * (g - 1)], 0) != cudaSuccess;
+    h->stream = S;
+    h->cur_group = g;
+    if (!rc) rc = phase_prim(h, -1);
+    if (!rc) rc = phase_rhs(h, -1, sp, false);
+    if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g], S) != cudaSuccess;
+    for (int dir = 0; dir < 3 && !rc; ++dir) rc = phase_solve(h, dir, -1, dir == 2 ? 1 : 0, true);
+    if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g + 1], S) != cudaSuccess;
+  }
+  h->stream = cs;
+  h->cur_group = -1;
+  for (int g = 0; g < G && !rc; ++g) rc = cudaStreamWaitEvent(cs, h->grp_ev[2 * g + 1], 0) != cudaSuccess;
+  if (rc && h->err.empty()) h->err = "grouped step capture failed";
+  return rc ? -1 : 0;
+}
+
+bool use_groups(const npbmz_t* h) {
+  return h->ngroups > 1 && !use_exact(h) && !(h->flags & NPBMZ_PERZONE);
+}
+
 int capture_step_graph(npbmz_t* h) {
   drop_graph(h);
+  if (use_groups(h)) {
+    for (int g = 0; g < h->ngroups; ++g)
+      if (!h->grp_stream[g]) CK(h, cudaStreamCreateWithFlags(&h->grp_stream[g], cudaStreamNonBlocking));
+    for (int e = 0; e < 2 * h->ngroups + 1; ++e)
+      if (!h->grp_ev[e]) CK(h, cudaEventCreateWithFlags(&h->grp_ev[e], cudaEventDisableTiming));
+  }
   if (flush_boundary(h)) return -1;  // keep the one-off reset out of the graph
   // Capture is not allowed on the legacy default stream: capture and replay
   // on an owned stream, fenced against the caller's stream by events.
@@ -450,7 +553,7 @@ int capture_step_graph(npbmz_t* h) {
   cudaStream_t saved = h->stream;
   h->stream = cs;
   CK(h, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-  int rc = one_step(h, false, nullptr);
+  int rc = use_groups(h) ? grouped_step(h, cs) : one_step(h, false, nullptr);
   cudaError_t e = cudaStreamEndCapture(cs, &g);
   h->stream = saved;
   if (rc) { if (g) cudaGraphDestroy(g); return -1; }
@@ -475,10 +578,17 @@ int replay_graph(npbmz_t* h, int nsteps) {
   return 0;
 }
 
+// Kernel launches of one npbmz_step step: exch_qbc, then per batch (all
+// zones, each zone with PERZONE, each zone group in the grouped graph) the
+// primitive kernel, compute_rhs and the three sweeps (two kernels each when
+// the FP32 solves are refined).
 int count_launches(npbmz_t* h) {
-  const int adi = 5;  // prim, rhs, x, y, z
-  int n = (h->nzones > 1 ? 1 : 0) + ((h->flags & NPBMZ_PERZONE) ? adi * h->nzones : adi);
-  return n;
+  const bool refined = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE);
+  const int adi = 2 + 3 * (refined ? 2 : 1);
+  int batches = 1;
+  if (h->flags & NPBMZ_PERZONE) batches = h->nzones;
+  else if ((h->flags & NPBMZ_GRAPH) && h->ngroups > 1 && !(h->flags & NPBMZ_EXACT)) batches = h->ngroups;
+  return (h->nzones > 1 ? 1 : 0) + adi * batches;
 }
 
 int ensure_stage(npbmz_t* h, size_t elems) {
@@ -982,6 +1092,14 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess) { h->stream = s; h->own_stream = true; }
   h->launches_per_step = count_launches(h);
   *out = h;
+  // the step graph of a batched FMA-build step runs in zone-group branches
+  if ((variant_flags & NPBMZ_GRAPH) && !(variant_flags & (NPBMZ_EXACT | NPBMZ_PERZONE)) && nzones >= 8 &&
+      npbmz_set_step_groups(h, 4)) {
+    const std::string msg = h->err;
+    npbmz_destroy(h);
+    *out = nullptr;
+    return fail(nullptr, "%s", msg.c_str());
+  }
   return 0;
 }
 
@@ -1139,6 +1257,23 @@ int npbmz_phase(npbmz_t* h, int phase, int zone) {
   }
 }
 
+int npbmz_set_step_groups(npbmz_t* h, int groups) {
+  if (!h) return fail(nullptr, "null handle");
+  if (groups < 1 || groups > 8) return fail(h, "groups must be 1..8");
+  CK(h, cudaStreamSynchronize(h->stream));
+  drop_graph(h);
+  h->ngroups = groups;
+  assign_zone_groups(h);
+  if (build_work_lists(h) || build_line_lists(h)) return -1;
+  if (h->ngroups > 1 && !h->scratch_yz[0])
+    for (int d = 0; d < 2; ++d) {
+      CK(h, cudaMalloc(&h->scratch_yz[d], std::max<size_t>(h->scratch_bytes, 16)));
+      h->device_bytes += (int64_t)h->scratch_bytes;
+    }
+  h->launches_per_step = count_launches(h);
+  return 0;
+}
+
 int npbmz_set_stream(npbmz_t* h, void* stream) {
   if (!h) return fail(nullptr, "null handle");
   if (h->own_stream && h->stream) {
@@ -1234,7 +1369,7 @@ int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->part_rhs,
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->scratch_yz[0], h->scratch_yz[1], h->part_rhs,
                   h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wint_d, h->zblk_int_d,
                   h->wline_d[0], h->wline_d[1],
                   h->wline_d[2]};
@@ -1245,6 +1380,10 @@ int npbmz_destroy(npbmz_t* h) {
       if (h->soff_d[l][f]) cudaFree(h->soff_d[l][f]);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   if (h->aux_stream) { cudaStreamSynchronize(h->aux_stream); cudaStreamDestroy(h->aux_stream); }
+  for (cudaStream_t gs : h->grp_stream)
+    if (gs) { cudaStreamSynchronize(gs); cudaStreamDestroy(gs); }
+  for (cudaEvent_t e : h->grp_ev)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : h->fence)
     if (e) cudaEventDestroy(e);
   delete h;

@@ -43,7 +43,7 @@ EXPORTS = [
     "npbmz_download", "npbmz_upload_async", "npbmz_download_async", "npbmz_exch_qbc", "npbmz_adi", "npbmz_step",
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
-    "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile",
+    "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
 ]
 PROF_PHASES = ("exch", "prim", "rhs", "x", "y", "z")
 
@@ -132,6 +132,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_bt_xsolve_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, vp, vp, vp]
     L.npbmz_adjoint.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp]
     L.npbmz_step_profile.argtypes = [vp, ctypes.c_int, dp]
+    L.npbmz_set_step_groups.argtypes = [vp, ctypes.c_int]
     _lib = L
     return L
 
@@ -288,6 +289,10 @@ class Problem:
 
     def set_stream(self, stream_ptr: int):
         self._check(lib().npbmz_set_stream(self._h, ctypes.c_void_p(stream_ptr)), "npbmz_set_stream")
+
+    def set_step_groups(self, groups: int):
+        """Zone groups of the step graph (pipelined branches), 1..8."""
+        self._check(lib().npbmz_set_step_groups(self._h, groups), "npbmz_set_step_groups")
 
     def autotune(self):
         self._check(lib().npbmz_autotune(self._h), "npbmz_autotune")
