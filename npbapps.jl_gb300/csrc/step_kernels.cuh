@@ -638,13 +638,21 @@ __device__ __forceinline__ void bt_asm_b(const T n[5][5], T tmp1, const T dd[5],
     }
 }
 
+// Pivot reciprocal: IEEE division in FP64 (the reference's arithmetic); in
+// the FP32 solves, which a double-float refinement corrects, the fast
+// reciprocal (within 2 ulp).
+template <typename T>
+__device__ __forceinline__ T pivot_recip(T b) { return (T)1.0 / b; }
+template <>
+__device__ __forceinline__ float pivot_recip<float>(float b) { return __fdividef(1.0f, b); }
+
 // binvcrhs (src/BT/solve_subs.jl:468-723): Gauss-Jordan on B, no pivoting,
 // applied to C and r.
 template <typename T>
 __device__ __forceinline__ void binvcrhs(T B[5][5], T C[5][5], T r[5]) {
 #pragma unroll
   for (int p = 0; p < 5; ++p) {
-    const T pivot = (T)1.0 / B[p][p];
+    const T pivot = pivot_recip<T>(B[p][p]);
 #pragma unroll
     for (int c = p + 1; c < 5; ++c) B[p][c] *= pivot;
 #pragma unroll
@@ -1865,7 +1873,7 @@ __global__ void __launch_bounds__(128) k_sp_solve(Fields F, Consts K, const Work
     for (int m = 0; m < 5; ++m) rr[2][m] = (T)rhs[m * NP + pt2];
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-      const T fac1 = (T)1.0 / cur3[s];
+      const T fac1 = pivot_recip<T>(cur3[s]);
       cur4[s] *= fac1;
       cur5[s] *= fac1;
 #pragma unroll
@@ -1896,7 +1904,7 @@ __global__ void __launch_bounds__(128) k_sp_solve(Fields F, Consts K, const Work
   // last two rows: p = n-2 (current), n-1 (next)
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
-    const T fac1 = (T)1.0 / cur3[s];
+    const T fac1 = pivot_recip<T>(cur3[s]);
     cur4[s] *= fac1;
     cur5[s] *= fac1;
 #pragma unroll
@@ -1905,7 +1913,7 @@ __global__ void __launch_bounds__(128) k_sp_solve(Fields F, Consts K, const Work
     nx4[s] -= nx2[s] * cur5[s];
 #pragma unroll
     for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
-    const T fac2 = (T)1.0 / nx3[s];
+    const T fac2 = pivot_recip<T>(nx3[s]);
     nx4[s] *= fac2;
     nx5[s] *= fac2;
 #pragma unroll
@@ -2064,7 +2072,7 @@ __device__ __forceinline__ void sp_forward_f32(int n, float* __restrict__ scr, i
     row_at(p + 2, L2, rr[2]);
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-      const float fac1 = 1.0f / cur3[s];
+      const float fac1 = __fdividef(1.0f, cur3[s]);
       cur4[s] *= fac1;
       cur5[s] *= fac1;
 #pragma unroll
@@ -2092,7 +2100,7 @@ __device__ __forceinline__ void sp_forward_f32(int n, float* __restrict__ scr, i
   }
 #pragma unroll
   for (int s = 0; s < 3; ++s) {
-    const float fac1 = 1.0f / cur3[s];
+    const float fac1 = __fdividef(1.0f, cur3[s]);
     cur4[s] *= fac1;
     cur5[s] *= fac1;
 #pragma unroll
@@ -2101,7 +2109,7 @@ __device__ __forceinline__ void sp_forward_f32(int n, float* __restrict__ scr, i
     nx4[s] -= nx2[s] * cur5[s];
 #pragma unroll
     for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] -= nx2[s] * rr[0][m];
-    const float fac2 = 1.0f / nx3[s];
+    const float fac2 = __fdividef(1.0f, nx3[s]);
 #pragma unroll
     for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr[1][m] *= fac2;
     tail.cur4[s] = cur4[s];
