@@ -316,7 +316,9 @@ def run_gpu(args):
         nv = max(3, min(args.steps, 10))
         for name, fl in (("fp64_batched", 0), ("fp64_exact_batched", npbmz.EXACT),
                          ("mixed_batched", npbmz.MIXED), ("mixed_batched_graph", npbmz.MIXED | npbmz.GRAPH),
-                         ("fp64_batched_graph", npbmz.GRAPH), ("fp64_perzone", npbmz.PERZONE)):
+                         ("fp64_batched_graph", npbmz.GRAPH),
+                         ("mixed_batched_graph_persistent", npbmz.MIXED | npbmz.GRAPH | npbmz.PERSIST),
+                         ("fp64_perzone", npbmz.PERZONE)):
             q = make(fl)
             steps_v = 2 if fl & npbmz.PERZONE else nv
             mv = time_steps(q, torch, stream, steps_v, 1)

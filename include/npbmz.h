@@ -55,8 +55,11 @@ typedef struct npbmz_handle npbmz_t;
                               per-zone adi order; default is all zones batched
                               in one launch per phase */
 #define NPBMZ_GRAPH   0x8  /* npbmz_step replays one captured CUDA graph per step */
-#define NPBMZ_PERSIST 0x10 /* line solves run as persistent kernels (one CTA set
-                              per SM pulling zone x line work items) */
+#define NPBMZ_PERSIST 0x10 /* the batched step's primitive, compute_rhs and
+                              pipelined FP32 BT sweep kernels (FMA build) run
+                              persistent: as many CTAs as fit on the SMs at
+                              once, each looping over zone x point or
+                              zone x line work items; results are unchanged */
 #define NPBMZ_REFINE_FP64 0x40 /* with NPBMZ_MIXED on BT: the refinement residual
                               in FP64 instead of double-float (FP32 pairs,
                               about 48 bits) */

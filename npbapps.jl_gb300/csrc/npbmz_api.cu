@@ -101,6 +101,10 @@ struct Range {
 
 }  // namespace
 
+struct HandleLimits {
+  static constexpr int MAXB = 3;  // zone-size buckets per sweep direction
+};
+
 struct npbmz_handle {
   int kind = 0, nzones = 0, flags = 0;
   Consts K;
@@ -158,7 +162,14 @@ struct npbmz_handle {
   int cur_group = -1;              // >= 0 while the phases of one group are issued
   cudaStream_t grp_stream[8] = {};
   cudaEvent_t grp_ev[2 * 8 + 1] = {};
-  int tpb_line[3] = {64, 64, 64};
+  // Lines per CTA of the line solves, per sweep direction and zone-size
+  // bucket: zones are split by line length into nbkt buckets per direction
+  // (npbmz_autotune sets 3 and picks each bucket's lines per CTA).
+  int nbkt = 1;
+  std::vector<int> zone_bucket[3];
+  int tpb_bkt[3][HandleLimits::MAXB] = {{64, 64, 64}, {64, 64, 64}, {64, 64, 64}};
+  std::vector<Range> gb_line[3];   // per (group, bucket): slice of the line list
+  int cur_bucket = -1;             // >= 0: line launches of that bucket only
   int64_t nlines[3] = {0, 0, 0};
   // execution
   cudaStream_t stream = nullptr;
@@ -334,6 +345,9 @@ int build_work_lists(npbmz_t* h) {
   return 0;
 }
 
+template <typename Fn>
+int line_launches(npbmz_t* h, int dir, int zone, Fn fn);
+
 // The boundary points of rhs hold the forcing (compute_rhs sets rhs = forcing
 // on the whole cell, src/BT/rhs.jl:85-93, and no solve rewrites them); the
 // rhs kernel only visits interior points, so reset them after an upload.
@@ -345,32 +359,95 @@ int flush_boundary(npbmz_t* h) {
     CKL(h);
   }
   if (h->rdx) {
-    fast::launch_xline_ends(fields(h), h->wline_d[0], h->nwline[0], h->tpb_line[0], h->stream);
-    CKL(h);
+    const Fields F = fields(h);
+    const int saved = h->cur_group;
+    h->cur_group = -1;
+    const int rc = line_launches(h, 0, -1, [&](int lo, int hi, int tpb) {
+      fast::launch_xline_ends(F, h->wline_d[0] + lo, hi - lo, tpb, h->stream);
+      CKL(h);
+      return 0;
+    });
+    h->cur_group = saved;
+    if (rc) return -1;
   }
   h->bnd_dirty = false;
   return 0;
+}
+
+// Zone-size buckets of one sweep direction: zones by decreasing line length
+// cut into nbkt runs of near-equal line counts.
+void assign_buckets(npbmz_t* h, int dir) {
+  const int nz = h->nzones;
+  std::vector<int> order(nz);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return zone_line_len(h->zh[a], dir) > zone_line_len(h->zh[b], dir);
+  });
+  int64_t total = 0;
+  for (int z = 0; z < nz; ++z) total += zone_lines(h->zh[z], dir);
+  h->zone_bucket[dir].assign(nz, 0);
+  int64_t acc = 0;
+  for (int z : order) {
+    h->zone_bucket[dir][z] = (int)std::min<int64_t>(h->nbkt - 1, acc * h->nbkt / std::max<int64_t>(total, 1));
+    acc += zone_lines(h->zh[z], dir);
+  }
 }
 
 int build_line_lists(npbmz_t* h) {
   const int nz = h->nzones;
   for (int dir = 0; dir < 3; ++dir) {
     if (h->wline_d[dir]) { cudaFree(h->wline_d[dir]); h->wline_d[dir] = nullptr; }
-    const std::vector<int> order = group_order(h, [&](int z) { return (int64_t)zone_line_len(h->zh[z], dir); });
-    const int tpb = h->tpb_line[dir];
+    if ((int)h->zone_bucket[dir].size() != nz) assign_buckets(h, dir);
+    const std::vector<int>& bk = h->zone_bucket[dir];
+    // group-major, then bucket, then the longest lines first
+    std::vector<int> order(nz);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      if (h->zone_group[a] != h->zone_group[b]) return h->zone_group[a] < h->zone_group[b];
+      if (bk[a] != bk[b]) return bk[a] < bk[b];
+      return zone_line_len(h->zh[a], dir) > zone_line_len(h->zh[b], dir);
+    });
     std::vector<Work> w;
     h->line_range[dir].assign(nz, Range());
+    h->gb_line[dir].assign((size_t)h->ngroups * h->nbkt, Range());
+    for (Range& r : h->gb_line[dir]) { r.lo = 1 << 30; r.hi = 0; }
     for (int z : order) {
+      const int tpb = h->tpb_bkt[dir][bk[z]];
       const int nl = zone_lines(h->zh[z], dir);
       h->line_range[dir][z].lo = (int)w.size();
       for (int f = 0; f < nl; f += tpb) w.push_back(Work{z, f});
       h->line_range[dir][z].hi = (int)w.size();
+      Range& r = h->gb_line[dir][(size_t)h->zone_group[z] * h->nbkt + bk[z]];
+      r.lo = std::min(r.lo, h->line_range[dir][z].lo);
+      r.hi = std::max(r.hi, h->line_range[dir][z].hi);
     }
+    for (Range& r : h->gb_line[dir])
+      if (r.hi < r.lo) r.lo = r.hi = 0;
     h->nwline[dir] = (int)w.size();
     CK(h, cudaMalloc((void**)&h->wline_d[dir], std::max<size_t>(1, w.size()) * sizeof(Work)));
     CK(h, cudaMemcpy(h->wline_d[dir], w.data(), w.size() * sizeof(Work), cudaMemcpyHostToDevice));
     h->grp_line[dir] = group_ranges(h, h->line_range[dir]);
   }
+  return 0;
+}
+
+// Every launch over a line list goes through here: fn(lo, hi, tpb) for each
+// slice whose work items were built with tpb lines -- one zone, the current
+// zone group or all groups, bucket by bucket (the current bucket only when
+// one is set).
+template <typename Fn>
+int line_launches(npbmz_t* h, int dir, int zone, Fn fn) {
+  if (zone >= 0) {
+    const Range r = h->line_range[dir][zone];
+    return r.hi > r.lo ? fn(r.lo, r.hi, h->tpb_bkt[dir][h->zone_bucket[dir][zone]]) : 0;
+  }
+  const int g0 = h->cur_group >= 0 ? h->cur_group : 0, g1 = h->cur_group >= 0 ? h->cur_group + 1 : h->ngroups;
+  for (int g = g0; g < g1; ++g)
+    for (int b = 0; b < h->nbkt; ++b) {
+      if (h->cur_bucket >= 0 && b != h->cur_bucket) continue;
+      const Range r = h->gb_line[dir][(size_t)g * h->nbkt + b];
+      if (r.hi > r.lo && fn(r.lo, r.hi, h->tpb_bkt[dir][b])) return -1;
+    }
   return 0;
 }
 
@@ -391,7 +468,7 @@ int phase_prim(npbmz_t* h, int zone) {
     int wlo = 0, whi = h->nwpts;
     if (zone >= 0) { wlo = h->pts_range[zone].lo; whi = h->pts_range[zone].hi; }
     else if (h->cur_group >= 0) { wlo = h->grp_pts[h->cur_group].lo; whi = h->grp_pts[h->cur_group].hi; }
-    fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream);
+    fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
   }
   CKL(h);
   return 0;
@@ -404,7 +481,8 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
   if (zone >= 0) { lo = h->int_range[zone].lo; hi = h->int_range[zone].hi; }
   else if (h->cur_group >= 0) { lo = h->grp_int[h->cur_group].lo; hi = h->grp_int[h->cur_group].hi; }
   if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
-  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->lw);
+  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->lw,
+                        (h->flags & NPBMZ_PERSIST) != 0);
   CKL(h);
   return 0;
 }
@@ -418,19 +496,22 @@ void* line_scratch(npbmz_t* h, int dir) {
 
 int phase_solve(npbmz_t* h, int dir, int zone, int add_u, bool fused = false) {
   const Fields F = fields(h);
-  int lo = 0, hi = h->nwline[dir];
-  if (zone >= 0) { lo = h->line_range[dir][zone].lo; hi = h->line_range[dir][zone].hi; }
-  else if (h->cur_group >= 0) { lo = h->grp_line[dir][h->cur_group].lo; hi = h->grp_line[dir][h->cur_group].hi; }
   const bool sp = h->kind == NPBMZ_SP;
-  if (use_exact(h))
-    exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], line_scratch(h, dir),
-                        h->nlines[dir], add_u, nullptr, h->stream);
-  else
-    fast::launch_solve(sp, !use_fp32(h) ? 0 : ((h->flags & NPBMZ_FP32_NOREFINE) ? 1 : ((h->flags & NPBMZ_REFINE_FP64) ? 3 : (fused && h->rdf ? 4 : 2))), dir, F, h->K,
-                       h->wline_d[dir] + lo, hi - lo, h->tpb_line[dir], line_scratch(h, dir), h->nlines[dir], add_u, h->xw,
-                       h->stream);
-  CKL(h);
-  return 0;
+  const int mode = use_exact(h) ? 0
+                   : !use_fp32(h) ? 0
+                   : (h->flags & NPBMZ_FP32_NOREFINE) ? 1
+                   : (h->flags & NPBMZ_REFINE_FP64) ? 3
+                   : (fused && h->rdf ? 4 : 2);
+  return line_launches(h, dir, zone, [&](int lo, int hi, int tpb) {
+    if (use_exact(h))
+      exact::launch_solve(sp, 0, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, tpb, line_scratch(h, dir),
+                          h->nlines[dir], add_u, nullptr, h->stream);
+    else
+      fast::launch_solve(sp, mode, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, tpb, line_scratch(h, dir),
+                         h->nlines[dir], add_u, h->xw, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+    CKL(h);
+    return 0;
+  });
 }
 
 int phase_add(npbmz_t* h, int zone) {
@@ -792,9 +873,13 @@ int adjoint_back_step(npbmz_t* h, double* const x[3], double* ub, double* vb, do
   CKL(h);
   // the sweeps in reverse order
   for (int dir = 2; dir >= 0; --dir) {
-    adj_launch_solve(dir, F, h->K, h->wline_d[dir], h->nwline[dir], h->tpb_line[dir], yb, x[dir], vb, scr,
-                     h->nlines[dir], h->stream);
-    CKL(h);
+    if (line_launches(h, dir, -1, [&](int lo, int hi, int tpb) {
+          adj_launch_solve(dir, F, h->K, h->wline_d[dir] + lo, hi - lo, tpb, yb, x[dir], vb, scr, h->nlines[dir],
+                           h->stream);
+          CKL(h);
+          return 0;
+        }))
+      return -1;
   }
   // compute_rhs (yb is now the adjoint of rhs)
   adj_launch_rhs(F, h->K, h->wpts_d, h->nwpts, yb, vb, fb, h->stream);
@@ -1295,54 +1380,115 @@ int npbmz_synchronize(npbmz_t* h) {
 
 int npbmz_autotune(npbmz_t* h) {
   if (!h) return fail(nullptr, "null handle");
-  // Candidate lines per CTA for each sweep direction; timed on a snapshot of
-  // u so that the handle's state is unchanged afterwards.
+  // 1. Lines per CTA of each sweep direction and zone-size bucket: the zones
+  //    of a direction are split by line length into up to 3 buckets, and each
+  //    bucket's candidates are timed on its own launches.  2. For graph
+  //    handles, the number of zone-group branches of the step graph, timed on
+  //    whole steps.  Timed on a snapshot of u and rhs, restored afterwards.
   const int cand[] = {32, 64, 128};
+  const size_t bytes = 5 * (size_t)h->NP * sizeof(double);
   double* usave = nullptr;
-  CK(h, cudaMalloc(&usave, 5 * h->NP * sizeof(double)));
   double* rsave = nullptr;
-  if (cudaMalloc(&rsave, 5 * h->NP * sizeof(double)) != cudaSuccess) { cudaFree(usave); return fail(h, "autotune alloc"); }
-  cudaMemcpyAsync(usave, h->u, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
-  cudaMemcpyAsync(rsave, h->rhs, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  CK(h, cudaMalloc(&usave, bytes));
+  if (cudaMalloc(&rsave, bytes) != cudaSuccess) { cudaFree(usave); return fail(h, "autotune alloc"); }
+  cudaMemcpyAsync(usave, h->u, bytes, cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(rsave, h->rhs, bytes, cudaMemcpyDeviceToDevice, h->stream);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  auto elapsed = [&]() {
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  drop_graph(h);
   int rc = 0;
-  // prim + rhs once so that the solves read defined data
-  rc |= phase_prim(h, -1);
-  rc |= phase_rhs(h, -1, h->kind == NPBMZ_SP, false);
-  for (int dir = 0; dir < 3 && !rc; ++dir) {
-    float best = 1e30f;
-    int best_tpb = h->tpb_line[dir];
-    for (int c : cand) {
-      h->tpb_line[dir] = c;
-      if (build_line_lists(h)) { rc = -1; break; }
-      // warm-up, then 3 timed repetitions (the solve rewrites rhs in place;
-      // restore it between repetitions)
-      float tot = 0.f;
-      for (int rep = 0; rep < 4 && !rc; ++rep) {
-        cudaMemcpyAsync(h->rhs, rsave, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
-        cudaEventRecord(e0, h->stream);
-        rc |= phase_solve(h, dir, -1, 0);
-        cudaEventRecord(e1, h->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (rep > 0) tot += ms;
-      }
-      if (tot < best) { best = tot; best_tpb = c; }
-    }
-    h->tpb_line[dir] = best_tpb;
+  h->nbkt = std::min(HandleLimits::MAXB, h->nzones);
+  for (int dir = 0; dir < 3; ++dir) {
+    assign_buckets(h, dir);
+    for (int bk = 0; bk < HandleLimits::MAXB; ++bk) h->tpb_bkt[dir][bk] = 64;
   }
+  if (build_line_lists(h)) rc = -1;
+  // prim + rhs once so that the solves read defined data
+  if (!rc) rc = phase_prim(h, -1);
+  if (!rc) rc = phase_rhs(h, -1, h->kind == NPBMZ_SP, false);
+  for (int dir = 0; dir < 3 && !rc; ++dir)
+    for (int bk = 0; bk < h->nbkt && !rc; ++bk) {
+      float best = 1e30f;
+      int best_tpb = h->tpb_bkt[dir][bk];
+      for (int c : cand) {
+        h->tpb_bkt[dir][bk] = c;
+        if (build_line_lists(h)) { rc = -1; break; }
+        h->cur_bucket = bk;
+        float tot = 0.f;
+        for (int rep = 0; rep < 4 && !rc; ++rep) {  // warm-up + 3 timed
+          cudaMemcpyAsync(h->rhs, rsave, bytes, cudaMemcpyDeviceToDevice, h->stream);
+          cudaEventRecord(e0, h->stream);
+          rc |= phase_solve(h, dir, -1, 0, true);
+          cudaEventRecord(e1, h->stream);
+          const float ms = elapsed();
+          if (rep > 0) tot += ms;
+        }
+        h->cur_bucket = -1;
+        if (tot < best) { best = tot; best_tpb = c; }
+      }
+      h->tpb_bkt[dir][bk] = best_tpb;
+    }
   if (!rc) rc = build_line_lists(h);
-  cudaMemcpyAsync(h->u, usave, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
-  cudaMemcpyAsync(h->rhs, rsave, 5 * h->NP * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  // Whole steps decide: the bucket-tuned shapes against one bucket of 64
+  // lines per CTA, then (graph handles) the number of zone-group branches;
+  // each candidate runs 2 + 6 steps from the saved state.
+  auto step_ms = [&]() -> float {
+    cudaMemcpyAsync(h->u, usave, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(h->rhs, rsave, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (npbmz_step(h, 2, nullptr)) return -1.f;
+    cudaEventRecord(e0, h->stream);
+    if (npbmz_step(h, 6, nullptr)) return -1.f;
+    cudaEventRecord(e1, h->stream);
+    return elapsed();
+  };
+  if (!rc) {
+    int tuned[3][HandleLimits::MAXB];
+    std::memcpy(tuned, h->tpb_bkt, sizeof(tuned));
+    const int tuned_nbkt = h->nbkt;
+    drop_graph(h);
+    const float t_tuned = step_ms();
+    h->nbkt = 1;
+    for (int dir = 0; dir < 3; ++dir) { assign_buckets(h, dir); h->tpb_bkt[dir][0] = 64; }
+    drop_graph(h);
+    if (build_line_lists(h)) rc = -1;
+    const float t_plain = rc ? -1.f : step_ms();
+    if (t_tuned < 0.f || t_plain < 0.f) rc = -1;
+    else if (t_tuned < t_plain) {
+      h->nbkt = tuned_nbkt;
+      for (int dir = 0; dir < 3; ++dir) assign_buckets(h, dir);
+      std::memcpy(h->tpb_bkt, tuned, sizeof(tuned));
+      drop_graph(h);
+      if (build_line_lists(h)) rc = -1;
+    }
+  }
+  if (!rc && (h->flags & NPBMZ_GRAPH) && !(h->flags & (NPBMZ_EXACT | NPBMZ_PERZONE)) && h->nzones >= 8) {
+    const int gcand[] = {1, 2, 4, 6};
+    float best = 1e30f;
+    int best_g = h->ngroups;
+    for (int G : gcand) {
+      if (G > h->nzones || npbmz_set_step_groups(h, G)) continue;
+      const float ms = step_ms();
+      if (ms < 0.f) { rc = -1; break; }
+      if (ms < best) { best = ms; best_g = G; }
+    }
+    if (!rc) rc = npbmz_set_step_groups(h, best_g);
+  }
+  cudaMemcpyAsync(h->u, usave, bytes, cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(h->rhs, rsave, bytes, cudaMemcpyDeviceToDevice, h->stream);
   cudaStreamSynchronize(h->stream);
   cudaFree(usave);
   cudaFree(rsave);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   drop_graph(h);
+  h->launches_per_step = count_launches(h);
   return rc ? -1 : 0;
 }
 
@@ -1355,11 +1501,18 @@ int npbmz_launches_per_step(npbmz_t* h) { return h ? h->launches_per_step : -1; 
 int64_t npbmz_device_bytes(npbmz_t* h) { return h ? h->device_bytes : -1; }
 
 int npbmz_describe(npbmz_t* h, char* buf, size_t n) {
-  if (!h || !buf || n == 0) return -1;
-  snprintf(buf, n, "{\"kind\":\"%s\",\"zones\":%d,\"points\":%lld,\"flags\":%d,\"tpb_line\":[%d,%d,%d],"
-                   "\"launches_per_step\":%d,\"device_bytes\":%lld}",
-           h->kind == NPBMZ_BT ? "BT" : "SP", h->nzones, (long long)h->NP, h->flags, h->tpb_line[0], h->tpb_line[1],
-           h->tpb_line[2], h->launches_per_step, (long long)h->device_bytes);
+  if (!h || !buf || n == 0) return fail(h, "bad arguments");
+  std::string tp = "[";
+  for (int d = 0; d < 3; ++d) {
+    tp += d ? ",[" : "[";
+    for (int b = 0; b < h->nbkt; ++b) tp += (b ? "," : "") + std::to_string(h->tpb_bkt[d][b]);
+    tp += "]";
+  }
+  tp += "]";
+  snprintf(buf, n, "{\"kind\":\"%s\",\"zones\":%d,\"points\":%lld,\"flags\":%d,\"lines_per_cta\":%s,"
+           "\"zone_size_buckets\":%d,\"step_groups\":%d,\"launches_per_step\":%d,\"device_bytes\":%lld}",
+           h->kind == NPBMZ_BT ? "BT" : "SP", h->nzones, (long long)h->NP, h->flags, tp.c_str(), h->nbkt, h->ngroups,
+           h->launches_per_step, (long long)h->device_bytes);
   return 0;
 }
 

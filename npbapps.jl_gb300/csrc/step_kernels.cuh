@@ -102,13 +102,18 @@ __global__ void __launch_bounds__(256) k_prim(Fields F, Consts K, int64_t lo, in
 
 // Over the point work list (zone known): also the x-line-major state copy.
 template <bool SP>
-__global__ void __launch_bounds__(128) k_prim_w(Fields F, Consts K, const Work* __restrict__ work) {
-  const Work w = work[blockIdx.x];
-  const ZoneDev Z = F.zones[w.zone];
-  const int q = w.first + threadIdx.x;
-  if (q >= Z.nx * Z.ny * Z.nz) return;
-  const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
-  prim_point<SP>(F, K, Z.off + q, xline_of(Z, j, k), i);
+// Work-item loop (here and in the other kernels of the batched FMA step):
+// CTA b takes items b, b + gridDim.x, ...; launched with one CTA per item, or
+// as a persistent kernel with as many CTAs as fit on the SMs (NPBMZ_PERSIST).
+__global__ void __launch_bounds__(128) k_prim_w(Fields F, Consts K, const Work* __restrict__ work, int nwork) {
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
+    const Work w = work[it];
+    const ZoneDev Z = F.zones[w.zone];
+    const int q = w.first + threadIdx.x;
+    if (q >= Z.nx * Z.ny * Z.nz) continue;
+    const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
+    prim_point<SP>(F, K, Z.off + q, xline_of(Z, j, k), i);
+  }
 }
 
 // ============================================================================
@@ -334,12 +339,13 @@ __device__ __forceinline__ void rhs_dir(double r[5], const double* __restrict__ 
 
 template <bool TX, bool NORM>
 __global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, LinWeights LW, const Work* __restrict__ work,
-                                                  double* __restrict__ partials) {
+                                                  int nwork, double* __restrict__ partials) {
   __shared__ double red[5 * 128];
   __shared__ double wt[3 * 32 * 5];
   for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&LW.w[0][0][0])[e];
   __syncthreads();
-  const Work w = work[blockIdx.x];
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
+  const Work w = work[it];
   const ZoneDev Z = F.zones[w.zone];
   const int64_t NP = F.NP;
   const int ix = Z.nx - 2, iy = Z.ny - 2;
@@ -416,7 +422,8 @@ __global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, LinWeights
   if (NORM) {
     block_sum5(sq, red);
     if (threadIdx.x == 0)
-      for (int m = 0; m < 5; ++m) partials[blockIdx.x * 5 + m] = sq[m];
+      for (int m = 0; m < 5; ++m) partials[it * 5 + m] = sq[m];
+  }
   }
 }
 
@@ -1447,10 +1454,9 @@ __host__ __device__ constexpr size_t pl_refine_smem(int tpb, bool out_df) {
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(128) k_bt_mixed_pl(Fields F, Consts K, const Work* __restrict__ work,
-                                                     float* __restrict__ scr, int64_t nlt, float* __restrict__ x0) {
-  extern __shared__ __align__(16) unsigned char pl_smem[];
-  const Work w = work[blockIdx.x];
+__device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& K, const Work w,
+                                                 float* __restrict__ scr, int64_t nlt, float* __restrict__ x0,
+                                                 unsigned char* pl_smem) {
   const ZoneDev Z = F.zones[w.zone];
   const int line = w.first + threadIdx.x;
   if (line >= zone_lines(Z, DIR)) return;
@@ -1546,12 +1552,17 @@ __global__ void __launch_bounds__(128) k_bt_mixed_pl(Fields F, Consts K, const W
   cpa_wait<0>();
 }
 
-template <int DIR, bool OUT_DF>
-__global__ void __launch_bounds__(128) k_bt_refine_pl(Fields F, Consts K, const Work* __restrict__ work,
-                                                      float* __restrict__ scr, int64_t nlt, int add_u,
-                                                      const float* __restrict__ x0f) {
+template <int DIR>
+__global__ void __launch_bounds__(128) k_bt_mixed_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
+                                                     float* __restrict__ scr, int64_t nlt, float* __restrict__ x0) {
   extern __shared__ __align__(16) unsigned char pl_smem[];
-  const Work w = work[blockIdx.x];
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) bt_mixed_pl_item<DIR>(F, K, work[it], scr, nlt, x0, pl_smem);
+}
+
+template <int DIR, bool OUT_DF>
+__device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts& K, const Work w,
+                                                  float* __restrict__ scr, int64_t nlt, int add_u,
+                                                  const float* __restrict__ x0f, unsigned char* pl_smem) {
   const ZoneDev Z = F.zones[w.zone];
   const int line = w.first + threadIdx.x;
   if (line >= zone_lines(Z, DIR)) return;
@@ -1740,6 +1751,15 @@ __global__ void __launch_bounds__(128) k_bt_refine_pl(Fields F, Consts K, const 
     }
   }
   cpa_wait<0>();
+}
+
+template <int DIR, bool OUT_DF>
+__global__ void __launch_bounds__(128) k_bt_refine_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
+                                                      float* __restrict__ scr, int64_t nlt, int add_u,
+                                                      const float* __restrict__ x0f) {
+  extern __shared__ __align__(16) unsigned char pl_smem[];
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x)
+    bt_refine_pl_item<DIR, OUT_DF>(F, K, work[it], scr, nlt, add_u, x0f, pl_smem);
 }
 #endif  // NPBMZ_HAS_FP32
 
@@ -2315,10 +2335,22 @@ __global__ void __launch_bounds__(128) k_add(Fields F, const Work* __restrict__ 
 // ============================================================================
 // host-side launchers (declared in step_launch.h)
 // ============================================================================
-void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s) {
+// Grid of a work-item kernel: one CTA per item, or (persistent) as many CTAs
+// as fit on the device at once, each looping over items.
+static int item_grid(const void* f, int nwork, int tpb, size_t smem, bool persist) {
+  if (!persist) return nwork;
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, tpb, smem) != cudaSuccess || per < 1) per = 1;
+  return nwork < per * sms ? nwork : per * sms;
+}
+
+void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s,
+                   bool persist) {
   if (nwork <= 0) return;
-  if (sp) k_prim_w<true><<<nwork, 128, 0, s>>>(F, K, work);
-  else k_prim_w<false><<<nwork, 128, 0, s>>>(F, K, work);
+  if (sp) k_prim_w<true><<<item_grid((const void*)k_prim_w<true>, nwork, 128, 0, persist), 128, 0, s>>>(F, K, work, nwork);
+  else k_prim_w<false><<<item_grid((const void*)k_prim_w<false>, nwork, 128, 0, persist), 128, 0, s>>>(F, K, work, nwork);
 }
 
 void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s) {
@@ -2330,17 +2362,21 @@ void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t 
 }
 
 void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork, double* partials,
-                cudaStream_t s, const LinWeights* lw) {
+                cudaStream_t s, const LinWeights* lw, bool persist) {
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
   if (F.flux && lw) {
+#define NPBMZ_RHS_FLUX(A, B)                                                                                  \
+  k_rhs_flux<A, B><<<item_grid((const void*)k_rhs_flux<A, B>, nwork, 128, 0, persist), 128, 0, s>>>(F, K, *lw, work, \
+                                                                                                  nwork, partials)
     if (tx) {
-      if (norm) k_rhs_flux<true, true><<<nwork, 128, 0, s>>>(F, K, *lw, work, partials);
-      else k_rhs_flux<true, false><<<nwork, 128, 0, s>>>(F, K, *lw, work, partials);
+      if (norm) NPBMZ_RHS_FLUX(true, true);
+      else NPBMZ_RHS_FLUX(true, false);
     } else {
-      if (norm) k_rhs_flux<false, true><<<nwork, 128, 0, s>>>(F, K, *lw, work, partials);
-      else k_rhs_flux<false, false><<<nwork, 128, 0, s>>>(F, K, *lw, work, partials);
+      if (norm) NPBMZ_RHS_FLUX(false, true);
+      else NPBMZ_RHS_FLUX(false, false);
     }
+#undef NPBMZ_RHS_FLUX
     return;
   }
 #endif
@@ -2372,7 +2408,7 @@ static void launch_solve_t(bool sp, int dir, const Fields& F, const Consts& K, c
 // double-float residual (BT; SP: FP64 residual); 3: FP32 + refinement with
 // an FP64 residual (xw: a [5][NP] buffer for the first solution).
 void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb,
-                  void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s) {
+                  void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s, bool persist) {
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
   if (mode == 1) { launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s); return; }
@@ -2383,16 +2419,17 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
     float* scr = reinterpret_cast<float*>(scratch);
     float* x0 = reinterpret_cast<float*>(xw);
     const size_t sm_m = pl_mixed_smem(tpb), sm_r = pl_refine_smem(tpb, dir != 2);
-    if (dir == 0) {
-      k_bt_mixed_pl<0><<<nwork, tpb, sm_m, s>>>(F, K, work, scr, nlt, x0);
-      k_bt_refine_pl<0, true><<<nwork, tpb, sm_r, s>>>(F, K, work, scr, nlt, add_u, x0);
-    } else if (dir == 1) {
-      k_bt_mixed_pl<1><<<nwork, tpb, sm_m, s>>>(F, K, work, scr, nlt, x0);
-      k_bt_refine_pl<1, true><<<nwork, tpb, sm_r, s>>>(F, K, work, scr, nlt, add_u, x0);
-    } else {
-      k_bt_mixed_pl<2><<<nwork, tpb, sm_m, s>>>(F, K, work, scr, nlt, x0);
-      k_bt_refine_pl<2, false><<<nwork, tpb, sm_r, s>>>(F, K, work, scr, nlt, add_u, x0);
-    }
+#define NPBMZ_PL(D, OD)                                                                                          \
+  do {                                                                                                           \
+    k_bt_mixed_pl<D><<<item_grid((const void*)k_bt_mixed_pl<D>, nwork, tpb, sm_m, persist), tpb, sm_m, s>>>(       \
+        F, K, work, nwork, scr, nlt, x0);                                                                        \
+    k_bt_refine_pl<D, OD><<<item_grid((const void*)k_bt_refine_pl<D, OD>, nwork, tpb, sm_r, persist), tpb, sm_r,   \
+                            s>>>(F, K, work, nwork, scr, nlt, add_u, x0);                                        \
+  } while (0)
+    if (dir == 0) NPBMZ_PL(0, true);
+    else if (dir == 1) NPBMZ_PL(1, true);
+    else NPBMZ_PL(2, false);
+#undef NPBMZ_PL
     return;
   }
   if (mode == 4) mode = 2;

@@ -10,11 +10,13 @@ namespace npbmz {
 #define NPBMZ_DECLARE_LAUNCHERS(NS)                                                                                  \
   namespace NS {                                                                                                     \
   void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t hi, cudaStream_t s);                                   \
-  void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s);       \
+  void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s,        \
+                     bool persist = false);                                                                          \
   void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork,                 \
-                  double* partials, cudaStream_t s, const LinWeights* lw = nullptr);                                 \
+                  double* partials, cudaStream_t s, const LinWeights* lw = nullptr, bool persist = false);           \
   void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork,       \
-                    int tpb, void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s);                     \
+                    int tpb, void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s,                      \
+                    bool persist = false);                                                                           \
   void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s);                                     \
   }
 NPBMZ_DECLARE_LAUNCHERS(exact)

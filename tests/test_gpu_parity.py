@@ -203,6 +203,25 @@ def test_zone_group_graph_equals_direct_launches(flags, groups):
     np.testing.assert_array_equal(np.concatenate(a.verify()), np.concatenate(b.verify()))
 
 
+@pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.GRAPH], ids=["fp64", "mixed", "mixed-graph"])
+def test_persistent_kernels_equal_one_cta_per_item(flags):
+    """NPBMZ_PERSIST: the same work items looped over by a resident grid --
+    bit-identical u and per-step norms."""
+    geom, dt, _ = geom_class("BT", "W")
+    ce = seeded(geom)
+    a = npbmz.Problem(geom, dt, flags)
+    b = npbmz.Problem(geom, dt, flags | npbmz.PERSIST)
+    a.setup(ce)
+    b.setup(ce)
+    a.step(4)
+    b.step(4)
+    na = a.step(2, norms=True)
+    nb = b.step(2, norms=True)
+    np.testing.assert_array_equal(na, nb)
+    for z in range(geom.nzones):
+        np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
+
+
 def test_reference_layout_round_trip():
     """Upload u in the reference's OffsetArray memory layout, download it dense
     and in the reference layout again (halo untouched)."""
@@ -328,16 +347,28 @@ def test_config2_bt_class_b_final_norms(oracle_mod, flags, rel):
     np.testing.assert_allclose(xg, xo, rtol=rel, atol=0)
 
 
-def test_config2_autotuned_launch_shapes_keep_results(oracle_mod):
+@pytest.mark.parametrize("flags", [0, npbmz.MIXED | npbmz.GRAPH], ids=["fp64", "mixed-graph"])
+def test_config2_autotuned_launch_shapes_keep_results(oracle_mod, flags):
+    """The autotuner (lines per CTA per sweep direction and zone-size bucket;
+    zone-group branches for graph handles) changes launch shapes only: the
+    state it leaves is the one it found, and later steps are bit-identical
+    to untuned direct launches."""
     geom, dt, niter = geom_class("BT", "B")
     ce = seeded(geom)
-    a = npbmz.Problem(geom, dt, 0)
+    a = npbmz.Problem(geom, dt, flags)
     a.setup(ce)
+    u_before = [a.download(npbmz.U, z) for z in range(geom.nzones)]
     a.autotune()
-    a.setup(ce)
-    b = npbmz.Problem(geom, dt, 0)
+    d = a.describe()
+    assert d["zone_size_buckets"] in (1, 3) and len(d["lines_per_cta"]) == 3
+    assert all(len(per_dir) == d["zone_size_buckets"] for per_dir in d["lines_per_cta"])
+    assert all(t in (32, 64, 128) for per_dir in d["lines_per_cta"] for t in per_dir)
+    for z in range(geom.nzones):
+        np.testing.assert_array_equal(a.download(npbmz.U, z), u_before[z])
+    b = npbmz.Problem(geom, dt, flags & ~npbmz.GRAPH)
     b.setup(ce)
     a.step(5)
     b.step(5)
+    a.synchronize()
     for z in range(0, geom.nzones, 7):
         np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
