@@ -37,6 +37,7 @@ mutable struct Problem
     handle::Ptr{Cvoid}
     kind::Cint
     nzones::Int
+    lock::ReentrantLock          # serialises calls on the handle (adi from Threads.@threads)
     function Problem(kind, nx::Vector{<:Integer}, ny, nz, nbr, dt, gx, gy, gz, x_zones, y_zones; flags = Cint(0))
         n = length(nx)
         # nbr: 4 per zone (west, east, south, north), 0-based zone numbers
@@ -46,7 +47,7 @@ mutable struct Problem
                    (Cint, Cint, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cdouble}, Cint, Ptr{Ptr{Cvoid}}),
                    kind, n, Cint.(nx), Cint.(ny), Cint.(nz), Cint.(nbr), params, flags, out)
         rc == 0 || error("npbmz_create: " * unsafe_string(ccall((:npbmz_last_error, libnpbmz), Cstring, (Ptr{Cvoid},), C_NULL)))
-        p = new(out[], Cint(kind), n)
+        p = new(out[], Cint(kind), n, ReentrantLock())
         finalizer(p) do q
             q.handle != C_NULL && ccall((:npbmz_destroy, libnpbmz), Cint, (Ptr{Cvoid},), q.handle)
             q.handle = C_NULL
@@ -157,5 +158,21 @@ function terminal_objective(p::Problem, forcing::Vector{Float64}, u0::Vector{Flo
     upload_all!(p, U, u0)
     return 0.5 * sum(abs2, a)
 end
+
+"""
+One zone's field held on the GPU.  Vectors of these stand in for the
+reference's per-zone arrays u, rhs, forcing in its node loop, so that its own
+adi / exch_qbc calls reach the GPU methods of NPBAppsGPUShim.jl.
+"""
+struct DeviceZone
+    p::Problem
+    zone::Int        # 1-based
+    field::Cint
+end
+
+device_zones(p::Problem, field) = [DeviceZone(p, iz, Cint(field)) for iz in 1:p.nzones]
+
+"""adi of one zone under the handle's lock (the reference calls adi from Threads.@threads)."""
+adi_locked!(p::Problem, iz::Integer) = lock(() -> adi!(p, iz), p.lock)
 
 end # module
