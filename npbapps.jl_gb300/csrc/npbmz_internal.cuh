@@ -105,6 +105,35 @@ struct LinWeights {
   double w[3][32][5];
 };
 
+// FP64 value -> FP32 pair (hi = rn(v), lo = rn(v - hi)), the same bits as the
+// conversions __double2float_rn(v) and __double2float_rn(v - (double)hi),
+// formed with integer operations from v's bit pattern: on GB300 each FP64
+// conversion or subtraction takes a slot of the 1/64-rate FP64 pipe, and the
+// kernels that split are FP64-pipe bound.  hi keeps the top 24 significand
+// bits rounded to nearest even; the 29 bits below (minus 2^29 when hi rounded
+// up) are the exact v - hi in units of 2^(e-52), converted to float (one
+// rounding) and scaled by that power of two (exact while 2^(e-52) is a normal
+// float, e >= -74).  Outside -74 <= e <= 126 (zero, subnormal, tiny, huge,
+// inf, nan) it falls back to the conversions.
+__device__ __forceinline__ void split_df(double v, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ffull) - 1023;
+  if (e < -74 || e > 126) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+    return;
+  }
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned long long man = b & 0xfffffffffffffull;
+  const unsigned r = (unsigned)(man & 0x1fffffffull);    // the 29 bits below hi
+  const unsigned mhi = (unsigned)(man >> 29);             // 23 stored bits of hi
+  const bool up = r > 0x10000000u || (r == 0x10000000u && (mhi & 1u));
+  hi = __uint_as_float(sign | ((((unsigned)(e + 127) << 23) | mhi) + (up ? 1u : 0u)));
+  const int L = up ? (int)r - 0x20000000 : (int)r;       // v - hi = L * 2^(e-52), |L| <= 2^28
+  const float mag = (float)L * __int_as_float((e - 52 + 127) << 23);
+  lo = sign ? -mag : mag;
+}
+
 // Lines per sweep direction of a zone (interior transverse indices only).
 __host__ __device__ inline int zone_lines(const ZoneDev& z, int dir) {
   return dir == 0 ? (z.ny - 2) * (z.nz - 2) : (dir == 1 ? (z.nx - 2) * (z.nz - 2) : (z.nx - 2) * (z.ny - 2));

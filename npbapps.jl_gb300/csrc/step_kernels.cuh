@@ -57,8 +57,8 @@ __device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int
       const double v[PF_HI_COUNT] = {rho_inv, square * rho_inv, u2, u3, u4, F.u[4 * NP + p]};
 #pragma unroll
       for (int e = 0; e < PF_HI_COUNT; ++e) {
-        const float hi = __double2float_rn(v[e]);
-        const float lo = __double2float_rn(v[e] - (double)hi);
+        float hi, lo;
+        split_df(v[e], hi, lo);
         F.primf[e * NP + p] = hi;
         F.primf[(PF_HI_COUNT + e) * NP + p] = lo;
         if (F.pfx && xl >= 0) {
@@ -406,16 +406,18 @@ __global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, LinWeights
       const int64_t xl = xline_of(Z, j, k);
 #pragma unroll
       for (int m = 0; m < 5; ++m) {
-        const float hi = __double2float_rn(r[m]);
+        float hi, lo;
+        split_df(r[m], hi, lo);
         F.rdx[((int64_t)i * 10 + m) * F.nlx + xl] = hi;
-        F.rdx[((int64_t)i * 10 + 5 + m) * F.nlx + xl] = __double2float_rn(r[m] - (double)hi);
+        F.rdx[((int64_t)i * 10 + 5 + m) * F.nlx + xl] = lo;
       }
     } else if (F.rdf) {
 #pragma unroll
       for (int m = 0; m < 5; ++m) {
-        const float hi = __double2float_rn(r[m]);
+        float hi, lo;
+        split_df(r[m], hi, lo);
         F.rdf[m * NP + p] = hi;
-        F.rdf[(5 + m) * NP + p] = __double2float_rn(r[m] - (double)hi);
+        F.rdf[(5 + m) * NP + p] = lo;
       }
     }
   }
