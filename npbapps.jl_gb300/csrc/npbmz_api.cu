@@ -441,6 +441,8 @@ int line_launches(npbmz_t* h, int dir, int zone, Fn fn) {
     const Range r = h->line_range[dir][zone];
     return r.hi > r.lo ? fn(r.lo, r.hi, h->tpb_bkt[dir][h->zone_bucket[dir][zone]]) : 0;
   }
+  if (h->cur_group < 0 && h->cur_bucket < 0 && h->nbkt == 1)  // one shape: the whole list in one launch
+    return h->nwline[dir] > 0 ? fn(0, h->nwline[dir], h->tpb_bkt[dir][0]) : 0;
   const int g0 = h->cur_group >= 0 ? h->cur_group : 0, g1 = h->cur_group >= 0 ? h->cur_group + 1 : h->ngroups;
   for (int g = g0; g < g1; ++g)
     for (int b = 0; b < h->nbkt; ++b) {

@@ -322,12 +322,11 @@ __device__ __forceinline__ void rhs_dir(double r[5], const double* __restrict__ 
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
     const double* um = u + m * NP;
-    double s = w1 * um[p - st];
+    double s = fma(w1, um[p - st], r[m]);
     s = fma(w3, um[p + st], s);
     s = fma(w2, um[p], s);
     s = fma(w0, um[pm2], s);
-    s = fma(w4, um[pp2], s);
-    r[m] += s;
+    r[m] = fma(w4, um[pp2], s);
   }
   r[0] -= t2 * (un[p + st] - un[p - st]);
 #pragma unroll
