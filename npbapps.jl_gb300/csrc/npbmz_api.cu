@@ -1122,7 +1122,7 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? (int)PF_COUNT : (int)PS_COUNT) * h->NP);
   if (!(variant_flags & NPBMZ_EXACT) && make_lin_weights(h->K, h->lw)) {
     rc |= dalloc(h, &h->flux, (size_t)PX_COUNT * h->NP);
-    if (kind == NPBMZ_BT && refined && !(variant_flags & NPBMZ_REFINE_FP64)) {
+    if (refined && !(variant_flags & NPBMZ_REFINE_FP64)) {
       rc |= dalloc(h, &h->rdf, 10 * (size_t)h->NP);
       int maxnx = 0;
       for (int z = 0; z < nzones; ++z) maxnx = std::max(maxnx, nx[z]);

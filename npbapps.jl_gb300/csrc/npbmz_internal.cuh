@@ -50,8 +50,9 @@ enum { PR_RHOI = 0, PR_US, PR_VS, PR_WS, PR_QS, PR_SQUARE, PR_SPEED, PR_AINV, PR
 // 0..5 hold the rounded values (hi), planes 6..11 the remainders (lo), so
 // that hi + lo carries the FP64 value to about 48 bits (double-float).
 enum { PF_RHOI = 0, PF_QS, PF_U2, PF_U3, PF_U4, PF_U5, PF_HI_COUNT, PF_COUNT = 2 * PF_HI_COUNT };
-// SP: FP32 copies of 1/rho, the three velocities and the speed of sound.
-enum { PS_RHOI = 0, PS_US, PS_VS, PS_WS, PS_SPEED, PS_COUNT };
+// SP: FP32 copies of 1/rho, the three velocities and the speed of sound:
+// planes 0..4 the rounded values (hi), 5..9 the remainders (lo).
+enum { PS_RHOI = 0, PS_US, PS_VS, PS_WS, PS_SPEED, PS_HI_COUNT, PS_COUNT = 2 * PS_HI_COUNT };
 
 // Point functions of compute_rhs written by the primitive kernel of the FMA
 // build (one value per point, shared by both neighbours that difference it):

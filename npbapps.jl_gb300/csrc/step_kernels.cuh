@@ -48,11 +48,18 @@ __device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int
       F.prim[PR_AINV * NP + p] = 1.0e0 / aux;
     }
     if (SP && F.primf) {
-      F.primf[PS_RHOI * NP + p] = (float)rho_inv;
-      F.primf[PS_US * NP + p] = (float)(u2 * rho_inv);
-      F.primf[PS_VS * NP + p] = (float)(u3 * rho_inv);
-      F.primf[PS_WS * NP + p] = (float)(u4 * rho_inv);
-      F.primf[PS_SPEED * NP + p] = (float)F.prim[PR_SPEED * NP + p];
+      const double v[PS_HI_COUNT] = {rho_inv, u2 * rho_inv, u3 * rho_inv, u4 * rho_inv, F.prim[PR_SPEED * NP + p]};
+#pragma unroll
+      for (int e = 0; e < PS_HI_COUNT; ++e) {
+        float hi, lo;
+        split_df(v[e], hi, lo);
+        F.primf[e * NP + p] = hi;
+        F.primf[(PS_HI_COUNT + e) * NP + p] = lo;
+        if (F.pfx && xl >= 0) {
+          F.pfx[((int64_t)xi * PS_COUNT + e) * F.nlx + xl] = hi;
+          F.pfx[((int64_t)xi * PS_COUNT + PS_HI_COUNT + e) * F.nlx + xl] = lo;
+        }
+      }
     } else if (F.primf) {
       const double v[PF_HI_COUNT] = {rho_inv, square * rho_inv, u2, u3, u4, F.u[4 * NP + p]};
 #pragma unroll
@@ -2318,6 +2325,10 @@ __global__ void __launch_bounds__(128) k_sp_refine(Fields F, Consts K, const Wor
   });
 }
 
+#if NPBMZ_HAS_FP32
+#include "sp_pipelined.cuh"
+#endif
+
 // ============================================================================
 // add (src/BT/add.jl:5-24, src/SP/add.jl:6-26) as a separate phase.
 // ============================================================================
@@ -2413,6 +2424,25 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
   if (mode == 1) { launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s); return; }
+  if (mode == 4 && sp) {
+    // one fused step, SP: the pipelined passes with a double-float residual;
+    // x and y hand their transformed results on as double-float
+    float* scr = reinterpret_cast<float*>(scratch);
+    float* x0 = reinterpret_cast<float*>(xw);
+    const size_t sm_m = pls_mixed_smem(tpb), sm_r = pls_refine_smem(tpb, dir != 2);
+#define NPBMZ_SPL(D, OD)                                                                                          \
+  do {                                                                                                            \
+    k_sp_mixed_pl<D><<<item_grid((const void*)k_sp_mixed_pl<D>, nwork, tpb, sm_m, persist), tpb, sm_m, s>>>(       \
+        F, K, work, nwork, scr, nlt, x0);                                                                         \
+    k_sp_refine_pl<D, OD><<<item_grid((const void*)k_sp_refine_pl<D, OD>, nwork, tpb, sm_r, persist), tpb, sm_r,   \
+                            s>>>(F, K, work, nwork, scr, nlt, add_u, x0);                                         \
+  } while (0)
+    if (dir == 0) NPBMZ_SPL(0, true);
+    else if (dir == 1) NPBMZ_SPL(1, true);
+    else NPBMZ_SPL(2, false);
+#undef NPBMZ_SPL
+    return;
+  }
   if (mode == 4 && !sp) {
     // one fused step: b of the x sweep comes from compute_rhs's double-float
     // copy, x and y hand their results on as double-float, z writes FP64
@@ -2478,7 +2508,8 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
 // Opt the pipelined sweeps into their dynamic shared memory (above 48 KB for
 // 128 threads per CTA); called once per handle, outside any stream capture.
 int configure_kernels() {
-  const int cap = (int)pl_refine_smem(128, false);
+  const size_t bt_cap = pl_refine_smem(128, false), sp_cap = pls_refine_smem(128, false);
+  const int cap = (int)(bt_cap > sp_cap ? bt_cap : sp_cap);
   cudaError_t e = cudaSuccess;
   auto set = [&](const void* f) {
     const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
@@ -2490,6 +2521,12 @@ int configure_kernels() {
   set((const void*)k_bt_refine_pl<0, true>);
   set((const void*)k_bt_refine_pl<1, true>);
   set((const void*)k_bt_refine_pl<2, false>);
+  set((const void*)k_sp_mixed_pl<0>);
+  set((const void*)k_sp_mixed_pl<1>);
+  set((const void*)k_sp_mixed_pl<2>);
+  set((const void*)k_sp_refine_pl<0, true>);
+  set((const void*)k_sp_refine_pl<1, true>);
+  set((const void*)k_sp_refine_pl<2, false>);
   return e == cudaSuccess ? 0 : -1;
 }
 

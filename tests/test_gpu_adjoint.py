@@ -239,6 +239,6 @@ def test_torch_autograd_function(config3):
     u = torch.tensor(u0, requires_grad=True)
     J = terminal_objective(p, f, u, torch.tensor(p.flatten(target)), nsteps)
     (2.0 * J).backward()
-    assert float(J) == J0
+    assert float(J.detach()) == J0
     np.testing.assert_array_equal(f.grad.numpy(), 2.0 * p.flatten(gf))
     np.testing.assert_array_equal(u.grad.numpy(), 2.0 * p.flatten(gu))

@@ -182,13 +182,14 @@ def test_graph_replay_equals_direct_launches():
         np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
 
 
+@pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("groups", [2, 3, 5])
-def test_zone_group_graph_equals_direct_launches(flags, groups):
+def test_zone_group_graph_equals_direct_launches(kind, flags, groups):
     """The step graph with zone-group branches (npbmz_set_step_groups) runs the
     same kernels per zone: bit-identical to direct launches of the batched
-    step, on uneven zones (BT class W geometry, 16 zones)."""
-    geom, dt, _ = geom_class("BT", "W")
+    step (class W geometry, 16 zones; uneven for BT)."""
+    geom, dt, _ = geom_class(kind, "W")
     ce = seeded(geom)
     a = npbmz.Problem(geom, dt, flags)
     b = npbmz.Problem(geom, dt, flags | npbmz.GRAPH)
@@ -203,11 +204,12 @@ def test_zone_group_graph_equals_direct_launches(flags, groups):
     np.testing.assert_array_equal(np.concatenate(a.verify()), np.concatenate(b.verify()))
 
 
+@pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.GRAPH], ids=["fp64", "mixed", "mixed-graph"])
-def test_persistent_kernels_equal_one_cta_per_item(flags):
+def test_persistent_kernels_equal_one_cta_per_item(kind, flags):
     """NPBMZ_PERSIST: the same work items looped over by a resident grid --
     bit-identical u and per-step norms."""
-    geom, dt, _ = geom_class("BT", "W")
+    geom, dt, _ = geom_class(kind, "W")
     ce = seeded(geom)
     a = npbmz.Problem(geom, dt, flags)
     b = npbmz.Problem(geom, dt, flags | npbmz.PERSIST)
