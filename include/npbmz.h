@@ -49,7 +49,9 @@ typedef struct npbmz_handle npbmz_t;
                               reference's arithmetic */
 #define NPBMZ_MIXED   0x2  /* line solves in FP32 on the FP64 rhs, refined once
                               against a residual of the line operator formed in
-                              double-float (BT) or FP64 (SP); compute_rhs, add,
+                              double-float (FP32 pairs, about 48 bits) -- in
+                              FP64 for single phases (npbmz_phase) and for SP
+                              with NPBMZ_REFINE_FP64; compute_rhs, add,
                               exch_qbc and the norms stay FP64 */
 #define NPBMZ_PERZONE 0x4  /* one launch per zone per phase, the reference's
                               per-zone adi order; default is all zones batched
@@ -60,9 +62,8 @@ typedef struct npbmz_handle npbmz_t;
                               persistent: as many CTAs as fit on the SMs at
                               once, each looping over zone x point or
                               zone x line work items; results are unchanged */
-#define NPBMZ_REFINE_FP64 0x40 /* with NPBMZ_MIXED on BT: the refinement residual
-                              in FP64 instead of double-float (FP32 pairs,
-                              about 48 bits) */
+#define NPBMZ_REFINE_FP64 0x40 /* with NPBMZ_MIXED: the refinement residual in
+                              FP64 instead of double-float */
 #define NPBMZ_FP32_NOREFINE 0x20 /* FP32 line solves without the refinement
                               pass (the error of plain FP32 solves, for
                               comparison); implies NPBMZ_MIXED */
