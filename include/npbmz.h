@@ -58,7 +58,7 @@ typedef struct npbmz_handle npbmz_t;
                               in one launch per phase */
 #define NPBMZ_GRAPH   0x8  /* npbmz_step replays one captured CUDA graph per step */
 #define NPBMZ_PERSIST 0x10 /* the batched step's primitive, compute_rhs and
-                              pipelined FP32 BT sweep kernels (FMA build) run
+                              pipelined FP32 sweep kernels (FMA build) run
                               persistent: as many CTAs as fit on the SMs at
                               once, each looping over zone x point or
                               zone x line work items; results are unchanged */
