@@ -40,6 +40,7 @@ WORKLOADS = {
     "bt-c": ("BT", "C", "BT-MZ 480x320x28, 16x16 geometric zones (area ratio 20.8), dt 1e-4"),
     "sp-c": ("SP", "C", "SP-MZ 480x320x28, 16x16 equal zones (30x20x28), dt 6.7e-4"),
     "bt-b": ("BT", "B", "BT-MZ 304x208x17, 8x8 geometric zones (area ratio 20.05), dt 3e-4"),
+    "sp-b": ("SP", "B", "SP-MZ 304x208x17, 8x8 equal zones (38x26x17), dt 1e-3"),
     "sp-a": ("SP", "A", "SP-MZ 128x128x16, 4x4 equal zones (32x32x16), dt 1.5e-3"),
 }
 SEED = 20261203
@@ -50,9 +51,14 @@ SEED = 20261203
 BYTES_PER_POINT = {"prim": 40.0, "rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
 # Kernels of each phase of the batched step (for the per-kernel ncu figures).
 PHASE_KERNELS = {
-    "mixed": {"prim": ["k_prim_w<0>"], "rhs": ["k_rhs_flux<0, 0>"],
-              "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>"], "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
-              "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
+    ("BT", "mixed"): {"prim": ["k_prim_w<0>"], "rhs": ["k_rhs_flux<0, 0>"],
+                      "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>"],
+                      "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
+                      "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
+    ("SP", "mixed"): {"prim": ["k_prim_w<1>"], "rhs": ["k_rhs_flux<1, 0>"],
+                      "x": ["k_sp_mixed_pl<0>", "k_sp_refine_pl<0, 1>"],
+                      "y": ["k_sp_mixed_pl<1>", "k_sp_refine_pl<1, 1>"],
+                      "z": ["k_sp_mixed_pl<2>", "k_sp_refine_pl<2, 0>"]},
 }
 
 
@@ -163,13 +169,13 @@ def phase_times(p, nsteps):
 
 def kernel_metrics(workload, variant):
     """Per-point ncu figures of the step kernels (profiles/ncu_kernel_metrics.json):
-    from a capture of this workload, else of the BT-B workload (same kernels),
-    per point."""
+    from a capture of this workload, else of the class-B workload of the same
+    kind (same kernels, 1.07 M points), per point."""
     try:
         allm = json.loads((ROOT / "profiles" / "ncu_kernel_metrics.json").read_text())
     except Exception:
         return None, None
-    for w in (workload, "bt-b"):
+    for w in (workload, workload[:2] + "-b"):
         m = allm.get(w, {}).get(variant)
         if m:
             return m, w
@@ -288,8 +294,7 @@ def run_gpu(args):
         achieved = BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
         fp64 = npbmz.fp64_peak_gflops()
         km, km_src = kernel_metrics(args.workload, args.variant)
-        kvar = "mixed" if flags & npbmz.MIXED and kind == "BT" else None
-        knames = PHASE_KERNELS.get(kvar, {}).get(top, []) if kvar else []
+        knames = PHASE_KERNELS.get((kind, "mixed"), {}).get(top, []) if flags & npbmz.MIXED else []
         traffic = None
         fp64_obj = None
         if km and knames and all(k in km for k in knames):
