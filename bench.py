@@ -159,6 +159,19 @@ def time_steps(p, torch, stream, steps, warmup, dist=None):
     return e0.elapsed_time(e1)
 
 
+def whole_job(ms_local, pts, steps, world, dist=None, device="cuda"):
+    """Replicas: every rank runs the workload on its own GPU; the job's time is
+    the slowest rank's (max over ranks) and its value counts the points of
+    all ranks.  Returns (ms_max, Mgridpt-steps/s)."""
+    import torch
+
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, pts * world * steps / (ms_max * 1e-3) / 1e6
+
+
 def phase_times(p, nsteps):
     """Per-phase device time of the batched step -- the kernels the timed
     steps run -- from CUDA events the library records around each phase on
@@ -274,11 +287,7 @@ def run_gpu(args):
         p.setup(ce)
     with ClockSampler(local) as clk:
         ms = time_steps(p, torch, stream, args.steps, args.warmup, dist)
-    t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = pts * world * args.steps / (ms_max * 1e-3) / 1e6
+    ms_max, value = whole_job(ms, pts, args.steps, world, dist)
     launches = p.launches_per_step * args.steps
 
     extra = {}
