@@ -51,11 +51,11 @@ SEED = 20261203
 BYTES_PER_POINT = {"prim": 40.0, "rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
 # Kernels of each phase of the batched step (for the per-kernel ncu figures).
 PHASE_KERNELS = {
-    ("BT", "mixed"): {"prim": ["k_prim_w<0>"], "rhs": ["k_rhs_flux<0, 0>"],
+    ("BT", "mixed"): {"prim": ["k_prim_df<0>"], "rhs": ["k_rhs_df<0, 0>"],
                       "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>"],
                       "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
                       "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
-    ("SP", "mixed"): {"prim": ["k_prim_w<1>"], "rhs": ["k_rhs_flux<1, 0>"],
+    ("SP", "mixed"): {"prim": ["k_prim_df<1>"], "rhs": ["k_rhs_df<1, 0>"],
                       "x": ["k_sp_mixed_pl<0>", "k_sp_refine_pl<0, 1>"],
                       "y": ["k_sp_mixed_pl<1>", "k_sp_refine_pl<1, 1>"],
                       "z": ["k_sp_mixed_pl<2>", "k_sp_refine_pl<2, 0>"]},
@@ -273,6 +273,7 @@ def run_gpu(args):
     pts = g.points
     ce, escale = npbmz.seeded_coefficients(SEED, g.nx, g.ny, g.nz, g.gx, g.gy, g.gz, g.x_zones, g.y_zones)
     flags = {"mixed-graph": npbmz.MIXED | npbmz.GRAPH, "fp64-graph": npbmz.GRAPH,
+             "mixed-rhs64-graph": npbmz.MIXED | npbmz.RHS_FP64 | npbmz.GRAPH,
              "mixed": npbmz.MIXED, "fp64": 0}[args.variant]
 
     def make(fl):
@@ -303,7 +304,8 @@ def run_gpu(args):
         achieved = BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
         fp64 = npbmz.fp64_peak_gflops()
         km, km_src = kernel_metrics(args.workload, args.variant)
-        knames = PHASE_KERNELS.get((kind, "mixed"), {}).get(top, []) if flags & npbmz.MIXED else []
+        knames = (PHASE_KERNELS.get((kind, "mixed"), {}).get(top, [])
+                  if flags & npbmz.MIXED and not flags & npbmz.RHS_FP64 else [])
         traffic = None
         fp64_obj = None
         if km and knames and all(k in km for k in knames):
@@ -332,6 +334,7 @@ def run_gpu(args):
                          ("mixed_batched", npbmz.MIXED), ("mixed_batched_graph", npbmz.MIXED | npbmz.GRAPH),
                          ("fp64_batched_graph", npbmz.GRAPH),
                          ("mixed_batched_graph_persistent", npbmz.MIXED | npbmz.GRAPH | npbmz.PERSIST),
+                         ("mixed_fp64_rhs_batched_graph", npbmz.MIXED | npbmz.RHS_FP64 | npbmz.GRAPH),
                          ("fp64_perzone", npbmz.PERZONE)):
             q = make(fl)
             steps_v = 2 if fl & npbmz.PERZONE else nv
@@ -407,7 +410,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bt-c", choices=sorted(WORKLOADS))
-    ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed", "fp64"])
+    ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed-rhs64-graph", "mixed", "fp64"])
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",

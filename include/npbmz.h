@@ -47,12 +47,13 @@ typedef struct npbmz_handle npbmz_t;
 #define NPBMZ_EXACT   0x1  /* FP64 kernels built without FMA contraction, in the
                               reference's operation order: bit-for-bit the
                               reference's arithmetic */
-#define NPBMZ_MIXED   0x2  /* line solves in FP32 on the FP64 rhs, refined once
-                              against a residual of the line operator formed in
+#define NPBMZ_MIXED   0x2  /* line solves in FP32, refined once against a
+                              residual of the line operator formed in
                               double-float (FP32 pairs, about 48 bits) -- in
-                              FP64 for single phases (npbmz_phase) and for SP
-                              with NPBMZ_REFINE_FP64; compute_rhs, add,
-                              exch_qbc and the norms stay FP64 */
+                              FP64 with NPBMZ_REFINE_FP64; the primitive
+                              kernel and compute_rhs run in double-float too
+                              (FP64 with NPBMZ_RHS_FP64 or NPBMZ_REFINE_FP64);
+                              u, add, exch_qbc and the norms stay FP64 */
 #define NPBMZ_PERZONE 0x4  /* one launch per zone per phase, the reference's
                               per-zone adi order; default is all zones batched
                               in one launch per phase */
@@ -64,6 +65,8 @@ typedef struct npbmz_handle npbmz_t;
                               zone x line work items; results are unchanged */
 #define NPBMZ_REFINE_FP64 0x40 /* with NPBMZ_MIXED: the refinement residual in
                               FP64 instead of double-float */
+#define NPBMZ_RHS_FP64 0x80 /* with NPBMZ_MIXED: the primitive kernel and
+                              compute_rhs in FP64 */
 #define NPBMZ_FP32_NOREFINE 0x20 /* FP32 line solves without the refinement
                               pass (the error of plain FP32 solves, for
                               comparison); implies NPBMZ_MIXED */

@@ -94,6 +94,39 @@ bool make_lin_weights(const Consts& k, LinWeights& lw) {
   return true;
 }
 
+float2 split_const(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
+// The double-float constants of the primitive kernel and compute_rhs.
+void make_rhs_df_consts(const Consts& k, const LinWeights& lw, RhsDfConsts& c) {
+  for (int d = 0; d < 3; ++d)
+    for (int cl = 0; cl < 32; ++cl)
+      for (int o = 0; o < 5; ++o) c.w[d][cl][o] = split_const(lw.w[d][cl][o]);
+  const double vc[3][3] = {{k.xxcon2 * k.con43, k.xxcon2, k.xxcon2},
+                           {k.yycon2, k.yycon2 * k.con43, k.yycon2},
+                           {k.zzcon2, k.zzcon2, k.zzcon2 * k.con43}};
+  for (int d = 0; d < 3; ++d)
+    for (int m = 0; m < 3; ++m) c.vc[d][m] = split_const(vc[d][m]);
+  for (int m = 0; m < 3; ++m) c.vcc[m] = split_const(-2.0 * (vc[0][m] + vc[1][m] + vc[2][m]));
+  c.t2[0] = split_const(k.tx2);
+  c.t2[1] = split_const(k.ty2);
+  c.t2[2] = split_const(k.tz2);
+  c.dt = split_const(k.dt);
+  c.c1 = split_const(k.c1);
+  c.c2 = split_const(k.c2);
+  c.c1c2 = split_const(k.c1c2);
+  c.bt = split_const(k.bt);
+  const double c3[3] = {k.xxcon3, k.yycon3, k.zzcon3}, c4[3] = {k.xxcon4, k.yycon4, k.zzcon4},
+               c5[3] = {k.xxcon5, k.yycon5, k.zzcon5};
+  for (int d = 0; d < 3; ++d) {
+    c.con3[d] = split_const(c3[d]);
+    c.con4[d] = split_const(c4[d]);
+    c.con5[d] = split_const(c5[d]);
+  }
+}
+
 // A contiguous slice of a work list: items [lo, hi) belong to one zone.
 struct Range {
   int lo = 0, hi = 0;
@@ -128,6 +161,12 @@ struct npbmz_handle {
   float* rdx = nullptr;
   float* x0x = nullptr;
   LinWeights lw;             // compute_rhs linear stencil weights (FMA build)
+  // refined mixed step with the double-float primitive kernel and compute_rhs
+  bool dfrhs = false;
+  float2* ud = nullptr;      // [5][NP] u
+  float2* xd = nullptr;      // [XD_COUNT][NP] point functions
+  float2* fd = nullptr;      // [5][NP] forcing
+  RhsDfConsts rdc;
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
   // y and z line scratch of the grouped step graph, where sweeps of
@@ -233,6 +272,9 @@ Fields fields(const npbmz_t* h) {
   F.rdx = h->rdx;
   F.x0x = h->x0x;
   F.nlx = h->nlines[0];
+  F.ud = h->ud;
+  F.xd = h->xd;
+  F.fd = h->fd;
   return F;
 }
 
@@ -358,6 +400,10 @@ int flush_boundary(npbmz_t* h) {
     fast::launch_split_df(h->forcing, h->rdf, h->NP, h->stream);
     CKL(h);
   }
+  if (h->fd) {
+    fast::launch_split_f2(h->forcing, h->fd, h->NP, h->stream);
+    CKL(h);
+  }
   if (h->rdx) {
     const Fields F = fields(h);
     const int saved = h->cur_group;
@@ -454,8 +500,11 @@ int line_launches(npbmz_t* h, int dir, int zone, Fn fn) {
 }
 
 // ---- phases ---------------------------------------------------------------
-int phase_prim(npbmz_t* h, int zone) {
-  const Fields F = fields(h);
+// fused: part of a whole step (run_adi): with the double-float primitive
+// kernel, the FP64 prim planes that only single phases read are skipped.
+int phase_prim(npbmz_t* h, int zone, bool fused = false) {
+  Fields F = fields(h);
+  F.prim64 = !fused;
   int64_t lo = 0, hi = h->NP;
   if (zone >= 0) {
     lo = h->zh[zone].off;
@@ -470,19 +519,28 @@ int phase_prim(npbmz_t* h, int zone) {
     int wlo = 0, whi = h->nwpts;
     if (zone >= 0) { wlo = h->pts_range[zone].lo; whi = h->pts_range[zone].hi; }
     else if (h->cur_group >= 0) { wlo = h->grp_pts[h->cur_group].lo; whi = h->grp_pts[h->cur_group].hi; }
-    fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+    if (h->dfrhs)
+      fast::launch_prim_df(sp, F, h->rdc, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+    else
+      fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
   }
   CKL(h);
   return 0;
 }
 
-int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm) {
+// fused: part of a whole step, whose sweeps read only the double-float copy
+// of rhs (the z sweep rewrites rhs in FP64).
+int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm, bool fused = false) {
   if (flush_boundary(h)) return -1;
-  const Fields F = fields(h);
+  Fields F = fields(h);
+  F.rhs64 = !fused;
   int lo = 0, hi = h->nwint;
   if (zone >= 0) { lo = h->int_range[zone].lo; hi = h->int_range[zone].hi; }
   else if (h->cur_group >= 0) { lo = h->grp_int[h->cur_group].lo; hi = h->grp_int[h->cur_group].hi; }
   if (use_exact(h)) exact::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream);
+  else if (h->dfrhs)
+    fast::launch_rhs_df(tx, norm, F, h->rdc, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream,
+                        (h->flags & NPBMZ_PERSIST) != 0);
   else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->lw,
                         (h->flags & NPBMZ_PERSIST) != 0);
   CKL(h);
@@ -541,8 +599,8 @@ int run_adi(npbmz_t* h, int zone, bool norm) {
       if (run_adi(h, z, norm)) return -1;
     return 0;
   }
-  if (phase_prim(h, zone)) return -1;
-  if (phase_rhs(h, zone, sp, norm)) return -1;
+  if (phase_prim(h, zone, true)) return -1;
+  if (phase_rhs(h, zone, sp, norm, true)) return -1;
   if (phase_solve(h, 0, zone, 0, true)) return -1;
   if (phase_solve(h, 1, zone, 0, true)) return -1;
   if (phase_solve(h, 2, zone, 1, true)) return -1;  // add fused into the z sweep
@@ -595,8 +653,8 @@ int grouped_step(npbmz_t* h, cudaStream_t cs) {
     if (g > 0) rc |= cudaStreamWaitEvent(S, h->grp_ev[2 * (g - 1)], 0) != cudaSuccess;
     h->stream = S;
     h->cur_group = g;
-    if (!rc) rc = phase_prim(h, -1);
-    if (!rc) rc = phase_rhs(h, -1, sp, false);
+    if (!rc) rc = phase_prim(h, -1, true);
+    if (!rc) rc = phase_rhs(h, -1, sp, false, true);
     if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g], S) != cudaSuccess;
     for (int dir = 0; dir < 3 && !rc; ++dir) rc = phase_solve(h, dir, -1, dir == 2 ? 1 : 0, true);
     if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g + 1], S) != cudaSuccess;
@@ -1121,7 +1179,15 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
   if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? (int)PF_COUNT : (int)PS_COUNT) * h->NP);
   if (!(variant_flags & NPBMZ_EXACT) && make_lin_weights(h->K, h->lw)) {
-    rc |= dalloc(h, &h->flux, (size_t)PX_COUNT * h->NP);
+    h->dfrhs = refined && !(variant_flags & (NPBMZ_REFINE_FP64 | NPBMZ_RHS_FP64));
+    if (h->dfrhs) {
+      make_rhs_df_consts(h->K, h->lw, h->rdc);
+      rc |= dalloc(h, &h->ud, 5 * (size_t)h->NP);
+      rc |= dalloc(h, &h->xd, (size_t)XD_COUNT * h->NP);
+      rc |= dalloc(h, &h->fd, 5 * (size_t)h->NP);
+    } else {
+      rc |= dalloc(h, &h->flux, (size_t)PX_COUNT * h->NP);
+    }
     if (refined && !(variant_flags & NPBMZ_REFINE_FP64)) {
       rc |= dalloc(h, &h->rdf, 10 * (size_t)h->NP);
       int maxnx = 0;
@@ -1166,6 +1232,11 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
     if (cudaMemset(h->forcing, 0, 5 * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
     if (cudaMemset(h->prim, 0, PR_COUNT * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
     if (cudaMemset(h->uex, 0, 5 * h->NP * sizeof(double)) != cudaSuccess) rc = -1;
+    if (h->dfrhs) {
+      if (cudaMemset(h->ud, 0, 5 * h->NP * sizeof(float2)) != cudaSuccess) rc = -1;
+      if (cudaMemset(h->xd, 0, XD_COUNT * h->NP * sizeof(float2)) != cudaSuccess) rc = -1;
+      if (cudaMemset(h->fd, 0, 5 * h->NP * sizeof(float2)) != cudaSuccess) rc = -1;
+    }
     if (cudaDeviceSynchronize() != cudaSuccess) rc = -1;
   }
   if (rc) {
@@ -1270,9 +1341,9 @@ int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms) {
     rc |= cudaEventRecord(E[0], h->stream) != cudaSuccess;
     if (!rc) rc = phase_exch(h);
     rc |= cudaEventRecord(E[1], h->stream) != cudaSuccess;
-    if (!rc) rc = phase_prim(h, -1);
+    if (!rc) rc = phase_prim(h, -1, true);
     rc |= cudaEventRecord(E[2], h->stream) != cudaSuccess;
-    if (!rc) rc = phase_rhs(h, -1, h->kind == NPBMZ_SP, false);
+    if (!rc) rc = phase_rhs(h, -1, h->kind == NPBMZ_SP, false, true);
     rc |= cudaEventRecord(E[3], h->stream) != cudaSuccess;
     for (int dir = 0; dir < 3 && !rc; ++dir) {
       rc = phase_solve(h, dir, -1, dir == 2 ? 1 : 0, true);
@@ -1413,8 +1484,8 @@ int npbmz_autotune(npbmz_t* h) {
   }
   if (build_line_lists(h)) rc = -1;
   // prim + rhs once so that the solves read defined data
-  if (!rc) rc = phase_prim(h, -1);
-  if (!rc) rc = phase_rhs(h, -1, h->kind == NPBMZ_SP, false);
+  if (!rc) rc = phase_prim(h, -1, true);
+  if (!rc) rc = phase_rhs(h, -1, h->kind == NPBMZ_SP, false, true);
   for (int dir = 0; dir < 3 && !rc; ++dir)
     for (int bk = 0; bk < h->nbkt && !rc; ++bk) {
       float best = 1e30f;
@@ -1524,7 +1595,7 @@ int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->scratch_yz[0], h->scratch_yz[1], h->part_rhs,
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->ud, h->xd, h->fd, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->scratch_yz[0], h->scratch_yz[1], h->part_rhs,
                   h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wint_d, h->zblk_int_d,
                   h->wline_d[0], h->wline_d[1],
                   h->wline_d[2]};

@@ -67,6 +67,22 @@ enum {
   PX_COUNT
 };
 
+// Double-float point planes of compute_rhs for the refined mixed step
+// (float2 {hi, lo} per point, one plane per quantity): the twelve PX_*
+// functions, then the three velocities and (SP) qs for txinvr.
+enum { XD_US = PX_COUNT, XD_VS, XD_WS, XD_QS, XD_COUNT };
+
+// Double-float constants of compute_rhs and the primitive kernel of the
+// refined mixed step, split on the host ({hi, lo} = rn(c), rn(c - hi)).
+struct RhsDfConsts {
+  float2 w[3][32][5];  // LinWeights
+  float2 vc[3][3];     // velocity second-difference factors per direction, variables 2..4
+  float2 vcc[3];       // centre point: -2 * sum over the directions of vc
+  float2 t2[3];        // tx2, ty2, tz2
+  float2 dt, c1, c2, c1c2, bt;
+  float2 con3[3], con4[3], con5[3];  // xxcon3..5, yycon3..5, zzcon3..5
+};
+
 struct Fields {
   double* u;        // [5][NP]
   double* rhs;      // [5][NP]
@@ -87,6 +103,15 @@ struct Fields {
   float* rdx = nullptr;  // E = 10: double-float rhs (compute_rhs; line ends: the forcing)
   float* x0x = nullptr;  // E = 5: first-pass solution
   int64_t nlx = 0;       // x lines of all zones
+  // refined mixed step with the double-float compute_rhs (else null):
+  float2* ud = nullptr;        // [5][NP] u
+  float2* xd = nullptr;        // [XD_COUNT][NP] point functions of compute_rhs
+  const float2* fd = nullptr;  // [5][NP] forcing
+  // the primitive kernel writes the FP64 planes prim (single phases; SP's
+  // z sweep reads us, vs, ws, speed, ainv, qs in every step)
+  bool prim64 = true;
+  // compute_rhs writes rhs in FP64 as well as its double-float copy
+  bool rhs64 = true;
 };
 
 // x line through interior point (j, k) of zone z (-1 when j or k is a face).

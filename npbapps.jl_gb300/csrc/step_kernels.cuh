@@ -2327,6 +2327,7 @@ __global__ void __launch_bounds__(128) k_sp_refine(Fields F, Consts K, const Wor
 
 #if NPBMZ_HAS_FP32
 #include "sp_pipelined.cuh"
+#include "rhs_df.cuh"
 #endif
 
 // ============================================================================
@@ -2532,6 +2533,34 @@ int configure_kernels() {
 
 void launch_xline_ends(const Fields& F, const Work* work, int nwork, int tpb, cudaStream_t s) {
   if (nwork > 0) k_xline_ends<<<nwork, tpb, 0, s>>>(F, work);
+}
+
+void launch_prim_df(bool sp, const Fields& F, const RhsDfConsts& C, const Work* work, int nwork, cudaStream_t s,
+                    bool persist) {
+  if (nwork <= 0) return;
+  if (sp) k_prim_df<true><<<item_grid((const void*)k_prim_df<true>, nwork, 128, 0, persist), 128, 0, s>>>(F, C, work, nwork);
+  else k_prim_df<false><<<item_grid((const void*)k_prim_df<false>, nwork, 128, 0, persist), 128, 0, s>>>(F, C, work, nwork);
+}
+
+void launch_rhs_df(bool tx, bool norm, const Fields& F, const RhsDfConsts& C, const Work* work, int nwork,
+                   double* partials, cudaStream_t s, bool persist) {
+  if (nwork <= 0) return;
+#define NPBMZ_RHS_DF(A, B)                                                                                     \
+  k_rhs_df<A, B><<<item_grid((const void*)k_rhs_df<A, B>, nwork, 128, 0, persist), 128, 0, s>>>(F, C, work, nwork, \
+                                                                                              partials)
+  if (tx) {
+    if (norm) NPBMZ_RHS_DF(true, true);
+    else NPBMZ_RHS_DF(true, false);
+  } else {
+    if (norm) NPBMZ_RHS_DF(false, true);
+    else NPBMZ_RHS_DF(false, false);
+  }
+#undef NPBMZ_RHS_DF
+}
+
+void launch_split_f2(const double* src, float2* dst, int64_t NP, cudaStream_t s) {
+  int64_t g = (5 * NP + 255) / 256;
+  k_split_f2<<<(int)(g > 8192 ? 8192 : g), 256, 0, s>>>(src, dst, NP);
 }
 
 void launch_split_df(const double* src, float* dst, int64_t NP, cudaStream_t s) {

@@ -25,6 +25,13 @@ NPBMZ_DECLARE_LAUNCHERS(fast)
 namespace fast {
 // dst (10 float planes: double-float hi 0..4, lo 5..9) <- src (5 FP64 planes)
 void launch_split_df(const double* src, float* dst, int64_t NP, cudaStream_t s);
+// dst (5 float2 planes {hi, lo}) <- src (5 FP64 planes)
+void launch_split_f2(const double* src, float2* dst, int64_t NP, cudaStream_t s);
+// primitive kernel and compute_rhs of the refined mixed step in double-float
+void launch_prim_df(bool sp, const Fields& F, const RhsDfConsts& C, const Work* work, int nwork, cudaStream_t s,
+                    bool persist);
+void launch_rhs_df(bool tx, bool norm, const Fields& F, const RhsDfConsts& C, const Work* work, int nwork,
+                   double* partials, cudaStream_t s, bool persist);
 // the forcing at both ends of every x line into Fields::rdx
 void launch_xline_ends(const Fields& F, const Work* work, int nwork, int tpb, cudaStream_t s);
 // dynamic shared memory limits of the pipelined sweeps; 0 on success

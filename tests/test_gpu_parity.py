@@ -119,6 +119,47 @@ def test_each_phase_fast_path_within_1e12(oracle_mod, gname):
             p.upload(npbmz.RHS, z, o.get(npbmz.RHS, z))
 
 
+DF_RHS_REL = 1e-12   # compute_rhs in double-float (FP32 pairs, about 48 bits)
+
+
+@pytest.mark.parametrize("gname", list(GEOMS))
+def test_double_float_compute_rhs_phase(oracle_mod, gname):
+    """MIXED handles form the primitive variables and compute_rhs (with SP's
+    txinvr) in double-float arithmetic on the FP32 pipe: the compute_rhs phase
+    of each zone against the oracle from identical inputs."""
+    geom, dt, _ = GEOMS[gname]()
+    p, o = make_pair(oracle_mod, geom, dt, npbmz.MIXED, seeded(geom))
+    p.phase(npbmz.PHASE_EXCH)
+    o.phase(5)
+    worst = 0.0
+    for z in range(geom.nzones):
+        p.phase(npbmz.PHASE_RHS, z)
+        o.phase(0, z)
+        worst = max(worst, compare(p, o, npbmz.RHS, DF_RHS_REL, [z]))
+    print(f"double-float compute_rhs: worst rel err {worst:.3e}")
+
+
+@pytest.mark.parametrize("kind", ["BT", "SP"])
+def test_double_float_rhs_steps_match_fp64_rhs(kind):
+    """The same refined mixed step with compute_rhs in double-float (default)
+    and in FP64 (NPBMZ_RHS_FP64): u and the verification norms after 20
+    steps of class W agree to 1e-12."""
+    geom, dt, _ = geom_class(kind, "W")
+    ce = seeded(geom)
+    a = npbmz.Problem(geom, dt, npbmz.MIXED)
+    b = npbmz.Problem(geom, dt, npbmz.MIXED | npbmz.RHS_FP64)
+    a.setup(ce)
+    b.setup(ce)
+    a.step(20)
+    b.step(20)
+    worst = 0.0
+    for z in range(geom.nzones):
+        ua, ub = a.download(npbmz.U, z), b.download(npbmz.U, z)
+        worst = max(worst, float(np.max(np.abs(ua - ub)) / np.max(np.abs(ub))))
+    assert worst <= 1e-12, worst
+    np.testing.assert_allclose(np.concatenate(a.verify()), np.concatenate(b.verify()), rtol=1e-12, atol=0)
+
+
 @pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 20), ("sp_classS", 40)])
 def test_steps_exact_path_bit_exact(oracle_mod, gname, nsteps):
     geom, dt, _ = GEOMS[gname]()
@@ -271,7 +312,8 @@ MIXED_REL = 1e-10   # FP32 line solves refined against an FP64 residual
 
 
 @pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 60), ("sp_classS", 100)])
-@pytest.mark.parametrize("flags", [npbmz.MIXED, npbmz.MIXED | npbmz.REFINE_FP64], ids=["df64-residual", "fp64-residual"])
+@pytest.mark.parametrize("flags", [npbmz.MIXED, npbmz.MIXED | npbmz.RHS_FP64, npbmz.MIXED | npbmz.REFINE_FP64],
+                         ids=["df64-residual", "fp64-rhs", "fp64-residual"])
 def test_mixed_precision_within_1e10_of_fp64_oracle(oracle_mod, gname, nsteps, flags):
     geom, dt, _ = GEOMS[gname]()
     p, o = make_pair(oracle_mod, geom, dt, flags, seeded(geom))
