@@ -519,9 +519,18 @@ int phase_prim(npbmz_t* h, int zone, bool fused = false) {
     int wlo = 0, whi = h->nwpts;
     if (zone >= 0) { wlo = h->pts_range[zone].lo; whi = h->pts_range[zone].hi; }
     else if (h->cur_group >= 0) { wlo = h->grp_pts[h->cur_group].lo; whi = h->grp_pts[h->cur_group].hi; }
-    if (h->dfrhs)
+    if (h->dfrhs) {
       fast::launch_prim_df(sp, F, h->rdc, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
-    else
+      CKL(h);
+      // the x sweep of a fused step reads x-line-major copies of the state
+      if (fused && h->pfx &&
+          line_launches(h, 0, zone, [&](int llo, int lhi, int tpb) {
+            fast::launch_xline_copy(sp, F, h->wline_d[0] + llo, lhi - llo, tpb, h->stream);
+            CKL(h);
+            return 0;
+          }))
+        return -1;
+    } else
       fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
   }
   CKL(h);
@@ -725,7 +734,7 @@ int replay_graph(npbmz_t* h, int nsteps) {
 // the FP32 solves are refined).
 int count_launches(npbmz_t* h) {
   const bool refined = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE);
-  const int adi = 2 + 3 * (refined ? 2 : 1);
+  const int adi = 2 + (h->dfrhs && h->pfx ? 1 : 0) + 3 * (refined ? 2 : 1);
   int batches = 1;
   if (h->flags & NPBMZ_PERZONE) batches = h->nzones;
   else if ((h->flags & NPBMZ_GRAPH) && h->ngroups > 1 && !(h->flags & NPBMZ_EXACT)) batches = h->ngroups;

@@ -82,10 +82,10 @@ __device__ __forceinline__ df64 df_sqrt(df64 a) {
 // Per point: u in double-float (exact split), 1/rho, the velocities, square
 // and qs (src/BT/rhs.jl:62-77; SP src/SP/rhs.jl:62-89 with the speed of
 // sound), the point functions of compute_rhs, the FP32 state pairs of the
-// sweeps (and their x-line-major copies), and the FP64 prim planes that are
-// read in FP64.
+// sweeps, and the FP64 prim planes that are read in FP64.  The x-line-major
+// copies of the state pairs come from k_xline_copy.
 template <bool SP>
-__device__ __forceinline__ void prim_df_point(const Fields& F, const RhsDfConsts& C, int64_t p, int64_t xl, int xi) {
+__device__ __forceinline__ void prim_df_point(const Fields& F, const RhsDfConsts& C, int64_t p) {
   const int64_t NP = F.NP;
   df64 u[5];
 #pragma unroll
@@ -129,10 +129,6 @@ __device__ __forceinline__ void prim_df_point(const Fields& F, const RhsDfConsts
     for (int e = 0; e < PS_HI_COUNT; ++e) {
       F.primf[e * NP + p] = v[e].hi;
       F.primf[(PS_HI_COUNT + e) * NP + p] = v[e].lo;
-      if (F.pfx && xl >= 0) {
-        F.pfx[((int64_t)xi * PS_COUNT + e) * F.nlx + xl] = v[e].hi;
-        F.pfx[((int64_t)xi * PS_COUNT + PS_HI_COUNT + e) * F.nlx + xl] = v[e].lo;
-      }
     }
     // the z sweep's tzetar and add run in FP64 from these
     F.prim[PR_US * NP + p] = df_to_double(us);
@@ -147,10 +143,6 @@ __device__ __forceinline__ void prim_df_point(const Fields& F, const RhsDfConsts
     for (int e = 0; e < PF_HI_COUNT; ++e) {
       F.primf[e * NP + p] = v[e].hi;
       F.primf[(PF_HI_COUNT + e) * NP + p] = v[e].lo;
-      if (F.pfx && xl >= 0) {
-        F.pfx[((int64_t)xi * PF_COUNT + e) * F.nlx + xl] = v[e].hi;
-        F.pfx[((int64_t)xi * PF_COUNT + PF_HI_COUNT + e) * F.nlx + xl] = v[e].lo;
-      }
     }
   }
   if (F.prim64) {
@@ -172,8 +164,7 @@ __global__ void __launch_bounds__(128) k_prim_df(Fields F, RhsDfConsts C, const 
     const ZoneDev Z = F.zones[w.zone];
     const int q = w.first + threadIdx.x;
     if (q >= Z.nx * Z.ny * Z.nz) continue;
-    const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
-    prim_df_point<SP>(F, C, Z.off + q, xline_of(Z, j, k), i);
+    prim_df_point<SP>(F, C, Z.off + q);
   }
 }
 
@@ -319,6 +310,58 @@ __global__ void __launch_bounds__(128) k_rhs_df(Fields F, RhsDfConsts C, const W
       if (threadIdx.x == 0)
         for (int m = 0; m < 5; ++m) partials[it * 5 + m] = sq[m];
     }
+  }
+}
+
+// ---- x-line-major copies of the state pairs ---------------------------------
+// The x sweep gives each thread one x line, so that a warp's lines sit nx
+// points apart in the zone layout; it reads x-line-major copies of the FP32
+// state pairs instead (plane e of point i of line g at [(i * E + e) * nlx +
+// g]).  This kernel makes them for the lines of each x-sweep work item (lpi
+// lines of one zone from `first`, every point of each line): 32-line x
+// 32-point tiles of PB planes at a time go through shared memory, so that
+// the zone-layout reads (along i) and the x-line-major writes (along g) are
+// both coalesced, with 4 * PB loads in flight per thread.
+template <bool SP>
+__global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __restrict__ work, int nwork, int lpi) {
+  constexpr int E = SP ? (int)PS_COUNT : (int)PF_COUNT;
+  constexpr int PB = E / 2;
+  __shared__ float tile[PB][32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
+  const int64_t NP = F.NP;
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
+    const Work w = work[it];
+    const ZoneDev Z = F.zones[w.zone];
+    const int l1 = min(w.first + lpi, zone_lines(Z, 0));
+    const int iy = Z.ny - 2;
+    for (int l0 = w.first; l0 < l1; l0 += 32)
+      for (int i0 = 0; i0 < Z.nx; i0 += 32)
+#pragma unroll 1
+        for (int e0 = 0; e0 < E; e0 += PB) {
+          float v[PB][4];
+#pragma unroll
+          for (int r4 = 0; r4 < 4; ++r4) {  // row ty + 8 r4: line l0 + row, column tx: point i0 + tx
+            const int l = l0 + ty + 8 * r4, i = i0 + tx;
+            const bool ok = l < l1 && i < Z.nx;
+            const int64_t p = ok ? Z.off + ((int64_t)(1 + l / iy) * Z.ny + 1 + l % iy) * Z.nx + i : 0;
+#pragma unroll
+            for (int b = 0; b < PB; ++b) v[b][r4] = ok ? F.primf[(int64_t)(e0 + b) * NP + p] : 0.f;
+          }
+#pragma unroll
+          for (int b = 0; b < PB; ++b)
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4) tile[b][ty + 8 * r4][tx] = v[b][r4];
+          __syncthreads();
+#pragma unroll
+          for (int r4 = 0; r4 < 4; ++r4) {  // point i0 + ty + 8 r4 of line l0 + tx
+            const int i = i0 + ty + 8 * r4, l = l0 + tx;
+            if (l < l1 && i < Z.nx)
+#pragma unroll
+              for (int b = 0; b < PB; ++b)
+                F.pfx[((int64_t)i * E + e0 + b) * F.nlx + Z.lineoff[0] + l] = tile[b][tx][ty + 8 * r4];
+          }
+          __syncthreads();
+        }
   }
 }
 

@@ -2558,6 +2558,12 @@ void launch_rhs_df(bool tx, bool norm, const Fields& F, const RhsDfConsts& C, co
 #undef NPBMZ_RHS_DF
 }
 
+void launch_xline_copy(bool sp, const Fields& F, const Work* work, int nwork, int lpi, cudaStream_t s) {
+  if (nwork <= 0) return;
+  if (sp) k_xline_copy<true><<<nwork, 256, 0, s>>>(F, work, nwork, lpi);
+  else k_xline_copy<false><<<nwork, 256, 0, s>>>(F, work, nwork, lpi);
+}
+
 void launch_split_f2(const double* src, float2* dst, int64_t NP, cudaStream_t s) {
   int64_t g = (5 * NP + 255) / 256;
   k_split_f2<<<(int)(g > 8192 ? 8192 : g), 256, 0, s>>>(src, dst, NP);

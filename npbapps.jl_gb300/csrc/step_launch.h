@@ -32,6 +32,9 @@ void launch_prim_df(bool sp, const Fields& F, const RhsDfConsts& C, const Work* 
                     bool persist);
 void launch_rhs_df(bool tx, bool norm, const Fields& F, const RhsDfConsts& C, const Work* work, int nwork,
                    double* partials, cudaStream_t s, bool persist);
+// x-line-major copies of the FP32 state pairs for the x-sweep items
+// work[0..nwork) of lpi lines each
+void launch_xline_copy(bool sp, const Fields& F, const Work* work, int nwork, int lpi, cudaStream_t s);
 // the forcing at both ends of every x line into Fields::rdx
 void launch_xline_ends(const Fields& F, const Work* work, int nwork, int tpb, cudaStream_t s);
 // dynamic shared memory limits of the pipelined sweeps; 0 on success
