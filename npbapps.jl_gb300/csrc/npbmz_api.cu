@@ -734,7 +734,9 @@ int replay_graph(npbmz_t* h, int nsteps) {
 // the FP32 solves are refined).
 int count_launches(npbmz_t* h) {
   const bool refined = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE);
-  const int adi = 2 + (h->dfrhs && h->pfx ? 1 : 0) + 3 * (refined ? 2 : 1);
+  // prim, its x-line-major copy (double-float compute_rhs), compute_rhs,
+  // two kernels per refined sweep and the x result's copy back
+  const int adi = 2 + (h->dfrhs && h->pfx ? 1 : 0) + 3 * (refined ? 2 : 1) + (h->rdx ? 1 : 0);
   int batches = 1;
   if (h->flags & NPBMZ_PERZONE) batches = h->nzones;
   else if ((h->flags & NPBMZ_GRAPH) && h->ngroups > 1 && !(h->flags & NPBMZ_EXACT)) batches = h->ngroups;

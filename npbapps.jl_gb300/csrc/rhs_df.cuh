@@ -365,6 +365,51 @@ __global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __rest
   }
 }
 
+// The reverse copy for the refined x sweep's result: its double-float x
+// (10 planes, interior points) goes from the x-line-major rdx, where each
+// thread wrote its own line, to the zone-layout rdf that the y sweep reads.
+__global__ void __launch_bounds__(256) k_xline_back(Fields F, const Work* __restrict__ work, int nwork, int lpi) {
+  constexpr int PB = 5;
+  __shared__ float tile[PB][32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
+  const int64_t NP = F.NP;
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
+    const Work w = work[it];
+    const ZoneDev Z = F.zones[w.zone];
+    const int l1 = min(w.first + lpi, zone_lines(Z, 0));
+    const int iy = Z.ny - 2;
+    for (int l0 = w.first; l0 < l1; l0 += 32)
+      for (int i0 = 1; i0 < Z.nx - 1; i0 += 32)
+#pragma unroll 1
+        for (int e0 = 0; e0 < 10; e0 += PB) {
+          float v[PB][4];
+#pragma unroll
+          for (int r4 = 0; r4 < 4; ++r4) {  // row ty + 8 r4: point i0 + row, column tx: line l0 + tx
+            const int i = i0 + ty + 8 * r4, l = l0 + tx;
+            const bool ok = l < l1 && i < Z.nx - 1;
+#pragma unroll
+            for (int b = 0; b < PB; ++b)
+              v[b][r4] = ok ? F.rdx[((int64_t)i * 10 + e0 + b) * F.nlx + Z.lineoff[0] + l] : 0.f;
+          }
+#pragma unroll
+          for (int b = 0; b < PB; ++b)
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4) tile[b][ty + 8 * r4][tx] = v[b][r4];
+          __syncthreads();
+#pragma unroll
+          for (int r4 = 0; r4 < 4; ++r4) {  // line l0 + ty + 8 r4, point i0 + tx
+            const int l = l0 + ty + 8 * r4, i = i0 + tx;
+            if (l < l1 && i < Z.nx - 1) {
+              const int64_t p = Z.off + ((int64_t)(1 + l / iy) * Z.ny + 1 + l % iy) * Z.nx + i;
+#pragma unroll
+              for (int b = 0; b < PB; ++b) F.rdf[(int64_t)(e0 + b) * NP + p] = tile[b][tx][ty + 8 * r4];
+            }
+          }
+          __syncthreads();
+        }
+  }
+}
+
 // dst[m][p] = {rn(v), rn(v - rn(v))} of src[m][p] (5 planes)
 __global__ void __launch_bounds__(256) k_split_f2(const double* __restrict__ src, float2* __restrict__ dst, int64_t NP) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 5 * NP; t += (int64_t)gridDim.x * blockDim.x) {

@@ -499,10 +499,14 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
         o[0] = df_mul(c.bt, df_sub(v[3], v[4])); o[1] = df_neg(v[2]); o[2] = v[1];
         o[3] = df_sub(t2, t1); o[4] = df_add(t1, t2);
       }
+      // x: in place of b in the x-line-major copy (k_xline_back moves it
+      // to rdf); y: rdf
 #pragma unroll
       for (int m = 0; m < 5; ++m) {
-        F.rdf[m * NP + pt] = o[m].hi;
-        F.rdf[(5 + m) * NP + pt] = o[m].lo;
+        float* dst = DIR == 0 ? F.rdx + ((int64_t)p * 10 + m) * F.nlx + Ln.gl : F.rdf + m * NP + pt;
+        const int64_t lo_off = DIR == 0 ? 5 * F.nlx : 5 * NP;
+        dst[0] = o[m].hi;
+        dst[lo_off] = o[m].lo;
       }
     } else {  // tzetar in FP64, then add
       double r[5];

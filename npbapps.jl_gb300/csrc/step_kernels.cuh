@@ -1747,9 +1747,13 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
     for (int m = 0; m < 5; ++m) {
       const float xv = *S(slot, 30 + m);
       if (OUT_DF) {
+        // x: in place of b in the x-line-major copy (k_xline_back moves it
+        // to rdf); y: rdf
         const df64 v = df_two_sum(xv, d[m]);
-        bdf[m * NP + pt] = v.hi;
-        bdf[(5 + m) * NP + pt] = v.lo;
+        float* o = DIR == 0 ? F.rdx + ((int64_t)p * 10 + m) * F.nlx + gl : bdf + m * NP + pt;
+        const int64_t lo_off = DIR == 0 ? 5 * F.nlx : 5 * NP;
+        o[0] = v.hi;
+        o[lo_off] = v.lo;
       } else {
         const double v = (double)xv + (double)d[m];
         rhs[m * NP + pt] = v;
@@ -2438,16 +2442,18 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
     k_sp_refine_pl<D, OD><<<item_grid((const void*)k_sp_refine_pl<D, OD>, nwork, tpb, sm_r, persist), tpb, sm_r,   \
                             s>>>(F, K, work, nwork, scr, nlt, add_u, x0);                                         \
   } while (0)
-    if (dir == 0) NPBMZ_SPL(0, true);
-    else if (dir == 1) NPBMZ_SPL(1, true);
+    if (dir == 0) {
+      NPBMZ_SPL(0, true);
+      k_xline_back<<<nwork, 256, 0, s>>>(F, work, nwork, tpb);
+    } else if (dir == 1) NPBMZ_SPL(1, true);
     else NPBMZ_SPL(2, false);
 #undef NPBMZ_SPL
     return;
   }
   if (mode == 4 && !sp) {
     // one fused step: b of the x sweep comes from compute_rhs's double-float
-    // copy, x and y hand their results on as double-float, z writes FP64
-    // rhs (and u)
+    // copy, x and y hand their results on as double-float (x through its
+    // x-line-major copy), z writes FP64 rhs (and u)
     float* scr = reinterpret_cast<float*>(scratch);
     float* x0 = reinterpret_cast<float*>(xw);
     const size_t sm_m = pl_mixed_smem(tpb), sm_r = pl_refine_smem(tpb, dir != 2);
@@ -2458,8 +2464,10 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
     k_bt_refine_pl<D, OD><<<item_grid((const void*)k_bt_refine_pl<D, OD>, nwork, tpb, sm_r, persist), tpb, sm_r,   \
                             s>>>(F, K, work, nwork, scr, nlt, add_u, x0);                                        \
   } while (0)
-    if (dir == 0) NPBMZ_PL(0, true);
-    else if (dir == 1) NPBMZ_PL(1, true);
+    if (dir == 0) {
+      NPBMZ_PL(0, true);
+      k_xline_back<<<nwork, 256, 0, s>>>(F, work, nwork, tpb);
+    } else if (dir == 1) NPBMZ_PL(1, true);
     else NPBMZ_PL(2, false);
 #undef NPBMZ_PL
     return;
