@@ -62,6 +62,29 @@ Consts make_consts(double dt, int gx, int gy, int gz, int xz, int yz) {
   k.yycon4 = c3c4ty3 * k.con16 * k.ty3; k.yycon5 = c3c4ty3 * k.c1c5 * k.ty3;
   k.zzcon1 = c3c4tz3 * k.con43 * k.tz3; k.zzcon2 = c3c4tz3 * k.tz3; k.zzcon3 = c3c4tz3 * k.conz1 * k.tz3;
   k.zzcon4 = c3c4tz3 * k.con16 * k.tz3; k.zzcon5 = c3c4tz3 * k.c1c5 * k.tz3;
+  // FP32 and double-float copies for the FP32 sweeps
+  auto pr = [](double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+  };
+  k.f_c1 = (float)k.c1; k.f_c2 = (float)k.c2; k.f_c3 = (float)k.c3; k.f_c4 = (float)k.c4;
+  k.f_c3c4 = (float)k.c3c4; k.f_c1345 = (float)k.c1345; k.f_con43 = (float)k.con43; k.f_c1c5 = (float)k.c1c5;
+  k.f_comz1 = (float)k.comz1; k.f_comz4 = (float)k.comz4; k.f_comz5 = (float)k.comz5; k.f_comz6 = (float)k.comz6;
+  const double dtt1[3] = {k.dttx1, k.dtty1, k.dttz1}, dtt2[3] = {k.dttx2, k.dtty2, k.dttz2};
+  const double c2dtt1[3] = {k.c2dttx1, k.c2dtty1, k.c2dttz1}, dmax[3] = {k.dxmax, k.dymax, k.dzmax};
+  const double dd[3][5] = {{k.dx1, k.dx2, k.dx3, k.dx4, k.dx5}, {k.dy1, k.dy2, k.dy3, k.dy4, k.dy5},
+                           {k.dz1, k.dz2, k.dz3, k.dz4, k.dz5}};
+  for (int d = 0; d < 3; ++d) {
+    k.f_dtt1[d] = (float)dtt1[d]; k.f_dtt2[d] = (float)dtt2[d]; k.f_c2dtt1[d] = (float)c2dtt1[d];
+    k.f_dmax[d] = (float)dmax[d];
+    k.p_dtt1[d] = pr(dtt1[d]); k.p_dtt2[d] = pr(dtt2[d]); k.p_c2dtt1[d] = pr(c2dtt1[d]); k.p_dmax[d] = pr(dmax[d]);
+    for (int m = 0; m < 5; ++m) { k.f_d[d][m] = (float)dd[d][m]; k.p_d[d][m] = pr(dd[d][m]); }
+  }
+  k.p_c1 = pr(k.c1); k.p_c2 = pr(k.c2); k.p_two_m_c2 = pr(2.0 - k.c2);
+  k.p_k43 = pr(k.con43 * k.c3c4); k.p_c3c4 = pr(k.c3c4); k.p_c1345 = pr(k.c1345);
+  k.p_k43m = pr(k.con43 * k.c3c4 - k.c1345); k.p_c3c4m = pr(k.c3c4 - k.c1345);
+  k.p_con43 = pr(k.con43); k.p_c1c5 = pr(k.c1c5); k.p_comz1 = pr(k.comz1); k.p_comz4 = pr(k.comz4);
+  k.p_comz5 = pr(k.comz5); k.p_comz6 = pr(k.comz6); k.p_bt = pr(k.bt);
   return k;
 }
 

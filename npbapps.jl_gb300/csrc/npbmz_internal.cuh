@@ -28,7 +28,26 @@ struct Consts {
   double xxcon1, xxcon2, xxcon3, xxcon4, xxcon5;
   double yycon1, yycon2, yycon3, yycon4, yycon5;
   double zzcon1, zzcon2, zzcon3, zzcon4, zzcon5;
+  // FP32 values (f_) and double-float pairs (p_: {rn(v), rn(v - rn(v))}) of
+  // the constants that the FP32 sweeps and their refinement passes read,
+  // formed on the host so that no kernel converts them: on GB300 every
+  // FP64-to-FP32 conversion is an instruction of the 1/64-rate FP64 pipe.
+  // Index [d] is the sweep direction; f_d / p_d hold dx1..dx5, dy1..dy5,
+  // dz1..dz5.
+  float f_c1, f_c2, f_c3, f_c4, f_c3c4, f_c1345, f_con43, f_c1c5, f_comz1, f_comz4, f_comz5, f_comz6;
+  float f_dtt1[3], f_dtt2[3], f_c2dtt1[3], f_d[3][5], f_dmax[3];
+  float2 p_c1, p_c2, p_two_m_c2, p_k43, p_c3c4, p_c1345, p_k43m, p_c3c4m;
+  float2 p_con43, p_c1c5, p_comz1, p_comz4, p_comz5, p_comz6, p_bt;
+  float2 p_dtt1[3], p_dtt2[3], p_c2dtt1[3], p_d[3][5], p_dmax[3];
 };
+
+// The FP32 (T = float) or FP64 (T = double) copy of a constant.
+template <typename T>
+__host__ __device__ inline T kv(double d, float f);
+template <>
+__host__ __device__ inline float kv<float>(double, float f) { return f; }
+template <>
+__host__ __device__ inline double kv<double>(double d, float) { return d; }
 
 struct ZoneDev {
   int nx, ny, nz, pad;

@@ -54,8 +54,6 @@ __device__ __forceinline__ void acc_sub2(DAcc& a, float2 x) {  // a -= 2x (exact
   acc_exact(a, __fmul_rn(-2.f, x.x));
 }
 
-__device__ __forceinline__ df64 f2df(float2 v) { return {v.x, v.y}; }
-__device__ __forceinline__ float2 df2f(df64 v) { return make_float2(v.hi, v.lo); }
 __device__ __forceinline__ double df_to_double(df64 v) { return (double)v.hi + (double)v.lo; }
 
 // 1/a: FP32 estimate x, residual e = 1 - a x formed exactly to first order

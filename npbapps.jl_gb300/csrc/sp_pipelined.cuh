@@ -34,21 +34,21 @@ struct SpDfK {
 template <int DIR>
 __device__ __forceinline__ SpDfK sp_df_consts(const Consts& K) {
   SpDfK c;
-  c.dtt1 = df_from(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
-  c.dtt2 = df_from(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
-  c.c2dtt1 = df_from(DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1);
-  c.comz1 = df_from(K.comz1);
-  c.comz4 = df_from(K.comz4);
-  c.comz5 = df_from(K.comz5);
-  c.comz6 = df_from(K.comz6);
-  c.c3c4 = df_from(K.c3c4);
-  c.con43 = df_from(K.con43);
-  c.c1c5 = df_from(K.c1c5);
-  c.da = df_from(DIR == 0 ? K.dx2 : DIR == 1 ? K.dy3 : K.dz4);
-  c.db = df_from(DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5);
-  c.dm = df_from(DIR == 0 ? K.dxmax : DIR == 1 ? K.dymax : K.dzmax);
-  c.dc = df_from(DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1);
-  c.bt = df_from(K.bt);
+  c.dtt1 = f2df(K.p_dtt1[DIR]);
+  c.dtt2 = f2df(K.p_dtt2[DIR]);
+  c.c2dtt1 = f2df(K.p_c2dtt1[DIR]);
+  c.comz1 = f2df(K.p_comz1);
+  c.comz4 = f2df(K.p_comz4);
+  c.comz5 = f2df(K.p_comz5);
+  c.comz6 = f2df(K.p_comz6);
+  c.c3c4 = f2df(K.p_c3c4);
+  c.con43 = f2df(K.p_con43);
+  c.c1c5 = f2df(K.p_c1c5);
+  c.da = f2df(K.p_d[DIR][DIR + 1]);
+  c.db = f2df(K.p_d[DIR][4]);
+  c.dm = f2df(K.p_dmax[DIR]);
+  c.dc = f2df(K.p_d[DIR][0]);
+  c.bt = f2df(K.p_bt);
   return c;
 }
 

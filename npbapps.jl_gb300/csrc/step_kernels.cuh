@@ -505,7 +505,8 @@ __host__ __device__ constexpr bool bnz(int a, int b) { return nnz(a, b) || a == 
 // z_solve.jl:537-618); only structural nonzeros are written.
 template <int DIR, typename T>
 __device__ __forceinline__ void bt_jac(const Consts& K, T tmp1, T u2, T u3, T u4, T u5, T q, T f[5][5], T n[5][5]) {
-  const T c1 = (T)K.c1, c2 = (T)K.c2, c3c4 = (T)K.c3c4, c1345 = (T)K.c1345, con43 = (T)K.con43;
+  const T c1 = kv<T>(K.c1, K.f_c1), c2 = kv<T>(K.c2, K.f_c2), c3c4 = kv<T>(K.c3c4, K.f_c3c4);
+  const T c1345 = kv<T>(K.c1345, K.f_c1345), con43 = kv<T>(K.con43, K.f_con43);
   const T tmp2 = tmp1 * tmp1;
   const T tmp3 = tmp1 * tmp2;
   if (DIR == 0) {
@@ -569,7 +570,7 @@ __device__ __forceinline__ void bt_jac(const Consts& K, T tmp1, T u2, T u3, T u4
     n[4][3] = (c3c4 - c1345) * tmp2 * u4;
     n[4][4] = (c1345) * tmp1;
   } else {
-    const T c3 = (T)K.c3, c4 = (T)K.c4;
+    const T c3 = kv<T>(K.c3, K.f_c3), c4 = kv<T>(K.c4, K.f_c4);
     f[0][3] = (T)1.0;
     f[1][0] = -(u2 * u4) * tmp2;
     f[1][1] = u4 * tmp1;
@@ -714,12 +715,14 @@ __global__ void __launch_bounds__(128) k_bt_solve(Fields F, Consts K, const Work
   const int64_t NP = F.NP;
   double* __restrict__ rhs = F.rhs;
 
-  const T tmp1 = (T)(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
-  const T tmp2 = (T)(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  const T tmp1 = kv<T>(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1, K.f_dtt1[DIR]);
+  const T tmp2 = kv<T>(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2, K.f_dtt2[DIR]);
+  const double d64[5] = {DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1, DIR == 0 ? K.dx2 : DIR == 1 ? K.dy2 : K.dz2,
+                         DIR == 0 ? K.dx3 : DIR == 1 ? K.dy3 : K.dz3, DIR == 0 ? K.dx4 : DIR == 1 ? K.dy4 : K.dz4,
+                         DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5};
   T dd[5];
-  if (DIR == 0) { dd[0] = (T)K.dx1; dd[1] = (T)K.dx2; dd[2] = (T)K.dx3; dd[3] = (T)K.dx4; dd[4] = (T)K.dx5; }
-  else if (DIR == 1) { dd[0] = (T)K.dy1; dd[1] = (T)K.dy2; dd[2] = (T)K.dy3; dd[3] = (T)K.dy4; dd[4] = (T)K.dy5; }
-  else { dd[0] = (T)K.dz1; dd[1] = (T)K.dz2; dd[2] = (T)K.dz3; dd[3] = (T)K.dz4; dd[4] = (T)K.dz5; }
+#pragma unroll
+  for (int m = 0; m < 5; ++m) dd[m] = kv<T>(d64[m], K.f_d[DIR][m]);
 
   T rp[5];          // r' at p-1
   T Cp[5][5];       // C' at p-1
@@ -894,11 +897,10 @@ struct BtF32Carry {
 
 template <int DIR>
 __device__ __forceinline__ void bt_f32_consts(const Consts& K, float& tmp1, float& tmp2, float dd[5]) {
-  tmp1 = (float)(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
-  tmp2 = (float)(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
-  if (DIR == 0) { dd[0] = (float)K.dx1; dd[1] = (float)K.dx2; dd[2] = (float)K.dx3; dd[3] = (float)K.dx4; dd[4] = (float)K.dx5; }
-  else if (DIR == 1) { dd[0] = (float)K.dy1; dd[1] = (float)K.dy2; dd[2] = (float)K.dy3; dd[3] = (float)K.dy4; dd[4] = (float)K.dy5; }
-  else { dd[0] = (float)K.dz1; dd[1] = (float)K.dz2; dd[2] = (float)K.dz3; dd[3] = (float)K.dz4; dd[4] = (float)K.dz5; }
+  tmp1 = K.f_dtt1[DIR];
+  tmp2 = K.f_dtt2[DIR];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) dd[m] = K.f_d[DIR][m];
 }
 
 // Start of the elimination: Jacobians at points 0 and 1 (FP32 state s0, s1 =
@@ -1219,6 +1221,8 @@ __device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
   return df_quick(p, e);
 }
 __device__ __forceinline__ df64 df_scale2(df64 a) { return {2.f * a.hi, 2.f * a.lo}; }  // exact
+__device__ __forceinline__ df64 f2df(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ float2 df2f(df64 v) { return make_float2(v.hi, v.lo); }
 __device__ __forceinline__ df64 df_from(double d) {
   const float h = __double2float_rn(d);
   return {h, __double2float_rn(d - (double)h)};
@@ -1294,16 +1298,14 @@ __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const 
   double* __restrict__ rhs = F.rhs;
   float* __restrict__ bdf = F.rdf;
 
-  const df64 t1 = df_from(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
-  const df64 t2 = df_from(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  const df64 t1 = f2df(K.p_dtt1[DIR]);
+  const df64 t2 = f2df(K.p_dtt2[DIR]);
   df64 D[5];
-  if (DIR == 0) { D[0] = df_from(K.dx1); D[1] = df_from(K.dx2); D[2] = df_from(K.dx3); D[3] = df_from(K.dx4); D[4] = df_from(K.dx5); }
-  else if (DIR == 1) { D[0] = df_from(K.dy1); D[1] = df_from(K.dy2); D[2] = df_from(K.dy3); D[3] = df_from(K.dy4); D[4] = df_from(K.dy5); }
-  else { D[0] = df_from(K.dz1); D[1] = df_from(K.dz2); D[2] = df_from(K.dz3); D[3] = df_from(K.dz4); D[4] = df_from(K.dz5); }
-  const df64 c1 = df_from(K.c1), c2 = df_from(K.c2), two_m_c2 = df_from(2.0 - K.c2);
-  const double k43d = K.con43 * K.c3c4;
-  const df64 k43 = df_from(k43d), c3c4 = df_from(K.c3c4), c1345 = df_from(K.c1345);
-  const df64 k43m = df_from(k43d - K.c1345), c3c4m = df_from(K.c3c4 - K.c1345);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) D[m] = f2df(K.p_d[DIR][m]);
+  const df64 c1 = f2df(K.p_c1), c2 = f2df(K.p_c2), two_m_c2 = f2df(K.p_two_m_c2);
+  const df64 k43 = f2df(K.p_k43), c3c4 = f2df(K.p_c3c4), c1345 = f2df(K.p_c1345);
+  const df64 k43m = f2df(K.p_k43m), c3c4m = f2df(K.p_c3c4m);
 
   auto load_x = [&](int q, df64 x[5]) {
     const int64_t pt = base + (int64_t)q * st;
@@ -1600,16 +1602,14 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
     return DIR == 0 ? F.x0x + ((int64_t)q * 5 + m) * F.nlx + gl : x0f + m * NP + base + (int64_t)q * st;
   };
 
-  const df64 t1 = df_from(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
-  const df64 t2 = df_from(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
+  const df64 t1 = f2df(K.p_dtt1[DIR]);
+  const df64 t2 = f2df(K.p_dtt2[DIR]);
   df64 D[5];
-  if (DIR == 0) { D[0] = df_from(K.dx1); D[1] = df_from(K.dx2); D[2] = df_from(K.dx3); D[3] = df_from(K.dx4); D[4] = df_from(K.dx5); }
-  else if (DIR == 1) { D[0] = df_from(K.dy1); D[1] = df_from(K.dy2); D[2] = df_from(K.dy3); D[3] = df_from(K.dy4); D[4] = df_from(K.dy5); }
-  else { D[0] = df_from(K.dz1); D[1] = df_from(K.dz2); D[2] = df_from(K.dz3); D[3] = df_from(K.dz4); D[4] = df_from(K.dz5); }
-  const df64 c1 = df_from(K.c1), c2 = df_from(K.c2), two_m_c2 = df_from(2.0 - K.c2);
-  const double k43d = K.con43 * K.c3c4;
-  const df64 k43 = df_from(k43d), c3c4 = df_from(K.c3c4), c1345 = df_from(K.c1345);
-  const df64 k43m = df_from(k43d - K.c1345), c3c4m = df_from(K.c3c4 - K.c1345);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) D[m] = f2df(K.p_d[DIR][m]);
+  const df64 c1 = f2df(K.p_c1), c2 = f2df(K.p_c2), two_m_c2 = f2df(K.p_two_m_c2);
+  const df64 k43 = f2df(K.p_k43), c3c4 = f2df(K.p_c3c4), c1345 = f2df(K.p_c1345);
+  const df64 k43m = f2df(K.p_k43m), c3c4m = f2df(K.p_c3c4m);
 
   auto pq = [&](const df64 s[6], const df64 x[5], df64 P[5], df64 Q[5]) {
     df64 Fq[5], Nq[5];
@@ -1799,10 +1799,11 @@ __device__ __forceinline__ void sp_assemble(const Consts& K, int q, int n, const
     for (int s = 0; s < 3; ++s) { L[s][0] = (T)0.0; L[s][1] = (T)0.0; L[s][2] = (T)1.0; L[s][3] = (T)0.0; L[s][4] = (T)0.0; }
     return;
   }
-  const G dtt1 = (G)(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1);
-  const G dtt2 = (G)(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2);
-  const G c2dtt1 = (G)(DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1);
-  const G comz1 = (G)K.comz1, comz4 = (G)K.comz4, comz5 = (G)K.comz5, comz6 = (G)K.comz6;
+  const G dtt1 = kv<G>(DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1, K.f_dtt1[DIR]);
+  const G dtt2 = kv<G>(DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2, K.f_dtt2[DIR]);
+  const G c2dtt1 = kv<G>(DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1, K.f_c2dtt1[DIR]);
+  const G comz1 = kv<G>(K.comz1, K.f_comz1), comz4 = kv<G>(K.comz4, K.f_comz4);
+  const G comz5 = kv<G>(K.comz5, K.f_comz5), comz6 = kv<G>(K.comz6, K.f_comz6);
   G L1 = (G)0.0;
   G L2 = -dtt2 * cv[0] - dtt1 * rhon[0];
   G L3 = (G)1.0 + c2dtt1 * rhon[1];
@@ -2064,13 +2065,13 @@ __device__ __forceinline__ void sp_transform(const Fields& F, const Consts& K, i
 // Geometry of one point for the SP band assembly, generic in the type.
 template <int DIR, typename G>
 __device__ __forceinline__ void sp_geom_t(G ri, G cvel, G spd_in, const Consts& K, G& cv, G& rhon, G& spd) {
-  const G ru1 = (G)K.c3c4 * ri;
+  const G ru1 = kv<G>(K.c3c4, K.f_c3c4) * ri;
   cv = cvel;
-  const G da = (G)(DIR == 0 ? K.dx2 : DIR == 1 ? K.dy3 : K.dz4);
-  const G db = (G)(DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5);
-  const G dm = (G)(DIR == 0 ? K.dxmax : DIR == 1 ? K.dymax : K.dzmax);
-  const G dc = (G)(DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1);
-  rhon = fmax(fmax(fmax(da + (G)K.con43 * ru1, db + (G)K.c1c5 * ru1), dm + ru1), dc);
+  const G da = kv<G>(DIR == 0 ? K.dx2 : DIR == 1 ? K.dy3 : K.dz4, K.f_d[DIR][DIR + 1]);
+  const G db = kv<G>(DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5, K.f_d[DIR][4]);
+  const G dm = kv<G>(DIR == 0 ? K.dxmax : DIR == 1 ? K.dymax : K.dzmax, K.f_dmax[DIR]);
+  const G dc = kv<G>(DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1, K.f_d[DIR][0]);
+  rhon = fmax(fmax(fmax(da + kv<G>(K.con43, K.f_con43) * ru1, db + kv<G>(K.c1c5, K.f_c1c5) * ru1), dm + ru1), dc);
   spd = spd_in;
 }
 
