@@ -84,7 +84,7 @@ Consts make_consts(double dt, int gx, int gy, int gz, int xz, int yz) {
   k.p_k43 = pr(k.con43 * k.c3c4); k.p_c3c4 = pr(k.c3c4); k.p_c1345 = pr(k.c1345);
   k.p_k43m = pr(k.con43 * k.c3c4 - k.c1345); k.p_c3c4m = pr(k.c3c4 - k.c1345);
   k.p_con43 = pr(k.con43); k.p_c1c5 = pr(k.c1c5); k.p_comz1 = pr(k.comz1); k.p_comz4 = pr(k.comz4);
-  k.p_comz5 = pr(k.comz5); k.p_comz6 = pr(k.comz6); k.p_bt = pr(k.bt);
+  k.p_comz5 = pr(k.comz5); k.p_comz6 = pr(k.comz6); k.p_bt = pr(k.bt); k.p_c2iv = pr(k.c2iv);
   return k;
 }
 

@@ -37,7 +37,7 @@ struct Consts {
   float f_c1, f_c2, f_c3, f_c4, f_c3c4, f_c1345, f_con43, f_c1c5, f_comz1, f_comz4, f_comz5, f_comz6;
   float f_dtt1[3], f_dtt2[3], f_c2dtt1[3], f_d[3][5], f_dmax[3];
   float2 p_c1, p_c2, p_two_m_c2, p_k43, p_c3c4, p_c1345, p_k43m, p_c3c4m;
-  float2 p_con43, p_c1c5, p_comz1, p_comz4, p_comz5, p_comz6, p_bt;
+  float2 p_con43, p_c1c5, p_comz1, p_comz4, p_comz5, p_comz6, p_bt, p_c2iv;
   float2 p_dtt1[3], p_dtt2[3], p_c2dtt1[3], p_d[3][5], p_dmax[3];
 };
 

@@ -9,8 +9,7 @@
 // transformations on the FP32 pipe: Knuth's two-sum, the FMA two-product,
 // Dekker's normalisation, and one Newton step for 1/x and sqrt(x) from the
 // FP32 estimate.  No FP64 arithmetic runs except the conversions of the
-// planes that stay FP64 (prim for single phases and SP's z sweep; rhs
-// outside a fused step).
+// planes that stay FP64 outside a fused step (prim, rhs).
 //
 // The statements are compute_rhs's (src/BT/rhs.jl:62-460, SP
 // src/SP/rhs.jl:62-452 and txinvr src/SP/txinvr.jl:28-49) in the regrouped
@@ -54,18 +53,7 @@ __device__ __forceinline__ void acc_sub2(DAcc& a, float2 x) {  // a -= 2x (exact
   acc_exact(a, __fmul_rn(-2.f, x.x));
 }
 
-__device__ __forceinline__ double df_to_double(df64 v) { return (double)v.hi + (double)v.lo; }
 
-// 1/a: FP32 estimate x, residual e = 1 - a x formed exactly to first order
-// (a.hi x = p + pe exactly; 1 - p is exact since p is within 2^-23 of 1),
-// then x + x e.
-__device__ __forceinline__ df64 df_rcp(df64 a) {
-  const float x = __frcp_rn(a.hi);
-  const float p = __fmul_rn(a.hi, x);
-  const float pe = __fmaf_rn(a.hi, x, -p);
-  const float e = __fmaf_rn(-a.lo, x, __fsub_rn(__fsub_rn(1.f, p), pe));
-  return df_quick(x, __fmul_rn(x, e));
-}
 // sqrt(a), a > 0: FP32 estimate x, a - x^2 formed exactly to first order,
 // then x + (a - x^2) / (2x).
 __device__ __forceinline__ df64 df_sqrt(df64 a) {
@@ -128,13 +116,14 @@ __device__ __forceinline__ void prim_df_point(const Fields& F, const RhsDfConsts
       F.primf[e * NP + p] = v[e].hi;
       F.primf[(PS_HI_COUNT + e) * NP + p] = v[e].lo;
     }
-    // the z sweep's tzetar and add run in FP64 from these
-    F.prim[PR_US * NP + p] = df_to_double(us);
-    F.prim[PR_VS * NP + p] = df_to_double(vs);
-    F.prim[PR_WS * NP + p] = df_to_double(ws);
-    F.prim[PR_QS * NP + p] = df_to_double(qs);
-    F.prim[PR_SPEED * NP + p] = df_to_double(speed);
-    F.prim[PR_AINV * NP + p] = df_to_double(df_rcp(speed));
+    if (F.prim64) {  // the FP64 SP sweeps of single phases read these
+      F.prim[PR_US * NP + p] = df_to_double(us);
+      F.prim[PR_VS * NP + p] = df_to_double(vs);
+      F.prim[PR_WS * NP + p] = df_to_double(ws);
+      F.prim[PR_QS * NP + p] = df_to_double(qs);
+      F.prim[PR_SPEED * NP + p] = df_to_double(speed);
+      F.prim[PR_AINV * NP + p] = df_to_double(df_rcp(speed));
+    }
   } else {
     const df64 v[PF_HI_COUNT] = {ri, qs, u[1], u[2], u[3], u[4]};
 #pragma unroll

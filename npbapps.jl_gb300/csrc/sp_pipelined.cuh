@@ -7,8 +7,10 @@
 //   pass 1: L x0 = b in FP32 (bands from the FP32 state copies);
 //   pass 2: r = b - L x0 with the bands assembled in double-float from the
 //           FP32 pairs of the state, L d = r in FP32, x = x0 + d,
-// so that no FP64 arithmetic runs except in the z sweep's output (tzetar and
-// add, src/SP/tzetar.jl:27-52, src/SP/add.jl:14-23).  The x and y sweeps hand
+// so that no FP64 arithmetic runs except in the z sweep's output: add
+// (src/SP/add.jl:14-23) in FP64, after tzetar (src/SP/tzetar.jl:27-52) in
+// double-float from the double-float primitives of the double-float
+// compute_rhs, or in FP64 from the FP64 ones (NPBMZ_RHS_FP64).  The x and y sweeps hand
 // their transformed results (ninvr, src/SP/ninvr.jl:19-32; pinvr,
 // src/SP/pinvr.jl:20-33, applied in double-float) to the next sweep as
 // double-float planes.  Each thread streams its line's data PIPE points ahead
@@ -473,12 +475,24 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
         } else {
           cpa8(SU(slot, 0), F.u + pt);
         }
-        cpa8(SU(slot, 5), F.prim + PR_US * NP + pt);
-        cpa8(SU(slot, 6), F.prim + PR_VS * NP + pt);
-        cpa8(SU(slot, 7), F.prim + PR_WS * NP + pt);
-        cpa8(SU(slot, 8), F.prim + PR_SPEED * NP + pt);
-        cpa8(SU(slot, 9), F.prim + PR_AINV * NP + pt);
-        cpa8(SU(slot, 10), F.prim + PR_QS * NP + pt);
+        if (F.xd) {  // double-float primitives (8-byte words: float2 pairs)
+          const float2* X = F.xd;
+          cpa8(SU(slot, 5), X + XD_US * NP + pt);
+          cpa8(SU(slot, 6), X + XD_VS * NP + pt);
+          cpa8(SU(slot, 7), X + XD_WS * NP + pt);
+          float* spd = reinterpret_cast<float*>(SU(slot, 8));
+          cpa4(spd, F.primf + PS_SPEED * NP + pt);
+          cpa4(spd + 1, F.primf + (PS_HI_COUNT + PS_SPEED) * NP + pt);
+          cpa8(SU(slot, 9), X + XD_QS * NP + pt);
+          cpa8(SU(slot, 10), F.ud + pt);
+        } else {
+          cpa8(SU(slot, 5), F.prim + PR_US * NP + pt);
+          cpa8(SU(slot, 6), F.prim + PR_VS * NP + pt);
+          cpa8(SU(slot, 7), F.prim + PR_WS * NP + pt);
+          cpa8(SU(slot, 8), F.prim + PR_SPEED * NP + pt);
+          cpa8(SU(slot, 9), F.prim + PR_AINV * NP + pt);
+          cpa8(SU(slot, 10), F.prim + PR_QS * NP + pt);
+        }
       }
     }
     cpa_commit();
@@ -507,6 +521,30 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
         const int64_t lo_off = DIR == 0 ? 5 * F.nlx : 5 * NP;
         dst[0] = o[m].hi;
         dst[lo_off] = o[m].lo;
+      }
+    } else if (F.xd) {  // tzetar in double-float, then add in FP64
+      df64 r[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) r[m] = df_two_sum(*S(slot, 11 + m), d[m]);
+      auto w2 = [&](int e) -> df64 { const float* q = reinterpret_cast<const float*>(SU(slot, e)); return {q[0], q[1]}; };
+      const df64 xvel = w2(5), yvel = w2(6), zvel = w2(7), ac = w2(8), qs = w2(9), uzik1 = w2(10);
+      const df64 acinv = df_rcp(ac);
+      const df64 btuz = df_mul(f2df(K.p_bt), uzik1);
+      const df64 t1 = df_mul(df_mul(btuz, acinv), df_add(r[3], r[4]));
+      const df64 t2 = df_add(r[2], t1);
+      const df64 t3 = df_mul(btuz, df_sub(r[3], r[4]));
+      df64 o[5];
+      o[0] = t2;
+      o[1] = df_add(df_neg(df_mul(uzik1, r[1])), df_mul(xvel, t2));
+      o[2] = df_add(df_mul(uzik1, r[0]), df_mul(yvel, t2));
+      o[3] = df_add(df_mul(zvel, t2), t3);
+      o[4] = df_add(df_add(df_mul(uzik1, df_sub(df_mul(yvel, r[0]), df_mul(xvel, r[1]))), df_mul(qs, t2)),
+                    df_add(df_mul(df_mul(f2df(K.p_c2iv), df_mul(ac, ac)), t1), df_mul(zvel, t3)));
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const double v = df_to_double(o[m]);
+        F.rhs[m * NP + pt] = v;
+        if (add_u) F.u[m * NP + pt] = *SU(slot, m) + v;
       }
     } else {  // tzetar in FP64, then add
       double r[5];

@@ -1222,6 +1222,27 @@ __device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
 }
 __device__ __forceinline__ df64 df_scale2(df64 a) { return {2.f * a.hi, 2.f * a.lo}; }  // exact
 __device__ __forceinline__ df64 f2df(float2 v) { return {v.x, v.y}; }
+// FP32 -> FP64 (exact) from the bit pattern: sign, exponent rebiased by
+// 1023 - 127, significand shifted into place; zero, subnormals, inf and nan
+// take the conversion instruction, which on GB300 is an FP64-pipe slot.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e - 1u >= 254u) return (double)f;
+  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b >> 3) & 0xfffffu);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+__device__ __forceinline__ double df_to_double(df64 v) { return f32_to_f64(v.hi) + f32_to_f64(v.lo); }
+// 1/a: FP32 estimate x, residual e = 1 - a x formed exactly to first order
+// (a.hi x = p + pe exactly; 1 - p is exact since p is within 2^-23 of 1),
+// then x + x e.
+__device__ __forceinline__ df64 df_rcp(df64 a) {
+  const float x = __frcp_rn(a.hi);
+  const float p = __fmul_rn(a.hi, x);
+  const float pe = __fmaf_rn(a.hi, x, -p);
+  const float e = __fmaf_rn(-a.lo, x, __fsub_rn(__fsub_rn(1.f, p), pe));
+  return df_quick(x, __fmul_rn(x, e));
+}
 __device__ __forceinline__ float2 df2f(df64 v) { return make_float2(v.hi, v.lo); }
 __device__ __forceinline__ df64 df_from(double d) {
   const float h = __double2float_rn(d);
