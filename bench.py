@@ -51,12 +51,12 @@ SEED = 20261203
 BYTES_PER_POINT = {"prim": 40.0, "rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
 # Kernels of each phase of the batched step (for the per-kernel ncu figures).
 PHASE_KERNELS = {
-    ("BT", "mixed"): {"prim": ["k_prim_df<0>"], "rhs": ["k_rhs_df<0, 0>"],
-                      "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>"],
+    ("BT", "mixed"): {"prim": ["k_prim_df<0>", "k_xline_copy<0>"], "rhs": ["k_rhs_df<0, 0>"],
+                      "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>", "k_xline_back"],
                       "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
                       "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
-    ("SP", "mixed"): {"prim": ["k_prim_df<1>"], "rhs": ["k_rhs_df<1, 0>"],
-                      "x": ["k_sp_mixed_pl<0>", "k_sp_refine_pl<0, 1>"],
+    ("SP", "mixed"): {"prim": ["k_prim_df<1>", "k_xline_copy<1>"], "rhs": ["k_rhs_df<1, 0>"],
+                      "x": ["k_sp_mixed_pl<0>", "k_sp_refine_pl<0, 1>", "k_xline_back"],
                       "y": ["k_sp_mixed_pl<1>", "k_sp_refine_pl<1, 1>"],
                       "z": ["k_sp_mixed_pl<2>", "k_sp_refine_pl<2, 0>"]},
 }
@@ -283,9 +283,14 @@ def run_gpu(args):
         return p
 
     p = make(flags)
-    if args.autotune:
+    tuned = None
+    if not args.quick and not args.no_autotune:
+        # launch shapes, zone-group branches and persistent kernels, chosen by
+        # timing whole steps on this handle (results unchanged)
         p.autotune()
         p.setup(ce)
+        d = p.describe()
+        tuned = {k: d[k] for k in ("lines_per_cta", "zone_size_buckets", "step_groups", "persistent")}
     with ClockSampler(local) as clk:
         ms = time_steps(p, torch, stream, args.steps, args.warmup, dist)
     ms_max, value = whole_job(ms, pts, args.steps, world, dist)
@@ -307,15 +312,21 @@ def run_gpu(args):
         knames = (PHASE_KERNELS.get((kind, "mixed"), {}).get(top, [])
                   if flags & npbmz.MIXED and not flags & npbmz.RHS_FP64 else [])
         traffic = None
-        fp64_obj = None
+        issue_obj = None
         if km and knames and all(k in km for k in knames):
             traffic = sum(km[k]["dram_bytes_per_point"] for k in knames) * pts
-            flops_pt = sum(km[k]["fp64_flops_per_point"] for k in knames)
-            fp64_ach = flops_pt * pts / (ph[top] * 1e-3) / 1e9
-            fp64_obj = {"achieved": fp64_ach, "peak": fp64, "unit": "GFLOP/s", "frac": fp64_ach / fp64,
-                        "flops_per_point": flops_pt,
-                        "pipe_active_ncu": max(km[k]["fp64_pipe_active"] for k in knames),
-                        "peak_source": "npbmz_fp64_peak: FP64 FMA chains on this GPU, measured in this run"}
+            if all("inst_per_point" in km[k] for k in knames):
+                # instruction issue: 4 schedulers per SM, one warp instruction per cycle each
+                inst_pt = sum(km[k]["inst_per_point"] for k in knames)
+                nsm = torch.cuda.get_device_properties(local).multi_processor_count
+                mhz = clk.summary().get("sm_mhz") or 2070.0
+                peak_gi = 4 * nsm * mhz * 1e-3
+                ach_gi = inst_pt / 32 * pts / (ph[top] * 1e-3) / 1e9
+                issue_obj = {"achieved": ach_gi, "peak": peak_gi, "unit": "G warp-inst/s", "frac": ach_gi / peak_gi,
+                             "inst_per_point": inst_pt,
+                             "issue_active_ncu": {k: km[k]["issue_active"] for k in knames},
+                             "warps_per_sm_ncu": {k: km[k]["warps_per_sm"] for k in knames},
+                             "peak_source": "4 warp instructions per SM cycle x SMs x median SM clock of the timed run"}
         extra["roofline"] = {"bound": "hbm", "kernel": "+".join(knames) if knames else top, "phase": top,
                              "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                              "traffic": traffic,
@@ -324,7 +335,8 @@ def run_gpu(args):
                              if traffic is not None else None,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
                              "bytes_per_point": BYTES_PER_POINT[top], "launch_ms": ph[top],
-                             "binding_ceiling": "fp64" if fp64_obj else None, "fp64": fp64_obj}
+                             "binding_ceiling": "instruction issue (latency-bound sweeps)" if issue_obj else None,
+                             "issue": issue_obj}
         extra["phase_ms"] = ph
         extra["fp64_peak_gflops_measured"] = fp64
         # variants (fewer steps each)
@@ -358,7 +370,7 @@ def run_gpu(args):
         # uploaded and downloaded every step
         sizes = [npbmz.ref_elems(g.kind, npbmz.U, int(g.nx[z]), int(g.ny[z]), int(g.nz[z])) for z in range(g.nzones)]
         host = torch.empty(int(sum(sizes)), dtype=torch.float64, pin_memory=True)
-        q = make(flags)
+        q = p  # the timed (tuned) handle
         q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, host.data_ptr(), False)
         ptr = host.data_ptr()
         for _ in range(args.warmup):
@@ -372,7 +384,6 @@ def run_gpu(args):
             q.step(1)
             q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, False, sync=True)
         te = time.perf_counter() - t0
-        q.close()
         moved = 5 * 8 * pts
         extra["e2e"] = {"value": pts * world * args.steps / te / 1e6, "unit": "Mgridpt-steps/s",
                         "h2d_bytes_per_step": moved, "d2h_bytes_per_step": moved,
@@ -388,9 +399,12 @@ def run_gpu(args):
             "data": "synthetic",
             "config": {"workload": desc, "points_per_gpu": pts, "zones": g.nzones, "variant": args.variant,
                        "batched": True, "cuda_graph": bool(flags & npbmz.GRAPH),
-                       "line_solves": "fp32 + fp64-residual refinement" if flags & npbmz.MIXED else "fp64",
-                       "seed": SEED, "energy_row_scale": 2 ** escale,
-                       "l2": "state 1.7 GB >> 129 MB L2; no flush needed", "parallelism": f"replicas x{world}"},
+                       "line_solves": ("fp32 + double-float-residual refinement; primitives and compute_rhs "
+                                       + ("fp64" if flags & npbmz.RHS_FP64 else "double-float"))
+                       if flags & npbmz.MIXED else "fp64",
+                       "seed": SEED, "energy_row_scale": 2 ** escale, "autotuned": tuned,
+                       "l2": f"state {p.device_bytes / 1e9:.1f} GB >> 129 MB L2; no flush needed",
+                       "parallelism": f"replicas x{world}"},
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }
@@ -411,7 +425,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bt-c", choices=sorted(WORKLOADS))
     ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed-rhs64-graph", "mixed", "fp64"])
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="time the default launch configuration (the timed handle is autotuned otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="only the timed variant and its phase times (for profiler runs)")

@@ -177,7 +177,7 @@ int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_
  * branch.  Each branch starts when the previous group's compute_rhs is done,
  * so FP64-bound phases of one group run beside the FP32 sweeps of the
  * previous one.  Results are unchanged (zones are independent within a step
- * after exch_qbc).  npbmz_create sets 4 groups for NPBMZ_GRAPH handles with
+ * after exch_qbc).  npbmz_create sets 2 groups for NPBMZ_GRAPH handles with
  * at least 8 zones (not NPBMZ_EXACT or NPBMZ_PERZONE).  No counterpart in the
  * reference. */
 int npbmz_set_step_groups(npbmz_t* h, int groups);
@@ -188,8 +188,11 @@ int npbmz_set_stream(npbmz_t* h, void* stream);
 int npbmz_synchronize(npbmz_t* h);
 
 /* Autotune the launch shapes (threads per block and work-item size per
- * phase and zone-size bucket) by timing candidates on the handle's own data.
- * Leaves u, rhs and forcing as they were.  Synchronous. */
+ * phase and zone-size bucket), the number of zone-group branches of the step
+ * graph (NPBMZ_GRAPH) and persistent kernels on or off (the NPBMZ_PERSIST bit
+ * of the handle's flags) by timing candidates on the handle's own data; none
+ * of them changes the results.  Leaves u, rhs and forcing as they were.
+ * Synchronous.  No counterpart in the reference. */
 int npbmz_autotune(npbmz_t* h);
 
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (an FMA

@@ -405,6 +405,7 @@ def test_config2_autotuned_launch_shapes_keep_results(oracle_mod, flags):
     a.autotune()
     d = a.describe()
     assert d["zone_size_buckets"] in (1, 3) and len(d["lines_per_cta"]) == 3
+    assert d["persistent"] in (True, False)
     assert all(len(per_dir) == d["zone_size_buckets"] for per_dir in d["lines_per_cta"])
     assert all(t in (32, 64, 128) for per_dir in d["lines_per_cta"] for t in per_dir)
     for z in range(geom.nzones):
