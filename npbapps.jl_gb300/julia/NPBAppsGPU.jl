@@ -98,6 +98,14 @@ function step!(p::Problem, niter::Integer; norms = false)
     return nothing
 end
 
+"""Choose the launch configuration (lines per CTA, zone-group branches of the
+step graph, persistent kernels) by timing whole steps on the problem's own
+data; u, rhs and forcing are left as they were and results do not change."""
+function autotune!(p::Problem)
+    check(p, ccall((:npbmz_autotune, libnpbmz), Cint, (Ptr{Cvoid},), p.handle), "npbmz_autotune")
+    return nothing
+end
+
 """verify's node part (src/BT/verify.jl:411-505): (xcr, xce) summed over zones."""
 function verify(p::Problem)
     xcr = zeros(Cdouble, 5); xce = zeros(Cdouble, 5)
