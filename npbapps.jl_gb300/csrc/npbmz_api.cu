@@ -148,6 +148,18 @@ void make_rhs_df_consts(const Consts& k, const LinWeights& lw, RhsDfConsts& c) {
     c.con4[d] = split_const(c4[d]);
     c.con5[d] = split_const(c5[d]);
   }
+  // The low words of the stencil weights and t2 are dropped when none
+  // exceeds 2^-47 of its high word: below the compensated sum's own rounding
+  // (a few units of 2^-48 of the largest term), as for the class grids,
+  // whose d*t1 factors are integers plus a few FP64 roundings.
+  auto small_lo = [](float2 v) { return std::fabs((double)v.y) <= std::ldexp(std::fabs((double)v.x), -47); };
+  c.exact_w = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (!small_lo(c.t2[d])) c.exact_w = 0;
+    for (int cl = 0; cl < 32; ++cl)
+      for (int o = 0; o < 5; ++o)
+        if (!small_lo(c.w[d][cl][o])) c.exact_w = 0;
+  }
 }
 
 // A contiguous slice of a work list: items [lo, hi) belong to one zone.

@@ -100,6 +100,7 @@ struct RhsDfConsts {
   float2 t2[3];        // tx2, ty2, tz2
   float2 dt, c1, c2, c1c2, bt;
   float2 con3[3], con4[3], con5[3];  // xxcon3..5, yycon3..5, zzcon3..5
+  int exact_w;  // the low words of every w and t2 are at most 2^-47 of the high: left out
 };
 
 struct Fields {

@@ -37,12 +37,29 @@ __device__ __forceinline__ void acc_exact(DAcc& a, float p) {  // a += p, the ro
 }
 // a += w * x (w, x double-float): the FP32 product to s, its exact rounding
 // error and the two cross terms to c (w.lo * x.lo is below 2^-48)
+// (WX: w.lo is negligible and left out)
+template <bool WX = false>
 __device__ __forceinline__ void acc_mul(DAcc& a, float2 w, float2 x) {
   const float p = __fmul_rn(w.x, x.x);
   a.c = __fadd_rn(a.c, __fmaf_rn(w.x, x.x, -p));
   a.c = __fmaf_rn(w.x, x.y, a.c);
-  a.c = __fmaf_rn(w.y, x.x, a.c);
+  if (!WX) a.c = __fmaf_rn(w.y, x.x, a.c);
   acc_exact(a, p);
+}
+// a - b and a + b of double-float values: the rounded FP32 difference (sum)
+// of the high words, its exact error plus the low words' difference (sum) in
+// the second word (not renormalised)
+__device__ __forceinline__ float2 df_diff(float2 a, float2 b) {
+  const float s = __fsub_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  const float err = __fsub_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fadd_rn(b.x, bb));
+  return make_float2(s, __fadd_rn(err, __fsub_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 df_sum(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  return make_float2(s, __fadd_rn(err, __fadd_rn(a.y, b.y)));
 }
 __device__ __forceinline__ void acc_add(DAcc& a, float2 x) {  // a += x
   a.c = __fadd_rn(a.c, x.y);
@@ -157,8 +174,11 @@ __global__ void __launch_bounds__(128) k_prim_df(Fields F, RhsDfConsts C, const 
 
 // ---- compute_rhs -------------------------------------------------------------
 // One direction (stride st, position q of n): the stencil's four off-centre
-// points (weights W), the normal momentum and the fluxes (+-t2), the
-// velocities' off-centre points (vc) and the viscous energy term (1, -2, 1).
+// points (weights W), the differences of the normal momentum and the fluxes
+// (-t2), the sums of the velocities' off-centre points (vc) and the viscous
+// energy term (1, -2, 1).  WX: the low words of the weights and t2 are left
+// out (RhsDfConsts::exact_w).
+template <bool WX>
 __device__ __forceinline__ void rhs_dir_df(DAcc a[5], const float2* __restrict__ ud, int64_t NP, int64_t p, int64_t st,
                                            int q, int n, const float2* __restrict__ W, const float2* const fx[4],
                                            const float2* __restrict__ un, const float2* const vel[3],
@@ -170,31 +190,25 @@ __device__ __forceinline__ void rhs_dir_df(DAcc a[5], const float2* __restrict__
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
     const float2* um = ud + m * NP;
-    acc_mul(a[m], w1, um[p - st]);
-    acc_mul(a[m], w3, um[p + st]);
-    acc_mul(a[m], w0, um[pm2]);
-    acc_mul(a[m], w4, um[pp2]);
+    acc_mul<WX>(a[m], w1, um[p - st]);
+    acc_mul<WX>(a[m], w3, um[p + st]);
+    acc_mul<WX>(a[m], w0, um[pm2]);
+    acc_mul<WX>(a[m], w4, um[pp2]);
   }
-  acc_mul(a[0], mt2, un[p + st]);
-  acc_mul(a[0], t2, un[p - st]);
+  acc_mul<WX>(a[0], mt2, df_diff(un[p + st], un[p - st]));
 #pragma unroll
-  for (int m = 0; m < 4; ++m) {
-    acc_mul(a[m + 1], mt2, fx[m][p + st]);
-    acc_mul(a[m + 1], t2, fx[m][p - st]);
-  }
+  for (int m = 0; m < 4; ++m) acc_mul<WX>(a[m + 1], mt2, df_diff(fx[m][p + st], fx[m][p - st]));
 #pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    acc_mul(a[m + 1], vc[m], vel[m][p + st]);
-    acc_mul(a[m + 1], vc[m], vel[m][p - st]);
-  }
+  for (int m = 0; m < 3; ++m) acc_mul(a[m + 1], vc[m], df_sum(vel[m][p + st], vel[m][p - st]));
   acc_add(a[4], wv[p + st]);
   acc_add(a[4], wv[p - st]);
   acc_sub2(a[4], wv[p]);
 }
 
 // One thread per interior point; TX: txinvr after *dt (SP); NORM: this CTA's
-// sum of rhs^2 (before txinvr) into partials[item][5].
-template <bool TX, bool NORM>
+// sum of rhs^2 (before txinvr) into partials[item][5]; WX: the low words of
+// the stencil weights and t2 are left out (RhsDfConsts::exact_w).
+template <bool TX, bool NORM, bool WX>
 __global__ void __launch_bounds__(128) k_rhs_df(Fields F, RhsDfConsts C, const Work* __restrict__ work, int nwork,
                                                 double* __restrict__ partials) {
   __shared__ double red[NORM ? 5 * 128 : 1];
@@ -226,15 +240,15 @@ __global__ void __launch_bounds__(128) k_rhs_df(Fields F, RhsDfConsts C, const W
       const float2* Wz = wt + (2 * 32 + dissip_class(k, Z.nz)) * 5;
       {
         const float2* fx[4] = {X + PX_XX * NP, X + PX_UV * NP, X + PX_UW * NP, X + PX_EX * NP};
-        rhs_dir_df(a, ud, NP, p, 1, i, Z.nx, Wx, fx, ud + NP, vel, C.vc[0], X + PX_WX * NP, C.t2[0]);
+        rhs_dir_df<WX>(a, ud, NP, p, 1, i, Z.nx, Wx, fx, ud + NP, vel, C.vc[0], X + PX_WX * NP, C.t2[0]);
       }
       {
         const float2* fx[4] = {X + PX_UV * NP, X + PX_YY * NP, X + PX_VW * NP, X + PX_EY * NP};
-        rhs_dir_df(a, ud, NP, p, Z.nx, j, Z.ny, Wy, fx, ud + 2 * NP, vel, C.vc[1], X + PX_WY * NP, C.t2[1]);
+        rhs_dir_df<WX>(a, ud, NP, p, Z.nx, j, Z.ny, Wy, fx, ud + 2 * NP, vel, C.vc[1], X + PX_WY * NP, C.t2[1]);
       }
       {
         const float2* fx[4] = {X + PX_UW * NP, X + PX_VW * NP, X + PX_ZZ * NP, X + PX_EZ * NP};
-        rhs_dir_df(a, ud, NP, p, (int64_t)Z.nx * Z.ny, k, Z.nz, Wz, fx, ud + 3 * NP, vel, C.vc[2], X + PX_WZ * NP,
+        rhs_dir_df<WX>(a, ud, NP, p, (int64_t)Z.nx * Z.ny, k, Z.nz, Wz, fx, ud + 3 * NP, vel, C.vc[2], X + PX_WZ * NP,
                    C.t2[2]);
       }
       // centre point: the three directions' weights summed first

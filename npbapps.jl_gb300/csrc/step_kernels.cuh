@@ -2575,9 +2575,15 @@ void launch_prim_df(bool sp, const Fields& F, const RhsDfConsts& C, const Work* 
 void launch_rhs_df(bool tx, bool norm, const Fields& F, const RhsDfConsts& C, const Work* work, int nwork,
                    double* partials, cudaStream_t s, bool persist) {
   if (nwork <= 0) return;
-#define NPBMZ_RHS_DF(A, B)                                                                                     \
-  k_rhs_df<A, B><<<item_grid((const void*)k_rhs_df<A, B>, nwork, 128, 0, persist), 128, 0, s>>>(F, C, work, nwork, \
-                                                                                              partials)
+#define NPBMZ_RHS_DF(A, B)                                                                                      \
+  do {                                                                                                          \
+    if (C.exact_w)                                                                                              \
+      k_rhs_df<A, B, true><<<item_grid((const void*)k_rhs_df<A, B, true>, nwork, 128, 0, persist), 128, 0, s>>>(  \
+          F, C, work, nwork, partials);                                                                         \
+    else                                                                                                        \
+      k_rhs_df<A, B, false><<<item_grid((const void*)k_rhs_df<A, B, false>, nwork, 128, 0, persist), 128, 0, s>>>( \
+          F, C, work, nwork, partials);                                                                         \
+  } while (0)
   if (tx) {
     if (norm) NPBMZ_RHS_DF(true, true);
     else NPBMZ_RHS_DF(true, false);
