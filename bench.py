@@ -273,7 +273,7 @@ def run_gpu(args):
     pts = g.points
     ce, escale = npbmz.seeded_coefficients(SEED, g.nx, g.ny, g.nz, g.gx, g.gy, g.gz, g.x_zones, g.y_zones)
     flags = {"mixed-graph": npbmz.MIXED | npbmz.GRAPH, "fp64-graph": npbmz.GRAPH,
-             "mixed-rhs64-graph": npbmz.MIXED | npbmz.RHS_FP64 | npbmz.GRAPH,
+             "mixed-dfrhs-graph": npbmz.MIXED | npbmz.RHS_DF | npbmz.GRAPH,
              "mixed": npbmz.MIXED, "fp64": 0}[args.variant]
 
     def make(fl):
@@ -310,7 +310,7 @@ def run_gpu(args):
         fp64 = npbmz.fp64_peak_gflops()
         km, km_src = kernel_metrics(args.workload, args.variant)
         knames = (PHASE_KERNELS.get((kind, "mixed"), {}).get(top, [])
-                  if flags & npbmz.MIXED and not flags & npbmz.RHS_FP64 else [])
+                  if flags & npbmz.MIXED else [])
         traffic = None
         issue_obj = None
         if km and knames and all(k in km for k in knames):
@@ -346,7 +346,8 @@ def run_gpu(args):
                          ("mixed_batched", npbmz.MIXED), ("mixed_batched_graph", npbmz.MIXED | npbmz.GRAPH),
                          ("fp64_batched_graph", npbmz.GRAPH),
                          ("mixed_batched_graph_persistent", npbmz.MIXED | npbmz.GRAPH | npbmz.PERSIST),
-                         ("mixed_fp64_rhs_batched_graph", npbmz.MIXED | npbmz.RHS_FP64 | npbmz.GRAPH),
+                         ("mixed_double_float_rhs_batched_graph (compute_rhs not FP64)",
+                          npbmz.MIXED | npbmz.RHS_DF | npbmz.GRAPH),
                          ("fp64_perzone", npbmz.PERZONE)):
             q = make(fl)
             steps_v = 2 if fl & npbmz.PERZONE else nv
@@ -400,7 +401,7 @@ def run_gpu(args):
             "config": {"workload": desc, "points_per_gpu": pts, "zones": g.nzones, "variant": args.variant,
                        "batched": True, "cuda_graph": bool(flags & npbmz.GRAPH),
                        "line_solves": ("fp32 + double-float-residual refinement; primitives and compute_rhs "
-                                       + ("fp64" if flags & npbmz.RHS_FP64 else "double-float"))
+                                       + ("double-float" if flags & npbmz.RHS_DF else "fp64"))
                        if flags & npbmz.MIXED else "fp64",
                        "seed": SEED, "energy_row_scale": 2 ** escale, "autotuned": tuned,
                        "l2": f"state {p.device_bytes / 1e9:.1f} GB >> 129 MB L2; no flush needed",
@@ -424,7 +425,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bt-c", choices=sorted(WORKLOADS))
-    ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed-rhs64-graph", "mixed", "fp64"])
+    ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed-dfrhs-graph", "mixed", "fp64"])
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the default launch configuration (the timed handle is autotuned otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -47,13 +47,13 @@ typedef struct npbmz_handle npbmz_t;
 #define NPBMZ_EXACT   0x1  /* FP64 kernels built without FMA contraction, in the
                               reference's operation order: bit-for-bit the
                               reference's arithmetic */
-#define NPBMZ_MIXED   0x2  /* line solves in FP32, refined once against a
-                              residual of the line operator formed in
-                              double-float (FP32 pairs, about 48 bits) -- in
-                              FP64 with NPBMZ_REFINE_FP64; the primitive
-                              kernel and compute_rhs run in double-float too
-                              (FP64 with NPBMZ_RHS_FP64 or NPBMZ_REFINE_FP64);
-                              u, add, exch_qbc and the norms stay FP64 */
+#define NPBMZ_MIXED   0x2  /* line solves in FP32 as a defect correction on
+                              the FP64 rhs: refined once against a residual of
+                              the line operator formed in double-float (FP32
+                              pairs, about 48 bits), in FP64 with
+                              NPBMZ_REFINE_FP64; compute_rhs, add, exch_qbc
+                              and the norms stay FP64, so the fixed point is
+                              the FP64 one */
 #define NPBMZ_PERZONE 0x4  /* one launch per zone per phase, the reference's
                               per-zone adi order; default is all zones batched
                               in one launch per phase */
@@ -65,8 +65,11 @@ typedef struct npbmz_handle npbmz_t;
                               zone x line work items; results are unchanged */
 #define NPBMZ_REFINE_FP64 0x40 /* with NPBMZ_MIXED: the refinement residual in
                               FP64 instead of double-float */
-#define NPBMZ_RHS_FP64 0x80 /* with NPBMZ_MIXED: the primitive kernel and
-                              compute_rhs in FP64 */
+#define NPBMZ_RHS_DF 0x80  /* with NPBMZ_MIXED: the primitive kernel and
+                              compute_rhs in double-float too (FP32 pairs on
+                              the FP32 pipe; faster on GB300, but compute_rhs
+                              is then not FP64: the fixed point moves at the
+                              1e-14 relative level) */
 #define NPBMZ_FP32_NOREFINE 0x20 /* FP32 line solves without the refinement
                               pass (the error of plain FP32 solves, for
                               comparison); implies NPBMZ_MIXED */

@@ -117,6 +117,23 @@ bool make_lin_weights(const Consts& k, LinWeights& lw) {
   return true;
 }
 
+// The FMA build's compute_rhs constants: every factor times dt.
+void make_rhs_f64_consts(const Consts& k, const LinWeights& lw, RhsF64Consts& c) {
+  for (int d = 0; d < 3; ++d)
+    for (int cl = 0; cl < 32; ++cl)
+      for (int o = 0; o < 5; ++o) c.w[d][cl][o] = k.dt * lw.w[d][cl][o];
+  const double vc[3][3] = {{k.xxcon2 * k.con43, k.xxcon2, k.xxcon2},
+                           {k.yycon2, k.yycon2 * k.con43, k.yycon2},
+                           {k.zzcon2, k.zzcon2, k.zzcon2 * k.con43}};
+  for (int d = 0; d < 3; ++d)
+    for (int m = 0; m < 3; ++m) c.vc[d][m] = k.dt * vc[d][m];
+  for (int m = 0; m < 3; ++m) c.vcc[m] = -2.0 * (c.vc[0][m] + c.vc[1][m] + c.vc[2][m]);
+  c.t2[0] = k.dttx2;
+  c.t2[1] = k.dtty2;
+  c.t2[2] = k.dttz2;
+  c.dt = k.dt;
+}
+
 float2 split_const(double v) {
   const float hi = (float)v;
   return make_float2(hi, (float)(v - (double)hi));
@@ -196,6 +213,8 @@ struct npbmz_handle {
   float* rdx = nullptr;
   float* x0x = nullptr;
   LinWeights lw;             // compute_rhs linear stencil weights (FMA build)
+  RhsF64Consts rc64;         // the FMA build's compute_rhs constants (dt folded in)
+  double* fdt = nullptr;     // [5][NP] dt * forcing (FMA build's compute_rhs)
   // refined mixed step with the double-float primitive kernel and compute_rhs
   bool dfrhs = false;
   float2* ud = nullptr;      // [5][NP] u
@@ -310,6 +329,7 @@ Fields fields(const npbmz_t* h) {
   F.ud = h->ud;
   F.xd = h->xd;
   F.fd = h->fd;
+  F.fdt = h->fdt;
   return F;
 }
 
@@ -439,6 +459,10 @@ int flush_boundary(npbmz_t* h) {
     fast::launch_split_f2(h->forcing, h->fd, h->NP, h->stream);
     CKL(h);
   }
+  if (h->fdt) {
+    fast::launch_scale(h->forcing, h->fdt, h->K.dt, 5 * h->NP, h->stream);
+    CKL(h);
+  }
   if (h->rdx) {
     const Fields F = fields(h);
     const int saved = h->cur_group;
@@ -549,24 +573,25 @@ int phase_prim(npbmz_t* h, int zone, bool fused = false) {
   if (use_exact(h)) {
     exact::launch_prim(sp, F, h->K, lo, hi, h->stream);
   } else {
-    // over the point work list: the zone of each point is known, so the
-    // x-line-major state copy can be written too
+    // over the point work list
     int wlo = 0, whi = h->nwpts;
     if (zone >= 0) { wlo = h->pts_range[zone].lo; whi = h->pts_range[zone].hi; }
     else if (h->cur_group >= 0) { wlo = h->grp_pts[h->cur_group].lo; whi = h->grp_pts[h->cur_group].hi; }
-    if (h->dfrhs) {
-      fast::launch_prim_df(sp, F, h->rdc, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
-      CKL(h);
-      // the x sweep of a fused step reads x-line-major copies of the state
-      if (fused && h->pfx &&
-          line_launches(h, 0, zone, [&](int llo, int lhi, int tpb) {
-            fast::launch_xline_copy(sp, F, h->wline_d[0] + llo, lhi - llo, tpb, h->stream);
-            CKL(h);
-            return 0;
-          }))
-        return -1;
-    } else
-      fast::launch_prim_w(sp, F, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+    Fields Fp = F;
+    Fp.pfx = nullptr;  // the x-line-major state copies come from k_xline_copy
+    if (h->dfrhs)
+      fast::launch_prim_df(sp, Fp, h->rdc, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+    else
+      fast::launch_prim_w(sp, Fp, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+    CKL(h);
+    // the x sweep of a fused step reads x-line-major copies of the state
+    if (fused && h->pfx &&
+        line_launches(h, 0, zone, [&](int llo, int lhi, int tpb) {
+          fast::launch_xline_copy(sp, F, h->wline_d[0] + llo, lhi - llo, tpb, h->stream);
+          CKL(h);
+          return 0;
+        }))
+      return -1;
   }
   CKL(h);
   return 0;
@@ -585,7 +610,7 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm, bool fused = false) {
   else if (h->dfrhs)
     fast::launch_rhs_df(tx, norm, F, h->rdc, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream,
                         (h->flags & NPBMZ_PERSIST) != 0);
-  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->lw,
+  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->rc64,
                         (h->flags & NPBMZ_PERSIST) != 0);
   CKL(h);
   return 0;
@@ -771,7 +796,7 @@ int count_launches(npbmz_t* h) {
   const bool refined = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE);
   // prim, its x-line-major copy (double-float compute_rhs), compute_rhs,
   // two kernels per refined sweep and the x result's copy back
-  const int adi = 2 + (h->dfrhs && h->pfx ? 1 : 0) + 3 * (refined ? 2 : 1) + (h->rdx ? 1 : 0);
+  const int adi = 2 + (h->pfx ? 1 : 0) + 3 * (refined ? 2 : 1) + (h->rdx ? 1 : 0);
   int batches = 1;
   if (h->flags & NPBMZ_PERZONE) batches = h->nzones;
   else if ((h->flags & NPBMZ_GRAPH) && h->ngroups > 1 && !(h->flags & NPBMZ_EXACT)) batches = h->ngroups;
@@ -1225,14 +1250,16 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
   if (variant_flags & NPBMZ_MIXED) rc |= dalloc(h, &h->xw, 5 * (size_t)h->NP);
   if (refined) rc |= dalloc(h, &h->primf, (size_t)(kind == NPBMZ_BT ? (int)PF_COUNT : (int)PS_COUNT) * h->NP);
   if (!(variant_flags & NPBMZ_EXACT) && make_lin_weights(h->K, h->lw)) {
-    h->dfrhs = refined && !(variant_flags & (NPBMZ_REFINE_FP64 | NPBMZ_RHS_FP64));
+    h->dfrhs = refined && !(variant_flags & NPBMZ_REFINE_FP64) && (variant_flags & NPBMZ_RHS_DF);
     if (h->dfrhs) {
       make_rhs_df_consts(h->K, h->lw, h->rdc);
       rc |= dalloc(h, &h->ud, 5 * (size_t)h->NP);
       rc |= dalloc(h, &h->xd, (size_t)XD_COUNT * h->NP);
       rc |= dalloc(h, &h->fd, 5 * (size_t)h->NP);
     } else {
+      make_rhs_f64_consts(h->K, h->lw, h->rc64);
       rc |= dalloc(h, &h->flux, (size_t)PX_COUNT * h->NP);
+      rc |= dalloc(h, &h->fdt, 5 * (size_t)h->NP);
     }
     if (refined && !(variant_flags & NPBMZ_REFINE_FP64)) {
       rc |= dalloc(h, &h->rdf, 10 * (size_t)h->NP);
@@ -1658,7 +1685,7 @@ int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->ud, h->xd, h->fd, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->scratch_yz[0], h->scratch_yz[1], h->part_rhs,
+  void* bufs[] = {h->zones_d, h->nbr_d, h->u, h->rhs, h->forcing, h->prim, h->uex, h->xw, h->primf, h->flux, h->fdt, h->ud, h->xd, h->fd, h->rdf, h->pfx, h->rdx, h->x0x, h->scratch, h->scratch_yz[0], h->scratch_yz[1], h->part_rhs,
                   h->part_err, h->norms_d, h->stage, h->wpts_d, h->zblk_pts_d, h->wint_d, h->zblk_int_d,
                   h->wline_d[0], h->wline_d[1],
                   h->wline_d[2]};

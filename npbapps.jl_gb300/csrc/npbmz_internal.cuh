@@ -127,6 +127,7 @@ struct Fields {
   float2* ud = nullptr;        // [5][NP] u
   float2* xd = nullptr;        // [XD_COUNT][NP] point functions of compute_rhs
   const float2* fd = nullptr;  // [5][NP] forcing
+  const double* fdt = nullptr;  // [5][NP] dt * forcing (FMA build's compute_rhs)
   // the primitive kernel writes the FP64 planes prim (single phases; SP's
   // z sweep reads us, vs, ws, speed, ainv, qs in every step)
   bool prim64 = true;
@@ -149,6 +150,19 @@ __host__ __device__ inline int64_t xline_of(const ZoneDev& z, int j, int k) {
 // five variables of a direction, as set_constants makes it.
 struct LinWeights {
   double w[3][32][5];
+};
+
+// The constants of the FMA build's compute_rhs with dt folded in (its rhs is
+// dt * (forcing + terms); here the forcing comes as dt * forcing and every
+// term's factor carries dt): LinWeights times dt, dt*t2 per direction, the
+// velocity second-difference factors times dt per direction, and the centre
+// point's velocity factor -2 * sum over the directions.
+struct RhsF64Consts {
+  double w[3][32][5];
+  double t2[3];
+  double vc[3][3];
+  double vcc[3];
+  double dt;
 };
 
 // FP64 value -> FP32 pair (hi = rn(v), lo = rn(v - hi)), the same bits as the

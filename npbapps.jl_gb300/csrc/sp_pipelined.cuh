@@ -9,8 +9,8 @@
 //           FP32 pairs of the state, L d = r in FP32, x = x0 + d,
 // so that no FP64 arithmetic runs except in the z sweep's output: add
 // (src/SP/add.jl:14-23) in FP64, after tzetar (src/SP/tzetar.jl:27-52) in
-// double-float from the double-float primitives of the double-float
-// compute_rhs, or in FP64 from the FP64 ones (NPBMZ_RHS_FP64).  The x and y sweeps hand
+// FP64 from the FP64 primitives, or in double-float from the double-float
+// ones of the double-float compute_rhs (NPBMZ_RHS_DF).  The x and y sweeps hand
 // their transformed results (ninvr, src/SP/ninvr.jl:19-32; pinvr,
 // src/SP/pinvr.jl:20-33, applied in double-float) to the next sweep as
 // double-float planes.  Each thread streams its line's data PIPE points ahead

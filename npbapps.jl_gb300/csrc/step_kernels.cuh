@@ -316,39 +316,40 @@ __device__ __forceinline__ int dissip_class(int q, int n) {
   return (q == 1) | ((q == 2) << 1) | ((q >= 3 && q <= n - 4) << 2) | ((q == n - 3) << 3) | ((q == n - 2) << 4);
 }
 
-// One direction: stride st, position q of n, weights W (5), flux planes of
+// One direction: stride st, position q of n, weights W (5; the centre one,
+// W[2], is summed over the directions by the caller), flux planes of
 // variables 1..4 (fx[0..3]), normal momentum plane (variable a = 1 + dir),
-// velocity-term coefficients vc[3], viscous energy plane wv, t2.
+// velocity-term factors vc[3] (their centre term likewise), viscous energy
+// plane wv, t2; every factor carries dt.
 __device__ __forceinline__ void rhs_dir(double r[5], const double* __restrict__ u, int64_t NP, int64_t p, int64_t st,
                                         int q, int n, const double* __restrict__ W, const double* const fx[4],
                                         const double* __restrict__ un, const double* const vel[3], const double vc[3],
-                                        const double* __restrict__ wv, double t2) {
+                                        const double* __restrict__ wv, double t2, double dt) {
   const int64_t pm2 = q >= 2 ? p - 2 * st : p;
   const int64_t pp2 = q + 2 <= n - 1 ? p + 2 * st : p;
-  const double w0 = W[0], w1 = W[1], w2 = W[2], w3 = W[3], w4 = W[4];
+  const double w0 = W[0], w1 = W[1], w3 = W[3], w4 = W[4];
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
     const double* um = u + m * NP;
     double s = fma(w1, um[p - st], r[m]);
     s = fma(w3, um[p + st], s);
-    s = fma(w2, um[p], s);
     s = fma(w0, um[pm2], s);
     r[m] = fma(w4, um[pp2], s);
   }
-  r[0] -= t2 * (un[p + st] - un[p - st]);
+  r[0] = fma(-t2, un[p + st] - un[p - st], r[0]);
 #pragma unroll
-  for (int m = 0; m < 4; ++m) r[m + 1] -= t2 * (fx[m][p + st] - fx[m][p - st]);
+  for (int m = 0; m < 4; ++m) r[m + 1] = fma(-t2, fx[m][p + st] - fx[m][p - st], r[m + 1]);
 #pragma unroll
-  for (int m = 0; m < 3; ++m) r[m + 1] += vc[m] * ((vel[m][p + st] + vel[m][p - st]) - 2.0 * vel[m][p]);
-  r[4] += (wv[p + st] + wv[p - st]) - 2.0 * wv[p];
+  for (int m = 0; m < 3; ++m) r[m + 1] = fma(vc[m], vel[m][p + st] + vel[m][p - st], r[m + 1]);
+  r[4] = fma(dt, (wv[p + st] + wv[p - st]) - 2.0 * wv[p], r[4]);
 }
 
 template <bool TX, bool NORM>
-__global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, LinWeights LW, const Work* __restrict__ work,
+__global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, RhsF64Consts RC, const Work* __restrict__ work,
                                                   int nwork, double* __restrict__ partials) {
-  __shared__ double red[5 * 128];
+  __shared__ double red[NORM ? 5 * 128 : 1];
   __shared__ double wt[3 * 32 * 5];
-  for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&LW.w[0][0][0])[e];
+  for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&RC.w[0][0][0])[e];
   __syncthreads();
   for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
   const Work w = work[it];
@@ -367,35 +368,38 @@ __global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, LinWeights
     const double* vel[3] = {pr + PR_US * NP, pr + PR_VS * NP, pr + PR_WS * NP};
     double r[5];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) r[m] = F.forcing[m * NP + p];
+    for (int m = 0; m < 5; ++m) r[m] = F.fdt[m * NP + p];
+    const double* Wx = wt + (0 * 32 + dissip_class(i, Z.nx)) * 5;
+    const double* Wy = wt + (1 * 32 + dissip_class(j, Z.ny)) * 5;
+    const double* Wz = wt + (2 * 32 + dissip_class(k, Z.nz)) * 5;
     {
       const double* fx[4] = {X + PX_XX * NP, X + PX_UV * NP, X + PX_UW * NP, X + PX_EX * NP};
-      const double vc[3] = {K.xxcon2 * K.con43, K.xxcon2, K.xxcon2};
-      rhs_dir(r, u, NP, p, 1, i, Z.nx, wt + (0 * 32 + dissip_class(i, Z.nx)) * 5, fx, u + NP, vel, vc,
-              X + PX_WX * NP, K.tx2);
+      rhs_dir(r, u, NP, p, 1, i, Z.nx, Wx, fx, u + NP, vel, RC.vc[0], X + PX_WX * NP, RC.t2[0], RC.dt);
     }
     {
       const double* fx[4] = {X + PX_UV * NP, X + PX_YY * NP, X + PX_VW * NP, X + PX_EY * NP};
-      const double vc[3] = {K.yycon2, K.yycon2 * K.con43, K.yycon2};
-      rhs_dir(r, u, NP, p, Z.nx, j, Z.ny, wt + (1 * 32 + dissip_class(j, Z.ny)) * 5, fx, u + 2 * NP, vel, vc,
-              X + PX_WY * NP, K.ty2);
+      rhs_dir(r, u, NP, p, Z.nx, j, Z.ny, Wy, fx, u + 2 * NP, vel, RC.vc[1], X + PX_WY * NP, RC.t2[1], RC.dt);
     }
     {
       const double* fx[4] = {X + PX_UW * NP, X + PX_VW * NP, X + PX_ZZ * NP, X + PX_EZ * NP};
-      const double vc[3] = {K.zzcon2, K.zzcon2, K.zzcon2 * K.con43};
-      rhs_dir(r, u, NP, p, (int64_t)Z.nx * Z.ny, k, Z.nz, wt + (2 * 32 + dissip_class(k, Z.nz)) * 5, fx, u + 3 * NP,
-              vel, vc, X + PX_WZ * NP, K.tz2);
+      rhs_dir(r, u, NP, p, (int64_t)Z.nx * Z.ny, k, Z.nz, Wz, fx, u + 3 * NP, vel, RC.vc[2], X + PX_WZ * NP,
+              RC.t2[2], RC.dt);
     }
+    // centre point: the three directions' stencil weights and velocity
+    // factors summed first
+    const double wc = (Wx[2] + Wy[2]) + Wz[2];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) r[m] *= K.dt;
+    for (int m = 0; m < 5; ++m) r[m] = fma(wc, u[m * NP + p], r[m]);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) r[m + 1] = fma(RC.vcc[m], vel[m][p], r[m + 1]);
     if (NORM)
 #pragma unroll
       for (int m = 0; m < 5; ++m) sq[m] = r[m] * r[m];
     if (TX) {
-      // txinvr (src/SP/txinvr.jl:28-49)
+      // txinvr (src/SP/txinvr.jl:28-49); 1/speed^2 as ainv^2
       const double ru1 = pr[PR_RHOI * NP + p], uu = vel[0][p], vv = vel[1][p], ww = vel[2][p];
-      const double ac = pr[PR_SPEED * NP + p];
-      const double ac2inv = 1.0 / (ac * ac);
+      const double ac = pr[PR_SPEED * NP + p], ainv = pr[PR_AINV * NP + p];
+      const double ac2inv = ainv * ainv;
       const double r1 = r[0], r2 = r[1], r3 = r[2], r4 = r[3], r5 = r[4];
       const double t1 = K.c2 * ac2inv * (pr[PR_QS * NP + p] * r1 - uu * r2 - vv * r3 - ww * r4 + r5);
       const double t2 = K.bt * ru1 * (uu * r1 - r2);
@@ -455,6 +459,13 @@ __global__ void __launch_bounds__(128) k_xline_ends(Fields F, const Work* __rest
       F.rdx[((int64_t)ends[e] * 10 + m) * F.nlx + gl] = hi;
       F.rdx[((int64_t)ends[e] * 10 + 5 + m) * F.nlx + gl] = __double2float_rn(v - (double)hi);
     }
+}
+
+// dst = a * src (n values)
+__global__ void __launch_bounds__(256) k_scale(const double* __restrict__ src, double* __restrict__ dst, double a,
+                                               int64_t n) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    dst[t] = a * src[t];
 }
 
 // dst (double-float planes 0..4 hi, 5..9 lo) <- src (5 FP64 planes)
@@ -2401,12 +2412,12 @@ void launch_prim(bool sp, const Fields& F, const Consts& K, int64_t lo, int64_t 
 }
 
 void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork, double* partials,
-                cudaStream_t s, const LinWeights* lw, bool persist) {
+                cudaStream_t s, const RhsF64Consts* rc, bool persist) {
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
-  if (F.flux && lw) {
+  if (F.flux && F.fdt && rc) {
 #define NPBMZ_RHS_FLUX(A, B)                                                                                  \
-  k_rhs_flux<A, B><<<item_grid((const void*)k_rhs_flux<A, B>, nwork, 128, 0, persist), 128, 0, s>>>(F, K, *lw, work, \
+  k_rhs_flux<A, B><<<item_grid((const void*)k_rhs_flux<A, B>, nwork, 128, 0, persist), 128, 0, s>>>(F, K, *rc, work, \
                                                                                                   nwork, partials)
     if (tx) {
       if (norm) NPBMZ_RHS_FLUX(true, true);
@@ -2598,6 +2609,11 @@ void launch_xline_copy(bool sp, const Fields& F, const Work* work, int nwork, in
   if (nwork <= 0) return;
   if (sp) k_xline_copy<true><<<nwork, 256, 0, s>>>(F, work, nwork, lpi);
   else k_xline_copy<false><<<nwork, 256, 0, s>>>(F, work, nwork, lpi);
+}
+
+void launch_scale(const double* src, double* dst, double a, int64_t n, cudaStream_t s) {
+  int64_t g = (n + 255) / 256;
+  k_scale<<<(int)(g > 8192 ? 8192 : g), 256, 0, s>>>(src, dst, a, n);
 }
 
 void launch_split_f2(const double* src, float2* dst, int64_t NP, cudaStream_t s) {

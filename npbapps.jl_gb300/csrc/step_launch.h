@@ -13,7 +13,7 @@ namespace npbmz {
   void launch_prim_w(bool sp, const Fields& F, const Consts& K, const Work* work, int nwork, cudaStream_t s,        \
                      bool persist = false);                                                                          \
   void launch_rhs(bool tx, bool norm, const Fields& F, const Consts& K, const Work* work, int nwork,                 \
-                  double* partials, cudaStream_t s, const LinWeights* lw = nullptr, bool persist = false);           \
+                  double* partials, cudaStream_t s, const RhsF64Consts* rc = nullptr, bool persist = false);         \
   void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork,       \
                     int tpb, void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s,                      \
                     bool persist = false);                                                                           \
@@ -25,6 +25,8 @@ NPBMZ_DECLARE_LAUNCHERS(fast)
 namespace fast {
 // dst (10 float planes: double-float hi 0..4, lo 5..9) <- src (5 FP64 planes)
 void launch_split_df(const double* src, float* dst, int64_t NP, cudaStream_t s);
+// dst = a * src (n values)
+void launch_scale(const double* src, double* dst, double a, int64_t n, cudaStream_t s);
 // dst (5 float2 planes {hi, lo}) <- src (5 FP64 planes)
 void launch_split_f2(const double* src, float2* dst, int64_t NP, cudaStream_t s);
 // primitive kernel and compute_rhs of the refined mixed step in double-float

@@ -30,7 +30,7 @@ const GRAPH = Cint(0x8)
 const PERSIST = Cint(0x10)
 const FP32_NOREFINE = Cint(0x20)
 const REFINE_FP64 = Cint(0x40)
-const RHS_FP64 = Cint(0x80)
+const RHS_DF = Cint(0x80)
 const U = Cint(0)
 const RHS = Cint(1)
 const FORCING = Cint(2)

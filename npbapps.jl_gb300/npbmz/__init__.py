@@ -32,7 +32,7 @@ from . import build as _build
 BT, SP = 0, 1
 KINDS = {"BT": BT, "SP": SP}
 
-EXACT, MIXED, PERZONE, GRAPH, PERSIST, FP32_NOREFINE, REFINE_FP64, RHS_FP64 = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20, 0x40, 0x80
+EXACT, MIXED, PERZONE, GRAPH, PERSIST, FP32_NOREFINE, REFINE_FP64, RHS_DF = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20, 0x40, 0x80
 U, RHS, FORCING = 0, 1, 2
 LAYOUT_DENSE, LAYOUT_REF = 0, 1
 PHASE_RHS, PHASE_XSOLVE, PHASE_YSOLVE, PHASE_ZSOLVE, PHASE_ADD, PHASE_EXCH, PHASE_RHSONLY = range(7)

@@ -124,11 +124,11 @@ DF_RHS_REL = 1e-12   # compute_rhs in double-float (FP32 pairs, about 48 bits)
 
 @pytest.mark.parametrize("gname", list(GEOMS))
 def test_double_float_compute_rhs_phase(oracle_mod, gname):
-    """MIXED handles form the primitive variables and compute_rhs (with SP's
-    txinvr) in double-float arithmetic on the FP32 pipe: the compute_rhs phase
-    of each zone against the oracle from identical inputs."""
+    """NPBMZ_RHS_DF handles form the primitive variables and compute_rhs (with
+    SP's txinvr) in double-float arithmetic on the FP32 pipe: the compute_rhs
+    phase of each zone against the oracle from identical inputs."""
     geom, dt, _ = GEOMS[gname]()
-    p, o = make_pair(oracle_mod, geom, dt, npbmz.MIXED, seeded(geom))
+    p, o = make_pair(oracle_mod, geom, dt, npbmz.MIXED | npbmz.RHS_DF, seeded(geom))
     p.phase(npbmz.PHASE_EXCH)
     o.phase(5)
     worst = 0.0
@@ -141,13 +141,13 @@ def test_double_float_compute_rhs_phase(oracle_mod, gname):
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
 def test_double_float_rhs_steps_match_fp64_rhs(kind):
-    """The same refined mixed step with compute_rhs in double-float (default)
-    and in FP64 (NPBMZ_RHS_FP64): u and the verification norms after 20
-    steps of class W agree to 1e-12."""
+    """The same refined mixed step with compute_rhs in double-float
+    (NPBMZ_RHS_DF) and in FP64 (default): u and the verification norms after
+    20 steps of class W agree to 1e-12."""
     geom, dt, _ = geom_class(kind, "W")
     ce = seeded(geom)
-    a = npbmz.Problem(geom, dt, npbmz.MIXED)
-    b = npbmz.Problem(geom, dt, npbmz.MIXED | npbmz.RHS_FP64)
+    a = npbmz.Problem(geom, dt, npbmz.MIXED | npbmz.RHS_DF)
+    b = npbmz.Problem(geom, dt, npbmz.MIXED)
     a.setup(ce)
     b.setup(ce)
     a.step(20)
@@ -224,7 +224,7 @@ def test_graph_replay_equals_direct_launches():
 
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
-@pytest.mark.parametrize("flags", [0, npbmz.MIXED], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.RHS_DF], ids=["fp64", "mixed", "mixed-dfrhs"])
 @pytest.mark.parametrize("groups", [2, 3, 5])
 def test_zone_group_graph_equals_direct_launches(kind, flags, groups):
     """The step graph with zone-group branches (npbmz_set_step_groups) runs the
@@ -246,7 +246,8 @@ def test_zone_group_graph_equals_direct_launches(kind, flags, groups):
 
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
-@pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.GRAPH], ids=["fp64", "mixed", "mixed-graph"])
+@pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.GRAPH, npbmz.MIXED | npbmz.RHS_DF | npbmz.GRAPH],
+                         ids=["fp64", "mixed", "mixed-graph", "mixed-dfrhs-graph"])
 def test_persistent_kernels_equal_one_cta_per_item(kind, flags):
     """NPBMZ_PERSIST: the same work items looped over by a resident grid --
     bit-identical u and per-step norms."""
@@ -312,8 +313,8 @@ MIXED_REL = 1e-10   # FP32 line solves refined against an FP64 residual
 
 
 @pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 60), ("sp_classS", 100)])
-@pytest.mark.parametrize("flags", [npbmz.MIXED, npbmz.MIXED | npbmz.RHS_FP64, npbmz.MIXED | npbmz.REFINE_FP64],
-                         ids=["df64-residual", "fp64-rhs", "fp64-residual"])
+@pytest.mark.parametrize("flags", [npbmz.MIXED, npbmz.MIXED | npbmz.RHS_DF, npbmz.MIXED | npbmz.REFINE_FP64],
+                         ids=["df64-residual", "df64-rhs", "fp64-residual"])
 def test_mixed_precision_within_1e10_of_fp64_oracle(oracle_mod, gname, nsteps, flags):
     geom, dt, _ = GEOMS[gname]()
     p, o = make_pair(oracle_mod, geom, dt, flags, seeded(geom))
