@@ -50,15 +50,19 @@ SEED = 20261203
 # and writes rhs; the z sweep also updates u (add); the primitive kernel reads u.
 BYTES_PER_POINT = {"prim": 40.0, "rhs": 120.0, "x": 120.0, "y": 120.0, "z": 160.0, "exch": 0.0}
 # Kernels of each phase of the batched step (for the per-kernel ncu figures).
+_SWEEPS = {
+    "BT": {"x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>", "k_xline_back"],
+           "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
+           "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
+    "SP": {"x": ["k_sp_mixed_pl<0>", "k_sp_refine_pl<0, 1>", "k_xline_back"],
+           "y": ["k_sp_mixed_pl<1>", "k_sp_refine_pl<1, 1>"],
+           "z": ["k_sp_mixed_pl<2>", "k_sp_refine_pl<2, 0>"]},
+}
 PHASE_KERNELS = {
-    ("BT", "mixed"): {"prim": ["k_prim_df<0>", "k_xline_copy<0>"], "rhs": ["k_rhs_df<0, 0>"],
-                      "x": ["k_bt_mixed_pl<0>", "k_bt_refine_pl<0, 1>", "k_xline_back"],
-                      "y": ["k_bt_mixed_pl<1>", "k_bt_refine_pl<1, 1>"],
-                      "z": ["k_bt_mixed_pl<2>", "k_bt_refine_pl<2, 0>"]},
-    ("SP", "mixed"): {"prim": ["k_prim_df<1>", "k_xline_copy<1>"], "rhs": ["k_rhs_df<1, 0>"],
-                      "x": ["k_sp_mixed_pl<0>", "k_sp_refine_pl<0, 1>", "k_xline_back"],
-                      "y": ["k_sp_mixed_pl<1>", "k_sp_refine_pl<1, 1>"],
-                      "z": ["k_sp_mixed_pl<2>", "k_sp_refine_pl<2, 0>"]},
+    ("BT", "mixed"): {"prim": ["k_prim_w<0>", "k_xline_copy<0>"], "rhs": ["k_rhs_flux<0, 0>"], **_SWEEPS["BT"]},
+    ("SP", "mixed"): {"prim": ["k_prim_w<1>", "k_xline_copy<1>"], "rhs": ["k_rhs_flux<1, 0>"], **_SWEEPS["SP"]},
+    ("BT", "mixed-dfrhs"): {"prim": ["k_prim_df<0>", "k_xline_copy<0>"], "rhs": ["k_rhs_df<0, 0, 1>"], **_SWEEPS["BT"]},
+    ("SP", "mixed-dfrhs"): {"prim": ["k_prim_df<1>", "k_xline_copy<1>"], "rhs": ["k_rhs_df<1, 0, 1>"], **_SWEEPS["SP"]},
 }
 
 
@@ -309,12 +313,20 @@ def run_gpu(args):
         achieved = BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
         fp64 = npbmz.fp64_peak_gflops()
         km, km_src = kernel_metrics(args.workload, args.variant)
-        knames = (PHASE_KERNELS.get((kind, "mixed"), {}).get(top, [])
-                  if flags & npbmz.MIXED else [])
+        pk_key = (kind, "mixed-dfrhs" if flags & npbmz.RHS_DF else "mixed")
+        knames = PHASE_KERNELS.get(pk_key, {}).get(top, []) if flags & npbmz.MIXED else []
         traffic = None
         issue_obj = None
+        fp64_obj = None
         if km and knames and all(k in km for k in knames):
             traffic = sum(km[k]["dram_bytes_per_point"] for k in knames) * pts
+            flops_pt = sum(km[k]["fp64_flops_per_point"] for k in knames)
+            if flops_pt > 1.0:
+                fp64_ach = flops_pt * pts / (ph[top] * 1e-3) / 1e9
+                fp64_obj = {"achieved": fp64_ach, "peak": fp64, "unit": "GFLOP/s", "frac": fp64_ach / fp64,
+                            "flops_per_point": flops_pt,
+                            "pipe_active_ncu": max(km[k]["fp64_pipe_active"] for k in knames),
+                            "peak_source": "npbmz_fp64_peak: FP64 FMA chains on this GPU, measured in this run"}
             if all("inst_per_point" in km[k] for k in knames):
                 # instruction issue: 4 schedulers per SM, one warp instruction per cycle each
                 inst_pt = sum(km[k]["inst_per_point"] for k in knames)
@@ -335,8 +347,9 @@ def run_gpu(args):
                              if traffic is not None else None,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
                              "bytes_per_point": BYTES_PER_POINT[top], "launch_ms": ph[top],
-                             "binding_ceiling": "instruction issue (latency-bound sweeps)" if issue_obj else None,
-                             "issue": issue_obj}
+                             "binding_ceiling": ("fp64 pipe" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6
+                                                 else "instruction issue" if issue_obj else None),
+                             "fp64": fp64_obj, "issue": issue_obj}
         extra["phase_ms"] = ph
         extra["fp64_peak_gflops_measured"] = fp64
         # variants (fewer steps each)
