@@ -152,6 +152,14 @@ int npbmz_adi(npbmz_t* h, int zone);
  * Synchronous when norms != NULL. */
 int npbmz_step(npbmz_t* h, int nsteps, double* norms);
 
+/* nsteps steps, then u of every zone to `host` (layout as npbmz_download,
+ * zone = -1): the same result as npbmz_step followed by npbmz_download.  For
+ * NPBMZ_GRAPH handles with zone-group branches and a page-locked `host`, each
+ * group's zones are copied out as soon as the last step's z sweep has written
+ * them, while the other groups still compute.  Synchronous.  No counterpart
+ * in the reference (whose u lives in host memory). */
+int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host);
+
 /* The node part of verify (src/BT/verify.jl:411-505): error_norm of u, then
  * compute_rhs without an exchange, rhs_norm; sums over zones.  Synchronous. */
 int npbmz_verify(npbmz_t* h, double* xcr, double* xce);

@@ -268,7 +268,8 @@ __device__ __forceinline__ int64_t ref_index(int kind, int field, const ZoneDev&
   return i + ni * (j + nj * (k + nk * (int64_t)m));
 }
 
-// blockIdx.y = zone index within [zone_lo, zone_lo + gridDim.y).  The host
+// blockIdx.y = zone index within [zone_lo, zone_lo + gridDim.y), or the
+// zone zlist[blockIdx.y] when zlist is given.  The host
 // side array of zone z starts at element soff[z] - sub of `stage`, which is
 // either the device staging buffer (sub = 0) or the device mapping of a
 // page-locked host buffer holding zones from zone_lo (sub = soff[zone_lo]).
@@ -276,8 +277,9 @@ __device__ __forceinline__ int64_t ref_index(int kind, int field, const ZoneDev&
 // 2: compact reference order without halo (BT [k][j][i][m], SP = dense).
 __global__ void __launch_bounds__(256) k_convert(Fields F, double* __restrict__ field_planes,
                                                  double* __restrict__ stage, const int64_t* __restrict__ soff,
-                                                 int64_t sub, int zone_lo, int kind, int field, int layout, int dir) {
-  const int zone = zone_lo + blockIdx.y;
+                                                 int64_t sub, int zone_lo, int kind, int field, int layout, int dir,
+                                                 const int* __restrict__ zlist) {
+  const int zone = zlist ? zlist[blockIdx.y] : zone_lo + blockIdx.y;
   const ZoneDev Z = F.zones[zone];
   const int np = Z.nx * Z.ny * Z.nz;
   double* st = stage + (soff[zone] - sub);
@@ -337,12 +339,12 @@ void launch_norm_finish(const ZoneDev* zones, const double* partials, const int*
 }
 
 void launch_convert(const Fields& F, double* planes, double* stage, const int64_t* soff, int64_t sub, int zone_lo,
-                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s) {
+                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s, const int* zlist) {
   if (nzn <= 0) return;
   int gx = (5 * max_np + 255) / 256;
   if (gx > 512) gx = 512;
   dim3 grid(gx, nzn);
-  k_convert<<<grid, 256, 0, s>>>(F, planes, stage, soff, sub, zone_lo, kind, field, layout, dir);
+  k_convert<<<grid, 256, 0, s>>>(F, planes, stage, soff, sub, zone_lo, kind, field, layout, dir, zlist);
 }
 
 void launch_fill(double* a, int64_t n, double v, cudaStream_t s) {

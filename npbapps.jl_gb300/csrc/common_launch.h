@@ -14,8 +14,10 @@ void launch_exch_qbc(const Fields& F, const int* nbr_dev, int zone_lo, int nz_co
 void launch_err_partials(const Fields& F, const Work* work, int nwork, double* partials, cudaStream_t s);
 void launch_norm_finish(const ZoneDev* zones, const double* partials, const int* zblk, int nzones, double scale,
                         double* out, cudaStream_t s);
+// zlist (optional, device): the nzn zones to convert instead of [zone_lo, zone_lo + nzn)
 void launch_convert(const Fields& F, double* planes, double* stage, const int64_t* soff, int64_t sub, int zone_lo,
-                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s);
+                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s,
+                    const int* zlist = nullptr);
 void launch_fill(double* a, int64_t n, double v, cudaStream_t s);
 int probe_fp64(double* gflops);
 }  // namespace npbmz

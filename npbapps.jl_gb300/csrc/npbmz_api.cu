@@ -255,6 +255,14 @@ struct npbmz_handle {
   int cur_group = -1;              // >= 0 while the phases of one group are issued
   cudaStream_t grp_stream[8] = {};
   cudaEvent_t grp_ev[2 * 8 + 1] = {};
+  // npbmz_step_download: the graph records grp_out_ev[g] (an external event)
+  // when group g's z sweep has written its zones' u; io_stream then copies
+  // those zones out while the other groups compute.
+  cudaEvent_t grp_out_ev[8] = {};
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t io_done = nullptr;
+  int* grp_zones_d = nullptr;        // zones of each group, group-major
+  std::vector<int> grp_zone_off;     // group g's zones at [off[g], off[g+1])
   // Lines per CTA of the line solves, per sweep direction and zone-size
   // bucket: zones are split by line length into nbkt buckets per direction
   // (npbmz_autotune sets 3 and picks each bucket's lines per CTA).
@@ -726,6 +734,8 @@ int grouped_step(npbmz_t* h, cudaStream_t cs) {
     if (!rc) rc = phase_rhs(h, -1, sp, false, true);
     if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g], S) != cudaSuccess;
     for (int dir = 0; dir < 3 && !rc; ++dir) rc = phase_solve(h, dir, -1, dir == 2 ? 1 : 0, true);
+    // group g's u is final: an event that work outside the graph can wait on
+    if (!rc) rc = cudaEventRecordWithFlags(h->grp_out_ev[g], S, cudaEventRecordExternal) != cudaSuccess;
     if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g + 1], S) != cudaSuccess;
   }
   h->stream = cs;
@@ -746,6 +756,8 @@ int capture_step_graph(npbmz_t* h) {
       if (!h->grp_stream[g]) CK(h, cudaStreamCreateWithFlags(&h->grp_stream[g], cudaStreamNonBlocking));
     for (int e = 0; e < 2 * h->ngroups + 1; ++e)
       if (!h->grp_ev[e]) CK(h, cudaEventCreateWithFlags(&h->grp_ev[e], cudaEventDisableTiming));
+    for (int g = 0; g < h->ngroups; ++g)
+      if (!h->grp_out_ev[g]) CK(h, cudaEventCreateWithFlags(&h->grp_out_ev[g], cudaEventDisableTiming));
   }
   if (flush_boundary(h)) return -1;  // keep the one-off reset out of the graph
   // Capture is not allowed on the legacy default stream: capture and replay
@@ -1400,6 +1412,41 @@ int npbmz_step(npbmz_t* h, int nsteps, double* norms) {
   return 0;
 }
 
+int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
+  if (!h) return fail(nullptr, "null handle");
+  if (nsteps < 1) return fail(h, "nsteps must be >= 1");
+  if (!host) return fail(h, "null host buffer");
+  if (layout != NPBMZ_LAYOUT_DENSE && layout != NPBMZ_LAYOUT_REF) return fail(h, "bad layout %d", layout);
+  cudaPointerAttributes attr;
+  std::memset(&attr, 0, sizeof(attr));
+  const bool mapped = cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+                      attr.devicePointer != nullptr;
+  cudaGetLastError();
+  if (!mapped || !(h->flags & NPBMZ_GRAPH) || !use_groups(h) || h->stream == nullptr) {
+    if (npbmz_step(h, nsteps, nullptr)) return -1;
+    return transfer(h, -1, NPBMZ_U, layout, host, 1, true);
+  }
+  if (!h->graph_exec || h->graph_stream != h->stream)
+    if (capture_step_graph(h)) return -1;
+  if (flush_boundary(h)) return -1;
+  if (nsteps > 1 && replay_graph(h, nsteps - 1)) return -1;
+  CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
+  if (!h->io_stream) CK(h, cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
+  if (!h->io_done) CK(h, cudaEventCreateWithFlags(&h->io_done, cudaEventDisableTiming));
+  const Fields F = fields(h);
+  for (int g = 0; g < h->ngroups; ++g) {
+    const int z0 = h->grp_zone_off[g], nz = h->grp_zone_off[g + 1] - z0;
+    CK(h, cudaStreamWaitEvent(h->io_stream, h->grp_out_ev[g], 0));
+    launch_convert(F, h->u, reinterpret_cast<double*>(attr.devicePointer), h->soff_d[layout][NPBMZ_U], 0, 0, nz,
+                   h->max_np, h->kind, NPBMZ_U, layout, 1, h->io_stream, h->grp_zones_d + z0);
+    CKL(h);
+  }
+  CK(h, cudaEventRecord(h->io_done, h->io_stream));
+  CK(h, cudaStreamWaitEvent(h->stream, h->io_done, 0));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
 int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms) {
   if (!h) return fail(nullptr, "null handle");
   if (nsteps < 1 || !phase_ms) return fail(h, "nsteps must be >= 1 and phase_ms non-null");
@@ -1496,6 +1543,17 @@ int npbmz_set_step_groups(npbmz_t* h, int groups) {
   h->ngroups = groups;
   assign_zone_groups(h);
   if (build_work_lists(h) || build_line_lists(h)) return -1;
+  {  // zones of each group (npbmz_step_download)
+    std::vector<int> zl;
+    h->grp_zone_off.assign(h->ngroups + 1, 0);
+    for (int g = 0; g < h->ngroups; ++g) {
+      for (int z = 0; z < h->nzones; ++z)
+        if (h->zone_group[z] == g) zl.push_back(z);
+      h->grp_zone_off[g + 1] = (int)zl.size();
+    }
+    if (!h->grp_zones_d) CK(h, cudaMalloc((void**)&h->grp_zones_d, std::max(1, h->nzones) * sizeof(int)));
+    CK(h, cudaMemcpy(h->grp_zones_d, zl.data(), zl.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
   if (h->ngroups > 1 && !h->scratch_yz[0])
     for (int d = 0; d < 2; ++d) {
       CK(h, cudaMalloc(&h->scratch_yz[d], std::max<size_t>(h->scratch_bytes, 16)));
@@ -1700,6 +1758,11 @@ int npbmz_destroy(npbmz_t* h) {
     if (gs) { cudaStreamSynchronize(gs); cudaStreamDestroy(gs); }
   for (cudaEvent_t e : h->grp_ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->grp_out_ev)
+    if (e) cudaEventDestroy(e);
+  if (h->io_stream) { cudaStreamSynchronize(h->io_stream); cudaStreamDestroy(h->io_stream); }
+  if (h->io_done) cudaEventDestroy(h->io_done);
+  if (h->grp_zones_d) cudaFree(h->grp_zones_d);
   for (cudaEvent_t e : h->fence)
     if (e) cudaEventDestroy(e);
   delete h;

@@ -44,6 +44,7 @@ EXPORTS = [
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
     "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
+    "npbmz_step_download",
 ]
 PROF_PHASES = ("exch", "prim", "rhs", "x", "y", "z")
 
@@ -116,6 +117,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_exch_qbc.argtypes = [vp]
     L.npbmz_adi.argtypes = [vp, ctypes.c_int]
     L.npbmz_step.argtypes = [vp, ctypes.c_int, dp]
+    L.npbmz_step_download.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     L.npbmz_verify.argtypes = [vp, dp, dp]
     L.npbmz_phase.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.npbmz_set_stream.argtypes = [vp, vp]
@@ -268,6 +270,12 @@ class Problem:
         out = np.zeros(10 * max(nsteps, 1)) if norms else None
         self._check(lib().npbmz_step(self._h, nsteps, _dp(out) if norms else None), "npbmz_step")
         return out[: 10 * nsteps].reshape(nsteps, 2, 5) if norms else None
+
+    def step_download(self, nsteps: int, layout: int, ptr: int):
+        """nsteps steps, then u of all zones to the host buffer at ptr (layout as
+        transfer_raw); with a page-locked buffer and zone-group branches the
+        copies of each group overlap the other groups' work."""
+        self._check(lib().npbmz_step_download(self._h, nsteps, layout, ctypes.c_void_p(ptr)), "npbmz_step_download")
 
     def step_profile(self, nsteps: int = 1):
         """Mean device milliseconds per step of each phase of the batched step

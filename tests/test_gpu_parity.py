@@ -246,6 +246,36 @@ def test_zone_group_graph_equals_direct_launches(kind, flags, groups):
 
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
+@pytest.mark.parametrize("flags,groups", [(npbmz.MIXED | npbmz.GRAPH, 3), (npbmz.GRAPH, 2), (npbmz.MIXED, 1)],
+                         ids=["mixed-graph-3groups", "fp64-graph-2groups", "mixed-direct"])
+def test_step_download_equals_step_then_download(kind, flags, groups):
+    """npbmz_step_download (each zone group copied out of the last step as soon
+    as its z sweep is done, into page-locked memory) leaves the same host array
+    as npbmz_step followed by npbmz_download, and the same device state."""
+    torch = pytest.importorskip("torch")
+    geom, dt, _ = geom_class(kind, "W")
+    ce = seeded(geom)
+    sizes = [npbmz.ref_elems(geom.kind, npbmz.U, int(geom.nx[z]), int(geom.ny[z]), int(geom.nz[z]))
+             for z in range(geom.nzones)]
+    a = npbmz.Problem(geom, dt, flags)
+    b = npbmz.Problem(geom, dt, flags)
+    a.setup(ce)
+    b.setup(ce)
+    if flags & npbmz.GRAPH:
+        a.set_step_groups(groups)
+        b.set_step_groups(groups)
+    ha = torch.full((sum(sizes),), -1.0, dtype=torch.float64, pin_memory=True)
+    hb = torch.full((sum(sizes),), -1.0, dtype=torch.float64, pin_memory=True)
+    for _ in range(3):
+        a.step(2)
+        a.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ha.data_ptr(), False)
+        b.step_download(2, npbmz.LAYOUT_REF, hb.data_ptr())
+        np.testing.assert_array_equal(ha.numpy(), hb.numpy())
+    for z in range(geom.nzones):
+        np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
+
+
+@pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.GRAPH, npbmz.MIXED | npbmz.RHS_DF | npbmz.GRAPH],
                          ids=["fp64", "mixed", "mixed-graph", "mixed-dfrhs-graph"])
 def test_persistent_kernels_equal_one_cta_per_item(kind, flags):
