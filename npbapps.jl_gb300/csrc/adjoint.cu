@@ -1,4 +1,4 @@
-// adjoint.cu -- discrete adjoint of the BT-MZ time step (FP64).
+// adjoint.cu -- discrete adjoint of the BT-MZ and SP-MZ time steps (FP64).
 //
 // One time step is u' = E u (exch_qbc), r = R(u', f) (compute_rhs),
 // r1 = Tx(u')^-1 r, r2 = Ty(u')^-1 r1, r3 = Tz(u')^-1 r2, and
@@ -12,6 +12,15 @@
 // The pointwise derivatives (of the flux-Jacobian products and of the
 // compute_rhs flux and viscous terms) are taken with forward-mode dual
 // numbers over the five conserved variables of one point.
+//
+// SP (src/SP/adi.jl:6-258): r0 = R(u', f), r = Tx(u') r0 (txinvr), and per
+// sweep d = x, y, z: y_d = L_d(u')^-1 x_{d-1} (three scalar pentadiagonal
+// systems, identity rows at the line ends), x_d = P_d y_d (ninvr, pinvr:
+// constant; tzetar: state-dependent) on the interior, u_next = u' + x_z.
+// The band entries of row q that depend on the state are its sub- and
+// super-diagonal and diagonal, each a function of the geometry (velocity,
+// rhon, speed) of its own column's point only; so the linearisation of
+// L(u') y at point j gathers lambda_{j-1}, lambda_j and lambda_{j+1}.
 #define NPBMZ_NS adjk
 #define NPBMZ_HAS_FP32 1
 #define NPBMZ_NO_LAUNCHERS
@@ -83,6 +92,17 @@ __device__ __forceinline__ D5 dinv(const D5& a) {
   for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
   return r;
 }
+
+__device__ __forceinline__ D5 dsqrt(const D5& a) {
+  D5 r;
+  r.v = sqrt(a.v);
+  const double g = 0.5 / r.v;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+  return r;
+}
+__device__ __forceinline__ D5 dmax(const D5& a, const D5& b) { return a.v >= b.v ? a : b; }
+__device__ __forceinline__ D5 dval(const D5& a) { return dconst(a.v); }
 
 __device__ __forceinline__ void seed_state(const Fields& F, int64_t pt, D5 u[5]) {
 #pragma unroll
@@ -434,6 +454,306 @@ __global__ void __launch_bounds__(128) k_adj_seed(Fields F, const Work* __restri
   }
 }
 
+// ---- SP ------------------------------------------------------------------------
+// Primitive variables of one point's state, as the primitive kernel forms
+// them (src/SP/rhs.jl:62-89).
+struct SpPrim {
+  D5 ri, vel[3], sq, qs, speed, ainv;
+};
+__device__ __forceinline__ SpPrim sp_prim(const Consts& K, const D5 u[5]) {
+  SpPrim P;
+  P.ri = dinv(u[0]);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) P.vel[d] = u[d + 1] * P.ri;
+  P.sq = 0.5 * ((u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) * P.ri);
+  P.qs = P.sq * P.ri;
+  P.speed = dsqrt(K.c1c2 * (P.ri * (u[4] - P.sq)));
+  P.ainv = dinv(P.speed);
+  return P;
+}
+__device__ __forceinline__ SpPrim sp_prim_value(const SpPrim& a) {  // derivatives dropped
+  SpPrim P;
+  P.ri = dval(a.ri);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) P.vel[d] = dval(a.vel[d]);
+  P.sq = dval(a.sq);
+  P.qs = dval(a.qs);
+  P.speed = dval(a.speed);
+  P.ainv = dval(a.ainv);
+  return P;
+}
+
+// txinvr (src/SP/txinvr.jl:28-49), 1/speed^2 as ainv^2 like the forward kernel
+__device__ __forceinline__ void sp_txinvr(const Consts& K, const SpPrim& P, const D5 r[5], D5 o[5]) {
+  const D5 ac2inv = P.ainv * P.ainv;
+  const D5 t1 = K.c2 * (ac2inv * (P.qs * r[0] - P.vel[0] * r[1] - P.vel[1] * r[2] - P.vel[2] * r[3] + r[4]));
+  const D5 t2 = K.bt * (P.ri * (P.vel[0] * r[0] - r[1]));
+  const D5 t3 = (K.bt * (P.ri * P.speed)) * t1;
+  o[0] = r[0] - t1;
+  o[1] = -(P.ri * (P.vel[2] * r[0] - r[3]));
+  o[2] = P.ri * (P.vel[1] * r[0] - r[2]);
+  o[3] = t3 - t2;
+  o[4] = t2 + t3;
+}
+
+// The transform after sweep DIR: ninvr (src/SP/ninvr.jl:19-32), pinvr
+// (src/SP/pinvr.jl:20-33), tzetar (src/SP/tzetar.jl:27-52; uzik1 = u1).
+template <int DIR>
+__device__ __forceinline__ void sp_post(const Consts& K, const SpPrim& P, const D5& uzik1, const D5 r[5], D5 o[5]) {
+  if (DIR == 0) {
+    const D5 t1 = K.bt * r[2];
+    const D5 t2 = 0.5 * (r[3] + r[4]);
+    o[0] = -r[1]; o[1] = r[0]; o[2] = K.bt * (r[3] - r[4]); o[3] = t2 - t1; o[4] = t1 + t2;
+  } else if (DIR == 1) {
+    const D5 t1 = K.bt * r[0];
+    const D5 t2 = 0.5 * (r[3] + r[4]);
+    o[0] = K.bt * (r[3] - r[4]); o[1] = -r[2]; o[2] = r[1]; o[3] = t2 - t1; o[4] = t1 + t2;
+  } else {
+    const D5 btuz = K.bt * uzik1;
+    const D5 t1 = (btuz * P.ainv) * (r[3] + r[4]);
+    const D5 t2 = r[2] + t1;
+    const D5 t3 = btuz * (r[3] - r[4]);
+    o[0] = t2;
+    o[1] = P.vel[0] * t2 - uzik1 * r[1];
+    o[2] = uzik1 * r[0] + P.vel[1] * t2;
+    o[3] = P.vel[2] * t2 + t3;
+    o[4] = uzik1 * (P.vel[1] * r[0] - P.vel[0] * r[1]) + P.qs * t2 + (K.c2iv * (P.speed * P.speed)) * t1 +
+           P.vel[2] * t3;
+  }
+}
+
+// ybar = T^T xbar for a map o = T r linear in r (T at fixed primitives).
+template <typename Map>
+__device__ __forceinline__ void transpose_apply(Map map, const double xb[5], double yb[5]) {
+  D5 rs[5], o[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    rs[m] = dconst(0.0);
+    rs[m].d[m] = 1.0;
+  }
+  map(rs, o);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    double t = 0.0;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) t += o[m].d[j] * xb[m];
+    yb[j] = t;
+  }
+}
+
+// Forward recomputation: the transform of sweep DIR applied to the
+// untransformed solution ys, into rhs, at the interior points.
+template <int DIR>
+__global__ void __launch_bounds__(128) k_sp_apply_post(Fields F, Consts K, const Work* __restrict__ work,
+                                                       const double* __restrict__ ys) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int qi = w.first + threadIdx.x;
+  if (qi >= Z.nx * Z.ny * Z.nz) return;
+  const int i = qi % Z.nx, j = (qi / Z.nx) % Z.ny, k = qi / (Z.nx * Z.ny);
+  if (i < 1 || i > Z.nx - 2 || j < 1 || j > Z.ny - 2 || k < 1 || k > Z.nz - 2) return;
+  const int64_t NP = F.NP, pt = Z.off + qi;
+  double v[5], o[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) v[m] = ys[m * NP + pt];
+  sp_transform<DIR>(F, K, pt, v, o);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) F.rhs[m * NP + pt] = o[m];
+}
+
+// txinvr adjoint at the interior points: vb += (d(Tx(u') r0)/du')^T rb, then
+// rb <- Tx^T rb (rb in: adjoint of txinvr's output, out: of compute_rhs's).
+__global__ void __launch_bounds__(128) k_adj_sp_txinvr(Fields F, Consts K, const Work* __restrict__ work,
+                                                       double* __restrict__ rb, const double* __restrict__ r0,
+                                                       double* __restrict__ vb) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int qi = w.first + threadIdx.x;
+  if (qi >= Z.nx * Z.ny * Z.nz) return;
+  const int i = qi % Z.nx, j = (qi / Z.nx) % Z.ny, k = qi / (Z.nx * Z.ny);
+  if (i < 1 || i > Z.nx - 2 || j < 1 || j > Z.ny - 2 || k < 1 || k > Z.nz - 2) return;
+  const int64_t NP = F.NP, pt = Z.off + qi;
+  D5 u[5];
+  seed_state(F, pt, u);
+  const SpPrim P = sp_prim(K, u);
+  double xb[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) xb[m] = rb[m * NP + pt];
+  {
+    D5 rc[5], o[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) rc[m] = dconst(r0[m * NP + pt]);
+    sp_txinvr(K, P, rc, o);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      double g = 0.0;
+#pragma unroll
+      for (int m = 0; m < 5; ++m) g += xb[m] * o[m].d[c];
+      vb[c * NP + pt] += g;
+    }
+  }
+  const SpPrim Pv = sp_prim_value(P);
+  double yt[5];
+  transpose_apply([&](const D5 rs[5], D5 o[5]) { sp_txinvr(K, Pv, rs, o); }, xb, yt);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) rb[m * NP + pt] = yt[m];
+}
+
+// Transposed SP sweep DIR, one thread per line.  yb in: adjoint of the
+// sweep's output (transformed on the interior), out: of its input; ys: the
+// forward untransformed solution (with the line's end values); vb gets the
+// linearisations of the transform (tzetar) and of the bands.  Line scratch
+// per point (30 doubles): bands of the three systems (0..14), the
+// eliminated upper bands (15..20), the right-hand side / lambda (21..25),
+// the geometry cv, rhon, speed (26..28).
+template <int DIR>
+__global__ void __launch_bounds__(128) k_adj_sp_solve(Fields F, Consts K, const Work* __restrict__ work,
+                                                     double* __restrict__ yb, const double* __restrict__ ys,
+                                                     double* __restrict__ vb, double* __restrict__ scr, int64_t nlt) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int line = w.first + threadIdx.x;
+  if (line >= zone_lines(Z, DIR)) return;
+  int64_t base, st;
+  line_geometry(Z, DIR, line, base, st);
+  const int n = zone_line_len(Z, DIR);
+  const int64_t gl = Z.lineoff[DIR] + line;
+  const int64_t NP = F.NP;
+  const double dtt1 = DIR == 0 ? K.dttx1 : DIR == 1 ? K.dtty1 : K.dttz1;
+  const double dtt2 = DIR == 0 ? K.dttx2 : DIR == 1 ? K.dtty2 : K.dttz2;
+  const double c2dtt1 = DIR == 0 ? K.c2dttx1 : DIR == 1 ? K.c2dtty1 : K.c2dttz1;
+  auto S = [&](int p, int e) -> double& { return scr[((int64_t)p * 30 + e) * nlt + gl]; };
+  // geometry and bands (the forward solve's sp_geom / sp_assemble)
+  for (int p = 0; p < n; ++p) sp_geom<DIR>(F, K, base + (int64_t)p * st, S(p, 26), S(p, 27), S(p, 28));
+  for (int q = 0; q < n; ++q) {
+    double cv[3], rh[3], sp[3], L[3][5];
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+      const int r = min(max(q + o - 1, 0), n - 1);
+      cv[o] = S(r, 26); rh[o] = S(r, 27); sp[o] = S(r, 28);
+    }
+    sp_assemble<DIR, double, double>(K, q, n, cv, rh, sp, L);
+#pragma unroll
+    for (int s = 0; s < 3; ++s)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) S(q, 5 * s + b) = L[s][b];
+  }
+  // right-hand side: the transform's transpose on the interior (tzetar also
+  // linearised in the state)
+  for (int p = 0; p < n; ++p) {
+    const int64_t pt = base + (int64_t)p * st;
+    double xb[5], yt[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) xb[m] = yb[m * NP + pt];
+    if (p >= 1 && p <= n - 2) {
+      D5 u[5];
+      seed_state(F, pt, u);
+      const SpPrim P = sp_prim(K, u);
+      if (DIR == 2) {
+        D5 yc[5], o[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) yc[m] = dconst(ys[m * NP + pt]);
+        sp_post<2>(K, P, u[0], yc, o);
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          double g = 0.0;
+#pragma unroll
+          for (int m = 0; m < 5; ++m) g += xb[m] * o[m].d[c];
+          vb[c * NP + pt] += g;
+        }
+      }
+      const SpPrim Pv = sp_prim_value(P);
+      const D5 uz = dval(u[0]);
+      transpose_apply([&](const D5 rs[5], D5 o[5]) { sp_post<DIR>(K, Pv, uz, rs, o); }, xb, yt);
+    } else {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) yt[m] = xb[m];
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) S(p, 21 + m) = yt[m];
+  }
+  // L^T lambda = ybar per system: row q of L^T holds column q of L,
+  // L^T[q][q + c - 2] = band (4 - c) of row q + c - 2
+  auto LT = [&](int q, int s, int c) -> double {
+    const int r = q + c - 2;
+    return (r < 0 || r > n - 1) ? 0.0 : S(r, 5 * s + 4 - c);
+  };
+  for (int q = 0; q < n; ++q) {
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      double a2 = LT(q, s, 0), a1 = LT(q, s, 1), d = LT(q, s, 2), e1 = LT(q, s, 3);
+      const double e2 = LT(q, s, 4);
+      double b[3];
+      const int m0 = SP_M0(s), m1 = SP_M1(s);
+      for (int m = m0; m <= m1; ++m) b[m - m0] = S(q, 21 + m);
+      if (q >= 2) {
+        a1 -= a2 * S(q - 2, 15 + 2 * s);
+        d -= a2 * S(q - 2, 16 + 2 * s);
+        for (int m = m0; m <= m1; ++m) b[m - m0] -= a2 * S(q - 2, 21 + m);
+      }
+      if (q >= 1) {
+        d -= a1 * S(q - 1, 15 + 2 * s);
+        e1 -= a1 * S(q - 1, 16 + 2 * s);
+        for (int m = m0; m <= m1; ++m) b[m - m0] -= a1 * S(q - 1, 21 + m);
+      }
+      const double inv = 1.0 / d;
+      S(q, 15 + 2 * s) = e1 * inv;
+      S(q, 16 + 2 * s) = e2 * inv;
+      for (int m = m0; m <= m1; ++m) S(q, 21 + m) = b[m - m0] * inv;
+    }
+  }
+  for (int q = n - 2; q >= 0; --q) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int s = m < 3 ? 0 : m - 2;
+      double t = S(q, 21 + m) - S(q, 15 + 2 * s) * S(q + 1, 21 + m);
+      if (q + 2 <= n - 1) t -= S(q, 16 + 2 * s) * S(q + 2, 21 + m);
+      S(q, 21 + m) = t;
+    }
+  }
+  // linearisation of the bands at each point j, and the output
+  const double da = DIR == 0 ? K.dx2 : DIR == 1 ? K.dy3 : K.dz4;
+  const double db = DIR == 0 ? K.dx5 : DIR == 1 ? K.dy5 : K.dz5;
+  const double dm = DIR == 0 ? K.dxmax : DIR == 1 ? K.dymax : K.dzmax;
+  const double dc = DIR == 0 ? K.dx1 : DIR == 1 ? K.dy1 : K.dz1;
+  for (int j = 0; j < n; ++j) {
+    const int64_t pt = base + (int64_t)j * st;
+    double y[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) y[m] = ys[m * NP + pt];
+    // dot(q, s) = lambda_q . y_j over the components of system s
+    auto dot = [&](int q, int s) -> double {
+      if (q < 1 || q > n - 2) return 0.0;  // identity rows do not depend on the state
+      double t = 0.0;
+      for (int m = SP_M0(s); m <= SP_M1(s); ++m) t += S(q, 21 + m) * y[m];
+      return t;
+    };
+    double gcv = 0.0, grh = 0.0, gsp = 0.0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const double up = dot(j - 1, s), mid = dot(j, s), dn = dot(j + 1, s);
+      gcv += dtt2 * (up - dn);
+      grh += -dtt1 * dn + c2dtt1 * mid - dtt1 * up;
+      if (s == 1) gsp += dtt2 * (up - dn);
+      if (s == 2) gsp += dtt2 * (dn - up);
+    }
+    if (gcv != 0.0 || grh != 0.0 || gsp != 0.0) {
+      D5 u[5];
+      seed_state(F, pt, u);
+      const SpPrim P = sp_prim(K, u);
+      const D5 ru1 = K.c3c4 * P.ri;
+      const D5 rhon = dmax(dmax(dmax(ru1 * K.con43 + da, ru1 * K.c1c5 + db), ru1 + dm), dconst(dc));
+      const D5& cv = P.vel[DIR];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) vb[c * NP + pt] -= gcv * cv.d[c] + grh * rhon.d[c] + gsp * P.speed.d[c];
+    }
+  }
+#pragma unroll 1
+  for (int p = 0; p < n; ++p)
+#pragma unroll
+    for (int m = 0; m < 5; ++m) yb[m * NP + base + (int64_t)p * st] = S(p, 21 + m);
+}
+
 }  // namespace adjk
 
 // ================================ launchers ================================
@@ -464,6 +784,35 @@ void adj_launch_exch(const Fields& F, const int* nbr, int nzones, int max_face, 
 void adj_launch_seed(const Fields& F, const Work* work, int nwork, const double* a, const double* b, double* out,
                      double* partial, int interior_only, cudaStream_t s) {
   if (nwork > 0) adjk::k_adj_seed<<<nwork, 128, 0, s>>>(F, work, a, b, out, partial, interior_only);
+}
+
+void sp_fwd_launch_solve(int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb, double* ys,
+                         double* scr, int64_t nlt, cudaStream_t s) {
+  if (nwork <= 0) return;
+  if (dir == 0) adjk::k_sp_solve<0, double><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, 0, ys, 0);
+  else if (dir == 1) adjk::k_sp_solve<1, double><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, 0, ys, 0);
+  else adjk::k_sp_solve<2, double><<<nwork, tpb, 0, s>>>(F, K, work, scr, nlt, 0, ys, 0);
+}
+
+void sp_fwd_launch_post(int dir, const Fields& F, const Consts& K, const Work* work, int nwork, const double* ys,
+                        cudaStream_t s) {
+  if (nwork <= 0) return;
+  if (dir == 0) adjk::k_sp_apply_post<0><<<nwork, 128, 0, s>>>(F, K, work, ys);
+  else if (dir == 1) adjk::k_sp_apply_post<1><<<nwork, 128, 0, s>>>(F, K, work, ys);
+  else adjk::k_sp_apply_post<2><<<nwork, 128, 0, s>>>(F, K, work, ys);
+}
+
+void adj_launch_sp_solve(int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb, double* yb,
+                         const double* ys, double* vb, double* scr, int64_t nlt, cudaStream_t s) {
+  if (nwork <= 0) return;
+  if (dir == 0) adjk::k_adj_sp_solve<0><<<nwork, tpb, 0, s>>>(F, K, work, yb, ys, vb, scr, nlt);
+  else if (dir == 1) adjk::k_adj_sp_solve<1><<<nwork, tpb, 0, s>>>(F, K, work, yb, ys, vb, scr, nlt);
+  else adjk::k_adj_sp_solve<2><<<nwork, tpb, 0, s>>>(F, K, work, yb, ys, vb, scr, nlt);
+}
+
+void adj_launch_sp_txinvr(const Fields& F, const Consts& K, const Work* work, int nwork, double* rb, const double* r0,
+                          double* vb, cudaStream_t s) {
+  if (nwork > 0) adjk::k_adj_sp_txinvr<<<nwork, 128, 0, s>>>(F, K, work, rb, r0, vb);
 }
 
 }  // namespace npbmz

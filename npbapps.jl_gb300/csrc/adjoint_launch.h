@@ -1,5 +1,5 @@
 // adjoint_launch.h -- host launchers of adjoint.cu (discrete adjoint of the
-// BT-MZ step).
+// BT-MZ and SP-MZ steps).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -21,4 +21,19 @@ void adj_launch_exch(const Fields& F, const int* nbr, int nzones, int max_face, 
                      cudaStream_t s);
 void adj_launch_seed(const Fields& F, const Work* work, int nwork, const double* a, const double* b, double* out,
                      double* partial, int interior_only, cudaStream_t s);
+// SP forward recomputation: sweep dir's untransformed FP64 solution of the
+// lines into ys (ys must hold the sweep's input, whose line ends it keeps;
+// scr: 6 doubles per line point), and its transform from ys into rhs.
+void sp_fwd_launch_solve(int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb, double* ys,
+                         double* scr, int64_t nlt, cudaStream_t s);
+void sp_fwd_launch_post(int dir, const Fields& F, const Consts& K, const Work* work, int nwork, const double* ys,
+                        cudaStream_t s);
+// SP transposed sweep dir (yb in/out as adj_launch_solve; ys the forward
+// untransformed solution; scr 30 doubles per line point) and the txinvr
+// adjoint (rb in: adjoint of txinvr's output, out: of compute_rhs's; r0 the
+// forward compute_rhs output) over the all-points work list.
+void adj_launch_sp_solve(int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb, double* yb,
+                         const double* ys, double* vb, double* scr, int64_t nlt, cudaStream_t s);
+void adj_launch_sp_txinvr(const Fields& F, const Consts& K, const Work* work, int nwork, double* rb, const double* r0,
+                          double* vb, cudaStream_t s);
 }  // namespace npbmz

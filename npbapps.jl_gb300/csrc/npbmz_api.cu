@@ -1005,6 +1005,62 @@ int adjoint_recompute(npbmz_t* h, double* const x[3]) {
   return 0;
 }
 
+// SP: step n recomputed from u_n (FP64): h->u becomes v = exch_qbc(u_n),
+// r0 the compute_rhs output before txinvr, y[d] sweep d's untransformed
+// solution (its input at the line ends).
+int adjoint_recompute_sp(npbmz_t* h, double* const y[3], double* r0, double* scr) {
+  const size_t bytes = 5 * (size_t)h->NP * sizeof(double);
+  if (phase_exch(h)) return -1;
+  if (phase_prim(h, -1)) return -1;
+  if (phase_rhs(h, -1, false, false)) return -1;
+  CK(h, cudaMemcpyAsync(r0, h->rhs, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  if (phase_rhs(h, -1, true, false)) return -1;
+  const Fields F = fields(h);
+  for (int dir = 0; dir < 3; ++dir) {
+    CK(h, cudaMemcpyAsync(y[dir], h->rhs, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    if (line_launches(h, dir, -1, [&](int lo, int hi, int tpb) {
+          sp_fwd_launch_solve(dir, F, h->K, h->wline_d[dir] + lo, hi - lo, tpb, y[dir], scr, h->nlines[dir],
+                              h->stream);
+          CKL(h);
+          return 0;
+        }))
+      return -1;
+    sp_fwd_launch_post(dir, F, h->K, h->wpts_d, h->nwpts, y[dir], h->stream);
+    CKL(h);
+  }
+  return 0;
+}
+
+// SP: ub <- (d u_{n+1} / d u_n)^T ub, fb += (d u_{n+1} / d forcing)^T ub,
+// after adjoint_recompute_sp of step n.
+int adjoint_back_step_sp(npbmz_t* h, double* const y[3], const double* r0, double* ub, double* vb, double* yb,
+                         double* fb, double* scr) {
+  const size_t bytes = 5 * (size_t)h->NP * sizeof(double);
+  const Fields F = fields(h);
+  CK(h, cudaMemcpyAsync(vb, ub, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  adj_launch_seed(F, h->wpts_d, h->nwpts, ub, nullptr, yb, nullptr, 1, h->stream);
+  CKL(h);
+  for (int dir = 2; dir >= 0; --dir) {
+    if (line_launches(h, dir, -1, [&](int lo, int hi, int tpb) {
+          adj_launch_sp_solve(dir, F, h->K, h->wline_d[dir] + lo, hi - lo, tpb, yb, y[dir], vb, scr, h->nlines[dir],
+                              h->stream);
+          CKL(h);
+          return 0;
+        }))
+      return -1;
+  }
+  adj_launch_sp_txinvr(F, h->K, h->wpts_d, h->nwpts, yb, r0, vb, h->stream);
+  CKL(h);
+  adj_launch_rhs(F, h->K, h->wpts_d, h->nwpts, yb, vb, fb, h->stream);
+  CKL(h);
+  CK(h, cudaMemcpyAsync(ub, vb, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->nzones > 1) {
+    adj_launch_exch(F, h->nbr_d, h->nzones, h->max_face, vb, ub, h->stream);
+    CKL(h);
+  }
+  return 0;
+}
+
 // ub <- (d u_{n+1} / d u_n)^T ub and fb += (d u_{n+1} / d forcing)^T ub,
 // after adjoint_recompute of step n.
 int adjoint_back_step(npbmz_t* h, double* const x[3], double* ub, double* vb, double* yb, double* fb, double* scr) {
@@ -1049,10 +1105,12 @@ int adjoint_run(npbmz_t* h, int nsteps, int every, const double* u_target, doubl
     scr_elems = std::max<int64_t>(scr_elems, 30 * (int64_t)maxlen * h->nlines[dir]);
   }
   AdjointBuffers B;
-  double *ck, *seg, *x[3], *yb, *vb, *ub, *fb, *tgt, *scr, *part;
+  const bool sp = h->kind == NPBMZ_SP;
+  double *ck, *seg, *x[3], *yb, *vb, *ub, *fb, *tgt, *scr, *part, *r0 = nullptr;
   if (B.get(h, &ck, (size_t)nck * F5) || B.get(h, &seg, (size_t)seglen * F5) || B.get(h, &x[0], F5) ||
       B.get(h, &x[1], F5) || B.get(h, &x[2], F5) || B.get(h, &yb, F5) || B.get(h, &vb, F5) || B.get(h, &ub, F5) ||
-      B.get(h, &fb, F5) || B.get(h, &tgt, F5) || B.get(h, &scr, (size_t)scr_elems) || B.get(h, &part, 5 * (size_t)h->nwpts))
+      B.get(h, &fb, F5) || B.get(h, &tgt, F5) || B.get(h, &scr, (size_t)scr_elems) || B.get(h, &part, 5 * (size_t)h->nwpts) ||
+      (sp && B.get(h, &r0, F5)))
     return -1;
   CK(h, cudaMemsetAsync(fb, 0, bytes, s));
   CK(h, cudaMemsetAsync(tgt, 0, bytes, s));
@@ -1087,8 +1145,13 @@ int adjoint_run(npbmz_t* h, int nsteps, int every, const double* u_target, doubl
     }
     for (int n = n1 - 1; n >= n0 && !rc; --n) {
       rc = cudaMemcpyAsync(h->u, seg + (size_t)(n - n0) * F5, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess;
-      if (!rc) rc = adjoint_recompute(h, x);
-      if (!rc) rc = adjoint_back_step(h, x, ub, vb, yb, fb, scr);
+      if (sp) {
+        if (!rc) rc = adjoint_recompute_sp(h, x, r0, scr);
+        if (!rc) rc = adjoint_back_step_sp(h, x, r0, ub, vb, yb, fb, scr);
+      } else {
+        if (!rc) rc = adjoint_recompute(h, x);
+        if (!rc) rc = adjoint_back_step(h, x, ub, vb, yb, fb, scr);
+      }
     }
   }
   if (!rc && grad_forcing) rc = dense_io(h, fb, grad_forcing, 1);
@@ -1507,7 +1570,6 @@ int npbmz_verify(npbmz_t* h, double* xcr, double* xce) {
 int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_target, double* J,
                   double* grad_forcing, double* grad_u0) {
   if (!h) return fail(nullptr, "null handle");
-  if (h->kind != NPBMZ_BT) return fail(h, "the discrete adjoint covers BT-MZ only");
   if (nsteps < 1 || checkpoint_every < 1) return fail(h, "nsteps and checkpoint_every must be >= 1");
   if (!u_target) return fail(h, "u_target is null");
   h->err.clear();

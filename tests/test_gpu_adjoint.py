@@ -213,16 +213,60 @@ def test_adjoint_rejects_bad_arguments(config3):
     p, target, _ = config3
     with pytest.raises(npbmz.NpbmzError, match="checkpoint_every"):
         p.adjoint(5, target, checkpoint_every=0)
-    geom, dt, _ = geom_class_sp()
-    q = npbmz.Problem(geom, dt, 0)
-    with pytest.raises(npbmz.NpbmzError, match="BT-MZ only"):
-        q.adjoint(1, [np.zeros(q.zone_shape(z)) for z in range(geom.nzones)])
+    with pytest.raises(npbmz.NpbmzError, match="nsteps"):
+        p.adjoint(0, target)
 
 
-def geom_class_sp():
-    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES["SP"]["S"]
-    nx, ny, nz, nbr = npbmz.zone_setup(npbmz.SP, gx, gy, gz, xz, yz, ratio)
-    return npbmz.Geometry(npbmz.SP, nx, ny, nz, nbr, gx, gy, gz, xz, yz), dt, niter
+# ---- SP-MZ ----------------------------------------------------------------------
+# SP-MZ 64x64x8 split 4x4 into equal 16x16x8 zones, dt 1.5e-3 (the class W
+# geometry), 30 steps, checkpoints every 10.  The transposed pentadiagonal
+# sweeps, the transposes of ninvr / pinvr / tzetar / txinvr and the
+# linearisations of the bands (velocity, rhon, speed of each column's point)
+# and of tzetar / txinvr in the state are SP's own; compute_rhs and exch_qbc
+# share BT's adjoint.
+
+def geom_sp():
+    gx, gy, gz, xz, yz = 64, 64, 8, 4, 4
+    nx, ny, nz, nbr = npbmz.zone_setup(npbmz.SP, gx, gy, gz, xz, yz, 1.0)
+    return npbmz.Geometry(npbmz.SP, nx, ny, nz, nbr, gx, gy, gz, xz, yz), 0.0015, 30
+
+
+@pytest.fixture(scope="module")
+def sp_case():
+    geom, dt, nsteps = geom_sp()
+    p, ce, target = build_case(geom, dt, seed=5)
+    return p, target, nsteps
+
+
+@pytest.mark.parametrize("field,h", [(npbmz.FORCING, 1e-5), (npbmz.U, 1e-6)], ids=["forcing", "u0"])
+def test_sp_adjoint_matches_central_differences(sp_case, field, h):
+    p, target, nsteps = sp_case
+    J, grad, errs = fd_check(p, target, nsteps, 10, field, seed=91, h=h)
+    print(f"SP field {field} h {h:.0e}: worst {max(errs):.2e}, median {np.median(errs):.2e}")
+    assert J > 0.0 and np.all(np.isfinite(grad))
+    assert max(errs) <= ADJ_REL, f"max rel err {max(errs):.3e} over {NDIR} directions: {errs}"
+
+
+def test_sp_checkpoint_interval_does_not_change_the_gradient(sp_case):
+    p, target, nsteps = sp_case
+    ref = p.adjoint(nsteps, target, checkpoint_every=10)
+    for every in (1, 7, 30):
+        got = p.adjoint(nsteps, target, checkpoint_every=every)
+        assert got[0] == ref[0]
+        for a, b in zip(got[1] + got[2], ref[1] + ref[2]):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_sp_objective_matches_forward_path(sp_case):
+    p, target, nsteps = sp_case
+    u0 = p.flatten(p.download_all(npbmz.U))
+    J, _, _ = p.adjoint(nsteps, target, checkpoint_every=10, grad_forcing=False, grad_u0=False)
+    assert np.array_equal(p.flatten(p.download_all(npbmz.U)), u0)
+    p.step(nsteps)
+    p.synchronize()
+    a = p.flatten(p.download_all(npbmz.U)) - p.flatten(target)
+    np.testing.assert_allclose(J, 0.5 * math.fsum(a * a), rtol=1e-12)
+    p.upload_all(npbmz.U, u0)
 
 
 def test_torch_autograd_function(config3):
