@@ -37,9 +37,10 @@
 //
 // The state (u, rhs, forcing and the primitive variables) has the scalar type
 // `real`, double here.  oracle/npbmz_tangent.cpp includes this file with a
-// forward-mode dual number as `real` (ORACLE_REAL, ORACLE_BT_ONLY) to push
-// directional derivatives through the same BT statements; the dual's value
-// part then follows exactly the double operations of this file.
+// forward-mode dual number as `real` (ORACLE_REAL, ORACLE_TANGENT) to push
+// directional derivatives through the same BT and SP statements, with the
+// line solves in `real`; the dual's value part then follows exactly the
+// double operations of this file.
 
 #include <algorithm>
 #include <cmath>
@@ -50,14 +51,16 @@
 #ifndef ORACLE_REAL
 #define ORACLE_REAL double
 #endif
-#ifndef ORACLE_BT_ONLY
-#define ORACLE_BT_ONLY 0
+#ifndef ORACLE_TANGENT
+#define ORACLE_TANGENT 0
 #endif
 
 namespace {
 
 typedef ORACLE_REAL real;
 inline double value(double x) { return x; }
+// std::max(a, b) on the value part: b when a < b, else a
+inline real rmax(const real& a, const real& b) { return value(a) < value(b) ? b : a; }
 
 constexpr int KIND_BT = 0;
 constexpr int KIND_SP = 1;
@@ -916,7 +919,6 @@ void bt_sweep(Problem& pb, Zone& z, int dir) {
     }
 }
 
-#if !ORACLE_BT_ONLY
 // ======================= SP scalar pentadiagonal solves ======================
 // txinvr (src/SP/txinvr.jl:5-56)
 void txinvr(Zone& z) {
@@ -924,13 +926,13 @@ void txinvr(Zone& z) {
     for (int j = 1; j <= z.ny - 2; ++j)
       for (int i = 1; i <= z.nx - 2; ++i) {
         size_t P = z.P(i, j, k);
-        double ru1 = z.rho_i[P], uu = z.us[P], vv = z.vs[P], ww = z.ws[P], ac = z.speed[P];
-        double ac2inv = 1.0 / (ac * ac);
-        double r1 = z.R(0, i, j, k), r2 = z.R(1, i, j, k), r3 = z.R(2, i, j, k), r4 = z.R(3, i, j, k),
+        real ru1 = z.rho_i[P], uu = z.us[P], vv = z.vs[P], ww = z.ws[P], ac = z.speed[P];
+        real ac2inv = 1.0 / (ac * ac);
+        real r1 = z.R(0, i, j, k), r2 = z.R(1, i, j, k), r3 = z.R(2, i, j, k), r4 = z.R(3, i, j, k),
                r5 = z.R(4, i, j, k);
-        double t1 = c2 * ac2inv * (z.qs[P] * r1 - uu * r2 - vv * r3 - ww * r4 + r5);
-        double t2 = bt_ * ru1 * (uu * r1 - r2);
-        double t3 = (bt_ * ru1 * ac) * t1;
+        real t1 = c2 * ac2inv * (z.qs[P] * r1 - uu * r2 - vv * r3 - ww * r4 + r5);
+        real t2 = bt_ * ru1 * (uu * r1 - r2);
+        real t3 = (bt_ * ru1 * ac) * t1;
         z.R(0, i, j, k) = r1 - t1;
         z.R(1, i, j, k) = -ru1 * (ww * r1 - r4);
         z.R(2, i, j, k) = ru1 * (vv * r1 - r3);
@@ -944,13 +946,13 @@ void txinvr(Zone& z) {
 // n-1 are the identity rows lhsinit leaves there (src/SP/initialize.jl:235-256);
 // the in-place updates the reference applies to them leave them unchanged.
 template <class T>
-void sp_line(int n, const double* rho_i, const double* cvel, const double* speed, double* rl, const Consts& K,
+void sp_line(int n, const real* rho_i, const real* cvel, const real* speed, real* rl, const Consts& K,
              int dir) {
   double dtt1, dtt2, c2dtt1, da, db, dmax_, dc;
   if (dir == 0) { dtt1 = K.dttx1; dtt2 = K.dttx2; c2dtt1 = K.c2dttx1; da = dx2; db = dx5; dmax_ = dxmax; dc = dx1; }
   else if (dir == 1) { dtt1 = K.dtty1; dtt2 = K.dtty2; c2dtt1 = K.c2dtty1; da = dy3; db = dy5; dmax_ = dymax; dc = dy1; }
   else { dtt1 = K.dttz1; dtt2 = K.dttz2; c2dtt1 = K.c2dttz1; da = dz4; db = dz5; dmax_ = dzmax; dc = dz1; }
-  static thread_local std::vector<double> rhon, cv, L64;
+  static thread_local std::vector<real> rhon, cv, L64;
   static thread_local std::vector<T> L, r;
   rhon.resize(n);
   cv.resize(n);
@@ -961,13 +963,13 @@ void sp_line(int n, const double* rho_i, const double* cvel, const double* speed
   for (int p = 0; p < n; ++p)
     for (int b = 0; b < 15; ++b) l(p, b) = (b == 2 || b == 7 || b == 12) ? (T)1 : (T)0;
   for (int p = 0; p < n; ++p) {
-    double ru1 = c3c4 * rho_i[p];
+    real ru1 = c3c4 * rho_i[p];
     cv[p] = cvel[p];
-    rhon[p] = std::max(std::max(std::max(da + con43 * ru1, db + c1c5 * ru1), dmax_ + ru1), dc);
+    rhon[p] = rmax(rmax(rmax(da + con43 * ru1, db + c1c5 * ru1), dmax_ + ru1), real(dc));
   }
   // lhs assembly is FP64 in the reference; it is converted to T afterwards.
-  L64.assign((size_t)n * 5, 0.0);
-  auto l64 = [&](int p, int b) -> double& { return L64[(size_t)p * 5 + b]; };
+  L64.assign((size_t)n * 5, real(0.0));
+  auto l64 = [&](int p, int b) -> real& { return L64[(size_t)p * 5 + b]; };
   for (int p = 1; p <= n - 2; ++p) {
     l64(p, 0) = 0.0e0;
     l64(p, 1) = -dtt2 * cv[p - 1] - dtt1 * rhon[p - 1];
@@ -989,7 +991,7 @@ void sp_line(int n, const double* rho_i, const double* cvel, const double* speed
     l64(p + 1, 0) += K.comz1; l64(p + 1, 1) -= K.comz4; l64(p + 1, 2) += K.comz5;
   }
   for (int p = 1; p <= n - 2; ++p) {
-    double L1 = l64(p, 0), L2 = l64(p, 1), L3 = l64(p, 2), L4 = l64(p, 3), L5 = l64(p, 4);
+    real L1 = l64(p, 0), L2 = l64(p, 1), L3 = l64(p, 2), L4 = l64(p, 3), L5 = l64(p, 4);
     l(p, 0) = (T)L1; l(p, 1) = (T)L2; l(p, 2) = (T)L3; l(p, 3) = (T)L4; l(p, 4) = (T)L5;
     l(p, 5) = (T)L1;
     l(p, 6) = (T)(L2 - dtt2 * speed[p - 1]);
@@ -1041,7 +1043,7 @@ void sp_line(int n, const double* rho_i, const double* cvel, const double* speed
     for (p = n - 3; p >= 0; --p)
       r[p * 5 + m] -= l(p, nb + 3) * r[(p + 1) * 5 + m] + l(p, nb + 4) * r[(p + 2) * 5 + m];
   }
-  for (int p = 0; p < n * 5; ++p) rl[p] = (double)r[p];
+  for (int p = 0; p < n * 5; ++p) rl[p] = (real)r[p];
 }
 
 template <class T>
@@ -1049,7 +1051,7 @@ void sp_sweep(Problem& pb, Zone& z, int dir) {
   int n = dir == 0 ? z.nx : (dir == 1 ? z.ny : z.nz);
   int na = dir == 0 ? z.ny : z.nx;
   int nb = dir == 2 ? z.ny : z.nz;
-  std::vector<double> ri(n), cvel(n), spd(n), rl(n * 5);
+  std::vector<real> ri(n), cvel(n), spd(n), rl(n * 5);
   for (int b = 1; b <= nb - 2; ++b)
     for (int a = 1; a <= na - 2; ++a) {
       for (int p = 0; p < n; ++p) {
@@ -1070,19 +1072,19 @@ void sp_sweep(Problem& pb, Zone& z, int dir) {
   for (int k = 1; k <= z.nz - 2; ++k)
     for (int j = 1; j <= z.ny - 2; ++j)
       for (int i = 1; i <= z.nx - 2; ++i) {
-        double r1 = z.R(0, i, j, k), r2 = z.R(1, i, j, k), r3 = z.R(2, i, j, k), r4 = z.R(3, i, j, k),
-               r5 = z.R(4, i, j, k);
+        real r1 = z.R(0, i, j, k), r2 = z.R(1, i, j, k), r3 = z.R(2, i, j, k), r4 = z.R(3, i, j, k),
+             r5 = z.R(4, i, j, k);
         if (dir == 0) {  // src/SP/ninvr.jl:19-32
-          double t1 = bt_ * r3;
-          double t2 = 0.5e0 * (r4 + r5);
+          real t1 = bt_ * r3;
+          real t2 = 0.5e0 * (r4 + r5);
           z.R(0, i, j, k) = -r2;
           z.R(1, i, j, k) = r1;
           z.R(2, i, j, k) = bt_ * (r4 - r5);
           z.R(3, i, j, k) = -t1 + t2;
           z.R(4, i, j, k) = t1 + t2;
         } else if (dir == 1) {  // src/SP/pinvr.jl:20-33
-          double t1 = bt_ * r1;
-          double t2 = 0.5e0 * (r4 + r5);
+          real t1 = bt_ * r1;
+          real t2 = 0.5e0 * (r4 + r5);
           z.R(0, i, j, k) = bt_ * (r4 - r5);
           z.R(1, i, j, k) = -r3;
           z.R(2, i, j, k) = r2;
@@ -1090,13 +1092,13 @@ void sp_sweep(Problem& pb, Zone& z, int dir) {
           z.R(4, i, j, k) = t1 + t2;
         } else {  // src/SP/tzetar.jl:27-52
           size_t P = z.P(i, j, k);
-          double xvel = z.us[P], yvel = z.vs[P], zvel = z.ws[P], ac = z.speed[P], acinv = z.ainv[P];
-          double ac2u = ac * ac;
-          double uzik1 = z.U(0, i, j, k);
-          double btuz = bt_ * uzik1;
-          double t1 = btuz * acinv * (r4 + r5);
-          double t2 = r3 + t1;
-          double t3 = btuz * (r4 - r5);
+          real xvel = z.us[P], yvel = z.vs[P], zvel = z.ws[P], ac = z.speed[P], acinv = z.ainv[P];
+          real ac2u = ac * ac;
+          real uzik1 = z.U(0, i, j, k);
+          real btuz = bt_ * uzik1;
+          real t1 = btuz * acinv * (r4 + r5);
+          real t2 = r3 + t1;
+          real t3 = btuz * (r4 - r5);
           z.R(0, i, j, k) = t2;
           z.R(1, i, j, k) = -uzik1 * r2 + xvel * t2;
           z.R(2, i, j, k) = uzik1 * r1 + yvel * t2;
@@ -1106,7 +1108,6 @@ void sp_sweep(Problem& pb, Zone& z, int dir) {
       }
 }
 
-#endif  // !ORACLE_BT_ONLY
 
 void add(Zone& z) {
   for (int k = 1; k <= z.nz - 2; ++k)
@@ -1126,8 +1127,13 @@ void adi(Problem& pb, Zone& z, double* xcr = nullptr) {
     double xce_unused[5];
     zone_norms(pb, z, xce_unused, xcr);
   }
-#if ORACLE_BT_ONLY
-  for (int d = 0; d < 3; ++d) bt_sweep<real>(pb, z, d);
+#if ORACLE_TANGENT
+  if (pb.kind == KIND_BT) {
+    for (int d = 0; d < 3; ++d) bt_sweep<real>(pb, z, d);
+  } else {
+    txinvr(z);
+    for (int d = 0; d < 3; ++d) sp_sweep<real>(pb, z, d);
+  }
 #else
   if (pb.kind == KIND_BT) {
     for (int d = 0; d < 3; ++d) {
@@ -1178,7 +1184,7 @@ void zone_norms(Problem& pb, Zone& z, double xce[5], double xcr[5]) {
 
 }  // namespace
 
-#if !ORACLE_BT_ONLY
+#if !ORACLE_TANGENT
 // =============================== C ABI ======================================
 extern "C" {
 
@@ -1357,4 +1363,4 @@ int oracle_set(oracle_t* h, int which, int zone, const double* in) {
 }
 
 }  // extern "C"
-#endif  // !ORACLE_BT_ONLY
+#endif  // !ORACLE_TANGENT

@@ -1,17 +1,20 @@
 // npbmz_tangent.cpp -- forward-mode dual numbers through the CPU oracle's BT-MZ
-// time step: the reference gradient for the discrete adjoint.
+// and SP-MZ time steps: the reference gradient for the discrete adjoint.
 //
 // TEST INFRASTRUCTURE ONLY (like npbmz_oracle.cpp, which this file compiles a
 // second time): only tests/ load libnpbmz_tangent.so, as the checker of the
 // GPU adjoint (npbmz_adjoint).  The reference would take this gradient with
 // ForwardDiff.jl dual numbers pushed through its Julia step (exch_qbc + adi,
-// src/BT/bt-node.jl:280-395); Julia is not available here, so the oracle's
+// src/BT/bt-node.jl:280-395, src/SP/sp-node.jl:258-297); Julia is not
+// available here, so the oracle's
 // restatement of that step (npbmz_oracle.cpp, state type `real`) is
 // instantiated with a dual number of NDIR directional parts.  The value part
 // of every dual performs exactly the double operations of the oracle, so the
 // primal trajectory is the oracle's bit for bit; each directional part is the
 // exact derivative (up to rounding) of the discrete step along one seeded
-// direction of (u_0, forcing).
+// direction of (u_0, forcing).  The line solves run in the dual type too (the
+// oracle's FP64 reference path); SP's std::max of the viscous band term
+// compares value parts, so its derivative is that of the selected branch.
 #include <cmath>
 
 namespace npbmz_tangent {
@@ -118,26 +121,27 @@ inline Dual sqrt(const Dual& a) {
 }  // namespace npbmz_tangent
 
 #define ORACLE_REAL npbmz_tangent::Dual
-#define ORACLE_BT_ONLY 1
+#define ORACLE_TANGENT 1
 #include "npbmz_oracle.cpp"
 
 extern "C" {
 
 // J = 1/2 sum over every stored point of every zone of (u_N - u_target)^2
-// after nsteps BT-MZ steps (exch_qbc over all zones when there are several,
-// then adi per zone) from u0 with the given forcing, and its derivatives
-// dJ[d] along ndir <= 16 directions (du0[d], dforcing[d]; either array may be
-// NULL for zero).  Every array is the dense layout of all zones back to back
-// (zone z: [5][nz][ny][nx]); du0 and dforcing hold ndir such arrays.  uN
-// (nullable) receives the value part of u_N.
-int tangent_bt_objective(int nzones, const int* nx, const int* ny, const int* nz, const int* nbr, double dt, int gx,
-                         int gy, int gz, int xz, int yz, const double* u0, const double* forcing,
-                         const double* u_target, int nsteps, int ndir, const double* du0, const double* dforcing,
-                         double* J, double* dJ, double* uN) {
+// after nsteps BT-MZ (kind 0) or SP-MZ (kind 1) steps (exch_qbc over all zones
+// when there are several, then adi per zone) from u0 with the given forcing,
+// and its derivatives dJ[d] along ndir <= 16 directions (du0[d], dforcing[d];
+// either array may be NULL for zero).  Every array is the dense layout of all
+// zones back to back (zone z: [5][nz][ny][nx]); du0 and dforcing hold ndir
+// such arrays.  uN (nullable) receives the value part of u_N.
+int tangent_objective(int kind, int nzones, const int* nx, const int* ny, const int* nz, const int* nbr, double dt,
+                      int gx, int gy, int gz, int xz, int yz, const double* u0, const double* forcing,
+                      const double* u_target, int nsteps, int ndir, const double* du0, const double* dforcing,
+                      double* J, double* dJ, double* uN) {
   using npbmz_tangent::Dual;
   if (ndir < 0 || ndir > npbmz_tangent::NDIR || nzones < 1 || nsteps < 0) return -1;
+  if (kind != KIND_BT && kind != KIND_SP) return -1;
   Problem pb;
-  pb.kind = KIND_BT;
+  pb.kind = kind;
   pb.nzones = nzones;
   pb.k = set_constants(dt, gx, gy, gz, xz, yz);
   std::memset(pb.ce, 0, sizeof(pb.ce));
@@ -192,6 +196,15 @@ int tangent_bt_objective(int nzones, const int* nx, const int* ny, const int* nz
   if (dJ)
     for (int d = 0; d < ndir; ++d) dJ[d] = 0.5 * acc.d[d];
   return 0;
+}
+
+// the BT-MZ form of tangent_objective
+int tangent_bt_objective(int nzones, const int* nx, const int* ny, const int* nz, const int* nbr, double dt, int gx,
+                         int gy, int gz, int xz, int yz, const double* u0, const double* forcing,
+                         const double* u_target, int nsteps, int ndir, const double* du0, const double* dforcing,
+                         double* J, double* dJ, double* uN) {
+  return tangent_objective(KIND_BT, nzones, nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, u0, forcing, u_target, nsteps,
+                           ndir, du0, dforcing, J, dJ, uN);
 }
 
 }  // extern "C"

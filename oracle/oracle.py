@@ -3,7 +3,7 @@
 The oracle restates the NPBApps.jl BT-MZ/SP-MZ single-rank time step on the
 CPU (oracle/npbmz_oracle.cpp).  Only tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py use it, always as the checker.  The tangent
-library (oracle/npbmz_tangent.cpp) is the same BT restatement with
+library (oracle/npbmz_tangent.cpp) is the same BT and SP restatement with
 forward-mode dual numbers: the reference directional derivatives against
 which tests check the GPU adjoint.
 """
@@ -39,18 +39,19 @@ def tangent_lib():
         L = ctypes.CDLL(str(_TAN_PATH))
         ip = ctypes.POINTER(ctypes.c_int)
         dp = ctypes.POINTER(ctypes.c_double)
-        L.tangent_bt_objective.argtypes = ([ctypes.c_int, ip, ip, ip, ip, ctypes.c_double] + [ctypes.c_int] * 5 +
-                                           [dp, dp, dp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp])
+        L.tangent_objective.argtypes = ([ctypes.c_int] * 2 + [ip, ip, ip, ip, ctypes.c_double] + [ctypes.c_int] * 5 +
+                                        [dp, dp, dp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp])
         _tan = L
     return _tan
 
 
-def tangent_bt_objective(nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, u0, forcing, u_target, nsteps, du0=None,
-                         dforcing=None):
-    """J = 1/2 sum (u_N - u_target)^2 after nsteps BT-MZ steps and its
-    derivatives along up to 16 directions, by dual numbers through the
-    oracle.  Flat dense arrays (zone z: [5][nz][ny][nx], zones back to back);
-    du0 / dforcing: (ndir, total) or None.  Returns (J, dJ[ndir], u_N)."""
+def tangent_objective(kind, nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, u0, forcing, u_target, nsteps, du0=None,
+                      dforcing=None):
+    """J = 1/2 sum (u_N - u_target)^2 after nsteps BT-MZ (KIND_BT) or SP-MZ
+    (KIND_SP) steps and its derivatives along up to 16 directions, by dual
+    numbers through the oracle.  Flat dense arrays (zone z: [5][nz][ny][nx],
+    zones back to back); du0 / dforcing: (ndir, total) or None.  Returns
+    (J, dJ[ndir], u_N)."""
     nx, ny, nz, nbr = (np.ascontiguousarray(a, np.int32) for a in (nx, ny, nz, nbr))
     u0, forcing, u_target = (np.ascontiguousarray(a, np.float64) for a in (u0, forcing, u_target))
     total = u0.size
@@ -62,12 +63,17 @@ def tangent_bt_objective(nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, u0, forcing, u
     J = np.zeros(1)
     dJ = np.zeros(max(ndir, 1))
     uN = np.zeros(total)
-    rc = tangent_lib().tangent_bt_objective(len(nx), _ip(nx), _ip(ny), _ip(nz), _ip(nbr), dt, gx, gy, gz, xz, yz,
-                                            _dp(u0), _dp(forcing), _dp(u_target), nsteps, ndir,
-                                            _dp(du0) if du0 is not None else None,
-                                            _dp(dforcing) if dforcing is not None else None, _dp(J), _dp(dJ), _dp(uN))
+    rc = tangent_lib().tangent_objective(kind, len(nx), _ip(nx), _ip(ny), _ip(nz), _ip(nbr), dt, gx, gy, gz, xz, yz,
+                                         _dp(u0), _dp(forcing), _dp(u_target), nsteps, ndir,
+                                         _dp(du0) if du0 is not None else None,
+                                         _dp(dforcing) if dforcing is not None else None, _dp(J), _dp(dJ), _dp(uN))
     assert rc == 0, rc
     return float(J[0]), dJ[:ndir], uN
+
+
+def tangent_bt_objective(*args, **kw):
+    """tangent_objective for BT-MZ."""
+    return tangent_objective(KIND_BT, *args, **kw)
 
 
 def lib():

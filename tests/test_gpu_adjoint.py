@@ -31,7 +31,7 @@ of 16: 4.6e-8; J is nearly linear in the forcing, so the O(h^2) term stays
 below 1e-9).  SP-MZ (below) meets the bar at h = 1e-6 for u_0.
 
 The gradient is also checked against forward-mode dual numbers pushed
-through the CPU oracle's BT step (oracle/npbmz_tangent.cpp, the stand-in for
+through the CPU oracle's BT and SP steps (oracle/npbmz_tangent.cpp, the stand-in for
 ForwardDiff through the reference's Julia code) along 8 directions in u_0
 and 8 in the forcing, to 1e-9 relative: both are exact derivatives of the
 same discrete step, apart from rounding and the FMA contraction of the GPU
@@ -169,8 +169,8 @@ def test_config3_adjoint_matches_dual_numbers(config3):
     df = np.zeros((16, u0.size))
     du[:8] = rng.standard_normal((8, u0.size)) * variable_scale(p, u0)
     df[8:] = rng.standard_normal((8, u0.size)) * variable_scale(p, f0)
-    Jd, dJ, _ = oracle.tangent_bt_objective(g.nx, g.ny, g.nz, g.nbr, p.dt, g.gx, g.gy, g.gz, g.x_zones, g.y_zones,
-                                            u0, f0, t, nsteps, du0=du, dforcing=df)
+    Jd, dJ, _ = oracle.tangent_objective(oracle.KIND_BT, g.nx, g.ny, g.nz, g.nbr, p.dt, g.gx, g.gy, g.gz, g.x_zones,
+                                         g.y_zones, u0, f0, t, nsteps, du0=du, dforcing=df)
     assert J == pytest.approx(Jd, rel=1e-10)
     ad = du @ p.flatten(gu) + df @ p.flatten(gf)
     rel = np.abs(ad - dJ) / np.abs(dJ)
@@ -252,6 +252,32 @@ def test_sp_adjoint_matches_central_differences(sp_case, field, h):
     print(f"SP field {field} h {h:.0e}: worst {max(errs):.2e}, median {np.median(errs):.2e}")
     assert J > 0.0 and np.all(np.isfinite(grad))
     assert max(errs) <= ADJ_REL, f"max rel err {max(errs):.3e} over {NDIR} directions: {errs}"
+
+
+def test_sp_adjoint_matches_dual_numbers(sp_case):
+    """The SP adjoint against dual numbers through the oracle's SP step (line
+    solves in FP64 there, as on this path) along 8 directions in u_0 and 8 in
+    the forcing, to 1e-9 relative."""
+    from oracle import oracle
+
+    p, target, nsteps = sp_case
+    g = p.geom
+    u0 = p.flatten(p.download_all(npbmz.U))
+    f0 = p.flatten(p.download_all(npbmz.FORCING))
+    t = p.flatten(target)
+    J, gf, gu = p.adjoint(nsteps, target, checkpoint_every=10)
+    rng = np.random.default_rng(2025)
+    du = np.zeros((16, u0.size))
+    df = np.zeros((16, u0.size))
+    du[:8] = rng.standard_normal((8, u0.size)) * variable_scale(p, u0)
+    df[8:] = rng.standard_normal((8, u0.size)) * variable_scale(p, f0)
+    Jd, dJ, _ = oracle.tangent_objective(oracle.KIND_SP, g.nx, g.ny, g.nz, g.nbr, p.dt, g.gx, g.gy, g.gz, g.x_zones,
+                                         g.y_zones, u0, f0, t, nsteps, du0=du, dforcing=df)
+    assert J == pytest.approx(Jd, rel=1e-10)
+    ad = du @ p.flatten(gu) + df @ p.flatten(gf)
+    rel = np.abs(ad - dJ) / np.abs(dJ)
+    print(f"SP adjoint vs dual numbers: worst {rel.max():.2e}")
+    assert rel.max() <= DUAL_REL, rel
 
 
 def test_sp_checkpoint_interval_does_not_change_the_gradient(sp_case):
