@@ -71,6 +71,17 @@ CLASSES = {
         "E": (500, 0.0002, 1.0, 64, 64, 4224, 3456, 92),
         "F": (500, 0.0001, 1.0, 128, 128, 12032, 8960, 250),
     },
+    # LU-MZ (src/LU/classes.jl): itmax, dt, ratio, 4x4 zones; omega 1.2 (src/LU/lu_data.jl)
+    "LU": {
+        "S": (50, 0.5, 1.0, 4, 4, 24, 24, 6),
+        "W": (300, 1.5e-3, 1.0, 4, 4, 64, 64, 8),
+        "A": (250, 2.0, 1.0, 4, 4, 128, 128, 16),
+        "B": (250, 2.0, 1.0, 4, 4, 304, 208, 17),
+        "C": (250, 2.0, 1.0, 4, 4, 480, 320, 28),
+        "D": (300, 1.0, 1.0, 4, 4, 1632, 1216, 34),
+        "E": (300, 0.5, 1.0, 4, 4, 4224, 3456, 92),
+        "F": (300, 0.2, 1.0, 4, 4, 12032, 8960, 250),
+    },
 }
 
 # The reference's fixed exact-solution coefficients (src/BT/set_constants.jl:47-51), row-major [5][13].

@@ -5,7 +5,8 @@ CPU (oracle/npbmz_oracle.cpp).  Only tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py use it, always as the checker.  The tangent
 library (oracle/npbmz_tangent.cpp) is the same BT and SP restatement with
 forward-mode dual numbers: the reference directional derivatives against
-which tests check the GPU adjoint.
+which tests check the GPU adjoint.  liblumz_oracle.so (oracle/lumz_oracle.cpp)
+restates LU-MZ's SSOR iteration; LuOracle wraps it.
 """
 import ctypes
 import os
@@ -17,17 +18,19 @@ import numpy as np
 _HERE = Path(__file__).resolve().parent
 _LIB_PATH = _HERE / "_build" / "libnpbmz_oracle.so"
 _TAN_PATH = _HERE / "_build" / "libnpbmz_tangent.so"
+_LU_PATH = _HERE / "_build" / "liblumz_oracle.so"
 _lib = None
 _tan = None
+_lu = None
 TANGENT_NDIR = 16
 
 KIND_BT, KIND_SP = 0, 1
 
 
 def build(force=False):
-    srcs = [_HERE / "npbmz_oracle.cpp", _HERE / "npbmz_tangent.cpp"]
+    srcs = [_HERE / "npbmz_oracle.cpp", _HERE / "npbmz_tangent.cpp", _HERE / "lumz_oracle.cpp"]
     newest = max(p.stat().st_mtime for p in srcs)
-    if force or any(not p.exists() or p.stat().st_mtime < newest for p in (_LIB_PATH, _TAN_PATH)):
+    if force or any(not p.exists() or p.stat().st_mtime < newest for p in (_LIB_PATH, _TAN_PATH, _LU_PATH)):
         subprocess.run(["make", "-s", "-C", str(_HERE)], check=True)
     return _LIB_PATH
 
@@ -160,3 +163,82 @@ class Oracle:
         a = np.ascontiguousarray(arr, np.float64)
         assert a.shape == (5, int(self.nz[zone]), int(self.ny[zone]), int(self.nx[zone]))
         lib().oracle_set(self._h, which, zone, _dp(a))
+
+
+def lu_lib():
+    global _lu
+    if _lu is None:
+        build()
+        L = ctypes.CDLL(str(_LU_PATH))
+        ip = ctypes.POINTER(ctypes.c_int)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.lu_oracle_zone_setup.argtypes = [ctypes.c_int] * 5 + [ctypes.c_double, ip, ip, ip, ip]
+        L.lu_oracle_create.restype = ctypes.c_void_p
+        L.lu_oracle_create.argtypes = [ctypes.c_int, ip, ip, ip, ip, ctypes.c_double, ctypes.c_double, dp,
+                                       ctypes.c_int]
+        L.lu_oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.lu_oracle_iterate.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.lu_oracle_phase.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.lu_oracle_verify.argtypes = [ctypes.c_void_p] + [dp] * 6
+        L.lu_oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp]
+        L.lu_oracle_set.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp]
+        _lu = L
+    return _lu
+
+
+# LU-MZ phases of lu_oracle_phase
+LU_RHS, LU_SCALE, LU_LOWER, LU_UPPER, LU_UPDATE, LU_EXCH, LU_SSOR = range(7)
+
+
+def lu_zone_setup(gx, gy, gz, xz, yz, ratio=1.0):
+    n = xz * yz
+    nx, ny, nz = (np.zeros(n, np.int32) for _ in range(3))
+    nbr = np.zeros(4 * n, np.int32)
+    rc = lu_lib().lu_oracle_zone_setup(gx, gy, gz, xz, yz, ratio, _ip(nx), _ip(ny), _ip(nz), _ip(nbr))
+    assert rc == 0, rc
+    return nx, ny, nz, nbr
+
+
+class LuOracle:
+    """One LU-MZ problem held by the CPU oracle (setbv, setiv, erhs, rhs done)."""
+
+    def __init__(self, nx, ny, nz, nbr, dt, omega=1.2, ce=None, faces_npb=False):
+        self.nx, self.ny, self.nz, self.nbr = (np.ascontiguousarray(a, np.int32) for a in (nx, ny, nz, nbr))
+        self.nzones = len(self.nx)
+        self.ce = None if ce is None else np.ascontiguousarray(ce, np.float64).reshape(65)
+        self._h = lu_lib().lu_oracle_create(self.nzones, _ip(self.nx), _ip(self.ny), _ip(self.nz), _ip(self.nbr),
+                                            dt, omega, _dp(self.ce) if self.ce is not None else None,
+                                            int(faces_npb))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lu_lib().lu_oracle_destroy(self._h)
+            self._h = None
+
+    def iterate(self, niter):
+        lu_lib().lu_oracle_iterate(self._h, niter)
+
+    def phase(self, phase, zone=-1):
+        rc = lu_lib().lu_oracle_phase(self._h, phase, zone)
+        assert rc == 0, rc
+
+    def verify(self, per_zone=False):
+        xcr, xce, xci = np.zeros(5), np.zeros(5), np.zeros(1)
+        z = [np.zeros(5 * self.nzones), np.zeros(5 * self.nzones), np.zeros(self.nzones)] if per_zone else None
+        lu_lib().lu_oracle_verify(self._h, _dp(xcr), _dp(xce), _dp(xci), *((_dp(a) for a in z) if z else (None,) * 3))
+        if per_zone:
+            return xcr, xce, float(xci[0]), z[0].reshape(-1, 5), z[1].reshape(-1, 5), z[2]
+        return xcr, xce, float(xci[0])
+
+    def get(self, which, zone):
+        out = np.zeros((5, int(self.nz[zone]), int(self.ny[zone]), int(self.nx[zone])))
+        lu_lib().lu_oracle_get(self._h, which, zone, _dp(out))
+        return out
+
+    def get_all(self, which):
+        return np.concatenate([self.get(which, z).reshape(-1) for z in range(self.nzones)])
+
+    def set(self, which, zone, arr):
+        a = np.ascontiguousarray(arr, np.float64)
+        assert a.shape == (5, int(self.nz[zone]), int(self.ny[zone]), int(self.nx[zone]))
+        lu_lib().lu_oracle_set(self._h, which, zone, _dp(a))
