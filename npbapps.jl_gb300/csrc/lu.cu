@@ -1,0 +1,1564 @@
+// lu.cu -- LU-MZ's SSOR iteration (NPBApps.jl src/LU) on the GPU, and its
+// C ABI (include/npbmz_lu.h).  Built with -fmad=false: every FP64 statement
+// rounds as the reference's Julia does (no a*b+c contraction), so the result
+// is bit-for-bit the oracle's.
+//
+// Data in HBM: u, rsd, frct variable-major over the points of all zones,
+// field[m*NP + zone.off + ((k-1)*ny + (j-1))*nx + (i-1)] (1-based i, j, k as
+// in the reference; zone offsets rounded to 32 points).
+//
+// One iteration (src/LU/lu-node.jl:233-270 with ssor src/LU/ssor.jl:9-254):
+//   exch_qbc       k_lu_pack + k_lu_unpack (every face packed before any is
+//                  unpacked, as the reference's sends are)
+//   rsd *= dt      fused into the first touch of each point in k_lu_lower
+//   jacld + blts   k_lu_lower, one launch per hyperplane i+j+k = l
+//   jacu + buts    k_lu_upper, one launch per hyperplane, l descending
+//   update         k_lu_update
+//   rhs            k_lu_rhs<false>, one thread per point
+// blts / buts make point (i,j,k) depend on (i-1,j,k), (i,j-1,k), (i,j,k-1)
+// (resp. +1): within a hyperplane every point is independent, and every
+// zone's hyperplane l runs in the same launch.  The arithmetic of each point
+// is the reference's, statement for statement; only the order in which
+// independent points are visited changes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/npbmz_lu.h"
+
+namespace {
+
+constexpr double c1 = 1.40e+00, c2 = 0.40e+00, c3 = 1.00e-01, c4 = 1.00e+00, c5 = 1.40e+00;
+constexpr double dx1 = 0.75e+00, dx2 = dx1, dx3 = dx1, dx4 = dx1, dx5 = dx1;
+constexpr double dy1 = 0.75e+00, dy2 = dy1, dy3 = dy1, dy4 = dy1, dy5 = dy1;
+constexpr double dz1 = 1.00e+00, dz2 = dz1, dz3 = dz1, dz4 = dz1, dz5 = dz1;
+constexpr double dssp = 1.00e+00 / 4.0e+00;  // max(dx1, dy1, dz1) / 4 (src/LU/setcoeff.jl)
+constexpr int ii1 = 2, ji1 = 2, ki1 = 3;
+constexpr int TPB = 128;
+
+// the reference's ce table (src/LU/setcoeff.jl), row m, 13 columns
+const double ce_reference[5][13] = {
+    {2.0e0, 0.0e0, 0.0e0, 4.0e0, 5.0e0, 3.0e0, 0.5e0, 0.02e0, 0.01e0, 0.03e0, 0.5e0, 0.4e0, 0.3e0},
+    {1.0e0, 0.0e0, 0.0e0, 0.0e0, 1.0e0, 2.0e0, 3.0e0, 0.01e0, 0.03e0, 0.02e0, 0.4e0, 0.3e0, 0.5e0},
+    {2.0e0, 2.0e0, 0.0e0, 0.0e0, 0.0e0, 2.0e0, 3.0e0, 0.04e0, 0.03e0, 0.05e0, 0.3e0, 0.5e0, 0.4e0},
+    {2.0e0, 2.0e0, 0.0e0, 0.0e0, 0.0e0, 2.0e0, 3.0e0, 0.03e0, 0.05e0, 0.04e0, 0.2e0, 0.1e0, 0.3e0},
+    {5.0e0, 4.0e0, 3.0e0, 2.0e0, 0.1e0, 0.4e0, 0.3e0, 0.05e0, 0.04e0, 0.03e0, 0.1e0, 0.3e0, 0.2e0}};
+
+struct CeTable {
+  double c[5][13];
+};
+
+// setcoeff of one zone (src/LU/setcoeff.jl) and its place in HBM
+struct LuZone {
+  long long off;
+  int nx, ny, nz, np;
+  double dxi, deta, dzeta, tx1, tx2, tx3, ty1, ty2, ty3, tz1, tz2, tz3;
+  int ii2, ji2, ki2;
+};
+
+struct LuDev {
+  double* u;
+  double* rsd;
+  double* frct;
+  long long NP;
+  const LuZone* zones;
+  double dt, omega;
+};
+
+struct LuWork {  // one block of TPB consecutive points of one zone
+  int zone, first;
+};
+
+__host__ __device__ inline long long pidx(const LuZone& Z, int i, int j, int k) {
+  return Z.off + ((long long)(k - 1) * Z.ny + (j - 1)) * Z.nx + (i - 1);
+}
+
+// ---- exact solution (src/LU/exact.jl) ---------------------------------------
+__device__ inline void exact_point(const CeTable& ce, int i, int j, int k, int nx0, int ny0, int nz0, double out[5]) {
+  const double xi = (double)(i - 1) / (nx0 - 1);
+  const double eta = (double)(j - 1) / (ny0 - 1);
+  const double zeta = (double)(k - 1) / (nz0 - 1);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    const double* c = ce.c[m];
+    out[m] = c[0] + (c[1] + (c[4] + (c[7] + c[10] * xi) * xi) * xi) * xi +
+             (c[2] + (c[5] + (c[8] + c[11] * eta) * eta) * eta) * eta +
+             (c[3] + (c[6] + (c[9] + c[12] * zeta) * zeta) * zeta) * zeta;
+  }
+}
+
+// ---- rhs / erhs point operator (src/LU/rhs.jl, src/LU/erhs.jl) -------------
+// o: the point's output, holding -frct (rhs) or 0 (erhs) on entry.  ERHS
+// selects erhs's z second difference order (g(k+1) first) and its viscous
+// association ((o + A) + B instead of o + (A + B)).
+template <bool ERHS>
+__device__ inline double visc_up(double o, double a, double b) {
+  return ERHS ? (o + a) + b : o + (a + b);
+}
+
+template <bool ERHS>
+__device__ void flux_point(const double* __restrict__ g, long long NP, const LuZone& Z, int i, int j, int k,
+                           double o[5]) {
+  const int nx = Z.nx, ny = Z.ny, nz = Z.nz;
+  auto G = [&](int m, int ii, int jj, int kk) -> double { return g[m * NP + pidx(Z, ii, jj, kk)]; };
+  const double tx1 = Z.tx1, tx2 = Z.tx2, tx3 = Z.tx3, ty1 = Z.ty1, ty2 = Z.ty2, ty3 = Z.ty3, tz1 = Z.tz1,
+               tz2 = Z.tz2, tz3 = Z.tz3;
+  // ---------------- xi ----------------
+  {
+    double fp[5], fm[5];
+    auto conv = [&](int ii, double f[5]) {
+      const double g1 = G(0, ii, j, k), g2 = G(1, ii, j, k), g3 = G(2, ii, j, k), g4 = G(3, ii, j, k),
+                   g5 = G(4, ii, j, k);
+      f[0] = g2;
+      const double u21 = g2 / g1;
+      const double q = 0.50e+00 * (g2 * g2 + g3 * g3 + g4 * g4) / g1;
+      f[1] = g2 * u21 + c2 * (g5 - q);
+      f[2] = g3 * u21;
+      f[3] = g4 * u21;
+      f[4] = (c1 * g5 - c2 * q) * u21;
+    };
+    conv(i + 1, fp);
+    conv(i - 1, fm);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) o[m] = o[m] - tx2 * (fp[m] - fm[m]);
+    auto visc = [&](int ii, double f[5]) {
+      double tmp = 1.0e+00 / G(0, ii, j, k);
+      const double u21i = tmp * G(1, ii, j, k), u31i = tmp * G(2, ii, j, k), u41i = tmp * G(3, ii, j, k),
+                   u51i = tmp * G(4, ii, j, k);
+      tmp = 1.0e+00 / G(0, ii - 1, j, k);
+      const double u21im1 = tmp * G(1, ii - 1, j, k), u31im1 = tmp * G(2, ii - 1, j, k),
+                   u41im1 = tmp * G(3, ii - 1, j, k), u51im1 = tmp * G(4, ii - 1, j, k);
+      f[1] = (4.0e+00 / 3.0e+00) * tx3 * (u21i - u21im1);
+      f[2] = tx3 * (u31i - u31im1);
+      f[3] = tx3 * (u41i - u41im1);
+      f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * tx3 *
+                 ((u21i * u21i + u31i * u31i + u41i * u41i) - (u21im1 * u21im1 + u31im1 * u31im1 + u41im1 * u41im1)) +
+             (1.0e+00 / 6.0e+00) * tx3 * (u21i * u21i - u21im1 * u21im1) + c1 * c5 * tx3 * (u51i - u51im1);
+    };
+    visc(i + 1, fp);
+    visc(i, fm);
+    o[0] = o[0] + dx1 * tx1 * (G(0, i - 1, j, k) - 2.0e+00 * G(0, i, j, k) + G(0, i + 1, j, k));
+    const double dxm[5] = {dx1, dx2, dx3, dx4, dx5};
+#pragma unroll
+    for (int m = 1; m < 5; ++m)
+      o[m] = visc_up<ERHS>(o[m], tx3 * c3 * c4 * (fp[m] - fm[m]),
+                           dxm[m] * tx1 * (G(m, i - 1, j, k) - 2.0e+00 * G(m, i, j, k) + G(m, i + 1, j, k)));
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (i == 2) o[m] = o[m] - dssp * (+5.0e+00 * G(m, 2, j, k) - 4.0e+00 * G(m, 3, j, k) + G(m, 4, j, k));
+      if (i == 3)
+        o[m] = o[m] - dssp * (-4.0e+00 * G(m, 2, j, k) + 6.0e+00 * G(m, 3, j, k) - 4.0e+00 * G(m, 4, j, k) +
+                              G(m, 5, j, k));
+      if (i >= 4 && i <= nx - 3)
+        o[m] = o[m] - dssp * (G(m, i - 2, j, k) - 4.0e+00 * G(m, i - 1, j, k) + 6.0e+00 * G(m, i, j, k) -
+                              4.0e+00 * G(m, i + 1, j, k) + G(m, i + 2, j, k));
+      if (i == nx - 2)
+        o[m] = o[m] - dssp * (G(m, nx - 4, j, k) - 4.0e+00 * G(m, nx - 3, j, k) + 6.0e+00 * G(m, nx - 2, j, k) -
+                              4.0e+00 * G(m, nx - 1, j, k));
+      if (i == nx - 1)
+        o[m] = o[m] - dssp * (G(m, nx - 3, j, k) - 4.0e+00 * G(m, nx - 2, j, k) + 5.0e+00 * G(m, nx - 1, j, k));
+    }
+  }
+  // ---------------- eta ----------------
+  {
+    double fp[5], fm[5];
+    auto conv = [&](int jj, double f[5]) {
+      const double g1 = G(0, i, jj, k), g2 = G(1, i, jj, k), g3 = G(2, i, jj, k), g4 = G(3, i, jj, k),
+                   g5 = G(4, i, jj, k);
+      f[0] = g3;
+      const double u31 = g3 / g1;
+      const double q = 0.50e+00 * (g2 * g2 + g3 * g3 + g4 * g4) / g1;
+      f[1] = g2 * u31;
+      f[2] = g3 * u31 + c2 * (g5 - q);
+      f[3] = g4 * u31;
+      f[4] = (c1 * g5 - c2 * q) * u31;
+    };
+    conv(j + 1, fp);
+    conv(j - 1, fm);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) o[m] = o[m] - ty2 * (fp[m] - fm[m]);
+    auto visc = [&](int jj, double f[5]) {
+      double tmp = 1.0e+00 / G(0, i, jj, k);
+      const double u21j = tmp * G(1, i, jj, k), u31j = tmp * G(2, i, jj, k), u41j = tmp * G(3, i, jj, k),
+                   u51j = tmp * G(4, i, jj, k);
+      tmp = 1.0e+00 / G(0, i, jj - 1, k);
+      const double u21jm1 = tmp * G(1, i, jj - 1, k), u31jm1 = tmp * G(2, i, jj - 1, k),
+                   u41jm1 = tmp * G(3, i, jj - 1, k), u51jm1 = tmp * G(4, i, jj - 1, k);
+      f[1] = ty3 * (u21j - u21jm1);
+      f[2] = (4.0e+00 / 3.0e+00) * ty3 * (u31j - u31jm1);
+      f[3] = ty3 * (u41j - u41jm1);
+      f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * ty3 *
+                 ((u21j * u21j + u31j * u31j + u41j * u41j) - (u21jm1 * u21jm1 + u31jm1 * u31jm1 + u41jm1 * u41jm1)) +
+             (1.0e+00 / 6.0e+00) * ty3 * (u31j * u31j - u31jm1 * u31jm1) + c1 * c5 * ty3 * (u51j - u51jm1);
+    };
+    visc(j + 1, fp);
+    visc(j, fm);
+    o[0] = o[0] + dy1 * ty1 * (G(0, i, j - 1, k) - 2.0e+00 * G(0, i, j, k) + G(0, i, j + 1, k));
+    const double dym[5] = {dy1, dy2, dy3, dy4, dy5};
+#pragma unroll
+    for (int m = 1; m < 5; ++m)
+      o[m] = visc_up<ERHS>(o[m], ty3 * c3 * c4 * (fp[m] - fm[m]),
+                           dym[m] * ty1 * (G(m, i, j - 1, k) - 2.0e+00 * G(m, i, j, k) + G(m, i, j + 1, k)));
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (j == 2) o[m] = o[m] - dssp * (+5.0e+00 * G(m, i, 2, k) - 4.0e+00 * G(m, i, 3, k) + G(m, i, 4, k));
+      if (j == 3)
+        o[m] = o[m] - dssp * (-4.0e+00 * G(m, i, 2, k) + 6.0e+00 * G(m, i, 3, k) - 4.0e+00 * G(m, i, 4, k) +
+                              G(m, i, 5, k));
+      if (j >= 4 && j <= ny - 3)
+        o[m] = o[m] - dssp * (G(m, i, j - 2, k) - 4.0e+00 * G(m, i, j - 1, k) + 6.0e+00 * G(m, i, j, k) -
+                              4.0e+00 * G(m, i, j + 1, k) + G(m, i, j + 2, k));
+      if (j == ny - 2)
+        o[m] = o[m] - dssp * (G(m, i, ny - 4, k) - 4.0e+00 * G(m, i, ny - 3, k) + 6.0e+00 * G(m, i, ny - 2, k) -
+                              4.0e+00 * G(m, i, ny - 1, k));
+      if (j == ny - 1)
+        o[m] = o[m] - dssp * (G(m, i, ny - 3, k) - 4.0e+00 * G(m, i, ny - 2, k) + 5.0e+00 * G(m, i, ny - 1, k));
+    }
+  }
+  // ---------------- zeta ----------------
+  {
+    double fp[5], fm[5];
+    auto conv = [&](int kk, double f[5]) {
+      const double g1 = G(0, i, j, kk), g2 = G(1, i, j, kk), g3 = G(2, i, j, kk), g4 = G(3, i, j, kk),
+                   g5 = G(4, i, j, kk);
+      f[0] = g4;
+      const double u41 = g4 / g1;
+      const double q = 0.50e+00 * (g2 * g2 + g3 * g3 + g4 * g4) / g1;
+      f[1] = g2 * u41;
+      f[2] = g3 * u41;
+      f[3] = g4 * u41 + c2 * (g5 - q);
+      f[4] = (c1 * g5 - c2 * q) * u41;
+    };
+    conv(k + 1, fp);
+    conv(k - 1, fm);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) o[m] = o[m] - tz2 * (fp[m] - fm[m]);
+    auto visc = [&](int kk, double f[5]) {
+      double tmp = 1.0e+00 / G(0, i, j, kk);
+      const double u21k = tmp * G(1, i, j, kk), u31k = tmp * G(2, i, j, kk), u41k = tmp * G(3, i, j, kk),
+                   u51k = tmp * G(4, i, j, kk);
+      tmp = 1.0e+00 / G(0, i, j, kk - 1);
+      const double u21km1 = tmp * G(1, i, j, kk - 1), u31km1 = tmp * G(2, i, j, kk - 1),
+                   u41km1 = tmp * G(3, i, j, kk - 1), u51km1 = tmp * G(4, i, j, kk - 1);
+      f[1] = tz3 * (u21k - u21km1);
+      f[2] = tz3 * (u31k - u31km1);
+      f[3] = (4.0e+00 / 3.0e+00) * tz3 * (u41k - u41km1);
+      f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * tz3 *
+                 ((u21k * u21k + u31k * u31k + u41k * u41k) - (u21km1 * u21km1 + u31km1 * u31km1 + u41km1 * u41km1)) +
+             (1.0e+00 / 6.0e+00) * tz3 * (u41k * u41k - u41km1 * u41km1) + c1 * c5 * tz3 * (u51k - u51km1);
+    };
+    visc(k + 1, fp);
+    visc(k, fm);
+    auto sd = [&](int m) {
+      return ERHS ? (G(m, i, j, k + 1) - 2.0e+00 * G(m, i, j, k) + G(m, i, j, k - 1))
+                  : (G(m, i, j, k - 1) - 2.0e+00 * G(m, i, j, k) + G(m, i, j, k + 1));
+    };
+    o[0] = o[0] + dz1 * tz1 * sd(0);
+    const double dzm[5] = {dz1, dz2, dz3, dz4, dz5};
+#pragma unroll
+    for (int m = 1; m < 5; ++m) o[m] = visc_up<ERHS>(o[m], tz3 * c3 * c4 * (fp[m] - fm[m]), dzm[m] * tz1 * sd(m));
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (k == 2) o[m] = o[m] - dssp * (+5.0e+00 * G(m, i, j, 2) - 4.0e+00 * G(m, i, j, 3) + G(m, i, j, 4));
+      if (k == 3)
+        o[m] = o[m] - dssp * (-4.0e+00 * G(m, i, j, 2) + 6.0e+00 * G(m, i, j, 3) - 4.0e+00 * G(m, i, j, 4) +
+                              G(m, i, j, 5));
+      if (k >= 4 && k <= nz - 3)
+        o[m] = o[m] - dssp * (G(m, i, j, k - 2) - 4.0e+00 * G(m, i, j, k - 1) + 6.0e+00 * G(m, i, j, k) -
+                              4.0e+00 * G(m, i, j, k + 1) + G(m, i, j, k + 2));
+      if (k == nz - 2)
+        o[m] = o[m] - dssp * (G(m, i, j, nz - 4) - 4.0e+00 * G(m, i, j, nz - 3) + 6.0e+00 * G(m, i, j, nz - 2) -
+                              4.0e+00 * G(m, i, j, nz - 1));
+      if (k == nz - 1)
+        o[m] = o[m] - dssp * (G(m, i, j, nz - 3) - 4.0e+00 * G(m, i, j, nz - 2) + 5.0e+00 * G(m, i, j, nz - 1));
+    }
+  }
+}
+
+__device__ inline bool decode(const LuZone& Z, int q, int& i, int& j, int& k) {
+  if (q >= Z.np) return false;
+  i = q % Z.nx + 1;
+  j = (q / Z.nx) % Z.ny + 1;
+  k = q / (Z.nx * Z.ny) + 1;
+  return true;
+}
+
+__device__ inline bool interior(const LuZone& Z, int i, int j, int k) {
+  return i >= 2 && i <= Z.nx - 1 && j >= 2 && j <= Z.ny - 1 && k >= 2 && k <= Z.nz - 1;
+}
+
+// rhs (ERHS = false: g = u, out = rsd starting at -frct) or erhs's flux part
+// (ERHS = true: g = the exact polynomial in rsd, out = frct starting at 0)
+template <bool ERHS>
+__global__ void __launch_bounds__(TPB) k_lu_rhs(LuDev D, const LuWork* __restrict__ work, const double* g,
+                                                double* out) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  int i, j, k;
+  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
+  const long long p = pidx(Z, i, j, k);
+  double o[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) o[m] = ERHS ? 0.0 : -D.frct[m * D.NP + p];
+  if (interior(Z, i, j, k)) flux_point<ERHS>(g, D.NP, Z, i, j, k, o);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) out[m * D.NP + p] = o[m];
+}
+
+// setbv + setiv (src/LU/setbv.jl, src/LU/setiv.jl); every face point of
+// setbv gets exact() of its own (i, j, k), whichever face writes it last
+__global__ void __launch_bounds__(TPB) k_lu_init(LuDev D, const LuWork* __restrict__ work, CeTable ce) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  int i, j, k;
+  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
+  const int nx = Z.nx, ny = Z.ny, nz = Z.nz;
+  const long long p = pidx(Z, i, j, k);
+  double out[5];
+  if (!interior(Z, i, j, k)) {
+    exact_point(ce, i, j, k, nx, ny, nz, out);
+  } else {
+    const double zeta = (double)(k - 1) / (nz - 1);
+    const double eta = (double)(j - 1) / (ny - 1);
+    const double xi = (double)(i - 1) / (nx - 1);
+    double a1[5], a2[5], b1[5], b2[5], g1[5], g2[5];
+    exact_point(ce, 1, j, k, nx, ny, nz, a1);
+    exact_point(ce, nx, j, k, nx, ny, nz, a2);
+    exact_point(ce, i, 1, k, nx, ny, nz, b1);
+    exact_point(ce, i, ny, k, nx, ny, nz, b2);
+    exact_point(ce, i, j, 1, nx, ny, nz, g1);
+    exact_point(ce, i, j, nz, nx, ny, nz, g2);
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double pxi = (1.0e+00 - xi) * a1[m] + xi * a2[m];
+      const double peta = (1.0e+00 - eta) * b1[m] + eta * b2[m];
+      const double pzeta = (1.0e+00 - zeta) * g1[m] + zeta * g2[m];
+      out[m] = pxi + peta + pzeta - pxi * peta - peta * pzeta - pzeta * pxi + pxi * peta * pzeta;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 5; ++m) D.u[m * D.NP + p] = out[m];
+}
+
+// erhs's first part: rsd = the exact polynomial (non-Horner, src/LU/erhs.jl:24-47)
+__global__ void __launch_bounds__(TPB) k_lu_poly(LuDev D, const LuWork* __restrict__ work, CeTable ce) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  int i, j, k;
+  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
+  const long long p = pidx(Z, i, j, k);
+  const double zeta = (double)(k - 1) / (Z.nz - 1);
+  const double eta = (double)(j - 1) / (Z.ny - 1);
+  const double xi = (double)(i - 1) / (Z.nx - 1);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    const double* c = ce.c[m];
+    D.rsd[m * D.NP + p] = c[0] + c[1] * xi + c[2] * eta + c[3] * zeta + c[4] * xi * xi + c[5] * eta * eta +
+                          c[6] * zeta * zeta + c[7] * xi * xi * xi + c[8] * eta * eta * eta +
+                          c[9] * zeta * zeta * zeta + c[10] * xi * xi * xi * xi + c[11] * eta * eta * eta * eta +
+                          c[12] * zeta * zeta * zeta * zeta;
+  }
+}
+
+// rsd *= dt (SCALE) or u += tmp * rsd (UPDATE) on the interior
+template <bool UPDATE>
+__global__ void __launch_bounds__(TPB) k_lu_pointwise(LuDev D, const LuWork* __restrict__ work, double tmp) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  int i, j, k;
+  if (!decode(Z, w.first + threadIdx.x, i, j, k) || !interior(Z, i, j, k)) return;
+  const long long p = pidx(Z, i, j, k);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    if (UPDATE)
+      D.u[m * D.NP + p] = D.u[m * D.NP + p] + tmp * D.rsd[m * D.NP + p];
+    else
+      D.rsd[m * D.NP + p] = D.dt * D.rsd[m * D.NP + p];
+  }
+}
+
+// ---- Jacobian blocks of jacld / jacu (src/LU/jacld.jl, src/LU/jacu.jl) -----
+struct JC {
+  double dt, tx1, tx2, ty1, ty2, tz1, tz2;
+};
+constexpr double r43 = (4.0e+00 / 3.0e+00);
+constexpr double c1345 = c1 * c3 * c4 * c5;
+constexpr double c34 = c3 * c4;
+
+// the diagonal block (identical in jacld and jacu) at the point's own state
+__device__ inline void jac_d(const JC& J, double u1, double u2, double u3, double u4, double u5, double d[5][5]) {
+  const double dt = J.dt, tx1 = J.tx1, ty1 = J.ty1, tz1 = J.tz1;
+  const double tmp1 = 1.0e+00 / u1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
+  d[0][0] = 1.0e+00 + dt * 2.0e+00 * (tx1 * dx1 + ty1 * dy1 + tz1 * dz1);
+  d[0][1] = 0.0; d[0][2] = 0.0; d[0][3] = 0.0; d[0][4] = 0.0;
+  d[1][0] = dt * 2.0e+00 * (tx1 * (-r43 * c34 * tmp2 * u2) + ty1 * (-c34 * tmp2 * u2) + tz1 * (-c34 * tmp2 * u2));
+  d[1][1] = 1.0e+00 + dt * 2.0e+00 * (tx1 * r43 * c34 * tmp1 + ty1 * c34 * tmp1 + tz1 * c34 * tmp1) +
+            dt * 2.0e+00 * (tx1 * dx2 + ty1 * dy2 + tz1 * dz2);
+  d[1][2] = 0.0; d[1][3] = 0.0; d[1][4] = 0.0;
+  d[2][0] = dt * 2.0e+00 * (tx1 * (-c34 * tmp2 * u3) + ty1 * (-r43 * c34 * tmp2 * u3) + tz1 * (-c34 * tmp2 * u3));
+  d[2][1] = 0.0;
+  d[2][2] = 1.0e+00 + dt * 2.0e+00 * (tx1 * c34 * tmp1 + ty1 * r43 * c34 * tmp1 + tz1 * c34 * tmp1) +
+            dt * 2.0e+00 * (tx1 * dx3 + ty1 * dy3 + tz1 * dz3);
+  d[2][3] = 0.0; d[2][4] = 0.0;
+  d[3][0] = dt * 2.0e+00 * (tx1 * (-c34 * tmp2 * u4) + ty1 * (-c34 * tmp2 * u4) + tz1 * (-r43 * c34 * tmp2 * u4));
+  d[3][1] = 0.0; d[3][2] = 0.0;
+  d[3][3] = 1.0e+00 + dt * 2.0e+00 * (tx1 * c34 * tmp1 + ty1 * c34 * tmp1 + tz1 * r43 * c34 * tmp1) +
+            dt * 2.0e+00 * (tx1 * dx4 + ty1 * dy4 + tz1 * dz4);
+  d[3][4] = 0.0;
+  d[4][0] = dt * 2.0e+00 *
+            (tx1 * (-(r43 * c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
+                    (c34 - c1345) * tmp3 * (u4 * u4) - (c1345)*tmp2 * u5) +
+             ty1 * (-(c34 - c1345) * tmp3 * (u2 * u2) - (r43 * c34 - c1345) * tmp3 * (u3 * u3) -
+                    (c34 - c1345) * tmp3 * (u4 * u4) - (c1345)*tmp2 * u5) +
+             tz1 * (-(c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
+                    (r43 * c34 - c1345) * tmp3 * (u4 * u4) - (c1345)*tmp2 * u5));
+  d[4][1] = dt * 2.0e+00 *
+            (tx1 * (r43 * c34 - c1345) * tmp2 * u2 + ty1 * (c34 - c1345) * tmp2 * u2 + tz1 * (c34 - c1345) * tmp2 * u2);
+  d[4][2] = dt * 2.0e+00 *
+            (tx1 * (c34 - c1345) * tmp2 * u3 + ty1 * (r43 * c34 - c1345) * tmp2 * u3 + tz1 * (c34 - c1345) * tmp2 * u3);
+  d[4][3] = dt * 2.0e+00 *
+            (tx1 * (c34 - c1345) * tmp2 * u4 + ty1 * (c34 - c1345) * tmp2 * u4 + tz1 * (r43 * c34 - c1345) * tmp2 * u4);
+  d[4][4] = 1.0e+00 + dt * 2.0e+00 * (tx1 * c1345 * tmp1 + ty1 * c1345 * tmp1 + tz1 * c1345 * tmp1) +
+            dt * 2.0e+00 * (tx1 * dx5 + ty1 * dy5 + tz1 * dz5);
+}
+
+// Off-diagonal block of direction DIR (0 x, 1 y, 2 z) from the neighbour's
+// state; SG = -1: jacld's (the neighbour at -1), SG = +1: jacu's (at +1).
+// The entries are the reference's statements with dt*t?2 negated for jacld.
+template <int DIR, int SG>
+__device__ inline void jac_off(const JC& J, double u1, double u2, double u3, double u4, double u5, double a[5][5]) {
+  const double dt = J.dt;
+  const double tmp1 = 1.0e+00 / u1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
+  if (DIR == 2) {
+    const double tz1 = J.tz1, tz2 = J.tz2;
+    if (SG < 0) {
+      a[0][0] = -dt * tz1 * dz1;
+      a[0][1] = 0.0;
+      a[0][2] = 0.0;
+      a[0][3] = -dt * tz2;
+      a[0][4] = 0.0;
+      a[1][0] = -dt * tz2 * (-(u2 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u2);
+      a[1][1] = -dt * tz2 * (u4 * tmp1) - dt * tz1 * c34 * tmp1 - dt * tz1 * dz2;
+      a[1][2] = 0.0;
+      a[1][3] = -dt * tz2 * (u2 * tmp1);
+      a[1][4] = 0.0;
+      a[2][0] = -dt * tz2 * (-(u3 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u3);
+      a[2][1] = 0.0;
+      a[2][2] = -dt * tz2 * (u4 * tmp1) - dt * tz1 * (c34 * tmp1) - dt * tz1 * dz3;
+      a[2][3] = -dt * tz2 * (u3 * tmp1);
+      a[2][4] = 0.0;
+      a[3][0] = -dt * tz2 * (-((u4 * tmp1) * (u4 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
+                dt * tz1 * (-r43 * c34 * tmp2 * u4);
+      a[3][1] = -dt * tz2 * (-c2 * (u2 * tmp1));
+      a[3][2] = -dt * tz2 * (-c2 * (u3 * tmp1));
+      a[3][3] = -dt * tz2 * (2.0e+00 - c2) * (u4 * tmp1) - dt * tz1 * (r43 * c34 * tmp1) - dt * tz1 * dz4;
+      a[3][4] = -dt * tz2 * c2;
+      a[4][0] = -dt * tz2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u4 * tmp1)) -
+                dt * tz1 *
+                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
+                     (r43 * c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
+      a[4][1] = -dt * tz2 * (-c2 * (u2 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u2;
+      a[4][2] = -dt * tz2 * (-c2 * (u3 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u3;
+      a[4][3] = -dt * tz2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + 3.0e+00 * u4 * u4) * tmp2)) -
+                dt * tz1 * (r43 * c34 - c1345) * tmp2 * u4;
+      a[4][4] = -dt * tz2 * (c1 * (u4 * tmp1)) - dt * tz1 * c1345 * tmp1 - dt * tz1 * dz5;
+    } else {
+      a[0][0] = -dt * tz1 * dz1;
+      a[0][1] = 0.0;
+      a[0][2] = 0.0;
+      a[0][3] = dt * tz2;
+      a[0][4] = 0.0;
+      a[1][0] = dt * tz2 * (-(u2 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u2);
+      a[1][1] = dt * tz2 * (u4 * tmp1) - dt * tz1 * c34 * tmp1 - dt * tz1 * dz2;
+      a[1][2] = 0.0;
+      a[1][3] = dt * tz2 * (u2 * tmp1);
+      a[1][4] = 0.0;
+      a[2][0] = dt * tz2 * (-(u3 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u3);
+      a[2][1] = 0.0;
+      a[2][2] = dt * tz2 * (u4 * tmp1) - dt * tz1 * (c34 * tmp1) - dt * tz1 * dz3;
+      a[2][3] = dt * tz2 * (u3 * tmp1);
+      a[2][4] = 0.0;
+      a[3][0] = dt * tz2 * (-((u4 * tmp1) * (u4 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
+                dt * tz1 * (-r43 * c34 * tmp2 * u4);
+      a[3][1] = dt * tz2 * (-c2 * (u2 * tmp1));
+      a[3][2] = dt * tz2 * (-c2 * (u3 * tmp1));
+      a[3][3] = dt * tz2 * (2.0e+00 - c2) * (u4 * tmp1) - dt * tz1 * (r43 * c34 * tmp1) - dt * tz1 * dz4;
+      a[3][4] = dt * tz2 * c2;
+      a[4][0] = dt * tz2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u4 * tmp1)) -
+                dt * tz1 *
+                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
+                     (r43 * c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
+      a[4][1] = dt * tz2 * (-c2 * (u2 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u2;
+      a[4][2] = dt * tz2 * (-c2 * (u3 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u3;
+      a[4][3] = dt * tz2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + 3.0e+00 * u4 * u4) * tmp2)) -
+                dt * tz1 * (r43 * c34 - c1345) * tmp2 * u4;
+      a[4][4] = dt * tz2 * (c1 * (u4 * tmp1)) - dt * tz1 * c1345 * tmp1 - dt * tz1 * dz5;
+    }
+  } else if (DIR == 1) {
+    const double ty1 = J.ty1, ty2 = J.ty2;
+    if (SG < 0) {
+      a[0][0] = -dt * ty1 * dy1;
+      a[0][1] = 0.0;
+      a[0][2] = -dt * ty2;
+      a[0][3] = 0.0;
+      a[0][4] = 0.0;
+      a[1][0] = -dt * ty2 * (-(u2 * u3) * tmp2) - dt * ty1 * (-c34 * tmp2 * u2);
+      a[1][1] = -dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy2;
+      a[1][2] = -dt * ty2 * (u2 * tmp1);
+      a[1][3] = 0.0;
+      a[1][4] = 0.0;
+      a[2][0] = -dt * ty2 * (-((u3 * tmp1) * (u3 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
+                dt * ty1 * (-r43 * c34 * tmp2 * u3);
+      a[2][1] = -dt * ty2 * (-c2 * (u2 * tmp1));
+      a[2][2] = -dt * ty2 * ((2.0e+00 - c2) * (u3 * tmp1)) - dt * ty1 * (r43 * c34 * tmp1) - dt * ty1 * dy3;
+      a[2][3] = -dt * ty2 * (-c2 * (u4 * tmp1));
+      a[2][4] = -dt * ty2 * c2;
+      a[3][0] = -dt * ty2 * (-(u3 * u4) * tmp2) - dt * ty1 * (-c34 * tmp2 * u4);
+      a[3][1] = 0.0;
+      a[3][2] = -dt * ty2 * (u4 * tmp1);
+      a[3][3] = -dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy4;
+      a[3][4] = 0.0;
+      a[4][0] = -dt * ty2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u3 * tmp1)) -
+                dt * ty1 *
+                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (r43 * c34 - c1345) * tmp3 * (u3 * u3) -
+                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
+      a[4][1] = -dt * ty2 * (-c2 * (u2 * u3) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u2;
+      a[4][2] = -dt * ty2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + 3.0e+00 * u3 * u3 + u4 * u4) * tmp2)) -
+                dt * ty1 * (r43 * c34 - c1345) * tmp2 * u3;
+      a[4][3] = -dt * ty2 * (-c2 * (u3 * u4) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u4;
+      a[4][4] = -dt * ty2 * (c1 * (u3 * tmp1)) - dt * ty1 * c1345 * tmp1 - dt * ty1 * dy5;
+    } else {
+      a[0][0] = -dt * ty1 * dy1;
+      a[0][1] = 0.0;
+      a[0][2] = dt * ty2;
+      a[0][3] = 0.0;
+      a[0][4] = 0.0;
+      a[1][0] = dt * ty2 * (-(u2 * u3) * tmp2) - dt * ty1 * (-c34 * tmp2 * u2);
+      a[1][1] = dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy2;
+      a[1][2] = dt * ty2 * (u2 * tmp1);
+      a[1][3] = 0.0;
+      a[1][4] = 0.0;
+      a[2][0] = dt * ty2 * (-((u3 * tmp1) * (u3 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
+                dt * ty1 * (-r43 * c34 * tmp2 * u3);
+      a[2][1] = dt * ty2 * (-c2 * (u2 * tmp1));
+      a[2][2] = dt * ty2 * ((2.0e+00 - c2) * (u3 * tmp1)) - dt * ty1 * (r43 * c34 * tmp1) - dt * ty1 * dy3;
+      a[2][3] = dt * ty2 * (-c2 * (u4 * tmp1));
+      a[2][4] = dt * ty2 * c2;
+      a[3][0] = dt * ty2 * (-(u3 * u4) * tmp2) - dt * ty1 * (-c34 * tmp2 * u4);
+      a[3][1] = 0.0;
+      a[3][2] = dt * ty2 * (u4 * tmp1);
+      a[3][3] = dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy4;
+      a[3][4] = 0.0;
+      a[4][0] = dt * ty2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u3 * tmp1)) -
+                dt * ty1 *
+                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (r43 * c34 - c1345) * tmp3 * (u3 * u3) -
+                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
+      a[4][1] = dt * ty2 * (-c2 * (u2 * u3) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u2;
+      a[4][2] = dt * ty2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + 3.0e+00 * u3 * u3 + u4 * u4) * tmp2)) -
+                dt * ty1 * (r43 * c34 - c1345) * tmp2 * u3;
+      a[4][3] = dt * ty2 * (-c2 * (u3 * u4) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u4;
+      a[4][4] = dt * ty2 * (c1 * (u3 * tmp1)) - dt * ty1 * c1345 * tmp1 - dt * ty1 * dy5;
+    }
+  } else {
+    const double tx1 = J.tx1, tx2 = J.tx2;
+    if (SG < 0) {
+      a[0][0] = -dt * tx1 * dx1;
+      a[0][1] = -dt * tx2;
+      a[0][2] = 0.0;
+      a[0][3] = 0.0;
+      a[0][4] = 0.0;
+      a[1][0] = -dt * tx2 * (-((u2 * tmp1) * (u2 * tmp1)) + c2 * 0.50e+00 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2) -
+                dt * tx1 * (-r43 * c34 * tmp2 * u2);
+      a[1][1] = -dt * tx2 * ((2.0e+00 - c2) * (u2 * tmp1)) - dt * tx1 * (r43 * c34 * tmp1) - dt * tx1 * dx2;
+      a[1][2] = -dt * tx2 * (-c2 * (u3 * tmp1));
+      a[1][3] = -dt * tx2 * (-c2 * (u4 * tmp1));
+      a[1][4] = -dt * tx2 * c2;
+      a[2][0] = -dt * tx2 * (-(u2 * u3) * tmp2) - dt * tx1 * (-c34 * tmp2 * u3);
+      a[2][1] = -dt * tx2 * (u3 * tmp1);
+      a[2][2] = -dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx3;
+      a[2][3] = 0.0;
+      a[2][4] = 0.0;
+      a[3][0] = -dt * tx2 * (-(u2 * u4) * tmp2) - dt * tx1 * (-c34 * tmp2 * u4);
+      a[3][1] = -dt * tx2 * (u4 * tmp1);
+      a[3][2] = 0.0;
+      a[3][3] = -dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx4;
+      a[3][4] = 0.0;
+      a[4][0] = -dt * tx2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u2 * tmp1)) -
+                dt * tx1 *
+                    (-(r43 * c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
+                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
+      a[4][1] = -dt * tx2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((3.0e+00 * u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
+                dt * tx1 * (r43 * c34 - c1345) * tmp2 * u2;
+      a[4][2] = -dt * tx2 * (-c2 * (u3 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u3;
+      a[4][3] = -dt * tx2 * (-c2 * (u4 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u4;
+      a[4][4] = -dt * tx2 * (c1 * (u2 * tmp1)) - dt * tx1 * c1345 * tmp1 - dt * tx1 * dx5;
+    } else {
+      a[0][0] = -dt * tx1 * dx1;
+      a[0][1] = dt * tx2;
+      a[0][2] = 0.0;
+      a[0][3] = 0.0;
+      a[0][4] = 0.0;
+      a[1][0] = dt * tx2 * (-((u2 * tmp1) * (u2 * tmp1)) + c2 * 0.50e+00 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2) -
+                dt * tx1 * (-r43 * c34 * tmp2 * u2);
+      a[1][1] = dt * tx2 * ((2.0e+00 - c2) * (u2 * tmp1)) - dt * tx1 * (r43 * c34 * tmp1) - dt * tx1 * dx2;
+      a[1][2] = dt * tx2 * (-c2 * (u3 * tmp1));
+      a[1][3] = dt * tx2 * (-c2 * (u4 * tmp1));
+      a[1][4] = dt * tx2 * c2;
+      a[2][0] = dt * tx2 * (-(u2 * u3) * tmp2) - dt * tx1 * (-c34 * tmp2 * u3);
+      a[2][1] = dt * tx2 * (u3 * tmp1);
+      a[2][2] = dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx3;
+      a[2][3] = 0.0;
+      a[2][4] = 0.0;
+      a[3][0] = dt * tx2 * (-(u2 * u4) * tmp2) - dt * tx1 * (-c34 * tmp2 * u4);
+      a[3][1] = dt * tx2 * (u4 * tmp1);
+      a[3][2] = 0.0;
+      a[3][3] = dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx4;
+      a[3][4] = 0.0;
+      a[4][0] = dt * tx2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u2 * tmp1)) -
+                dt * tx1 *
+                    (-(r43 * c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
+                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
+      a[4][1] = dt * tx2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((3.0e+00 * u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
+                dt * tx1 * (r43 * c34 - c1345) * tmp2 * u2;
+      a[4][2] = dt * tx2 * (-c2 * (u3 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u3;
+      a[4][3] = dt * tx2 * (-c2 * (u4 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u4;
+      a[4][4] = dt * tx2 * (c1 * (u2 * tmp1)) - dt * tx1 * c1345 * tmp1 - dt * tx1 * dx5;
+    }
+  }
+}
+
+// Elimination of tmat without pivoting with right-hand side v, then the back
+// substitution: blts (src/LU/blts.jl:106-193) or, BUTS, buts as the
+// reference states it (src/LU/buts.jl:113-200: tmat[5,5] -=- tmp*tmat[2,5]
+// and the signs of its back substitution; d's strict upper triangle is +0
+// throughout, so these change no value, but they are kept statement for
+// statement).
+template <bool BUTS>
+__device__ inline void block_solve(double t[5][5], double v[5]) {
+  double tmp1, tmp;
+  tmp1 = 1.0e+00 / t[0][0];
+#pragma unroll
+  for (int r = 1; r < 5; ++r) {
+    tmp = tmp1 * t[r][0];
+#pragma unroll
+    for (int c = 1; c < 5; ++c) t[r][c] = t[r][c] - tmp * t[0][c];
+    v[r] = v[r] - v[0] * tmp;
+  }
+  tmp1 = 1.0e+00 / t[1][1];
+#pragma unroll
+  for (int r = 2; r < 5; ++r) {
+    tmp = tmp1 * t[r][1];
+#pragma unroll
+    for (int c = 2; c < 5; ++c) {
+      if (BUTS && r == 4 && c == 4)
+        t[r][c] = t[r][c] - (-tmp * t[1][c]);
+      else
+        t[r][c] = t[r][c] - tmp * t[1][c];
+    }
+    v[r] = v[r] - v[1] * tmp;
+  }
+  tmp1 = 1.0e+00 / t[2][2];
+#pragma unroll
+  for (int r = 3; r < 5; ++r) {
+    tmp = tmp1 * t[r][2];
+#pragma unroll
+    for (int c = 3; c < 5; ++c) t[r][c] = t[r][c] - tmp * t[2][c];
+    v[r] = v[r] - v[2] * tmp;
+  }
+  tmp1 = 1.0e+00 / t[3][3];
+  tmp = tmp1 * t[4][3];
+  t[4][4] = t[4][4] - tmp * t[3][4];
+  v[4] = v[4] - v[3] * tmp;
+  v[4] = v[4] / t[4][4];
+  v[3] = v[3] - t[3][4] * v[4];
+  v[3] = v[3] / t[3][3];
+  if (BUTS) {
+    v[2] = v[2] - (t[2][3] * v[3] - t[2][4] * v[4]);
+    v[2] = v[2] / t[2][2];
+    v[1] = v[1] - (t[1][2] * v[2] - t[1][3] * v[3] - t[1][4] * v[4]);
+    v[1] = v[1] / t[1][1];
+    v[0] = v[0] - (t[0][1] * v[1] - t[0][2] * v[2] - t[0][3] * v[3] - t[0][4] * v[4]);
+    v[0] = v[0] / t[0][0];
+  } else {
+    v[2] = v[2] - (t[2][3] * v[3] + t[2][4] * v[4]);
+    v[2] = v[2] / t[2][2];
+    v[1] = v[1] - (t[1][2] * v[2] + t[1][3] * v[3] + t[1][4] * v[4]);
+    v[1] = v[1] / t[1][1];
+    v[0] = v[0] - (t[0][1] * v[1] + t[0][2] * v[2] + t[0][3] * v[3] + t[0][4] * v[4]);
+    v[0] = v[0] / t[0][0];
+  }
+}
+
+// The t-th point (0-based) of hyperplane i + j + k = l of a zone's interior,
+// enumerated by k ascending, then j ascending.
+__device__ inline bool hyperplane_point(const LuZone& Z, int l, int t, int& i, int& j, int& k) {
+  const int klo = max(2, l - (Z.nx - 1) - (Z.ny - 1)), khi = min(Z.nz - 1, l - 4);
+  for (int kk = klo; kk <= khi; ++kk) {
+    const int s = l - kk;
+    const int jlo = max(2, s - (Z.nx - 1)), jhi = min(Z.ny - 1, s - 2);
+    const int c = jhi - jlo + 1;
+    if (c <= 0) continue;
+    if (t < c) {
+      k = kk;
+      j = jlo + t;
+      i = s - j;
+      return true;
+    }
+    t -= c;
+  }
+  return false;
+}
+
+__device__ inline void load5(const double* f, long long NP, long long p, double v[5]) {
+#pragma unroll
+  for (int m = 0; m < 5; ++m) v[m] = f[m * NP + p];
+}
+
+// jacld + blts at every point of hyperplane l (blockIdx.y: zone - zone0).
+// SCALE: rsd *= dt at the point first (ssor's scaling, fused: blts reads
+// only points it has already scaled and solved, or boundary points, which
+// the scaling does not touch).
+template <bool SCALE>
+__global__ void __launch_bounds__(TPB) k_lu_lower(LuDev D, int l, int zone0) {
+  const LuZone Z = D.zones[zone0 + blockIdx.y];
+  int i, j, k;
+  if (!hyperplane_point(Z, l, blockIdx.x * TPB + threadIdx.x, i, j, k)) return;
+  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
+  const long long NP = D.NP, p = pidx(Z, i, j, k);
+  const double omega = D.omega;
+  double v[5], w[5], x[5], blk[5][5], blk2[5][5];
+  load5(D.rsd, NP, p, v);
+  if (SCALE) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) v[m] = D.dt * v[m];
+  }
+  // ldz (a): from (i, j, k-1)
+  load5(D.u, NP, pidx(Z, i, j, k - 1), w);
+  jac_off<2, -1>(J, w[0], w[1], w[2], w[3], w[4], blk);
+  load5(D.rsd, NP, pidx(Z, i, j, k - 1), w);
+#pragma unroll
+  for (int m = 0; m < 5; ++m)
+    v[m] = v[m] - omega * (blk[m][0] * w[0] + blk[m][1] * w[1] + blk[m][2] * w[2] + blk[m][3] * w[3] +
+                           blk[m][4] * w[4]);
+  // ldy (b): from (i, j-1, k); ldx (c): from (i-1, j, k)
+  load5(D.u, NP, pidx(Z, i, j - 1, k), w);
+  jac_off<1, -1>(J, w[0], w[1], w[2], w[3], w[4], blk);
+  load5(D.u, NP, pidx(Z, i - 1, j, k), w);
+  jac_off<0, -1>(J, w[0], w[1], w[2], w[3], w[4], blk2);
+  load5(D.rsd, NP, pidx(Z, i, j - 1, k), w);
+  load5(D.rsd, NP, pidx(Z, i - 1, j, k), x);
+#pragma unroll
+  for (int m = 0; m < 5; ++m)
+    v[m] = v[m] - omega * (blk[m][0] * w[0] + blk2[m][0] * x[0] + blk[m][1] * w[1] + blk2[m][1] * x[1] +
+                           blk[m][2] * w[2] + blk2[m][2] * x[2] + blk[m][3] * w[3] + blk2[m][3] * x[3] +
+                           blk[m][4] * w[4] + blk2[m][4] * x[4]);
+  load5(D.u, NP, p, w);
+  jac_d(J, w[0], w[1], w[2], w[3], w[4], blk);
+  block_solve<false>(blk, v);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) D.rsd[m * NP + p] = v[m];
+}
+
+// jacu + buts at every point of hyperplane l
+__global__ void __launch_bounds__(TPB) k_lu_upper(LuDev D, int l, int zone0) {
+  const LuZone Z = D.zones[zone0 + blockIdx.y];
+  int i, j, k;
+  if (!hyperplane_point(Z, l, blockIdx.x * TPB + threadIdx.x, i, j, k)) return;
+  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
+  const long long NP = D.NP, p = pidx(Z, i, j, k);
+  const double omega = D.omega;
+  double tv[5], w[5], x[5], blk[5][5], blk2[5][5];
+  // udz (c): from (i, j, k+1)
+  load5(D.u, NP, pidx(Z, i, j, k + 1), w);
+  jac_off<2, 1>(J, w[0], w[1], w[2], w[3], w[4], blk);
+  load5(D.rsd, NP, pidx(Z, i, j, k + 1), w);
+#pragma unroll
+  for (int m = 0; m < 5; ++m)
+    tv[m] = omega * (blk[m][0] * w[0] + blk[m][1] * w[1] + blk[m][2] * w[2] + blk[m][3] * w[3] + blk[m][4] * w[4]);
+  // udy (b): from (i, j+1, k); udx (a): from (i+1, j, k)
+  load5(D.u, NP, pidx(Z, i, j + 1, k), w);
+  jac_off<1, 1>(J, w[0], w[1], w[2], w[3], w[4], blk);
+  load5(D.u, NP, pidx(Z, i + 1, j, k), w);
+  jac_off<0, 1>(J, w[0], w[1], w[2], w[3], w[4], blk2);
+  load5(D.rsd, NP, pidx(Z, i, j + 1, k), w);
+  load5(D.rsd, NP, pidx(Z, i + 1, j, k), x);
+#pragma unroll
+  for (int m = 0; m < 5; ++m)
+    tv[m] = tv[m] + omega * (blk[m][0] * w[0] + blk2[m][0] * x[0] + blk[m][1] * w[1] + blk2[m][1] * x[1] +
+                             blk[m][2] * w[2] + blk2[m][2] * x[2] + blk[m][3] * w[3] + blk2[m][3] * x[3] +
+                             blk[m][4] * w[4] + blk2[m][4] * x[4]);
+  load5(D.u, NP, p, w);
+  jac_d(J, w[0], w[1], w[2], w[3], w[4], blk);
+  block_solve<true>(blk, tv);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) D.rsd[m * NP + p] = D.rsd[m * NP + p] - tv[m];
+}
+
+// ---- exch_qbc (src/LU/exchange_qbc.jl) --------------------------------------
+// Staging per zone: east face (j = ny-1) and west face (j = 2), nx*nkp points
+// each; south face (i = nx-1) and north face (i = 2), ny*nkp points each;
+// planes k = klo..klo+nkp-1; element [m][k][pos].
+struct Faces {
+  double* stage;
+  const long long* zoff;  // staging offset of each zone
+  const int* nbr;         // west, east, south, north per zone
+  int klo, nkp;
+};
+
+__device__ inline void face_sizes(const LuZone& Z, int nkp, long long& e, long long& s) {
+  e = (long long)Z.nx * nkp;
+  s = (long long)Z.ny * nkp;
+}
+
+__global__ void __launch_bounds__(TPB) k_lu_pack(LuDev D, Faces F, int nzones) {
+  const int z = blockIdx.y;
+  if (z >= nzones) return;
+  const LuZone Z = D.zones[z];
+  const int per = 2 * Z.nx + 2 * Z.ny;
+  const int t = blockIdx.x * TPB + threadIdx.x;
+  if (t >= per * F.nkp) return;
+  const int kq = t / per, pos = t % per, k = F.klo + kq;
+  long long ne, ns;
+  face_sizes(Z, F.nkp, ne, ns);
+  double* base = F.stage + F.zoff[z];
+  int i, j;
+  long long so;
+  if (pos < Z.nx) {  // east face
+    i = pos + 1; j = Z.ny - 1; so = 0 * ne + (long long)kq * Z.nx + pos;
+  } else if (pos < 2 * Z.nx) {  // west face
+    i = pos - Z.nx + 1; j = 2; so = 5 * ne + (long long)kq * Z.nx + (pos - Z.nx);
+  } else if (pos < 2 * Z.nx + Z.ny) {  // south face
+    i = Z.nx - 1; j = pos - 2 * Z.nx + 1; so = 10 * ne + (long long)kq * Z.ny + (j - 1);
+  } else {  // north face
+    i = 2; j = pos - 2 * Z.nx - Z.ny + 1; so = 10 * ne + 5 * ns + (long long)kq * Z.ny + (j - 1);
+  }
+  const long long p = pidx(Z, i, j, k);
+  const long long stride = pos < 2 * Z.nx ? ne : ns;
+#pragma unroll
+  for (int m = 0; m < 5; ++m) base[so + m * stride] = D.u[m * D.NP + p];
+}
+
+// Every ghost point has one writer: j = 1 / j = ny (west / east) include the
+// corners, which the reference's unpack order (south, north, west, east)
+// leaves to them.
+__global__ void __launch_bounds__(TPB) k_lu_unpack(LuDev D, Faces F, int nzones) {
+  const int z = blockIdx.y;
+  if (z >= nzones) return;
+  const LuZone Z = D.zones[z];
+  const int per = 2 * Z.nx + 2 * (Z.ny - 2);
+  const int t = blockIdx.x * TPB + threadIdx.x;
+  if (t >= per * F.nkp) return;
+  const int kq = t / per, pos = t % per, k = F.klo + kq;
+  int i, j, src;
+  long long so, stride;
+  if (pos < Z.nx) {  // west ghost j = 1 <- west zone's east face
+    i = pos + 1; j = 1; src = F.nbr[4 * z + 0];
+    const LuZone S = D.zones[src];
+    long long ne, ns;
+    face_sizes(S, F.nkp, ne, ns);
+    so = F.zoff[src] + 0 * ne + (long long)kq * S.nx + (i - 1); stride = ne;
+  } else if (pos < 2 * Z.nx) {  // east ghost j = ny <- east zone's west face
+    i = pos - Z.nx + 1; j = Z.ny; src = F.nbr[4 * z + 1];
+    const LuZone S = D.zones[src];
+    long long ne, ns;
+    face_sizes(S, F.nkp, ne, ns);
+    so = F.zoff[src] + 5 * ne + (long long)kq * S.nx + (i - 1); stride = ne;
+  } else if (pos < 2 * Z.nx + (Z.ny - 2)) {  // north ghost i = 1 <- north zone's south face
+    i = 1; j = pos - 2 * Z.nx + 2; src = F.nbr[4 * z + 3];
+    const LuZone S = D.zones[src];
+    long long ne, ns;
+    face_sizes(S, F.nkp, ne, ns);
+    so = F.zoff[src] + 10 * ne + (long long)kq * S.ny + (j - 1); stride = ns;
+  } else {  // south ghost i = nx <- south zone's north face
+    i = Z.nx; j = pos - 2 * Z.nx - (Z.ny - 2) + 2; src = F.nbr[4 * z + 2];
+    const LuZone S = D.zones[src];
+    long long ne, ns;
+    face_sizes(S, F.nkp, ne, ns);
+    so = F.zoff[src] + 10 * ne + 5 * ns + (long long)kq * S.ny + (j - 1); stride = ns;
+  }
+  const long long p = pidx(Z, i, j, k);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) D.u[m * D.NP + p] = F.stage[so + m * stride];
+}
+
+// ---- norms (src/LU/l2norm.jl, src/LU/error.jl, src/LU/pintgr.jl) -----------
+// WHICH 0: sum of rsd^2, 1: sum of (exact - u)^2 over the interior; one row
+// of 5 partial sums per work block (fixed-order tree reduction)
+template <int WHICH>
+__global__ void __launch_bounds__(TPB) k_lu_norm_partial(LuDev D, const LuWork* __restrict__ work, CeTable ce,
+                                                         double* partial) {
+  __shared__ double sh[5][TPB];
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  double s[5] = {0, 0, 0, 0, 0};
+  int i, j, k;
+  if (decode(Z, w.first + threadIdx.x, i, j, k) && interior(Z, i, j, k)) {
+    const long long p = pidx(Z, i, j, k);
+    if (WHICH == 0) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const double r = D.rsd[m * D.NP + p];
+        s[m] = r * r;
+      }
+    } else {
+      double e[5];
+      exact_point(ce, i, j, k, Z.nx, Z.ny, Z.nz, e);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const double t = e[m] - D.u[m * D.NP + p];
+        s[m] = t * t;
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 5; ++m) sh[m][threadIdx.x] = s[m];
+  __syncthreads();
+  for (int h = TPB / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+#pragma unroll
+      for (int m = 0; m < 5; ++m) sh[m][threadIdx.x] += sh[m][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x < 5) partial[(long long)blockIdx.x * 5 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// per zone: sqrt(sum / ((nx-2)(ny-2)(nz-2))), then summed over zones in
+// order into out[5] (+ out_zone[5*z + m] when non-null); one thread per m
+__global__ void k_lu_norm_finish(const LuZone* zones, const int* zblock, int nzones, const double* partial,
+                                 double* out, double* out_zone) {
+  const int m = threadIdx.x;
+  if (m >= 5) return;
+  double total = 0.0;
+  for (int z = 0; z < nzones; ++z) {
+    double s = 0.0;
+    for (int b = zblock[z]; b < zblock[z + 1]; ++b) s += partial[(long long)b * 5 + m];
+    const LuZone Z = zones[z];
+    const double r = sqrt(s / ((double)(Z.nx - 2) * (Z.ny - 2) * (Z.nz - 2)));
+    if (out_zone) out_zone[5 * z + m] = r;
+    total += r;
+  }
+  out[m] = total;
+}
+
+// pintgr of one zone per block (one process: ibeg = ii1, ifin = ii2,
+// jbeg = ji1, jfin = ji2); frc[z] = 0.25 (frc1 + frc2 + frc3)
+__global__ void __launch_bounds__(TPB) k_lu_pintgr(LuDev D, double* frc) {
+  __shared__ double sh[3][TPB];
+  const LuZone Z = D.zones[blockIdx.x];
+  const int ibeg = ii1, ifin = Z.ii2, jbeg = ji1, jfin = Z.ji2, ifin1 = ifin - 1, jfin1 = jfin - 1;
+  auto phi = [&](int i, int j, int k) {
+    const long long p = pidx(Z, i, j, k);
+    const double u1 = D.u[p], u2 = D.u[D.NP + p], u3 = D.u[2 * D.NP + p], u4 = D.u[3 * D.NP + p],
+                 u5 = D.u[4 * D.NP + p];
+    return c2 * (u5 - 0.50e+00 * (u2 * u2 + u3 * u3 + u4 * u4) / u1);
+  };
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const int n1i = ifin1 - ibeg + 1, n1j = jfin1 - jbeg + 1, nk = Z.ki2 - 1 - ki1 + 1;
+  for (int t = threadIdx.x; t < n1i * n1j; t += TPB) {
+    const int i = ibeg + t % n1i, j = jbeg + t / n1i;
+    s1 += (phi(i, j, ki1) + phi(i + 1, j, ki1) + phi(i, j + 1, ki1) + phi(i + 1, j + 1, ki1) + phi(i, j, Z.ki2) +
+           phi(i + 1, j, Z.ki2) + phi(i, j + 1, Z.ki2) + phi(i + 1, j + 1, Z.ki2));
+  }
+  for (int t = threadIdx.x; t < n1i * nk; t += TPB) {
+    const int i = ibeg + t % n1i, k = ki1 + t / n1i;
+    s2 += (phi(i, jbeg, k) + phi(i + 1, jbeg, k) + phi(i, jbeg, k + 1) + phi(i + 1, jbeg, k + 1) + phi(i, jfin, k) +
+           phi(i + 1, jfin, k) + phi(i, jfin, k + 1) + phi(i + 1, jfin, k + 1));
+  }
+  for (int t = threadIdx.x; t < n1j * nk; t += TPB) {
+    const int j = jbeg + t % n1j, k = ki1 + t / n1j;
+    s3 += (phi(ibeg, j, k) + phi(ibeg, j + 1, k) + phi(ibeg, j, k + 1) + phi(ibeg, j + 1, k + 1) + phi(ifin, j, k) +
+           phi(ifin, j + 1, k) + phi(ifin, j, k + 1) + phi(ifin, j + 1, k + 1));
+  }
+  sh[0][threadIdx.x] = s1;
+  sh[1][threadIdx.x] = s2;
+  sh[2][threadIdx.x] = s3;
+  __syncthreads();
+  for (int h = TPB / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+      for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double frc1 = Z.dxi * Z.deta * sh[0][0];
+    const double frc2 = Z.dxi * Z.dzeta * sh[1][0];
+    const double frc3 = Z.deta * Z.dzeta * sh[2][0];
+    frc[blockIdx.x] = 0.25e+00 * (frc1 + frc2 + frc3);
+  }
+}
+
+// ---- layout conversion --------------------------------------------------------
+// REF: [1:5, -1:nx+2, -1:ny+2, 1:nz] column-major; DENSE: [m][k][j][i]
+template <bool REF, bool TO_DEV>
+__global__ void __launch_bounds__(TPB) k_lu_convert(LuDev D, double* field, double* host_img, int zone) {
+  const LuZone Z = D.zones[zone];
+  const int q = blockIdx.x * TPB + threadIdx.x;
+  if (q >= Z.np) return;
+  const int i = q % Z.nx + 1, j = (q / Z.nx) % Z.ny + 1, k = q / (Z.nx * Z.ny) + 1;
+  const long long p = pidx(Z, i, j, k);
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    const long long h = REF ? m + 5LL * ((i + 1) + (long long)(Z.nx + 4) * ((j + 1) + (long long)(Z.ny + 4) * (k - 1)))
+                            : (long long)m * Z.np + q;
+    if (TO_DEV)
+      field[m * D.NP + p] = host_img[h];
+    else
+      host_img[h] = field[m * D.NP + p];
+  }
+}
+
+}  // namespace
+
+// ============================== C ABI =========================================
+struct npbmz_lu_handle {
+  int nzones = 0, flags = 0;
+  double dt = 0, omega = 0;
+  long long NP = 0;
+  std::vector<LuZone> zh;
+  std::vector<int> nbr;
+  LuZone* zones_d = nullptr;
+  int* nbr_d = nullptr;
+  double *u = nullptr, *rsd = nullptr, *frct = nullptr;
+  // work lists: all zones, and per zone a contiguous range
+  std::vector<LuWork> work_h;
+  std::vector<int> zblock;  // first block of each zone, nzones+1 entries
+  LuWork* work_d = nullptr;
+  int* zblock_d = nullptr;
+  double* partial = nullptr;  // 5 per work block
+  double* norms_d = nullptr;  // per-iteration rsd norms, 5 per iteration (grown on demand)
+  int norms_cap = 0;
+  double* zone_out_d = nullptr;  // 5*nzones + nzones scratch
+  // exch_qbc staging
+  double* stage = nullptr;
+  long long* zoff_d = nullptr;
+  int klo = 1, nkp = 0;
+  int lmin = 6, lmax = 6;
+  std::vector<int> lcount;  // max points over zones per hyperplane l
+  double* img = nullptr;    // host-image staging for transfers
+  size_t img_cap = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  CeTable ce{};
+  std::string err;
+  std::mutex mu;
+};
+
+namespace {
+
+int fail(npbmz_lu_t* h, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  return -1;
+}
+
+#define LU_CK(h, call)                                                                                      \
+  do {                                                                                                      \
+    cudaError_t e_ = (call);                                                                                \
+    if (e_ != cudaSuccess) return fail(h, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+LuDev dev(npbmz_lu_t* h) { return LuDev{h->u, h->rsd, h->frct, h->NP, h->zones_d, h->dt, h->omega}; }
+
+Faces faces(npbmz_lu_t* h) { return Faces{h->stage, h->zoff_d, h->nbr_d, h->klo, h->nkp}; }
+
+int hp_count(const LuZone& Z, int l) {
+  int n = 0;
+  for (int k = std::max(2, l - (Z.nx - 1) - (Z.ny - 1)); k <= std::min(Z.nz - 1, l - 4); ++k) {
+    const int s = l - k;
+    n += std::max(0, std::min(Z.ny - 1, s - 2) - std::max(2, s - (Z.nx - 1)) + 1);
+  }
+  return n;
+}
+
+// blocks of one zone (zone >= 0) or all zones
+void work_range(npbmz_lu_t* h, int zone, const LuWork** w, int* n) {
+  if (zone < 0) {
+    *w = h->work_d;
+    *n = (int)h->work_h.size();
+  } else {
+    *w = h->work_d + h->zblock[zone];
+    *n = h->zblock[zone + 1] - h->zblock[zone];
+  }
+}
+
+int launch_exch(npbmz_lu_t* h) {
+  int maxper = 0;
+  for (const LuZone& Z : h->zh) maxper = std::max(maxper, 2 * Z.nx + 2 * Z.ny);
+  const dim3 g((maxper * h->nkp + TPB - 1) / TPB, h->nzones);
+  k_lu_pack<<<g, TPB, 0, h->stream>>>(dev(h), faces(h), h->nzones);
+  k_lu_unpack<<<g, TPB, 0, h->stream>>>(dev(h), faces(h), h->nzones);
+  LU_CK(h, cudaGetLastError());
+  return 0;
+}
+
+int launch_phase(npbmz_lu_t* h, int phase, int zone) {
+  const LuWork* w;
+  int n;
+  work_range(h, zone, &w, &n);
+  const int z0 = zone < 0 ? 0 : zone, nzs = zone < 0 ? h->nzones : 1;
+  switch (phase) {
+    case NPBMZ_LU_PHASE_RHS:
+      k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), w, h->u, h->rsd);
+      break;
+    case NPBMZ_LU_PHASE_SCALE:
+      k_lu_pointwise<false><<<n, TPB, 0, h->stream>>>(dev(h), w, 0.0);
+      break;
+    case NPBMZ_LU_PHASE_UPDATE:
+      k_lu_pointwise<true><<<n, TPB, 0, h->stream>>>(dev(h), w, 1.0e+00 / (h->omega * (2.0e+00 - h->omega)));
+      break;
+    case NPBMZ_LU_PHASE_EXCH:
+      return launch_exch(h);
+    case NPBMZ_LU_PHASE_LOWER:
+    case NPBMZ_LU_PHASE_SSOR + 100:  // lower with the scaling fused
+      for (int l = h->lmin; l <= h->lmax; ++l) {
+        int c = 0;
+        for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
+        if (!c) continue;
+        const dim3 g((c + TPB - 1) / TPB, nzs);
+        if (phase == NPBMZ_LU_PHASE_LOWER)
+          k_lu_lower<false><<<g, TPB, 0, h->stream>>>(dev(h), l, z0);
+        else
+          k_lu_lower<true><<<g, TPB, 0, h->stream>>>(dev(h), l, z0);
+      }
+      break;
+    case NPBMZ_LU_PHASE_UPPER:
+      for (int l = h->lmax; l >= h->lmin; --l) {
+        int c = 0;
+        for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
+        if (!c) continue;
+        const dim3 g((c + TPB - 1) / TPB, nzs);
+        k_lu_upper<<<g, TPB, 0, h->stream>>>(dev(h), l, z0);
+      }
+      break;
+    case NPBMZ_LU_PHASE_SSOR: {
+      int rc = launch_phase(h, NPBMZ_LU_PHASE_SSOR + 100, zone);
+      if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPPER, zone);
+      if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPDATE, zone);
+      if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_RHS, zone);
+      return rc;
+    }
+    default:
+      return fail(h, "unknown LU phase %d", phase);
+  }
+  LU_CK(h, cudaGetLastError());
+  return 0;
+}
+
+int launch_iteration(npbmz_lu_t* h) {
+  int rc = launch_exch(h);
+  if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_SSOR, -1);
+  return rc;
+}
+
+int launch_rsd_norm(npbmz_lu_t* h, double* out) {
+  k_lu_norm_partial<0><<<(int)h->work_h.size(), TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce, h->partial);
+  k_lu_norm_finish<<<1, 32, 0, h->stream>>>(h->zones_d, h->zblock_d, h->nzones, h->partial, out, nullptr);
+  LU_CK(h, cudaGetLastError());
+  return 0;
+}
+
+int ensure_img(npbmz_lu_t* h, size_t bytes) {
+  if (h->img_cap >= bytes) return 0;
+  if (h->img) cudaFree(h->img);
+  h->img = nullptr;
+  h->img_cap = 0;
+  LU_CK(h, cudaMalloc(&h->img, bytes));
+  h->img_cap = bytes;
+  return 0;
+}
+
+size_t zone_elems(const LuZone& Z, int layout) {
+  return layout == NPBMZ_LAYOUT_REF ? (size_t)5 * (Z.nx + 4) * (Z.ny + 4) * Z.nz : (size_t)5 * Z.np;
+}
+
+double* field_ptr(npbmz_lu_t* h, int field) {
+  return field == NPBMZ_LU_U ? h->u : (field == NPBMZ_LU_RSD ? h->rsd : (field == NPBMZ_LU_FRCT ? h->frct : nullptr));
+}
+
+int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool up) {
+  double* f = field_ptr(h, field);
+  if (!f) return fail(h, "unknown field %d", field);
+  if (layout != NPBMZ_LAYOUT_DENSE && layout != NPBMZ_LAYOUT_REF) return fail(h, "unknown layout %d", layout);
+  if (zone < -1 || zone >= h->nzones) return fail(h, "zone %d out of range", zone);
+  if (!host) return fail(h, "null host buffer");
+  const int z0 = zone < 0 ? 0 : zone, z1 = zone < 0 ? h->nzones : zone + 1;
+  for (int z = z0; z < z1; ++z) {
+    const LuZone& Z = h->zh[z];
+    const size_t n = zone_elems(Z, layout);
+    if (ensure_img(h, n * sizeof(double))) return -1;
+    const int blocks = (Z.np + TPB - 1) / TPB;
+    if (up) {
+      LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+      if (layout == NPBMZ_LAYOUT_REF)
+        k_lu_convert<true, true><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+      else
+        k_lu_convert<false, true><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+    } else {
+      if (layout == NPBMZ_LAYOUT_REF)  // keep the host halo: start from the host image
+        LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+      if (layout == NPBMZ_LAYOUT_REF)
+        k_lu_convert<true, false><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+      else
+        k_lu_convert<false, false><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+      LU_CK(h, cudaMemcpyAsync(host, h->img, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    LU_CK(h, cudaGetLastError());
+    LU_CK(h, cudaStreamSynchronize(h->stream));
+    host += n;
+  }
+  return 0;
+}
+
+void free_all(npbmz_lu_t* h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->work_d,
+                  (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
+                  (void*)h->zoff_d, (void*)h->img})
+    if (p) cudaFree(p);
+  if (h->own) cudaStreamDestroy(h->own);
+}
+
+}  // namespace
+
+extern "C" {
+
+int npbmz_lu_zone_setup(int gx, int gy, int gz, int xz, int yz, double ratio, int* nx, int* ny, int* nz, int* nbr) {
+  if (xz < 1 || yz < 1 || gx < 1 || gy < 1 || gz < 1 || !nx || !ny || !nz || !nbr) return -1;
+  std::vector<long> x_end(xz), y_end(yz), x_start(xz), y_start(yz), x_size(xz), y_size(yz);
+  if (std::fabs(ratio - 1.0e0) > 1.0e-10) {
+    if (xz < 2 || yz < 2) return -1;
+    const double x_r = std::exp(std::log(ratio) / (xz - 1));
+    const double y_r = std::exp(std::log(ratio) / (yz - 1));
+    const double x_smallest = (double)gx * (x_r - 1.0e0) / (std::pow(x_r, xz) - 1.0e0);
+    const double y_smallest = (double)gy * (y_r - 1.0e0) / (std::pow(y_r, yz) - 1.0e0);
+    // Julia's round: to nearest, ties to even
+    for (int i = 1; i <= xz; ++i)
+      x_end[i - 1] = (long)std::nearbyint(x_smallest * (std::pow(x_r, i) - 1.0e0) / (x_r - 1.0e0) + 0.45e0);
+    for (int j = 1; j <= yz; ++j)
+      y_end[j - 1] = (long)std::nearbyint(y_smallest * (std::pow(y_r, j) - 1.0e0) / (y_r - 1.0e0) + 0.45e0);
+  } else {
+    for (int i = 1; i <= xz; ++i) {
+      if (((long)i * gx) % xz) return -1;
+      x_end[i - 1] = (long)i * gx / xz;
+    }
+    for (int j = 1; j <= yz; ++j) {
+      if (((long)j * gy) % yz) return -1;
+      y_end[j - 1] = (long)j * gy / yz;
+    }
+  }
+  x_start[0] = 1;
+  for (int i = 0; i < xz; ++i) {
+    if (i != xz - 1) x_start[i + 1] = x_end[i] + 1;
+    x_size[i] = x_end[i] - x_start[i] + 1;
+  }
+  y_start[0] = 1;
+  for (int j = 0; j < yz; ++j) {
+    if (j != yz - 1) y_start[j + 1] = y_end[j] + 1;
+    y_size[j] = y_end[j] - y_start[j] + 1;
+  }
+  const int nzones = xz * yz;
+  for (int j = 1; j <= yz; ++j)
+    for (int i = 1; i <= xz; ++i) {
+      const int zn = (i - 1) + (j - 1) * xz + 1;
+      nx[zn - 1] = (int)x_size[i - 1];
+      ny[zn - 1] = (int)y_size[j - 1];
+      nz[zn - 1] = gz;
+      const int north = i > 1 ? zn - 1 : j * xz;
+      const int south = i < xz ? zn + 1 : zn - xz + 1;
+      const int west = j > 1 ? zn - xz : zn + yz * (xz - 1);
+      const int east = j < yz ? zn + xz : zn - yz * (xz - 1);
+      for (int q : {north, south, west, east})
+        if (q < 1 || q > nzones) return -1;
+      nbr[4 * (zn - 1) + 0] = west - 1;
+      nbr[4 * (zn - 1) + 1] = east - 1;
+      nbr[4 * (zn - 1) + 2] = south - 1;
+      nbr[4 * (zn - 1) + 3] = north - 1;
+    }
+  return 0;
+}
+
+int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, const int* nbr, const double* params,
+                    int flags, npbmz_lu_t** out) {
+  if (!out) return -1;
+  *out = nullptr;
+  if (nzones < 1 || !nx || !ny || !nz || !nbr || !params) return -1;
+  if (flags & ~(NPBMZ_LU_FACES_NPB | NPBMZ_LU_GRAPH)) return -1;
+  npbmz_lu_t* h = new npbmz_lu_t();
+  h->nzones = nzones;
+  h->flags = flags;
+  h->dt = params[0];
+  h->omega = params[1];
+  std::memcpy(h->ce.c, ce_reference, sizeof(h->ce.c));
+  h->nbr.assign(nbr, nbr + 4 * nzones);
+  long long off = 0;
+  int gz = nz[0];
+  for (int z = 0; z < nzones; ++z) {
+    // ssor's stencils and pintgr need 5 points per axis (the reference's
+    // SUBDOMAIN SIZE check asks for 3; its fourth-difference dissipation
+    // reads 5)
+    if (nx[z] < 5 || ny[z] < 5 || nz[z] < 5 || nz[z] != gz) {
+      delete h;
+      return -1;
+    }
+    for (int q = 0; q < 4; ++q)
+      if (nbr[4 * z + q] < 0 || nbr[4 * z + q] >= nzones) {
+        delete h;
+        return -1;
+      }
+    LuZone Z{};
+    Z.off = off;
+    Z.nx = nx[z]; Z.ny = ny[z]; Z.nz = nz[z];
+    Z.np = nx[z] * ny[z] * nz[z];
+    Z.dxi = 1.0e+00 / (Z.nx - 1);
+    Z.deta = 1.0e+00 / (Z.ny - 1);
+    Z.dzeta = 1.0e+00 / (Z.nz - 1);
+    Z.tx1 = 1.0e+00 / (Z.dxi * Z.dxi);
+    Z.tx2 = 1.0e+00 / (2.0e+00 * Z.dxi);
+    Z.tx3 = 1.0e+00 / Z.dxi;
+    Z.ty1 = 1.0e+00 / (Z.deta * Z.deta);
+    Z.ty2 = 1.0e+00 / (2.0e+00 * Z.deta);
+    Z.ty3 = 1.0e+00 / Z.deta;
+    Z.tz1 = 1.0e+00 / (Z.dzeta * Z.dzeta);
+    Z.tz2 = 1.0e+00 / (2.0e+00 * Z.dzeta);
+    Z.tz3 = 1.0e+00 / Z.dzeta;
+    Z.ii2 = Z.nx - 1;
+    Z.ji2 = Z.ny - 2;
+    Z.ki2 = Z.nz - 1;
+    h->zh.push_back(Z);
+    off += ((long long)Z.np + 31) / 32 * 32;
+  }
+  // faces between neighbours must match: west/east share nx, south/north ny
+  for (int z = 0; z < nzones; ++z) {
+    if (h->zh[h->nbr[4 * z + 0]].nx != h->zh[z].nx || h->zh[h->nbr[4 * z + 1]].nx != h->zh[z].nx ||
+        h->zh[h->nbr[4 * z + 2]].ny != h->zh[z].ny || h->zh[h->nbr[4 * z + 3]].ny != h->zh[z].ny) {
+      delete h;
+      return -1;
+    }
+  }
+  h->NP = off;
+  h->klo = (flags & NPBMZ_LU_FACES_NPB) ? 2 : 1;
+  h->nkp = gz - 2;
+  h->lmin = 6;
+  h->lmax = 6;
+  for (const LuZone& Z : h->zh) h->lmax = std::max(h->lmax, Z.nx + Z.ny + Z.nz - 3);
+  h->zblock.push_back(0);
+  for (int z = 0; z < nzones; ++z) {
+    for (int f = 0; f < h->zh[z].np; f += TPB) h->work_h.push_back(LuWork{z, f});
+    h->zblock.push_back((int)h->work_h.size());
+  }
+  std::vector<long long> zoff(nzones);
+  long long so = 0;
+  for (int z = 0; z < nzones; ++z) {
+    zoff[z] = so;
+    so += 10LL * h->zh[z].nx * h->nkp + 10LL * h->zh[z].ny * h->nkp;
+  }
+  auto bail = [&](const char* what) {
+    fail(h, "%s", what);
+    free_all(h);
+    delete h;
+    return -1;
+  };
+  const size_t F = (size_t)5 * h->NP * sizeof(double);
+  if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess) return bail("stream");
+  h->stream = h->own;
+  if (cudaMalloc(&h->zones_d, nzones * sizeof(LuZone)) || cudaMalloc(&h->nbr_d, 4 * nzones * sizeof(int)) ||
+      cudaMalloc(&h->u, F) || cudaMalloc(&h->rsd, F) || cudaMalloc(&h->frct, F) ||
+      cudaMalloc(&h->work_d, h->work_h.size() * sizeof(LuWork)) ||
+      cudaMalloc(&h->zblock_d, h->zblock.size() * sizeof(int)) ||
+      cudaMalloc(&h->partial, h->work_h.size() * 5 * sizeof(double)) ||
+      cudaMalloc(&h->zone_out_d, (6 * (size_t)nzones + 16) * sizeof(double)) ||
+      cudaMalloc(&h->stage, so * sizeof(double)) || cudaMalloc(&h->zoff_d, nzones * sizeof(long long)))
+    return bail("device allocation failed");
+  if (cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(LuZone), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->nbr_d, h->nbr.data(), 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->work_d, h->work_h.data(), h->work_h.size() * sizeof(LuWork), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->zblock_d, h->zblock.data(), h->zblock.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->zoff_d, zoff.data(), nzones * sizeof(long long), cudaMemcpyHostToDevice) ||
+      cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F))
+    return bail("device initialisation failed");
+  *out = h;
+  return 0;
+}
+
+int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  std::memcpy(h->ce.c, ce ? ce : &ce_reference[0][0], sizeof(h->ce.c));
+  const int n = (int)h->work_h.size();
+  k_lu_init<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce);
+  k_lu_poly<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce);
+  k_lu_rhs<true><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->rsd, h->frct);
+  k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->u, h->rsd);
+  LU_CK(h, cudaGetLastError());
+  return 0;
+}
+
+int npbmz_lu_upload(npbmz_lu_t* h, int zone, int field, int layout, const double* host) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  return transfer(h, zone, field, layout, const_cast<double*>(host), true);
+}
+
+int npbmz_lu_download(npbmz_lu_t* h, int zone, int field, int layout, double* host) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  return transfer(h, zone, field, layout, host, false);
+}
+
+int npbmz_lu_exch_qbc(npbmz_lu_t* h) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  return launch_exch(h);
+}
+
+int npbmz_lu_ssor(npbmz_lu_t* h, int zone) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  if (zone < -1 || zone >= h->nzones) return fail(h, "zone %d out of range", zone);
+  return launch_phase(h, NPBMZ_LU_PHASE_SSOR, zone);
+}
+
+int npbmz_lu_phase(npbmz_lu_t* h, int phase, int zone) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  if (zone < -1 || zone >= h->nzones) return fail(h, "zone %d out of range", zone);
+  if (phase < 0 || phase > NPBMZ_LU_PHASE_SSOR) return fail(h, "unknown LU phase %d", phase);
+  return launch_phase(h, phase, zone);
+}
+
+int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  if (niter < 0) return fail(h, "niter < 0");
+  if (rsdnm && niter > h->norms_cap) {
+    if (h->norms_d) cudaFree(h->norms_d);
+    h->norms_d = nullptr;
+    h->norms_cap = 0;
+    LU_CK(h, cudaMalloc(&h->norms_d, (size_t)5 * niter * sizeof(double)));
+    h->norms_cap = niter;
+  }
+  if ((h->flags & NPBMZ_LU_GRAPH) && !h->graph) {
+    cudaGraph_t gr;
+    LU_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = launch_iteration(h);
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
+    if (rc) return rc;
+    LU_CK(h, e);
+    const cudaError_t ie = cudaGraphInstantiate(&h->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    LU_CK(h, ie);
+  }
+  for (int it = 0; it < niter; ++it) {
+    if (h->graph) {
+      LU_CK(h, cudaGraphLaunch(h->graph, h->stream));
+    } else if (int rc = launch_iteration(h)) {
+      return rc;
+    }
+    if (rsdnm && launch_rsd_norm(h, h->norms_d + 5 * (size_t)it)) return -1;
+  }
+  if (rsdnm) {
+    LU_CK(h, cudaMemcpyAsync(rsdnm, h->norms_d, (size_t)5 * niter * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+    LU_CK(h, cudaStreamSynchronize(h->stream));
+  }
+  return 0;
+}
+
+int npbmz_lu_verify(npbmz_lu_t* h, double* xcr, double* xce, double* xci) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  if (!xcr || !xce || !xci) return fail(h, "null output");
+  double* o = h->zone_out_d;  // [0,5) xcr, [5,10) xce, [16, 16+nzones) frc per zone
+  if (launch_rsd_norm(h, o)) return -1;
+  k_lu_norm_partial<1><<<(int)h->work_h.size(), TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce, h->partial);
+  k_lu_norm_finish<<<1, 32, 0, h->stream>>>(h->zones_d, h->zblock_d, h->nzones, h->partial, o + 5, nullptr);
+  k_lu_pintgr<<<h->nzones, TPB, 0, h->stream>>>(dev(h), o + 16);
+  LU_CK(h, cudaGetLastError());
+  std::vector<double> host(16 + h->nzones);
+  LU_CK(h, cudaMemcpyAsync(host.data(), o, host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LU_CK(h, cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < 5; ++m) {
+    xcr[m] = host[m];
+    xce[m] = host[5 + m];
+  }
+  double f = 0.0;
+  for (int z = 0; z < h->nzones; ++z) f += host[16 + z];
+  *xci = f;
+  return 0;
+}
+
+int npbmz_lu_set_stream(npbmz_lu_t* h, void* stream) {
+  if (!h) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  h->stream = stream ? (cudaStream_t)stream : h->own;
+  return 0;
+}
+
+int npbmz_lu_synchronize(npbmz_lu_t* h) {
+  if (!h) return -1;
+  LU_CK(h, cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
+  if (!h) return -1;
+  int n = 2 + 2;  // exch (pack, unpack) + update + rhs
+  for (int l = h->lmin; l <= h->lmax; ++l) {
+    int c = 0;
+    for (const LuZone& Z : h->zh) c = std::max(c, hp_count(Z, l));
+    if (c) n += 2;
+  }
+  return n;
+}
+
+int npbmz_lu_profile(npbmz_lu_t* h, int niter, double* phase_ms) {
+  if (!h || !phase_ms || niter < 1) return -1;
+  std::lock_guard<std::mutex> g(h->mu);
+  cudaEvent_t ev[6];
+  for (auto& e : ev) LU_CK(h, cudaEventCreate(&e));
+  for (int q = 0; q < 5; ++q) phase_ms[q] = 0.0;
+  int rc = 0;
+  for (int it = 0; it < niter && !rc; ++it) {
+    cudaEventRecord(ev[0], h->stream);
+    rc = launch_exch(h);
+    cudaEventRecord(ev[1], h->stream);
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_SSOR + 100, -1);
+    cudaEventRecord(ev[2], h->stream);
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPPER, -1);
+    cudaEventRecord(ev[3], h->stream);
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPDATE, -1);
+    cudaEventRecord(ev[4], h->stream);
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_RHS, -1);
+    cudaEventRecord(ev[5], h->stream);
+    if (cudaEventSynchronize(ev[5]) != cudaSuccess) rc = fail(h, "event synchronisation failed");
+    for (int q = 0; q < 5 && !rc; ++q) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+      phase_ms[q] += ms;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+const char* npbmz_lu_last_error(npbmz_lu_t* h) { return h ? h->err.c_str() : "null handle"; }
+
+int npbmz_lu_destroy(npbmz_lu_t* h) {
+  if (!h) return -1;
+  cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return 0;
+}
+
+}  // extern "C"

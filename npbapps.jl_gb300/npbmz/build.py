@@ -6,7 +6,8 @@ The translation units compile in parallel:
   step_fast.cu       -fmad=true   FP64 (FMA) and FP32 line-solve kernels
   npbmz_api.cu                    the C ABI (include/npbmz.h)
   noalloc.cu         -fmad=true   the x sweep over a file-scope device array
-  adjoint.cu         -fmad=true   the discrete adjoint of the BT step
+  adjoint.cu         -fmad=true   the discrete adjoint of the BT and SP steps
+  lu.cu              -fmad=false  LU-MZ's SSOR iteration and its C ABI (include/npbmz_lu.h)
 and are linked into npbapps.jl_gb300/npbmz/_build/libnpbmz_gpu.so.
 """
 import os
@@ -31,6 +32,7 @@ UNITS = {
     "npbmz_api.cu": [],
     "noalloc.cu": ["-fmad=true"],
     "adjoint.cu": ["-fmad=true"],
+    "lu.cu": ["-fmad=false"],
 }
 
 
@@ -42,7 +44,7 @@ def nvcc():
 
 
 def _sources():
-    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [INCLUDE / "npbmz.h"]
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
 
 
 def up_to_date():

@@ -1,5 +1,6 @@
 """The C ABI library builds for sm_103a, loads, and exports every entry point
-include/npbmz.h declares; host-side helpers that need no GPU."""
+include/npbmz.h and include/npbmz_lu.h declare; host-side helpers that need
+no GPU."""
 import re
 from pathlib import Path
 
@@ -8,22 +9,32 @@ import pytest
 
 import npbmz
 
-HEADER = Path(__file__).resolve().parents[1] / "include" / "npbmz.h"
+INCLUDE = Path(__file__).resolve().parents[1] / "include"
+HEADER = INCLUDE / "npbmz.h"
+LU_HEADER = INCLUDE / "npbmz_lu.h"
 
 
-def declared_functions():
-    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+def declared_functions(header=HEADER):
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
     return sorted(set(re.findall(r"\b(npbmz_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_header_declares_the_exported_list():
+    from npbmz import lu
+
     assert sorted(npbmz.EXPORTS) == declared_functions()
+    assert sorted(lu.LU_EXPORTS) == declared_functions(LU_HEADER)
+
+
+def test_every_header_is_covered():
+    assert sorted(p.name for p in INCLUDE.glob("*.h")) == ["npbmz.h", "npbmz_lu.h"]
 
 
 def test_library_exports_every_declared_symbol(npbmz_mod):
     L = npbmz_mod.lib()
-    for name in declared_functions():
-        assert hasattr(L, name), name
+    for header in (HEADER, LU_HEADER):
+        for name in declared_functions(header):
+            assert hasattr(L, name), name
 
 
 def test_library_is_built_for_sm_103a():
@@ -80,3 +91,21 @@ def test_ref_layout_sizes():
     assert npbmz.ref_elems(npbmz.BT, npbmz.FORCING, 8, 10, 6) == 5 * 9 * 11 * 7
     assert npbmz.ref_elems(npbmz.SP, npbmz.U, 12, 12, 6) == 5 * 17 * 17 * 11
     assert npbmz.ref_elems(npbmz.SP, npbmz.RHS, 12, 12, 6) == 5 * 13 * 13 * 7
+
+
+@pytest.mark.parametrize("cls", list("SWABCD"))
+def test_lu_zone_setup_matches_oracle(npbmz_mod, oracle_mod, cls):
+    from npbmz import lu
+
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES["LU"][cls]
+    a = lu.lu_zone_setup(gx, gy, gz, xz, yz, ratio)
+    b = oracle_mod.lu_zone_setup(gx, gy, gz, xz, yz, ratio)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_lu_zone_setup_rejects_non_integer_extents(npbmz_mod):
+    from npbmz import lu
+
+    with pytest.raises(npbmz.NpbmzError):
+        lu.lu_zone_setup(25, 24, 6, 4, 4)

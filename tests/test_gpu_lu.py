@@ -1,0 +1,173 @@
+"""LU-MZ on the GPU (include/npbmz_lu.h) against the CPU oracle
+(oracle/lumz_oracle.cpp, pinned to the reference's LU-MZ verification norms).
+
+The kernels are built without FMA contraction and follow the reference's
+statements point for point, so u, rsd and frct are compared bit for bit:
+after setup (setbv, setiv, erhs, rhs), after every phase of ssor, and after
+whole iterations, in both exch_qbc plane modes.  Norms (sums in another
+order) are held to 1e-13.  Geometries: LU-MZ classes S and W (4x4 zones of
+6x6x6 and 16x16x8), zones of the minimum size 5x5x5 (where the fourth-
+difference boundary stencils overlap), rectangular 9x7x7 zones, and 2x2
+zones.
+"""
+import numpy as np
+import pytest
+
+import npbmz
+from npbmz import lu
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_lu():
+    from oracle import oracle
+
+    return oracle
+
+
+def make(geom, dt, flags=0):
+    """GPU problem and oracle from the same geometry, both after setup."""
+    o = oracle_lu()
+    nx, ny, nz, nbr = geom
+    p = lu.LuProblem(nx, ny, nz, nbr, dt, flags=flags)
+    p.setup()
+    r = o.LuOracle(nx, ny, nz, nbr, dt, faces_npb=bool(flags & lu.FACES_NPB))
+    return p, r
+
+
+def assert_state_equal(p, r, fields=(lu.U, lu.RSD, lu.FRCT)):
+    for z in range(p.nzones):
+        for f in fields:
+            np.testing.assert_array_equal(p.download(z, f), r.get(f, z), err_msg=f"zone {z} field {f}")
+
+
+GEOMS = {
+    "S": (lambda: lu.lu_zone_setup(24, 24, 6, 4, 4), 0.5),
+    "W": (lambda: lu.lu_zone_setup(64, 64, 8, 4, 4), 1.5e-3),
+    "min5": (lambda: lu.lu_zone_setup(20, 20, 5, 4, 4), 0.5),
+    "rect": (lambda: lu.lu_zone_setup(36, 28, 7, 4, 4), 0.5),
+    "2x2": (lambda: lu.lu_zone_setup(18, 14, 6, 2, 2), 0.5),
+}
+
+
+@pytest.mark.parametrize("name", list(GEOMS))
+def test_setup_is_bit_exact(name):
+    g, dt = GEOMS[name]
+    p, r = make(g(), dt)
+    assert_state_equal(p, r)
+
+
+@pytest.mark.parametrize("name", ["S", "min5", "rect"])
+@pytest.mark.parametrize("faces_npb", [False, True], ids=["ref-faces", "npb-faces"])
+def test_phases_are_bit_exact(name, faces_npb):
+    """Each phase from the same state: exch_qbc, rsd *= dt, jacld + blts,
+    jacu + buts, update, rhs; then a whole ssor."""
+    from oracle import oracle
+
+    g, dt = GEOMS[name]
+    p, r = make(g(), dt, lu.FACES_NPB if faces_npb else 0)
+    for gp, op in [(lu.PHASE_EXCH, oracle.LU_EXCH), (lu.PHASE_SCALE, oracle.LU_SCALE),
+                   (lu.PHASE_LOWER, oracle.LU_LOWER), (lu.PHASE_UPPER, oracle.LU_UPPER),
+                   (lu.PHASE_UPDATE, oracle.LU_UPDATE), (lu.PHASE_RHS, oracle.LU_RHS),
+                   (lu.PHASE_SSOR, oracle.LU_SSOR)]:
+        p.phase(gp)
+        r.phase(op)
+        assert_state_equal(p, r, (lu.U, lu.RSD))
+
+
+@pytest.mark.parametrize("name,niter", [("S", 50), ("W", 40), ("min5", 20), ("rect", 20), ("2x2", 20)])
+@pytest.mark.parametrize("flags", [0, lu.FACES_NPB, lu.FACES_NPB | lu.GRAPH], ids=["ref", "npb", "npb-graph"])
+def test_iterations_are_bit_exact(name, niter, flags):
+    g, dt = GEOMS[name]
+    p, r = make(g(), dt, flags)
+    p.iterate(niter)
+    r.iterate(niter)
+    assert_state_equal(p, r, (lu.U, lu.RSD))
+    a, b = p.verify(), r.verify()
+    np.testing.assert_allclose(a[0], b[0], rtol=1e-13)
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-13)
+    np.testing.assert_allclose(a[2], b[2], rtol=1e-13)
+
+
+def test_per_zone_ssor_equals_batched():
+    g, dt = GEOMS["rect"]
+    a, _ = make(g(), dt, lu.FACES_NPB)
+    b, _ = make(g(), dt, lu.FACES_NPB)
+    for _ in range(3):
+        a.exch_qbc()
+        a.ssor(-1)
+        b.exch_qbc()
+        for z in range(b.nzones):
+            b.ssor(z)
+    for z in range(a.nzones):
+        for f in (lu.U, lu.RSD):
+            np.testing.assert_array_equal(a.download(z, f), b.download(z, f))
+
+
+def test_iteration_norms_match_verify():
+    g, dt = GEOMS["S"]
+    p, _ = make(g(), dt, lu.FACES_NPB | lu.GRAPH)
+    norms = p.iterate(7, norms=True)
+    assert norms.shape == (7, 5) and np.all(norms > 0)
+    xcr, _, _ = p.verify()
+    np.testing.assert_array_equal(norms[-1], xcr)
+
+
+@pytest.mark.parametrize("cls", ["S", "W", "A"])
+def test_go_meets_the_golden_norms(cls):
+    xcr, xce, xci, verified = lu.go(cls)
+    assert verified, (xcr, xce, xci)
+
+
+def test_reference_faces_miss_the_golden_norms_as_the_oracle_does():
+    xcr, _, _, verified = lu.go("S", flags=lu.GRAPH)
+    assert verified is False
+
+
+def test_ref_layout_round_trip_keeps_the_halo():
+    g, dt = GEOMS["rect"]
+    p, r = make(g(), dt)
+    z = 5
+    nx, ny, nz = int(p.nx[z]), int(p.ny[z]), int(p.nz[z])
+    img = np.full(lu.ref_elems(nx, ny, nz), 7.25)
+    p.download(z, lu.U, npbmz.LAYOUT_REF, out=img)
+    a = img.reshape(nz, ny + 4, nx + 4, 5)  # column-major [m, i, j, k] read back to front
+    dense = r.get(lu.U, z)
+    for m in range(5):
+        np.testing.assert_array_equal(a[:, 2:ny + 2, 2:nx + 2, m], dense[m])
+    assert np.all(a[:, :2, :, :] == 7.25) and np.all(a[:, :, :2, :] == 7.25)
+    assert np.all(a[:, ny + 2:, :, :] == 7.25) and np.all(a[:, :, nx + 2:, :] == 7.25)
+    a[:, 2:ny + 2, 2:nx + 2, :] *= 1.5
+    p.upload(z, lu.U, img, npbmz.LAYOUT_REF)
+    np.testing.assert_array_equal(p.download(z, lu.U), dense * 1.5)
+
+
+def test_upload_download_all_zones_dense():
+    g, dt = GEOMS["2x2"]
+    p, r = make(g(), dt)
+    flat = r.get_all(lu.FRCT) * 0.5
+    lu.lib().npbmz_lu_upload(p._h, -1, lu.FRCT, npbmz.LAYOUT_DENSE, flat.ctypes.data)
+    back = np.empty_like(flat)
+    lu.lib().npbmz_lu_download(p._h, -1, lu.FRCT, npbmz.LAYOUT_DENSE, back.ctypes.data)
+    np.testing.assert_array_equal(back, flat)
+
+
+def test_create_rejects_bad_geometry():
+    nx, ny, nz, nbr = lu.lu_zone_setup(16, 16, 6, 4, 4)  # zones 4 wide: below the 5-point stencil
+    with pytest.raises(npbmz.NpbmzError):
+        lu.LuProblem(nx, ny, nz, nbr, 0.5)
+    nx, ny, nz, nbr = lu.lu_zone_setup(24, 24, 6, 4, 4)
+    with pytest.raises(npbmz.NpbmzError):
+        lu.LuProblem(nx, ny, nz, nbr, 0.5, flags=0x80)
+    with pytest.raises(npbmz.NpbmzError):
+        lu.lu_zone_setup(24, 24, 6, 3, 2)  # the reference's neighbour rule leaves the zone range
+
+
+def test_phase_and_zone_errors_are_reported():
+    g, dt = GEOMS["S"]
+    p, _ = make(g(), dt)
+    with pytest.raises(npbmz.NpbmzError, match="phase"):
+        p.phase(17)
+    with pytest.raises(npbmz.NpbmzError, match="zone"):
+        p.ssor(16)
+    assert p.launches_per_iteration() == 4 + 2 * (6 + 6 + 6 - 3 - 6 + 1)
