@@ -1,7 +1,7 @@
 """Benchmark of the GB300 BT-MZ / SP-MZ ADI time step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload bt-c|sp-c|bt-b|sp-a]
+                    [--workload bt-c|sp-c|bt-b|sp-b|sp-a|lu-c|lu-b|lu-a]
 
 A step is one time step of the node loop -- exch_qbc over all zones, then adi
 (compute_rhs, x/y/z line solves, add) over all zones -- on the workload's
@@ -16,6 +16,10 @@ than the 129 MB L2, so no flush is needed); `e2e` is the same metric through
 the C ABI with the reference-layout arrays in page-locked host memory, copied
 in and out every step.  With N > 1 GPUs each rank runs an independent replica
 (the path's only exchange is on-device between zones of one GPU).
+
+The lu-* workloads time LU-MZ's SSOR iteration instead (a step is one
+iteration: exch_qbc + ssor of every zone, src/LU/lu-node.jl:233-270), FP64
+throughout, bit-exact with the oracle, replayed as one CUDA graph.
 """
 from __future__ import annotations
 
@@ -42,7 +46,16 @@ WORKLOADS = {
     "bt-b": ("BT", "B", "BT-MZ 304x208x17, 8x8 geometric zones (area ratio 20.05), dt 3e-4"),
     "sp-b": ("SP", "B", "SP-MZ 304x208x17, 8x8 equal zones (38x26x17), dt 1e-3"),
     "sp-a": ("SP", "A", "SP-MZ 128x128x16, 4x4 equal zones (32x32x16), dt 1.5e-3"),
+    "lu-c": ("LU", "C", "LU-MZ 480x320x28, 4x4 equal zones (120x80x28), dt 2.0, omega 1.2"),
+    "lu-b": ("LU", "B", "LU-MZ 304x208x17, 4x4 equal zones (76x52x17), dt 2.0, omega 1.2"),
+    "lu-a": ("LU", "A", "LU-MZ 128x128x16, 4x4 equal zones (32x32x16), dt 2.0, omega 1.2"),
 }
+# LU-MZ: algorithmic HBM bytes per grid point of each phase (FP64): the
+# sweeps read u and rsd and write rsd, rhs reads u and frct and writes rsd,
+# update reads u and rsd and writes u.
+LU_BYTES_PER_POINT = {"lower": 120.0, "upper": 120.0, "rhs": 120.0, "update": 120.0, "exch": 0.0}
+LU_KERNELS = {"lower": "k_lu_lower<1>", "upper": "k_lu_upper", "rhs": "k_lu_rhs<0>", "update": "k_lu_pointwise<1>",
+              "exch": "k_lu_pack+k_lu_unpack"}
 SEED = 20261203
 # Algorithmic HBM bytes per grid point of each phase (the 600 B/pt-step model:
 # FP64 state, intermediates and line-solve scratch kept out of the count):
@@ -224,6 +237,33 @@ def cpu_baseline(kind, cls, ce, target_s=15.0):
             "sample": f"{n} full time steps of the {kind}-MZ class {cls} grid ({pts} points, all zones) after 1 untimed step"}
 
 
+def lu_cpu_run(cls, warmup, steps):
+    """The LU-MZ oracle on the host cores (OpenMP over zones, like the
+    reference's Threads.@threads): seconds for `steps` iterations after
+    `warmup`, and the point count."""
+    from oracle import oracle
+
+    import npbmz
+
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES["LU"][cls]
+    g = oracle.lu_zone_setup(gx, gy, gz, xz, yz, ratio)
+    pts = int(np.sum(g[0].astype(np.int64) * g[1] * g[2]))
+    o = oracle.LuOracle(*g, dt, faces_npb=False)
+    o.iterate(warmup)
+    t0 = time.perf_counter()
+    o.iterate(steps)
+    return time.perf_counter() - t0, pts, len(g[0])
+
+
+def lu_cpu_baseline(cls, target_s=15.0):
+    t1, pts, _ = lu_cpu_run(cls, 0, 1)
+    n = max(1, min(50, int(target_s / max(t1, 1e-3))))
+    t, pts, _ = lu_cpu_run(cls, 1, n)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": pts * n / t / 1e6, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n} SSOR iterations of the LU-MZ class {cls} grid ({pts} points, all zones) after 1 untimed"}
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -231,6 +271,22 @@ def run_reference(args):
     import npbmz
 
     kind, cls, desc = WORKLOADS[args.workload]
+    if kind == "LU":
+        t, pts, nzones = lu_cpu_run(cls, args.warmup, args.steps)
+        value = pts * args.steps / t / 1e6
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        line = {
+            "impl": "reference", "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "points": pts, "zones": nzones,
+                       "variant": "reference CPU path (LU-MZ oracle port), FP64"},
+            "cpu_baseline": {"value": value, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} SSOR iterations after {args.warmup} warm-up iterations"},
+            "e2e": {"value": value, "unit": "Mgridpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return 0
     niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
     from oracle import oracle
 
@@ -258,11 +314,150 @@ def run_reference(args):
     return 0
 
 
+def run_gpu_lu(args, cls, desc):
+    """LU-MZ: one step = one SSOR iteration of every zone (exch_qbc + ssor)."""
+    import torch
+
+    import npbmz
+    from npbmz import lu
+
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+        dist = tdist
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    flags = lu.GRAPH
+
+    def make(fl):
+        p = lu.LuProblem.from_class(cls, fl)
+        p.set_stream(stream.cuda_stream)
+        p.setup()
+        return p
+
+    p = make(flags)
+    pts = p.points
+
+    def timed(q, steps, warmup):
+        q.iterate(warmup)
+        stream.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        q.iterate(steps)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return e0.elapsed_time(e1)
+
+    with ClockSampler(local) as clk:
+        ms = timed(p, args.steps, args.warmup)
+    ms_max, value = whole_job(ms, pts, args.steps, world, dist)
+    extra = {}
+    if rank == 0 and args.quick:
+        extra["phase_ms"] = p.profile(max(2, min(args.steps, 5)))
+    elif rank == 0:
+        ph = p.profile(max(2, min(args.steps, 5)))
+        extra["phase_ms"] = ph
+        top = max((k for k in ph if k != "exch"), key=lambda k: ph[k])
+        pk = peaks()
+        hbm = float(pk.get("hbm_gbs", 6800.0))
+        achieved = LU_BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
+        fp64 = npbmz.fp64_peak_gflops()
+        km = None
+        try:
+            km = json.loads((ROOT / "profiles" / "ncu_kernel_metrics.json").read_text()).get(args.workload, {}).get("lu")
+        except Exception:
+            km = None
+        kn = LU_KERNELS[top]
+        traffic = fp64_obj = None
+        if km and kn in km:
+            traffic = km[kn]["dram_bytes_per_point"] * pts
+            fl = km[kn]["fp64_flops_per_point"]
+            fa = fl * pts / (ph[top] * 1e-3) / 1e9
+            fp64_obj = {"achieved": fa, "peak": fp64, "unit": "GFLOP/s", "frac": fa / fp64, "flops_per_point": fl,
+                        "pipe_active_ncu": km[kn]["fp64_pipe_active"],
+                        "peak_source": "npbmz_fp64_peak: FP64 FMA chains on this GPU, measured in this run"}
+        extra["roofline"] = {"bound": "hbm", "kernel": kn, "phase": top, "achieved": achieved, "peak": hbm,
+                             "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per point of this "
+                                                "workload's capture (profiles/ncu_kernel_metrics.json), times its points")
+                             if traffic is not None else None,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
+                             "bytes_per_point": LU_BYTES_PER_POINT[top], "launch_ms": ph[top],
+                             "fp64": fp64_obj}
+        extra["fp64_peak_gflops_measured"] = fp64
+        var = {}
+        for name, fl in (("fp64_batched", 0), ("fp64_batched_graph", lu.GRAPH),
+                         ("fp64_batched_graph_npb_faces", lu.GRAPH | lu.FACES_NPB)):
+            q = make(fl)
+            mv = timed(q, max(2, min(args.steps, 5)), 1)
+            var[name] = pts * max(2, min(args.steps, 5)) / (mv * 1e-3) / 1e6
+            q.close()
+        extra["variants_mgridpt_steps_per_s"] = var
+        # e2e through the C ABI: the reference-layout u of every zone in
+        # page-locked host memory, uploaded and downloaded every iteration
+        sizes = [lu.ref_elems(int(p.nx[z]), int(p.ny[z]), int(p.nz[z])) for z in range(p.nzones)]
+        host = torch.empty(int(sum(sizes)), dtype=torch.float64, pin_memory=True)
+        L = lu.lib()
+        ptr = host.data_ptr()
+        assert L.npbmz_lu_download(p._h, -1, lu.U, npbmz.LAYOUT_REF, ptr) == 0
+        for _ in range(args.warmup):
+            assert L.npbmz_lu_upload(p._h, -1, lu.U, npbmz.LAYOUT_REF, ptr) == 0
+            p.iterate(1)
+            assert L.npbmz_lu_download(p._h, -1, lu.U, npbmz.LAYOUT_REF, ptr) == 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            assert L.npbmz_lu_upload(p._h, -1, lu.U, npbmz.LAYOUT_REF, ptr) == 0
+            p.iterate(1)
+            assert L.npbmz_lu_download(p._h, -1, lu.U, npbmz.LAYOUT_REF, ptr) == 0
+        te = time.perf_counter() - t0
+        moved = 8 * int(sum(sizes))
+        extra["e2e"] = {"value": pts * world * args.steps / te / 1e6, "unit": "Mgridpt-steps/s",
+                        "h2d_bytes_per_step": moved, "d2h_bytes_per_step": 2 * moved,
+                        "path": "npbmz_lu_upload + npbmz_lu_iterate(1) + npbmz_lu_download (zone=-1, "
+                                "NPBMZ_LAYOUT_REF) on page-locked reference-layout u; the download copies the "
+                                "host image in first so that the halo is kept"}
+        if not args.no_cpu_baseline:
+            extra["cpu_baseline"] = lu_cpu_baseline(cls)
+    if rank == 0:
+        line = {
+            "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "points_per_gpu": pts, "zones": p.nzones, "variant": "fp64-graph",
+                       "batched": True, "cuda_graph": True, "exch_planes": "reference (k = 1..nz-2)",
+                       "ce": "the reference's table", "l2": f"state {3 * 40 * pts / 1e9:.2f} GB > 129 MB L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "gpu_launches": p.launches_per_iteration() * args.steps,
+            "clocks": clk.summary(),
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    p.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
 def run_gpu(args):
     import torch
 
     import npbmz
 
+    kind_, cls_, desc_ = WORKLOADS[args.workload]
+    if kind_ == "LU":
+        return run_gpu_lu(args, cls_, desc_)
     rank, world, local = env_rank()
     dist = None
     if world > 1:
