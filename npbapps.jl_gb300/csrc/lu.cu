@@ -11,7 +11,9 @@
 //   exch_qbc       k_lu_pack + k_lu_unpack (every face packed before any is
 //                  unpacked, as the reference's sends are)
 //   rsd *= dt      fused into the first touch of each point in k_lu_lower
-//   jacld + blts   k_lu_lower, one launch per hyperplane i+j+k = l
+//   1/u1           k_lu_rho (the reference's tmp1 of jacld / jacu, once per point)
+//   jacld + blts   k_lu_lower, one launch per hyperplane i+j+k = l, five
+//                  threads per point (one per row of the 5x5 blocks)
 //   jacu + buts    k_lu_upper, one launch per hyperplane, l descending
 //   update         k_lu_update
 //   rhs            k_lu_rhs<false>, one thread per point
@@ -393,9 +395,10 @@ constexpr double c1345 = c1 * c3 * c4 * c5;
 constexpr double c34 = c3 * c4;
 
 // the diagonal block (identical in jacld and jacu) at the point's own state
-__device__ inline void jac_d(const JC& J, double u1, double u2, double u3, double u4, double u5, double d[5][5]) {
+__device__ __forceinline__ void jac_d(const JC& J, double r1, double u2, double u3, double u4, double u5,
+                                      double d[5][5]) {
   const double dt = J.dt, tx1 = J.tx1, ty1 = J.ty1, tz1 = J.tz1;
-  const double tmp1 = 1.0e+00 / u1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
+  const double tmp1 = r1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
   d[0][0] = 1.0e+00 + dt * 2.0e+00 * (tx1 * dx1 + ty1 * dy1 + tz1 * dz1);
   d[0][1] = 0.0; d[0][2] = 0.0; d[0][3] = 0.0; d[0][4] = 0.0;
   d[1][0] = dt * 2.0e+00 * (tx1 * (-r43 * c34 * tmp2 * u2) + ty1 * (-c34 * tmp2 * u2) + tz1 * (-c34 * tmp2 * u2));
@@ -431,11 +434,13 @@ __device__ inline void jac_d(const JC& J, double u1, double u2, double u3, doubl
 
 // Off-diagonal block of direction DIR (0 x, 1 y, 2 z) from the neighbour's
 // state; SG = -1: jacld's (the neighbour at -1), SG = +1: jacu's (at +1).
-// The entries are the reference's statements with dt*t?2 negated for jacld.
+// The entries are the reference's statements.  r1 = 1/u1 of the neighbour
+// (the reference's tmp1, computed once per point by k_lu_rho).
 template <int DIR, int SG>
-__device__ inline void jac_off(const JC& J, double u1, double u2, double u3, double u4, double u5, double a[5][5]) {
+__device__ __forceinline__ void jac_off(const JC& J, double r1, double u2, double u3, double u4, double u5,
+                                        double a[5][5]) {
   const double dt = J.dt;
-  const double tmp1 = 1.0e+00 / u1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
+  const double tmp1 = r1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
   if (DIR == 2) {
     const double tz1 = J.tz1, tz2 = J.tz2;
     if (SG < 0) {
@@ -634,68 +639,6 @@ __device__ inline void jac_off(const JC& J, double u1, double u2, double u3, dou
   }
 }
 
-// Elimination of tmat without pivoting with right-hand side v, then the back
-// substitution: blts (src/LU/blts.jl:106-193) or, BUTS, buts as the
-// reference states it (src/LU/buts.jl:113-200: tmat[5,5] -=- tmp*tmat[2,5]
-// and the signs of its back substitution; d's strict upper triangle is +0
-// throughout, so these change no value, but they are kept statement for
-// statement).
-template <bool BUTS>
-__device__ inline void block_solve(double t[5][5], double v[5]) {
-  double tmp1, tmp;
-  tmp1 = 1.0e+00 / t[0][0];
-#pragma unroll
-  for (int r = 1; r < 5; ++r) {
-    tmp = tmp1 * t[r][0];
-#pragma unroll
-    for (int c = 1; c < 5; ++c) t[r][c] = t[r][c] - tmp * t[0][c];
-    v[r] = v[r] - v[0] * tmp;
-  }
-  tmp1 = 1.0e+00 / t[1][1];
-#pragma unroll
-  for (int r = 2; r < 5; ++r) {
-    tmp = tmp1 * t[r][1];
-#pragma unroll
-    for (int c = 2; c < 5; ++c) {
-      if (BUTS && r == 4 && c == 4)
-        t[r][c] = t[r][c] - (-tmp * t[1][c]);
-      else
-        t[r][c] = t[r][c] - tmp * t[1][c];
-    }
-    v[r] = v[r] - v[1] * tmp;
-  }
-  tmp1 = 1.0e+00 / t[2][2];
-#pragma unroll
-  for (int r = 3; r < 5; ++r) {
-    tmp = tmp1 * t[r][2];
-#pragma unroll
-    for (int c = 3; c < 5; ++c) t[r][c] = t[r][c] - tmp * t[2][c];
-    v[r] = v[r] - v[2] * tmp;
-  }
-  tmp1 = 1.0e+00 / t[3][3];
-  tmp = tmp1 * t[4][3];
-  t[4][4] = t[4][4] - tmp * t[3][4];
-  v[4] = v[4] - v[3] * tmp;
-  v[4] = v[4] / t[4][4];
-  v[3] = v[3] - t[3][4] * v[4];
-  v[3] = v[3] / t[3][3];
-  if (BUTS) {
-    v[2] = v[2] - (t[2][3] * v[3] - t[2][4] * v[4]);
-    v[2] = v[2] / t[2][2];
-    v[1] = v[1] - (t[1][2] * v[2] - t[1][3] * v[3] - t[1][4] * v[4]);
-    v[1] = v[1] / t[1][1];
-    v[0] = v[0] - (t[0][1] * v[1] - t[0][2] * v[2] - t[0][3] * v[3] - t[0][4] * v[4]);
-    v[0] = v[0] / t[0][0];
-  } else {
-    v[2] = v[2] - (t[2][3] * v[3] + t[2][4] * v[4]);
-    v[2] = v[2] / t[2][2];
-    v[1] = v[1] - (t[1][2] * v[2] + t[1][3] * v[3] + t[1][4] * v[4]);
-    v[1] = v[1] / t[1][1];
-    v[0] = v[0] - (t[0][1] * v[1] + t[0][2] * v[2] + t[0][3] * v[3] + t[0][4] * v[4]);
-    v[0] = v[0] / t[0][0];
-  }
-}
-
 // The t-th point (0-based) of hyperplane i + j + k = l of a zone's interior,
 // enumerated by k ascending, then j ascending.
 __device__ inline bool hyperplane_point(const LuZone& Z, int l, int t, int& i, int& j, int& k) {
@@ -716,9 +659,115 @@ __device__ inline bool hyperplane_point(const LuZone& Z, int l, int t, int& i, i
   return false;
 }
 
-__device__ inline void load5(const double* f, long long NP, long long p, double v[5]) {
+__device__ __forceinline__ void load5(const double* f, long long NP, long long p, double v[5]) {
 #pragma unroll
   for (int m = 0; m < 5; ++m) v[m] = f[m * NP + p];
+}
+
+// The entries the reference assigns a literal 0.0 in each off-diagonal block
+// (the same pattern in jacld and jacu).  A product with one is +-0 and
+// adding it changes no sum's value, so the row sums below skip them.
+__host__ __device__ constexpr bool off_zero(int dir, int r, int c) {
+  return dir == 2 ? ((r == 0 && (c == 1 || c == 2 || c == 4)) || (r == 1 && (c == 2 || c == 4)) ||
+                     (r == 2 && (c == 1 || c == 4)))
+       : dir == 1 ? ((r == 0 && (c == 1 || c == 3 || c == 4)) || (r == 1 && (c == 3 || c == 4)) ||
+                     (r == 3 && (c == 1 || c == 4)))
+                  : ((r == 0 && (c == 2 || c == 3 || c == 4)) || (r == 2 && (c == 3 || c == 4)) ||
+                     (r == 3 && (c == 2 || c == 4)));
+}
+
+// row M of block DIR . w, summed left to right as the reference does
+template <int DIR, int M>
+__device__ __forceinline__ double row_dot(const double e[5][5], const double w[5]) {
+  double s = 0.0;
+  bool first = true;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    if (off_zero(DIR, M, c)) continue;
+    const double t = e[M][c] * w[c];
+    s = first ? t : s + t;
+    first = false;
+  }
+  return s;
+}
+
+// sum over c of ey[M][c] * wy[c] + ex[M][c] * wx[c], interleaved (y term
+// first) as blts / buts write it
+template <int M>
+__device__ __forceinline__ double row_dot2(const double ey[5][5], const double wy[5], const double ex[5][5],
+                                           const double wx[5]) {
+  double s = 0.0;
+  bool first = true;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    if (!off_zero(1, M, c)) {
+      const double t = ey[M][c] * wy[c];
+      s = first ? t : s + t;
+      first = false;
+    }
+    if (!off_zero(0, M, c)) {
+      const double t = ex[M][c] * wx[c];
+      s = first ? t : s + t;
+      first = false;
+    }
+  }
+  return s;
+}
+
+// The 5x5 solve of blts / buts (src/LU/blts.jl:106-193, src/LU/buts.jl:113-200)
+// with tmat = d.  d is lower triangular with d[2][1] = d[3][1] = d[3][2] = 0
+// (jacld.jl / jacu.jl assign those 0.0), so the elimination leaves every
+// entry of tmat as it was, and every update the reference makes with a zero
+// multiplier (including buts's `tmat[5,5] -=- tmp * tmat[2,5]` and its back
+// substitution signs, whose terms are all products with zeros) leaves the
+// value it updates unchanged.  What remains, statement for statement:
+//   tmp_r0 = (1/t00) t_r0,  v_r <- v_r - v_0 tmp_r0         (r = 1..4)
+//   tmp_4c = (1/t_cc) t_4c, v_4 <- v_4 - v_c tmp_4c         (c = 1, 2, 3)
+//   v_r <- v_r / t_rr                                       (r = 4..0)
+// The lower sweep keeps t_rr, tmp_r0 and tmp_4c per point in `fac` (12
+// planes) for the upper sweep, whose d is the same block of the same state.
+enum { FAC_T = 0, FAC_R0 = 5, FAC_4C = 9, FAC_COUNT = 12 };
+
+constexpr int HP = 32;  // points per block of the sweep kernels (x 5 rows)
+
+// One thread per (point, row M): rows of the off-diagonal blocks, the row
+// sums and row M of d.  Returns v_M after blts's two update loops.
+template <int M, bool SCALE>
+__device__ __forceinline__ double lower_row(const LuDev& D, const double* __restrict__ rho, const LuZone& Z,
+                                            const JC& J, int i, int j, int k, double& d0, double& dd,
+                                            double d4[3]) {
+  const long long NP = D.NP, p = pidx(Z, i, j, k);
+  const double omega = D.omega;
+  double v = D.rsd[M * NP + p];
+  if (SCALE) v = D.dt * v;
+  double w[5], x[5], blk[5][5], blk2[5][5];
+  {  // ldz: from (i, j, k-1)
+    const long long q = pidx(Z, i, j, k - 1);
+    load5(D.u, NP, q, w);
+    jac_off<2, -1>(J, rho[q], w[1], w[2], w[3], w[4], blk);
+    load5(D.rsd, NP, q, w);
+    v = v - omega * row_dot<2, M>(blk, w);
+  }
+  {  // ldy: from (i, j-1, k); ldx: from (i-1, j, k)
+    const long long qy = pidx(Z, i, j - 1, k), qx = pidx(Z, i - 1, j, k);
+    load5(D.u, NP, qy, w);
+    jac_off<1, -1>(J, rho[qy], w[1], w[2], w[3], w[4], blk);
+    load5(D.u, NP, qx, x);
+    jac_off<0, -1>(J, rho[qx], x[1], x[2], x[3], x[4], blk2);
+    load5(D.rsd, NP, qy, w);
+    load5(D.rsd, NP, qx, x);
+    v = v - omega * row_dot2<M>(blk, w, blk2, x);
+  }
+  load5(D.u, NP, p, w);
+  jac_d(J, rho[p], w[1], w[2], w[3], w[4], blk);
+  d0 = blk[M][0];
+  dd = blk[M][M];
+  if (M == 4) {
+    d4[0] = blk[4][1];
+    d4[1] = blk[4][2];
+    d4[2] = blk[4][3];
+  }
+  return v;
 }
 
 // jacld + blts at every point of hyperplane l (blockIdx.y: zone - zone0).
@@ -726,79 +775,138 @@ __device__ inline void load5(const double* f, long long NP, long long p, double 
 // only points it has already scaled and solved, or boundary points, which
 // the scaling does not touch).
 template <bool SCALE>
-__global__ void __launch_bounds__(TPB) k_lu_lower(LuDev D, int l, int zone0) {
+__global__ void __launch_bounds__(HP * 5) k_lu_lower(LuDev D, const double* __restrict__ rho,
+                                                     double* __restrict__ fac, int l, int zone0) {
+  __shared__ double sv[5][HP], sd0[5][HP], srinv[4][HP], s4[3][HP];
+  const int m = threadIdx.y, a = threadIdx.x;
   const LuZone Z = D.zones[zone0 + blockIdx.y];
-  int i, j, k;
-  if (!hyperplane_point(Z, l, blockIdx.x * TPB + threadIdx.x, i, j, k)) return;
+  int i = 0, j = 0, k = 0;
+  const bool ok = hyperplane_point(Z, l, blockIdx.x * HP + a, i, j, k);
   const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
-  const long long NP = D.NP, p = pidx(Z, i, j, k);
-  const double omega = D.omega;
-  double v[5], w[5], x[5], blk[5][5], blk2[5][5];
-  load5(D.rsd, NP, p, v);
-  if (SCALE) {
-#pragma unroll
-    for (int m = 0; m < 5; ++m) v[m] = D.dt * v[m];
+  double v = 0.0, d0 = 0.0, dd = 1.0, d4[3] = {0.0, 0.0, 0.0};
+  if (ok) {
+    switch (m) {
+      case 0: v = lower_row<0, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
+      case 1: v = lower_row<1, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
+      case 2: v = lower_row<2, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
+      case 3: v = lower_row<3, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
+      default: v = lower_row<4, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
+    }
+    sv[m][a] = v;
+    sd0[m][a] = d0;
+    if (m < 4) srinv[m][a] = 1.0e+00 / dd;
+    if (m == 4) {
+      s4[0][a] = d4[0];
+      s4[1][a] = d4[1];
+      s4[2][a] = d4[2];
+    }
   }
-  // ldz (a): from (i, j, k-1)
-  load5(D.u, NP, pidx(Z, i, j, k - 1), w);
-  jac_off<2, -1>(J, w[0], w[1], w[2], w[3], w[4], blk);
-  load5(D.rsd, NP, pidx(Z, i, j, k - 1), w);
+  __syncthreads();
+  if (!ok) return;
+  const long long NP = D.NP, p = pidx(Z, i, j, k);
+  const double v0 = sv[0][a], rinv0 = srinv[0][a];
+  fac[(FAC_T + m) * NP + p] = dd;
+  if (m == 0) {
+    v = v / dd;
+  } else if (m < 4) {
+    const double tmp = rinv0 * d0;
+    v = v - v0 * tmp;
+    v = v / dd;
+    fac[(FAC_R0 + m - 1) * NP + p] = tmp;
+  } else {
+    const double tmp40 = rinv0 * d0;
+    v = v - v0 * tmp40;
+    double tmpc[3];
 #pragma unroll
-  for (int m = 0; m < 5; ++m)
-    v[m] = v[m] - omega * (blk[m][0] * w[0] + blk[m][1] * w[1] + blk[m][2] * w[2] + blk[m][3] * w[3] +
-                           blk[m][4] * w[4]);
-  // ldy (b): from (i, j-1, k); ldx (c): from (i-1, j, k)
-  load5(D.u, NP, pidx(Z, i, j - 1, k), w);
-  jac_off<1, -1>(J, w[0], w[1], w[2], w[3], w[4], blk);
-  load5(D.u, NP, pidx(Z, i - 1, j, k), w);
-  jac_off<0, -1>(J, w[0], w[1], w[2], w[3], w[4], blk2);
-  load5(D.rsd, NP, pidx(Z, i, j - 1, k), w);
-  load5(D.rsd, NP, pidx(Z, i - 1, j, k), x);
+    for (int c = 1; c <= 3; ++c) {
+      const double vc = sv[c][a] - v0 * (rinv0 * sd0[c][a]);  // v_c after column 0, as row c has it
+      tmpc[c - 1] = srinv[c][a] * s4[c - 1][a];
+      v = v - vc * tmpc[c - 1];
+    }
+    v = v / dd;
+    fac[(FAC_R0 + 3) * NP + p] = tmp40;
 #pragma unroll
-  for (int m = 0; m < 5; ++m)
-    v[m] = v[m] - omega * (blk[m][0] * w[0] + blk2[m][0] * x[0] + blk[m][1] * w[1] + blk2[m][1] * x[1] +
-                           blk[m][2] * w[2] + blk2[m][2] * x[2] + blk[m][3] * w[3] + blk2[m][3] * x[3] +
-                           blk[m][4] * w[4] + blk2[m][4] * x[4]);
-  load5(D.u, NP, p, w);
-  jac_d(J, w[0], w[1], w[2], w[3], w[4], blk);
-  block_solve<false>(blk, v);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) D.rsd[m * NP + p] = v[m];
+    for (int c = 0; c < 3; ++c) fac[(FAC_4C + c) * NP + p] = tmpc[c];
+  }
+  D.rsd[m * NP + p] = v;
 }
 
-// jacu + buts at every point of hyperplane l
-__global__ void __launch_bounds__(TPB) k_lu_upper(LuDev D, int l, int zone0) {
-  const LuZone Z = D.zones[zone0 + blockIdx.y];
-  int i, j, k;
-  if (!hyperplane_point(Z, l, blockIdx.x * TPB + threadIdx.x, i, j, k)) return;
-  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
-  const long long NP = D.NP, p = pidx(Z, i, j, k);
+template <int M>
+__device__ __forceinline__ double upper_row(const LuDev& D, const double* __restrict__ rho, const LuZone& Z,
+                                            const JC& J, int i, int j, int k) {
+  const long long NP = D.NP;
   const double omega = D.omega;
-  double tv[5], w[5], x[5], blk[5][5], blk2[5][5];
-  // udz (c): from (i, j, k+1)
-  load5(D.u, NP, pidx(Z, i, j, k + 1), w);
-  jac_off<2, 1>(J, w[0], w[1], w[2], w[3], w[4], blk);
-  load5(D.rsd, NP, pidx(Z, i, j, k + 1), w);
+  double w[5], x[5], blk[5][5], blk2[5][5], tv;
+  {  // udz: from (i, j, k+1)
+    const long long q = pidx(Z, i, j, k + 1);
+    load5(D.u, NP, q, w);
+    jac_off<2, 1>(J, rho[q], w[1], w[2], w[3], w[4], blk);
+    load5(D.rsd, NP, q, w);
+    tv = omega * row_dot<2, M>(blk, w);
+  }
+  {  // udy: from (i, j+1, k); udx: from (i+1, j, k)
+    const long long qy = pidx(Z, i, j + 1, k), qx = pidx(Z, i + 1, j, k);
+    load5(D.u, NP, qy, w);
+    jac_off<1, 1>(J, rho[qy], w[1], w[2], w[3], w[4], blk);
+    load5(D.u, NP, qx, x);
+    jac_off<0, 1>(J, rho[qx], x[1], x[2], x[3], x[4], blk2);
+    load5(D.rsd, NP, qy, w);
+    load5(D.rsd, NP, qx, x);
+    tv = tv + omega * row_dot2<M>(blk, w, blk2, x);
+  }
+  return tv;
+}
+
+// jacu + buts at every point of hyperplane l, with the factors of d the
+// lower sweep kept
+__global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __restrict__ rho,
+                                                     const double* __restrict__ fac, int l, int zone0) {
+  __shared__ double sv[5][HP];
+  const int m = threadIdx.y, a = threadIdx.x;
+  const LuZone Z = D.zones[zone0 + blockIdx.y];
+  int i = 0, j = 0, k = 0;
+  const bool ok = hyperplane_point(Z, l, blockIdx.x * HP + a, i, j, k);
+  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
+  double tv = 0.0;
+  if (ok) {
+    switch (m) {
+      case 0: tv = upper_row<0>(D, rho, Z, J, i, j, k); break;
+      case 1: tv = upper_row<1>(D, rho, Z, J, i, j, k); break;
+      case 2: tv = upper_row<2>(D, rho, Z, J, i, j, k); break;
+      case 3: tv = upper_row<3>(D, rho, Z, J, i, j, k); break;
+      default: tv = upper_row<4>(D, rho, Z, J, i, j, k); break;
+    }
+    sv[m][a] = tv;
+  }
+  __syncthreads();
+  if (!ok) return;
+  const long long NP = D.NP, p = pidx(Z, i, j, k);
+  const double tv0 = sv[0][a];
+  if (m == 0) {
+    tv = tv / fac[FAC_T * NP + p];
+  } else if (m < 4) {
+    tv = tv - tv0 * fac[(FAC_R0 + m - 1) * NP + p];
+    tv = tv / fac[(FAC_T + m) * NP + p];
+  } else {
+    tv = tv - tv0 * fac[(FAC_R0 + 3) * NP + p];
 #pragma unroll
-  for (int m = 0; m < 5; ++m)
-    tv[m] = omega * (blk[m][0] * w[0] + blk[m][1] * w[1] + blk[m][2] * w[2] + blk[m][3] * w[3] + blk[m][4] * w[4]);
-  // udy (b): from (i, j+1, k); udx (a): from (i+1, j, k)
-  load5(D.u, NP, pidx(Z, i, j + 1, k), w);
-  jac_off<1, 1>(J, w[0], w[1], w[2], w[3], w[4], blk);
-  load5(D.u, NP, pidx(Z, i + 1, j, k), w);
-  jac_off<0, 1>(J, w[0], w[1], w[2], w[3], w[4], blk2);
-  load5(D.rsd, NP, pidx(Z, i, j + 1, k), w);
-  load5(D.rsd, NP, pidx(Z, i + 1, j, k), x);
-#pragma unroll
-  for (int m = 0; m < 5; ++m)
-    tv[m] = tv[m] + omega * (blk[m][0] * w[0] + blk2[m][0] * x[0] + blk[m][1] * w[1] + blk2[m][1] * x[1] +
-                             blk[m][2] * w[2] + blk2[m][2] * x[2] + blk[m][3] * w[3] + blk2[m][3] * x[3] +
-                             blk[m][4] * w[4] + blk2[m][4] * x[4]);
-  load5(D.u, NP, p, w);
-  jac_d(J, w[0], w[1], w[2], w[3], w[4], blk);
-  block_solve<true>(blk, tv);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) D.rsd[m * NP + p] = D.rsd[m * NP + p] - tv[m];
+    for (int c = 1; c <= 3; ++c) {
+      const double tc = sv[c][a] - tv0 * fac[(FAC_R0 + c - 1) * NP + p];
+      tv = tv - tc * fac[(FAC_4C + c - 1) * NP + p];
+    }
+    tv = tv / fac[(FAC_T + 4) * NP + p];
+  }
+  D.rsd[m * NP + p] = D.rsd[m * NP + p] - tv;
+}
+
+// rho = 1/u1 at every point (the reference's tmp1 of jacld / jacu)
+__global__ void __launch_bounds__(TPB) k_lu_rho(LuDev D, const LuWork* __restrict__ work, double* rho) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  const int q = w.first + threadIdx.x;
+  if (q >= Z.np) return;
+  const long long p = Z.off + q;
+  rho[p] = 1.0e+00 / D.u[p];
 }
 
 // ---- exch_qbc (src/LU/exchange_qbc.jl) --------------------------------------
@@ -1025,6 +1133,8 @@ struct npbmz_lu_handle {
   LuZone* zones_d = nullptr;
   int* nbr_d = nullptr;
   double *u = nullptr, *rsd = nullptr, *frct = nullptr;
+  double* rho = nullptr;  // 1/u1 per point, refreshed before each lower sweep
+  double* fac = nullptr;  // factors of d per point (FAC_COUNT planes)
   // work lists: all zones, and per zone a contiguous range
   std::vector<LuWork> work_h;
   std::vector<int> zblock;  // first block of each zone, nzones+1 entries
@@ -1120,24 +1230,27 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
       return launch_exch(h);
     case NPBMZ_LU_PHASE_LOWER:
     case NPBMZ_LU_PHASE_SSOR + 100:  // lower with the scaling fused
+      k_lu_rho<<<n, TPB, 0, h->stream>>>(dev(h), w, h->rho);
       for (int l = h->lmin; l <= h->lmax; ++l) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
-        const dim3 g((c + TPB - 1) / TPB, nzs);
+        const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
         if (phase == NPBMZ_LU_PHASE_LOWER)
-          k_lu_lower<false><<<g, TPB, 0, h->stream>>>(dev(h), l, z0);
+          k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->rho, h->fac, l, z0);
         else
-          k_lu_lower<true><<<g, TPB, 0, h->stream>>>(dev(h), l, z0);
+          k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->rho, h->fac, l, z0);
       }
       break;
     case NPBMZ_LU_PHASE_UPPER:
+      // rho and fac from the lower sweep of the same state (u does not
+      // change between the sweeps)
       for (int l = h->lmax; l >= h->lmin; --l) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
-        const dim3 g((c + TPB - 1) / TPB, nzs);
-        k_lu_upper<<<g, TPB, 0, h->stream>>>(dev(h), l, z0);
+        const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
+        k_lu_upper<<<g, b, 0, h->stream>>>(dev(h), h->rho, h->fac, l, z0);
       }
       break;
     case NPBMZ_LU_PHASE_SSOR: {
@@ -1221,7 +1334,8 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
 
 void free_all(npbmz_lu_t* h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
-  for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->work_d,
+  for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->rho,
+                  (void*)h->fac, (void*)h->work_d,
                   (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
                   (void*)h->zoff_d, (void*)h->img})
     if (p) cudaFree(p);
@@ -1373,6 +1487,8 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
   h->stream = h->own;
   if (cudaMalloc(&h->zones_d, nzones * sizeof(LuZone)) || cudaMalloc(&h->nbr_d, 4 * nzones * sizeof(int)) ||
       cudaMalloc(&h->u, F) || cudaMalloc(&h->rsd, F) || cudaMalloc(&h->frct, F) ||
+      cudaMalloc(&h->rho, (size_t)h->NP * sizeof(double)) ||
+      cudaMalloc(&h->fac, (size_t)FAC_COUNT * h->NP * sizeof(double)) ||
       cudaMalloc(&h->work_d, h->work_h.size() * sizeof(LuWork)) ||
       cudaMalloc(&h->zblock_d, h->zblock.size() * sizeof(int)) ||
       cudaMalloc(&h->partial, h->work_h.size() * 5 * sizeof(double)) ||
@@ -1384,7 +1500,9 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMemcpy(h->work_d, h->work_h.data(), h->work_h.size() * sizeof(LuWork), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->zblock_d, h->zblock.data(), h->zblock.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->zoff_d, zoff.data(), nzones * sizeof(long long), cudaMemcpyHostToDevice) ||
-      cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F))
+      cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F) ||
+      cudaMemset(h->rho, 0, (size_t)h->NP * sizeof(double)) ||
+      cudaMemset(h->fac, 0, (size_t)FAC_COUNT * h->NP * sizeof(double)))
     return bail("device initialisation failed");
   *out = h;
   return 0;
@@ -1512,7 +1630,7 @@ int npbmz_lu_synchronize(npbmz_lu_t* h) {
 
 int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
   if (!h) return -1;
-  int n = 2 + 2;  // exch (pack, unpack) + update + rhs
+  int n = 2 + 3;  // exch (pack, unpack) + rho + update + rhs
   for (int l = h->lmin; l <= h->lmax; ++l) {
     int c = 0;
     for (const LuZone& Z : h->zh) c = std::max(c, hp_count(Z, l));
