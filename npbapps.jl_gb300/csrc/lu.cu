@@ -11,7 +11,10 @@
 //   exch_qbc       k_lu_pack + k_lu_unpack (every face packed before any is
 //                  unpacked, as the reference's sends are)
 //   rsd *= dt      fused into the first touch of each point in k_lu_lower
-//   1/u1           k_lu_rho (the reference's tmp1 of jacld / jacu, once per point)
+//   flux prims     per-point quantities of the flux functions (1/u1, the
+//                  viscous u21.., the convective u21 and q), refreshed where
+//                  u changes: k_lu_unpack (ghost faces), k_lu_pointwise<1>
+//                  (update), uploads; read by the sweeps and rhs
 //   jacld + blts   k_lu_lower, one launch per hyperplane i+j+k = l, five
 //                  threads per point (one per row of the 5x5 blocks)
 //   jacu + buts    k_lu_upper, one launch per hyperplane, l descending
@@ -69,6 +72,7 @@ struct LuDev {
   double* u;
   double* rsd;
   double* frct;
+  double* prim;  // PR_COUNT planes of per-point flux quantities of u
   long long NP;
   const LuZone* zones;
   double dt, omega;
@@ -105,47 +109,94 @@ __device__ inline double visc_up(double o, double a, double b) {
   return ERHS ? (o + a) + b : o + (a + b);
 }
 
+// Per-point quantities of the flux functions (planes of `prim`), each the
+// reference's own expression evaluated once per point instead of once per
+// use (rhs.jl and erhs.jl evaluate them at every neighbour):
+//   PR_RHO  1/g1                          (the viscous tmp, jacld's tmp1)
+//   PR_U21..PR_U51  tmp*g2 .. tmp*g5      (the viscous u21i .. u51i)
+//   PR_S    u21^2 + u31^2 + u41^2         (their sum of squares)
+//   PR_C21, PR_C31, PR_C41  g2/g1, g3/g1, g4/g1  (the convective u21, u31, u41)
+//   PR_Q    0.5 (g2^2 + g3^2 + g4^2) / g1 (the convective q)
+enum { PR_RHO = 0, PR_U21, PR_U31, PR_U41, PR_U51, PR_S, PR_C21, PR_C31, PR_C41, PR_Q, PR_COUNT };
+
+__device__ __forceinline__ void prim_point(const double g[5], double pr[PR_COUNT]) {
+  const double tmp = 1.0e+00 / g[0];
+  pr[PR_RHO] = tmp;
+  pr[PR_U21] = tmp * g[1];
+  pr[PR_U31] = tmp * g[2];
+  pr[PR_U41] = tmp * g[3];
+  pr[PR_U51] = tmp * g[4];
+  pr[PR_S] = pr[PR_U21] * pr[PR_U21] + pr[PR_U31] * pr[PR_U31] + pr[PR_U41] * pr[PR_U41];
+  pr[PR_C21] = g[1] / g[0];
+  pr[PR_C31] = g[2] / g[0];
+  pr[PR_C41] = g[3] / g[0];
+  pr[PR_Q] = 0.50e+00 * (g[1] * g[1] + g[2] * g[2] + g[3] * g[3]) / g[0];
+}
+
+__device__ __forceinline__ void store_prim(double* prim, long long NP, long long p, const double g[5]) {
+  double pr[PR_COUNT];
+  prim_point(g, pr);
+#pragma unroll
+  for (int q = 0; q < PR_COUNT; ++q) prim[q * NP + p] = pr[q];
+}
+
 template <bool ERHS>
-__device__ void flux_point(const double* __restrict__ g, long long NP, const LuZone& Z, int i, int j, int k,
-                           double o[5]) {
+__device__ void flux_point(const double* __restrict__ g, const double* __restrict__ prim, long long NP,
+                           const LuZone& Z, int i, int j, int k, double o[5]) {
   const int nx = Z.nx, ny = Z.ny, nz = Z.nz;
   auto G = [&](int m, int ii, int jj, int kk) -> double { return g[m * NP + pidx(Z, ii, jj, kk)]; };
+  auto P = [&](int q, int ii, int jj, int kk) -> double { return prim[q * NP + pidx(Z, ii, jj, kk)]; };
   const double tx1 = Z.tx1, tx2 = Z.tx2, tx3 = Z.tx3, ty1 = Z.ty1, ty2 = Z.ty2, ty3 = Z.ty3, tz1 = Z.tz1,
                tz2 = Z.tz2, tz3 = Z.tz3;
-  // ---------------- xi ----------------
-  {
-    double fp[5], fm[5];
-    auto conv = [&](int ii, double f[5]) {
-      const double g1 = G(0, ii, j, k), g2 = G(1, ii, j, k), g3 = G(2, ii, j, k), g4 = G(3, ii, j, k),
-                   g5 = G(4, ii, j, k);
+  // convective flux of direction D (0 x, 1 y, 2 z) at a point
+  auto conv = [&](int D, int ii, int jj, int kk, double f[5]) {
+    const double g2 = G(1, ii, jj, kk), g3 = G(2, ii, jj, kk), g4 = G(3, ii, jj, kk), g5 = G(4, ii, jj, kk);
+    const double q = P(PR_Q, ii, jj, kk);
+    if (D == 0) {
+      const double u21 = P(PR_C21, ii, jj, kk);
       f[0] = g2;
-      const double u21 = g2 / g1;
-      const double q = 0.50e+00 * (g2 * g2 + g3 * g3 + g4 * g4) / g1;
       f[1] = g2 * u21 + c2 * (g5 - q);
       f[2] = g3 * u21;
       f[3] = g4 * u21;
       f[4] = (c1 * g5 - c2 * q) * u21;
-    };
-    conv(i + 1, fp);
-    conv(i - 1, fm);
+    } else if (D == 1) {
+      const double u31 = P(PR_C31, ii, jj, kk);
+      f[0] = g3;
+      f[1] = g2 * u31;
+      f[2] = g3 * u31 + c2 * (g5 - q);
+      f[3] = g4 * u31;
+      f[4] = (c1 * g5 - c2 * q) * u31;
+    } else {
+      const double u41 = P(PR_C41, ii, jj, kk);
+      f[0] = g4;
+      f[1] = g2 * u41;
+      f[2] = g3 * u41;
+      f[3] = g4 * u41 + c2 * (g5 - q);
+      f[4] = (c1 * g5 - c2 * q) * u41;
+    }
+  };
+  // viscous flux of direction D between point b (the - side) and point a
+  auto visc = [&](int D, double t3, int ai, int aj, int ak, int bi, int bj, int bk, double f[5]) {
+    const double u21i = P(PR_U21, ai, aj, ak), u31i = P(PR_U31, ai, aj, ak), u41i = P(PR_U41, ai, aj, ak),
+                 u51i = P(PR_U51, ai, aj, ak), si = P(PR_S, ai, aj, ak);
+    const double u21m = P(PR_U21, bi, bj, bk), u31m = P(PR_U31, bi, bj, bk), u41m = P(PR_U41, bi, bj, bk),
+                 u51m = P(PR_U51, bi, bj, bk), sm = P(PR_S, bi, bj, bk);
+    f[1] = (D == 0 ? (4.0e+00 / 3.0e+00) * t3 : t3) * (u21i - u21m);
+    f[2] = (D == 1 ? (4.0e+00 / 3.0e+00) * t3 : t3) * (u31i - u31m);
+    f[3] = (D == 2 ? (4.0e+00 / 3.0e+00) * t3 : t3) * (u41i - u41m);
+    const double ui = D == 0 ? u21i : (D == 1 ? u31i : u41i), um = D == 0 ? u21m : (D == 1 ? u31m : u41m);
+    f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * t3 * (si - sm) + (1.0e+00 / 6.0e+00) * t3 * (ui * ui - um * um) +
+           c1 * c5 * t3 * (u51i - u51m);
+  };
+  // ---------------- xi ----------------
+  {
+    double fp[5], fm[5];
+    conv(0, i + 1, j, k, fp);
+    conv(0, i - 1, j, k, fm);
 #pragma unroll
     for (int m = 0; m < 5; ++m) o[m] = o[m] - tx2 * (fp[m] - fm[m]);
-    auto visc = [&](int ii, double f[5]) {
-      double tmp = 1.0e+00 / G(0, ii, j, k);
-      const double u21i = tmp * G(1, ii, j, k), u31i = tmp * G(2, ii, j, k), u41i = tmp * G(3, ii, j, k),
-                   u51i = tmp * G(4, ii, j, k);
-      tmp = 1.0e+00 / G(0, ii - 1, j, k);
-      const double u21im1 = tmp * G(1, ii - 1, j, k), u31im1 = tmp * G(2, ii - 1, j, k),
-                   u41im1 = tmp * G(3, ii - 1, j, k), u51im1 = tmp * G(4, ii - 1, j, k);
-      f[1] = (4.0e+00 / 3.0e+00) * tx3 * (u21i - u21im1);
-      f[2] = tx3 * (u31i - u31im1);
-      f[3] = tx3 * (u41i - u41im1);
-      f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * tx3 *
-                 ((u21i * u21i + u31i * u31i + u41i * u41i) - (u21im1 * u21im1 + u31im1 * u31im1 + u41im1 * u41im1)) +
-             (1.0e+00 / 6.0e+00) * tx3 * (u21i * u21i - u21im1 * u21im1) + c1 * c5 * tx3 * (u51i - u51im1);
-    };
-    visc(i + 1, fp);
-    visc(i, fm);
+    visc(0, tx3, i + 1, j, k, i, j, k, fp);
+    visc(0, tx3, i, j, k, i - 1, j, k, fm);
     o[0] = o[0] + dx1 * tx1 * (G(0, i - 1, j, k) - 2.0e+00 * G(0, i, j, k) + G(0, i + 1, j, k));
     const double dxm[5] = {dx1, dx2, dx3, dx4, dx5};
 #pragma unroll
@@ -171,37 +222,12 @@ __device__ void flux_point(const double* __restrict__ g, long long NP, const LuZ
   // ---------------- eta ----------------
   {
     double fp[5], fm[5];
-    auto conv = [&](int jj, double f[5]) {
-      const double g1 = G(0, i, jj, k), g2 = G(1, i, jj, k), g3 = G(2, i, jj, k), g4 = G(3, i, jj, k),
-                   g5 = G(4, i, jj, k);
-      f[0] = g3;
-      const double u31 = g3 / g1;
-      const double q = 0.50e+00 * (g2 * g2 + g3 * g3 + g4 * g4) / g1;
-      f[1] = g2 * u31;
-      f[2] = g3 * u31 + c2 * (g5 - q);
-      f[3] = g4 * u31;
-      f[4] = (c1 * g5 - c2 * q) * u31;
-    };
-    conv(j + 1, fp);
-    conv(j - 1, fm);
+    conv(1, i, j + 1, k, fp);
+    conv(1, i, j - 1, k, fm);
 #pragma unroll
     for (int m = 0; m < 5; ++m) o[m] = o[m] - ty2 * (fp[m] - fm[m]);
-    auto visc = [&](int jj, double f[5]) {
-      double tmp = 1.0e+00 / G(0, i, jj, k);
-      const double u21j = tmp * G(1, i, jj, k), u31j = tmp * G(2, i, jj, k), u41j = tmp * G(3, i, jj, k),
-                   u51j = tmp * G(4, i, jj, k);
-      tmp = 1.0e+00 / G(0, i, jj - 1, k);
-      const double u21jm1 = tmp * G(1, i, jj - 1, k), u31jm1 = tmp * G(2, i, jj - 1, k),
-                   u41jm1 = tmp * G(3, i, jj - 1, k), u51jm1 = tmp * G(4, i, jj - 1, k);
-      f[1] = ty3 * (u21j - u21jm1);
-      f[2] = (4.0e+00 / 3.0e+00) * ty3 * (u31j - u31jm1);
-      f[3] = ty3 * (u41j - u41jm1);
-      f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * ty3 *
-                 ((u21j * u21j + u31j * u31j + u41j * u41j) - (u21jm1 * u21jm1 + u31jm1 * u31jm1 + u41jm1 * u41jm1)) +
-             (1.0e+00 / 6.0e+00) * ty3 * (u31j * u31j - u31jm1 * u31jm1) + c1 * c5 * ty3 * (u51j - u51jm1);
-    };
-    visc(j + 1, fp);
-    visc(j, fm);
+    visc(1, ty3, i, j + 1, k, i, j, k, fp);
+    visc(1, ty3, i, j, k, i, j - 1, k, fm);
     o[0] = o[0] + dy1 * ty1 * (G(0, i, j - 1, k) - 2.0e+00 * G(0, i, j, k) + G(0, i, j + 1, k));
     const double dym[5] = {dy1, dy2, dy3, dy4, dy5};
 #pragma unroll
@@ -227,37 +253,12 @@ __device__ void flux_point(const double* __restrict__ g, long long NP, const LuZ
   // ---------------- zeta ----------------
   {
     double fp[5], fm[5];
-    auto conv = [&](int kk, double f[5]) {
-      const double g1 = G(0, i, j, kk), g2 = G(1, i, j, kk), g3 = G(2, i, j, kk), g4 = G(3, i, j, kk),
-                   g5 = G(4, i, j, kk);
-      f[0] = g4;
-      const double u41 = g4 / g1;
-      const double q = 0.50e+00 * (g2 * g2 + g3 * g3 + g4 * g4) / g1;
-      f[1] = g2 * u41;
-      f[2] = g3 * u41;
-      f[3] = g4 * u41 + c2 * (g5 - q);
-      f[4] = (c1 * g5 - c2 * q) * u41;
-    };
-    conv(k + 1, fp);
-    conv(k - 1, fm);
+    conv(2, i, j, k + 1, fp);
+    conv(2, i, j, k - 1, fm);
 #pragma unroll
     for (int m = 0; m < 5; ++m) o[m] = o[m] - tz2 * (fp[m] - fm[m]);
-    auto visc = [&](int kk, double f[5]) {
-      double tmp = 1.0e+00 / G(0, i, j, kk);
-      const double u21k = tmp * G(1, i, j, kk), u31k = tmp * G(2, i, j, kk), u41k = tmp * G(3, i, j, kk),
-                   u51k = tmp * G(4, i, j, kk);
-      tmp = 1.0e+00 / G(0, i, j, kk - 1);
-      const double u21km1 = tmp * G(1, i, j, kk - 1), u31km1 = tmp * G(2, i, j, kk - 1),
-                   u41km1 = tmp * G(3, i, j, kk - 1), u51km1 = tmp * G(4, i, j, kk - 1);
-      f[1] = tz3 * (u21k - u21km1);
-      f[2] = tz3 * (u31k - u31km1);
-      f[3] = (4.0e+00 / 3.0e+00) * tz3 * (u41k - u41km1);
-      f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * tz3 *
-                 ((u21k * u21k + u31k * u31k + u41k * u41k) - (u21km1 * u21km1 + u31km1 * u31km1 + u41km1 * u41km1)) +
-             (1.0e+00 / 6.0e+00) * tz3 * (u41k * u41k - u41km1 * u41km1) + c1 * c5 * tz3 * (u51k - u51km1);
-    };
-    visc(k + 1, fp);
-    visc(k, fm);
+    visc(2, tz3, i, j, k + 1, i, j, k, fp);
+    visc(2, tz3, i, j, k, i, j, k - 1, fm);
     auto sd = [&](int m) {
       return ERHS ? (G(m, i, j, k + 1) - 2.0e+00 * G(m, i, j, k) + G(m, i, j, k - 1))
                   : (G(m, i, j, k - 1) - 2.0e+00 * G(m, i, j, k) + G(m, i, j, k + 1));
@@ -300,7 +301,7 @@ __device__ inline bool interior(const LuZone& Z, int i, int j, int k) {
 // (ERHS = true: g = the exact polynomial in rsd, out = frct starting at 0)
 template <bool ERHS>
 __global__ void __launch_bounds__(TPB) k_lu_rhs(LuDev D, const LuWork* __restrict__ work, const double* g,
-                                                double* out) {
+                                                const double* __restrict__ prim, double* out) {
   const LuWork w = work[blockIdx.x];
   const LuZone Z = D.zones[w.zone];
   int i, j, k;
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(TPB) k_lu_rhs(LuDev D, const LuWork* __restric
   double o[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) o[m] = ERHS ? 0.0 : -D.frct[m * D.NP + p];
-  if (interior(Z, i, j, k)) flux_point<ERHS>(g, D.NP, Z, i, j, k, o);
+  if (interior(Z, i, j, k)) flux_point<ERHS>(g, prim, D.NP, Z, i, j, k, o);
 #pragma unroll
   for (int m = 0; m < 5; ++m) out[m * D.NP + p] = o[m];
 }
@@ -369,7 +370,8 @@ __global__ void __launch_bounds__(TPB) k_lu_poly(LuDev D, const LuWork* __restri
   }
 }
 
-// rsd *= dt (SCALE) or u += tmp * rsd (UPDATE) on the interior
+// rsd *= dt (SCALE) or u += tmp * rsd (UPDATE, with the point's prim
+// planes refreshed from the new u) on the interior
 template <bool UPDATE>
 __global__ void __launch_bounds__(TPB) k_lu_pointwise(LuDev D, const LuWork* __restrict__ work, double tmp) {
   const LuWork w = work[blockIdx.x];
@@ -377,13 +379,31 @@ __global__ void __launch_bounds__(TPB) k_lu_pointwise(LuDev D, const LuWork* __r
   int i, j, k;
   if (!decode(Z, w.first + threadIdx.x, i, j, k) || !interior(Z, i, j, k)) return;
   const long long p = pidx(Z, i, j, k);
+  if (UPDATE) {
+    double g[5];
 #pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    if (UPDATE)
-      D.u[m * D.NP + p] = D.u[m * D.NP + p] + tmp * D.rsd[m * D.NP + p];
-    else
-      D.rsd[m * D.NP + p] = D.dt * D.rsd[m * D.NP + p];
+    for (int m = 0; m < 5; ++m) {
+      g[m] = D.u[m * D.NP + p] + tmp * D.rsd[m * D.NP + p];
+      D.u[m * D.NP + p] = g[m];
+    }
+    store_prim(D.prim, D.NP, p, g);
+  } else {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) D.rsd[m * D.NP + p] = D.dt * D.rsd[m * D.NP + p];
   }
+}
+
+// prim planes of g (u, or erhs's exact polynomial) at every point
+__global__ void __launch_bounds__(TPB) k_lu_prim(LuDev D, const LuWork* __restrict__ work, const double* g) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
+  const int q = w.first + threadIdx.x;
+  if (q >= Z.np) return;
+  const long long p = Z.off + q;
+  double v[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) v[m] = g[m * D.NP + p];
+  store_prim(D.prim, D.NP, p, v);
 }
 
 // ---- Jacobian blocks of jacld / jacu (src/LU/jacld.jl, src/LU/jacu.jl) -----
@@ -435,7 +455,7 @@ __device__ __forceinline__ void jac_d(const JC& J, double r1, double u2, double 
 // Off-diagonal block of direction DIR (0 x, 1 y, 2 z) from the neighbour's
 // state; SG = -1: jacld's (the neighbour at -1), SG = +1: jacu's (at +1).
 // The entries are the reference's statements.  r1 = 1/u1 of the neighbour
-// (the reference's tmp1, computed once per point by k_lu_rho).
+// (the reference's tmp1: the PR_RHO plane).
 template <int DIR, int SG>
 __device__ __forceinline__ void jac_off(const JC& J, double r1, double u2, double u3, double u4, double u5,
                                         double a[5][5]) {
@@ -899,16 +919,6 @@ __global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __re
   D.rsd[m * NP + p] = D.rsd[m * NP + p] - tv;
 }
 
-// rho = 1/u1 at every point (the reference's tmp1 of jacld / jacu)
-__global__ void __launch_bounds__(TPB) k_lu_rho(LuDev D, const LuWork* __restrict__ work, double* rho) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  const int q = w.first + threadIdx.x;
-  if (q >= Z.np) return;
-  const long long p = Z.off + q;
-  rho[p] = 1.0e+00 / D.u[p];
-}
-
 // ---- exch_qbc (src/LU/exchange_qbc.jl) --------------------------------------
 // Staging per zone: east face (j = ny-1) and west face (j = 2), nx*nkp points
 // each; south face (i = nx-1) and north face (i = 2), ny*nkp points each;
@@ -992,8 +1002,13 @@ __global__ void __launch_bounds__(TPB) k_lu_unpack(LuDev D, Faces F, int nzones)
     so = F.zoff[src] + 10 * ne + 5 * ns + (long long)kq * S.ny + (j - 1); stride = ns;
   }
   const long long p = pidx(Z, i, j, k);
+  double g[5];
 #pragma unroll
-  for (int m = 0; m < 5; ++m) D.u[m * D.NP + p] = F.stage[so + m * stride];
+  for (int m = 0; m < 5; ++m) {
+    g[m] = F.stage[so + m * stride];
+    D.u[m * D.NP + p] = g[m];
+  }
+  store_prim(D.prim, D.NP, p, g);
 }
 
 // ---- norms (src/LU/l2norm.jl, src/LU/error.jl, src/LU/pintgr.jl) -----------
@@ -1133,7 +1148,7 @@ struct npbmz_lu_handle {
   LuZone* zones_d = nullptr;
   int* nbr_d = nullptr;
   double *u = nullptr, *rsd = nullptr, *frct = nullptr;
-  double* rho = nullptr;  // 1/u1 per point, refreshed before each lower sweep
+  double* prim = nullptr;  // PR_COUNT planes (PR_RHO first: 1/u1 for the sweeps)
   double* fac = nullptr;  // factors of d per point (FAC_COUNT planes)
   // work lists: all zones, and per zone a contiguous range
   std::vector<LuWork> work_h;
@@ -1177,7 +1192,7 @@ int fail(npbmz_lu_t* h, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(h, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
 
-LuDev dev(npbmz_lu_t* h) { return LuDev{h->u, h->rsd, h->frct, h->NP, h->zones_d, h->dt, h->omega}; }
+LuDev dev(npbmz_lu_t* h) { return LuDev{h->u, h->rsd, h->frct, h->prim, h->NP, h->zones_d, h->dt, h->omega}; }
 
 Faces faces(npbmz_lu_t* h) { return Faces{h->stage, h->zoff_d, h->nbr_d, h->klo, h->nkp}; }
 
@@ -1218,7 +1233,7 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
   const int z0 = zone < 0 ? 0 : zone, nzs = zone < 0 ? h->nzones : 1;
   switch (phase) {
     case NPBMZ_LU_PHASE_RHS:
-      k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), w, h->u, h->rsd);
+      k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), w, h->u, h->prim, h->rsd);
       break;
     case NPBMZ_LU_PHASE_SCALE:
       k_lu_pointwise<false><<<n, TPB, 0, h->stream>>>(dev(h), w, 0.0);
@@ -1230,16 +1245,15 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
       return launch_exch(h);
     case NPBMZ_LU_PHASE_LOWER:
     case NPBMZ_LU_PHASE_SSOR + 100:  // lower with the scaling fused
-      k_lu_rho<<<n, TPB, 0, h->stream>>>(dev(h), w, h->rho);
       for (int l = h->lmin; l <= h->lmax; ++l) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
         const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
         if (phase == NPBMZ_LU_PHASE_LOWER)
-          k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->rho, h->fac, l, z0);
+          k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->prim, h->fac, l, z0);
         else
-          k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->rho, h->fac, l, z0);
+          k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->prim, h->fac, l, z0);
       }
       break;
     case NPBMZ_LU_PHASE_UPPER:
@@ -1250,7 +1264,7 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
         const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
-        k_lu_upper<<<g, b, 0, h->stream>>>(dev(h), h->rho, h->fac, l, z0);
+        k_lu_upper<<<g, b, 0, h->stream>>>(dev(h), h->prim, h->fac, l, z0);
       }
       break;
     case NPBMZ_LU_PHASE_SSOR: {
@@ -1316,6 +1330,8 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
         k_lu_convert<true, true><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
       else
         k_lu_convert<false, true><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+      if (field == NPBMZ_LU_U)
+        k_lu_prim<<<h->zblock[z + 1] - h->zblock[z], TPB, 0, h->stream>>>(dev(h), h->work_d + h->zblock[z], h->u);
     } else {
       if (layout == NPBMZ_LAYOUT_REF)  // keep the host halo: start from the host image
         LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -1334,7 +1350,7 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
 
 void free_all(npbmz_lu_t* h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
-  for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->rho,
+  for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->prim,
                   (void*)h->fac, (void*)h->work_d,
                   (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
                   (void*)h->zoff_d, (void*)h->img})
@@ -1487,7 +1503,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
   h->stream = h->own;
   if (cudaMalloc(&h->zones_d, nzones * sizeof(LuZone)) || cudaMalloc(&h->nbr_d, 4 * nzones * sizeof(int)) ||
       cudaMalloc(&h->u, F) || cudaMalloc(&h->rsd, F) || cudaMalloc(&h->frct, F) ||
-      cudaMalloc(&h->rho, (size_t)h->NP * sizeof(double)) ||
+      cudaMalloc(&h->prim, (size_t)PR_COUNT * h->NP * sizeof(double)) ||
       cudaMalloc(&h->fac, (size_t)FAC_COUNT * h->NP * sizeof(double)) ||
       cudaMalloc(&h->work_d, h->work_h.size() * sizeof(LuWork)) ||
       cudaMalloc(&h->zblock_d, h->zblock.size() * sizeof(int)) ||
@@ -1501,7 +1517,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMemcpy(h->zblock_d, h->zblock.data(), h->zblock.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->zoff_d, zoff.data(), nzones * sizeof(long long), cudaMemcpyHostToDevice) ||
       cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F) ||
-      cudaMemset(h->rho, 0, (size_t)h->NP * sizeof(double)) ||
+      cudaMemset(h->prim, 0, (size_t)PR_COUNT * h->NP * sizeof(double)) ||
       cudaMemset(h->fac, 0, (size_t)FAC_COUNT * h->NP * sizeof(double)))
     return bail("device initialisation failed");
   *out = h;
@@ -1515,8 +1531,10 @@ int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
   const int n = (int)h->work_h.size();
   k_lu_init<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce);
   k_lu_poly<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce);
-  k_lu_rhs<true><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->rsd, h->frct);
-  k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->u, h->rsd);
+  k_lu_prim<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->rsd);
+  k_lu_rhs<true><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->rsd, h->prim, h->frct);
+  k_lu_prim<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->u);
+  k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->u, h->prim, h->rsd);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
@@ -1630,7 +1648,7 @@ int npbmz_lu_synchronize(npbmz_lu_t* h) {
 
 int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
   if (!h) return -1;
-  int n = 2 + 3;  // exch (pack, unpack) + rho + update + rhs
+  int n = 2 + 2;  // exch (pack, unpack) + update + rhs
   for (int l = h->lmin; l <= h->lmax; ++l) {
     int c = 0;
     for (const LuZone& Z : h->zh) c = std::max(c, hp_count(Z, l));
