@@ -11,13 +11,15 @@
 //   exch_qbc       k_lu_pack + k_lu_unpack (every face packed before any is
 //                  unpacked, as the reference's sends are)
 //   rsd *= dt      fused into the first touch of each point in k_lu_lower
+//   Jacobians      k_lu_jac: jacld's and jacu's off-diagonal blocks and the
+//                  factors of d at every point, fully parallel
 //   flux prims     per-point quantities of the flux functions (1/u1, the
 //                  viscous u21.., the convective u21 and q), refreshed where
 //                  u changes: k_lu_unpack (ghost faces), k_lu_pointwise<1>
 //                  (update), uploads; read by the sweeps and rhs
-//   jacld + blts   k_lu_lower, one launch per hyperplane i+j+k = l, five
+//   blts           k_lu_lower, one launch per hyperplane i+j+k = l, five
 //                  threads per point (one per row of the 5x5 blocks)
-//   jacu + buts    k_lu_upper, one launch per hyperplane, l descending
+//   buts           k_lu_upper, one launch per hyperplane, l descending
 //   update         k_lu_update
 //   rhs            k_lu_rhs<false>, one thread per point
 // blts / buts make point (i,j,k) depend on (i-1,j,k), (i,j-1,k), (i,j,k-1)
@@ -696,43 +698,18 @@ __host__ __device__ constexpr bool off_zero(int dir, int r, int c) {
                      (r == 3 && (c == 2 || c == 4)));
 }
 
-// row M of block DIR . w, summed left to right as the reference does
-template <int DIR, int M>
-__device__ __forceinline__ double row_dot(const double e[5][5], const double w[5]) {
-  double s = 0.0;
-  bool first = true;
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    if (off_zero(DIR, M, c)) continue;
-    const double t = e[M][c] * w[c];
-    s = first ? t : s + t;
-    first = false;
-  }
-  return s;
-}
-
-// sum over c of ey[M][c] * wy[c] + ex[M][c] * wx[c], interleaved (y term
-// first) as blts / buts write it
-template <int M>
-__device__ __forceinline__ double row_dot2(const double ey[5][5], const double wy[5], const double ex[5][5],
-                                           const double wx[5]) {
-  double s = 0.0;
-  bool first = true;
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    if (!off_zero(1, M, c)) {
-      const double t = ey[M][c] * wy[c];
-      s = first ? t : s + t;
-      first = false;
+// Position of entry (r, c) among the 18 entries of block DIR that are not
+// structural zeros, row-major.
+__host__ __device__ constexpr int blk_idx(int dir, int r, int c) {
+  int n = 0;
+  for (int rr = 0; rr < 5; ++rr)
+    for (int cc = 0; cc < 5; ++cc) {
+      if (rr == r && cc == c) return n;
+      if (!off_zero(dir, rr, cc)) ++n;
     }
-    if (!off_zero(0, M, c)) {
-      const double t = ex[M][c] * wx[c];
-      s = first ? t : s + t;
-      first = false;
-    }
-  }
-  return s;
+  return n;
 }
+constexpr int BLK_NZ = 18;
 
 // The 5x5 solve of blts / buts (src/LU/blts.jl:106-193, src/LU/buts.jl:113-200)
 // with tmat = d.  d is lower triangular with d[2][1] = d[3][1] = d[3][2] = 0
@@ -744,179 +721,230 @@ __device__ __forceinline__ double row_dot2(const double ey[5][5], const double w
 //   tmp_r0 = (1/t00) t_r0,  v_r <- v_r - v_0 tmp_r0         (r = 1..4)
 //   tmp_4c = (1/t_cc) t_4c, v_4 <- v_4 - v_c tmp_4c         (c = 1, 2, 3)
 //   v_r <- v_r / t_rr                                       (r = 4..0)
-// The lower sweep keeps t_rr, tmp_r0 and tmp_4c per point in `fac` (12
-// planes) for the upper sweep, whose d is the same block of the same state.
-enum { FAC_T = 0, FAC_R0 = 5, FAC_4C = 9, FAC_COUNT = 12 };
+// `jac` planes per interior point, stored at the point's hyperplane-ordered
+// index h = zone.off + hps[l] + t (t: its place in hyperplane l = i+j+k,
+// k then j ascending; hps[l]: the zone's interior points with i+j+k < l), so
+// that the sweeps, which run one hyperplane per launch, read them coalesced.
+// Written by k_lu_jac before the sweeps (u does not change until the
+// update):
+//   FAC_T + r, FAC_R0 + r-1, FAC_4C + c-1   t_rr, tmp_r0, tmp_4c of d
+//   FAC_BLK + (2 dir + s) * 18 + blk_idx    the non-zero entries of the
+//       off-diagonal block of direction dir: s = 0 jacld's (from the point
+//       at -1 in dir), s = 1 jacu's (from the point at +1)
+enum { FAC_T = 0, FAC_R0 = 5, FAC_4C = 9, FAC_BLK = 12, FAC_COUNT = 12 + 6 * 18 };
+
+template <int DIR, int S>
+__device__ __forceinline__ void store_blk(double* jac, long long NP, long long h, const double b[5][5]) {
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c)
+      if (!off_zero(DIR, r, c)) jac[(FAC_BLK + (2 * DIR + S) * BLK_NZ + blk_idx(DIR, r, c)) * NP + h] = b[r][c];
+}
+
+// the off-diagonal block (DIR, SG) from the state at q
+template <int DIR, int SG>
+__device__ __forceinline__ void blk_from(const LuDev& D, const JC& J, long long q, double b[5][5]) {
+  double w[5];
+  load5(D.u, D.NP, q, w);
+  jac_off<DIR, SG>(J, D.prim[PR_RHO * D.NP + q], w[1], w[2], w[3], w[4], b);
+}
+
+// jacld's and jacu's blocks and d's factors of every interior point (the
+// Jacobian work of ssor, taken off the wavefront), one thread per point in
+// hyperplane order (blockIdx.y: zone)
+__global__ void __launch_bounds__(TPB) k_lu_jac(LuDev D, const int* __restrict__ hps, int hstride,
+                                                double* __restrict__ jac) {
+  const int z = blockIdx.y;
+  const LuZone Z = D.zones[z];
+  const int* H = hps + (long long)z * hstride;
+  const int t = blockIdx.x * TPB + threadIdx.x;
+  const int lend = Z.nx + Z.ny + Z.nz - 3;
+  if (t >= H[lend + 1]) return;
+  int lo = 6, hi = lend;  // the hyperplane of t: largest l with H[l] <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (H[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  int i, j, k;
+  if (!hyperplane_point(Z, lo, t - H[lo], i, j, k)) return;
+  const long long NP = D.NP, p = pidx(Z, i, j, k), h = Z.off + t;
+  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
+  double b[5][5];
+  blk_from<0, -1>(D, J, pidx(Z, i - 1, j, k), b);
+  store_blk<0, 0>(jac, NP, h, b);
+  blk_from<0, 1>(D, J, pidx(Z, i + 1, j, k), b);
+  store_blk<0, 1>(jac, NP, h, b);
+  blk_from<1, -1>(D, J, pidx(Z, i, j - 1, k), b);
+  store_blk<1, 0>(jac, NP, h, b);
+  blk_from<1, 1>(D, J, pidx(Z, i, j + 1, k), b);
+  store_blk<1, 1>(jac, NP, h, b);
+  blk_from<2, -1>(D, J, pidx(Z, i, j, k - 1), b);
+  store_blk<2, 0>(jac, NP, h, b);
+  blk_from<2, 1>(D, J, pidx(Z, i, j, k + 1), b);
+  store_blk<2, 1>(jac, NP, h, b);
+  double w[5];
+  load5(D.u, NP, p, w);
+  jac_d(J, D.prim[PR_RHO * NP + p], w[1], w[2], w[3], w[4], b);
+  const double rinv0 = 1.0e+00 / b[0][0];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) jac[(FAC_T + r) * NP + h] = b[r][r];
+#pragma unroll
+  for (int r = 1; r < 5; ++r) jac[(FAC_R0 + r - 1) * NP + h] = rinv0 * b[r][0];
+#pragma unroll
+  for (int c = 1; c <= 3; ++c) jac[(FAC_4C + c - 1) * NP + h] = (1.0e+00 / b[c][c]) * b[4][c];
+}
+
+// row M of the point's block (DIR, S) dotted with w, summed left to right as
+// the reference does (structural zeros skipped: a product with one is +-0
+// and adding it changes no sum's value)
+template <int DIR, int S, int M>
+__device__ __forceinline__ double row_dot(const double* __restrict__ jac, long long NP, long long h,
+                                          const double w[5]) {
+  double s = 0.0;
+  bool first = true;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    if (off_zero(DIR, M, c)) continue;
+    const double t = jac[(FAC_BLK + (2 * DIR + S) * BLK_NZ + blk_idx(DIR, M, c)) * NP + h] * w[c];
+    s = first ? t : s + t;
+    first = false;
+  }
+  return s;
+}
+
+// sum over c of Y[M][c] wy[c] + X[M][c] wx[c] (y term first, as blts / buts
+// write it)
+template <int S, int M>
+__device__ __forceinline__ double row_dot2(const double* __restrict__ jac, long long NP, long long h,
+                                           const double wy[5], const double wx[5]) {
+  double s = 0.0;
+  bool first = true;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    if (!off_zero(1, M, c)) {
+      const double t = jac[(FAC_BLK + (2 + S) * BLK_NZ + blk_idx(1, M, c)) * NP + h] * wy[c];
+      s = first ? t : s + t;
+      first = false;
+    }
+    if (!off_zero(0, M, c)) {
+      const double t = jac[(FAC_BLK + S * BLK_NZ + blk_idx(0, M, c)) * NP + h] * wx[c];
+      s = first ? t : s + t;
+      first = false;
+    }
+  }
+  return s;
+}
 
 constexpr int HP = 32;  // points per block of the sweep kernels (x 5 rows)
 
-// One thread per (point, row M): rows of the off-diagonal blocks, the row
-// sums and row M of d.  Returns v_M after blts's two update loops.
+// blts's two update loops for row M of one point (h: its jac index)
 template <int M, bool SCALE>
-__device__ __forceinline__ double lower_row(const LuDev& D, const double* __restrict__ rho, const LuZone& Z,
-                                            const JC& J, int i, int j, int k, double& d0, double& dd,
-                                            double d4[3]) {
+__device__ __forceinline__ double lower_row(const LuDev& D, const double* __restrict__ jac, const LuZone& Z, int i,
+                                            int j, int k, long long h) {
   const long long NP = D.NP, p = pidx(Z, i, j, k);
   const double omega = D.omega;
   double v = D.rsd[M * NP + p];
   if (SCALE) v = D.dt * v;
-  double w[5], x[5], blk[5][5], blk2[5][5];
-  {  // ldz: from (i, j, k-1)
-    const long long q = pidx(Z, i, j, k - 1);
-    load5(D.u, NP, q, w);
-    jac_off<2, -1>(J, rho[q], w[1], w[2], w[3], w[4], blk);
-    load5(D.rsd, NP, q, w);
-    v = v - omega * row_dot<2, M>(blk, w);
-  }
-  {  // ldy: from (i, j-1, k); ldx: from (i-1, j, k)
-    const long long qy = pidx(Z, i, j - 1, k), qx = pidx(Z, i - 1, j, k);
-    load5(D.u, NP, qy, w);
-    jac_off<1, -1>(J, rho[qy], w[1], w[2], w[3], w[4], blk);
-    load5(D.u, NP, qx, x);
-    jac_off<0, -1>(J, rho[qx], x[1], x[2], x[3], x[4], blk2);
-    load5(D.rsd, NP, qy, w);
-    load5(D.rsd, NP, qx, x);
-    v = v - omega * row_dot2<M>(blk, w, blk2, x);
-  }
-  load5(D.u, NP, p, w);
-  jac_d(J, rho[p], w[1], w[2], w[3], w[4], blk);
-  d0 = blk[M][0];
-  dd = blk[M][M];
-  if (M == 4) {
-    d4[0] = blk[4][1];
-    d4[1] = blk[4][2];
-    d4[2] = blk[4][3];
-  }
+  double w[5], x[5];
+  load5(D.rsd, NP, pidx(Z, i, j, k - 1), w);
+  v = v - omega * row_dot<2, 0, M>(jac, NP, h, w);
+  load5(D.rsd, NP, pidx(Z, i, j - 1, k), w);
+  load5(D.rsd, NP, pidx(Z, i - 1, j, k), x);
+  v = v - omega * row_dot2<0, M>(jac, NP, h, w, x);
   return v;
 }
 
-// jacld + blts at every point of hyperplane l (blockIdx.y: zone - zone0).
-// SCALE: rsd *= dt at the point first (ssor's scaling, fused: blts reads
-// only points it has already scaled and solved, or boundary points, which
-// the scaling does not touch).
+// the forward substitution with d's factors (rows exchanged through shared
+// memory); v: this thread's row, sv: every row of the point
+__device__ __forceinline__ double d_solve(const double* __restrict__ jac, long long NP, long long h, int m, double v,
+                                          const double sv[5]) {
+  const double v0 = sv[0];
+  if (m == 0) return v / jac[FAC_T * NP + h];
+  if (m < 4) {
+    v = v - v0 * jac[(FAC_R0 + m - 1) * NP + h];
+    return v / jac[(FAC_T + m) * NP + h];
+  }
+  v = v - v0 * jac[(FAC_R0 + 3) * NP + h];
+#pragma unroll
+  for (int c = 1; c <= 3; ++c) {
+    const double vc = sv[c] - v0 * jac[(FAC_R0 + c - 1) * NP + h];  // v_c after column 0, as row c has it
+    v = v - vc * jac[(FAC_4C + c - 1) * NP + h];
+  }
+  return v / jac[(FAC_T + 4) * NP + h];
+}
+
+// jacld + blts at every point of hyperplane l (blockIdx.y: zone - zone0),
+// five threads per point (threadIdx.y: row).  SCALE: rsd *= dt at the point
+// first (ssor's scaling, fused: blts reads only points it has already scaled
+// and solved, or boundary points, which the scaling does not touch).
 template <bool SCALE>
-__global__ void __launch_bounds__(HP * 5) k_lu_lower(LuDev D, const double* __restrict__ rho,
-                                                     double* __restrict__ fac, int l, int zone0) {
-  __shared__ double sv[5][HP], sd0[5][HP], srinv[4][HP], s4[3][HP];
-  const int m = threadIdx.y, a = threadIdx.x;
-  const LuZone Z = D.zones[zone0 + blockIdx.y];
+__global__ void __launch_bounds__(HP * 5) k_lu_lower(LuDev D, const double* __restrict__ jac,
+                                                     const int* __restrict__ hps, int hstride, int l, int zone0) {
+  __shared__ double sv[HP][5];
+  const int m = threadIdx.y, a = threadIdx.x, z = zone0 + blockIdx.y;
+  const LuZone Z = D.zones[z];
+  const int t = blockIdx.x * HP + a;
   int i = 0, j = 0, k = 0;
-  const bool ok = hyperplane_point(Z, l, blockIdx.x * HP + a, i, j, k);
-  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
-  double v = 0.0, d0 = 0.0, dd = 1.0, d4[3] = {0.0, 0.0, 0.0};
+  const bool ok = hyperplane_point(Z, l, t, i, j, k);
+  const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
+  double v = 0.0;
   if (ok) {
     switch (m) {
-      case 0: v = lower_row<0, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
-      case 1: v = lower_row<1, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
-      case 2: v = lower_row<2, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
-      case 3: v = lower_row<3, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
-      default: v = lower_row<4, SCALE>(D, rho, Z, J, i, j, k, d0, dd, d4); break;
+      case 0: v = lower_row<0, SCALE>(D, jac, Z, i, j, k, h); break;
+      case 1: v = lower_row<1, SCALE>(D, jac, Z, i, j, k, h); break;
+      case 2: v = lower_row<2, SCALE>(D, jac, Z, i, j, k, h); break;
+      case 3: v = lower_row<3, SCALE>(D, jac, Z, i, j, k, h); break;
+      default: v = lower_row<4, SCALE>(D, jac, Z, i, j, k, h); break;
     }
-    sv[m][a] = v;
-    sd0[m][a] = d0;
-    if (m < 4) srinv[m][a] = 1.0e+00 / dd;
-    if (m == 4) {
-      s4[0][a] = d4[0];
-      s4[1][a] = d4[1];
-      s4[2][a] = d4[2];
-    }
+    sv[a][m] = v;
   }
   __syncthreads();
   if (!ok) return;
-  const long long NP = D.NP, p = pidx(Z, i, j, k);
-  const double v0 = sv[0][a], rinv0 = srinv[0][a];
-  fac[(FAC_T + m) * NP + p] = dd;
-  if (m == 0) {
-    v = v / dd;
-  } else if (m < 4) {
-    const double tmp = rinv0 * d0;
-    v = v - v0 * tmp;
-    v = v / dd;
-    fac[(FAC_R0 + m - 1) * NP + p] = tmp;
-  } else {
-    const double tmp40 = rinv0 * d0;
-    v = v - v0 * tmp40;
-    double tmpc[3];
-#pragma unroll
-    for (int c = 1; c <= 3; ++c) {
-      const double vc = sv[c][a] - v0 * (rinv0 * sd0[c][a]);  // v_c after column 0, as row c has it
-      tmpc[c - 1] = srinv[c][a] * s4[c - 1][a];
-      v = v - vc * tmpc[c - 1];
-    }
-    v = v / dd;
-    fac[(FAC_R0 + 3) * NP + p] = tmp40;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) fac[(FAC_4C + c) * NP + p] = tmpc[c];
-  }
-  D.rsd[m * NP + p] = v;
+  D.rsd[m * D.NP + pidx(Z, i, j, k)] = d_solve(jac, D.NP, h, m, v, sv[a]);
 }
 
+// buts's two tv loops for row M of one point
 template <int M>
-__device__ __forceinline__ double upper_row(const LuDev& D, const double* __restrict__ rho, const LuZone& Z,
-                                            const JC& J, int i, int j, int k) {
+__device__ __forceinline__ double upper_row(const LuDev& D, const double* __restrict__ jac, const LuZone& Z, int i,
+                                            int j, int k, long long h) {
   const long long NP = D.NP;
   const double omega = D.omega;
-  double w[5], x[5], blk[5][5], blk2[5][5], tv;
-  {  // udz: from (i, j, k+1)
-    const long long q = pidx(Z, i, j, k + 1);
-    load5(D.u, NP, q, w);
-    jac_off<2, 1>(J, rho[q], w[1], w[2], w[3], w[4], blk);
-    load5(D.rsd, NP, q, w);
-    tv = omega * row_dot<2, M>(blk, w);
-  }
-  {  // udy: from (i, j+1, k); udx: from (i+1, j, k)
-    const long long qy = pidx(Z, i, j + 1, k), qx = pidx(Z, i + 1, j, k);
-    load5(D.u, NP, qy, w);
-    jac_off<1, 1>(J, rho[qy], w[1], w[2], w[3], w[4], blk);
-    load5(D.u, NP, qx, x);
-    jac_off<0, 1>(J, rho[qx], x[1], x[2], x[3], x[4], blk2);
-    load5(D.rsd, NP, qy, w);
-    load5(D.rsd, NP, qx, x);
-    tv = tv + omega * row_dot2<M>(blk, w, blk2, x);
-  }
+  double w[5], x[5];
+  load5(D.rsd, NP, pidx(Z, i, j, k + 1), w);
+  double tv = omega * row_dot<2, 1, M>(jac, NP, h, w);
+  load5(D.rsd, NP, pidx(Z, i, j + 1, k), w);
+  load5(D.rsd, NP, pidx(Z, i + 1, j, k), x);
+  tv = tv + omega * row_dot2<1, M>(jac, NP, h, w, x);
   return tv;
 }
 
-// jacu + buts at every point of hyperplane l, with the factors of d the
-// lower sweep kept
-__global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __restrict__ rho,
-                                                     const double* __restrict__ fac, int l, int zone0) {
-  __shared__ double sv[5][HP];
-  const int m = threadIdx.y, a = threadIdx.x;
-  const LuZone Z = D.zones[zone0 + blockIdx.y];
+// jacu + buts at every point of hyperplane l
+__global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __restrict__ jac,
+                                                     const int* __restrict__ hps, int hstride, int l, int zone0) {
+  __shared__ double sv[HP][5];
+  const int m = threadIdx.y, a = threadIdx.x, z = zone0 + blockIdx.y;
+  const LuZone Z = D.zones[z];
+  const int t = blockIdx.x * HP + a;
   int i = 0, j = 0, k = 0;
-  const bool ok = hyperplane_point(Z, l, blockIdx.x * HP + a, i, j, k);
-  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
+  const bool ok = hyperplane_point(Z, l, t, i, j, k);
+  const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
   double tv = 0.0;
   if (ok) {
     switch (m) {
-      case 0: tv = upper_row<0>(D, rho, Z, J, i, j, k); break;
-      case 1: tv = upper_row<1>(D, rho, Z, J, i, j, k); break;
-      case 2: tv = upper_row<2>(D, rho, Z, J, i, j, k); break;
-      case 3: tv = upper_row<3>(D, rho, Z, J, i, j, k); break;
-      default: tv = upper_row<4>(D, rho, Z, J, i, j, k); break;
+      case 0: tv = upper_row<0>(D, jac, Z, i, j, k, h); break;
+      case 1: tv = upper_row<1>(D, jac, Z, i, j, k, h); break;
+      case 2: tv = upper_row<2>(D, jac, Z, i, j, k, h); break;
+      case 3: tv = upper_row<3>(D, jac, Z, i, j, k, h); break;
+      default: tv = upper_row<4>(D, jac, Z, i, j, k, h); break;
     }
-    sv[m][a] = tv;
+    sv[a][m] = tv;
   }
   __syncthreads();
   if (!ok) return;
-  const long long NP = D.NP, p = pidx(Z, i, j, k);
-  const double tv0 = sv[0][a];
-  if (m == 0) {
-    tv = tv / fac[FAC_T * NP + p];
-  } else if (m < 4) {
-    tv = tv - tv0 * fac[(FAC_R0 + m - 1) * NP + p];
-    tv = tv / fac[(FAC_T + m) * NP + p];
-  } else {
-    tv = tv - tv0 * fac[(FAC_R0 + 3) * NP + p];
-#pragma unroll
-    for (int c = 1; c <= 3; ++c) {
-      const double tc = sv[c][a] - tv0 * fac[(FAC_R0 + c - 1) * NP + p];
-      tv = tv - tc * fac[(FAC_4C + c - 1) * NP + p];
-    }
-    tv = tv / fac[(FAC_T + 4) * NP + p];
-  }
-  D.rsd[m * NP + p] = D.rsd[m * NP + p] - tv;
+  tv = d_solve(jac, D.NP, h, m, tv, sv[a]);
+  const long long p = pidx(Z, i, j, k);
+  D.rsd[m * D.NP + p] = D.rsd[m * D.NP + p] - tv;
 }
 
 // ---- exch_qbc (src/LU/exchange_qbc.jl) --------------------------------------
@@ -1149,7 +1177,10 @@ struct npbmz_lu_handle {
   int* nbr_d = nullptr;
   double *u = nullptr, *rsd = nullptr, *frct = nullptr;
   double* prim = nullptr;  // PR_COUNT planes (PR_RHO first: 1/u1 for the sweeps)
-  double* fac = nullptr;  // factors of d per point (FAC_COUNT planes)
+  double* fac = nullptr;  // FAC_COUNT planes per point: d's factors and the off-diagonal blocks
+  int* hps_d = nullptr;   // per zone, hstride ints: interior points with i+j+k < l
+  int hstride = 0;
+  int max_interior = 0;
   // work lists: all zones, and per zone a contiguous range
   std::vector<LuWork> work_h;
   std::vector<int> zblock;  // first block of each zone, nzones+1 entries
@@ -1193,6 +1224,13 @@ int fail(npbmz_lu_t* h, const char* fmt, ...) {
   } while (0)
 
 LuDev dev(npbmz_lu_t* h) { return LuDev{h->u, h->rsd, h->frct, h->prim, h->NP, h->zones_d, h->dt, h->omega}; }
+
+// the same, with zones starting at z0 (kernels that index zones by blockIdx.y)
+LuDev dev_zone0(npbmz_lu_t* h, int z0) {
+  LuDev d = dev(h);
+  d.zones = h->zones_d + z0;
+  return d;
+}
 
 Faces faces(npbmz_lu_t* h) { return Faces{h->stage, h->zoff_d, h->nbr_d, h->klo, h->nkp}; }
 
@@ -1244,27 +1282,31 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
     case NPBMZ_LU_PHASE_EXCH:
       return launch_exch(h);
     case NPBMZ_LU_PHASE_LOWER:
-    case NPBMZ_LU_PHASE_SSOR + 100:  // lower with the scaling fused
+    case NPBMZ_LU_PHASE_SSOR + 100: {  // lower with the scaling fused
+      // the blocks and d's factors of every interior point, then the wavefront
+      const dim3 gj((h->max_interior + TPB - 1) / TPB, nzs);
+      k_lu_jac<<<gj, TPB, 0, h->stream>>>(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride, h->fac);
       for (int l = h->lmin; l <= h->lmax; ++l) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
         const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
         if (phase == NPBMZ_LU_PHASE_LOWER)
-          k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->prim, h->fac, l, z0);
+          k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
         else
-          k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->prim, h->fac, l, z0);
+          k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
       }
       break;
+    }
     case NPBMZ_LU_PHASE_UPPER:
-      // rho and fac from the lower sweep of the same state (u does not
-      // change between the sweeps)
+      // the blocks and factors k_lu_jac made before the lower sweep (u does
+      // not change between the sweeps)
       for (int l = h->lmax; l >= h->lmin; --l) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
         const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
-        k_lu_upper<<<g, b, 0, h->stream>>>(dev(h), h->prim, h->fac, l, z0);
+        k_lu_upper<<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
       }
       break;
     case NPBMZ_LU_PHASE_SSOR: {
@@ -1353,7 +1395,7 @@ void free_all(npbmz_lu_t* h) {
   for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->prim,
                   (void*)h->fac, (void*)h->work_d,
                   (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
-                  (void*)h->zoff_d, (void*)h->img})
+                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d})
     if (p) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
 }
@@ -1481,6 +1523,16 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
   h->lmin = 6;
   h->lmax = 6;
   for (const LuZone& Z : h->zh) h->lmax = std::max(h->lmax, Z.nx + Z.ny + Z.nz - 3);
+  h->hstride = h->lmax + 2;
+  std::vector<int> hps((size_t)nzones * h->hstride, 0);
+  for (int z = 0; z < nzones; ++z) {
+    int acc = 0;
+    for (int l = 0; l < h->hstride; ++l) {
+      hps[(size_t)z * h->hstride + l] = acc;
+      if (l >= 6) acc += hp_count(h->zh[z], l);
+    }
+    h->max_interior = std::max(h->max_interior, acc);
+  }
   h->zblock.push_back(0);
   for (int z = 0; z < nzones; ++z) {
     for (int f = 0; f < h->zh[z].np; f += TPB) h->work_h.push_back(LuWork{z, f});
@@ -1509,13 +1561,15 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMalloc(&h->zblock_d, h->zblock.size() * sizeof(int)) ||
       cudaMalloc(&h->partial, h->work_h.size() * 5 * sizeof(double)) ||
       cudaMalloc(&h->zone_out_d, (6 * (size_t)nzones + 16) * sizeof(double)) ||
-      cudaMalloc(&h->stage, so * sizeof(double)) || cudaMalloc(&h->zoff_d, nzones * sizeof(long long)))
+      cudaMalloc(&h->stage, so * sizeof(double)) || cudaMalloc(&h->zoff_d, nzones * sizeof(long long)) ||
+      cudaMalloc(&h->hps_d, hps.size() * sizeof(int)))
     return bail("device allocation failed");
   if (cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(LuZone), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->nbr_d, h->nbr.data(), 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->work_d, h->work_h.data(), h->work_h.size() * sizeof(LuWork), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->zblock_d, h->zblock.data(), h->zblock.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->zoff_d, zoff.data(), nzones * sizeof(long long), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->hps_d, hps.data(), hps.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F) ||
       cudaMemset(h->prim, 0, (size_t)PR_COUNT * h->NP * sizeof(double)) ||
       cudaMemset(h->fac, 0, (size_t)FAC_COUNT * h->NP * sizeof(double)))
@@ -1648,7 +1702,7 @@ int npbmz_lu_synchronize(npbmz_lu_t* h) {
 
 int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
   if (!h) return -1;
-  int n = 2 + 2;  // exch (pack, unpack) + update + rhs
+  int n = 2 + 3;  // exch (pack, unpack) + jac + update + rhs
   for (int l = h->lmin; l <= h->lmax; ++l) {
     int c = 0;
     for (const LuZone& Z : h->zh) c = std::max(c, hp_count(Z, l));

@@ -170,4 +170,4 @@ def test_phase_and_zone_errors_are_reported():
         p.phase(17)
     with pytest.raises(npbmz.NpbmzError, match="zone"):
         p.ssor(16)
-    assert p.launches_per_iteration() == 4 + 2 * (6 + 6 + 6 - 3 - 6 + 1)
+    assert p.launches_per_iteration() == 5 + 2 * (6 + 6 + 6 - 3 - 6 + 1)
