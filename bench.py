@@ -50,12 +50,15 @@ WORKLOADS = {
     "lu-b": ("LU", "B", "LU-MZ 304x208x17, 4x4 equal zones (76x52x17), dt 2.0, omega 1.2"),
     "lu-a": ("LU", "A", "LU-MZ 128x128x16, 4x4 equal zones (32x32x16), dt 2.0, omega 1.2"),
 }
-# LU-MZ: algorithmic HBM bytes per grid point of each phase (FP64): the
-# sweeps read u and rsd and write rsd, rhs reads u and frct and writes rsd,
-# update reads u and rsd and writes u.
-LU_BYTES_PER_POINT = {"lower": 120.0, "upper": 120.0, "rhs": 120.0, "update": 120.0, "exch": 0.0}
-LU_KERNELS = {"lower": "k_lu_lower<1>", "upper": "k_lu_upper", "rhs": "k_lu_rhs<0>", "update": "k_lu_pointwise<1>",
-              "exch": "k_lu_pack+k_lu_unpack"}
+# LU-MZ: algorithmic HBM bytes per grid point of each phase (FP64, every
+# point of the zones): jac reads u and 1/u1 (48 B) and writes 120 planes of
+# blocks and factors per interior point (960 B); the sweeps read rsd and the
+# 66 planes of their direction (rsd in, rsd out: 80 B + 528 B); rhs reads u,
+# frct and ten planes of flux quantities and writes rsd (200 B); update reads
+# u and rsd and writes u and the flux quantities (200 B).
+LU_BYTES_PER_POINT = {"jac": 1008.0, "lower": 608.0, "upper": 608.0, "rhs": 200.0, "update": 200.0, "exch": 0.0}
+LU_KERNELS = {"jac": "k_lu_jac", "lower": "k_lu_lower<1>", "upper": "k_lu_upper", "rhs": "k_lu_rhs<0>",
+              "update": "k_lu_pointwise<1>", "exch": "k_lu_pack+k_lu_unpack"}
 SEED = 20261203
 # Algorithmic HBM bytes per grid point of each phase (the 600 B/pt-step model:
 # FP64 state, intermediates and line-solve scratch kept out of the count):
@@ -370,7 +373,9 @@ def run_gpu_lu(args, cls, desc):
         top = max((k for k in ph if k != "exch"), key=lambda k: ph[k])
         pk = peaks()
         hbm = float(pk.get("hbm_gbs", 6800.0))
-        achieved = LU_BYTES_PER_POINT[top] * pts / (ph[top] * 1e-3) / 1e9
+        interior = int(np.sum((p.nx.astype(np.int64) - 2) * (p.ny - 2) * (p.nz - 2)))
+        units = interior if top in ("jac", "lower", "upper") else pts
+        achieved = LU_BYTES_PER_POINT[top] * units / (ph[top] * 1e-3) / 1e9
         fp64 = npbmz.fp64_peak_gflops()
         km = None
         try:
@@ -380,9 +385,9 @@ def run_gpu_lu(args, cls, desc):
         kn = LU_KERNELS[top]
         traffic = fp64_obj = None
         if km and kn in km:
-            traffic = km[kn]["dram_bytes_per_point"] * pts
+            traffic = km[kn]["dram_bytes_per_point"] * units
             fl = km[kn]["fp64_flops_per_point"]
-            fa = fl * pts / (ph[top] * 1e-3) / 1e9
+            fa = fl * units / (ph[top] * 1e-3) / 1e9
             fp64_obj = {"achieved": fa, "peak": fp64, "unit": "GFLOP/s", "frac": fa / fp64, "flops_per_point": fl,
                         "pipe_active_ncu": km[kn]["fp64_pipe_active"],
                         "peak_source": "npbmz_fp64_peak: FP64 FMA chains on this GPU, measured in this run"}
@@ -392,7 +397,10 @@ def run_gpu_lu(args, cls, desc):
                                                 "workload's capture (profiles/ncu_kernel_metrics.json), times its points")
                              if traffic is not None else None,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
-                             "bytes_per_point": LU_BYTES_PER_POINT[top], "launch_ms": ph[top],
+                             "bytes_per_point": LU_BYTES_PER_POINT[top],
+                             "points": f"{units} ({'interior' if units == interior else 'all'} points per launch)",
+                             "launch_ms": ph[top] / max(2, min(args.steps, 5)),
+                             "binding_ceiling": "fp64 pipe" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6 else None,
                              "fp64": fp64_obj}
         extra["fp64_peak_gflops_measured"] = fp64
         var = {}

@@ -116,8 +116,9 @@ int npbmz_lu_synchronize(npbmz_lu_t* h);
 int npbmz_lu_launches_per_iteration(npbmz_lu_t* h);
 
 /* Per-phase device time of niter batched iterations from CUDA events on the
- * handle's stream, summed: {exch, lower (jacld+blts, rsd *= dt fused),
- * upper (jacu+buts), update, rhs} in ms.  Advances the state. */
+ * handle's stream, summed: {exch, jac (jacld's and jacu's blocks of every
+ * point), lower (blts, rsd *= dt fused), upper (buts), update, rhs} in ms.
+ * Advances the state. */
 int npbmz_lu_profile(npbmz_lu_t* h, int niter, double* phase_ms);
 
 const char* npbmz_lu_last_error(npbmz_lu_t* h);

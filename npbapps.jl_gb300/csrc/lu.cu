@@ -1264,6 +1264,28 @@ int launch_exch(npbmz_lu_t* h) {
   return 0;
 }
 
+int launch_jac(npbmz_lu_t* h, int z0, int nzs) {
+  const dim3 gj((h->max_interior + TPB - 1) / TPB, nzs);
+  k_lu_jac<<<gj, TPB, 0, h->stream>>>(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride, h->fac);
+  LU_CK(h, cudaGetLastError());
+  return 0;
+}
+
+int launch_lower(npbmz_lu_t* h, bool scale, int z0, int nzs) {
+  for (int l = h->lmin; l <= h->lmax; ++l) {
+    int c = 0;
+    for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
+    if (!c) continue;
+    const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
+    if (scale)
+      k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
+    else
+      k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
+  }
+  LU_CK(h, cudaGetLastError());
+  return 0;
+}
+
 int launch_phase(npbmz_lu_t* h, int phase, int zone) {
   const LuWork* w;
   int n;
@@ -1284,19 +1306,9 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
     case NPBMZ_LU_PHASE_LOWER:
     case NPBMZ_LU_PHASE_SSOR + 100: {  // lower with the scaling fused
       // the blocks and d's factors of every interior point, then the wavefront
-      const dim3 gj((h->max_interior + TPB - 1) / TPB, nzs);
-      k_lu_jac<<<gj, TPB, 0, h->stream>>>(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride, h->fac);
-      for (int l = h->lmin; l <= h->lmax; ++l) {
-        int c = 0;
-        for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
-        if (!c) continue;
-        const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
-        if (phase == NPBMZ_LU_PHASE_LOWER)
-          k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
-        else
-          k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
-      }
-      break;
+      int rc = launch_jac(h, z0, nzs);
+      if (!rc) rc = launch_lower(h, phase != NPBMZ_LU_PHASE_LOWER, z0, nzs);
+      return rc;
     }
     case NPBMZ_LU_PHASE_UPPER:
       // the blocks and factors k_lu_jac made before the lower sweep (u does
@@ -1714,29 +1726,34 @@ int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
 int npbmz_lu_profile(npbmz_lu_t* h, int niter, double* phase_ms) {
   if (!h || !phase_ms || niter < 1) return -1;
   std::lock_guard<std::mutex> g(h->mu);
-  cudaEvent_t ev[6];
+  constexpr int NPH = 6;  // exch, jac, lower, upper, update, rhs
+  cudaEvent_t ev[NPH + 1];
   for (auto& e : ev) LU_CK(h, cudaEventCreate(&e));
-  for (int q = 0; q < 5; ++q) phase_ms[q] = 0.0;
+  for (int q = 0; q < NPH; ++q) phase_ms[q] = 0.0;
   int rc = 0;
+  const int n = (int)h->work_h.size();
   for (int it = 0; it < niter && !rc; ++it) {
     cudaEventRecord(ev[0], h->stream);
     rc = launch_exch(h);
     cudaEventRecord(ev[1], h->stream);
-    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_SSOR + 100, -1);
+    if (!rc) rc = launch_jac(h, 0, h->nzones);
     cudaEventRecord(ev[2], h->stream);
-    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPPER, -1);
+    if (!rc) rc = launch_lower(h, true, 0, h->nzones);
     cudaEventRecord(ev[3], h->stream);
-    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPDATE, -1);
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPPER, -1);
     cudaEventRecord(ev[4], h->stream);
-    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_RHS, -1);
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPDATE, -1);
     cudaEventRecord(ev[5], h->stream);
-    if (cudaEventSynchronize(ev[5]) != cudaSuccess) rc = fail(h, "event synchronisation failed");
-    for (int q = 0; q < 5 && !rc; ++q) {
+    if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_RHS, -1);
+    cudaEventRecord(ev[6], h->stream);
+    if (cudaEventSynchronize(ev[NPH]) != cudaSuccess) rc = fail(h, "event synchronisation failed");
+    for (int q = 0; q < NPH && !rc; ++q) {
       float ms = 0.0f;
       cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
       phase_ms[q] += ms;
     }
   }
+  (void)n;
   for (auto& e : ev) cudaEventDestroy(e);
   return rc;
 }

@@ -25,7 +25,7 @@ FACES_NPB = 0x1
 GRAPH = 0x2
 U, RSD, FRCT = 0, 1, 2
 PHASE_RHS, PHASE_SCALE, PHASE_LOWER, PHASE_UPPER, PHASE_UPDATE, PHASE_EXCH, PHASE_SSOR = range(7)
-PROFILE_PHASES = ("exch", "lower", "upper", "update", "rhs")
+PROFILE_PHASES = ("exch", "jac", "lower", "upper", "update", "rhs")
 OMEGA_DEFAULT = 1.2  # src/LU/lu_data.jl
 
 _typed = False
@@ -155,7 +155,7 @@ class LuProblem:
         return int(lib().npbmz_lu_launches_per_iteration(self._h))
 
     def profile(self, niter):
-        out = np.zeros(5)
+        out = np.zeros(len(PROFILE_PHASES))
         self._check(lib().npbmz_lu_profile(self._h, niter, _dp(out)), "profile")
         return dict(zip(PROFILE_PHASES, out.tolist()))
 
