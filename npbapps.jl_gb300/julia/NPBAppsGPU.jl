@@ -1,5 +1,5 @@
-# NPBAppsGPU.jl -- Julia binding of libnpbmz_gpu.so (include/npbmz.h) for the
-# NPBApps.jl BT-MZ / SP-MZ node time loop.
+# NPBAppsGPU.jl -- Julia binding of libnpbmz_gpu.so (include/npbmz.h,
+# include/npbmz_lu.h) for the NPBApps.jl BT-MZ / SP-MZ / LU-MZ node time loops.
 #
 # The reference's loop (src/BT/bt-node.jl:280-395, src/SP/sp-node.jl:252-397)
 # calls exch_qbc(Val(ncells), ...) over all zones and then adi(iz, ...) per zone
@@ -186,5 +186,95 @@ device_zones(p::Problem, field) = [DeviceZone(p, iz, Cint(field)) for iz in 1:p.
 
 """adi of one zone under the handle's lock (the reference calls adi from Threads.@threads)."""
 adi_locked!(p::Problem, iz::Integer) = lock(() -> adi!(p, iz), p.lock)
+
+# ---------------------------------------------------------------------------
+# LU-MZ (include/npbmz_lu.h).  The reference's LU loop (src/LU/lu-node.jl:
+# 233-270) keeps its shape:
+#
+#     lu = NPBAppsGPU.LuProblem(nx, ny, nz, nbr, dt)     # nbr from lu_zone_setup
+#     NPBAppsGPU.setup!(lu)                              # setbv, setiv, erhs, rhs
+#     for istep = 1:itmax
+#         NPBAppsGPU.exch_qbc!(lu)                       # replaces exch_qbc(...)
+#         NPBAppsGPU.ssor!(lu)                           # replaces the @threads ssor(iz, ...) loop
+#     end
+#     xcr, xce, xci = NPBAppsGPU.verify(lu)              # ERROR, l2norm, pintgr summed over zones
+
+const LU_FACES_NPB = Cint(0x1)
+const LU_GRAPH = Cint(0x2)
+const LU_U = Cint(0)
+const LU_RSD = Cint(1)
+const LU_FRCT = Cint(2)
+
+mutable struct LuProblem
+    handle::Ptr{Cvoid}
+    nzones::Int
+    function LuProblem(nx::Vector{<:Integer}, ny, nz, nbr, dt; omega = 1.2, flags = Cint(0))
+        n = length(nx)
+        params = Cdouble[dt, omega]
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:npbmz_lu_create, libnpbmz), Cint,
+                   (Cint, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cdouble}, Cint, Ptr{Ptr{Cvoid}}),
+                   n, Cint.(nx), Cint.(ny), Cint.(nz), Cint.(nbr), params, flags, out)
+        rc == 0 || error("npbmz_lu_create failed (zone sizes below 5, unequal nz, mismatched faces or bad flags)")
+        p = new(out[], n)
+        finalizer(p) do q
+            q.handle != C_NULL && ccall((:npbmz_lu_destroy, libnpbmz), Cint, (Ptr{Cvoid},), q.handle)
+            q.handle = C_NULL
+        end
+        return p
+    end
+end
+
+check(p::LuProblem, rc, what) =
+    rc == 0 || error(what * ": " * unsafe_string(ccall((:npbmz_lu_last_error, libnpbmz), Cstring, (Ptr{Cvoid},), p.handle)))
+
+"""Zone sizes and LU's neighbours (src/LU/zone_setup.jl); 0-based neighbours."""
+function lu_zone_setup(gx, gy, gz, x_zones, y_zones, ratio = 1.0)
+    n = x_zones * y_zones
+    nx = zeros(Cint, n); ny = zeros(Cint, n); nz = zeros(Cint, n); nbr = zeros(Cint, 4n)
+    rc = ccall((:npbmz_lu_zone_setup, libnpbmz), Cint,
+               (Cint, Cint, Cint, Cint, Cint, Cdouble, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}),
+               gx, gy, gz, x_zones, y_zones, ratio, nx, ny, nz, nbr)
+    rc == 0 || error("npbmz_lu_zone_setup failed")
+    return nx, ny, nz, nbr
+end
+
+"""setbv, setiv, erhs and rhs on the GPU; ce = nothing: the reference's table (setcoeff.jl)."""
+function setup!(p::LuProblem, ce::Union{Nothing, AbstractMatrix{Float64}} = nothing)
+    c = ce === nothing ? Ptr{Cdouble}(C_NULL) : Matrix{Float64}(permutedims(ce))
+    check(p, ccall((:npbmz_lu_setup, libnpbmz), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.handle, c), "npbmz_lu_setup")
+end
+
+"""Replaces exch_qbc(...) (src/LU/exchange_qbc.jl)."""
+exch_qbc!(p::LuProblem) =
+    check(p, ccall((:npbmz_lu_exch_qbc, libnpbmz), Cint, (Ptr{Cvoid},), p.handle), "npbmz_lu_exch_qbc")
+
+"""Replaces ssor(iz, ...) (src/LU/ssor.jl:9-254): zone iz (1-based), or all zones batched."""
+ssor!(p::LuProblem, iz::Integer = 0) =
+    check(p, ccall((:npbmz_lu_ssor, libnpbmz), Cint, (Ptr{Cvoid}, Cint), p.handle, iz - 1), "npbmz_lu_ssor")
+
+"""niter iterations of exch_qbc + ssor; the per-iteration rsd norms when norms = true."""
+function iterate!(p::LuProblem, niter::Integer; norms = false)
+    out = norms ? zeros(Cdouble, 5, niter) : nothing
+    check(p, ccall((:npbmz_lu_iterate, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}), p.handle, niter,
+                   norms ? out : Ptr{Cdouble}(C_NULL)), "npbmz_lu_iterate")
+    return out
+end
+
+"""ERROR, l2norm and pintgr summed over zones (src/LU/lu-node.jl:306-321): (xcr, xce, xci)."""
+function verify(p::LuProblem)
+    xcr = zeros(Cdouble, 5); xce = zeros(Cdouble, 5); xci = zeros(Cdouble, 1)
+    check(p, ccall((:npbmz_lu_verify, libnpbmz), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                   p.handle, xcr, xce, xci), "npbmz_lu_verify")
+    return xcr, xce, xci[1]
+end
+
+"""One zone's u, rsd or frct in the reference's OffsetArray memory ([1:5, -1:nx+2, -1:ny+2, 1:nz])."""
+upload!(p::LuProblem, zone::Integer, field, a) =
+    check(p, ccall((:npbmz_lu_upload, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
+                   p.handle, zone - 1, field, LAYOUT_REF, parent(a)), "npbmz_lu_upload")
+download!(p::LuProblem, zone::Integer, field, a) =
+    check(p, ccall((:npbmz_lu_download, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
+                   p.handle, zone - 1, field, LAYOUT_REF, parent(a)), "npbmz_lu_download")
 
 end # module

@@ -109,3 +109,18 @@ def test_lu_zone_setup_rejects_non_integer_extents(npbmz_mod):
 
     with pytest.raises(npbmz.NpbmzError):
         lu.lu_zone_setup(25, 24, 6, 4, 4)
+
+
+def test_julia_bindings_call_only_declared_entry_points():
+    """The Julia binding and shim (written against the ABI; Julia is not
+    installed here) name only functions the headers declare, and the LU
+    binding covers the LU time loop's calls."""
+    jl = Path(__file__).resolve().parents[1] / "npbapps.jl_gb300" / "julia"
+    declared = set(declared_functions(HEADER)) | set(declared_functions(LU_HEADER))
+    called = set()
+    for f in jl.glob("*.jl"):
+        called |= set(re.findall(r"ccall\(\(:(npbmz_[a-z_0-9]+)\s*,", f.read_text()))
+    assert called and called <= declared, sorted(called - declared)
+    for name in ("npbmz_lu_create", "npbmz_lu_setup", "npbmz_lu_exch_qbc", "npbmz_lu_ssor", "npbmz_lu_iterate",
+                 "npbmz_lu_verify", "npbmz_lu_upload", "npbmz_lu_download", "npbmz_lu_destroy"):
+        assert name in called, name
