@@ -405,7 +405,8 @@ def run_gpu_lu(args, cls, desc):
         extra["fp64_peak_gflops_measured"] = fp64
         var = {}
         for name, fl in (("fp64_batched", 0), ("fp64_batched_graph", lu.GRAPH),
-                         ("fp64_batched_graph_npb_faces", lu.GRAPH | lu.FACES_NPB)):
+                         ("fp64_batched_graph_npb_faces", lu.GRAPH | lu.FACES_NPB),
+                         ("fp64_fma_batched_graph (not bit-exact)", lu.GRAPH | lu.FMA)):
             q = make(fl)
             mv = timed(q, max(2, min(args.steps, 5)), 1)
             var[name] = pts * max(2, min(args.steps, 5)) / (mv * 1e-3) / 1e6

@@ -45,6 +45,11 @@ typedef struct npbmz_lu_handle npbmz_lu_t;
                                   with this flag */
 #define NPBMZ_LU_GRAPH 0x2     /* npbmz_lu_iterate replays one captured CUDA
                                   graph per iteration */
+#define NPBMZ_LU_FMA 0x4       /* the iteration's kernels built with FMA
+                                  contraction (a*b+c rounded once): faster on
+                                  the FP64 pipe, no longer bit-for-bit the
+                                  reference's rounding (set-up, exch_qbc and
+                                  the norms stay uncontracted) */
 
 /* fields */
 #define NPBMZ_LU_U 0

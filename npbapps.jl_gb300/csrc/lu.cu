@@ -1,7 +1,9 @@
-// lu.cu -- LU-MZ's SSOR iteration (NPBApps.jl src/LU) on the GPU, and its
-// C ABI (include/npbmz_lu.h).  Built with -fmad=false: every FP64 statement
-// rounds as the reference's Julia does (no a*b+c contraction), so the result
-// is bit-for-bit the oracle's.
+// lu.cu -- the host side of LU-MZ's SSOR iteration (NPBApps.jl src/LU) on
+// the GPU: its C ABI (include/npbmz_lu.h).  The kernels are in
+// lu_kernels.cuh, built twice: lu_exact (-fmad=false: every FP64 statement
+// rounds as the reference's Julia does, no a*b+c contraction, so the result
+// is bit-for-bit the oracle's; the default) and lu_fast (-fmad=true; the hot
+// kernels of an NPBMZ_LU_FMA handle).
 //
 // Data in HBM: u, rsd, frct variable-major over the points of all zones,
 // field[m*NP + zone.off + ((k-1)*ny + (j-1))*nx + (i-1)] (1-based i, j, k as
@@ -20,7 +22,7 @@
 //   blts           k_lu_lower, one launch per hyperplane i+j+k = l, five
 //                  threads per point (one per row of the 5x5 blocks)
 //   buts           k_lu_upper, one launch per hyperplane, l descending
-//   update         k_lu_update
+//   update         k_lu_pointwise<1>
 //   rhs            k_lu_rhs<false>, one thread per point
 // blts / buts make point (i,j,k) depend on (i-1,j,k), (i,j-1,k), (i,j,k-1)
 // (resp. +1): within a hyperplane every point is independent, and every
@@ -39,16 +41,11 @@
 #include <vector>
 
 #include "../../include/npbmz_lu.h"
+#include "lu_launch.h"
+
+using namespace npbmz_lu;
 
 namespace {
-
-constexpr double c1 = 1.40e+00, c2 = 0.40e+00, c3 = 1.00e-01, c4 = 1.00e+00, c5 = 1.40e+00;
-constexpr double dx1 = 0.75e+00, dx2 = dx1, dx3 = dx1, dx4 = dx1, dx5 = dx1;
-constexpr double dy1 = 0.75e+00, dy2 = dy1, dy3 = dy1, dy4 = dy1, dy5 = dy1;
-constexpr double dz1 = 1.00e+00, dz2 = dz1, dz3 = dz1, dz4 = dz1, dz5 = dz1;
-constexpr double dssp = 1.00e+00 / 4.0e+00;  // max(dx1, dy1, dz1) / 4 (src/LU/setcoeff.jl)
-constexpr int ii1 = 2, ji1 = 2, ki1 = 3;
-constexpr int TPB = 128;
 
 // the reference's ce table (src/LU/setcoeff.jl), row m, 13 columns
 const double ce_reference[5][13] = {
@@ -58,1117 +55,13 @@ const double ce_reference[5][13] = {
     {2.0e0, 2.0e0, 0.0e0, 0.0e0, 0.0e0, 2.0e0, 3.0e0, 0.03e0, 0.05e0, 0.04e0, 0.2e0, 0.1e0, 0.3e0},
     {5.0e0, 4.0e0, 3.0e0, 2.0e0, 0.1e0, 0.4e0, 0.3e0, 0.05e0, 0.04e0, 0.03e0, 0.1e0, 0.3e0, 0.2e0}};
 
-struct CeTable {
-  double c[5][13];
-};
-
-// setcoeff of one zone (src/LU/setcoeff.jl) and its place in HBM
-struct LuZone {
-  long long off;
-  int nx, ny, nz, np;
-  double dxi, deta, dzeta, tx1, tx2, tx3, ty1, ty2, ty3, tz1, tz2, tz3;
-  int ii2, ji2, ki2;
-};
-
-struct LuDev {
-  double* u;
-  double* rsd;
-  double* frct;
-  double* prim;  // PR_COUNT planes of per-point flux quantities of u
-  long long NP;
-  const LuZone* zones;
-  double dt, omega;
-};
-
-struct LuWork {  // one block of TPB consecutive points of one zone
-  int zone, first;
-};
-
-__host__ __device__ inline long long pidx(const LuZone& Z, int i, int j, int k) {
-  return Z.off + ((long long)(k - 1) * Z.ny + (j - 1)) * Z.nx + (i - 1);
-}
-
-// ---- exact solution (src/LU/exact.jl) ---------------------------------------
-__device__ inline void exact_point(const CeTable& ce, int i, int j, int k, int nx0, int ny0, int nz0, double out[5]) {
-  const double xi = (double)(i - 1) / (nx0 - 1);
-  const double eta = (double)(j - 1) / (ny0 - 1);
-  const double zeta = (double)(k - 1) / (nz0 - 1);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    const double* c = ce.c[m];
-    out[m] = c[0] + (c[1] + (c[4] + (c[7] + c[10] * xi) * xi) * xi) * xi +
-             (c[2] + (c[5] + (c[8] + c[11] * eta) * eta) * eta) * eta +
-             (c[3] + (c[6] + (c[9] + c[12] * zeta) * zeta) * zeta) * zeta;
-  }
-}
-
-// ---- rhs / erhs point operator (src/LU/rhs.jl, src/LU/erhs.jl) -------------
-// o: the point's output, holding -frct (rhs) or 0 (erhs) on entry.  ERHS
-// selects erhs's z second difference order (g(k+1) first) and its viscous
-// association ((o + A) + B instead of o + (A + B)).
-template <bool ERHS>
-__device__ inline double visc_up(double o, double a, double b) {
-  return ERHS ? (o + a) + b : o + (a + b);
-}
-
-// Per-point quantities of the flux functions (planes of `prim`), each the
-// reference's own expression evaluated once per point instead of once per
-// use (rhs.jl and erhs.jl evaluate them at every neighbour):
-//   PR_RHO  1/g1                          (the viscous tmp, jacld's tmp1)
-//   PR_U21..PR_U51  tmp*g2 .. tmp*g5      (the viscous u21i .. u51i)
-//   PR_S    u21^2 + u31^2 + u41^2         (their sum of squares)
-//   PR_C21, PR_C31, PR_C41  g2/g1, g3/g1, g4/g1  (the convective u21, u31, u41)
-//   PR_Q    0.5 (g2^2 + g3^2 + g4^2) / g1 (the convective q)
-enum { PR_RHO = 0, PR_U21, PR_U31, PR_U41, PR_U51, PR_S, PR_C21, PR_C31, PR_C41, PR_Q, PR_COUNT };
-
-__device__ __forceinline__ void prim_point(const double g[5], double pr[PR_COUNT]) {
-  const double tmp = 1.0e+00 / g[0];
-  pr[PR_RHO] = tmp;
-  pr[PR_U21] = tmp * g[1];
-  pr[PR_U31] = tmp * g[2];
-  pr[PR_U41] = tmp * g[3];
-  pr[PR_U51] = tmp * g[4];
-  pr[PR_S] = pr[PR_U21] * pr[PR_U21] + pr[PR_U31] * pr[PR_U31] + pr[PR_U41] * pr[PR_U41];
-  pr[PR_C21] = g[1] / g[0];
-  pr[PR_C31] = g[2] / g[0];
-  pr[PR_C41] = g[3] / g[0];
-  pr[PR_Q] = 0.50e+00 * (g[1] * g[1] + g[2] * g[2] + g[3] * g[3]) / g[0];
-}
-
-__device__ __forceinline__ void store_prim(double* prim, long long NP, long long p, const double g[5]) {
-  double pr[PR_COUNT];
-  prim_point(g, pr);
-#pragma unroll
-  for (int q = 0; q < PR_COUNT; ++q) prim[q * NP + p] = pr[q];
-}
-
-template <bool ERHS>
-__device__ void flux_point(const double* __restrict__ g, const double* __restrict__ prim, long long NP,
-                           const LuZone& Z, int i, int j, int k, double o[5]) {
-  const int nx = Z.nx, ny = Z.ny, nz = Z.nz;
-  auto G = [&](int m, int ii, int jj, int kk) -> double { return g[m * NP + pidx(Z, ii, jj, kk)]; };
-  auto P = [&](int q, int ii, int jj, int kk) -> double { return prim[q * NP + pidx(Z, ii, jj, kk)]; };
-  const double tx1 = Z.tx1, tx2 = Z.tx2, tx3 = Z.tx3, ty1 = Z.ty1, ty2 = Z.ty2, ty3 = Z.ty3, tz1 = Z.tz1,
-               tz2 = Z.tz2, tz3 = Z.tz3;
-  // convective flux of direction D (0 x, 1 y, 2 z) at a point
-  auto conv = [&](int D, int ii, int jj, int kk, double f[5]) {
-    const double g2 = G(1, ii, jj, kk), g3 = G(2, ii, jj, kk), g4 = G(3, ii, jj, kk), g5 = G(4, ii, jj, kk);
-    const double q = P(PR_Q, ii, jj, kk);
-    if (D == 0) {
-      const double u21 = P(PR_C21, ii, jj, kk);
-      f[0] = g2;
-      f[1] = g2 * u21 + c2 * (g5 - q);
-      f[2] = g3 * u21;
-      f[3] = g4 * u21;
-      f[4] = (c1 * g5 - c2 * q) * u21;
-    } else if (D == 1) {
-      const double u31 = P(PR_C31, ii, jj, kk);
-      f[0] = g3;
-      f[1] = g2 * u31;
-      f[2] = g3 * u31 + c2 * (g5 - q);
-      f[3] = g4 * u31;
-      f[4] = (c1 * g5 - c2 * q) * u31;
-    } else {
-      const double u41 = P(PR_C41, ii, jj, kk);
-      f[0] = g4;
-      f[1] = g2 * u41;
-      f[2] = g3 * u41;
-      f[3] = g4 * u41 + c2 * (g5 - q);
-      f[4] = (c1 * g5 - c2 * q) * u41;
-    }
-  };
-  // viscous flux of direction D between point b (the - side) and point a
-  auto visc = [&](int D, double t3, int ai, int aj, int ak, int bi, int bj, int bk, double f[5]) {
-    const double u21i = P(PR_U21, ai, aj, ak), u31i = P(PR_U31, ai, aj, ak), u41i = P(PR_U41, ai, aj, ak),
-                 u51i = P(PR_U51, ai, aj, ak), si = P(PR_S, ai, aj, ak);
-    const double u21m = P(PR_U21, bi, bj, bk), u31m = P(PR_U31, bi, bj, bk), u41m = P(PR_U41, bi, bj, bk),
-                 u51m = P(PR_U51, bi, bj, bk), sm = P(PR_S, bi, bj, bk);
-    f[1] = (D == 0 ? (4.0e+00 / 3.0e+00) * t3 : t3) * (u21i - u21m);
-    f[2] = (D == 1 ? (4.0e+00 / 3.0e+00) * t3 : t3) * (u31i - u31m);
-    f[3] = (D == 2 ? (4.0e+00 / 3.0e+00) * t3 : t3) * (u41i - u41m);
-    const double ui = D == 0 ? u21i : (D == 1 ? u31i : u41i), um = D == 0 ? u21m : (D == 1 ? u31m : u41m);
-    f[4] = 0.50e+00 * (1.0e+00 - c1 * c5) * t3 * (si - sm) + (1.0e+00 / 6.0e+00) * t3 * (ui * ui - um * um) +
-           c1 * c5 * t3 * (u51i - u51m);
-  };
-  // ---------------- xi ----------------
-  {
-    double fp[5], fm[5];
-    conv(0, i + 1, j, k, fp);
-    conv(0, i - 1, j, k, fm);
-#pragma unroll
-    for (int m = 0; m < 5; ++m) o[m] = o[m] - tx2 * (fp[m] - fm[m]);
-    visc(0, tx3, i + 1, j, k, i, j, k, fp);
-    visc(0, tx3, i, j, k, i - 1, j, k, fm);
-    o[0] = o[0] + dx1 * tx1 * (G(0, i - 1, j, k) - 2.0e+00 * G(0, i, j, k) + G(0, i + 1, j, k));
-    const double dxm[5] = {dx1, dx2, dx3, dx4, dx5};
-#pragma unroll
-    for (int m = 1; m < 5; ++m)
-      o[m] = visc_up<ERHS>(o[m], tx3 * c3 * c4 * (fp[m] - fm[m]),
-                           dxm[m] * tx1 * (G(m, i - 1, j, k) - 2.0e+00 * G(m, i, j, k) + G(m, i + 1, j, k)));
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      if (i == 2) o[m] = o[m] - dssp * (+5.0e+00 * G(m, 2, j, k) - 4.0e+00 * G(m, 3, j, k) + G(m, 4, j, k));
-      if (i == 3)
-        o[m] = o[m] - dssp * (-4.0e+00 * G(m, 2, j, k) + 6.0e+00 * G(m, 3, j, k) - 4.0e+00 * G(m, 4, j, k) +
-                              G(m, 5, j, k));
-      if (i >= 4 && i <= nx - 3)
-        o[m] = o[m] - dssp * (G(m, i - 2, j, k) - 4.0e+00 * G(m, i - 1, j, k) + 6.0e+00 * G(m, i, j, k) -
-                              4.0e+00 * G(m, i + 1, j, k) + G(m, i + 2, j, k));
-      if (i == nx - 2)
-        o[m] = o[m] - dssp * (G(m, nx - 4, j, k) - 4.0e+00 * G(m, nx - 3, j, k) + 6.0e+00 * G(m, nx - 2, j, k) -
-                              4.0e+00 * G(m, nx - 1, j, k));
-      if (i == nx - 1)
-        o[m] = o[m] - dssp * (G(m, nx - 3, j, k) - 4.0e+00 * G(m, nx - 2, j, k) + 5.0e+00 * G(m, nx - 1, j, k));
-    }
-  }
-  // ---------------- eta ----------------
-  {
-    double fp[5], fm[5];
-    conv(1, i, j + 1, k, fp);
-    conv(1, i, j - 1, k, fm);
-#pragma unroll
-    for (int m = 0; m < 5; ++m) o[m] = o[m] - ty2 * (fp[m] - fm[m]);
-    visc(1, ty3, i, j + 1, k, i, j, k, fp);
-    visc(1, ty3, i, j, k, i, j - 1, k, fm);
-    o[0] = o[0] + dy1 * ty1 * (G(0, i, j - 1, k) - 2.0e+00 * G(0, i, j, k) + G(0, i, j + 1, k));
-    const double dym[5] = {dy1, dy2, dy3, dy4, dy5};
-#pragma unroll
-    for (int m = 1; m < 5; ++m)
-      o[m] = visc_up<ERHS>(o[m], ty3 * c3 * c4 * (fp[m] - fm[m]),
-                           dym[m] * ty1 * (G(m, i, j - 1, k) - 2.0e+00 * G(m, i, j, k) + G(m, i, j + 1, k)));
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      if (j == 2) o[m] = o[m] - dssp * (+5.0e+00 * G(m, i, 2, k) - 4.0e+00 * G(m, i, 3, k) + G(m, i, 4, k));
-      if (j == 3)
-        o[m] = o[m] - dssp * (-4.0e+00 * G(m, i, 2, k) + 6.0e+00 * G(m, i, 3, k) - 4.0e+00 * G(m, i, 4, k) +
-                              G(m, i, 5, k));
-      if (j >= 4 && j <= ny - 3)
-        o[m] = o[m] - dssp * (G(m, i, j - 2, k) - 4.0e+00 * G(m, i, j - 1, k) + 6.0e+00 * G(m, i, j, k) -
-                              4.0e+00 * G(m, i, j + 1, k) + G(m, i, j + 2, k));
-      if (j == ny - 2)
-        o[m] = o[m] - dssp * (G(m, i, ny - 4, k) - 4.0e+00 * G(m, i, ny - 3, k) + 6.0e+00 * G(m, i, ny - 2, k) -
-                              4.0e+00 * G(m, i, ny - 1, k));
-      if (j == ny - 1)
-        o[m] = o[m] - dssp * (G(m, i, ny - 3, k) - 4.0e+00 * G(m, i, ny - 2, k) + 5.0e+00 * G(m, i, ny - 1, k));
-    }
-  }
-  // ---------------- zeta ----------------
-  {
-    double fp[5], fm[5];
-    conv(2, i, j, k + 1, fp);
-    conv(2, i, j, k - 1, fm);
-#pragma unroll
-    for (int m = 0; m < 5; ++m) o[m] = o[m] - tz2 * (fp[m] - fm[m]);
-    visc(2, tz3, i, j, k + 1, i, j, k, fp);
-    visc(2, tz3, i, j, k, i, j, k - 1, fm);
-    auto sd = [&](int m) {
-      return ERHS ? (G(m, i, j, k + 1) - 2.0e+00 * G(m, i, j, k) + G(m, i, j, k - 1))
-                  : (G(m, i, j, k - 1) - 2.0e+00 * G(m, i, j, k) + G(m, i, j, k + 1));
-    };
-    o[0] = o[0] + dz1 * tz1 * sd(0);
-    const double dzm[5] = {dz1, dz2, dz3, dz4, dz5};
-#pragma unroll
-    for (int m = 1; m < 5; ++m) o[m] = visc_up<ERHS>(o[m], tz3 * c3 * c4 * (fp[m] - fm[m]), dzm[m] * tz1 * sd(m));
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      if (k == 2) o[m] = o[m] - dssp * (+5.0e+00 * G(m, i, j, 2) - 4.0e+00 * G(m, i, j, 3) + G(m, i, j, 4));
-      if (k == 3)
-        o[m] = o[m] - dssp * (-4.0e+00 * G(m, i, j, 2) + 6.0e+00 * G(m, i, j, 3) - 4.0e+00 * G(m, i, j, 4) +
-                              G(m, i, j, 5));
-      if (k >= 4 && k <= nz - 3)
-        o[m] = o[m] - dssp * (G(m, i, j, k - 2) - 4.0e+00 * G(m, i, j, k - 1) + 6.0e+00 * G(m, i, j, k) -
-                              4.0e+00 * G(m, i, j, k + 1) + G(m, i, j, k + 2));
-      if (k == nz - 2)
-        o[m] = o[m] - dssp * (G(m, i, j, nz - 4) - 4.0e+00 * G(m, i, j, nz - 3) + 6.0e+00 * G(m, i, j, nz - 2) -
-                              4.0e+00 * G(m, i, j, nz - 1));
-      if (k == nz - 1)
-        o[m] = o[m] - dssp * (G(m, i, j, nz - 3) - 4.0e+00 * G(m, i, j, nz - 2) + 5.0e+00 * G(m, i, j, nz - 1));
-    }
-  }
-}
-
-__device__ inline bool decode(const LuZone& Z, int q, int& i, int& j, int& k) {
-  if (q >= Z.np) return false;
-  i = q % Z.nx + 1;
-  j = (q / Z.nx) % Z.ny + 1;
-  k = q / (Z.nx * Z.ny) + 1;
-  return true;
-}
-
-__device__ inline bool interior(const LuZone& Z, int i, int j, int k) {
-  return i >= 2 && i <= Z.nx - 1 && j >= 2 && j <= Z.ny - 1 && k >= 2 && k <= Z.nz - 1;
-}
-
-// rhs (ERHS = false: g = u, out = rsd starting at -frct) or erhs's flux part
-// (ERHS = true: g = the exact polynomial in rsd, out = frct starting at 0)
-template <bool ERHS>
-__global__ void __launch_bounds__(TPB) k_lu_rhs(LuDev D, const LuWork* __restrict__ work, const double* g,
-                                                const double* __restrict__ prim, double* out) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  int i, j, k;
-  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
-  const long long p = pidx(Z, i, j, k);
-  double o[5];
-#pragma unroll
-  for (int m = 0; m < 5; ++m) o[m] = ERHS ? 0.0 : -D.frct[m * D.NP + p];
-  if (interior(Z, i, j, k)) flux_point<ERHS>(g, prim, D.NP, Z, i, j, k, o);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) out[m * D.NP + p] = o[m];
-}
-
-// setbv + setiv (src/LU/setbv.jl, src/LU/setiv.jl); every face point of
-// setbv gets exact() of its own (i, j, k), whichever face writes it last
-__global__ void __launch_bounds__(TPB) k_lu_init(LuDev D, const LuWork* __restrict__ work, CeTable ce) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  int i, j, k;
-  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
-  const int nx = Z.nx, ny = Z.ny, nz = Z.nz;
-  const long long p = pidx(Z, i, j, k);
-  double out[5];
-  if (!interior(Z, i, j, k)) {
-    exact_point(ce, i, j, k, nx, ny, nz, out);
-  } else {
-    const double zeta = (double)(k - 1) / (nz - 1);
-    const double eta = (double)(j - 1) / (ny - 1);
-    const double xi = (double)(i - 1) / (nx - 1);
-    double a1[5], a2[5], b1[5], b2[5], g1[5], g2[5];
-    exact_point(ce, 1, j, k, nx, ny, nz, a1);
-    exact_point(ce, nx, j, k, nx, ny, nz, a2);
-    exact_point(ce, i, 1, k, nx, ny, nz, b1);
-    exact_point(ce, i, ny, k, nx, ny, nz, b2);
-    exact_point(ce, i, j, 1, nx, ny, nz, g1);
-    exact_point(ce, i, j, nz, nx, ny, nz, g2);
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      const double pxi = (1.0e+00 - xi) * a1[m] + xi * a2[m];
-      const double peta = (1.0e+00 - eta) * b1[m] + eta * b2[m];
-      const double pzeta = (1.0e+00 - zeta) * g1[m] + zeta * g2[m];
-      out[m] = pxi + peta + pzeta - pxi * peta - peta * pzeta - pzeta * pxi + pxi * peta * pzeta;
-    }
-  }
-#pragma unroll
-  for (int m = 0; m < 5; ++m) D.u[m * D.NP + p] = out[m];
-}
-
-// erhs's first part: rsd = the exact polynomial (non-Horner, src/LU/erhs.jl:24-47)
-__global__ void __launch_bounds__(TPB) k_lu_poly(LuDev D, const LuWork* __restrict__ work, CeTable ce) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  int i, j, k;
-  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
-  const long long p = pidx(Z, i, j, k);
-  const double zeta = (double)(k - 1) / (Z.nz - 1);
-  const double eta = (double)(j - 1) / (Z.ny - 1);
-  const double xi = (double)(i - 1) / (Z.nx - 1);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    const double* c = ce.c[m];
-    D.rsd[m * D.NP + p] = c[0] + c[1] * xi + c[2] * eta + c[3] * zeta + c[4] * xi * xi + c[5] * eta * eta +
-                          c[6] * zeta * zeta + c[7] * xi * xi * xi + c[8] * eta * eta * eta +
-                          c[9] * zeta * zeta * zeta + c[10] * xi * xi * xi * xi + c[11] * eta * eta * eta * eta +
-                          c[12] * zeta * zeta * zeta * zeta;
-  }
-}
-
-// rsd *= dt (SCALE) or u += tmp * rsd (UPDATE, with the point's prim
-// planes refreshed from the new u) on the interior
-template <bool UPDATE>
-__global__ void __launch_bounds__(TPB) k_lu_pointwise(LuDev D, const LuWork* __restrict__ work, double tmp) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  int i, j, k;
-  if (!decode(Z, w.first + threadIdx.x, i, j, k) || !interior(Z, i, j, k)) return;
-  const long long p = pidx(Z, i, j, k);
-  if (UPDATE) {
-    double g[5];
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      g[m] = D.u[m * D.NP + p] + tmp * D.rsd[m * D.NP + p];
-      D.u[m * D.NP + p] = g[m];
-    }
-    store_prim(D.prim, D.NP, p, g);
-  } else {
-#pragma unroll
-    for (int m = 0; m < 5; ++m) D.rsd[m * D.NP + p] = D.dt * D.rsd[m * D.NP + p];
-  }
-}
-
-// prim planes of g (u, or erhs's exact polynomial) at every point
-__global__ void __launch_bounds__(TPB) k_lu_prim(LuDev D, const LuWork* __restrict__ work, const double* g) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  const int q = w.first + threadIdx.x;
-  if (q >= Z.np) return;
-  const long long p = Z.off + q;
-  double v[5];
-#pragma unroll
-  for (int m = 0; m < 5; ++m) v[m] = g[m * D.NP + p];
-  store_prim(D.prim, D.NP, p, v);
-}
-
-// ---- Jacobian blocks of jacld / jacu (src/LU/jacld.jl, src/LU/jacu.jl) -----
-struct JC {
-  double dt, tx1, tx2, ty1, ty2, tz1, tz2;
-};
-constexpr double r43 = (4.0e+00 / 3.0e+00);
-constexpr double c1345 = c1 * c3 * c4 * c5;
-constexpr double c34 = c3 * c4;
-
-// the diagonal block (identical in jacld and jacu) at the point's own state
-__device__ __forceinline__ void jac_d(const JC& J, double r1, double u2, double u3, double u4, double u5,
-                                      double d[5][5]) {
-  const double dt = J.dt, tx1 = J.tx1, ty1 = J.ty1, tz1 = J.tz1;
-  const double tmp1 = r1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
-  d[0][0] = 1.0e+00 + dt * 2.0e+00 * (tx1 * dx1 + ty1 * dy1 + tz1 * dz1);
-  d[0][1] = 0.0; d[0][2] = 0.0; d[0][3] = 0.0; d[0][4] = 0.0;
-  d[1][0] = dt * 2.0e+00 * (tx1 * (-r43 * c34 * tmp2 * u2) + ty1 * (-c34 * tmp2 * u2) + tz1 * (-c34 * tmp2 * u2));
-  d[1][1] = 1.0e+00 + dt * 2.0e+00 * (tx1 * r43 * c34 * tmp1 + ty1 * c34 * tmp1 + tz1 * c34 * tmp1) +
-            dt * 2.0e+00 * (tx1 * dx2 + ty1 * dy2 + tz1 * dz2);
-  d[1][2] = 0.0; d[1][3] = 0.0; d[1][4] = 0.0;
-  d[2][0] = dt * 2.0e+00 * (tx1 * (-c34 * tmp2 * u3) + ty1 * (-r43 * c34 * tmp2 * u3) + tz1 * (-c34 * tmp2 * u3));
-  d[2][1] = 0.0;
-  d[2][2] = 1.0e+00 + dt * 2.0e+00 * (tx1 * c34 * tmp1 + ty1 * r43 * c34 * tmp1 + tz1 * c34 * tmp1) +
-            dt * 2.0e+00 * (tx1 * dx3 + ty1 * dy3 + tz1 * dz3);
-  d[2][3] = 0.0; d[2][4] = 0.0;
-  d[3][0] = dt * 2.0e+00 * (tx1 * (-c34 * tmp2 * u4) + ty1 * (-c34 * tmp2 * u4) + tz1 * (-r43 * c34 * tmp2 * u4));
-  d[3][1] = 0.0; d[3][2] = 0.0;
-  d[3][3] = 1.0e+00 + dt * 2.0e+00 * (tx1 * c34 * tmp1 + ty1 * c34 * tmp1 + tz1 * r43 * c34 * tmp1) +
-            dt * 2.0e+00 * (tx1 * dx4 + ty1 * dy4 + tz1 * dz4);
-  d[3][4] = 0.0;
-  d[4][0] = dt * 2.0e+00 *
-            (tx1 * (-(r43 * c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
-                    (c34 - c1345) * tmp3 * (u4 * u4) - (c1345)*tmp2 * u5) +
-             ty1 * (-(c34 - c1345) * tmp3 * (u2 * u2) - (r43 * c34 - c1345) * tmp3 * (u3 * u3) -
-                    (c34 - c1345) * tmp3 * (u4 * u4) - (c1345)*tmp2 * u5) +
-             tz1 * (-(c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
-                    (r43 * c34 - c1345) * tmp3 * (u4 * u4) - (c1345)*tmp2 * u5));
-  d[4][1] = dt * 2.0e+00 *
-            (tx1 * (r43 * c34 - c1345) * tmp2 * u2 + ty1 * (c34 - c1345) * tmp2 * u2 + tz1 * (c34 - c1345) * tmp2 * u2);
-  d[4][2] = dt * 2.0e+00 *
-            (tx1 * (c34 - c1345) * tmp2 * u3 + ty1 * (r43 * c34 - c1345) * tmp2 * u3 + tz1 * (c34 - c1345) * tmp2 * u3);
-  d[4][3] = dt * 2.0e+00 *
-            (tx1 * (c34 - c1345) * tmp2 * u4 + ty1 * (c34 - c1345) * tmp2 * u4 + tz1 * (r43 * c34 - c1345) * tmp2 * u4);
-  d[4][4] = 1.0e+00 + dt * 2.0e+00 * (tx1 * c1345 * tmp1 + ty1 * c1345 * tmp1 + tz1 * c1345 * tmp1) +
-            dt * 2.0e+00 * (tx1 * dx5 + ty1 * dy5 + tz1 * dz5);
-}
-
-// Off-diagonal block of direction DIR (0 x, 1 y, 2 z) from the neighbour's
-// state; SG = -1: jacld's (the neighbour at -1), SG = +1: jacu's (at +1).
-// The entries are the reference's statements.  r1 = 1/u1 of the neighbour
-// (the reference's tmp1: the PR_RHO plane).
-template <int DIR, int SG>
-__device__ __forceinline__ void jac_off(const JC& J, double r1, double u2, double u3, double u4, double u5,
-                                        double a[5][5]) {
-  const double dt = J.dt;
-  const double tmp1 = r1, tmp2 = tmp1 * tmp1, tmp3 = tmp1 * tmp2;
-  if (DIR == 2) {
-    const double tz1 = J.tz1, tz2 = J.tz2;
-    if (SG < 0) {
-      a[0][0] = -dt * tz1 * dz1;
-      a[0][1] = 0.0;
-      a[0][2] = 0.0;
-      a[0][3] = -dt * tz2;
-      a[0][4] = 0.0;
-      a[1][0] = -dt * tz2 * (-(u2 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u2);
-      a[1][1] = -dt * tz2 * (u4 * tmp1) - dt * tz1 * c34 * tmp1 - dt * tz1 * dz2;
-      a[1][2] = 0.0;
-      a[1][3] = -dt * tz2 * (u2 * tmp1);
-      a[1][4] = 0.0;
-      a[2][0] = -dt * tz2 * (-(u3 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u3);
-      a[2][1] = 0.0;
-      a[2][2] = -dt * tz2 * (u4 * tmp1) - dt * tz1 * (c34 * tmp1) - dt * tz1 * dz3;
-      a[2][3] = -dt * tz2 * (u3 * tmp1);
-      a[2][4] = 0.0;
-      a[3][0] = -dt * tz2 * (-((u4 * tmp1) * (u4 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
-                dt * tz1 * (-r43 * c34 * tmp2 * u4);
-      a[3][1] = -dt * tz2 * (-c2 * (u2 * tmp1));
-      a[3][2] = -dt * tz2 * (-c2 * (u3 * tmp1));
-      a[3][3] = -dt * tz2 * (2.0e+00 - c2) * (u4 * tmp1) - dt * tz1 * (r43 * c34 * tmp1) - dt * tz1 * dz4;
-      a[3][4] = -dt * tz2 * c2;
-      a[4][0] = -dt * tz2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u4 * tmp1)) -
-                dt * tz1 *
-                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
-                     (r43 * c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
-      a[4][1] = -dt * tz2 * (-c2 * (u2 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u2;
-      a[4][2] = -dt * tz2 * (-c2 * (u3 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u3;
-      a[4][3] = -dt * tz2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + 3.0e+00 * u4 * u4) * tmp2)) -
-                dt * tz1 * (r43 * c34 - c1345) * tmp2 * u4;
-      a[4][4] = -dt * tz2 * (c1 * (u4 * tmp1)) - dt * tz1 * c1345 * tmp1 - dt * tz1 * dz5;
-    } else {
-      a[0][0] = -dt * tz1 * dz1;
-      a[0][1] = 0.0;
-      a[0][2] = 0.0;
-      a[0][3] = dt * tz2;
-      a[0][4] = 0.0;
-      a[1][0] = dt * tz2 * (-(u2 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u2);
-      a[1][1] = dt * tz2 * (u4 * tmp1) - dt * tz1 * c34 * tmp1 - dt * tz1 * dz2;
-      a[1][2] = 0.0;
-      a[1][3] = dt * tz2 * (u2 * tmp1);
-      a[1][4] = 0.0;
-      a[2][0] = dt * tz2 * (-(u3 * u4) * tmp2) - dt * tz1 * (-c34 * tmp2 * u3);
-      a[2][1] = 0.0;
-      a[2][2] = dt * tz2 * (u4 * tmp1) - dt * tz1 * (c34 * tmp1) - dt * tz1 * dz3;
-      a[2][3] = dt * tz2 * (u3 * tmp1);
-      a[2][4] = 0.0;
-      a[3][0] = dt * tz2 * (-((u4 * tmp1) * (u4 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
-                dt * tz1 * (-r43 * c34 * tmp2 * u4);
-      a[3][1] = dt * tz2 * (-c2 * (u2 * tmp1));
-      a[3][2] = dt * tz2 * (-c2 * (u3 * tmp1));
-      a[3][3] = dt * tz2 * (2.0e+00 - c2) * (u4 * tmp1) - dt * tz1 * (r43 * c34 * tmp1) - dt * tz1 * dz4;
-      a[3][4] = dt * tz2 * c2;
-      a[4][0] = dt * tz2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u4 * tmp1)) -
-                dt * tz1 *
-                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
-                     (r43 * c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
-      a[4][1] = dt * tz2 * (-c2 * (u2 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u2;
-      a[4][2] = dt * tz2 * (-c2 * (u3 * u4) * tmp2) - dt * tz1 * (c34 - c1345) * tmp2 * u3;
-      a[4][3] = dt * tz2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + 3.0e+00 * u4 * u4) * tmp2)) -
-                dt * tz1 * (r43 * c34 - c1345) * tmp2 * u4;
-      a[4][4] = dt * tz2 * (c1 * (u4 * tmp1)) - dt * tz1 * c1345 * tmp1 - dt * tz1 * dz5;
-    }
-  } else if (DIR == 1) {
-    const double ty1 = J.ty1, ty2 = J.ty2;
-    if (SG < 0) {
-      a[0][0] = -dt * ty1 * dy1;
-      a[0][1] = 0.0;
-      a[0][2] = -dt * ty2;
-      a[0][3] = 0.0;
-      a[0][4] = 0.0;
-      a[1][0] = -dt * ty2 * (-(u2 * u3) * tmp2) - dt * ty1 * (-c34 * tmp2 * u2);
-      a[1][1] = -dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy2;
-      a[1][2] = -dt * ty2 * (u2 * tmp1);
-      a[1][3] = 0.0;
-      a[1][4] = 0.0;
-      a[2][0] = -dt * ty2 * (-((u3 * tmp1) * (u3 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
-                dt * ty1 * (-r43 * c34 * tmp2 * u3);
-      a[2][1] = -dt * ty2 * (-c2 * (u2 * tmp1));
-      a[2][2] = -dt * ty2 * ((2.0e+00 - c2) * (u3 * tmp1)) - dt * ty1 * (r43 * c34 * tmp1) - dt * ty1 * dy3;
-      a[2][3] = -dt * ty2 * (-c2 * (u4 * tmp1));
-      a[2][4] = -dt * ty2 * c2;
-      a[3][0] = -dt * ty2 * (-(u3 * u4) * tmp2) - dt * ty1 * (-c34 * tmp2 * u4);
-      a[3][1] = 0.0;
-      a[3][2] = -dt * ty2 * (u4 * tmp1);
-      a[3][3] = -dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy4;
-      a[3][4] = 0.0;
-      a[4][0] = -dt * ty2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u3 * tmp1)) -
-                dt * ty1 *
-                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (r43 * c34 - c1345) * tmp3 * (u3 * u3) -
-                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
-      a[4][1] = -dt * ty2 * (-c2 * (u2 * u3) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u2;
-      a[4][2] = -dt * ty2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + 3.0e+00 * u3 * u3 + u4 * u4) * tmp2)) -
-                dt * ty1 * (r43 * c34 - c1345) * tmp2 * u3;
-      a[4][3] = -dt * ty2 * (-c2 * (u3 * u4) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u4;
-      a[4][4] = -dt * ty2 * (c1 * (u3 * tmp1)) - dt * ty1 * c1345 * tmp1 - dt * ty1 * dy5;
-    } else {
-      a[0][0] = -dt * ty1 * dy1;
-      a[0][1] = 0.0;
-      a[0][2] = dt * ty2;
-      a[0][3] = 0.0;
-      a[0][4] = 0.0;
-      a[1][0] = dt * ty2 * (-(u2 * u3) * tmp2) - dt * ty1 * (-c34 * tmp2 * u2);
-      a[1][1] = dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy2;
-      a[1][2] = dt * ty2 * (u2 * tmp1);
-      a[1][3] = 0.0;
-      a[1][4] = 0.0;
-      a[2][0] = dt * ty2 * (-((u3 * tmp1) * (u3 * tmp1)) + 0.50e+00 * c2 * ((u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
-                dt * ty1 * (-r43 * c34 * tmp2 * u3);
-      a[2][1] = dt * ty2 * (-c2 * (u2 * tmp1));
-      a[2][2] = dt * ty2 * ((2.0e+00 - c2) * (u3 * tmp1)) - dt * ty1 * (r43 * c34 * tmp1) - dt * ty1 * dy3;
-      a[2][3] = dt * ty2 * (-c2 * (u4 * tmp1));
-      a[2][4] = dt * ty2 * c2;
-      a[3][0] = dt * ty2 * (-(u3 * u4) * tmp2) - dt * ty1 * (-c34 * tmp2 * u4);
-      a[3][1] = 0.0;
-      a[3][2] = dt * ty2 * (u4 * tmp1);
-      a[3][3] = dt * ty2 * (u3 * tmp1) - dt * ty1 * (c34 * tmp1) - dt * ty1 * dy4;
-      a[3][4] = 0.0;
-      a[4][0] = dt * ty2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u3 * tmp1)) -
-                dt * ty1 *
-                    (-(c34 - c1345) * tmp3 * (u2 * u2) - (r43 * c34 - c1345) * tmp3 * (u3 * u3) -
-                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
-      a[4][1] = dt * ty2 * (-c2 * (u2 * u3) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u2;
-      a[4][2] = dt * ty2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((u2 * u2 + 3.0e+00 * u3 * u3 + u4 * u4) * tmp2)) -
-                dt * ty1 * (r43 * c34 - c1345) * tmp2 * u3;
-      a[4][3] = dt * ty2 * (-c2 * (u3 * u4) * tmp2) - dt * ty1 * (c34 - c1345) * tmp2 * u4;
-      a[4][4] = dt * ty2 * (c1 * (u3 * tmp1)) - dt * ty1 * c1345 * tmp1 - dt * ty1 * dy5;
-    }
-  } else {
-    const double tx1 = J.tx1, tx2 = J.tx2;
-    if (SG < 0) {
-      a[0][0] = -dt * tx1 * dx1;
-      a[0][1] = -dt * tx2;
-      a[0][2] = 0.0;
-      a[0][3] = 0.0;
-      a[0][4] = 0.0;
-      a[1][0] = -dt * tx2 * (-((u2 * tmp1) * (u2 * tmp1)) + c2 * 0.50e+00 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2) -
-                dt * tx1 * (-r43 * c34 * tmp2 * u2);
-      a[1][1] = -dt * tx2 * ((2.0e+00 - c2) * (u2 * tmp1)) - dt * tx1 * (r43 * c34 * tmp1) - dt * tx1 * dx2;
-      a[1][2] = -dt * tx2 * (-c2 * (u3 * tmp1));
-      a[1][3] = -dt * tx2 * (-c2 * (u4 * tmp1));
-      a[1][4] = -dt * tx2 * c2;
-      a[2][0] = -dt * tx2 * (-(u2 * u3) * tmp2) - dt * tx1 * (-c34 * tmp2 * u3);
-      a[2][1] = -dt * tx2 * (u3 * tmp1);
-      a[2][2] = -dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx3;
-      a[2][3] = 0.0;
-      a[2][4] = 0.0;
-      a[3][0] = -dt * tx2 * (-(u2 * u4) * tmp2) - dt * tx1 * (-c34 * tmp2 * u4);
-      a[3][1] = -dt * tx2 * (u4 * tmp1);
-      a[3][2] = 0.0;
-      a[3][3] = -dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx4;
-      a[3][4] = 0.0;
-      a[4][0] = -dt * tx2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u2 * tmp1)) -
-                dt * tx1 *
-                    (-(r43 * c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
-                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
-      a[4][1] = -dt * tx2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((3.0e+00 * u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
-                dt * tx1 * (r43 * c34 - c1345) * tmp2 * u2;
-      a[4][2] = -dt * tx2 * (-c2 * (u3 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u3;
-      a[4][3] = -dt * tx2 * (-c2 * (u4 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u4;
-      a[4][4] = -dt * tx2 * (c1 * (u2 * tmp1)) - dt * tx1 * c1345 * tmp1 - dt * tx1 * dx5;
-    } else {
-      a[0][0] = -dt * tx1 * dx1;
-      a[0][1] = dt * tx2;
-      a[0][2] = 0.0;
-      a[0][3] = 0.0;
-      a[0][4] = 0.0;
-      a[1][0] = dt * tx2 * (-((u2 * tmp1) * (u2 * tmp1)) + c2 * 0.50e+00 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2) -
-                dt * tx1 * (-r43 * c34 * tmp2 * u2);
-      a[1][1] = dt * tx2 * ((2.0e+00 - c2) * (u2 * tmp1)) - dt * tx1 * (r43 * c34 * tmp1) - dt * tx1 * dx2;
-      a[1][2] = dt * tx2 * (-c2 * (u3 * tmp1));
-      a[1][3] = dt * tx2 * (-c2 * (u4 * tmp1));
-      a[1][4] = dt * tx2 * c2;
-      a[2][0] = dt * tx2 * (-(u2 * u3) * tmp2) - dt * tx1 * (-c34 * tmp2 * u3);
-      a[2][1] = dt * tx2 * (u3 * tmp1);
-      a[2][2] = dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx3;
-      a[2][3] = 0.0;
-      a[2][4] = 0.0;
-      a[3][0] = dt * tx2 * (-(u2 * u4) * tmp2) - dt * tx1 * (-c34 * tmp2 * u4);
-      a[3][1] = dt * tx2 * (u4 * tmp1);
-      a[3][2] = 0.0;
-      a[3][3] = dt * tx2 * (u2 * tmp1) - dt * tx1 * (c34 * tmp1) - dt * tx1 * dx4;
-      a[3][4] = 0.0;
-      a[4][0] = dt * tx2 * ((c2 * (u2 * u2 + u3 * u3 + u4 * u4) * tmp2 - c1 * (u5 * tmp1)) * (u2 * tmp1)) -
-                dt * tx1 *
-                    (-(r43 * c34 - c1345) * tmp3 * (u2 * u2) - (c34 - c1345) * tmp3 * (u3 * u3) -
-                     (c34 - c1345) * tmp3 * (u4 * u4) - c1345 * tmp2 * u5);
-      a[4][1] = dt * tx2 * (c1 * (u5 * tmp1) - 0.50e+00 * c2 * ((3.0e+00 * u2 * u2 + u3 * u3 + u4 * u4) * tmp2)) -
-                dt * tx1 * (r43 * c34 - c1345) * tmp2 * u2;
-      a[4][2] = dt * tx2 * (-c2 * (u3 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u3;
-      a[4][3] = dt * tx2 * (-c2 * (u4 * u2) * tmp2) - dt * tx1 * (c34 - c1345) * tmp2 * u4;
-      a[4][4] = dt * tx2 * (c1 * (u2 * tmp1)) - dt * tx1 * c1345 * tmp1 - dt * tx1 * dx5;
-    }
-  }
-}
-
-// The t-th point (0-based) of hyperplane i + j + k = l of a zone's interior,
-// enumerated by k ascending, then j ascending.
-__device__ inline bool hyperplane_point(const LuZone& Z, int l, int t, int& i, int& j, int& k) {
-  const int klo = max(2, l - (Z.nx - 1) - (Z.ny - 1)), khi = min(Z.nz - 1, l - 4);
-  for (int kk = klo; kk <= khi; ++kk) {
-    const int s = l - kk;
-    const int jlo = max(2, s - (Z.nx - 1)), jhi = min(Z.ny - 1, s - 2);
-    const int c = jhi - jlo + 1;
-    if (c <= 0) continue;
-    if (t < c) {
-      k = kk;
-      j = jlo + t;
-      i = s - j;
-      return true;
-    }
-    t -= c;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void load5(const double* f, long long NP, long long p, double v[5]) {
-#pragma unroll
-  for (int m = 0; m < 5; ++m) v[m] = f[m * NP + p];
-}
-
-// The entries the reference assigns a literal 0.0 in each off-diagonal block
-// (the same pattern in jacld and jacu).  A product with one is +-0 and
-// adding it changes no sum's value, so the row sums below skip them.
-__host__ __device__ constexpr bool off_zero(int dir, int r, int c) {
-  return dir == 2 ? ((r == 0 && (c == 1 || c == 2 || c == 4)) || (r == 1 && (c == 2 || c == 4)) ||
-                     (r == 2 && (c == 1 || c == 4)))
-       : dir == 1 ? ((r == 0 && (c == 1 || c == 3 || c == 4)) || (r == 1 && (c == 3 || c == 4)) ||
-                     (r == 3 && (c == 1 || c == 4)))
-                  : ((r == 0 && (c == 2 || c == 3 || c == 4)) || (r == 2 && (c == 3 || c == 4)) ||
-                     (r == 3 && (c == 2 || c == 4)));
-}
-
-// Position of entry (r, c) among the 18 entries of block DIR that are not
-// structural zeros, row-major.
-__host__ __device__ constexpr int blk_idx(int dir, int r, int c) {
-  int n = 0;
-  for (int rr = 0; rr < 5; ++rr)
-    for (int cc = 0; cc < 5; ++cc) {
-      if (rr == r && cc == c) return n;
-      if (!off_zero(dir, rr, cc)) ++n;
-    }
-  return n;
-}
-constexpr int BLK_NZ = 18;
-
-// The 5x5 solve of blts / buts (src/LU/blts.jl:106-193, src/LU/buts.jl:113-200)
-// with tmat = d.  d is lower triangular with d[2][1] = d[3][1] = d[3][2] = 0
-// (jacld.jl / jacu.jl assign those 0.0), so the elimination leaves every
-// entry of tmat as it was, and every update the reference makes with a zero
-// multiplier (including buts's `tmat[5,5] -=- tmp * tmat[2,5]` and its back
-// substitution signs, whose terms are all products with zeros) leaves the
-// value it updates unchanged.  What remains, statement for statement:
-//   tmp_r0 = (1/t00) t_r0,  v_r <- v_r - v_0 tmp_r0         (r = 1..4)
-//   tmp_4c = (1/t_cc) t_4c, v_4 <- v_4 - v_c tmp_4c         (c = 1, 2, 3)
-//   v_r <- v_r / t_rr                                       (r = 4..0)
-// `jac` planes per interior point, stored at the point's hyperplane-ordered
-// index h = zone.off + hps[l] + t (t: its place in hyperplane l = i+j+k,
-// k then j ascending; hps[l]: the zone's interior points with i+j+k < l), so
-// that the sweeps, which run one hyperplane per launch, read them coalesced.
-// Written by k_lu_jac before the sweeps (u does not change until the
-// update):
-//   FAC_T + r, FAC_R0 + r-1, FAC_4C + c-1   t_rr, tmp_r0, tmp_4c of d
-//   FAC_BLK + (2 dir + s) * 18 + blk_idx    the non-zero entries of the
-//       off-diagonal block of direction dir: s = 0 jacld's (from the point
-//       at -1 in dir), s = 1 jacu's (from the point at +1)
-enum { FAC_T = 0, FAC_R0 = 5, FAC_4C = 9, FAC_BLK = 12, FAC_COUNT = 12 + 6 * 18 };
-
-template <int DIR, int S>
-__device__ __forceinline__ void store_blk(double* jac, long long NP, long long h, const double b[5][5]) {
-#pragma unroll
-  for (int r = 0; r < 5; ++r)
-#pragma unroll
-    for (int c = 0; c < 5; ++c)
-      if (!off_zero(DIR, r, c)) jac[(FAC_BLK + (2 * DIR + S) * BLK_NZ + blk_idx(DIR, r, c)) * NP + h] = b[r][c];
-}
-
-// the off-diagonal block (DIR, SG) from the state at q
-template <int DIR, int SG>
-__device__ __forceinline__ void blk_from(const LuDev& D, const JC& J, long long q, double b[5][5]) {
-  double w[5];
-  load5(D.u, D.NP, q, w);
-  jac_off<DIR, SG>(J, D.prim[PR_RHO * D.NP + q], w[1], w[2], w[3], w[4], b);
-}
-
-// jacld's and jacu's blocks and d's factors of every interior point (the
-// Jacobian work of ssor, taken off the wavefront), one thread per point in
-// hyperplane order (blockIdx.y: zone)
-__global__ void __launch_bounds__(TPB) k_lu_jac(LuDev D, const int* __restrict__ hps, int hstride,
-                                                double* __restrict__ jac) {
-  const int z = blockIdx.y;
-  const LuZone Z = D.zones[z];
-  const int* H = hps + (long long)z * hstride;
-  const int t = blockIdx.x * TPB + threadIdx.x;
-  const int lend = Z.nx + Z.ny + Z.nz - 3;
-  if (t >= H[lend + 1]) return;
-  int lo = 6, hi = lend;  // the hyperplane of t: largest l with H[l] <= t
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) / 2;
-    if (H[mid] <= t) lo = mid; else hi = mid - 1;
-  }
-  int i, j, k;
-  if (!hyperplane_point(Z, lo, t - H[lo], i, j, k)) return;
-  const long long NP = D.NP, p = pidx(Z, i, j, k), h = Z.off + t;
-  const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
-  double b[5][5];
-  blk_from<0, -1>(D, J, pidx(Z, i - 1, j, k), b);
-  store_blk<0, 0>(jac, NP, h, b);
-  blk_from<0, 1>(D, J, pidx(Z, i + 1, j, k), b);
-  store_blk<0, 1>(jac, NP, h, b);
-  blk_from<1, -1>(D, J, pidx(Z, i, j - 1, k), b);
-  store_blk<1, 0>(jac, NP, h, b);
-  blk_from<1, 1>(D, J, pidx(Z, i, j + 1, k), b);
-  store_blk<1, 1>(jac, NP, h, b);
-  blk_from<2, -1>(D, J, pidx(Z, i, j, k - 1), b);
-  store_blk<2, 0>(jac, NP, h, b);
-  blk_from<2, 1>(D, J, pidx(Z, i, j, k + 1), b);
-  store_blk<2, 1>(jac, NP, h, b);
-  double w[5];
-  load5(D.u, NP, p, w);
-  jac_d(J, D.prim[PR_RHO * NP + p], w[1], w[2], w[3], w[4], b);
-  const double rinv0 = 1.0e+00 / b[0][0];
-#pragma unroll
-  for (int r = 0; r < 5; ++r) jac[(FAC_T + r) * NP + h] = b[r][r];
-#pragma unroll
-  for (int r = 1; r < 5; ++r) jac[(FAC_R0 + r - 1) * NP + h] = rinv0 * b[r][0];
-#pragma unroll
-  for (int c = 1; c <= 3; ++c) jac[(FAC_4C + c - 1) * NP + h] = (1.0e+00 / b[c][c]) * b[4][c];
-}
-
-// row M of the point's block (DIR, S) dotted with w, summed left to right as
-// the reference does (structural zeros skipped: a product with one is +-0
-// and adding it changes no sum's value)
-template <int DIR, int S, int M>
-__device__ __forceinline__ double row_dot(const double* __restrict__ jac, long long NP, long long h,
-                                          const double w[5]) {
-  double s = 0.0;
-  bool first = true;
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    if (off_zero(DIR, M, c)) continue;
-    const double t = jac[(FAC_BLK + (2 * DIR + S) * BLK_NZ + blk_idx(DIR, M, c)) * NP + h] * w[c];
-    s = first ? t : s + t;
-    first = false;
-  }
-  return s;
-}
-
-// sum over c of Y[M][c] wy[c] + X[M][c] wx[c] (y term first, as blts / buts
-// write it)
-template <int S, int M>
-__device__ __forceinline__ double row_dot2(const double* __restrict__ jac, long long NP, long long h,
-                                           const double wy[5], const double wx[5]) {
-  double s = 0.0;
-  bool first = true;
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    if (!off_zero(1, M, c)) {
-      const double t = jac[(FAC_BLK + (2 + S) * BLK_NZ + blk_idx(1, M, c)) * NP + h] * wy[c];
-      s = first ? t : s + t;
-      first = false;
-    }
-    if (!off_zero(0, M, c)) {
-      const double t = jac[(FAC_BLK + S * BLK_NZ + blk_idx(0, M, c)) * NP + h] * wx[c];
-      s = first ? t : s + t;
-      first = false;
-    }
-  }
-  return s;
-}
-
-constexpr int HP = 32;  // points per block of the sweep kernels (x 5 rows)
-
-// blts's two update loops for row M of one point (h: its jac index)
-template <int M, bool SCALE>
-__device__ __forceinline__ double lower_row(const LuDev& D, const double* __restrict__ jac, const LuZone& Z, int i,
-                                            int j, int k, long long h) {
-  const long long NP = D.NP, p = pidx(Z, i, j, k);
-  const double omega = D.omega;
-  double v = D.rsd[M * NP + p];
-  if (SCALE) v = D.dt * v;
-  double w[5], x[5];
-  load5(D.rsd, NP, pidx(Z, i, j, k - 1), w);
-  v = v - omega * row_dot<2, 0, M>(jac, NP, h, w);
-  load5(D.rsd, NP, pidx(Z, i, j - 1, k), w);
-  load5(D.rsd, NP, pidx(Z, i - 1, j, k), x);
-  v = v - omega * row_dot2<0, M>(jac, NP, h, w, x);
-  return v;
-}
-
-// the forward substitution with d's factors (rows exchanged through shared
-// memory); v: this thread's row, sv: every row of the point
-__device__ __forceinline__ double d_solve(const double* __restrict__ jac, long long NP, long long h, int m, double v,
-                                          const double sv[5]) {
-  const double v0 = sv[0];
-  if (m == 0) return v / jac[FAC_T * NP + h];
-  if (m < 4) {
-    v = v - v0 * jac[(FAC_R0 + m - 1) * NP + h];
-    return v / jac[(FAC_T + m) * NP + h];
-  }
-  v = v - v0 * jac[(FAC_R0 + 3) * NP + h];
-#pragma unroll
-  for (int c = 1; c <= 3; ++c) {
-    const double vc = sv[c] - v0 * jac[(FAC_R0 + c - 1) * NP + h];  // v_c after column 0, as row c has it
-    v = v - vc * jac[(FAC_4C + c - 1) * NP + h];
-  }
-  return v / jac[(FAC_T + 4) * NP + h];
-}
-
-// jacld + blts at every point of hyperplane l (blockIdx.y: zone - zone0),
-// five threads per point (threadIdx.y: row).  SCALE: rsd *= dt at the point
-// first (ssor's scaling, fused: blts reads only points it has already scaled
-// and solved, or boundary points, which the scaling does not touch).
-template <bool SCALE>
-__global__ void __launch_bounds__(HP * 5) k_lu_lower(LuDev D, const double* __restrict__ jac,
-                                                     const int* __restrict__ hps, int hstride, int l, int zone0) {
-  __shared__ double sv[HP][5];
-  const int m = threadIdx.y, a = threadIdx.x, z = zone0 + blockIdx.y;
-  const LuZone Z = D.zones[z];
-  const int t = blockIdx.x * HP + a;
-  int i = 0, j = 0, k = 0;
-  const bool ok = hyperplane_point(Z, l, t, i, j, k);
-  const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
-  double v = 0.0;
-  if (ok) {
-    switch (m) {
-      case 0: v = lower_row<0, SCALE>(D, jac, Z, i, j, k, h); break;
-      case 1: v = lower_row<1, SCALE>(D, jac, Z, i, j, k, h); break;
-      case 2: v = lower_row<2, SCALE>(D, jac, Z, i, j, k, h); break;
-      case 3: v = lower_row<3, SCALE>(D, jac, Z, i, j, k, h); break;
-      default: v = lower_row<4, SCALE>(D, jac, Z, i, j, k, h); break;
-    }
-    sv[a][m] = v;
-  }
-  __syncthreads();
-  if (!ok) return;
-  D.rsd[m * D.NP + pidx(Z, i, j, k)] = d_solve(jac, D.NP, h, m, v, sv[a]);
-}
-
-// buts's two tv loops for row M of one point
-template <int M>
-__device__ __forceinline__ double upper_row(const LuDev& D, const double* __restrict__ jac, const LuZone& Z, int i,
-                                            int j, int k, long long h) {
-  const long long NP = D.NP;
-  const double omega = D.omega;
-  double w[5], x[5];
-  load5(D.rsd, NP, pidx(Z, i, j, k + 1), w);
-  double tv = omega * row_dot<2, 1, M>(jac, NP, h, w);
-  load5(D.rsd, NP, pidx(Z, i, j + 1, k), w);
-  load5(D.rsd, NP, pidx(Z, i + 1, j, k), x);
-  tv = tv + omega * row_dot2<1, M>(jac, NP, h, w, x);
-  return tv;
-}
-
-// jacu + buts at every point of hyperplane l
-__global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __restrict__ jac,
-                                                     const int* __restrict__ hps, int hstride, int l, int zone0) {
-  __shared__ double sv[HP][5];
-  const int m = threadIdx.y, a = threadIdx.x, z = zone0 + blockIdx.y;
-  const LuZone Z = D.zones[z];
-  const int t = blockIdx.x * HP + a;
-  int i = 0, j = 0, k = 0;
-  const bool ok = hyperplane_point(Z, l, t, i, j, k);
-  const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
-  double tv = 0.0;
-  if (ok) {
-    switch (m) {
-      case 0: tv = upper_row<0>(D, jac, Z, i, j, k, h); break;
-      case 1: tv = upper_row<1>(D, jac, Z, i, j, k, h); break;
-      case 2: tv = upper_row<2>(D, jac, Z, i, j, k, h); break;
-      case 3: tv = upper_row<3>(D, jac, Z, i, j, k, h); break;
-      default: tv = upper_row<4>(D, jac, Z, i, j, k, h); break;
-    }
-    sv[a][m] = tv;
-  }
-  __syncthreads();
-  if (!ok) return;
-  tv = d_solve(jac, D.NP, h, m, tv, sv[a]);
-  const long long p = pidx(Z, i, j, k);
-  D.rsd[m * D.NP + p] = D.rsd[m * D.NP + p] - tv;
-}
-
-// ---- exch_qbc (src/LU/exchange_qbc.jl) --------------------------------------
-// Staging per zone: east face (j = ny-1) and west face (j = 2), nx*nkp points
-// each; south face (i = nx-1) and north face (i = 2), ny*nkp points each;
-// planes k = klo..klo+nkp-1; element [m][k][pos].
-struct Faces {
-  double* stage;
-  const long long* zoff;  // staging offset of each zone
-  const int* nbr;         // west, east, south, north per zone
-  int klo, nkp;
-};
-
-__device__ inline void face_sizes(const LuZone& Z, int nkp, long long& e, long long& s) {
-  e = (long long)Z.nx * nkp;
-  s = (long long)Z.ny * nkp;
-}
-
-__global__ void __launch_bounds__(TPB) k_lu_pack(LuDev D, Faces F, int nzones) {
-  const int z = blockIdx.y;
-  if (z >= nzones) return;
-  const LuZone Z = D.zones[z];
-  const int per = 2 * Z.nx + 2 * Z.ny;
-  const int t = blockIdx.x * TPB + threadIdx.x;
-  if (t >= per * F.nkp) return;
-  const int kq = t / per, pos = t % per, k = F.klo + kq;
-  long long ne, ns;
-  face_sizes(Z, F.nkp, ne, ns);
-  double* base = F.stage + F.zoff[z];
-  int i, j;
-  long long so;
-  if (pos < Z.nx) {  // east face
-    i = pos + 1; j = Z.ny - 1; so = 0 * ne + (long long)kq * Z.nx + pos;
-  } else if (pos < 2 * Z.nx) {  // west face
-    i = pos - Z.nx + 1; j = 2; so = 5 * ne + (long long)kq * Z.nx + (pos - Z.nx);
-  } else if (pos < 2 * Z.nx + Z.ny) {  // south face
-    i = Z.nx - 1; j = pos - 2 * Z.nx + 1; so = 10 * ne + (long long)kq * Z.ny + (j - 1);
-  } else {  // north face
-    i = 2; j = pos - 2 * Z.nx - Z.ny + 1; so = 10 * ne + 5 * ns + (long long)kq * Z.ny + (j - 1);
-  }
-  const long long p = pidx(Z, i, j, k);
-  const long long stride = pos < 2 * Z.nx ? ne : ns;
-#pragma unroll
-  for (int m = 0; m < 5; ++m) base[so + m * stride] = D.u[m * D.NP + p];
-}
-
-// Every ghost point has one writer: j = 1 / j = ny (west / east) include the
-// corners, which the reference's unpack order (south, north, west, east)
-// leaves to them.
-__global__ void __launch_bounds__(TPB) k_lu_unpack(LuDev D, Faces F, int nzones) {
-  const int z = blockIdx.y;
-  if (z >= nzones) return;
-  const LuZone Z = D.zones[z];
-  const int per = 2 * Z.nx + 2 * (Z.ny - 2);
-  const int t = blockIdx.x * TPB + threadIdx.x;
-  if (t >= per * F.nkp) return;
-  const int kq = t / per, pos = t % per, k = F.klo + kq;
-  int i, j, src;
-  long long so, stride;
-  if (pos < Z.nx) {  // west ghost j = 1 <- west zone's east face
-    i = pos + 1; j = 1; src = F.nbr[4 * z + 0];
-    const LuZone S = D.zones[src];
-    long long ne, ns;
-    face_sizes(S, F.nkp, ne, ns);
-    so = F.zoff[src] + 0 * ne + (long long)kq * S.nx + (i - 1); stride = ne;
-  } else if (pos < 2 * Z.nx) {  // east ghost j = ny <- east zone's west face
-    i = pos - Z.nx + 1; j = Z.ny; src = F.nbr[4 * z + 1];
-    const LuZone S = D.zones[src];
-    long long ne, ns;
-    face_sizes(S, F.nkp, ne, ns);
-    so = F.zoff[src] + 5 * ne + (long long)kq * S.nx + (i - 1); stride = ne;
-  } else if (pos < 2 * Z.nx + (Z.ny - 2)) {  // north ghost i = 1 <- north zone's south face
-    i = 1; j = pos - 2 * Z.nx + 2; src = F.nbr[4 * z + 3];
-    const LuZone S = D.zones[src];
-    long long ne, ns;
-    face_sizes(S, F.nkp, ne, ns);
-    so = F.zoff[src] + 10 * ne + (long long)kq * S.ny + (j - 1); stride = ns;
-  } else {  // south ghost i = nx <- south zone's north face
-    i = Z.nx; j = pos - 2 * Z.nx - (Z.ny - 2) + 2; src = F.nbr[4 * z + 2];
-    const LuZone S = D.zones[src];
-    long long ne, ns;
-    face_sizes(S, F.nkp, ne, ns);
-    so = F.zoff[src] + 10 * ne + 5 * ns + (long long)kq * S.ny + (j - 1); stride = ns;
-  }
-  const long long p = pidx(Z, i, j, k);
-  double g[5];
-#pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    g[m] = F.stage[so + m * stride];
-    D.u[m * D.NP + p] = g[m];
-  }
-  store_prim(D.prim, D.NP, p, g);
-}
-
-// ---- norms (src/LU/l2norm.jl, src/LU/error.jl, src/LU/pintgr.jl) -----------
-// WHICH 0: sum of rsd^2, 1: sum of (exact - u)^2 over the interior; one row
-// of 5 partial sums per work block (fixed-order tree reduction)
-template <int WHICH>
-__global__ void __launch_bounds__(TPB) k_lu_norm_partial(LuDev D, const LuWork* __restrict__ work, CeTable ce,
-                                                         double* partial) {
-  __shared__ double sh[5][TPB];
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
-  double s[5] = {0, 0, 0, 0, 0};
-  int i, j, k;
-  if (decode(Z, w.first + threadIdx.x, i, j, k) && interior(Z, i, j, k)) {
-    const long long p = pidx(Z, i, j, k);
-    if (WHICH == 0) {
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const double r = D.rsd[m * D.NP + p];
-        s[m] = r * r;
-      }
-    } else {
-      double e[5];
-      exact_point(ce, i, j, k, Z.nx, Z.ny, Z.nz, e);
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const double t = e[m] - D.u[m * D.NP + p];
-        s[m] = t * t;
-      }
-    }
-  }
-#pragma unroll
-  for (int m = 0; m < 5; ++m) sh[m][threadIdx.x] = s[m];
-  __syncthreads();
-  for (int h = TPB / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h)
-#pragma unroll
-      for (int m = 0; m < 5; ++m) sh[m][threadIdx.x] += sh[m][threadIdx.x + h];
-    __syncthreads();
-  }
-  if (threadIdx.x < 5) partial[(long long)blockIdx.x * 5 + threadIdx.x] = sh[threadIdx.x][0];
-}
-
-// per zone: sqrt(sum / ((nx-2)(ny-2)(nz-2))), then summed over zones in
-// order into out[5] (+ out_zone[5*z + m] when non-null); one thread per m
-__global__ void k_lu_norm_finish(const LuZone* zones, const int* zblock, int nzones, const double* partial,
-                                 double* out, double* out_zone) {
-  const int m = threadIdx.x;
-  if (m >= 5) return;
-  double total = 0.0;
-  for (int z = 0; z < nzones; ++z) {
-    double s = 0.0;
-    for (int b = zblock[z]; b < zblock[z + 1]; ++b) s += partial[(long long)b * 5 + m];
-    const LuZone Z = zones[z];
-    const double r = sqrt(s / ((double)(Z.nx - 2) * (Z.ny - 2) * (Z.nz - 2)));
-    if (out_zone) out_zone[5 * z + m] = r;
-    total += r;
-  }
-  out[m] = total;
-}
-
-// pintgr of one zone per block (one process: ibeg = ii1, ifin = ii2,
-// jbeg = ji1, jfin = ji2); frc[z] = 0.25 (frc1 + frc2 + frc3)
-__global__ void __launch_bounds__(TPB) k_lu_pintgr(LuDev D, double* frc) {
-  __shared__ double sh[3][TPB];
-  const LuZone Z = D.zones[blockIdx.x];
-  const int ibeg = ii1, ifin = Z.ii2, jbeg = ji1, jfin = Z.ji2, ifin1 = ifin - 1, jfin1 = jfin - 1;
-  auto phi = [&](int i, int j, int k) {
-    const long long p = pidx(Z, i, j, k);
-    const double u1 = D.u[p], u2 = D.u[D.NP + p], u3 = D.u[2 * D.NP + p], u4 = D.u[3 * D.NP + p],
-                 u5 = D.u[4 * D.NP + p];
-    return c2 * (u5 - 0.50e+00 * (u2 * u2 + u3 * u3 + u4 * u4) / u1);
-  };
-  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
-  const int n1i = ifin1 - ibeg + 1, n1j = jfin1 - jbeg + 1, nk = Z.ki2 - 1 - ki1 + 1;
-  for (int t = threadIdx.x; t < n1i * n1j; t += TPB) {
-    const int i = ibeg + t % n1i, j = jbeg + t / n1i;
-    s1 += (phi(i, j, ki1) + phi(i + 1, j, ki1) + phi(i, j + 1, ki1) + phi(i + 1, j + 1, ki1) + phi(i, j, Z.ki2) +
-           phi(i + 1, j, Z.ki2) + phi(i, j + 1, Z.ki2) + phi(i + 1, j + 1, Z.ki2));
-  }
-  for (int t = threadIdx.x; t < n1i * nk; t += TPB) {
-    const int i = ibeg + t % n1i, k = ki1 + t / n1i;
-    s2 += (phi(i, jbeg, k) + phi(i + 1, jbeg, k) + phi(i, jbeg, k + 1) + phi(i + 1, jbeg, k + 1) + phi(i, jfin, k) +
-           phi(i + 1, jfin, k) + phi(i, jfin, k + 1) + phi(i + 1, jfin, k + 1));
-  }
-  for (int t = threadIdx.x; t < n1j * nk; t += TPB) {
-    const int j = jbeg + t % n1j, k = ki1 + t / n1j;
-    s3 += (phi(ibeg, j, k) + phi(ibeg, j + 1, k) + phi(ibeg, j, k + 1) + phi(ibeg, j + 1, k + 1) + phi(ifin, j, k) +
-           phi(ifin, j + 1, k) + phi(ifin, j, k + 1) + phi(ifin, j + 1, k + 1));
-  }
-  sh[0][threadIdx.x] = s1;
-  sh[1][threadIdx.x] = s2;
-  sh[2][threadIdx.x] = s3;
-  __syncthreads();
-  for (int h = TPB / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h)
-      for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + h];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const double frc1 = Z.dxi * Z.deta * sh[0][0];
-    const double frc2 = Z.dxi * Z.dzeta * sh[1][0];
-    const double frc3 = Z.deta * Z.dzeta * sh[2][0];
-    frc[blockIdx.x] = 0.25e+00 * (frc1 + frc2 + frc3);
-  }
-}
-
-// ---- layout conversion --------------------------------------------------------
-// REF: [1:5, -1:nx+2, -1:ny+2, 1:nz] column-major; DENSE: [m][k][j][i]
-template <bool REF, bool TO_DEV>
-__global__ void __launch_bounds__(TPB) k_lu_convert(LuDev D, double* field, double* host_img, int zone) {
-  const LuZone Z = D.zones[zone];
-  const int q = blockIdx.x * TPB + threadIdx.x;
-  if (q >= Z.np) return;
-  const int i = q % Z.nx + 1, j = (q / Z.nx) % Z.ny + 1, k = q / (Z.nx * Z.ny) + 1;
-  const long long p = pidx(Z, i, j, k);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    const long long h = REF ? m + 5LL * ((i + 1) + (long long)(Z.nx + 4) * ((j + 1) + (long long)(Z.ny + 4) * (k - 1)))
-                            : (long long)m * Z.np + q;
-    if (TO_DEV)
-      field[m * D.NP + p] = host_img[h];
-    else
-      host_img[h] = field[m * D.NP + p];
-  }
-}
-
 }  // namespace
+
 
 // ============================== C ABI =========================================
 struct npbmz_lu_handle {
   int nzones = 0, flags = 0;
+  bool fast = false;  // NPBMZ_LU_FMA: the hot kernels from lu_fast
   double dt = 0, omega = 0;
   long long NP = 0;
   std::vector<LuZone> zh;
@@ -1258,15 +151,19 @@ int launch_exch(npbmz_lu_t* h) {
   int maxper = 0;
   for (const LuZone& Z : h->zh) maxper = std::max(maxper, 2 * Z.nx + 2 * Z.ny);
   const dim3 g((maxper * h->nkp + TPB - 1) / TPB, h->nzones);
-  k_lu_pack<<<g, TPB, 0, h->stream>>>(dev(h), faces(h), h->nzones);
-  k_lu_unpack<<<g, TPB, 0, h->stream>>>(dev(h), faces(h), h->nzones);
+  lu_exact::pack(dev(h), faces(h), h->nzones, g, h->stream);
+  if (h->fast)
+    lu_fast::unpack(dev(h), faces(h), h->nzones, g, h->stream);
+  else
+    lu_exact::unpack(dev(h), faces(h), h->nzones, g, h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
 
 int launch_jac(npbmz_lu_t* h, int z0, int nzs) {
   const dim3 gj((h->max_interior + TPB - 1) / TPB, nzs);
-  k_lu_jac<<<gj, TPB, 0, h->stream>>>(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride, h->fac);
+  (h->fast ? lu_fast::jac : lu_exact::jac)(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride,
+                                          h->fac, gj, h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
@@ -1276,11 +173,8 @@ int launch_lower(npbmz_lu_t* h, bool scale, int z0, int nzs) {
     int c = 0;
     for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
     if (!c) continue;
-    const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
-    if (scale)
-      k_lu_lower<true><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
-    else
-      k_lu_lower<false><<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
+    const dim3 g((c + HP - 1) / HP, nzs);
+    (h->fast ? lu_fast::lower : lu_exact::lower)(scale, dev(h), h->fac, h->hps_d, h->hstride, l, z0, g, h->stream);
   }
   LU_CK(h, cudaGetLastError());
   return 0;
@@ -1293,13 +187,14 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
   const int z0 = zone < 0 ? 0 : zone, nzs = zone < 0 ? h->nzones : 1;
   switch (phase) {
     case NPBMZ_LU_PHASE_RHS:
-      k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), w, h->u, h->prim, h->rsd);
+      (h->fast ? lu_fast::rhs : lu_exact::rhs)(false, dev(h), w, n, h->u, h->prim, h->rsd, h->stream);
       break;
     case NPBMZ_LU_PHASE_SCALE:
-      k_lu_pointwise<false><<<n, TPB, 0, h->stream>>>(dev(h), w, 0.0);
+      lu_exact::pointwise(false, dev(h), w, n, 0.0, h->stream);
       break;
     case NPBMZ_LU_PHASE_UPDATE:
-      k_lu_pointwise<true><<<n, TPB, 0, h->stream>>>(dev(h), w, 1.0e+00 / (h->omega * (2.0e+00 - h->omega)));
+      (h->fast ? lu_fast::pointwise : lu_exact::pointwise)(true, dev(h), w, n,
+                                                            1.0e+00 / (h->omega * (2.0e+00 - h->omega)), h->stream);
       break;
     case NPBMZ_LU_PHASE_EXCH:
       return launch_exch(h);
@@ -1317,8 +212,8 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
         if (!c) continue;
-        const dim3 g((c + HP - 1) / HP, nzs), b(HP, 5);
-        k_lu_upper<<<g, b, 0, h->stream>>>(dev(h), h->fac, h->hps_d, h->hstride, l, z0);
+        const dim3 g((c + HP - 1) / HP, nzs);
+        (h->fast ? lu_fast::upper : lu_exact::upper)(dev(h), h->fac, h->hps_d, h->hstride, l, z0, g, h->stream);
       }
       break;
     case NPBMZ_LU_PHASE_SSOR: {
@@ -1342,8 +237,8 @@ int launch_iteration(npbmz_lu_t* h) {
 }
 
 int launch_rsd_norm(npbmz_lu_t* h, double* out) {
-  k_lu_norm_partial<0><<<(int)h->work_h.size(), TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce, h->partial);
-  k_lu_norm_finish<<<1, 32, 0, h->stream>>>(h->zones_d, h->zblock_d, h->nzones, h->partial, out, nullptr);
+  lu_exact::norm_partial(0, dev(h), h->work_d, (int)h->work_h.size(), h->ce, h->partial, h->stream);
+  lu_exact::norm_finish(h->zones_d, h->zblock_d, h->nzones, h->partial, out, h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
@@ -1380,19 +275,14 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
     const int blocks = (Z.np + TPB - 1) / TPB;
     if (up) {
       LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-      if (layout == NPBMZ_LAYOUT_REF)
-        k_lu_convert<true, true><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
-      else
-        k_lu_convert<false, true><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+      lu_exact::convert(layout == NPBMZ_LAYOUT_REF, true, dev(h), f, h->img, z, blocks, h->stream);
       if (field == NPBMZ_LU_U)
-        k_lu_prim<<<h->zblock[z + 1] - h->zblock[z], TPB, 0, h->stream>>>(dev(h), h->work_d + h->zblock[z], h->u);
+        (h->fast ? lu_fast::prim : lu_exact::prim)(dev(h), h->work_d + h->zblock[z], h->zblock[z + 1] - h->zblock[z],
+                                                  h->u, h->stream);
     } else {
       if (layout == NPBMZ_LAYOUT_REF)  // keep the host halo: start from the host image
         LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-      if (layout == NPBMZ_LAYOUT_REF)
-        k_lu_convert<true, false><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
-      else
-        k_lu_convert<false, false><<<blocks, TPB, 0, h->stream>>>(dev(h), f, h->img, z);
+      lu_exact::convert(layout == NPBMZ_LAYOUT_REF, false, dev(h), f, h->img, z, blocks, h->stream);
       LU_CK(h, cudaMemcpyAsync(host, h->img, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     }
     LU_CK(h, cudaGetLastError());
@@ -1476,10 +366,11 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
   if (!out) return -1;
   *out = nullptr;
   if (nzones < 1 || !nx || !ny || !nz || !nbr || !params) return -1;
-  if (flags & ~(NPBMZ_LU_FACES_NPB | NPBMZ_LU_GRAPH)) return -1;
+  if (flags & ~(NPBMZ_LU_FACES_NPB | NPBMZ_LU_GRAPH | NPBMZ_LU_FMA)) return -1;
   npbmz_lu_t* h = new npbmz_lu_t();
   h->nzones = nzones;
   h->flags = flags;
+  h->fast = (flags & NPBMZ_LU_FMA) != 0;
   h->dt = params[0];
   h->omega = params[1];
   std::memcpy(h->ce.c, ce_reference, sizeof(h->ce.c));
@@ -1595,12 +486,13 @@ int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
   std::lock_guard<std::mutex> g(h->mu);
   std::memcpy(h->ce.c, ce ? ce : &ce_reference[0][0], sizeof(h->ce.c));
   const int n = (int)h->work_h.size();
-  k_lu_init<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce);
-  k_lu_poly<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce);
-  k_lu_prim<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->rsd);
-  k_lu_rhs<true><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->rsd, h->prim, h->frct);
-  k_lu_prim<<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->u);
-  k_lu_rhs<false><<<n, TPB, 0, h->stream>>>(dev(h), h->work_d, h->u, h->prim, h->rsd);
+  // set-up always without contraction: both builds start from the same state
+  lu_exact::init(dev(h), h->work_d, n, h->ce, h->stream);
+  lu_exact::poly(dev(h), h->work_d, n, h->ce, h->stream);
+  lu_exact::prim(dev(h), h->work_d, n, h->rsd, h->stream);
+  lu_exact::rhs(true, dev(h), h->work_d, n, h->rsd, h->prim, h->frct, h->stream);
+  (h->fast ? lu_fast::prim : lu_exact::prim)(dev(h), h->work_d, n, h->u, h->stream);
+  (h->fast ? lu_fast::rhs : lu_exact::rhs)(false, dev(h), h->work_d, n, h->u, h->prim, h->rsd, h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
@@ -1682,9 +574,9 @@ int npbmz_lu_verify(npbmz_lu_t* h, double* xcr, double* xce, double* xci) {
   if (!xcr || !xce || !xci) return fail(h, "null output");
   double* o = h->zone_out_d;  // [0,5) xcr, [5,10) xce, [16, 16+nzones) frc per zone
   if (launch_rsd_norm(h, o)) return -1;
-  k_lu_norm_partial<1><<<(int)h->work_h.size(), TPB, 0, h->stream>>>(dev(h), h->work_d, h->ce, h->partial);
-  k_lu_norm_finish<<<1, 32, 0, h->stream>>>(h->zones_d, h->zblock_d, h->nzones, h->partial, o + 5, nullptr);
-  k_lu_pintgr<<<h->nzones, TPB, 0, h->stream>>>(dev(h), o + 16);
+  lu_exact::norm_partial(1, dev(h), h->work_d, (int)h->work_h.size(), h->ce, h->partial, h->stream);
+  lu_exact::norm_finish(h->zones_d, h->zblock_d, h->nzones, h->partial, o + 5, h->stream);
+  lu_exact::pintgr(dev(h), h->nzones, o + 16, h->stream);
   LU_CK(h, cudaGetLastError());
   std::vector<double> host(16 + h->nzones);
   LU_CK(h, cudaMemcpyAsync(host.data(), o, host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));

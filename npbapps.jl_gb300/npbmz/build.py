@@ -7,7 +7,9 @@ The translation units compile in parallel:
   npbmz_api.cu                    the C ABI (include/npbmz.h)
   noalloc.cu         -fmad=true   the x sweep over a file-scope device array
   adjoint.cu         -fmad=true   the discrete adjoint of the BT and SP steps
-  lu.cu              -fmad=false  LU-MZ's SSOR iteration and its C ABI (include/npbmz_lu.h)
+  lu.cu                           the C ABI of LU-MZ's SSOR iteration (include/npbmz_lu.h)
+  lu_exact.cu        -fmad=false  its kernels (lu_kernels.cuh) with the reference's rounding
+  lu_fast.cu         -fmad=true   the same kernels with FMA contraction (NPBMZ_LU_FMA)
 and are linked into npbapps.jl_gb300/npbmz/_build/libnpbmz_gpu.so.
 """
 import os
@@ -32,7 +34,9 @@ UNITS = {
     "npbmz_api.cu": [],
     "noalloc.cu": ["-fmad=true"],
     "adjoint.cu": ["-fmad=true"],
-    "lu.cu": ["-fmad=false"],
+    "lu.cu": [],
+    "lu_exact.cu": ["-fmad=false"],
+    "lu_fast.cu": ["-fmad=true"],
 }
 
 

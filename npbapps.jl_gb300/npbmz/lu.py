@@ -23,6 +23,7 @@ LU_EXPORTS = [
 # flags, fields and phases (include/npbmz_lu.h)
 FACES_NPB = 0x1
 GRAPH = 0x2
+FMA = 0x4
 U, RSD, FRCT = 0, 1, 2
 PHASE_RHS, PHASE_SCALE, PHASE_LOWER, PHASE_UPPER, PHASE_UPDATE, PHASE_EXCH, PHASE_SSOR = range(7)
 PROFILE_PHASES = ("exch", "jac", "lower", "upper", "update", "rhs")

@@ -171,3 +171,32 @@ def test_phase_and_zone_errors_are_reported():
     with pytest.raises(npbmz.NpbmzError, match="zone"):
         p.ssor(16)
     assert p.launches_per_iteration() == 5 + 2 * (6 + 6 + 6 - 3 - 6 + 1)
+
+
+@pytest.mark.parametrize("name,niter", [("S", 50), ("W", 40), ("rect", 20)])
+def test_fma_build_stays_within_rounding_of_the_oracle(name, niter):
+    """NPBMZ_LU_FMA: the iteration's kernels with a*b+c contracted.  Not
+    bit-for-bit; after niter iterations u stays within 1e-12 (relative to
+    each variable's largest magnitude) and the norms within 1e-10 of the
+    oracle, and set-up is still bit-for-bit (it runs uncontracted)."""
+    g, dt = GEOMS[name]
+    p, r = make(g(), dt, lu.FACES_NPB | lu.GRAPH | lu.FMA)
+    for z in range(p.nzones):
+        np.testing.assert_array_equal(p.download(z, lu.U), r.get(lu.U, z))
+        np.testing.assert_array_equal(p.download(z, lu.FRCT), r.get(lu.FRCT, z))
+    p.iterate(niter)
+    r.iterate(niter)
+    for z in range(p.nzones):
+        a, b = p.download(z, lu.U), r.get(lu.U, z)
+        scale = np.max(np.abs(b), axis=(1, 2, 3), keepdims=True)
+        assert np.max(np.abs(a - b) / scale) <= 1e-12
+    x, y = p.verify(), r.verify()
+    np.testing.assert_allclose(x[0], y[0], rtol=1e-10)
+    np.testing.assert_allclose(x[1], y[1], rtol=1e-10)
+    np.testing.assert_allclose(x[2], y[2], rtol=1e-10)
+
+
+@pytest.mark.parametrize("cls", ["S", "W", "A"])
+def test_fma_build_meets_the_golden_norms(cls):
+    xcr, xce, xci, verified = lu.go(cls, flags=lu.FACES_NPB | lu.GRAPH | lu.FMA)
+    assert verified, (xcr, xce, xci)
