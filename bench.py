@@ -333,7 +333,7 @@ def run_gpu_lu(args, cls, desc):
         dist = tdist
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream()
-    flags = lu.GRAPH
+    flags = lu.GRAPH | (lu.FMA if args.variant == "fma-graph" else 0)
 
     def make(fl):
         p = lu.LuProblem.from_class(cls, fl)
@@ -443,7 +443,8 @@ def run_gpu_lu(args, cls, desc):
             "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "points_per_gpu": pts, "zones": p.nzones, "variant": "fp64-graph",
+            "config": {"workload": desc, "points_per_gpu": pts, "zones": p.nzones,
+                       "variant": "fma-graph (not bit-exact)" if flags & lu.FMA else "fp64-graph (bit-exact)",
                        "batched": True, "cuda_graph": True, "exch_planes": "reference (k = 1..nz-2)",
                        "ce": "the reference's table", "l2": f"state {3 * 40 * pts / 1e9:.2f} GB > 129 MB L2; no flush",
                        "parallelism": f"replicas x{world}"},
@@ -641,7 +642,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bt-c", choices=sorted(WORKLOADS))
-    ap.add_argument("--variant", default="mixed-graph", choices=["mixed-graph", "fp64-graph", "mixed-dfrhs-graph", "mixed", "fp64"])
+    ap.add_argument("--variant", default="mixed-graph",
+                    choices=["mixed-graph", "fp64-graph", "mixed-dfrhs-graph", "mixed", "fp64", "fma-graph"],
+                    help="BT/SP step variant; lu-* workloads: fma-graph times NPBMZ_LU_FMA, anything else the "
+                         "bit-exact build")
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the default launch configuration (the timed handle is autotuned otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
