@@ -72,6 +72,7 @@ struct npbmz_lu_handle {
   double* prim = nullptr;  // PR_COUNT planes (PR_RHO first: 1/u1 for the sweeps)
   double* fac = nullptr;  // FAC_COUNT planes per point: d's factors and the off-diagonal blocks
   int* hps_d = nullptr;   // per zone, hstride ints: interior points with i+j+k < l
+  std::vector<char> jac_ok;  // per zone: fac holds the blocks of the current u
   int hstride = 0;
   int max_interior = 0;
   // work lists: all zones, and per zone a contiguous range
@@ -148,6 +149,7 @@ void work_range(npbmz_lu_t* h, int zone, const LuWork** w, int* n) {
 }
 
 int launch_exch(npbmz_lu_t* h) {
+  jac_stale(h, 0, h->nzones);
   int maxper = 0;
   for (const LuZone& Z : h->zh) maxper = std::max(maxper, 2 * Z.nx + 2 * Z.ny);
   const dim3 g((maxper * h->nkp + TPB - 1) / TPB, h->nzones);
@@ -160,7 +162,13 @@ int launch_exch(npbmz_lu_t* h) {
   return 0;
 }
 
+// u of zones z0..z0+nzs-1 changed: their blocks must be made again
+void jac_stale(npbmz_lu_t* h, int z0, int nzs) {
+  for (int z = z0; z < z0 + nzs; ++z) h->jac_ok[z] = 0;
+}
+
 int launch_jac(npbmz_lu_t* h, int z0, int nzs) {
+  for (int z = z0; z < z0 + nzs; ++z) h->jac_ok[z] = 1;
   const dim3 gj((h->max_interior + TPB - 1) / TPB, nzs);
   (h->fast ? lu_fast::jac : lu_exact::jac)(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride,
                                           h->fac, gj, h->stream);
@@ -193,6 +201,7 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
       lu_exact::pointwise(false, dev(h), w, n, 0.0, h->stream);
       break;
     case NPBMZ_LU_PHASE_UPDATE:
+      jac_stale(h, z0, nzs);
       (h->fast ? lu_fast::pointwise : lu_exact::pointwise)(true, dev(h), w, n,
                                                             1.0e+00 / (h->omega * (2.0e+00 - h->omega)), h->stream);
       break;
@@ -205,9 +214,12 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
       if (!rc) rc = launch_lower(h, phase != NPBMZ_LU_PHASE_LOWER, z0, nzs);
       return rc;
     }
-    case NPBMZ_LU_PHASE_UPPER:
+    case NPBMZ_LU_PHASE_UPPER: {
       // the blocks and factors k_lu_jac made before the lower sweep (u does
-      // not change between the sweeps)
+      // not change between the sweeps), made again where u has changed since
+      bool stale = false;
+      for (int z = z0; z < z0 + nzs; ++z) stale = stale || !h->jac_ok[z];
+      if (stale && launch_jac(h, z0, nzs)) return -1;
       for (int l = h->lmax; l >= h->lmin; --l) {
         int c = 0;
         for (int z = z0; z < z0 + nzs; ++z) c = std::max(c, hp_count(h->zh[z], l));
@@ -216,6 +228,7 @@ int launch_phase(npbmz_lu_t* h, int phase, int zone) {
         (h->fast ? lu_fast::upper : lu_exact::upper)(dev(h), h->fac, h->hps_d, h->hstride, l, z0, g, h->stream);
       }
       break;
+    }
     case NPBMZ_LU_PHASE_SSOR: {
       int rc = launch_phase(h, NPBMZ_LU_PHASE_SSOR + 100, zone);
       if (!rc) rc = launch_phase(h, NPBMZ_LU_PHASE_UPPER, zone);
@@ -276,6 +289,7 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
     if (up) {
       LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
       lu_exact::convert(layout == NPBMZ_LAYOUT_REF, true, dev(h), f, h->img, z, blocks, h->stream);
+      if (field == NPBMZ_LU_U) jac_stale(h, z, 1);
       if (field == NPBMZ_LU_U)
         (h->fast ? lu_fast::prim : lu_exact::prim)(dev(h), h->work_d + h->zblock[z], h->zblock[z + 1] - h->zblock[z],
                                                   h->u, h->stream);
@@ -436,6 +450,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
     }
     h->max_interior = std::max(h->max_interior, acc);
   }
+  h->jac_ok.assign(nzones, 0);
   h->zblock.push_back(0);
   for (int z = 0; z < nzones; ++z) {
     for (int f = 0; f < h->zh[z].np; f += TPB) h->work_h.push_back(LuWork{z, f});
@@ -486,6 +501,7 @@ int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
   std::lock_guard<std::mutex> g(h->mu);
   std::memcpy(h->ce.c, ce ? ce : &ce_reference[0][0], sizeof(h->ce.c));
   const int n = (int)h->work_h.size();
+  jac_stale(h, 0, h->nzones);
   // set-up always without contraction: both builds start from the same state
   lu_exact::init(dev(h), h->work_d, n, h->ce, h->stream);
   lu_exact::poly(dev(h), h->work_d, n, h->ce, h->stream);

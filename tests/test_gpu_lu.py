@@ -200,3 +200,27 @@ def test_fma_build_stays_within_rounding_of_the_oracle(name, niter):
 def test_fma_build_meets_the_golden_norms(cls):
     xcr, xce, xci, verified = lu.go(cls, flags=lu.FACES_NPB | lu.GRAPH | lu.FMA)
     assert verified, (xcr, xce, xci)
+
+
+def test_upper_phase_alone_uses_the_current_state():
+    """jacu reads the current u (src/LU/jacu.jl): buts alone, after u has
+    changed since the last lower sweep (an upload), matches the oracle's."""
+    from oracle import oracle
+
+    g, dt = GEOMS["rect"]
+    p, r = make(g(), dt)
+    p.phase(lu.PHASE_LOWER)
+    r.phase(oracle.LU_LOWER)
+    for z in (0, 7):
+        u = r.get(lu.U, z)
+        u[:, 2:-2, 2:-2, 2:-2] *= 1.0 + 1e-3
+        r.set(lu.U, z, u)
+        p.upload(z, lu.U, u)
+    p.phase(lu.PHASE_UPPER)
+    r.phase(oracle.LU_UPPER)
+    assert_state_equal(p, r, (lu.U, lu.RSD))
+    p.phase(lu.PHASE_UPDATE)
+    r.phase(oracle.LU_UPDATE)
+    p.phase(lu.PHASE_UPPER)
+    r.phase(oracle.LU_UPPER)
+    assert_state_equal(p, r, (lu.U, lu.RSD))
