@@ -148,6 +148,11 @@ void work_range(npbmz_lu_t* h, int zone, const LuWork** w, int* n) {
   }
 }
 
+// u of zones z0..z0+nzs-1 changed: their blocks must be made again
+void jac_stale(npbmz_lu_t* h, int z0, int nzs) {
+  for (int z = z0; z < z0 + nzs; ++z) h->jac_ok[z] = 0;
+}
+
 int launch_exch(npbmz_lu_t* h) {
   jac_stale(h, 0, h->nzones);
   int maxper = 0;
@@ -160,11 +165,6 @@ int launch_exch(npbmz_lu_t* h) {
     lu_exact::unpack(dev(h), faces(h), h->nzones, g, h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
-}
-
-// u of zones z0..z0+nzs-1 changed: their blocks must be made again
-void jac_stale(npbmz_lu_t* h, int z0, int nzs) {
-  for (int z = z0; z < z0 + nzs; ++z) h->jac_ok[z] = 0;
 }
 
 int launch_jac(npbmz_lu_t* h, int z0, int nzs) {
