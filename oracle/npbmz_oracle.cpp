@@ -4,7 +4,7 @@
 // restatement of the reference's single-rank path (one MPI rank per cluster,
 // ncells = 1, so cell_start = cell_end = 1 and each line solve is one stage).
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
-// it, and only as the checker.  The product (libnpbmz_gpu.so) never calls it.
+// it, and only to compare against.  The product (libnpbmz_gpu.so) never calls it.
 //
 // Every arithmetic expression keeps the reference's operand order and
 // parenthesisation, and the file is compiled with -ffp-contract=off, because

@@ -2,7 +2,7 @@
 // and SP-MZ time steps: the reference gradient for the discrete adjoint.
 //
 // TEST INFRASTRUCTURE ONLY (like npbmz_oracle.cpp, which this file compiles a
-// second time): only tests/ load libnpbmz_tangent.so, as the checker of the
+// second time): only tests/ load libnpbmz_tangent.so, to compare against the
 // GPU adjoint (npbmz_adjoint).  The reference would take this gradient with
 // ForwardDiff.jl dual numbers pushed through its Julia step (exch_qbc + adi,
 // src/BT/bt-node.jl:280-395, src/SP/sp-node.jl:258-297); Julia is not

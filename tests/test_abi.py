@@ -56,7 +56,7 @@ def test_zone_setup_matches_oracle(npbmz_mod, oracle_mod, kind, cls):
 
 
 def test_bt_class_b_zone_widths():
-    """The geometric widths of BT class B (= BASELINE config 2's grid)."""
+    """The geometric widths of BT class B (the 304x208x17 grid in 8x8 zones)."""
     nx, ny, nz, nbr = npbmz.zone_setup(npbmz.BT, 304, 208, 17, 8, 8, 4.5)
     assert nx[:8].tolist() == [16, 20, 24, 30, 38, 47, 57, 72]
     assert ny[::8].tolist() == [11, 13, 17, 21, 26, 31, 40, 49]

@@ -15,7 +15,7 @@ with a = u_50 - u_target, so that it carries no cancellation error from two
 separately rounded sums of 160k terms.  How the directions are scaled decides
 whether h = 1e-6 lies between the rounding floor of the forward run (error
 ~ 1/h) and the curvature of the 50-step map (error ~ h^2); measured on
-config 3 (max relative error over the 16 directions at h = 1e-6):
+this workload (max relative error over the 16 directions at h = 1e-6):
   u_0, entries of unit RMS (absolute h; rho ~ 800 and rho E ~ 6e4 in the
       seeded state): 6.4e-7;  scaled by each variable's RMS: 1.1e-4
       (curvature);
@@ -52,7 +52,7 @@ H = 1e-6
 NDIR = 16
 
 
-def geom_config3():
+def geom_bt64():
     gx, gy, gz, xz, yz = 64, 64, 8, 4, 4
     nx, ny, nz, nbr = npbmz.zone_setup(npbmz.BT, gx, gy, gz, xz, yz, math.sqrt(6.0))
     return npbmz.Geometry(npbmz.BT, nx, ny, nz, nbr, gx, gy, gz, xz, yz), 0.0008, 50
@@ -135,30 +135,30 @@ def fd_check(p, target, nsteps, every, field, seed, h=H):
 
 
 @pytest.fixture(scope="module")
-def config3():
-    geom, dt, nsteps = geom_config3()
+def bt64():
+    geom, dt, nsteps = geom_bt64()
     p, ce, target = build_case(geom, dt)
     return p, target, nsteps
 
 
 @pytest.mark.parametrize("field,h", [(npbmz.FORCING, 1e-5), (npbmz.U, 2e-6)], ids=["forcing", "u0"])
-def test_config3_adjoint_matches_central_differences(config3, field, h):
+def test_bt64_adjoint_matches_central_differences(bt64, field, h):
     """u_0 at h = 2e-6: with the FP64 compute_rhs that folds dt into its
     factors, the forward path's rounding puts the difference quotient's floor
     at h = 1e-6 right at the bar (worst of 16: 1.18e-6, median 1.4e-7);
     measured worst at h = 2e-6, 3e-6, 5e-6: 4.9e-7, 3.9e-7, 2.1e-7 (no
     curvature term visible yet)."""
-    p, target, nsteps = config3
+    p, target, nsteps = bt64
     J, grad, errs = fd_check(p, target, nsteps, 10, field, seed=77, h=h)
     print(f"field {field} h {h:.0e}: worst {max(errs):.2e}, median {np.median(errs):.2e}")
     assert J > 0.0 and np.all(np.isfinite(grad))
     assert max(errs) <= ADJ_REL, f"max rel err {max(errs):.3e} over {NDIR} directions: {errs}"
 
 
-def test_config3_adjoint_matches_dual_numbers(config3):
+def test_bt64_adjoint_matches_dual_numbers(bt64):
     from oracle import oracle
 
-    p, target, nsteps = config3
+    p, target, nsteps = bt64
     g = p.geom
     u0 = p.flatten(p.download_all(npbmz.U))
     f0 = p.flatten(p.download_all(npbmz.FORCING))
@@ -177,10 +177,10 @@ def test_config3_adjoint_matches_dual_numbers(config3):
     assert rel.max() <= DUAL_REL, rel
 
 
-def test_config3_objective_matches_forward_path(config3):
+def test_bt64_objective_matches_forward_path(bt64):
     """J from the adjoint call equals J of a plain forward run, and the call
     leaves u as it was."""
-    p, target, nsteps = config3
+    p, target, nsteps = bt64
     u0 = p.flatten(p.download_all(npbmz.U))
     J, _, _ = p.adjoint(nsteps, target, checkpoint_every=10, grad_forcing=False, grad_u0=False)
     assert np.array_equal(p.flatten(p.download_all(npbmz.U)), u0)
@@ -191,10 +191,10 @@ def test_config3_objective_matches_forward_path(config3):
     p.upload_all(npbmz.U, u0)
 
 
-def test_checkpoint_interval_does_not_change_the_gradient(config3):
+def test_checkpoint_interval_does_not_change_the_gradient(bt64):
     """Recomputation is deterministic: every checkpoint interval gives the
     same bits."""
-    p, target, nsteps = config3
+    p, target, nsteps = bt64
     ref = p.adjoint(nsteps, target, checkpoint_every=10)
     for every in (1, 7, 50, 64):
         got = p.adjoint(nsteps, target, checkpoint_every=every)
@@ -216,8 +216,8 @@ def test_single_zone_adjoint_without_exchange():
         assert max(errs) <= ADJ_REL, errs
 
 
-def test_adjoint_rejects_bad_arguments(config3):
-    p, target, _ = config3
+def test_adjoint_rejects_bad_arguments(bt64):
+    p, target, _ = bt64
     with pytest.raises(npbmz.NpbmzError, match="checkpoint_every"):
         p.adjoint(5, target, checkpoint_every=0)
     with pytest.raises(npbmz.NpbmzError, match="nsteps"):
@@ -302,13 +302,13 @@ def test_sp_objective_matches_forward_path(sp_case):
     p.upload_all(npbmz.U, u0)
 
 
-def test_torch_autograd_function(config3):
+def test_torch_autograd_function(bt64):
     """TerminalObjective (the torch.autograd counterpart of the Julia rrule)
     returns the adjoint's J and gradients."""
     torch = pytest.importorskip("torch")
     from npbmz.autograd import terminal_objective
 
-    p, target, nsteps = config3
+    p, target, nsteps = bt64
     u0 = p.flatten(p.download_all(npbmz.U))
     f0 = p.flatten(p.download_all(npbmz.FORCING))
     J0, gf, gu = p.adjoint(nsteps, target, checkpoint_every=10)

@@ -26,7 +26,7 @@ def geom_class(kind, cls):
     return npbmz.Geometry(k, nx, ny, nz, nbr, gx, gy, gz, xz, yz), dt, niter
 
 
-def geom_config0():
+def geom_bt24_widths():
     """BT 24x24x6 split 2x2 with x widths 8/16 and y widths 10/14."""
     nx, ny, nz, nbr = npbmz.zones_from_widths([8, 16], [10, 14], 6)
     return npbmz.Geometry(npbmz.BT, nx, ny, nz, nbr, 24, 24, 6, 2, 2), 0.010, 60
@@ -63,7 +63,7 @@ def compare(p, o, field, rel, zones=None):
 
 GEOMS = {
     "bt_classS": lambda: geom_class("BT", "S"),
-    "bt_config0": geom_config0,
+    "bt_24x24x6_widths": geom_bt24_widths,
     "sp_classS": lambda: geom_class("SP", "S"),
 }
 
@@ -160,7 +160,7 @@ def test_double_float_rhs_steps_match_fp64_rhs(kind):
     np.testing.assert_allclose(np.concatenate(a.verify()), np.concatenate(b.verify()), rtol=1e-12, atol=0)
 
 
-@pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 20), ("sp_classS", 40)])
+@pytest.mark.parametrize("gname,nsteps", [("bt_24x24x6_widths", 60), ("bt_classS", 20), ("sp_classS", 40)])
 def test_steps_exact_path_bit_exact(oracle_mod, gname, nsteps):
     geom, dt, _ = GEOMS[gname]()
     p, o = make_pair(oracle_mod, geom, dt, npbmz.EXACT, seeded(geom))
@@ -171,7 +171,7 @@ def test_steps_exact_path_bit_exact(oracle_mod, gname, nsteps):
     np.testing.assert_allclose(ng, no, rtol=NORM_REL, atol=0)
 
 
-@pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("sp_classS", 100)])
+@pytest.mark.parametrize("gname,nsteps", [("bt_24x24x6_widths", 60), ("sp_classS", 100)])
 def test_steps_fast_path_within_1e12(oracle_mod, gname, nsteps):
     geom, dt, _ = GEOMS[gname]()
     p, o = make_pair(oracle_mod, geom, dt, 0, seeded(geom))
@@ -196,7 +196,7 @@ def test_gpu_reproduces_npb_golden_norms(kind, cls, flags):
 
 
 def test_perzone_launches_equal_batched(oracle_mod):
-    geom, dt, _ = geom_config0()
+    geom, dt, _ = geom_bt24_widths()
     ce = seeded(geom)
     a = npbmz.Problem(geom, dt, npbmz.EXACT)
     b = npbmz.Problem(geom, dt, npbmz.EXACT | npbmz.PERZONE)
@@ -342,7 +342,7 @@ def test_errors_are_reported_not_raised_across_the_abi():
 MIXED_REL = 1e-10   # FP32 line solves refined against an FP64 residual
 
 
-@pytest.mark.parametrize("gname,nsteps", [("bt_config0", 60), ("bt_classS", 60), ("sp_classS", 100)])
+@pytest.mark.parametrize("gname,nsteps", [("bt_24x24x6_widths", 60), ("bt_classS", 60), ("sp_classS", 100)])
 @pytest.mark.parametrize("flags", [npbmz.MIXED, npbmz.MIXED | npbmz.RHS_DF, npbmz.MIXED | npbmz.REFINE_FP64],
                          ids=["df64-residual", "df64-rhs", "fp64-residual"])
 def test_mixed_precision_within_1e10_of_fp64_oracle(oracle_mod, gname, nsteps, flags):
@@ -394,9 +394,9 @@ def test_reference_layout_round_trip_pinned():
         assert all(np.all(np.isfinite(b)) for b in before)
 
 
-# ---- BASELINE configurations at full size (the oracle runs them on the host cores) ----
+# ---- the benchmark configurations at full size (the oracle runs them on the host cores) ----
 
-def test_config1_sp_class_a_per_step_norms(oracle_mod):
+def test_sp_class_a_per_step_norms(oracle_mod):
     """SP-MZ 128x128x16 split 4x4 (32x32x16 zones), dt 1.5e-3, 400 steps: per-step
     residual and error norms of the FP64 GPU path within 1e-12 of the oracle."""
     geom, dt, niter = geom_class("SP", "A")
@@ -409,7 +409,7 @@ def test_config1_sp_class_a_per_step_norms(oracle_mod):
 
 @pytest.mark.parametrize("flags,rel", [(0, FAST_REL), (npbmz.MIXED, MIXED_REL), (npbmz.MIXED | npbmz.GRAPH, MIXED_REL)],
                          ids=["fp64", "mixed", "mixed-graph"])
-def test_config2_bt_class_b_final_norms(oracle_mod, flags, rel):
+def test_bt_class_b_final_norms(oracle_mod, flags, rel):
     """BT-MZ 304x208x17 split 8x8 (area ratio 20.05), dt 3e-4, 200 steps, batched:
     final norms of each variant against the FP64 oracle."""
     geom, dt, niter = geom_class("BT", "B")
@@ -423,7 +423,7 @@ def test_config2_bt_class_b_final_norms(oracle_mod, flags, rel):
 
 
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED | npbmz.GRAPH], ids=["fp64", "mixed-graph"])
-def test_config2_autotuned_launch_shapes_keep_results(oracle_mod, flags):
+def test_bt_class_b_autotuned_launch_shapes_keep_results(oracle_mod, flags):
     """The autotuner (lines per CTA per sweep direction and zone-size bucket;
     zone-group branches for graph handles) changes launch shapes only: the
     state it leaves is the one it found, and later steps are bit-identical
