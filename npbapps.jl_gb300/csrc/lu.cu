@@ -73,6 +73,8 @@ struct npbmz_lu_handle {
   double* fac = nullptr;  // FAC_COUNT planes per point: d's factors and the off-diagonal blocks
   int* hps_d = nullptr;   // per zone, hstride ints: interior points with i+j+k < l
   std::vector<char> jac_ok;  // per zone: fac holds the blocks of the current u
+  int* ri_d = nullptr;       // per zone, l and k: slot of the first interior point of row k of hyperplane l
+  int ri_ks = 0;
   int hstride = 0;
   int max_interior = 0;
   // work lists: all zones, and per zone a contiguous range
@@ -169,9 +171,9 @@ int launch_exch(npbmz_lu_t* h) {
 
 int launch_jac(npbmz_lu_t* h, int z0, int nzs) {
   for (int z = z0; z < z0 + nzs; ++z) h->jac_ok[z] = 1;
-  const dim3 gj((h->max_interior + TPB - 1) / TPB, nzs);
-  (h->fast ? lu_fast::jac : lu_exact::jac)(dev_zone0(h, z0), h->hps_d + (long long)z0 * h->hstride, h->hstride,
-                                          h->fac, gj, h->stream);
+  const int b0 = h->zblock[z0], b1 = h->zblock[z0 + nzs];
+  (h->fast ? lu_fast::jac : lu_exact::jac)(dev(h), h->work_d + b0, b1 - b0, h->ri_d, h->hstride, h->ri_ks, h->fac,
+                                          h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
@@ -311,7 +313,7 @@ void free_all(npbmz_lu_t* h) {
   for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->prim,
                   (void*)h->fac, (void*)h->work_d,
                   (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
-                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d})
+                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d, (void*)h->ri_d})
     if (p) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
 }
@@ -450,6 +452,23 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
     }
     h->max_interior = std::max(h->max_interior, acc);
   }
+  int maxnz = 0;
+  for (const LuZone& Z : h->zh) maxnz = std::max(maxnz, Z.nz);
+  h->ri_ks = maxnz + 2;
+  std::vector<int> ri((size_t)nzones * h->hstride * h->ri_ks, 0);
+  for (int z = 0; z < nzones; ++z) {
+    const LuZone& Z = h->zh[z];
+    for (int l = 0; l < h->hstride; ++l) {
+      int R = 0;
+      for (int k = 0; k < h->ri_ks; ++k) {
+        ri[((size_t)z * h->hstride + l) * h->ri_ks + k] = hps[(size_t)z * h->hstride + l] + R;
+        if (k >= 2 && k <= Z.nz - 1 && l >= 6 && l <= Z.nx + Z.ny + Z.nz - 3) {
+          const int s = l - k;
+          R += std::max(0, std::min(Z.ny - 1, s - 2) - std::max(2, s - (Z.nx - 1)) + 1);
+        }
+      }
+    }
+  }
   h->jac_ok.assign(nzones, 0);
   h->zblock.push_back(0);
   for (int z = 0; z < nzones; ++z) {
@@ -480,7 +499,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMalloc(&h->partial, h->work_h.size() * 5 * sizeof(double)) ||
       cudaMalloc(&h->zone_out_d, (6 * (size_t)nzones + 16) * sizeof(double)) ||
       cudaMalloc(&h->stage, so * sizeof(double)) || cudaMalloc(&h->zoff_d, nzones * sizeof(long long)) ||
-      cudaMalloc(&h->hps_d, hps.size() * sizeof(int)))
+      cudaMalloc(&h->hps_d, hps.size() * sizeof(int)) || cudaMalloc(&h->ri_d, ri.size() * sizeof(int)))
     return bail("device allocation failed");
   if (cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(LuZone), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->nbr_d, h->nbr.data(), 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) ||
@@ -488,6 +507,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMemcpy(h->zblock_d, h->zblock.data(), h->zblock.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->zoff_d, zoff.data(), nzones * sizeof(long long), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->hps_d, hps.data(), hps.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->ri_d, ri.data(), ri.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F) ||
       cudaMemset(h->prim, 0, (size_t)PR_COUNT * h->NP * sizeof(double)) ||
       cudaMemset(h->fac, 0, (size_t)FAC_COUNT * h->NP * sizeof(double)))

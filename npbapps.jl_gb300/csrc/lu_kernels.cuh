@@ -601,57 +601,73 @@ __device__ __forceinline__ void store_blk(double* jac, long long NP, long long h
       if (!off_zero(DIR, r, c)) jac[(FAC_BLK + (2 * DIR + S) * BLK_NZ + blk_idx(DIR, r, c)) * NP + h] = b[r][c];
 }
 
-// the off-diagonal block (DIR, SG) from the state at q
-template <int DIR, int SG>
-__device__ __forceinline__ void blk_from(const LuDev& D, const JC& J, long long q, double b[5][5]) {
-  double w[5];
-  load5(D.u, D.NP, q, w);
-  jac_off<DIR, SG>(J, D.prim[PR_RHO * D.NP + q], w[1], w[2], w[3], w[4], b);
+// jacld's (SG = -1) and jacu's (SG = +1) blocks of direction DIR built from
+// this point's state (r1 = 1/u1, u), stored at the interior consumers: the
+// point at +1 in DIR reads the jacld block, the point at -1 the jacu block.
+// Both signs from one state share most of their subexpressions.
+template <int DIR>
+__device__ __forceinline__ void jac_dir(const JC& J, double r1, const double u[5], double* __restrict__ jac,
+                                        long long NP, bool lo, long long slot_lo, bool up, long long slot_up) {
+  double b[5][5], c[5][5];
+  if (lo && up) {
+    jac_off<DIR, -1>(J, r1, u[1], u[2], u[3], u[4], b);
+    jac_off<DIR, 1>(J, r1, u[1], u[2], u[3], u[4], c);
+    store_blk<DIR, 0>(jac, NP, slot_lo, b);
+    store_blk<DIR, 1>(jac, NP, slot_up, c);
+  } else if (lo) {
+    jac_off<DIR, -1>(J, r1, u[1], u[2], u[3], u[4], b);
+    store_blk<DIR, 0>(jac, NP, slot_lo, b);
+  } else if (up) {
+    jac_off<DIR, 1>(J, r1, u[1], u[2], u[3], u[4], c);
+    store_blk<DIR, 1>(jac, NP, slot_up, c);
+  }
 }
 
-// jacld's and jacu's blocks and d's factors of every interior point (the
-// Jacobian work of ssor, taken off the wavefront), one thread per point in
-// hyperplane order (blockIdx.y: zone)
-__global__ void __launch_bounds__(TPB) k_lu_jac(LuDev D, const int* __restrict__ hps, int hstride,
-                                                double* __restrict__ jac) {
-  const int z = blockIdx.y;
-  const LuZone Z = D.zones[z];
-  const int* H = hps + (long long)z * hstride;
-  const int t = blockIdx.x * TPB + threadIdx.x;
-  const int lend = Z.nx + Z.ny + Z.nz - 3;
-  if (t >= H[lend + 1]) return;
-  int lo = 6, hi = lend;  // the hyperplane of t: largest l with H[l] <= t
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) / 2;
-    if (H[mid] <= t) lo = mid; else hi = mid - 1;
-  }
+// jacld's and jacu's blocks and d's factors (the Jacobian work of ssor,
+// taken off the wavefront): one thread per point of the zones, in natural
+// order, writing each block into its consumer's slot.  ri: per zone, l and
+// k, the slot of the first interior point of row k of hyperplane l.
+__global__ void __launch_bounds__(TPB) k_lu_jac(LuDev D, const LuWork* __restrict__ work, const int* __restrict__ ri,
+                                                int ls, int ks, double* __restrict__ jac) {
+  const LuWork w = work[blockIdx.x];
+  const LuZone Z = D.zones[w.zone];
   int i, j, k;
-  if (!hyperplane_point(Z, lo, t - H[lo], i, j, k)) return;
-  const long long NP = D.NP, p = pidx(Z, i, j, k), h = Z.off + t;
+  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
+  const long long NP = D.NP, p = pidx(Z, i, j, k);
   const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
-  double b[5][5];
-  blk_from<0, -1>(D, J, pidx(Z, i - 1, j, k), b);
-  store_blk<0, 0>(jac, NP, h, b);
-  blk_from<0, 1>(D, J, pidx(Z, i + 1, j, k), b);
-  store_blk<0, 1>(jac, NP, h, b);
-  blk_from<1, -1>(D, J, pidx(Z, i, j - 1, k), b);
-  store_blk<1, 0>(jac, NP, h, b);
-  blk_from<1, 1>(D, J, pidx(Z, i, j + 1, k), b);
-  store_blk<1, 1>(jac, NP, h, b);
-  blk_from<2, -1>(D, J, pidx(Z, i, j, k - 1), b);
-  store_blk<2, 0>(jac, NP, h, b);
-  blk_from<2, 1>(D, J, pidx(Z, i, j, k + 1), b);
-  store_blk<2, 1>(jac, NP, h, b);
-  double w[5];
-  load5(D.u, NP, p, w);
-  jac_d(J, D.prim[PR_RHO * NP + p], w[1], w[2], w[3], w[4], b);
-  const double rinv0 = 1.0e+00 / b[0][0];
+  const int* R = ri + (long long)w.zone * ls * ks;
+  auto slot = [&](int a, int b, int c) -> long long {
+    const int l = a + b + c;
+    return Z.off + R[(long long)l * ks + c] + (b - max(2, l - c - (Z.nx - 1)));
+  };
+  const double r1 = D.prim[PR_RHO * NP + p];
+  double u[5];
+  load5(D.u, NP, p, u);
+  const bool ii = i >= 2 && i <= Z.nx - 1, jj = j >= 2 && j <= Z.ny - 1, kk = k >= 2 && k <= Z.nz - 1;
+  if (jj && kk) {
+    const bool lo = i <= Z.nx - 2, up = i >= 3;
+    jac_dir<0>(J, r1, u, jac, NP, lo, lo ? slot(i + 1, j, k) : 0, up, up ? slot(i - 1, j, k) : 0);
+  }
+  if (ii && kk) {
+    const bool lo = j <= Z.ny - 2, up = j >= 3;
+    jac_dir<1>(J, r1, u, jac, NP, lo, lo ? slot(i, j + 1, k) : 0, up, up ? slot(i, j - 1, k) : 0);
+  }
+  if (ii && jj) {
+    const bool lo = k <= Z.nz - 2, up = k >= 3;
+    jac_dir<2>(J, r1, u, jac, NP, lo, lo ? slot(i, j, k + 1) : 0, up, up ? slot(i, j, k - 1) : 0);
+  }
+  if (ii && jj && kk) {
+    const long long h = slot(i, j, k);
+    double b[5][5];
+    jac_d(J, r1, u[1], u[2], u[3], u[4], b);
+    const double rinv0 = 1.0e+00 / b[0][0];
 #pragma unroll
-  for (int r = 0; r < 5; ++r) jac[(FAC_T + r) * NP + h] = b[r][r];
+    for (int r = 0; r < 5; ++r) jac[(FAC_T + r) * NP + h] = b[r][r];
 #pragma unroll
-  for (int r = 1; r < 5; ++r) jac[(FAC_R0 + r - 1) * NP + h] = rinv0 * b[r][0];
+    for (int r = 1; r < 5; ++r) jac[(FAC_R0 + r - 1) * NP + h] = rinv0 * b[r][0];
 #pragma unroll
-  for (int c = 1; c <= 3; ++c) jac[(FAC_4C + c - 1) * NP + h] = (1.0e+00 / b[c][c]) * b[4][c];
+    for (int c = 1; c <= 3; ++c) jac[(FAC_4C + c - 1) * NP + h] = (1.0e+00 / b[c][c]) * b[4][c];
+  }
 }
 
 // row M of the point's block (DIR, S) dotted with w, summed left to right as
@@ -1033,8 +1049,8 @@ void pointwise(bool update, const LuDev& D, const LuWork* w, int n, double tmp, 
   else
     k_lu_pointwise<false><<<n, TPB, 0, s>>>(D, w, tmp);
 }
-void jac(const LuDev& D, const int* hps, int hstride, double* jac, dim3 grid, cudaStream_t s) {
-  k_lu_jac<<<grid, TPB, 0, s>>>(D, hps, hstride, jac);
+void jac(const LuDev& D, const LuWork* w, int n, const int* ri, int ls, int ks, double* jac, cudaStream_t s) {
+  k_lu_jac<<<n, TPB, 0, s>>>(D, w, ri, ls, ks, jac);
 }
 void lower(bool scale, const LuDev& D, const double* jac, const int* hps, int hstride, int l, int z0, dim3 grid,
            cudaStream_t s) {

@@ -101,7 +101,7 @@ constexpr int BLK_NZ = 18;
 // k then j ascending; hps[l]: the zone's interior points with i+j+k < l), so
 // that the sweeps, which run one hyperplane per launch, read them coalesced.
 // Written by k_lu_jac before the sweeps (u does not change until the
-// update):
+// update), each block by the point whose state it is built from:
 //   FAC_T + r, FAC_R0 + r-1, FAC_4C + c-1   t_rr, tmp_r0, tmp_4c of d
 //   FAC_BLK + (2 dir + s) * 18 + blk_idx    the non-zero entries of the
 //       off-diagonal block of direction dir: s = 0 jacld's (from the point
