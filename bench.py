@@ -365,10 +365,13 @@ def run_gpu_lu(args, cls, desc):
         ms = timed(p, args.steps, args.warmup)
     ms_max, value = whole_job(ms, pts, args.steps, world, dist)
     extra = {}
+    nprof = max(2, min(args.steps, 5))
     if rank == 0 and args.quick:
-        extra["phase_ms"] = p.profile(max(2, min(args.steps, 5)))
+        extra["phase_ms"] = {k: v / nprof for k, v in p.profile(nprof).items()}
     elif rank == 0:
-        ph = p.profile(max(2, min(args.steps, 5)))
+        # per-iteration device time of each phase (events around the phases
+        # of nprof iterations, direct launches)
+        ph = {k: v / nprof for k, v in p.profile(nprof).items()}
         extra["phase_ms"] = ph
         top = max((k for k in ph if k != "exch"), key=lambda k: ph[k])
         pk = peaks()
@@ -399,7 +402,7 @@ def run_gpu_lu(args, cls, desc):
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
                              "bytes_per_point": LU_BYTES_PER_POINT[top],
                              "points": f"{units} ({'interior' if units == interior else 'all'} points per launch)",
-                             "launch_ms": ph[top] / max(2, min(args.steps, 5)),
+                             "launch_ms": ph[top],
                              "binding_ceiling": "fp64 pipe" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6 else None,
                              "fp64": fp64_obj}
         extra["fp64_peak_gflops_measured"] = fp64
