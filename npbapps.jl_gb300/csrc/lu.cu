@@ -580,10 +580,14 @@ int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
   if ((h->flags & NPBMZ_LU_GRAPH) && !h->graph) {
     cudaGraph_t gr;
     LU_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    gr = nullptr;
     const int rc = launch_iteration(h);
     const cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
-    if (rc) return rc;
-    LU_CK(h, e);
+    if (rc || e != cudaSuccess) {
+      if (gr) cudaGraphDestroy(gr);
+      if (rc) return rc;
+      LU_CK(h, e);
+    }
     const cudaError_t ie = cudaGraphInstantiate(&h->graph, gr, 0);
     cudaGraphDestroy(gr);
     LU_CK(h, ie);
@@ -596,7 +600,7 @@ int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
     }
     if (rsdnm && launch_rsd_norm(h, h->norms_d + 5 * (size_t)it)) return -1;
   }
-  if (rsdnm) {
+  if (rsdnm && niter > 0) {
     LU_CK(h, cudaMemcpyAsync(rsdnm, h->norms_d, (size_t)5 * niter * sizeof(double), cudaMemcpyDeviceToHost,
                              h->stream));
     LU_CK(h, cudaStreamSynchronize(h->stream));
