@@ -728,23 +728,39 @@ __device__ __forceinline__ double lower_row(const LuDev& D, const double* __rest
   return v;
 }
 
+// d's factors row m needs, loaded before the rows are exchanged (so that
+// their latency overlaps the row sums): f[0] = t_mm; rows 1..3 f[1] = tmp_m0;
+// row 4 f[1..4] = tmp_40, tmp_10, tmp_20, tmp_30, f[5..7] = tmp_41..tmp_43
+__device__ __forceinline__ void load_factors(const double* __restrict__ jac, long long NP, long long h, int m,
+                                             double f[8]) {
+  f[0] = jac[(FAC_T + m) * NP + h];
+  if (m >= 1 && m <= 3) f[1] = jac[(FAC_R0 + m - 1) * NP + h];
+  if (m == 4) {
+    f[1] = jac[(FAC_R0 + 3) * NP + h];
+#pragma unroll
+    for (int c = 1; c <= 3; ++c) {
+      f[1 + c] = jac[(FAC_R0 + c - 1) * NP + h];
+      f[4 + c] = jac[(FAC_4C + c - 1) * NP + h];
+    }
+  }
+}
+
 // the forward substitution with d's factors (rows exchanged through shared
 // memory); v: this thread's row, sv: every row of the point
-__device__ __forceinline__ double d_solve(const double* __restrict__ jac, long long NP, long long h, int m, double v,
-                                          const double sv[5]) {
+__device__ __forceinline__ double d_solve(const double f[8], int m, double v, const double sv[5]) {
   const double v0 = sv[0];
-  if (m == 0) return v / jac[FAC_T * NP + h];
+  if (m == 0) return v / f[0];
   if (m < 4) {
-    v = v - v0 * jac[(FAC_R0 + m - 1) * NP + h];
-    return v / jac[(FAC_T + m) * NP + h];
+    v = v - v0 * f[1];
+    return v / f[0];
   }
-  v = v - v0 * jac[(FAC_R0 + 3) * NP + h];
+  v = v - v0 * f[1];
 #pragma unroll
   for (int c = 1; c <= 3; ++c) {
-    const double vc = sv[c] - v0 * jac[(FAC_R0 + c - 1) * NP + h];  // v_c after column 0, as row c has it
-    v = v - vc * jac[(FAC_4C + c - 1) * NP + h];
+    const double vc = sv[c] - v0 * f[1 + c];  // v_c after column 0, as row c has it
+    v = v - vc * f[4 + c];
   }
-  return v / jac[(FAC_T + 4) * NP + h];
+  return v / f[0];
 }
 
 // jacld + blts at every point of hyperplane l (blockIdx.y: zone - zone0),
@@ -761,8 +777,9 @@ __global__ void __launch_bounds__(HP * 5) k_lu_lower(LuDev D, const double* __re
   int i = 0, j = 0, k = 0;
   const bool ok = hyperplane_point(Z, l, t, i, j, k);
   const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
-  double v = 0.0;
+  double v = 0.0, f[8];
   if (ok) {
+    load_factors(jac, D.NP, h, m, f);
     switch (m) {
       case 0: v = lower_row<0, SCALE>(D, jac, Z, i, j, k, h); break;
       case 1: v = lower_row<1, SCALE>(D, jac, Z, i, j, k, h); break;
@@ -774,7 +791,7 @@ __global__ void __launch_bounds__(HP * 5) k_lu_lower(LuDev D, const double* __re
   }
   __syncthreads();
   if (!ok) return;
-  D.rsd[m * D.NP + pidx(Z, i, j, k)] = d_solve(jac, D.NP, h, m, v, sv[a]);
+  D.rsd[m * D.NP + pidx(Z, i, j, k)] = d_solve(f, m, v, sv[a]);
 }
 
 // buts's two tv loops for row M of one point
@@ -802,8 +819,9 @@ __global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __re
   int i = 0, j = 0, k = 0;
   const bool ok = hyperplane_point(Z, l, t, i, j, k);
   const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
-  double tv = 0.0;
+  double tv = 0.0, f[8];
   if (ok) {
+    load_factors(jac, D.NP, h, m, f);
     switch (m) {
       case 0: tv = upper_row<0>(D, jac, Z, i, j, k, h); break;
       case 1: tv = upper_row<1>(D, jac, Z, i, j, k, h); break;
@@ -815,7 +833,7 @@ __global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __re
   }
   __syncthreads();
   if (!ok) return;
-  tv = d_solve(jac, D.NP, h, m, tv, sv[a]);
+  tv = d_solve(f, m, tv, sv[a]);
   const long long p = pidx(Z, i, j, k);
   D.rsd[m * D.NP + p] = D.rsd[m * D.NP + p] - tv;
 }
