@@ -819,9 +819,10 @@ __global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __re
   int i = 0, j = 0, k = 0;
   const bool ok = hyperplane_point(Z, l, t, i, j, k);
   const long long h = ok ? Z.off + hps[(long long)z * hstride + l] + t : 0;
-  double tv = 0.0, f[8];
+  double tv = 0.0, f[8], own = 0.0;
   if (ok) {
     load_factors(jac, D.NP, h, m, f);
+    own = D.rsd[m * D.NP + pidx(Z, i, j, k)];
     switch (m) {
       case 0: tv = upper_row<0>(D, jac, Z, i, j, k, h); break;
       case 1: tv = upper_row<1>(D, jac, Z, i, j, k, h); break;
@@ -834,8 +835,7 @@ __global__ void __launch_bounds__(HP * 5) k_lu_upper(LuDev D, const double* __re
   __syncthreads();
   if (!ok) return;
   tv = d_solve(f, m, tv, sv[a]);
-  const long long p = pidx(Z, i, j, k);
-  D.rsd[m * D.NP + p] = D.rsd[m * D.NP + p] - tv;
+  D.rsd[m * D.NP + pidx(Z, i, j, k)] = own - tv;
 }
 
 __device__ inline void face_sizes(const LuZone& Z, int nkp, long long& e, long long& s) {
