@@ -208,6 +208,7 @@ const LU_FRCT = Cint(2)
 mutable struct LuProblem
     handle::Ptr{Cvoid}
     nzones::Int
+    lock::ReentrantLock          # serialises calls on the handle (ssor from Threads.@threads)
     function LuProblem(nx::Vector{<:Integer}, ny, nz, nbr, dt; omega = 1.2, flags = Cint(0))
         n = length(nx)
         params = Cdouble[dt, omega]
@@ -216,7 +217,7 @@ mutable struct LuProblem
                    (Cint, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cdouble}, Cint, Ptr{Ptr{Cvoid}}),
                    n, Cint.(nx), Cint.(ny), Cint.(nz), Cint.(nbr), params, flags, out)
         rc == 0 || error("npbmz_lu_create failed (zone sizes below 5, unequal nz, mismatched faces or bad flags)")
-        p = new(out[], n)
+        p = new(out[], n, ReentrantLock())
         finalizer(p) do q
             q.handle != C_NULL && ccall((:npbmz_lu_destroy, libnpbmz), Cint, (Ptr{Cvoid},), q.handle)
             q.handle = C_NULL
@@ -276,5 +277,18 @@ upload!(p::LuProblem, zone::Integer, field, a) =
 download!(p::LuProblem, zone::Integer, field, a) =
     check(p, ccall((:npbmz_lu_download, libnpbmz), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}),
                    p.handle, zone - 1, field, LAYOUT_REF, parent(a)), "npbmz_lu_download")
+
+"""One zone's u, rsd or frct of an LuProblem: vectors of these stand in for
+the reference's u, rsd, frct in its LU loop (NPBAppsGPUShim.jl)."""
+struct LuDeviceZone
+    p::LuProblem
+    zone::Int        # 1-based
+    field::Cint
+end
+
+device_zones(p::LuProblem, field) = [LuDeviceZone(p, iz, Cint(field)) for iz in 1:p.nzones]
+
+"""ssor of one zone under the handle's lock (the reference calls ssor from Threads.@threads)."""
+ssor_locked!(p::LuProblem, iz::Integer) = lock(() -> ssor!(p, iz), p.lock)
 
 end # module

@@ -18,9 +18,10 @@
 # src/SP/exchange_qbc.jl).  adi of one zone runs under the handle's lock, as
 # the reference calls it from Threads.@threads; NPBAppsGPU.adi!(gpu) (all
 # zones batched in one launch per phase) is the fast form of the same loop.
-# Julia is not installed where this was written: unexecuted.
+# The same for LU-MZ's ssor and exch_qbc (below).  Julia is not installed
+# where this was written: unexecuted.
 import NPBApps
-using .NPBAppsGPU: DeviceZone
+using .NPBAppsGPU: DeviceZone, LuDeviceZone
 
 function NPBApps.BT.adi(iz, a2, a3, a4, a5, a6, a7, a8, a9, a10, a11, a12, a13,
                         forcing::DeviceZone, u::DeviceZone, rhs::DeviceZone, rest::Vararg{Any,60})
@@ -42,4 +43,21 @@ for M in (NPBApps.BT, NPBApps.SP)
         lock(() -> NPBAppsGPU.exch_qbc!(p), p.lock)
         return nothing
     end
+end
+
+# LU-MZ: ssor u / rsd / frct at 6 / 7 / 8 of 41 (src/LU/ssor.jl:9-50); exch_qbc
+# u at 4 of 36 (src/LU/exchange_qbc.jl:17).  Pass
+# NPBAppsGPU.device_zones(lu, NPBAppsGPU.LU_U) (LU_RSD, LU_FRCT) where
+# src/LU/lu-node.jl:233-270 passes u, rsd, frct.
+function NPBApps.LU.ssor(iz, ipt, jpt, proc_num_zones, comm_solve, u::LuDeviceZone, rsd::LuDeviceZone,
+                         frct::LuDeviceZone, rest::Vararg{Any,33})
+    NPBAppsGPU.ssor_locked!(u.p, u.zone)
+    return nothing
+end
+
+function NPBApps.LU.exch_qbc(proc_num_zones, zone_proc_id, proc_zone_id, u::AbstractVector{LuDeviceZone},
+                             rest::Vararg{Any,32})
+    p = u[1].p
+    lock(() -> NPBAppsGPU.exch_qbc!(p), p.lock)
+    return nothing
 end

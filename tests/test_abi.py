@@ -124,3 +124,22 @@ def test_julia_bindings_call_only_declared_entry_points():
     for name in ("npbmz_lu_create", "npbmz_lu_setup", "npbmz_lu_exch_qbc", "npbmz_lu_ssor", "npbmz_lu_iterate",
                  "npbmz_lu_verify", "npbmz_lu_upload", "npbmz_lu_download", "npbmz_lu_destroy"):
         assert name in called, name
+
+
+def test_julia_shim_arities_match_the_reference_signatures():
+    """The shim's methods take the reference functions' positional arity:
+    BT adi 76, SP adi 99, exch_qbc 25 (BT/SP), LU ssor 41, LU exch_qbc 36
+    (src/BT/adi.jl:5-80, src/SP/adi.jl:6-104, src/BT/exchange_qbc.jl:1-26,
+    src/LU/ssor.jl:9-50, src/LU/exchange_qbc.jl:17)."""
+    text = (Path(__file__).resolve().parents[1] / "npbapps.jl_gb300" / "julia" / "NPBAppsGPUShim.jl").read_text()
+    want = {"NPBApps.BT.adi": 76, "NPBApps.SP.adi": 99, "$M.exch_qbc": 25, "NPBApps.LU.ssor": 41,
+            "NPBApps.LU.exch_qbc": 36}
+    for name, arity in want.items():
+        m = re.search(re.escape(name) + r"\((.*?)\)\n", text, re.S)
+        assert m, name
+        sig = m.group(1)
+        rest = [int(x) for x in re.findall(r"\w+::Vararg\{Any,\s*(\d+)\}", sig)]
+        sig = re.sub(r"\w+::Vararg\{Any,\s*\d+\}", "", sig)
+        args = [a.strip() for a in sig.split(",") if a.strip()]
+        n = len(args) + sum(rest)
+        assert n == arity, (name, n, arity)
