@@ -5,10 +5,11 @@ The kernels are built without FMA contraction and follow the reference's
 statements point for point, so u, rsd and frct are compared bit for bit:
 after setup (setbv, setiv, erhs, rhs), after every phase of ssor, and after
 whole iterations, in both exch_qbc plane modes.  Norms (sums in another
-order) are held to 1e-13.  Geometries: LU-MZ classes S and W (4x4 zones of
-6x6x6 and 16x16x8), zones of the minimum size 5x5x5 (where the fourth-
-difference boundary stencils overlap), rectangular 9x7x7 zones, and 2x2
-zones.
+order) are held to 1e-13.  Geometries: LU-MZ classes S, W and B (4x4 zones
+of 6x6x6, 16x16x8 and 76x52x17), zones of the minimum size 5x5x5 (where the
+fourth-difference boundary stencils overlap), rectangular 9x7x7 zones, 2x2
+zones, and stretched zones of unequal sizes; the reference's ce table and a
+perturbed one.
 """
 import numpy as np
 import pytest
@@ -223,4 +224,45 @@ def test_upper_phase_alone_uses_the_current_state():
     r.phase(oracle.LU_UPDATE)
     p.phase(lu.PHASE_UPPER)
     r.phase(oracle.LU_UPPER)
+    assert_state_equal(p, r, (lu.U, lu.RSD))
+
+
+@pytest.mark.parametrize("flags", [0, lu.FACES_NPB], ids=["ref-faces", "npb-faces"])
+def test_stretched_unequal_zones_are_bit_exact(flags):
+    """zone_setup's stretched rule (ratio 3: zone widths 6..16 x 5..14): zones
+    of different sizes share every hyperplane launch, each with its own
+    hyperplane count and its own setcoeff constants."""
+    g = lu.lu_zone_setup(40, 36, 6, 4, 4, 3.0)
+    assert len(set(g[0].tolist())) > 1 and len(set(g[1].tolist())) > 1
+    p, r = make(g, 0.5, flags)
+    p.iterate(20)
+    r.iterate(20)
+    assert_state_equal(p, r, (lu.U, lu.RSD))
+
+
+def test_other_coefficient_table_is_bit_exact():
+    """setup from a ce table other than the reference's (each coefficient
+    perturbed by a seeded 10 %): setbv, setiv, erhs and 20 iterations."""
+    from oracle import oracle
+
+    rng = np.random.default_rng(31)
+    ce = np.array(npbmz.CE_REFERENCE) * (1.0 + 0.1 * rng.standard_normal((5, 13)))
+    nx, ny, nz, nbr = lu.lu_zone_setup(40, 40, 8, 4, 4)
+    p = lu.LuProblem(nx, ny, nz, nbr, 0.5, flags=lu.FACES_NPB | lu.GRAPH)
+    p.setup(ce)
+    r = oracle.LuOracle(nx, ny, nz, nbr, 0.5, ce=ce, faces_npb=True)
+    assert_state_equal(p, r)
+    p.iterate(20)
+    r.iterate(20)
+    assert_state_equal(p, r, (lu.U, lu.RSD))
+
+
+def test_class_b_zones_are_bit_exact():
+    """LU-MZ class B geometry (16 zones of 76x52x17, 1.07 M points), 5
+    iterations."""
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES["LU"]["B"]
+    g = lu.lu_zone_setup(gx, gy, gz, xz, yz, ratio)
+    p, r = make(g, dt, lu.GRAPH)
+    p.iterate(5)
+    r.iterate(5)
     assert_state_equal(p, r, (lu.U, lu.RSD))
