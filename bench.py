@@ -433,12 +433,12 @@ def run_gpu_lu(args, cls, desc):
             p.iterate(1)
             assert L.npbmz_lu_download(p._h, -1, lu.U, npbmz.LAYOUT_REF, ptr) == 0
         te = time.perf_counter() - t0
-        moved = 8 * int(sum(sizes))
+        moved = 5 * 8 * pts  # the interior points of the reference arrays, each way
         extra["e2e"] = {"value": pts * world * args.steps / te / 1e6, "unit": "Mgridpt-steps/s",
-                        "h2d_bytes_per_step": moved, "d2h_bytes_per_step": 2 * moved,
+                        "h2d_bytes_per_step": moved, "d2h_bytes_per_step": moved,
                         "path": "npbmz_lu_upload + npbmz_lu_iterate(1) + npbmz_lu_download (zone=-1, "
-                                "NPBMZ_LAYOUT_REF) on page-locked reference-layout u; the download copies the "
-                                "host image in first so that the halo is kept"}
+                                "NPBMZ_LAYOUT_REF) on page-locked reference-layout u, read and written in place "
+                                "(interior points only) by one kernel per zone each way"}
         if not args.no_cpu_baseline:
             extra["cpu_baseline"] = lu_cpu_baseline(cls)
     if rank == 0:

@@ -283,11 +283,36 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
   if (zone < -1 || zone >= h->nzones) return fail(h, "zone %d out of range", zone);
   if (!host) return fail(h, "null host buffer");
   const int z0 = zone < 0 ? 0 : zone, z1 = zone < 0 ? h->nzones : zone + 1;
+  // Page-locked (mapped) host memory: one kernel per zone reads or writes it
+  // in place (the reference layout's halo is not touched), one synchronise
+  // at the end.
+  cudaPointerAttributes attr;
+  std::memset(&attr, 0, sizeof(attr));
+  const bool mapped = cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+                      attr.devicePointer != nullptr;
+  cudaGetLastError();  // pageable memory is not an error to keep
+  if (mapped) {
+    double* dhost = reinterpret_cast<double*>(attr.devicePointer);
+    for (int z = z0; z < z1; ++z) {
+      const LuZone& Z = h->zh[z];
+      const int blocks = (int)((5LL * Z.np + TPB - 1) / TPB);
+      lu_exact::convert(layout == NPBMZ_LAYOUT_REF, up, dev(h), f, dhost, z, blocks, h->stream);
+      if (up && field == NPBMZ_LU_U) {
+        jac_stale(h, z, 1);
+        (h->fast ? lu_fast::prim : lu_exact::prim)(dev(h), h->work_d + h->zblock[z], h->zblock[z + 1] - h->zblock[z],
+                                                  h->u, h->stream);
+      }
+      dhost += zone_elems(Z, layout);
+    }
+    LU_CK(h, cudaGetLastError());
+    LU_CK(h, cudaStreamSynchronize(h->stream));
+    return 0;
+  }
   for (int z = z0; z < z1; ++z) {
     const LuZone& Z = h->zh[z];
     const size_t n = zone_elems(Z, layout);
     if (ensure_img(h, n * sizeof(double))) return -1;
-    const int blocks = (Z.np + TPB - 1) / TPB;
+    const int blocks = (int)((5LL * Z.np + TPB - 1) / TPB);
     if (up) {
       LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
       lu_exact::convert(layout == NPBMZ_LAYOUT_REF, true, dev(h), f, h->img, z, blocks, h->stream);

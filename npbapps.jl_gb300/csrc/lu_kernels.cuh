@@ -1025,23 +1025,39 @@ __global__ void __launch_bounds__(TPB) k_lu_pintgr(LuDev D, double* frc) {
 }
 
 // ---- layout conversion --------------------------------------------------------
-// REF: [1:5, -1:nx+2, -1:ny+2, 1:nz] column-major; DENSE: [m][k][j][i]
+// REF: [1:5, -1:nx+2, -1:ny+2, 1:nz] column-major; DENSE: [m][k][j][i].  One
+// thread per double, in the host array's order (REF: the 5*nx interior
+// doubles of each (j, k) row are contiguous), so that a warp's host accesses
+// are contiguous: the host side may be page-locked memory read or written
+// in place over the host link.
 template <bool REF, bool TO_DEV>
 __global__ void __launch_bounds__(TPB) k_lu_convert(LuDev D, double* field, double* host_img, int zone) {
   const LuZone Z = D.zones[zone];
-  const int q = blockIdx.x * TPB + threadIdx.x;
-  if (q >= Z.np) return;
-  const int i = q % Z.nx + 1, j = (q / Z.nx) % Z.ny + 1, k = q / (Z.nx * Z.ny) + 1;
-  const long long p = pidx(Z, i, j, k);
-#pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    const long long h = REF ? m + 5LL * ((i + 1) + (long long)(Z.nx + 4) * ((j + 1) + (long long)(Z.ny + 4) * (k - 1)))
-                            : (long long)m * Z.np + q;
-    if (TO_DEV)
-      field[m * D.NP + p] = host_img[h];
-    else
-      host_img[h] = field[m * D.NP + p];
+  const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+  if (t >= 5LL * Z.np) return;
+  int m, i, j, k;
+  long long h;
+  if (REF) {
+    const int rowlen = 5 * Z.nx;
+    const int row = (int)(t / rowlen), e = (int)(t % rowlen);
+    m = e % 5;
+    i = e / 5 + 1;
+    j = row % Z.ny + 1;
+    k = row / Z.ny + 1;
+    h = 5LL * (Z.nx + 4) * ((j + 1) + (long long)(Z.ny + 4) * (k - 1)) + 10 + e;
+  } else {
+    m = (int)(t / Z.np);
+    const int q = (int)(t % Z.np);
+    i = q % Z.nx + 1;
+    j = (q / Z.nx) % Z.ny + 1;
+    k = q / (Z.nx * Z.ny) + 1;
+    h = t;
   }
+  const long long p = m * D.NP + pidx(Z, i, j, k);
+  if (TO_DEV)
+    field[p] = host_img[h];
+  else
+    host_img[h] = field[p];
 }
 
 // ---- host launchers ------------------------------------------------------------

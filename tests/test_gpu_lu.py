@@ -266,3 +266,29 @@ def test_class_b_zones_are_bit_exact():
     p.iterate(5)
     r.iterate(5)
     assert_state_equal(p, r, (lu.U, lu.RSD))
+
+
+@pytest.mark.parametrize("layout", [npbmz.LAYOUT_DENSE, npbmz.LAYOUT_REF], ids=["dense", "ref"])
+def test_page_locked_transfers_match_pageable(layout):
+    """Page-locked host buffers are read and written in place by one kernel
+    per zone: the same values as the staged path for pageable memory, and
+    the reference layout's halo is left as it was."""
+    torch = pytest.importorskip("torch")
+    g, dt = GEOMS["rect"]
+    p, r = make(g(), dt)
+    sizes = [lu.ref_elems(int(p.nx[z]), int(p.ny[z]), int(p.nz[z])) if layout == npbmz.LAYOUT_REF
+             else 5 * int(p.nx[z]) * int(p.ny[z]) * int(p.nz[z]) for z in range(p.nzones)]
+    total = int(sum(sizes))
+    pinned = torch.full((total,), 7.25, dtype=torch.float64, pin_memory=True)
+    pageable = np.full(total, 7.25)
+    L = lu.lib()
+    assert L.npbmz_lu_download(p._h, -1, lu.U, layout, pinned.data_ptr()) == 0
+    assert L.npbmz_lu_download(p._h, -1, lu.U, layout, pageable.ctypes.data) == 0
+    np.testing.assert_array_equal(pinned.numpy(), pageable)
+    if layout == npbmz.LAYOUT_REF:
+        assert np.count_nonzero(pageable == 7.25) > 0
+    # upload a scaled copy through the pinned buffer and read it back
+    pinned.mul_(1.5)
+    assert L.npbmz_lu_upload(p._h, -1, lu.U, layout, pinned.data_ptr()) == 0
+    for z in range(p.nzones):
+        np.testing.assert_array_equal(p.download(z, lu.U), r.get(lu.U, z) * 1.5)
