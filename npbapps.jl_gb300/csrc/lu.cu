@@ -75,6 +75,8 @@ struct npbmz_lu_handle {
   std::vector<char> jac_ok;  // per zone: fac holds the blocks of the current u
   int* ri_d = nullptr;       // per zone, l and k: slot of the first interior point of row k of hyperplane l
   int ri_ks = 0;
+  int* fb_d = nullptr;       // per zone, l and k: the first point of row k of hyperplane l in the full box
+  int fb_ls = 0;
   int hstride = 0;
   int max_interior = 0;
   // work lists: all zones, and per zone a contiguous range
@@ -170,10 +172,16 @@ int launch_exch(npbmz_lu_t* h) {
 }
 
 int launch_jac(npbmz_lu_t* h, int z0, int nzs) {
-  for (int z = z0; z < z0 + nzs; ++z) h->jac_ok[z] = 1;
-  const int b0 = h->zblock[z0], b1 = h->zblock[z0 + nzs];
-  (h->fast ? lu_fast::jac : lu_exact::jac)(dev(h), h->work_d + b0, b1 - b0, h->ri_d, h->hstride, h->ri_ks, h->fac,
-                                          h->stream);
+  int maxnp = 0;
+  for (int z = z0; z < z0 + nzs; ++z) {
+    h->jac_ok[z] = 1;
+    maxnp = std::max(maxnp, h->zh[z].np);
+  }
+  const dim3 g((maxnp + TPB - 1) / TPB, nzs);
+  // thread order: hyperplane order (coalesced block writes) for the FMA
+  // build, natural order (coalesced state reads) for the FP64-bound exact one
+  (h->fast ? lu_fast::jac : lu_exact::jac)(h->fast, dev(h), h->fb_d, h->fb_ls, h->ri_d, h->hstride, h->ri_ks, h->fac,
+                                          z0, g, h->stream);
   LU_CK(h, cudaGetLastError());
   return 0;
 }
@@ -338,7 +346,7 @@ void free_all(npbmz_lu_t* h) {
   for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->prim,
                   (void*)h->fac, (void*)h->work_d,
                   (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
-                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d, (void*)h->ri_d})
+                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d, (void*)h->ri_d, (void*)h->fb_d})
     if (p) cudaFree(p);
   if (h->own) cudaStreamDestroy(h->own);
 }
@@ -477,9 +485,28 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
     }
     h->max_interior = std::max(h->max_interior, acc);
   }
-  int maxnz = 0;
-  for (const LuZone& Z : h->zh) maxnz = std::max(maxnz, Z.nz);
+  int maxnz = 0, maxl = 0;
+  for (const LuZone& Z : h->zh) {
+    maxnz = std::max(maxnz, Z.nz);
+    maxl = std::max(maxl, Z.nx + Z.ny + Z.nz);
+  }
   h->ri_ks = maxnz + 2;
+  // the full-box hyperplane order of every zone's points (k_lu_jac's threads)
+  h->fb_ls = maxl + 2;
+  std::vector<int> fb((size_t)nzones * h->fb_ls * h->ri_ks, 0);
+  for (int z = 0; z < nzones; ++z) {
+    const LuZone& Z = h->zh[z];
+    int F = 0;
+    for (int l = 0; l < h->fb_ls; ++l) {
+      int R = 0;
+      for (int k = 0; k < h->ri_ks; ++k) {
+        fb[((size_t)z * h->fb_ls + l) * h->ri_ks + k] = F + R;
+        if (k >= 1 && k <= Z.nz && l >= 3 && l <= Z.nx + Z.ny + Z.nz)
+          R += std::max(0, std::min(Z.ny, l - k - 1) - std::max(1, l - k - Z.nx) + 1);
+      }
+      F += R;
+    }
+  }
   std::vector<int> ri((size_t)nzones * h->hstride * h->ri_ks, 0);
   for (int z = 0; z < nzones; ++z) {
     const LuZone& Z = h->zh[z];
@@ -524,7 +551,8 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMalloc(&h->partial, h->work_h.size() * 5 * sizeof(double)) ||
       cudaMalloc(&h->zone_out_d, (6 * (size_t)nzones + 16) * sizeof(double)) ||
       cudaMalloc(&h->stage, so * sizeof(double)) || cudaMalloc(&h->zoff_d, nzones * sizeof(long long)) ||
-      cudaMalloc(&h->hps_d, hps.size() * sizeof(int)) || cudaMalloc(&h->ri_d, ri.size() * sizeof(int)))
+      cudaMalloc(&h->hps_d, hps.size() * sizeof(int)) || cudaMalloc(&h->ri_d, ri.size() * sizeof(int)) ||
+      cudaMalloc(&h->fb_d, fb.size() * sizeof(int)))
     return bail("device allocation failed");
   if (cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(LuZone), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->nbr_d, h->nbr.data(), 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) ||
@@ -533,6 +561,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMemcpy(h->zoff_d, zoff.data(), nzones * sizeof(long long), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->hps_d, hps.data(), hps.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->ri_d, ri.data(), ri.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(h->fb_d, fb.data(), fb.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemset(h->u, 0, F) || cudaMemset(h->rsd, 0, F) || cudaMemset(h->frct, 0, F) ||
       cudaMemset(h->prim, 0, (size_t)PR_COUNT * h->NP * sizeof(double)) ||
       cudaMemset(h->fac, 0, (size_t)FAC_COUNT * h->NP * sizeof(double)))

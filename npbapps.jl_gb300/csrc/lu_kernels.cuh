@@ -624,18 +624,45 @@ __device__ __forceinline__ void jac_dir(const JC& J, double r1, const double u[5
 }
 
 // jacld's and jacu's blocks and d's factors (the Jacobian work of ssor,
-// taken off the wavefront): one thread per point of the zones, in natural
-// order, writing each block into its consumer's slot.  ri: per zone, l and
-// k, the slot of the first interior point of row k of hyperplane l.
-__global__ void __launch_bounds__(TPB) k_lu_jac(LuDev D, const LuWork* __restrict__ work, const int* __restrict__ ri,
-                                                int ls, int ks, double* __restrict__ jac) {
-  const LuWork w = work[blockIdx.x];
-  const LuZone Z = D.zones[w.zone];
+// taken off the wavefront): one thread per point of the zones (blockIdx.y:
+// zone - z0), in the zone's full-box hyperplane order (i+j+k, then k, then
+// j), so that consecutive threads write consecutive consumer slots.
+// fb: per zone, l and k, the first full-box point of row k of hyperplane l;
+// ri: the same for the interior points (the consumers' slots).
+// HP_ORDER false: threads in the zone's natural order instead (coalesced
+// reads of the point's state, scattered block writes).  The FP64-bound
+// uncontracted build is faster so, the FMA build with HP_ORDER; the values
+// written are the same either way.
+template <bool HP_ORDER>
+__global__ void __launch_bounds__(TPB) k_lu_jac(LuDev D, const int* __restrict__ fb, int fls, const int* __restrict__ ri,
+                                                int ls, int ks, double* __restrict__ jac, int z0) {
+  const int zone = z0 + blockIdx.y;
+  const LuZone Z = D.zones[zone];
+  const int T = blockIdx.x * TPB + threadIdx.x;
+  if (T >= Z.np) return;
   int i, j, k;
-  if (!decode(Z, w.first + threadIdx.x, i, j, k)) return;
+  if (HP_ORDER) {
+    const int* FB = fb + (long long)zone * fls * ks;
+    int lo = 3, hi = Z.nx + Z.ny + Z.nz;  // the hyperplane: largest l starting at or before T
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (FB[mid * ks] <= T) lo = mid; else hi = mid - 1;
+    }
+    const int l = lo;
+    int klo = 1, khi = Z.nz;  // the row: largest k starting at or before T
+    while (klo < khi) {
+      const int mid = (klo + khi + 1) / 2;
+      if (FB[l * ks + mid] <= T) klo = mid; else khi = mid - 1;
+    }
+    k = klo;
+    j = max(1, l - k - Z.nx) + (T - FB[l * ks + k]);
+    i = l - j - k;
+  } else {
+    decode(Z, T, i, j, k);
+  }
   const long long NP = D.NP, p = pidx(Z, i, j, k);
   const JC J{D.dt, Z.tx1, Z.tx2, Z.ty1, Z.ty2, Z.tz1, Z.tz2};
-  const int* R = ri + (long long)w.zone * ls * ks;
+  const int* R = ri + (long long)zone * ls * ks;
   auto slot = [&](int a, int b, int c) -> long long {
     const int l = a + b + c;
     return Z.off + R[(long long)l * ks + c] + (b - max(2, l - c - (Z.nx - 1)));
@@ -1083,8 +1110,12 @@ void pointwise(bool update, const LuDev& D, const LuWork* w, int n, double tmp, 
   else
     k_lu_pointwise<false><<<n, TPB, 0, s>>>(D, w, tmp);
 }
-void jac(const LuDev& D, const LuWork* w, int n, const int* ri, int ls, int ks, double* jac, cudaStream_t s) {
-  k_lu_jac<<<n, TPB, 0, s>>>(D, w, ri, ls, ks, jac);
+void jac(bool hp_order, const LuDev& D, const int* fb, int fls, const int* ri, int ls, int ks, double* jac, int z0,
+         dim3 grid, cudaStream_t s) {
+  if (hp_order)
+    k_lu_jac<true><<<grid, TPB, 0, s>>>(D, fb, fls, ri, ls, ks, jac, z0);
+  else
+    k_lu_jac<false><<<grid, TPB, 0, s>>>(D, fb, fls, ri, ls, ks, jac, z0);
 }
 void lower(bool scale, const LuDev& D, const double* jac, const int* hps, int hstride, int l, int z0, dim3 grid,
            cudaStream_t s) {

@@ -12,7 +12,8 @@ namespace npbmz_lu {
   void poly(const LuDev& D, const LuWork* w, int n, const CeTable& ce, cudaStream_t s);                              \
   void prim(const LuDev& D, const LuWork* w, int n, const double* g, cudaStream_t s);                                \
   void pointwise(bool update, const LuDev& D, const LuWork* w, int n, double tmp, cudaStream_t s);                   \
-  void jac(const LuDev& D, const LuWork* w, int n, const int* ri, int ls, int ks, double* jac, cudaStream_t s);     \
+  void jac(bool hp_order, const LuDev& D, const int* fb, int fls, const int* ri, int ls, int ks, double* jac,      \
+           int z0, dim3 grid, cudaStream_t s);                                                                       \
   void lower(bool scale, const LuDev& D, const double* jac, const int* hps, int hstride, int l, int z0, dim3 grid,  \
              cudaStream_t s);                                                                                        \
   void upper(const LuDev& D, const double* jac, const int* hps, int hstride, int l, int z0, dim3 grid,              \
