@@ -114,7 +114,7 @@ def test_iteration_norms_match_verify():
     np.testing.assert_array_equal(norms[-1], xcr)
 
 
-@pytest.mark.parametrize("cls", ["S", "W", "A"])
+@pytest.mark.parametrize("cls", ["S", "W", "A", "B", "C"])
 def test_go_meets_the_golden_norms(cls):
     xcr, xce, xci, verified = lu.go(cls)
     assert verified, (xcr, xce, xci)
@@ -197,7 +197,7 @@ def test_fma_build_stays_within_rounding_of_the_oracle(name, niter):
     np.testing.assert_allclose(x[2], y[2], rtol=1e-10)
 
 
-@pytest.mark.parametrize("cls", ["S", "W", "A"])
+@pytest.mark.parametrize("cls", ["S", "W", "A", "B", "C"])
 def test_fma_build_meets_the_golden_norms(cls):
     xcr, xce, xci, verified = lu.go(cls, flags=lu.FACES_NPB | lu.GRAPH | lu.FMA)
     assert verified, (xcr, xce, xci)

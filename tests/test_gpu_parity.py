@@ -195,6 +195,16 @@ def test_gpu_reproduces_npb_golden_norms(kind, cls, flags):
     np.testing.assert_allclose(xce, g[1], rtol=1e-11)
 
 
+@pytest.mark.parametrize("kind,cls", [(k, c) for c in "ABC" for k in ("BT", "SP")])
+@pytest.mark.parametrize("flags", [npbmz.EXACT | npbmz.GRAPH, npbmz.MIXED | npbmz.GRAPH])
+def test_benchmark_classes_meet_the_golden_norms(kind, cls, flags):
+    """Classes A, B and C (C: the 480x320x28 grid of 256 zones the benchmark
+    times) over the reference's full step count verify against its norms, both
+    the bit-exact FP64 step and the mixed-precision step of the headline."""
+    xcr, xce, verified = npbmz.go(kind, cls, flags)
+    assert verified is True, (xcr, xce)
+
+
 def test_perzone_launches_equal_batched(oracle_mod):
     geom, dt, _ = geom_bt24_widths()
     ce = seeded(geom)
