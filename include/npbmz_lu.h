@@ -7,8 +7,10 @@
  * whole LU domain with its own unit-cube coordinates (src/LU/setcoeff.jl,
  * src/LU/exact.jl); one process per zone (the single-rank case: no
  * exchange_1/3/4/5/6 traffic inside a zone).  Every call returns an int
- * status (0 = success, negative = error, text from npbmz_lu_last_error).  A
- * handle is not re-entrant.  Device work is issued on the handle's stream.
+ * status (0 = success, negative = error, text from npbmz_lu_last_error; for
+ * npbmz_lu_zone_setup, a failed npbmz_lu_create and a NULL handle,
+ * npbmz_lu_last_error(NULL), kept per host thread).  A handle is not
+ * re-entrant.  Device work is issued on the handle's stream.
  *
  * Host layouts (one zone):
  *   NPBMZ_LAYOUT_DENSE  [m][k][j][i], m = 0..4, k < nz, j < ny, i < nx
@@ -74,7 +76,9 @@ typedef struct npbmz_lu_handle npbmz_lu_t;
 int npbmz_lu_zone_setup(int gx, int gy, int gz, int x_zones, int y_zones, double ratio, int* nx, int* ny, int* nz,
                         int* nbr);
 
-/* Create a handle on the current CUDA device and allocate its buffers.
+/* Create a handle on the current CUDA device and allocate its buffers
+ * (about 1.2 KB per point; a problem that does not fit in the device's free
+ * memory is rejected before anything is allocated).
  * params = {dt, omega} (the reference: dt from the class, omega_default 1.2,
  * src/LU/lu_data.jl:2).  setcoeff (src/LU/setcoeff.jl) is evaluated per zone.
  * Replaces alloc_field_space + setcoeff (src/LU/lu_data.jl:92, lu-node.jl:86-97). */

@@ -105,6 +105,10 @@ struct npbmz_lu_handle {
 
 namespace {
 
+// error text of the calls without a handle (npbmz_lu_zone_setup, a failed
+// npbmz_lu_create), reported by npbmz_lu_last_error(NULL)
+thread_local std::string g_lu_error;
+
 int fail(npbmz_lu_t* h, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -112,6 +116,7 @@ int fail(npbmz_lu_t* h, const char* fmt, ...) {
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
   if (h) h->err = buf;
+  else g_lu_error = buf;
   return -1;
 }
 
@@ -356,10 +361,11 @@ void free_all(npbmz_lu_t* h) {
 extern "C" {
 
 int npbmz_lu_zone_setup(int gx, int gy, int gz, int xz, int yz, double ratio, int* nx, int* ny, int* nz, int* nbr) {
-  if (xz < 1 || yz < 1 || gx < 1 || gy < 1 || gz < 1 || !nx || !ny || !nz || !nbr) return -1;
+  if (xz < 1 || yz < 1 || gx < 1 || gy < 1 || gz < 1 || !nx || !ny || !nz || !nbr)
+    return fail(nullptr, "zone_setup: bad arguments");
   std::vector<long> x_end(xz), y_end(yz), x_start(xz), y_start(yz), x_size(xz), y_size(yz);
   if (std::fabs(ratio - 1.0e0) > 1.0e-10) {
-    if (xz < 2 || yz < 2) return -1;
+    if (xz < 2 || yz < 2) return fail(nullptr, "zone_setup: a stretched split needs 2 zones per axis");
     const double x_r = std::exp(std::log(ratio) / (xz - 1));
     const double y_r = std::exp(std::log(ratio) / (yz - 1));
     const double x_smallest = (double)gx * (x_r - 1.0e0) / (std::pow(x_r, xz) - 1.0e0);
@@ -371,11 +377,11 @@ int npbmz_lu_zone_setup(int gx, int gy, int gz, int xz, int yz, double ratio, in
       y_end[j - 1] = (long)std::nearbyint(y_smallest * (std::pow(y_r, j) - 1.0e0) / (y_r - 1.0e0) + 0.45e0);
   } else {
     for (int i = 1; i <= xz; ++i) {
-      if (((long)i * gx) % xz) return -1;
+      if (((long)i * gx) % xz) return fail(nullptr, "zone_setup: %d points do not split into %d equal zones", gx, xz);
       x_end[i - 1] = (long)i * gx / xz;
     }
     for (int j = 1; j <= yz; ++j) {
-      if (((long)j * gy) % yz) return -1;
+      if (((long)j * gy) % yz) return fail(nullptr, "zone_setup: %d points do not split into %d equal zones", gy, yz);
       y_end[j - 1] = (long)j * gy / yz;
     }
   }
@@ -401,7 +407,7 @@ int npbmz_lu_zone_setup(int gx, int gy, int gz, int xz, int yz, double ratio, in
       const int west = j > 1 ? zn - xz : zn + yz * (xz - 1);
       const int east = j < yz ? zn + xz : zn - yz * (xz - 1);
       for (int q : {north, south, west, east})
-        if (q < 1 || q > nzones) return -1;
+        if (q < 1 || q > nzones) return fail(nullptr, "zone_setup: zone %d's neighbour %d is outside the zones", zn - 1, q - 1);
       nbr[4 * (zn - 1) + 0] = west - 1;
       nbr[4 * (zn - 1) + 1] = east - 1;
       nbr[4 * (zn - 1) + 2] = south - 1;
@@ -412,10 +418,10 @@ int npbmz_lu_zone_setup(int gx, int gy, int gz, int xz, int yz, double ratio, in
 
 int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, const int* nbr, const double* params,
                     int flags, npbmz_lu_t** out) {
-  if (!out) return -1;
+  if (!out) return fail(nullptr, "out is null");
   *out = nullptr;
-  if (nzones < 1 || !nx || !ny || !nz || !nbr || !params) return -1;
-  if (flags & ~(NPBMZ_LU_FACES_NPB | NPBMZ_LU_GRAPH | NPBMZ_LU_FMA)) return -1;
+  if (nzones < 1 || !nx || !ny || !nz || !nbr || !params) return fail(nullptr, "bad geometry arguments");
+  if (flags & ~(NPBMZ_LU_FACES_NPB | NPBMZ_LU_GRAPH | NPBMZ_LU_FMA)) return fail(nullptr, "unknown flags 0x%x", flags);
   npbmz_lu_t* h = new npbmz_lu_t();
   h->nzones = nzones;
   h->flags = flags;
@@ -432,12 +438,16 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
     // reads 5)
     if (nx[z] < 5 || ny[z] < 5 || nz[z] < 5 || nz[z] != gz) {
       delete h;
-      return -1;
+      return fail(nullptr, "zone %d: size %dx%dx%d (each extent >= 5, nz equal in all zones)", z, nx[z], ny[z], nz[z]);
+    }
+    if ((long long)nx[z] * ny[z] * nz[z] > (1LL << 30)) {
+      delete h;
+      return fail(nullptr, "zone %d: more than 2^30 points", z);
     }
     for (int q = 0; q < 4; ++q)
       if (nbr[4 * z + q] < 0 || nbr[4 * z + q] >= nzones) {
         delete h;
-        return -1;
+        return fail(nullptr, "zone %d: neighbour %d outside the zones", z, nbr[4 * z + q]);
       }
     LuZone Z{};
     Z.off = off;
@@ -466,10 +476,27 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
     if (h->zh[h->nbr[4 * z + 0]].nx != h->zh[z].nx || h->zh[h->nbr[4 * z + 1]].nx != h->zh[z].nx ||
         h->zh[h->nbr[4 * z + 2]].ny != h->zh[z].ny || h->zh[h->nbr[4 * z + 3]].ny != h->zh[z].ny) {
       delete h;
-      return -1;
+      return fail(nullptr, "zone %d: neighbour face sizes do not match", z);
     }
   }
   h->NP = off;
+  {
+    // u, rsd, frct, the flux quantities and the Jacobian planes, checked
+    // before anything is allocated
+    const double need = (double)(15 + PR_COUNT + FAC_COUNT) * (double)off * sizeof(double);
+    size_t free_b = 0, total_b = 0;
+    const cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      delete h;
+      return fail(nullptr, "no usable CUDA device: %s", cudaGetErrorString(e));
+    }
+    if (need > (double)free_b) {
+      delete h;
+      return fail(nullptr, "%lld points need %.1f GB of device memory, %.1f GB free", off, need / 1e9,
+                  (double)free_b / 1e9);
+    }
+  }
   h->klo = (flags & NPBMZ_LU_FACES_NPB) ? 2 : 1;
   h->nkp = gz - 2;
   h->lmin = 6;
@@ -534,7 +561,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
     so += 10LL * h->zh[z].nx * h->nkp + 10LL * h->zh[z].ny * h->nkp;
   }
   auto bail = [&](const char* what) {
-    fail(h, "%s", what);
+    fail(nullptr, "%s: %s", what, cudaGetErrorString(cudaGetLastError()));
     free_all(h);
     delete h;
     return -1;
@@ -571,7 +598,7 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
 }
 
 int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   std::memcpy(h->ce.c, ce ? ce : &ce_reference[0][0], sizeof(h->ce.c));
   const int n = (int)h->work_h.size();
@@ -588,32 +615,32 @@ int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
 }
 
 int npbmz_lu_upload(npbmz_lu_t* h, int zone, int field, int layout, const double* host) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   return transfer(h, zone, field, layout, const_cast<double*>(host), true);
 }
 
 int npbmz_lu_download(npbmz_lu_t* h, int zone, int field, int layout, double* host) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   return transfer(h, zone, field, layout, host, false);
 }
 
 int npbmz_lu_exch_qbc(npbmz_lu_t* h) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   return launch_exch(h);
 }
 
 int npbmz_lu_ssor(npbmz_lu_t* h, int zone) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   if (zone < -1 || zone >= h->nzones) return fail(h, "zone %d out of range", zone);
   return launch_phase(h, NPBMZ_LU_PHASE_SSOR, zone);
 }
 
 int npbmz_lu_phase(npbmz_lu_t* h, int phase, int zone) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   if (zone < -1 || zone >= h->nzones) return fail(h, "zone %d out of range", zone);
   if (phase < 0 || phase > NPBMZ_LU_PHASE_SSOR) return fail(h, "unknown LU phase %d", phase);
@@ -621,7 +648,7 @@ int npbmz_lu_phase(npbmz_lu_t* h, int phase, int zone) {
 }
 
 int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   if (niter < 0) return fail(h, "niter < 0");
   if (rsdnm && niter > h->norms_cap) {
@@ -663,7 +690,7 @@ int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
 }
 
 int npbmz_lu_verify(npbmz_lu_t* h, double* xcr, double* xce, double* xci) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   if (!xcr || !xce || !xci) return fail(h, "null output");
   double* o = h->zone_out_d;  // [0,5) xcr, [5,10) xce, [16, 16+nzones) frc per zone
@@ -686,20 +713,20 @@ int npbmz_lu_verify(npbmz_lu_t* h, double* xcr, double* xce, double* xci) {
 }
 
 int npbmz_lu_set_stream(npbmz_lu_t* h, void* stream) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   h->stream = stream ? (cudaStream_t)stream : h->own;
   return 0;
 }
 
 int npbmz_lu_synchronize(npbmz_lu_t* h) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   LU_CK(h, cudaStreamSynchronize(h->stream));
   return 0;
 }
 
 int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   int n = 2 + 3;  // exch (pack, unpack) + jac + update + rhs
   for (int l = h->lmin; l <= h->lmax; ++l) {
     int c = 0;
@@ -744,10 +771,10 @@ int npbmz_lu_profile(npbmz_lu_t* h, int niter, double* phase_ms) {
   return rc;
 }
 
-const char* npbmz_lu_last_error(npbmz_lu_t* h) { return h ? h->err.c_str() : "null handle"; }
+const char* npbmz_lu_last_error(npbmz_lu_t* h) { return h ? h->err.c_str() : g_lu_error.c_str(); }
 
 int npbmz_lu_destroy(npbmz_lu_t* h) {
-  if (!h) return -1;
+  if (!h) return fail(nullptr, "null handle");
   cudaStreamSynchronize(h->stream);
   free_all(h);
   delete h;

@@ -216,7 +216,7 @@ mutable struct LuProblem
         rc = ccall((:npbmz_lu_create, libnpbmz), Cint,
                    (Cint, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cdouble}, Cint, Ptr{Ptr{Cvoid}}),
                    n, Cint.(nx), Cint.(ny), Cint.(nz), Cint.(nbr), params, flags, out)
-        rc == 0 || error("npbmz_lu_create failed (zone sizes below 5, unequal nz, mismatched faces or bad flags)")
+        rc == 0 || error("npbmz_lu_create: " * unsafe_string(ccall((:npbmz_lu_last_error, libnpbmz), Cstring, (Ptr{Cvoid},), C_NULL)))
         p = new(out[], n, ReentrantLock())
         finalizer(p) do q
             q.handle != C_NULL && ccall((:npbmz_lu_destroy, libnpbmz), Cint, (Ptr{Cvoid},), q.handle)
@@ -236,7 +236,7 @@ function lu_zone_setup(gx, gy, gz, x_zones, y_zones, ratio = 1.0)
     rc = ccall((:npbmz_lu_zone_setup, libnpbmz), Cint,
                (Cint, Cint, Cint, Cint, Cint, Cdouble, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}),
                gx, gy, gz, x_zones, y_zones, ratio, nx, ny, nz, nbr)
-    rc == 0 || error("npbmz_lu_zone_setup failed")
+    rc == 0 || error("npbmz_lu_zone_setup: " * unsafe_string(ccall((:npbmz_lu_last_error, libnpbmz), Cstring, (Ptr{Cvoid},), C_NULL)))
     return nx, ny, nz, nbr
 end
 

@@ -77,7 +77,8 @@ def lu_zone_setup(gx, gy, gz, x_zones, y_zones, ratio=1.0):
     nbr = np.zeros(4 * n, np.int32)
     rc = lib().npbmz_lu_zone_setup(gx, gy, gz, x_zones, y_zones, ratio, _ip(nx), _ip(ny), _ip(nz), _ip(nbr))
     if rc != 0:
-        raise NpbmzError(f"npbmz_lu_zone_setup failed for {gx}x{gy}x{gz}, {x_zones}x{y_zones} zones")
+        raise NpbmzError(f"npbmz_lu_zone_setup failed for {gx}x{gy}x{gz}, {x_zones}x{y_zones} zones: "
+                         + lib().npbmz_lu_last_error(None).decode())
     return nx, ny, nz, nbr
 
 
@@ -98,7 +99,7 @@ class LuProblem:
         rc = lib().npbmz_lu_create(self.nzones, _ip(self.nx), _ip(self.ny), _ip(self.nz), _ip(self.nbr),
                                    _dp(params), flags, ctypes.byref(h))
         if rc != 0 or not h.value:
-            raise NpbmzError("npbmz_lu_create failed (zone sizes below 5, unequal nz, mismatched faces or bad flags)")
+            raise NpbmzError("npbmz_lu_create failed: " + lib().npbmz_lu_last_error(None).decode())
         self._h = h
 
     @classmethod

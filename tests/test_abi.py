@@ -107,8 +107,20 @@ def test_lu_zone_setup_matches_oracle(npbmz_mod, oracle_mod, cls):
 def test_lu_zone_setup_rejects_non_integer_extents(npbmz_mod):
     from npbmz import lu
 
-    with pytest.raises(npbmz.NpbmzError):
+    with pytest.raises(npbmz.NpbmzError, match="do not split into 4 equal zones"):
         lu.lu_zone_setup(25, 24, 6, 4, 4)
+
+
+def test_lu_calls_without_a_handle_report_an_error(npbmz_mod):
+    """A NULL handle is an error with text, read from npbmz_lu_last_error(NULL)
+    (no device work: the call returns before touching CUDA)."""
+    from npbmz import lu
+
+    L = lu.lib()
+    assert L.npbmz_lu_ssor(None, 0) < 0
+    assert L.npbmz_lu_last_error(None) == b"null handle"
+    with pytest.raises(npbmz.NpbmzError, match="outside the zones"):
+        lu.lu_zone_setup(24, 24, 6, 3, 2)
 
 
 def test_julia_bindings_call_only_declared_entry_points():

@@ -155,13 +155,26 @@ def test_upload_download_all_zones_dense():
 
 def test_create_rejects_bad_geometry():
     nx, ny, nz, nbr = lu.lu_zone_setup(16, 16, 6, 4, 4)  # zones 4 wide: below the 5-point stencil
-    with pytest.raises(npbmz.NpbmzError):
+    with pytest.raises(npbmz.NpbmzError, match="size 4x4x6"):
         lu.LuProblem(nx, ny, nz, nbr, 0.5)
     nx, ny, nz, nbr = lu.lu_zone_setup(24, 24, 6, 4, 4)
-    with pytest.raises(npbmz.NpbmzError):
+    with pytest.raises(npbmz.NpbmzError, match="unknown flags"):
         lu.LuProblem(nx, ny, nz, nbr, 0.5, flags=0x80)
-    with pytest.raises(npbmz.NpbmzError):
+    with pytest.raises(npbmz.NpbmzError, match="outside the zones"):
         lu.lu_zone_setup(24, 24, 6, 3, 2)  # the reference's neighbour rule leaves the zone range
+
+
+def test_create_rejects_a_problem_larger_than_device_memory():
+    """Class E (4224x3456x92, 1.34 G points, about 1.6 TB of state and Jacobian
+    planes) is refused before any device allocation, and leaves no pending
+    error behind: a handle created next runs."""
+    with pytest.raises(npbmz.NpbmzError, match="GB of device memory"):
+        lu.LuProblem.from_class("E")
+    g, dt = GEOMS["S"]
+    p, o = make(g(), dt)
+    p.iterate(2)
+    o.iterate(2)
+    np.testing.assert_array_equal(p.download(0, lu.U), o.get(lu.U, 0))
 
 
 def test_phase_and_zone_errors_are_reported():
