@@ -128,13 +128,6 @@ int fail(npbmz_lu_t* h, const char* fmt, ...) {
 
 LuDev dev(npbmz_lu_t* h) { return LuDev{h->u, h->rsd, h->frct, h->prim, h->NP, h->zones_d, h->dt, h->omega}; }
 
-// the same, with zones starting at z0 (kernels that index zones by blockIdx.y)
-LuDev dev_zone0(npbmz_lu_t* h, int z0) {
-  LuDev d = dev(h);
-  d.zones = h->zones_d + z0;
-  return d;
-}
-
 Faces faces(npbmz_lu_t* h) { return Faces{h->stage, h->zoff_d, h->nbr_d, h->klo, h->nkp}; }
 
 int hp_count(const LuZone& Z, int l) {
