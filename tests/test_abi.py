@@ -37,6 +37,45 @@ def test_library_exports_every_declared_symbol(npbmz_mod):
             assert hasattr(L, name), name
 
 
+def test_headers_compile_and_link_as_c(npbmz_mod, tmp_path):
+    """A C99 consumer (what a ccall, cgo or ctypes binding sees) compiles
+    against both headers with every warning an error, takes the address of
+    every declared entry point, links against libnpbmz_gpu.so, and runs the
+    calls that need no device: zone set-up and the NULL-handle errors."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = declared_functions(HEADER) + declared_functions(LU_HEADER)
+    src = tmp_path / "consumer.c"
+    src.write_text(
+        "#include <stdio.h>\n#include <string.h>\n"
+        '#include "npbmz.h"\n#include "npbmz_lu.h"\n'
+        "typedef void (*fn)(void);\n"
+        "static const fn entry[] = {" + ", ".join(f"(fn){n}" for n in names) + "};\n"
+        "int main(void) {\n"
+        "  int nx[16], ny[16], nz[16], nbr[64], i;\n"
+        "  for (i = 0; i < (int)(sizeof entry / sizeof entry[0]); ++i) if (!entry[i]) return 10;\n"
+        "  if (npbmz_zone_setup(NPBMZ_BT, 24, 24, 6, 2, 2, 1.0, nx, ny, nz, nbr) != 0) return 11;\n"
+        "  if (nx[0] != 12 || ny[3] != 12 || nz[2] != 6) return 12;\n"
+        "  if (npbmz_lu_zone_setup(24, 24, 6, 4, 4, 1.0, nx, ny, nz, nbr) != 0) return 13;\n"
+        "  if (nx[15] != 6 || nbr[0] != 12) return 14;\n"
+        "  if (npbmz_lu_ssor(NULL, 0) >= 0) return 15;\n"
+        '  if (strcmp(npbmz_lu_last_error(NULL), "null handle") != 0) return 16;\n'
+        "  if (npbmz_lu_zone_setup(25, 24, 6, 4, 4, 1.0, nx, ny, nz, nbr) == 0) return 17;\n"
+        '  if (!strstr(npbmz_lu_last_error(NULL), "equal zones")) return 18;\n'
+        '  printf("c consumer ok\\n");\n'
+        "  return 0;\n}\n")
+    libdir = npbmz_mod.lib_path().parent
+    exe = tmp_path / "consumer"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{INCLUDE}", str(src), "-o", str(exe),
+                    f"-L{libdir}", "-lnpbmz_gpu", f"-Wl,-rpath,{libdir}"], check=True, capture_output=True, text=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "c consumer ok" in r.stdout, (r.returncode, r.stdout, r.stderr)
+
+
 def test_library_is_built_for_sm_103a():
     from npbmz import build
 
