@@ -50,8 +50,11 @@ typedef struct npbmz_lu_handle npbmz_lu_t;
 #define NPBMZ_LU_FMA 0x4       /* the iteration's kernels built with FMA
                                   contraction (a*b+c rounded once): faster on
                                   the FP64 pipe, no longer bit-for-bit the
-                                  reference's rounding (set-up, exch_qbc and
-                                  the norms stay uncontracted) */
+                                  reference's rounding (setbv, setiv, erhs,
+                                  exch_qbc's face copies and the norms stay
+                                  uncontracted; the flux quantities of u and
+                                  every rhs, the first included, come from the
+                                  contracted build) */
 
 /* fields */
 #define NPBMZ_LU_U 0

@@ -596,7 +596,9 @@ int npbmz_lu_setup(npbmz_lu_t* h, const double* ce) {
   std::memcpy(h->ce.c, ce ? ce : &ce_reference[0][0], sizeof(h->ce.c));
   const int n = (int)h->work_h.size();
   jac_stale(h, 0, h->nzones);
-  // set-up always without contraction: both builds start from the same state
+  // setbv, setiv and erhs always without contraction: both builds start from
+  // the same u and frct; the flux quantities of u and the first rhs come from
+  // the iteration's build, as every later one does
   lu_exact::init(dev(h), h->work_d, n, h->ce, h->stream);
   lu_exact::poly(dev(h), h->work_d, n, h->ce, h->stream);
   lu_exact::prim(dev(h), h->work_d, n, h->rsd, h->stream);
@@ -730,14 +732,14 @@ int npbmz_lu_launches_per_iteration(npbmz_lu_t* h) {
 }
 
 int npbmz_lu_profile(npbmz_lu_t* h, int niter, double* phase_ms) {
-  if (!h || !phase_ms || niter < 1) return -1;
+  if (!h) return fail(nullptr, "null handle");
+  if (!phase_ms || niter < 1) return fail(h, "profile needs phase_ms and niter >= 1");
   std::lock_guard<std::mutex> g(h->mu);
   constexpr int NPH = 6;  // exch, jac, lower, upper, update, rhs
   cudaEvent_t ev[NPH + 1];
   for (auto& e : ev) LU_CK(h, cudaEventCreate(&e));
   for (int q = 0; q < NPH; ++q) phase_ms[q] = 0.0;
   int rc = 0;
-  const int n = (int)h->work_h.size();
   for (int it = 0; it < niter && !rc; ++it) {
     cudaEventRecord(ev[0], h->stream);
     rc = launch_exch(h);
@@ -759,7 +761,6 @@ int npbmz_lu_profile(npbmz_lu_t* h, int niter, double* phase_ms) {
       phase_ms[q] += ms;
     }
   }
-  (void)n;
   for (auto& e : ev) cudaEventDestroy(e);
   return rc;
 }
