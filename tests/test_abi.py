@@ -76,6 +76,20 @@ def test_headers_compile_and_link_as_c(npbmz_mod, tmp_path):
     assert r.returncode == 0 and "c consumer ok" in r.stdout, (r.returncode, r.stdout, r.stderr)
 
 
+def test_no_device_means_no_handle(npbmz_mod):
+    """Without a CUDA device the library refuses to create a problem, with the
+    CUDA error in its text: there is no CPU fallback to run instead."""
+    from npbmz import lu
+
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(npbmz.NpbmzError, match="CUDA|cuda"):
+        lu.LuProblem.from_class("S")
+    with pytest.raises(npbmz.NpbmzError, match="CUDA|cuda"):
+        npbmz.Problem.from_class("BT", "S")
+
+
 def test_library_is_built_for_sm_103a():
     from npbmz import build
 
