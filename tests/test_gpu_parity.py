@@ -205,6 +205,14 @@ def test_benchmark_classes_meet_the_golden_norms(kind, cls, flags):
     assert verified is True, (xcr, xce)
 
 
+def test_bt_class_d_meets_the_golden_norms():
+    """BT class D (1632x1216x34, 67.5 M points in 1024 zones, about 85 GB on
+    the device, 250 steps) on the mixed-precision graph step verifies against
+    the reference's norms."""
+    xcr, xce, verified = npbmz.go("BT", "D", npbmz.MIXED | npbmz.GRAPH)
+    assert verified is True, (xcr, xce)
+
+
 def test_perzone_launches_equal_batched(oracle_mod):
     geom, dt, _ = geom_bt24_widths()
     ce = seeded(geom)
