@@ -27,7 +27,10 @@ def run_class(oracle_mod, kind, cls):
 @pytest.mark.parametrize(
     "kind,cls",
     [("BT", "S"), ("BT", "W"), ("SP", "S"), ("SP", "W"), ("SP", "A"),
-     pytest.param("BT", "A", marks=pytest.mark.slow)],
+     pytest.param("BT", "A", marks=pytest.mark.slow),
+     # 304x208x17 in 64 geometric zones (ratio 4.5): the geometry of the
+     # BT class B benchmark configuration, about 45 s on 8 cores
+     pytest.param("BT", "B", marks=pytest.mark.slow)],
 )
 def test_oracle_reproduces_npb_golden_norms(oracle_mod, kind, cls):
     xcr, xce = run_class(oracle_mod, kind, cls)
