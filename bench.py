@@ -82,6 +82,10 @@ PHASE_KERNELS = {
 }
 
 
+def plural(n, noun):
+    return f"{n} {noun}" + ("" if n == 1 else "s")
+
+
 def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -237,7 +241,8 @@ def cpu_baseline(kind, cls, ce, target_s=15.0):
     t = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": pts * n / t / 1e6, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{n} full time steps of the {kind}-MZ class {cls} grid ({pts} points, all zones) after 1 untimed step"}
+            "sample": f"{plural(n, 'full time step')} of the {kind}-MZ class {cls} grid ({pts} points, all zones) "
+                      "after 1 untimed step"}
 
 
 def lu_cpu_run(cls, warmup, steps):
@@ -264,7 +269,8 @@ def lu_cpu_baseline(cls, target_s=15.0):
     t, pts, _ = lu_cpu_run(cls, 1, n)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": pts * n / t / 1e6, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{n} SSOR iterations of the LU-MZ class {cls} grid ({pts} points, all zones) after 1 untimed"}
+            "sample": f"{plural(n, 'SSOR iteration')} of the LU-MZ class {cls} grid ({pts} points, all zones) "
+                      "after 1 untimed iteration"}
 
 
 def run_reference(args):
@@ -285,7 +291,8 @@ def run_reference(args):
             "config": {"workload": desc, "points": pts, "zones": nzones,
                        "variant": "reference CPU path (LU-MZ oracle port), FP64"},
             "cpu_baseline": {"value": value, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} SSOR iterations after {args.warmup} warm-up iterations"},
+                             "sample": f"{plural(args.steps, 'SSOR iteration')} after "
+                                       f"{plural(args.warmup, 'warm-up iteration')}"},
             "e2e": {"value": value, "unit": "Mgridpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
@@ -310,7 +317,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc, "points": pts, "zones": len(nx), "variant": "reference CPU path (oracle port), FP64"},
         "cpu_baseline": {"value": value, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full time steps after {args.warmup} warm-up steps"},
+                         "sample": f"{plural(args.steps, 'full time step')} after {plural(args.warmup, 'warm-up step')}"},
         "e2e": {"value": value, "unit": "Mgridpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
