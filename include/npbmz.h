@@ -251,7 +251,8 @@ int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* params, const 
                             void* stream);
 
 /* Error text of the last failing call on h (h may be NULL for create and for
- * npbmz_bt_xsolve_noalloc). */
+ * npbmz_bt_xsolve_noalloc: the last such failure on the calling host
+ * thread). */
 const char* npbmz_last_error(npbmz_t* h);
 
 /* Free every device buffer and the handle. */

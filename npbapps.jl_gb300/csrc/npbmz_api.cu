@@ -24,7 +24,8 @@ namespace {
 
 constexpr int PTS_TPB = 128;   // points per CTA of the point kernels (power of two)
 
-std::string g_create_error;
+// error text of the calls without a handle, per host thread
+thread_local std::string g_create_error;
 
 Consts make_consts(double dt, int gx, int gy, int gz, int xz, int yz) {
   // set_constants, src/BT/set_constants.jl:1-130 (SP: the same file body)
