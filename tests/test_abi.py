@@ -208,3 +208,55 @@ def test_julia_shim_arities_match_the_reference_signatures():
         args = [a.strip() for a in sig.split(",") if a.strip()]
         n = len(args) + sum(rest)
         assert n == arity, (name, n, arity)
+
+
+def _zone_geometries(seed, count, square=False):
+    """Seeded random splits: equal zones (extent a multiple of the zone count)
+    and geometric ones (ratio in [1.5, 6]); square: x_zones == y_zones."""
+    rng = np.random.default_rng(seed)
+    for _ in range(count):
+        xz, yz = (int(v) for v in rng.integers(2, 17, size=2))
+        if square:
+            yz = xz
+        if rng.random() < 0.5:
+            gx, gy, ratio = xz * int(rng.integers(3, 40)), yz * int(rng.integers(3, 40)), 1.0
+        else:
+            gx, gy = (int(v) for v in rng.integers(16 * max(xz, yz), 40 * max(xz, yz) + 1, size=2))
+            ratio = float(rng.uniform(1.5, 6.0))
+        yield gx, gy, int(rng.integers(3, 40)), xz, yz, ratio
+
+
+def test_zone_setup_properties_on_random_splits(npbmz_mod, oracle_mod):
+    """300 seeded splits, BT/SP rule: the library's zone_setup equals the
+    oracle's, the widths tile the grid, and the neighbour table is the
+    periodic one (the east neighbour's west neighbour is the zone itself)."""
+    for gx, gy, gz, xz, yz, ratio in _zone_geometries(11, 300):
+        a = npbmz.zone_setup(npbmz.BT, gx, gy, gz, xz, yz, ratio)
+        b = oracle_mod.zone_setup(oracle_mod.KIND_BT, gx, gy, gz, xz, yz, ratio)
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y, err_msg=str((gx, gy, gz, xz, yz, ratio)))
+        nx, ny, nz, nbr = a
+        w = nbr.reshape(-1, 4)
+        assert nx.reshape(yz, xz)[0].sum() == gx and ny.reshape(yz, xz)[:, 0].sum() == gy
+        assert np.all(nz == gz)
+        z = np.arange(xz * yz)
+        assert np.array_equal(w[w[z, 1], 0], z) and np.array_equal(w[w[z, 3], 2], z)
+        assert np.array_equal(w[z, 1], (z // xz) * xz + (z % xz + 1) % xz)
+
+
+def test_lu_zone_setup_properties_on_random_splits(oracle_mod):
+    """200 seeded square splits (LU's neighbour rule assumes x_zones ==
+    y_zones), LU rule: the library equals the oracle, the widths tile the grid,
+    and south/north and west/east are inverse pairs."""
+    from npbmz import lu
+
+    for gx, gy, gz, xz, _, ratio in _zone_geometries(12, 200, square=True):
+        a = lu.lu_zone_setup(gx, gy, gz, xz, xz, ratio)
+        b = oracle_mod.lu_zone_setup(gx, gy, gz, xz, xz, ratio)
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y, err_msg=str((gx, gy, gz, xz, ratio)))
+        nx, ny, nz, nbr = a
+        w = nbr.reshape(-1, 4)
+        assert nx.reshape(xz, xz)[0].sum() == gx and ny.reshape(xz, xz)[:, 0].sum() == gy
+        z = np.arange(xz * xz)
+        assert np.array_equal(w[w[z, 1], 0], z) and np.array_equal(w[w[z, 3], 2], z)
