@@ -260,3 +260,87 @@ def test_lu_zone_setup_properties_on_random_splits(oracle_mod):
         assert nx.reshape(xz, xz)[0].sum() == gx and ny.reshape(xz, xz)[:, 0].sum() == gy
         z = np.arange(xz * xz)
         assert np.array_equal(w[w[z, 1], 0], z) and np.array_equal(w[w[z, 3], 2], z)
+
+
+def _c_prototypes():
+    """{name: (return type, [parameter types])} of both headers."""
+    protos = {}
+    for header in (HEADER, LU_HEADER):
+        text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+        text = re.sub(r"^\s*#.*$", "", text, flags=re.M)
+        for ret, name, params in re.findall(r"([A-Za-z_][\w \t*]*?)\s*\b(npbmz_\w+)\s*\(([^)]*)\)\s*;", text):
+            types = []
+            for prm in params.split(","):
+                prm = " ".join(prm.split())
+                if prm and prm != "void":
+                    types.append(re.sub(r"\b\w+$", "", prm).replace(" *", "*").strip())
+            protos[name] = (ret.strip(), types)
+    return protos
+
+
+def _julia_ccalls(text):
+    """(name, return type, [argument types]) of every ccall into libnpbmz."""
+    def split_top(s):
+        out, depth, cur = [], 0, ""
+        for ch in s:
+            if ch in "({":
+                depth += 1
+            elif ch in ")}":
+                depth -= 1
+            if ch == "," and depth == 0:
+                out.append(cur.strip())
+                cur = ""
+            else:
+                cur += ch
+        if cur.strip():
+            out.append(cur.strip())
+        return out
+
+    calls = []
+    for m in re.finditer(r"ccall\(\(:(\w+),\s*libnpbmz\),\s*", text):
+        rest = text[m.end():]
+        ret = rest[:rest.index(",")].strip()
+        rest = rest[rest.index(",") + 1:].lstrip()
+        assert rest.startswith("("), m.group(1)
+        depth = 0
+        for i, ch in enumerate(rest):
+            depth += ch == "("
+            depth -= ch == ")"
+            if depth == 0:
+                break
+        calls.append((m.group(1), ret, split_top(rest[1:i])))
+    return calls
+
+
+_JULIA_SCALAR = {"Cint": "int", "Cdouble": "double", "UInt64": "uint64_t", "Csize_t": "size_t"}
+
+
+def _compatible(c_type, jl_type):
+    if "*" in c_type:
+        base = c_type.replace("const ", "").rstrip("*").strip()
+        if c_type.count("*") == 2:
+            return jl_type in ("Ptr{Ptr{Cvoid}}", "Ref{Ptr{Cvoid}}")
+        if jl_type == "Ptr{Cvoid}":
+            return True
+        want = {"double": ("Ptr{Cdouble}", "Ref{Cdouble}"), "int": ("Ptr{Cint}", "Ref{Cint}"),
+                "char": ("Cstring", "Ptr{UInt8}")}.get(base, ())
+        return jl_type in want
+    return _JULIA_SCALAR.get(jl_type) == c_type
+
+
+def test_julia_ccalls_match_the_c_prototypes():
+    """Every ccall in the Julia binding passes as many arguments as the C
+    prototype declares, each of a compatible type, and expects its return
+    type (Julia is not installed here, so this is the check its calls get)."""
+    protos = _c_prototypes()
+    julia = Path(__file__).resolve().parents[1] / "npbapps.jl_gb300" / "julia"
+    n = 0
+    for f in sorted(julia.glob("*.jl")):
+        for name, ret, args in _julia_ccalls(f.read_text()):
+            c_ret, c_args = protos[name]
+            assert len(args) == len(c_args), (f.name, name, args, c_args)
+            for c, j in zip(c_args, args):
+                assert _compatible(c, j), (f.name, name, c, j)
+            assert (ret == "Cint") if c_ret == "int" else (ret in ("Cstring", "Ptr{UInt8}")), (f.name, name, ret)
+            n += 1
+    assert n >= 30
