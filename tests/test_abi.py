@@ -344,3 +344,35 @@ def test_julia_ccalls_match_the_c_prototypes():
             assert (ret == "Cint") if c_ret == "int" else (ret in ("Cstring", "Ptr{UInt8}")), (f.name, name, ret)
             n += 1
     assert n >= 30
+
+
+def _ctypes_compatible(c_type, ct):
+    import ctypes
+
+    if "*" in c_type:
+        base = c_type.replace("const ", "").rstrip("*").strip()
+        if c_type.count("*") == 2:
+            return ct is ctypes.POINTER(ctypes.c_void_p)
+        if ct is ctypes.c_void_p:
+            return True
+        want = {"double": ctypes.POINTER(ctypes.c_double), "int": ctypes.POINTER(ctypes.c_int),
+                "char": ctypes.c_char_p}.get(base)
+        return ct is want
+    return ct is {"int": ctypes.c_int, "double": ctypes.c_double, "uint64_t": ctypes.c_uint64,
+                  "size_t": ctypes.c_size_t, "int64_t": ctypes.c_int64}[c_type]
+
+
+def test_python_ctypes_declarations_match_the_c_prototypes(npbmz_mod):
+    """The ctypes binding declares every entry point of both headers with the
+    prototype's argument count, compatible argument types and return type."""
+    from npbmz import lu
+
+    L = npbmz_mod.lib()
+    lu.lib()
+    for name, (c_ret, c_args) in _c_prototypes().items():
+        f = getattr(L, name)
+        assert f.argtypes is not None, name
+        assert len(f.argtypes) == len(c_args), (name, f.argtypes, c_args)
+        for c, ct in zip(c_args, f.argtypes):
+            assert _ctypes_compatible(c, ct), (name, c, ct)
+        assert _ctypes_compatible(c_ret, f.restype), (name, c_ret, f.restype)
