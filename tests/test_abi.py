@@ -376,3 +376,31 @@ def test_python_ctypes_declarations_match_the_c_prototypes(npbmz_mod):
         for c, ct in zip(c_args, f.argtypes):
             assert _ctypes_compatible(c, ct), (name, c, ct)
         assert _ctypes_compatible(c_ret, f.restype), (name, c_ret, f.restype)
+
+
+def test_the_product_never_reaches_the_oracle(npbmz_mod):
+    """The oracle is test infrastructure: no module of the package imports it,
+    no CUDA/C++ source includes it, the build does not link it, and the built
+    library depends on the CUDA runtime and the C/C++ runtimes only."""
+    import ast
+    import subprocess
+
+    pkg = Path(__file__).resolve().parents[1] / "npbapps.jl_gb300"
+    for f in pkg.rglob("*.py"):
+        for node in ast.walk(ast.parse(f.read_text())):
+            if isinstance(node, ast.Import):
+                mods = [a.name for a in node.names]
+            elif isinstance(node, ast.ImportFrom):
+                mods = [node.module or ""]
+            else:
+                continue
+            assert not any(m.split(".")[0] == "oracle" for m in mods), (f, mods)
+    for f in list(pkg.rglob("*.cu")) + list(pkg.rglob("*.cuh")) + list(pkg.rglob("*.h")):
+        for inc in re.findall(r'#\s*include\s*[<"]([^>"]+)[>"]', f.read_text()):
+            assert "oracle" not in inc, (f, inc)
+    assert "oracle" not in (pkg / "npbmz" / "build.py").read_text()
+    out = subprocess.run(["readelf", "-d", str(npbmz_mod.lib_path())], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("readelf unavailable")
+    needed = re.findall(r"\(NEEDED\)\s+Shared library: \[([^\]]+)\]", out.stdout)
+    assert needed and all(re.match(r"lib(cudart|stdc\+\+|m|gcc_s|c|dl|pthread|rt)\.so|ld-linux", n) for n in needed), needed
