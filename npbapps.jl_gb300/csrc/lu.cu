@@ -322,10 +322,11 @@ int transfer(npbmz_lu_t* h, int zone, int field, int layout, double* host, bool 
     if (up) {
       LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
       lu_exact::convert(layout == NPBMZ_LAYOUT_REF, true, dev(h), f, h->img, z, blocks, h->stream);
-      if (field == NPBMZ_LU_U) jac_stale(h, z, 1);
-      if (field == NPBMZ_LU_U)
+      if (field == NPBMZ_LU_U) {
+        jac_stale(h, z, 1);
         (h->fast ? lu_fast::prim : lu_exact::prim)(dev(h), h->work_d + h->zblock[z], h->zblock[z + 1] - h->zblock[z],
                                                   h->u, h->stream);
+      }
     } else {
       if (layout == NPBMZ_LAYOUT_REF)  // keep the host halo: start from the host image
         LU_CK(h, cudaMemcpyAsync(h->img, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
