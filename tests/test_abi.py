@@ -1,6 +1,9 @@
-"""The C ABI library builds for sm_103a, loads, and exports every entry point
-include/npbmz.h and include/npbmz_lu.h declare; host-side helpers that need
-no GPU."""
+"""The C ABI without a GPU: the library builds for sm_103a, loads, and exports
+every entry point include/npbmz.h and include/npbmz_lu.h declare; a C99
+consumer compiles and links against both headers; the Julia ccalls and the
+Python ctypes declarations match the prototypes; the package never reaches
+the oracle and creates no handle without a device; and the host-side helpers
+(zone set-up, seeded coefficients, layouts) agree with the oracle."""
 import re
 from pathlib import Path
 

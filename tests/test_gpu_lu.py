@@ -9,7 +9,8 @@ order) are held to 1e-13.  Geometries: LU-MZ classes S, W and B (4x4 zones
 of 6x6x6, 16x16x8 and 76x52x17), zones of the minimum size 5x5x5 (where the
 fourth-difference boundary stencils overlap), rectangular 9x7x7 zones, 2x2
 zones, and stretched zones of unequal sizes; the reference's ce table and a
-perturbed one.
+perturbed one.  Whole runs of classes S to C, in the bit-exact and the FMA
+build, meet the reference's verification norms (epsilon 1e-8).
 """
 import numpy as np
 import pytest
