@@ -1,6 +1,8 @@
 // lumz_oracle.cpp -- CPU restatement of NPBApps.jl's LU-MZ single-rank SSOR
-// iteration (TEST INFRASTRUCTURE ONLY: tests/ load liblumz_oracle.so to
-// compare the GPU LU path against; nothing in the product links it).
+// iteration (TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and
+// bench.py's CPU-baseline leg and reference arm load liblumz_oracle.so, to
+// compare the GPU LU path against or to time the reference's CPU path;
+// nothing in the product links it).
 //
 // One MPI rank per zone, one process (the reference's single-rank case):
 // every zone is a whole LU domain (row = col = 1, all four process
