@@ -3,8 +3,9 @@
 // TEST INFRASTRUCTURE ONLY.  This file is the oracle: a scalar, loop-for-loop
 // restatement of the reference's single-rank path (one MPI rank per cluster,
 // ncells = 1, so cell_start = cell_end = 1 and each line solve is one stage).
-// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
-// it, and only to compare against.  The product (libnpbmz_gpu.so) never calls it.
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg and
+// reference arm may load it: to compare against, or to time the reference's
+// CPU path.  The product (libnpbmz_gpu.so) never calls it.
 //
 // Every arithmetic expression keeps the reference's operand order and
 // parenthesisation, and the file is compiled with -ffp-contract=off, because

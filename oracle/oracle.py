@@ -2,7 +2,8 @@
 
 The oracle restates the NPBApps.jl BT-MZ/SP-MZ single-rank time step on the
 CPU (oracle/npbmz_oracle.cpp).  Only tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py use it, always to compare against.  The tangent
+CPU-baseline leg and reference arm of bench.py use it: to compare against, or
+to time the reference's CPU path.  The tangent
 library (oracle/npbmz_tangent.cpp) is the same BT and SP restatement with
 forward-mode dual numbers: the reference directional derivatives against
 which tests check the GPU adjoint.  liblumz_oracle.so (oracle/lumz_oracle.cpp)
