@@ -13,10 +13,12 @@
 # Julia dispatch prefers it exactly when those arguments are DeviceZones; the
 # other arguments (MPI buffers, scratch, constants) are ignored: the library
 # holds its own.  Positions: BT adi forcing / u / rhs at 14 / 15 / 16 of 76
-# (src/BT/adi.jl:5-80); SP adi u / rhs at 11 / 12 and forcing at 25 of 99
-# (src/SP/adi.jl:6-104); exch_qbc u at 17 of 25 (src/BT/exchange_qbc.jl:1-26,
-# src/SP/exchange_qbc.jl).  adi of one zone runs under the handle's lock, as
-# the reference calls it from Threads.@threads; NPBAppsGPU.adi!(gpu) (all
+# (src/BT/adi.jl:5-80); SP adi u / rhs at 11 / 12 and forcing at 26 of 99,
+# after speed at 25 (src/SP/adi.jl:6-104, called so from
+# src/SP/sp-node.jl:291-316); exch_qbc u at 17 of 25
+# (src/BT/exchange_qbc.jl:1-26, src/SP/exchange_qbc.jl:1-26).  adi of one
+# zone runs under the handle's lock, as the reference calls it from
+# Threads.@threads; NPBAppsGPU.adi!(gpu) (all
 # zones batched in one launch per phase) is the fast form of the same loop.
 # The same for LU-MZ's ssor and exch_qbc (below).  Julia is not installed
 # where this was written: unexecuted.
@@ -30,8 +32,8 @@ function NPBApps.BT.adi(iz, a2, a3, a4, a5, a6, a7, a8, a9, a10, a11, a12, a13,
 end
 
 function NPBApps.SP.adi(z, a2, a3, a4, a5, a6, a7, a8, a9, a10, u::DeviceZone, rhs::DeviceZone,
-                        a13, a14, a15, a16, a17, a18, a19, a20, a21, a22, a23, a24,
-                        forcing::DeviceZone, rest::Vararg{Any,74})
+                        a13, a14, a15, a16, a17, a18, a19, a20, a21, a22, a23, a24, a25,
+                        forcing::DeviceZone, rest::Vararg{Any,73})
     NPBAppsGPU.adi_locked!(u.p, u.zone)
     return nothing
 end

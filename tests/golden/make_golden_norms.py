@@ -47,7 +47,9 @@ def parse(path):
 
 
 def main():
-    root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden_norms.py <NPBApps.jl source tree>")
+    root = Path(sys.argv[1])
     data = {
         "source": "NPBApps.jl src/BT/verify.jl:136-348, src/SP/verify.jl:137-282, src/LU/verify.jl "
                   "(epsilon 1e-8, verify.jl:113)",

@@ -4,6 +4,7 @@ consumer compiles and links against both headers; the Julia ccalls and the
 Python ctypes declarations match the prototypes; the package never reaches
 the oracle and creates no handle without a device; and the host-side helpers
 (zone set-up, seeded coefficients, layouts) agree with the oracle."""
+import json
 import re
 from pathlib import Path
 
@@ -194,23 +195,48 @@ def test_julia_bindings_call_only_declared_entry_points():
         assert name in called, name
 
 
-def test_julia_shim_arities_match_the_reference_signatures():
-    """The shim's methods take the reference functions' positional arity:
-    BT adi 76, SP adi 99, exch_qbc 25 (BT/SP), LU ssor 41, LU exch_qbc 36
-    (src/BT/adi.jl:5-80, src/SP/adi.jl:6-104, src/BT/exchange_qbc.jl:1-26,
-    src/LU/ssor.jl:9-50, src/LU/exchange_qbc.jl:17)."""
-    text = (Path(__file__).resolve().parents[1] / "npbapps.jl_gb300" / "julia" / "NPBAppsGPUShim.jl").read_text()
-    want = {"NPBApps.BT.adi": 76, "NPBApps.SP.adi": 99, "$M.exch_qbc": 25, "NPBApps.LU.ssor": 41,
-            "NPBApps.LU.exch_qbc": 36}
-    for name, arity in want.items():
-        m = re.search(re.escape(name) + r"\((.*?)\)\n", text, re.S)
-        assert m, name
-        sig = m.group(1)
-        rest = [int(x) for x in re.findall(r"\w+::Vararg\{Any,\s*(\d+)\}", sig)]
-        sig = re.sub(r"\w+::Vararg\{Any,\s*\d+\}", "", sig)
-        args = [a.strip() for a in sig.split(",") if a.strip()]
-        n = len(args) + sum(rest)
-        assert n == arity, (name, n, arity)
+SHIM_METHODS = {"NPBApps.BT.adi": "BT.adi", "NPBApps.SP.adi": "SP.adi", "$M.exch_qbc": ("BT.exch_qbc", "SP.exch_qbc"),
+                "NPBApps.LU.ssor": "LU.ssor", "NPBApps.LU.exch_qbc": "LU.exch_qbc"}
+
+
+def shim_parameters(text, name):
+    """(name, type) of each positional parameter of the shim method `name`,
+    with a trailing Vararg{Any,N} expanded into N untyped entries."""
+    m = re.search(re.escape(name) + r"\((.*?)\)\n", text, re.S)
+    assert m, name
+    out = []
+    for a in (x.strip() for x in re.split(r",(?![^{]*\})", m.group(1))):
+        if not a:
+            continue
+        v = re.fullmatch(r"\w+::Vararg\{Any,\s*(\d+)\}", a)
+        if v:
+            out += [("", None)] * int(v.group(1))
+            continue
+        nm, _, ty = a.partition("::")
+        out.append((nm.strip(), ty.strip() or None))
+    return out
+
+
+def test_julia_shim_dispatches_at_the_reference_argument_positions():
+    """Every DeviceZone / LuDeviceZone-typed parameter of the shim sits at the
+    position where the reference function takes the array of that name, and
+    each method has the reference's arity.  The reference parameter lists come
+    from the committed fixture tests/golden/reference_signatures.json, which
+    tests/golden/make_reference_signatures.py extracts from the function
+    headers (src/BT/adi.jl:5, src/SP/adi.jl:6, src/BT/exchange_qbc.jl:1,
+    src/SP/exchange_qbc.jl:1, src/LU/ssor.jl:9, src/LU/exchange_qbc.jl:17)."""
+    root = Path(__file__).resolve().parents[1]
+    text = (root / "npbapps.jl_gb300" / "julia" / "NPBAppsGPUShim.jl").read_text()
+    ref = json.loads((root / "tests" / "golden" / "reference_signatures.json").read_text())
+    for name, keys in SHIM_METHODS.items():
+        params = shim_parameters(text, name)
+        typed = [(i, nm, ty) for i, (nm, ty) in enumerate(params) if ty and "DeviceZone" in ty]
+        assert typed, name
+        for key in (keys if isinstance(keys, tuple) else (keys,)):
+            want = ref[key]["params"]
+            assert len(params) == len(want), (name, len(params), key, len(want))
+            for i, nm, ty in typed:
+                assert want[i] == nm, f"{name}: {nm}::{ty} at position {i + 1}; {ref[key]['file']} has {want[i]}"
 
 
 def _zone_geometries(seed, count, square=False):
