@@ -82,6 +82,20 @@ PHASE_KERNELS = {
 }
 
 
+def workload_config(desc, pts, nzones, world, variant, seed=None, escale=None):
+    """The `config` object of both arms' JSON lines: the same keys and values
+    for the GPU arm and the reference arm, except `variant`."""
+    cfg = {"workload": desc, "points_per_gpu": pts, "zones": nzones, "variant": variant,
+           "l2": f"u, rhs and forcing {3 * 40 * pts / 1e9:.2f} GB > 129 MB L2; no flush",
+           "parallelism": f"replicas x{world}"}
+    if seed is not None:
+        cfg["seed"] = seed
+        cfg["energy_row_scale"] = 2 ** escale
+    else:
+        cfg["ce"] = "the reference's table"
+    return cfg
+
+
 def plural(n, noun):
     return f"{n} {noun}" + ("" if n == 1 else "s")
 
@@ -288,8 +302,7 @@ def run_reference(args):
             "impl": "reference", "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "points": pts, "zones": nzones,
-                       "variant": "reference CPU path (LU-MZ oracle port), FP64"},
+            "config": workload_config(desc, pts, nzones, world, "reference CPU path (LU-MZ oracle port), FP64"),
             "cpu_baseline": {"value": value, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
                              "sample": f"{plural(args.steps, 'SSOR iteration')} after "
                                        f"{plural(args.warmup, 'warm-up iteration')}"},
@@ -300,9 +313,11 @@ def run_reference(args):
     niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
     from oracle import oracle
 
+    # the oracle alone: zone set-up, seeded coefficients and the time steps
+    # (no product library is loaded in this arm)
     k = npbmz.KINDS[kind]
     nx, ny, nz, nbr = oracle.zone_setup(k, gx, gy, gz, xz, yz, ratio)
-    ce, _ = npbmz.seeded_coefficients(SEED, nx, ny, nz, gx, gy, gz, xz, yz)
+    ce, escale = oracle.seeded_coefficients(SEED, nx, ny, nz, gx, gy, gz, xz, yz)
     pts = int(np.sum(nx.astype(np.int64) * ny * nz))
     o = oracle.Oracle(k, nx, ny, nz, nbr, dt, gx, gy, gz, xz, yz, ce)
     o.step(args.warmup)
@@ -315,7 +330,7 @@ def run_reference(args):
         "impl": "reference", "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "points": pts, "zones": len(nx), "variant": "reference CPU path (oracle port), FP64"},
+        "config": workload_config(desc, pts, len(nx), world, "reference CPU path (oracle port), FP64", SEED, escale),
         "cpu_baseline": {"value": value, "unit": "Mgridpt-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{plural(args.steps, 'full time step')} after {plural(args.warmup, 'warm-up step')}"},
         "e2e": {"value": value, "unit": "Mgridpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -401,17 +416,18 @@ def run_gpu_lu(args, cls, desc):
             fp64_obj = {"achieved": fa, "peak": fp64, "unit": "GFLOP/s", "frac": fa / fp64, "flops_per_point": fl,
                         "pipe_active_ncu": km[kn]["fp64_pipe_active"],
                         "peak_source": "npbmz_fp64_peak: FP64 FMA chains on this GPU, measured in this run"}
-        extra["roofline"] = {"bound": "hbm", "kernel": kn, "phase": top, "achieved": achieved, "peak": hbm,
-                             "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+        hbm_obj = {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                   "bytes_per_point": LU_BYTES_PER_POINT[top],
+                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback 6800 GB/s"}
+        binding = "fp64" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6 else "hbm"
+        head = fp64_obj if binding == "fp64" else hbm_obj
+        extra["roofline"] = {"bound": binding, "kernel": kn, "phase": top, "achieved": head["achieved"],
+                             "peak": head["peak"], "unit": head["unit"], "frac": head["frac"], "traffic": traffic,
                              "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per point of this "
                                                 "workload's capture (profiles/ncu_kernel_metrics.json), times its points")
                              if traffic is not None else None,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
-                             "bytes_per_point": LU_BYTES_PER_POINT[top],
                              "points": f"{units} ({'interior' if units == interior else 'all'} points per launch)",
-                             "launch_ms": ph[top],
-                             "binding_ceiling": "fp64 pipe" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6 else None,
-                             "fp64": fp64_obj}
+                             "launch_ms": ph[top], "hbm": hbm_obj, "fp64": fp64_obj}
         extra["fp64_peak_gflops_measured"] = fp64
         var = {}
         for name, fl in (("fp64_batched", 0), ("fp64_batched_graph", lu.GRAPH),
@@ -453,11 +469,9 @@ def run_gpu_lu(args, cls, desc):
             "metric": "Mgridpt-steps/s", "value": value, "unit": "Mgridpt-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "points_per_gpu": pts, "zones": p.nzones,
-                       "variant": "fma-graph (not bit-exact)" if flags & lu.FMA else "fp64-graph (bit-exact)",
-                       "batched": True, "cuda_graph": True, "exch_planes": "reference (k = 1..nz-2)",
-                       "ce": "the reference's table", "l2": f"state {3 * 40 * pts / 1e9:.2f} GB > 129 MB L2; no flush",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(desc, pts, p.nzones, world,
+                                      "fma-graph (not bit-exact)" if flags & lu.FMA else "fp64-graph (bit-exact)"),
+            "variant_detail": {"batched": True, "cuda_graph": True, "exch_planes": "reference (k = 1..nz-2)"},
             "gpu_launches": p.launches_per_iteration() * args.steps,
             "clocks": clk.summary(),
         }
@@ -554,17 +568,35 @@ def run_gpu(args):
                              "issue_active_ncu": {k: km[k]["issue_active"] for k in knames},
                              "warps_per_sm_ncu": {k: km[k]["warps_per_sm"] for k in knames},
                              "peak_source": "4 warp instructions per SM cycle x SMs x median SM clock of the timed run"}
-        extra["roofline"] = {"bound": "hbm", "kernel": "+".join(knames) if knames else top, "phase": top,
-                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+        hbm_obj = {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                   "bytes_per_point": BYTES_PER_POINT[top],
+                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback 6800 GB/s"}
+        binding = ("fp64" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6
+                   else "issue" if issue_obj and issue_obj["frac"] > hbm_obj["frac"] else "hbm")
+        head = {"fp64": fp64_obj, "issue": issue_obj, "hbm": hbm_obj}[binding]
+        extra["roofline"] = {"bound": binding, "kernel": "+".join(knames) if knames else top, "phase": top,
+                             "achieved": head["achieved"], "peak": head["peak"], "unit": head["unit"],
+                             "frac": head["frac"], "launch_ms": ph[top], "points": pts,
                              "traffic": traffic,
                              "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum per point, {km_src} "
                                                 "capture (profiles/ncu_kernel_metrics.json), times this workload's points")
                              if traffic is not None else None,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback",
-                             "bytes_per_point": BYTES_PER_POINT[top], "launch_ms": ph[top],
-                             "binding_ceiling": ("fp64 pipe" if fp64_obj and fp64_obj["pipe_active_ncu"] > 0.6
-                                                 else "instruction issue" if issue_obj else None),
-                             "fp64": fp64_obj, "issue": issue_obj}
+                             "hbm": hbm_obj, "fp64": fp64_obj, "issue": issue_obj}
+        # the whole step against both ceilings: the 600 B/pt HBM model and the
+        # FP64 instructions of every kernel of the step (ncu, per point)
+        step_ms = ms_max / args.steps
+        step_obj = {"ms_per_step": step_ms, "points": pts, "bytes_per_point": 600.0,
+                    "hbm_achieved_gbs": 600.0 * pts / (step_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm}
+        step_obj["hbm_frac"] = step_obj["hbm_achieved_gbs"] / hbm
+        step_obj["hbm_floor_ms"] = 600.0 * pts / (hbm * 1e9) * 1e3
+        kall = [k for k in (km or {}) if not k.startswith("_")] if flags & npbmz.MIXED else []
+        if kall:
+            fl_step = sum(km[k]["fp64_flops_per_point"] for k in kall)
+            step_obj.update({"fp64_flops_per_point": fl_step, "fp64_peak_gflops": fp64,
+                             "fp64_floor_ms": fl_step * pts / (fp64 * 1e9) * 1e3,
+                             "fp64_kernels": sorted(kall)})
+            step_obj["fp64_floor_frac"] = step_obj["fp64_floor_ms"] / step_ms
+        extra["roofline_step"] = step_obj
         extra["phase_ms"] = ph
         extra["fp64_peak_gflops_measured"] = fp64
         # variants (fewer steps each)
@@ -625,14 +657,12 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if flags & npbmz.MIXED else "f64",
             "data": "synthetic",
-            "config": {"workload": desc, "points_per_gpu": pts, "zones": g.nzones, "variant": args.variant,
-                       "batched": True, "cuda_graph": bool(flags & npbmz.GRAPH),
-                       "line_solves": ("fp32 + double-float-residual refinement; primitives and compute_rhs "
-                                       + ("double-float" if flags & npbmz.RHS_DF else "fp64"))
-                       if flags & npbmz.MIXED else "fp64",
-                       "seed": SEED, "energy_row_scale": 2 ** escale, "autotuned": tuned,
-                       "l2": f"state {p.device_bytes / 1e9:.1f} GB >> 129 MB L2; no flush needed",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(desc, pts, g.nzones, world, args.variant, SEED, escale),
+            "variant_detail": {"batched": True, "cuda_graph": bool(flags & npbmz.GRAPH),
+                               "line_solves": ("fp32 + double-float-residual refinement; primitives and compute_rhs "
+                                               + ("double-float" if flags & npbmz.RHS_DF else "fp64"))
+                               if flags & npbmz.MIXED else "fp64",
+                               "autotuned": tuned, "device_bytes": p.device_bytes},
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }

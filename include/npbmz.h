@@ -246,7 +246,11 @@ int npbmz_describe(npbmz_t* h, char* buf, size_t n);
  * call allocates nothing.  Its first call on a device looks up the array's
  * device address; make that first call before any stream capture.  Calls
  * share the array: calls whose kernels may overlap on the GPU race and must
- * be serialised by the caller.  Errors: npbmz_last_error(NULL). */
+ * be serialised by the caller.  Non-finite dt, gx/gy/gz < 2 or zone counts
+ * < 1 are rejected before anything runs.  A CUDA error already pending on the
+ * calling thread is reported (-1) and left pending.  After cudaDeviceReset of
+ * a device, do not call it on that device again.  Errors:
+ * npbmz_last_error(NULL). */
 int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* params, const double* u, double* rhs,
                             void* stream);
 

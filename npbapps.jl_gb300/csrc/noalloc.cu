@@ -16,12 +16,20 @@
 // host threads) race on it and must be serialised by the caller.  Nothing in
 // it has to start at zero: the primitive kernel writes every plane element the
 // sweep reads, and the sweep writes each 5x5 block before reading it back.
+//
+// The device addresses of the arrays are looked up once per device, on the
+// first call made with that device current, under a lock (host threads may
+// make their first calls at the same time).  cudaDeviceReset unloads the
+// library's module on that device: a process that resets a device must not
+// call this entry point on it afterwards.
 #define NPBMZ_NS noalloc
 #define NPBMZ_HAS_FP32 0
 #include "step_kernels.cuh"
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "../../include/npbmz.h"
 
@@ -48,6 +56,7 @@ struct DeviceSymbols {
   npbmz::Work* work = nullptr;
 };
 DeviceSymbols g_symbols[NOALLOC_MAX_DEVICES];
+std::mutex g_symbols_lock;  // guards the first lookup on each device
 int noalloc_fail(const char* msg, cudaError_t e = cudaSuccess, int code = -1) {
   char buf[320];
   if (e != cudaSuccess) snprintf(buf, sizeof(buf), "npbmz_bt_xsolve_noalloc: %s: %s", msg, cudaGetErrorString(e));
@@ -82,6 +91,7 @@ int symbols_for_current_device(DeviceSymbols** out) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail("cudaGetDevice failed", e);
   if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return noalloc_fail("device index out of range");
+  std::lock_guard<std::mutex> guard(g_symbols_lock);
   DeviceSymbols& s = g_symbols[dev];
   if (!s.scratch) {
     void* p = nullptr;
@@ -131,6 +141,15 @@ extern "C" int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* par
                                        void* stream) {
   if (!params || !u || !rhs) return noalloc_fail("null argument");
   if (nx < 3 || ny < 3 || nz < 3) return noalloc_fail("zone sizes must be at least 3");
+  // the handle path's npbmz_create checks: the constants divide by gx-1, gy-1,
+  // gz-1 and the zone counts, and a non-finite dt would poison every value
+  if (!std::isfinite(params[0])) return noalloc_fail("params[0] (dt) must be finite");
+  for (int q = 1; q < 6; ++q)
+    if (!std::isfinite(params[q]) || params[q] != std::floor(params[q]) || params[q] > 1e9)
+      return noalloc_fail("params[1..5] (gx, gy, gz, x_zones, y_zones) must be whole numbers");
+  if (params[1] < 2 || params[2] < 2 || params[3] < 2)
+    return noalloc_fail("params[1..3] (gx, gy, gz) must be at least 2");
+  if (params[4] < 1 || params[5] < 1) return noalloc_fail("params[4..5] (x_zones, y_zones) must be at least 1");
   const int64_t np = (int64_t)nx * ny * nz;
   const int64_t lines = (int64_t)(ny - 2) * (nz - 2);
   const int64_t prim_doubles = ((int64_t)npbmz::PR_COUNT * np + 31) / 32 * 32;
@@ -144,6 +163,10 @@ extern "C" int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* par
   }
   const int nwork = (int)((lines + NOALLOC_TPB - 1) / NOALLOC_TPB);
   if (nwork > NOALLOC_MAX_WORK) return noalloc_fail("too many lines for one call");
+  // An error left pending by the caller's own earlier work is reported, not
+  // consumed: cudaPeekAtLastError leaves it for the caller to read.
+  const cudaError_t before = cudaPeekAtLastError();
+  if (before != cudaSuccess) return noalloc_fail("a CUDA error from earlier work is pending", before);
   DeviceSymbols* sym = nullptr;
   if (symbols_for_current_device(&sym)) return -1;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -163,6 +186,7 @@ extern "C" int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* par
   npbmz::noalloc::launch_prim(false, F, K, 0, np, s);
   npbmz::noalloc::launch_solve(false, 0, 0, F, K, sym->work, nwork, NOALLOC_TPB, sym->scratch + prim_doubles, lines, 0,
                                nullptr, s, false);
+  // nothing was pending before the three launches, so this is theirs
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail("kernel launch failed", e);
   return 0;

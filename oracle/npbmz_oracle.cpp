@@ -1235,6 +1235,73 @@ int oracle_zone_setup(int kind, int gx, int gy, int gz, int xz, int yz, double r
   return 0;
 }
 
+// Seeded manufactured-solution coefficients (the benchmark's initial data;
+// the reference itself uses the fixed ce table of src/BT/set_constants.jl:47-51
+// instead).  All 65 entries are drawn U(0.5, 2.0) from one SplitMix64 stream
+// (ce row-major [5][13], one draw each in order: the 53 high bits of the word
+// scaled to [0, 1)).  Then the energy row is doubled until, at every grid
+// coordinate (xi, eta, zeta) = (i dnxm1, j dnym1, k dnzm1) of the largest zone
+// extents, the exact solution, its six face values and their transfinite
+// interpolation (the initialize formula above) all have rho > 0, rho E > 0
+// and rho E - |rho v|^2 / (2 rho) >= rho E / 4.  Returns the number of
+// doublings e (0..39) or -2 when none passes; the caller's ce is written in
+// every case.
+int oracle_seeded_coefficients(uint64_t seed, int nzones, const int* nx, const int* ny, const int* nz, int gx, int gy,
+                               int gz, int xz, int yz, double* ce) {
+  if (!nx || !ny || !nz || !ce || nzones < 1) return -1;
+  uint64_t state = seed;
+  for (int e = 0; e < 65; ++e) {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t w = state;
+    w = (w ^ (w >> 30)) * 0xBF58476D1CE4E5B9ull;
+    w = (w ^ (w >> 27)) * 0x94D049BB133111EBull;
+    w ^= w >> 31;
+    ce[e] = 0.5 + 1.5 * ((double)(w >> 11) * 0x1.0p-53);
+  }
+  const Consts K = set_constants(1.0, gx, gy, gz, xz, yz);
+  int ex = 0, ey = 0, ez = 0;
+  for (int zi = 0; zi < nzones; ++zi) {
+    ex = std::max(ex, nx[zi]);
+    ey = std::max(ey, ny[zi]);
+    ez = std::max(ez, nz[zi]);
+  }
+  auto admissible = [](const double* q) {
+    if (!(q[0] > 0.0) || !(q[4] > 0.0)) return false;
+    const double kinetic = 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / q[0];
+    return q[4] - kinetic >= 0.25 * q[4];
+  };
+  for (int doublings = 0; doublings < 40; ++doublings) {
+    bool pass = true;
+    for (int k = 0; k < ez && pass; ++k) {
+      const double zeta = (double)k * K.dnzm1;
+      for (int j = 0; j < ey && pass; ++j) {
+        const double eta = (double)j * K.dnym1;
+        for (int i = 0; i < ex && pass; ++i) {
+          const double xi = (double)i * K.dnxm1;
+          double q[5], fx[2][5], fy[2][5], fz[2][5], blend[5];
+          exact_solution(xi, eta, zeta, ce, q);
+          for (int s = 0; s < 2; ++s) {
+            exact_solution((double)s, eta, zeta, ce, fx[s]);
+            exact_solution(xi, (double)s, zeta, ce, fy[s]);
+            exact_solution(xi, eta, (double)s, ce, fz[s]);
+          }
+          for (int m = 0; m < 5; ++m) {
+            const double a = xi * fx[1][m] + (1.0 - xi) * fx[0][m];
+            const double b = eta * fy[1][m] + (1.0 - eta) * fy[0][m];
+            const double c = zeta * fz[1][m] + (1.0 - zeta) * fz[0][m];
+            blend[m] = a + b + c - a * b - a * c - b * c + a * b * c;
+          }
+          pass = admissible(q) && admissible(blend);
+          for (int s = 0; s < 2 && pass; ++s) pass = admissible(fx[s]) && admissible(fy[s]) && admissible(fz[s]);
+        }
+      }
+    }
+    if (pass) return doublings;
+    for (int n = 0; n < 13; ++n) ce[4 * 13 + n] *= 2.0;
+  }
+  return -2;
+}
+
 // Create a problem: constants, initialize, exact_rhs (the reference's warm-up
 // step is omitted: the reference re-initialises u after it, and rhs/lhs are
 // rewritten before they are read, so it changes no value).

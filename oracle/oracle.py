@@ -96,6 +96,7 @@ def lib():
         L.oracle_phase.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp]
         L.oracle_set.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp]
+        L.oracle_seeded_coefficients.argtypes = [ctypes.c_uint64, ctypes.c_int, ip, ip, ip] + [ctypes.c_int] * 5 + [dp]
         _lib = L
     return _lib
 
@@ -114,6 +115,17 @@ def zone_setup(kind, gx, gy, gz, xz, yz, ratio):
     nbr = np.zeros(4 * n, np.int32)
     lib().oracle_zone_setup(kind, gx, gy, gz, xz, yz, ratio, _ip(nx), _ip(ny), _ip(nz), _ip(nbr))
     return nx, ny, nz, nbr
+
+
+def seeded_coefficients(seed, nx, ny, nz, gx, gy, gz, xz, yz):
+    """Seeded 5x13 manufactured-solution coefficients with the energy-row
+    positivity rule (oracle_seeded_coefficients); returns (ce, doublings)."""
+    nx, ny, nz = (np.ascontiguousarray(a, np.int32) for a in (nx, ny, nz))
+    ce = np.zeros((5, 13))
+    e = lib().oracle_seeded_coefficients(seed, len(nx), _ip(nx), _ip(ny), _ip(nz), gx, gy, gz, xz, yz, _dp(ce))
+    if e < 0:
+        raise ValueError("no positivity-preserving energy scale found")
+    return ce, e
 
 
 class Oracle:

@@ -141,6 +141,40 @@ def test_seeded_coefficients_positivity_rule(npbmz_mod, seed):
     np.testing.assert_array_equal(ce, ce2)
 
 
+@pytest.mark.parametrize("kind,cls,seed", [("BT", "C", 20261203), ("SP", "C", 20261203), ("BT", "B", 3),
+                                           ("SP", "A", 3), ("BT", "S", 0), ("BT", "W", 99)])
+def test_seeded_coefficients_match_the_oracle(npbmz_mod, oracle_mod, kind, cls, seed):
+    """The library's seeded coefficients (host code of libnpbmz_gpu.so) and
+    the oracle's own restatement (which the bench's reference arm uses, so
+    that arm loads no product library) give the same ce and energy scale."""
+    niter, dt, ratio, xz, yz, gx, gy, gz = npbmz.CLASSES[kind][cls]
+    nx, ny, nz, nbr = oracle_mod.zone_setup(npbmz.KINDS[kind], gx, gy, gz, xz, yz, ratio)
+    a, ea = npbmz.seeded_coefficients(seed, nx, ny, nz, gx, gy, gz, xz, yz)
+    b, eb = oracle_mod.seeded_coefficients(seed, nx, ny, nz, gx, gy, gz, xz, yz)
+    assert ea == eb
+    np.testing.assert_array_equal(a, b)
+    if (cls, seed) == ("C", 20261203):
+        assert ea == 2  # the benchmark's energy-row scale 2^2
+
+
+@pytest.mark.parametrize("params,text", [
+    ([float("nan"), 24, 24, 6, 2, 2], b"dt"), ([float("inf"), 24, 24, 6, 2, 2], b"dt"),
+    ([0.01, 1, 24, 6, 2, 2], b"at least 2"), ([0.01, 24, 24, 1, 2, 2], b"at least 2"),
+    ([0.01, 24, 24, 6, 0, 2], b"zone"), ([0.01, 24, 24, 6, 2, 2.5], b"whole")])
+def test_noalloc_rejects_bad_parameters_before_any_cuda_call(npbmz_mod, params, text):
+    """npbmz_bt_xsolve_noalloc checks dt and the grid constants as
+    npbmz_create does, before it touches the GPU (so this runs without one)."""
+    import ctypes
+
+    L = npbmz.lib()
+    a = np.array(params, np.float64)
+    buf = np.zeros(8)
+    rc = L.npbmz_bt_xsolve_noalloc(8, 10, 6, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   ctypes.c_void_p(buf.ctypes.data), ctypes.c_void_p(buf.ctypes.data), None)
+    assert rc == -1
+    assert text in L.npbmz_last_error(None)
+
+
 def test_ref_layout_sizes():
     # BT u carries the 2-deep halo on i, j, k; SP pads i, j to odd extents
     assert npbmz.ref_elems(npbmz.BT, npbmz.U, 8, 10, 6) == 5 * 13 * 15 * 11
