@@ -149,15 +149,24 @@ int npbmz_adi(npbmz_t* h, int zone);
  * loop (src/BT/bt-node.jl:280-395).  norms (nullable, host) receives 10
  * doubles per step: xcr[5] (sum over zones of rhs_norm/dt of that step's
  * compute_rhs) then xce[5] (sum over zones of error_norm after the step).
- * Synchronous when norms != NULL. */
+ * Synchronous.  State check: the primitive kernel of every step checks the
+ * state entering that step, and one kernel checks the state the call leaves;
+ * when some point has a density rho or a pressure-like quantity
+ * rho E - |rho v|^2 / (2 rho) that is not positive and finite, the call
+ * returns NPBMZ_ERR_STATE after its steps, and npbmz_last_error names the
+ * failed quantity and the first such point (zone, i, j, k).  The reference
+ * has no such check: a diverging run continues until its final norms
+ * (src/BT/verify.jl). */
+#define NPBMZ_ERR_STATE (-3)
 int npbmz_step(npbmz_t* h, int nsteps, double* norms);
 
 /* nsteps steps, then u of every zone to `host` (layout as npbmz_download,
  * zone = -1): the same result as npbmz_step followed by npbmz_download.  For
  * NPBMZ_GRAPH handles with zone-group branches and a page-locked `host`, each
  * group's zones are copied out as soon as the last step's z sweep has written
- * them, while the other groups still compute.  Synchronous.  No counterpart
- * in the reference (whose u lives in host memory). */
+ * them, while the other groups still compute.  Synchronous.  The state check
+ * of npbmz_step applies (NPBMZ_ERR_STATE; u is copied out all the same).  No
+ * counterpart in the reference (whose u lives in host memory). */
 int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host);
 
 /* The node part of verify (src/BT/verify.jl:411-505): error_norm of u, then

@@ -301,6 +301,20 @@ __global__ void __launch_bounds__(256) k_convert(Fields F, double* __restrict__ 
   }
 }
 
+// ---------------------------------------------------------------------------
+// State check of u over the point work list (one thread per zone point): the
+// health word of Fields (see health_check) for the state a call leaves.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_state_check(Fields F, const Work* __restrict__ work) {
+  const Work w = work[blockIdx.x];
+  const ZoneDev Z = F.zones[w.zone];
+  const int q = w.first + threadIdx.x;
+  if (q >= Z.nx * Z.ny * Z.nz) return;
+  const int64_t p = Z.off + q, NP = F.NP;
+  const double rho = F.u[p], m1 = F.u[NP + p], m2 = F.u[2 * NP + p], m3 = F.u[3 * NP + p], e = F.u[4 * NP + p];
+  health_check(F, p, rho, e - 0.5 * (m1 * m1 + m2 * m2 + m3 * m3) / rho);
+}
+
 __global__ void k_fill(double* __restrict__ a, int64_t n, double v) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) a[t] = v;
 }
@@ -345,6 +359,10 @@ void launch_convert(const Fields& F, double* planes, double* stage, const int64_
   if (gx > 512) gx = 512;
   dim3 grid(gx, nzn);
   k_convert<<<grid, 256, 0, s>>>(F, planes, stage, soff, sub, zone_lo, kind, field, layout, dir, zlist);
+}
+
+void launch_state_check(const Fields& F, const Work* work, int nwork, cudaStream_t s) {
+  if (nwork > 0 && F.health) k_state_check<<<nwork, 128, 0, s>>>(F, work);
 }
 
 void launch_fill(double* a, int64_t n, double v, cudaStream_t s) {

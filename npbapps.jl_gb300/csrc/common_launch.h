@@ -19,5 +19,6 @@ void launch_convert(const Fields& F, double* planes, double* stage, const int64_
                     int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s,
                     const int* zlist = nullptr);
 void launch_fill(double* a, int64_t n, double v, cudaStream_t s);
+void launch_state_check(const Fields& F, const Work* work, int nwork, cudaStream_t s);
 int probe_fp64(double* gflops);
 }  // namespace npbmz

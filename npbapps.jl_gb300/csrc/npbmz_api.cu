@@ -282,6 +282,9 @@ struct npbmz_handle {
   cudaEvent_t fence[2] = {nullptr, nullptr};
   int launches_per_step = 0;
   int64_t device_bytes = 0;
+  // state check: the device word of Fields::health and its page-locked copy
+  unsigned long long* health_d = nullptr;
+  unsigned long long* health_h = nullptr;
   std::string err;
 };
 
@@ -339,6 +342,8 @@ Fields fields(const npbmz_t* h) {
   F.xd = h->xd;
   F.fd = h->fd;
   F.fdt = h->fdt;
+  F.health = h->health_d;
+  F.nzones = h->nzones;
   return F;
 }
 
@@ -799,6 +804,40 @@ int replay_graph(npbmz_t* h, int nsteps) {
   CK(h, cudaEventRecord(h->fence[1], h->aux_stream));
   CK(h, cudaStreamWaitEvent(nullptr, h->fence[1], 0));
   return 0;
+}
+
+// ---- state check (the health word) ----------------------------------------
+// Every step's primitive kernel checks the state entering that step; at the
+// end of a call k_state_check checks the state the call leaves.  The word is
+// cleared when a call starts and read once when it ends.
+int health_begin(npbmz_t* h) {
+  CK(h, cudaMemsetAsync(h->health_d, 0, sizeof(unsigned long long), h->stream));
+  CK(h, cudaMemsetAsync(h->health_d + 1, 0xFF, sizeof(unsigned long long), h->stream));
+  return 0;
+}
+
+// Enqueue the final check and the read-back (the caller synchronises).
+int health_read(npbmz_t* h) {
+  launch_state_check(fields(h), h->wpts_d, h->nwpts, h->stream);
+  CKL(h);
+  CK(h, cudaMemcpyAsync(h->health_h, h->health_d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  return 0;
+}
+
+// After the stream is synchronised: NPBMZ_ERR_STATE with the first bad point.
+int health_verdict(npbmz_t* h, const char* what) {
+  const unsigned long long bits = h->health_h[0], p = h->health_h[1];
+  if (!bits) return 0;
+  int z = 0;
+  while (z + 1 < h->nzones && (unsigned long long)h->zh[z + 1].off <= p) ++z;
+  const ZoneDev& d = h->zh[z];
+  const int64_t q = (int64_t)p - d.off;
+  fail(h, "%s: state check failed: %s%s%s in u; first bad point zone %d (i, j, k) = (%d, %d, %d)", what,
+       (bits & HEALTH_DENSITY) ? "non-positive or non-finite density" : "",
+       (bits & HEALTH_DENSITY) && (bits & HEALTH_PRESSURE) ? " and " : "",
+       (bits & HEALTH_PRESSURE) ? "non-positive or non-finite pressure (rho E - |rho v|^2 / (2 rho))" : "", z,
+       (int)(q % d.nx), (int)((q / d.nx) % d.ny), (int)(q / ((int64_t)d.nx * d.ny)));
+  return NPBMZ_ERR_STATE;
 }
 
 // Kernel launches of one npbmz_step step: exch_qbc, then per batch (all
@@ -1317,6 +1356,8 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
 
   int rc = 0;
   rc |= dalloc(h, &h->zones_d, nzones);
+  rc |= dalloc(h, &h->health_d, 2);
+  if (!rc && cudaMallocHost((void**)&h->health_h, 2 * sizeof(unsigned long long)) != cudaSuccess) rc = -1;
   rc |= dalloc(h, &h->nbr_d, 4 * (size_t)nzones);
   rc |= dalloc(h, &h->u, 5 * (size_t)h->NP);
   rc |= dalloc(h, &h->rhs, 5 * (size_t)h->NP);
@@ -1451,29 +1492,28 @@ int npbmz_adi(npbmz_t* h, int zone) {
 int npbmz_step(npbmz_t* h, int nsteps, double* norms) {
   if (!h) return fail(nullptr, "null handle");
   if (nsteps < 0) return fail(h, "nsteps < 0");
-  if (norms) {
-    if (nsteps > h->norms_cap) {
-      if (h->norms_d) { cudaFree(h->norms_d); h->device_bytes -= (int64_t)h->norms_cap * 10 * sizeof(double); }
-      h->norms_d = nullptr;
-      h->norms_cap = 0;
-      if (dalloc(h, &h->norms_d, 10 * (size_t)std::max(nsteps, 1))) return -1;
-      h->norms_cap = std::max(nsteps, 1);
-    }
-    for (int s = 0; s < nsteps; ++s)
-      if (one_step(h, true, h->norms_d + 10 * s)) return -1;
-    CK(h, cudaMemcpyAsync(norms, h->norms_d, 10 * sizeof(double) * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    return 0;
+  if (norms && nsteps > h->norms_cap) {
+    if (h->norms_d) { cudaFree(h->norms_d); h->device_bytes -= (int64_t)h->norms_cap * 10 * sizeof(double); }
+    h->norms_d = nullptr;
+    h->norms_cap = 0;
+    if (dalloc(h, &h->norms_d, 10 * (size_t)std::max(nsteps, 1))) return -1;
+    h->norms_cap = std::max(nsteps, 1);
   }
-  if (h->flags & NPBMZ_GRAPH) {
+  if (h->flags & NPBMZ_GRAPH && !norms) {
     if (!h->graph_exec || h->graph_stream != h->stream)
       if (capture_step_graph(h)) return -1;
     if (flush_boundary(h)) return -1;
-    return replay_graph(h, nsteps);
+    if (health_begin(h) || replay_graph(h, nsteps)) return -1;
+  } else {
+    if (health_begin(h)) return -1;
+    for (int s = 0; s < nsteps; ++s)
+      if (one_step(h, norms != nullptr, norms ? h->norms_d + 10 * s : nullptr)) return -1;
+    if (norms)
+      CK(h, cudaMemcpyAsync(norms, h->norms_d, 10 * sizeof(double) * nsteps, cudaMemcpyDeviceToHost, h->stream));
   }
-  for (int s = 0; s < nsteps; ++s)
-    if (one_step(h, false, nullptr)) return -1;
-  return 0;
+  if (health_read(h)) return -1;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return health_verdict(h, "npbmz_step");
 }
 
 int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
@@ -1493,6 +1533,7 @@ int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
   if (!h->graph_exec || h->graph_stream != h->stream)
     if (capture_step_graph(h)) return -1;
   if (flush_boundary(h)) return -1;
+  if (health_begin(h)) return -1;
   if (nsteps > 1 && replay_graph(h, nsteps - 1)) return -1;
   CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
   if (!h->io_stream) CK(h, cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
@@ -1506,9 +1547,10 @@ int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
     CKL(h);
   }
   CK(h, cudaEventRecord(h->io_done, h->io_stream));
+  if (health_read(h)) return -1;
   CK(h, cudaStreamWaitEvent(h->stream, h->io_done, 0));
   CK(h, cudaStreamSynchronize(h->stream));
-  return 0;
+  return health_verdict(h, "npbmz_step_download");
 }
 
 int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms) {
@@ -1826,6 +1868,8 @@ int npbmz_destroy(npbmz_t* h) {
   if (h->io_stream) { cudaStreamSynchronize(h->io_stream); cudaStreamDestroy(h->io_stream); }
   if (h->io_done) cudaEventDestroy(h->io_done);
   if (h->grp_zones_d) cudaFree(h->grp_zones_d);
+  if (h->health_d) cudaFree(h->health_d);
+  if (h->health_h) cudaFreeHost(h->health_h);
   for (cudaEvent_t e : h->fence)
     if (e) cudaEventDestroy(e);
   delete h;

@@ -133,7 +133,52 @@ struct Fields {
   bool prim64 = true;
   // compute_rhs writes rhs in FP64 as well as its double-float copy
   bool rhs64 = true;
+  // state check (null: off): word 0 ORs the HEALTH_* bits of every point
+  // found bad, word 1 keeps the smallest such global point index (all ones
+  // while none); nzones bounds the zone table for the padding test below
+  unsigned long long* health = nullptr;
+  int nzones = 0;
 };
+
+// ---- state check ------------------------------------------------------------
+// A point of u is healthy when its density rho and its pressure-like quantity
+// rho E - |rho v|^2 / (2 rho) are both positive and finite.
+constexpr unsigned HEALTH_DENSITY = 1u;
+constexpr unsigned HEALTH_PRESSURE = 2u;
+
+// v > 0 and finite, on the bit pattern (integer pipe): the positive finite
+// doubles are exactly the patterns 1 .. 0x7FEFFFFFFFFFFFFF; zero, negatives,
+// infinities and NaNs all fall outside.
+__device__ __forceinline__ bool positive_finite(double v) {
+  return (unsigned long long)__double_as_longlong(v) - 1ull < 0x7FEFFFFFFFFFFFFFull;
+}
+
+// Record a bad point p (global index) unless it lies in the padding between
+// zones (kernels over the padded plane visit those too).  Taken only when a
+// point fails, so the zone search costs nothing in a healthy run.
+static __device__ __noinline__ void health_report(const Fields& F, int64_t p, unsigned bits) {
+  int lo = 0, hi = F.nzones - 1;
+  while (lo < hi) {  // last zone whose first point is <= p
+    const int mid = (lo + hi + 1) / 2;
+    if (F.zones[mid].off <= p) lo = mid;
+    else hi = mid - 1;
+  }
+  const ZoneDev z = F.zones[lo];
+  if (p < z.off || p >= z.off + (int64_t)z.nx * z.ny * z.nz) return;
+  atomicOr(F.health, (unsigned long long)bits);
+  atomicMin(F.health + 1, (unsigned long long)p);
+}
+
+__device__ __forceinline__ bool positive_finite(float v) { return (unsigned)__float_as_uint(v) - 1u < 0x7F7FFFFFu; }
+
+// rho and pressure in FP64, or (the double-float kernels) as the high words
+// of their double-float values
+template <typename R>
+__device__ __forceinline__ void health_check(const Fields& F, int64_t p, R rho, R pressure) {
+  if (!F.health) return;
+  const unsigned bits = (positive_finite(rho) ? 0u : HEALTH_DENSITY) | (positive_finite(pressure) ? 0u : HEALTH_PRESSURE);
+  if (bits) health_report(F, p, bits);
+}
 
 // x line through interior point (j, k) of zone z (-1 when j or k is a face).
 __host__ __device__ inline int64_t xline_of(const ZoneDev& z, int j, int k) {

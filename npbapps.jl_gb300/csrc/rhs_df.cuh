@@ -100,6 +100,7 @@ __device__ __forceinline__ void prim_df_point(const Fields& F, const RhsDfConsts
   const df64 us = df_mul(u[1], ri), vs = df_mul(u[2], ri), ws = df_mul(u[3], ri);
   const df64 square = df_half(df_add(df_add(df_mul(u[1], us), df_mul(u[2], vs)), df_mul(u[3], ws)));
   const df64 qs = df_mul(square, ri);
+  health_check(F, p, u[0].hi, df_sub(u[4], square).hi);
   {
     float2* X = F.xd;
     const df64 c1 = f2df(C.c1), c2 = f2df(C.c2);

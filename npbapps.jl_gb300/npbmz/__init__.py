@@ -94,8 +94,15 @@ CE_REFERENCE = np.array([
 ])
 
 
+ERR_STATE = -3  # NPBMZ_ERR_STATE: the state check found a bad density or pressure
+
+
 class NpbmzError(RuntimeError):
-    pass
+    """A failed call: the library's message; `code` is its status."""
+
+    def __init__(self, msg, code=-1):
+        super().__init__(msg)
+        self.code = code
 
 
 _lib = None
@@ -262,7 +269,7 @@ class Problem:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise NpbmzError(f"{what}: " + lib().npbmz_last_error(self._h).decode())
+            raise NpbmzError(f"{what}: " + lib().npbmz_last_error(self._h).decode(), rc)
 
     # -- reference operations ---------------------------------------------------
     def setup(self, ce=None):
