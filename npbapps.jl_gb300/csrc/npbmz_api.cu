@@ -343,7 +343,6 @@ Fields fields(const npbmz_t* h) {
   F.fd = h->fd;
   F.fdt = h->fdt;
   F.health = h->health_d;
-  F.nzones = h->nzones;
   return F;
 }
 
@@ -832,7 +831,7 @@ int health_verdict(npbmz_t* h, const char* what) {
   while (z + 1 < h->nzones && (unsigned long long)h->zh[z + 1].off <= p) ++z;
   const ZoneDev& d = h->zh[z];
   const int64_t q = (int64_t)p - d.off;
-  fail(h, "%s: state check failed: %s%s%s in u; first bad point zone %d (i, j, k) = (%d, %d, %d)", what,
+  fail(h, "state check failed after %s: %s%s%s in u; first bad point zone %d (i, j, k) = (%d, %d, %d)", what,
        (bits & HEALTH_DENSITY) ? "non-positive or non-finite density" : "",
        (bits & HEALTH_DENSITY) && (bits & HEALTH_PRESSURE) ? " and " : "",
        (bits & HEALTH_PRESSURE) ? "non-positive or non-finite pressure (rho E - |rho v|^2 / (2 rho))" : "", z,
@@ -1513,7 +1512,7 @@ int npbmz_step(npbmz_t* h, int nsteps, double* norms) {
   }
   if (health_read(h)) return -1;
   CK(h, cudaStreamSynchronize(h->stream));
-  return health_verdict(h, "npbmz_step");
+  return health_verdict(h, "the steps");
 }
 
 int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
@@ -1550,7 +1549,7 @@ int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
   if (health_read(h)) return -1;
   CK(h, cudaStreamWaitEvent(h->stream, h->io_done, 0));
   CK(h, cudaStreamSynchronize(h->stream));
-  return health_verdict(h, "npbmz_step_download");
+  return health_verdict(h, "the steps");
 }
 
 int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms) {

@@ -135,9 +135,8 @@ struct Fields {
   bool rhs64 = true;
   // state check (null: off): word 0 ORs the HEALTH_* bits of every point
   // found bad, word 1 keeps the smallest such global point index (all ones
-  // while none); nzones bounds the zone table for the padding test below
+  // while none)
   unsigned long long* health = nullptr;
-  int nzones = 0;
 };
 
 // ---- state check ------------------------------------------------------------
@@ -153,18 +152,10 @@ __device__ __forceinline__ bool positive_finite(double v) {
   return (unsigned long long)__double_as_longlong(v) - 1ull < 0x7FEFFFFFFFFFFFFFull;
 }
 
-// Record a bad point p (global index) unless it lies in the padding between
-// zones (kernels over the padded plane visit those too).  Taken only when a
-// point fails, so the zone search costs nothing in a healthy run.
-static __device__ __noinline__ void health_report(const Fields& F, int64_t p, unsigned bits) {
-  int lo = 0, hi = F.nzones - 1;
-  while (lo < hi) {  // last zone whose first point is <= p
-    const int mid = (lo + hi + 1) / 2;
-    if (F.zones[mid].off <= p) lo = mid;
-    else hi = mid - 1;
-  }
-  const ZoneDev z = F.zones[lo];
-  if (p < z.off || p >= z.off + (int64_t)z.nx * z.ny * z.nz) return;
+// Record a bad point p (global index).  The padding points between zones
+// hold u = (1, 0, 0, 0, 1) from creation on (nothing writes them later), so
+// kernels over the padded plane find nothing there.
+__device__ __forceinline__ void health_report(const Fields& F, int64_t p, unsigned bits) {
   atomicOr(F.health, (unsigned long long)bits);
   atomicMin(F.health + 1, (unsigned long long)p);
 }
@@ -177,7 +168,7 @@ template <typename R>
 __device__ __forceinline__ void health_check(const Fields& F, int64_t p, R rho, R pressure) {
   if (!F.health) return;
   const unsigned bits = (positive_finite(rho) ? 0u : HEALTH_DENSITY) | (positive_finite(pressure) ? 0u : HEALTH_PRESSURE);
-  if (bits) health_report(F, p, bits);
+  if (__builtin_expect(bits != 0u, 0)) health_report(F, p, bits);
 }
 
 // x line through interior point (j, k) of zone z (-1 when j or k is a face).

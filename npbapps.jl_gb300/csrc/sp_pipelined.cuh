@@ -317,7 +317,7 @@ __device__ __forceinline__ void sp_mixed_pl_item(const Fields& F, const Consts& 
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(128, 3) k_sp_mixed_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
+__global__ void __launch_bounds__(128, NPBMZ_SP_MINB) k_sp_mixed_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
                                                      float* __restrict__ scr, int64_t nlt, float* __restrict__ x0) {
   extern __shared__ __align__(16) unsigned char pl_smem[];
   for (int it = blockIdx.x; it < nwork; it += gridDim.x) sp_mixed_pl_item<DIR>(F, K, work[it], scr, nlt, x0, pl_smem);
@@ -603,7 +603,7 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
 }
 
 template <int DIR, bool OUT_DF>
-__global__ void __launch_bounds__(128, 3) k_sp_refine_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
+__global__ void __launch_bounds__(128, NPBMZ_SP_MINB) k_sp_refine_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
                                                       float* __restrict__ scr, int64_t nlt, int add_u,
                                                       float* __restrict__ x0f) {
   extern __shared__ __align__(16) unsigned char pl_smem[];

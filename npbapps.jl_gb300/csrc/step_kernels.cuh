@@ -1471,7 +1471,23 @@ __global__ void __launch_bounds__(128) k_bt_refine_df(Fields F, Consts K, const 
 // The arithmetic is that of k_bt_mixed_solve<DIR, true> and
 // k_bt_refine_df<DIR, true, OUT_DF>.
 // ============================================================================
-constexpr int PIPE = 4;
+#ifndef NPBMZ_PIPE
+#define NPBMZ_PIPE 4
+#endif
+constexpr int PIPE = NPBMZ_PIPE;
+
+// Minimum resident CTAs of 128 threads per SM that the pipelined sweep
+// kernels are compiled for (__launch_bounds__): it caps their registers at
+// 65536 / (128 * n) and so sets their occupancy.
+#ifndef NPBMZ_BT_MIXED_MINB
+#define NPBMZ_BT_MIXED_MINB 1
+#endif
+#ifndef NPBMZ_BT_REFINE_MINB
+#define NPBMZ_BT_REFINE_MINB 1
+#endif
+#ifndef NPBMZ_SP_MINB
+#define NPBMZ_SP_MINB 3
+#endif
 
 __device__ __forceinline__ void cpa4(float* dst, const void* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -1596,7 +1612,7 @@ __device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& 
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(128) k_bt_mixed_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
+__global__ void __launch_bounds__(128, NPBMZ_BT_MIXED_MINB) k_bt_mixed_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
                                                      float* __restrict__ scr, int64_t nlt, float* __restrict__ x0) {
   extern __shared__ __align__(16) unsigned char pl_smem[];
   for (int it = blockIdx.x; it < nwork; it += gridDim.x) bt_mixed_pl_item<DIR>(F, K, work[it], scr, nlt, x0, pl_smem);
@@ -1799,7 +1815,7 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
 }
 
 template <int DIR, bool OUT_DF>
-__global__ void __launch_bounds__(128) k_bt_refine_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
+__global__ void __launch_bounds__(128, NPBMZ_BT_REFINE_MINB) k_bt_refine_pl(Fields F, Consts K, const Work* __restrict__ work, int nwork,
                                                       float* __restrict__ scr, int64_t nlt, int add_u,
                                                       const float* __restrict__ x0f) {
   extern __shared__ __align__(16) unsigned char pl_smem[];

@@ -44,7 +44,8 @@ def test_healthy_run_reports_nothing(kind, variant):
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("variant", list(VARIANTS))
-@pytest.mark.parametrize("what,m,value", [("pressure", 4, -1.0), ("density", 0, -0.5), ("density", 2, float("nan"))])
+@pytest.mark.parametrize("what,m,value", [("pressure", 4, -1.0), ("density", 0, -0.5), ("pressure", 2, float("nan")),
+                                          ("density", 0, float("inf"))])
 def test_planted_bad_point_is_reported(kind, variant, what, m, value):
     p = problem(kind, VARIANTS[variant])
     zone, ijk = 2, (3, 4, 2)
