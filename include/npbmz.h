@@ -140,6 +140,43 @@ int npbmz_download_async(npbmz_t* h, int zone, int field, int layout, double* ho
  * (src/BT/exchange_qbc.jl:1-122, src/SP/exchange_qbc.jl:1-122). */
 int npbmz_exch_qbc(npbmz_t* h);
 
+/* ---- zones of one problem spread over several ranks (one GPU each) ----
+ * A rank creates its handle with only its own zones (npbmz_create, zones
+ * renumbered 0..n-1) and marks each face whose neighbour zone lives on
+ * another rank with NPBMZ_REMOTE in nbr.  npbmz_exch_qbc and npbmz_step then
+ * copy only the faces between the rank's own zones; the others travel
+ * through caller-owned device buffers, once per step, before the step:
+ *     npbmz_pack_faces(h, send) -> the caller moves send to the peers'
+ *     recv (NCCL send/recv, a peer copy) -> npbmz_unpack_faces(h, recv).
+ * This is the inter-process part of exch_qbc: exch_qbc_send / exch_qbc_recv
+ * (src/BT/exchange_qbc.jl:145-465, src/SP/exchange_qbc.jl:145-465), with the
+ * zone-to-rank map of map_zones (src/BT/setup_mpi.jl:123-433) computed on the
+ * host (npbmz/shard.py). */
+#define NPBMZ_REMOTE (-1)
+
+/* Register the faces this rank sends and receives: send[2f], send[2f+1] =
+ * (zone, side) of face f, side 0..3 = west, east, south, north; recv likewise
+ * (each must be an NPBMZ_REMOTE face).  A sent face (z, s) is the interior
+ * plane the neighbour on side s reads (west i = 1, east i = nx-2, south
+ * j = 1, north j = ny-2); a received face (z, s) is z's ghost plane on side s
+ * (west i = 0, east i = nx-1, south j = 0, north j = ny-1).  Each face holds
+ * 5 (n-2)(nz-2) doubles (n = ny for west/east, nx for south/north) in the
+ * reference's packing order -- variable, then k = 1..nz-2, then the
+ * transverse index 1..n-2 (src/BT/exchange_qbc.jl:201-210) -- and the faces
+ * follow one another in list order.  Returns the doubles of the send and the
+ * receive buffer.  Synchronous.  No counterpart in the reference (which posts
+ * one MPI message per face). */
+int npbmz_face_plan(npbmz_t* h, int nsend, const int* send, int nrecv, const int* recv, int64_t* send_count,
+                    int64_t* recv_count);
+
+/* Pack the registered send faces of u into the device buffer send_buf
+ * (exch_qbc_send's packing, src/BT/exchange_qbc.jl:145-320). */
+int npbmz_pack_faces(npbmz_t* h, double* send_buf);
+
+/* Write the registered receive faces of the device buffer recv_buf into u's
+ * ghost planes (exch_qbc_recv's unpacking, src/BT/exchange_qbc.jl:323-465). */
+int npbmz_unpack_faces(npbmz_t* h, const double* recv_buf);
+
 /* adi: one ADI step (compute_rhs, x/y/z solves, add) for one zone, or for all
  * zones (zone = -1, batched).  Replaces adi (src/BT/adi.jl:5-251,
  * src/SP/adi.jl:6-258). */

@@ -178,8 +178,10 @@ __global__ void __launch_bounds__(128) k_exact_rhs(Fields F, Consts K, Coeffs ce
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_exch_qbc(Fields F, const int* __restrict__ nbr, int zone_lo) {
   const int z = zone_lo + blockIdx.y / 4, face = blockIdx.y % 4;
+  const int src_zone = nbr[4 * z + face];
+  if (src_zone < 0) return;  // a face of a zone on another rank: npbmz_unpack_faces fills it
   const ZoneDev Z = F.zones[z];
-  const ZoneDev S = F.zones[nbr[4 * z + face]];
+  const ZoneDev S = F.zones[src_zone];
   const int nt = face < 2 ? Z.ny - 2 : Z.nx - 2;  // transverse length
   const int count = 5 * nt * (Z.nz - 2);
   const int64_t NP = F.NP;
@@ -200,6 +202,42 @@ __global__ void __launch_bounds__(256) k_exch_qbc(Fields F, const int* __restric
       src = S.off + ((int64_t)k * S.ny + 1) * S.nx + (1 + a);
     }
     F.u[m * NP + dst] = F.u[m * NP + src];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Faces exchanged with zones on other ranks (the inter-process part of
+// exch_qbc, src/BT/exchange_qbc.jl:145-465).  Face f of the list is (zone,
+// side); its 5 (n-2)(nz-2) values sit at buf[off..] in the reference's packing
+// order: variable m outermost, then k = 1..nz-2, then the transverse index
+// (j for west/east, i for south/north) = 1..n-2.
+//   pack (side s): the interior plane the neighbour on side s reads --
+//     west i = 1, east i = nx-2, south j = 1, north j = ny-2;
+//   unpack (side s): the ghost plane on side s --
+//     west i = 0, east i = nx-1, south j = 0, north j = ny-1.
+// blockIdx.y = face.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t face_point(const ZoneDev& Z, int side, bool ghost, int a, int k) {
+  const int i_w = ghost ? 0 : 1, i_e = ghost ? Z.nx - 1 : Z.nx - 2;
+  const int j_s = ghost ? 0 : 1, j_n = ghost ? Z.ny - 1 : Z.ny - 2;
+  if (side == 0) return Z.off + ((int64_t)k * Z.ny + (1 + a)) * Z.nx + i_w;
+  if (side == 1) return Z.off + ((int64_t)k * Z.ny + (1 + a)) * Z.nx + i_e;
+  if (side == 2) return Z.off + ((int64_t)k * Z.ny + j_s) * Z.nx + (1 + a);
+  return Z.off + ((int64_t)k * Z.ny + j_n) * Z.nx + (1 + a);
+}
+
+template <bool PACK>
+__global__ void __launch_bounds__(256) k_faces(Fields F, const FaceDesc* __restrict__ faces, double* __restrict__ buf) {
+  const FaceDesc f = faces[blockIdx.y];
+  const ZoneDev Z = F.zones[f.zone];
+  const int nt = f.side < 2 ? Z.ny - 2 : Z.nx - 2;
+  const int count = 5 * nt * (Z.nz - 2);
+  const int64_t NP = F.NP;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+    const int a = t % nt, k = 1 + (t / nt) % (Z.nz - 2), m = t / (nt * (Z.nz - 2));
+    const int64_t p = m * NP + face_point(Z, f.side, !PACK, a, k);
+    if (PACK) buf[f.off + t] = F.u[p];
+    else F.u[p] = buf[f.off + t];
   }
 }
 
@@ -359,6 +397,17 @@ void launch_convert(const Fields& F, double* planes, double* stage, const int64_
   if (gx > 512) gx = 512;
   dim3 grid(gx, nzn);
   k_convert<<<grid, 256, 0, s>>>(F, planes, stage, soff, sub, zone_lo, kind, field, layout, dir, zlist);
+}
+
+void launch_faces(bool pack, const Fields& F, const FaceDesc* faces, int nfaces, int max_face, double* buf,
+                  cudaStream_t s) {
+  if (nfaces <= 0) return;
+  int gx = (max_face + 255) / 256;
+  if (gx < 1) gx = 1;
+  if (gx > 64) gx = 64;
+  dim3 grid(gx, nfaces);
+  if (pack) k_faces<true><<<grid, 256, 0, s>>>(F, faces, buf);
+  else k_faces<false><<<grid, 256, 0, s>>>(F, faces, buf);
 }
 
 void launch_state_check(const Fields& F, const Work* work, int nwork, cudaStream_t s) {

@@ -20,5 +20,8 @@ void launch_convert(const Fields& F, double* planes, double* stage, const int64_
                     const int* zlist = nullptr);
 void launch_fill(double* a, int64_t n, double v, cudaStream_t s);
 void launch_state_check(const Fields& F, const Work* work, int nwork, cudaStream_t s);
+// pack (true) or unpack the listed faces to / from the device buffer buf
+void launch_faces(bool pack, const Fields& F, const FaceDesc* faces, int nfaces, int max_face, double* buf,
+                  cudaStream_t s);
 int probe_fp64(double* gflops);
 }  // namespace npbmz

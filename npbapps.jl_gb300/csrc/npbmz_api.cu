@@ -282,6 +282,12 @@ struct npbmz_handle {
   cudaEvent_t fence[2] = {nullptr, nullptr};
   int launches_per_step = 0;
   int64_t device_bytes = 0;
+  // faces exchanged with other ranks (npbmz_face_plan): packed and unpacked
+  // through caller-owned device buffers
+  bool has_remote = false;
+  FaceDesc* send_faces_d = nullptr;
+  FaceDesc* recv_faces_d = nullptr;
+  int nsend = 0, nrecv = 0;
   // state check: the device word of Fields::health and its page-locked copy
   unsigned long long* health_d = nullptr;
   unsigned long long* health_h = nullptr;
@@ -667,7 +673,9 @@ int phase_add(npbmz_t* h, int zone) {
 }
 
 int phase_exch(npbmz_t* h) {
-  if (h->nzones < 2) return 0;  // the reference skips exch_qbc for one zone (bt-node.jl:286)
+  // the reference skips exch_qbc for a one-zone problem (bt-node.jl:286); a
+  // rank's one zone of a larger problem still copies the faces it owns
+  if (h->nzones < 2 && !h->has_remote) return 0;
   launch_exch_qbc(fields(h), h->nbr_d, 0, h->nzones, h->max_face, h->stream);
   CKL(h);
   return 0;
@@ -1307,20 +1315,23 @@ int npbmz_create(int kind, int nzones, const int* nx, const int* ny, const int* 
     if (nx[z] < 3 || ny[z] < 3 || nz[z] < 3) return fail(nullptr, "zone %d: size %dx%dx%d, minimum is 3", z, nx[z], ny[z], nz[z]);
     if ((int64_t)nx[z] * ny[z] * nz[z] > (1 << 30)) return fail(nullptr, "zone %d too large", z);
     for (int f = 0; f < 4; ++f)
-      if (nbr[4 * z + f] < 0 || nbr[4 * z + f] >= nzones) return fail(nullptr, "zone %d: bad neighbour", z);
+      if (nbr[4 * z + f] < NPBMZ_REMOTE || nbr[4 * z + f] >= nzones) return fail(nullptr, "zone %d: bad neighbour", z);
   }
-  for (int z = 0; z < nzones; ++z) {
-    const int w = nbr[4 * z], e = nbr[4 * z + 1], s = nbr[4 * z + 2], n = nbr[4 * z + 3];
-    if (ny[w] != ny[z] || nz[w] != nz[z] || ny[e] != ny[z] || nz[e] != nz[z] || nx[s] != nx[z] || nz[s] != nz[z] ||
-        nx[n] != nx[z] || nz[n] != nz[z])
-      return fail(nullptr, "zone %d: neighbour face sizes do not match", z);
-  }
+  bool remote = false;
+  for (int z = 0; z < nzones; ++z)
+    for (int f = 0; f < 4; ++f) {
+      const int o = nbr[4 * z + f];
+      if (o == NPBMZ_REMOTE) { remote = true; continue; }  // its size is the exchange plan's business
+      const bool ok = f < 2 ? (ny[o] == ny[z] && nz[o] == nz[z]) : (nx[o] == nx[z] && nz[o] == nz[z]);
+      if (!ok) return fail(nullptr, "zone %d: neighbour face sizes do not match", z);
+    }
   npbmz_t* h = new npbmz_t();
   h->kind = kind;
   h->nzones = nzones;
   h->flags = variant_flags;
   h->K = make_consts(params[0], (int)params[1], (int)params[2], (int)params[3], (int)params[4], (int)params[5]);
   h->nbr.assign(nbr, nbr + 4 * nzones);
+  h->has_remote = remote;
   h->zh.resize(nzones);
   int64_t off = 0, lines[3] = {0, 0, 0};
   int64_t scratch_elems = 0;
@@ -1614,6 +1625,7 @@ int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_
   if (!h) return fail(nullptr, "null handle");
   if (nsteps < 1 || checkpoint_every < 1) return fail(h, "nsteps and checkpoint_every must be >= 1");
   if (!u_target) return fail(h, "u_target is null");
+  if (h->has_remote) return fail(h, "the adjoint needs every zone of the problem on this handle (no NPBMZ_REMOTE faces)");
   h->err.clear();
   CK(h, cudaStreamSynchronize(h->stream));
   return adjoint_run(h, nsteps, checkpoint_every, u_target, J, grad_forcing, grad_u0);
@@ -1843,6 +1855,62 @@ int npbmz_describe(npbmz_t* h, char* buf, size_t n) {
 
 const char* npbmz_last_error(npbmz_t* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
+int npbmz_face_plan(npbmz_t* h, int nsend, const int* send, int nrecv, const int* recv, int64_t* send_count,
+                    int64_t* recv_count) {
+  if (!h) return fail(nullptr, "null handle");
+  if (nsend < 0 || nrecv < 0 || (nsend && !send) || (nrecv && !recv) || !send_count || !recv_count)
+    return fail(h, "bad face lists");
+  auto build = [&](int n, const int* list, bool incoming, std::vector<FaceDesc>& out, int64_t& total) -> int {
+    total = 0;
+    for (int f = 0; f < n; ++f) {
+      const int z = list[2 * f], side = list[2 * f + 1];
+      if (z < 0 || z >= h->nzones || side < 0 || side > 3) return fail(h, "face %d: bad zone %d or side %d", f, z, side);
+      // a received face must be one the handle was told is remote
+      if (incoming && h->nbr[4 * z + side] != NPBMZ_REMOTE)
+        return fail(h, "face %d: zone %d side %d is not an NPBMZ_REMOTE face", f, z, side);
+      const ZoneDev& d = h->zh[z];
+      out.push_back({z, side, total});
+      total += 5 * (int64_t)((side < 2 ? d.ny : d.nx) - 2) * (d.nz - 2);
+    }
+    return 0;
+  };
+  std::vector<FaceDesc> sf, rf;
+  int64_t ns = 0, nr = 0;
+  if (build(nsend, send, false, sf, ns) || build(nrecv, recv, true, rf, nr)) return -1;
+  if (h->send_faces_d) { cudaFree(h->send_faces_d); h->send_faces_d = nullptr; }
+  if (h->recv_faces_d) { cudaFree(h->recv_faces_d); h->recv_faces_d = nullptr; }
+  h->nsend = h->nrecv = 0;
+  if (nsend) {
+    CK(h, cudaMalloc((void**)&h->send_faces_d, sf.size() * sizeof(FaceDesc)));
+    CK(h, cudaMemcpy(h->send_faces_d, sf.data(), sf.size() * sizeof(FaceDesc), cudaMemcpyHostToDevice));
+  }
+  if (nrecv) {
+    CK(h, cudaMalloc((void**)&h->recv_faces_d, rf.size() * sizeof(FaceDesc)));
+    CK(h, cudaMemcpy(h->recv_faces_d, rf.data(), rf.size() * sizeof(FaceDesc), cudaMemcpyHostToDevice));
+  }
+  h->nsend = nsend;
+  h->nrecv = nrecv;
+  *send_count = ns;
+  *recv_count = nr;
+  return 0;
+}
+
+int npbmz_pack_faces(npbmz_t* h, double* send_buf) {
+  if (!h) return fail(nullptr, "null handle");
+  if (h->nsend && !send_buf) return fail(h, "null send buffer");
+  launch_faces(true, fields(h), h->send_faces_d, h->nsend, h->max_face, send_buf, h->stream);
+  CKL(h);
+  return 0;
+}
+
+int npbmz_unpack_faces(npbmz_t* h, const double* recv_buf) {
+  if (!h) return fail(nullptr, "null handle");
+  if (h->nrecv && !recv_buf) return fail(h, "null receive buffer");
+  launch_faces(false, fields(h), h->recv_faces_d, h->nrecv, h->max_face, const_cast<double*>(recv_buf), h->stream);
+  CKL(h);
+  return 0;
+}
+
 int npbmz_destroy(npbmz_t* h) {
   if (!h) return 0;
   if (h->stream) cudaStreamSynchronize(h->stream);
@@ -1868,6 +1936,8 @@ int npbmz_destroy(npbmz_t* h) {
   if (h->io_done) cudaEventDestroy(h->io_done);
   if (h->grp_zones_d) cudaFree(h->grp_zones_d);
   if (h->health_d) cudaFree(h->health_d);
+  if (h->send_faces_d) cudaFree(h->send_faces_d);
+  if (h->recv_faces_d) cudaFree(h->recv_faces_d);
   if (h->health_h) cudaFreeHost(h->health_h);
   for (cudaEvent_t e : h->fence)
     if (e) cudaEventDestroy(e);

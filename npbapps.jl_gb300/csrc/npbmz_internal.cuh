@@ -55,6 +55,13 @@ struct ZoneDev {
   int64_t lineoff[3];   // first global line index of the zone, per sweep direction
 };
 
+// One face exchanged with another rank: (zone, side 0..3 = west, east, south,
+// north) and the offset of its values in the exchange buffer.
+struct FaceDesc {
+  int zone, side;
+  int64_t off;
+};
+
 // One work item = one CTA's share: `first` is the first point (point lists)
 // or the first line (line lists) of zone `zone` that the CTA handles.
 struct Work {

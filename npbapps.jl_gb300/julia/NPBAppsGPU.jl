@@ -87,6 +87,32 @@ exch_qbc!(p::Problem) = check(p, ccall((:npbmz_exch_qbc, libnpbmz), Cint, (Ptr{C
 adi!(p::Problem, iz::Integer = 0) =
     check(p, ccall((:npbmz_adi, libnpbmz), Cint, (Ptr{Cvoid}, Cint), p.handle, iz - 1), "npbmz_adi")
 
+"""Faces exchanged with zones of other MPI ranks (exch_qbc_send / exch_qbc_recv,
+src/BT/exchange_qbc.jl:145-465): `send` and `recv` are vectors of (zone,
+side) pairs, 1-based zones of this handle and sides 0..3 = west, east,
+south, north, each received side marked NPBMZ_REMOTE (-1) in the nbr table
+the handle was created with.  Returns the Float64 counts of the send and
+receive buffers."""
+function face_plan!(p::Problem, send::AbstractVector, recv::AbstractVector)
+    flat(v) = Cint[x for (z, s) in v for x in (z - 1, s)]
+    s = flat(send); r = flat(recv)
+    ns = Ref{Int64}(0); nr = Ref{Int64}(0)
+    check(p, ccall((:npbmz_face_plan, libnpbmz), Cint,
+                   (Ptr{Cvoid}, Cint, Ptr{Cint}, Cint, Ptr{Cint}, Ref{Int64}, Ref{Int64}),
+                   p.handle, length(send), s, length(recv), r, ns, nr), "npbmz_face_plan")
+    return ns[], nr[]
+end
+
+"""Pack the registered send faces into a device buffer (CuPtr or raw address)."""
+pack_faces!(p::Problem, send_buf) =
+    check(p, ccall((:npbmz_pack_faces, libnpbmz), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.handle, send_buf),
+          "npbmz_pack_faces")
+
+"""Unpack the registered receive faces from a device buffer into u's ghost planes."""
+unpack_faces!(p::Problem, recv_buf) =
+    check(p, ccall((:npbmz_unpack_faces, libnpbmz), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.handle, recv_buf),
+          "npbmz_unpack_faces")
+
 """niter steps of exch_qbc + adi; returns the per-step (xcr, xce) norms when norms = true."""
 function step!(p::Problem, niter::Integer; norms = false)
     if norms

@@ -44,8 +44,9 @@ EXPORTS = [
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
     "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
-    "npbmz_step_download",
+    "npbmz_step_download", "npbmz_face_plan", "npbmz_pack_faces", "npbmz_unpack_faces",
 ]
+REMOTE = -1  # NPBMZ_REMOTE: a face whose neighbour zone lives on another rank
 PROF_PHASES = ("exch", "prim", "rhs", "x", "y", "z")
 
 # Problem classes (src/BT/classes.jl:15-24, src/SP/classes.jl:16-25):
@@ -153,6 +154,10 @@ def lib(build_if_missing: bool = True):
     L.npbmz_adjoint.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp]
     L.npbmz_step_profile.argtypes = [vp, ctypes.c_int, dp]
     L.npbmz_set_step_groups.argtypes = [vp, ctypes.c_int]
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    L.npbmz_face_plan.argtypes = [vp, ctypes.c_int, ip, ctypes.c_int, ip, i64p, i64p]
+    L.npbmz_pack_faces.argtypes = [vp, vp]
+    L.npbmz_unpack_faces.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -319,6 +324,22 @@ class Problem:
     def set_step_groups(self, groups: int):
         """Zone groups of the step graph (pipelined branches), 1..8."""
         self._check(lib().npbmz_set_step_groups(self._h, groups), "npbmz_set_step_groups")
+
+    def face_plan(self, send, recv):
+        """Register the (zone, side) faces sent to and received from other
+        ranks; returns the doubles of the send and receive buffers."""
+        s = np.ascontiguousarray(np.asarray(send, np.int32).reshape(-1))
+        r = np.ascontiguousarray(np.asarray(recv, np.int32).reshape(-1))
+        ns, nr = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(lib().npbmz_face_plan(self._h, len(s) // 2, _ip(s), len(r) // 2, _ip(r), ctypes.byref(ns),
+                                          ctypes.byref(nr)), "npbmz_face_plan")
+        return ns.value, nr.value
+
+    def pack_faces(self, send_ptr: int):
+        self._check(lib().npbmz_pack_faces(self._h, ctypes.c_void_p(send_ptr)), "npbmz_pack_faces")
+
+    def unpack_faces(self, recv_ptr: int):
+        self._check(lib().npbmz_unpack_faces(self._h, ctypes.c_void_p(recv_ptr)), "npbmz_unpack_faces")
 
     def autotune(self):
         self._check(lib().npbmz_autotune(self._h), "npbmz_autotune")

@@ -386,7 +386,7 @@ def _compatible(c_type, jl_type):
         if jl_type == "Ptr{Cvoid}":
             return True
         want = {"double": ("Ptr{Cdouble}", "Ref{Cdouble}"), "int": ("Ptr{Cint}", "Ref{Cint}"),
-                "char": ("Cstring", "Ptr{UInt8}")}.get(base, ())
+                "int64_t": ("Ptr{Int64}", "Ref{Int64}"), "char": ("Cstring", "Ptr{UInt8}")}.get(base, ())
         return jl_type in want
     return _JULIA_SCALAR.get(jl_type) == c_type
 
@@ -419,7 +419,7 @@ def _ctypes_compatible(c_type, ct):
         if ct is ctypes.c_void_p:
             return True
         want = {"double": ctypes.POINTER(ctypes.c_double), "int": ctypes.POINTER(ctypes.c_int),
-                "char": ctypes.c_char_p}.get(base)
+                "int64_t": ctypes.POINTER(ctypes.c_int64), "char": ctypes.c_char_p}.get(base)
         return ct is want
     return ct is {"int": ctypes.c_int, "double": ctypes.c_double, "uint64_t": ctypes.c_uint64,
                   "size_t": ctypes.c_size_t, "int64_t": ctypes.c_int64}[c_type]
