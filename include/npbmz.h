@@ -187,15 +187,27 @@ int npbmz_adi(npbmz_t* h, int zone);
  * doubles per step: xcr[5] (sum over zones of rhs_norm/dt of that step's
  * compute_rhs) then xce[5] (sum over zones of error_norm after the step).
  * Synchronous.  State check: the primitive kernel of every step checks the
- * state entering that step, and one kernel checks the state the call leaves;
- * when some point has a density rho or a pressure-like quantity
- * rho E - |rho v|^2 / (2 rho) that is not positive and finite, the call
- * returns NPBMZ_ERR_STATE after its steps, and npbmz_last_error names the
- * failed quantity and the first such point (zone, i, j, k).  The reference
- * has no such check: a diverging run continues until its final norms
- * (src/BT/verify.jl). */
+ * state entering that step, and one kernel checks the state the call leaves
+ * (npbmz_state_check returns what they found).  When some point has a density
+ * rho that is not positive and finite, or a non-finite value, the call
+ * returns NPBMZ_ERR_STATE after its steps and npbmz_last_error names the
+ * failure and the first such point (zone, i, j, k); for SP also when the
+ * pressure-like quantity rho E - |rho v|^2 / (2 rho) is not positive, whose
+ * square root SP takes (src/SP/rhs.jl:84-88).  BT never takes that root and
+ * the reference carries such a state on, so for BT a non-positive pressure is
+ * only reported by npbmz_state_check.  The reference has no such check: a
+ * diverging run continues until its final norms (src/BT/verify.jl). */
 #define NPBMZ_ERR_STATE (-3)
 int npbmz_step(npbmz_t* h, int nsteps, double* norms);
+
+/* What the state check of the last npbmz_step / npbmz_step_download found:
+ * bits = NPBMZ_STATE_* (0 when every point was healthy), and the first bad
+ * point's zone and (i, j, k) (all -1 when none).  zone, i, j, k nullable.  No
+ * counterpart in the reference. */
+#define NPBMZ_STATE_DENSITY 1   /* rho not positive and finite */
+#define NPBMZ_STATE_PRESSURE 2  /* rho E - |rho v|^2 / (2 rho) finite, not positive */
+#define NPBMZ_STATE_NONFINITE 4 /* a NaN or an infinity in u */
+int npbmz_state_check(npbmz_t* h, int* bits, int* zone, int* i, int* j, int* k);
 
 /* nsteps steps, then u of every zone to `host` (layout as npbmz_download,
  * zone = -1): the same result as npbmz_step followed by npbmz_download.  For
@@ -238,6 +250,15 @@ int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_
  * at least 8 zones (not NPBMZ_EXACT or NPBMZ_PERZONE).  No counterpart in the
  * reference. */
 int npbmz_set_step_groups(npbmz_t* h, int groups);
+
+/* Zone-group branches of the step graph: fp64_first != 0 issues every group's
+ * primitive kernel and compute_rhs (FP64-pipe bound) on one stream of the
+ * device's greatest priority, in group order, so that their CTAs reach the
+ * SMs ahead of the queued CTAs of the sweeps (FP32 pipe) they overlap;
+ * instantiated with per-node priorities.  Launch order only: results are
+ * unchanged.  npbmz_autotune chooses it with the group count.  No counterpart
+ * in the reference. */
+int npbmz_set_step_priority(npbmz_t* h, int fp64_first);
 
 /* Use `stream` (a cudaStream_t, NULL = the legacy default stream) for all
  * later work of the handle. */

@@ -255,6 +255,11 @@ struct npbmz_handle {
   std::vector<Range> grp_pts, grp_int, grp_line[3];
   int cur_group = -1;              // >= 0 while the phases of one group are issued
   cudaStream_t grp_stream[8] = {};
+  // the zone groups' primitive kernels and compute_rhs (FP64 pipe) on one
+  // stream of the device's greatest priority, so that their CTAs go to SMs
+  // ahead of the waiting CTAs of the sweeps (FP32 pipe) they run beside
+  bool fp64_prio = false;
+  cudaStream_t prio_stream = nullptr;
   cudaEvent_t grp_ev[2 * 8 + 1] = {};
   // npbmz_step_download: the graph records grp_out_ev[g] (an external event)
   // when group g's z sweep has written its zones' u; io_stream then copies
@@ -291,6 +296,8 @@ struct npbmz_handle {
   // state check: the device word of Fields::health and its page-locked copy
   unsigned long long* health_d = nullptr;
   unsigned long long* health_h = nullptr;
+  unsigned health_bits = 0;   // of the last npbmz_step / npbmz_step_download
+  int64_t health_point = -1;
   std::string err;
 };
 
@@ -739,13 +746,18 @@ int grouped_step(npbmz_t* h, cudaStream_t cs) {
   int rc = 0;
   for (int g = 0; g < G && !rc; ++g) {
     cudaStream_t S = h->grp_stream[g];
-    rc |= cudaStreamWaitEvent(S, start, 0) != cudaSuccess;
-    if (g > 0) rc |= cudaStreamWaitEvent(S, h->grp_ev[2 * (g - 1)], 0) != cudaSuccess;
-    h->stream = S;
+    // prim + compute_rhs of group g: on the priority stream (in group order),
+    // or on the group's own stream after group g-1's compute_rhs
+    cudaStream_t P = h->fp64_prio ? h->prio_stream : S;
+    rc |= cudaStreamWaitEvent(P, start, 0) != cudaSuccess;
+    if (g > 0 && P == S) rc |= cudaStreamWaitEvent(S, h->grp_ev[2 * (g - 1)], 0) != cudaSuccess;
+    h->stream = P;
     h->cur_group = g;
     if (!rc) rc = phase_prim(h, -1, true);
     if (!rc) rc = phase_rhs(h, -1, sp, false, true);
-    if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g], S) != cudaSuccess;
+    if (!rc) rc = cudaEventRecord(h->grp_ev[2 * g], P) != cudaSuccess;
+    if (!rc && P != S) rc = cudaStreamWaitEvent(S, h->grp_ev[2 * g], 0) != cudaSuccess;
+    h->stream = S;
     for (int dir = 0; dir < 3 && !rc; ++dir) rc = phase_solve(h, dir, -1, dir == 2 ? 1 : 0, true);
     // group g's u is final: an event that work outside the graph can wait on
     if (!rc) rc = cudaEventRecordWithFlags(h->grp_out_ev[g], S, cudaEventRecordExternal) != cudaSuccess;
@@ -771,6 +783,11 @@ int capture_step_graph(npbmz_t* h) {
       if (!h->grp_ev[e]) CK(h, cudaEventCreateWithFlags(&h->grp_ev[e], cudaEventDisableTiming));
     for (int g = 0; g < h->ngroups; ++g)
       if (!h->grp_out_ev[g]) CK(h, cudaEventCreateWithFlags(&h->grp_out_ev[g], cudaEventDisableTiming));
+    if (h->fp64_prio && !h->prio_stream) {
+      int least = 0, greatest = 0;
+      CK(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      CK(h, cudaStreamCreateWithPriority(&h->prio_stream, cudaStreamNonBlocking, greatest));
+    }
   }
   if (flush_boundary(h)) return -1;  // keep the one-off reset out of the graph
   // Capture is not allowed on the legacy default stream: capture and replay
@@ -793,7 +810,9 @@ int capture_step_graph(npbmz_t* h) {
   h->stream = saved;
   if (rc) { if (g) cudaGraphDestroy(g); return -1; }
   if (e != cudaSuccess) return fail(h, "stream capture failed: %s", cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&h->graph_exec, g, 0);
+  // kernel nodes keep the priority of the stream they were captured from
+  e = cudaGraphInstantiate(&h->graph_exec, g,
+                           use_groups(h) && h->fp64_prio ? cudaGraphInstantiateFlagUseNodePriority : 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(h, "graph instantiate failed: %s", cudaGetErrorString(e));
   h->graph_stream = h->stream;
@@ -831,19 +850,28 @@ int health_read(npbmz_t* h) {
   return 0;
 }
 
-// After the stream is synchronised: NPBMZ_ERR_STATE with the first bad point.
+// After the stream is synchronised: NPBMZ_ERR_STATE with the first bad point
+// when the state has a non-positive or non-finite density or a non-finite
+// value, and for SP also a non-positive pressure (SP takes its square root,
+// src/SP/rhs.jl:84-88; BT never does, and the reference carries such a state
+// on: npbmz_state_check reports it).
 int health_verdict(npbmz_t* h, const char* what) {
   const unsigned long long bits = h->health_h[0], p = h->health_h[1];
-  if (!bits) return 0;
+  h->health_bits = (unsigned)bits;
+  h->health_point = bits ? (int64_t)p : -1;
+  const unsigned fatal = HEALTH_DENSITY | HEALTH_NONFINITE | (h->kind == NPBMZ_SP ? HEALTH_PRESSURE : 0u);
+  if (!(bits & fatal)) return 0;
   int z = 0;
   while (z + 1 < h->nzones && (unsigned long long)h->zh[z + 1].off <= p) ++z;
   const ZoneDev& d = h->zh[z];
   const int64_t q = (int64_t)p - d.off;
-  fail(h, "state check failed after %s: %s%s%s in u; first bad point zone %d (i, j, k) = (%d, %d, %d)", what,
-       (bits & HEALTH_DENSITY) ? "non-positive or non-finite density" : "",
-       (bits & HEALTH_DENSITY) && (bits & HEALTH_PRESSURE) ? " and " : "",
-       (bits & HEALTH_PRESSURE) ? "non-positive or non-finite pressure (rho E - |rho v|^2 / (2 rho))" : "", z,
-       (int)(q % d.nx), (int)((q / d.nx) % d.ny), (int)(q / ((int64_t)d.nx * d.ny)));
+  std::string kinds;
+  if (bits & HEALTH_DENSITY) kinds += "non-positive or non-finite density";
+  if (bits & HEALTH_NONFINITE) kinds += std::string(kinds.empty() ? "" : " and ") + "a non-finite value";
+  if (bits & HEALTH_PRESSURE)
+    kinds += std::string(kinds.empty() ? "" : " and ") + "non-positive pressure (rho E - |rho v|^2 / (2 rho))";
+  fail(h, "state check failed after %s: %s in u; first bad point zone %d (i, j, k) = (%d, %d, %d)", what,
+       kinds.c_str(), z, (int)(q % d.nx), (int)((q / d.nx) % d.ny), (int)(q / ((int64_t)d.nx * d.ny)));
   return NPBMZ_ERR_STATE;
 }
 
@@ -1537,8 +1565,13 @@ int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
                       attr.devicePointer != nullptr;
   cudaGetLastError();
   if (!mapped || !(h->flags & NPBMZ_GRAPH) || !use_groups(h) || h->stream == nullptr) {
-    if (npbmz_step(h, nsteps, nullptr)) return -1;
-    return transfer(h, -1, NPBMZ_U, layout, host, 1, true);
+    // a failed state check still copies u out (and keeps its message)
+    const int rc = npbmz_step(h, nsteps, nullptr);
+    if (rc && rc != NPBMZ_ERR_STATE) return rc;
+    const std::string msg = h->err;
+    if (transfer(h, -1, NPBMZ_U, layout, host, 1, true)) return -1;
+    if (rc) h->err = msg;
+    return rc;
   }
   if (!h->graph_exec || h->graph_stream != h->stream)
     if (capture_step_graph(h)) return -1;
@@ -1679,6 +1712,35 @@ int npbmz_set_step_groups(npbmz_t* h, int groups) {
   return 0;
 }
 
+int npbmz_state_check(npbmz_t* h, int* bits, int* zone, int* i, int* j, int* k) {
+  if (!h || !bits) return fail(h, "null argument");
+  *bits = (int)h->health_bits;
+  int z = -1, ii = -1, jj = -1, kk = -1;
+  if (h->health_bits) {
+    const int64_t p = h->health_point;
+    z = 0;
+    while (z + 1 < h->nzones && h->zh[z + 1].off <= p) ++z;
+    const ZoneDev& d = h->zh[z];
+    const int64_t q = p - d.off;
+    ii = (int)(q % d.nx);
+    jj = (int)((q / d.nx) % d.ny);
+    kk = (int)(q / ((int64_t)d.nx * d.ny));
+  }
+  if (zone) *zone = z;
+  if (i) *i = ii;
+  if (j) *j = jj;
+  if (k) *k = kk;
+  return 0;
+}
+
+int npbmz_set_step_priority(npbmz_t* h, int fp64_first) {
+  if (!h) return fail(nullptr, "null handle");
+  CK(h, cudaStreamSynchronize(h->stream));
+  drop_graph(h);
+  h->fp64_prio = fp64_first != 0;
+  return 0;
+}
+
 int npbmz_set_stream(npbmz_t* h, void* stream) {
   if (!h) return fail(nullptr, "null handle");
   if (h->own_stream && h->stream) {
@@ -1796,15 +1858,20 @@ int npbmz_autotune(npbmz_t* h) {
     }
   }
   if (!rc && (h->flags & NPBMZ_GRAPH) && !(h->flags & (NPBMZ_EXACT | NPBMZ_PERZONE)) && h->nzones >= 8) {
-    const int gcand[] = {1, 2, 4, 6};
+    // zone-group branches, each count with and without the priority stream
+    const int gcand[] = {1, 2, 3, 4, 6, 8};
     float best = 1e30f;
     int best_g = h->ngroups;
-    for (int G : gcand) {
-      if (G > h->nzones || npbmz_set_step_groups(h, G)) continue;
-      const float ms = step_ms();
-      if (ms < 0.f) { rc = -1; break; }
-      if (ms < best) { best = ms; best_g = G; }
-    }
+    bool best_p = h->fp64_prio;
+    for (int G : gcand)
+      for (int prio = 0; prio < (G > 1 ? 2 : 1) && !rc; ++prio) {
+        if (G > h->nzones || npbmz_set_step_groups(h, G)) continue;
+        h->fp64_prio = prio != 0;
+        const float ms = step_ms();
+        if (ms < 0.f) { rc = -1; break; }
+        if (ms < best) { best = ms; best_g = G; best_p = prio != 0; }
+      }
+    h->fp64_prio = best_p;
     if (!rc) rc = npbmz_set_step_groups(h, best_g);
   }
   if (!rc && !(h->flags & (NPBMZ_EXACT | NPBMZ_PERZONE))) {
@@ -1846,10 +1913,11 @@ int npbmz_describe(npbmz_t* h, char* buf, size_t n) {
   }
   tp += "]";
   snprintf(buf, n, "{\"kind\":\"%s\",\"zones\":%d,\"points\":%lld,\"flags\":%d,\"lines_per_cta\":%s,"
-           "\"zone_size_buckets\":%d,\"step_groups\":%d,\"persistent\":%s,\"launches_per_step\":%d,"
-           "\"device_bytes\":%lld}",
+           "\"zone_size_buckets\":%d,\"step_groups\":%d,\"fp64_priority\":%s,\"persistent\":%s,"
+           "\"launches_per_step\":%d,\"device_bytes\":%lld}",
            h->kind == NPBMZ_BT ? "BT" : "SP", h->nzones, (long long)h->NP, h->flags, tp.c_str(), h->nbkt, h->ngroups,
-           (h->flags & NPBMZ_PERSIST) ? "true" : "false", h->launches_per_step, (long long)h->device_bytes);
+           h->fp64_prio ? "true" : "false", (h->flags & NPBMZ_PERSIST) ? "true" : "false", h->launches_per_step,
+           (long long)h->device_bytes);
   return 0;
 }
 
@@ -1928,6 +1996,7 @@ int npbmz_destroy(npbmz_t* h) {
   if (h->aux_stream) { cudaStreamSynchronize(h->aux_stream); cudaStreamDestroy(h->aux_stream); }
   for (cudaStream_t gs : h->grp_stream)
     if (gs) { cudaStreamSynchronize(gs); cudaStreamDestroy(gs); }
+  if (h->prio_stream) { cudaStreamSynchronize(h->prio_stream); cudaStreamDestroy(h->prio_stream); }
   for (cudaEvent_t e : h->grp_ev)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : h->grp_out_ev)

@@ -148,9 +148,12 @@ struct Fields {
 
 // ---- state check ------------------------------------------------------------
 // A point of u is healthy when its density rho and its pressure-like quantity
-// rho E - |rho v|^2 / (2 rho) are both positive and finite.
+// rho E - |rho v|^2 / (2 rho) are both positive and finite.  Bits: the
+// density is not positive and finite; the pressure is finite but not
+// positive; the pressure is not finite (a NaN or infinity anywhere in u).
 constexpr unsigned HEALTH_DENSITY = 1u;
 constexpr unsigned HEALTH_PRESSURE = 2u;
+constexpr unsigned HEALTH_NONFINITE = 4u;
 
 // v > 0 and finite, on the bit pattern (integer pipe): the positive finite
 // doubles are exactly the patterns 1 .. 0x7FEFFFFFFFFFFFFF; zero, negatives,
@@ -168,14 +171,20 @@ __device__ __forceinline__ void health_report(const Fields& F, int64_t p, unsign
 }
 
 __device__ __forceinline__ bool positive_finite(float v) { return (unsigned)__float_as_uint(v) - 1u < 0x7F7FFFFFu; }
+__device__ __forceinline__ bool finite_bits(double v) {
+  return ((unsigned long long)__double_as_longlong(v) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+}
+__device__ __forceinline__ bool finite_bits(float v) { return (__float_as_uint(v) & 0x7F800000u) != 0x7F800000u; }
 
 // rho and pressure in FP64, or (the double-float kernels) as the high words
 // of their double-float values
 template <typename R>
 __device__ __forceinline__ void health_check(const Fields& F, int64_t p, R rho, R pressure) {
   if (!F.health) return;
-  const unsigned bits = (positive_finite(rho) ? 0u : HEALTH_DENSITY) | (positive_finite(pressure) ? 0u : HEALTH_PRESSURE);
-  if (__builtin_expect(bits != 0u, 0)) health_report(F, p, bits);
+  if (__builtin_expect(positive_finite(rho) && positive_finite(pressure), 1)) return;
+  const unsigned bits = (positive_finite(rho) ? 0u : HEALTH_DENSITY) |
+                        (positive_finite(pressure) ? 0u : finite_bits(pressure) ? HEALTH_PRESSURE : HEALTH_NONFINITE);
+  health_report(F, p, bits);
 }
 
 // x line through interior point (j, k) of zone z (-1 when j or k is a face).

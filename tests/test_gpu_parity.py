@@ -243,11 +243,13 @@ def test_graph_replay_equals_direct_launches():
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.RHS_DF], ids=["fp64", "mixed", "mixed-dfrhs"])
-@pytest.mark.parametrize("groups", [2, 3, 5])
-def test_zone_group_graph_equals_direct_launches(kind, flags, groups):
-    """The step graph with zone-group branches (npbmz_set_step_groups) runs the
-    same kernels per zone: bit-identical to direct launches of the batched
-    step (class W geometry, 16 zones; uneven for BT)."""
+@pytest.mark.parametrize("groups,prio", [(2, False), (3, False), (5, False), (2, True), (4, True)])
+def test_zone_group_graph_equals_direct_launches(kind, flags, groups, prio):
+    """The step graph with zone-group branches (npbmz_set_step_groups), with
+    or without the priority stream for the FP64 phases
+    (npbmz_set_step_priority), runs the same kernels per zone: bit-identical
+    to direct launches of the batched step (class W geometry, 16 zones;
+    uneven for BT)."""
     geom, dt, _ = geom_class(kind, "W")
     ce = seeded(geom)
     a = npbmz.Problem(geom, dt, flags)
@@ -255,6 +257,7 @@ def test_zone_group_graph_equals_direct_launches(kind, flags, groups):
     a.setup(ce)
     b.setup(ce)
     b.set_step_groups(groups)
+    b.set_step_priority(prio)
     a.step(6)
     b.step(6)
     b.synchronize()
