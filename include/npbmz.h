@@ -251,14 +251,18 @@ int npbmz_adjoint(npbmz_t* h, int nsteps, int checkpoint_every, const double* u_
  * reference. */
 int npbmz_set_step_groups(npbmz_t* h, int groups);
 
-/* Zone-group branches of the step graph: fp64_first != 0 issues every group's
- * primitive kernel and compute_rhs (FP64-pipe bound) on one stream of the
- * device's greatest priority, in group order, so that their CTAs reach the
- * SMs ahead of the queued CTAs of the sweeps (FP32 pipe) they overlap;
- * instantiated with per-node priorities.  Launch order only: results are
- * unchanged.  npbmz_autotune chooses it with the group count.  No counterpart
- * in the reference. */
-int npbmz_set_step_priority(npbmz_t* h, int fp64_first);
+/* How the zone-group branches of the step graph share the SMs.
+ * fp64_first != 0 issues every group's primitive kernel and compute_rhs
+ * (FP64-pipe bound) on one stream of the device's greatest priority, in
+ * group order, so that their CTAs reach the SMs ahead of the queued CTAs of
+ * the sweeps (FP32 pipe) they overlap; the graph is instantiated with
+ * per-node priorities.  sweep_ctas_per_sm > 0 runs the pipelined sweep
+ * kernels as persistent grids of at most that many CTAs per SM, leaving
+ * registers on every SM for the FP64 kernels beside them (0: one CTA per
+ * work item).  Launch configuration only: results are unchanged.
+ * npbmz_autotune chooses both with the group count.  No counterpart in the
+ * reference. */
+int npbmz_set_step_overlap(npbmz_t* h, int fp64_first, int sweep_ctas_per_sm);
 
 /* Use `stream` (a cudaStream_t, NULL = the legacy default stream) for all
  * later work of the handle. */

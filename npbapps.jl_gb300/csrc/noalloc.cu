@@ -185,7 +185,7 @@ extern "C" int npbmz_bt_xsolve_noalloc(int nx, int ny, int nz, const double* par
   const npbmz::Consts K = noalloc_consts(params);
   npbmz::noalloc::launch_prim(false, F, K, 0, np, s);
   npbmz::noalloc::launch_solve(false, 0, 0, F, K, sym->work, nwork, NOALLOC_TPB, sym->scratch + prim_doubles, lines, 0,
-                               nullptr, s, false);
+                               nullptr, s, false, 0);
   // nothing was pending before the three launches, so this is theirs
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail("kernel launch failed", e);

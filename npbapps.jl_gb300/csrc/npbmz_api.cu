@@ -260,6 +260,10 @@ struct npbmz_handle {
   // ahead of the waiting CTAs of the sweeps (FP32 pipe) they run beside
   bool fp64_prio = false;
   cudaStream_t prio_stream = nullptr;
+  // resident CTAs per SM of the pipelined sweep kernels (0: one CTA per work
+  // item): a cap leaves registers on every SM for the FP64 kernels of the
+  // next zone group
+  int sweep_cap = 0;
   cudaEvent_t grp_ev[2 * 8 + 1] = {};
   // npbmz_step_download: the graph records grp_out_ev[g] (an external event)
   // when group g's z sweep has written its zones' u; io_stream then copies
@@ -663,7 +667,7 @@ int phase_solve(npbmz_t* h, int dir, int zone, int add_u, bool fused = false) {
                           h->nlines[dir], add_u, nullptr, h->stream);
     else
       fast::launch_solve(sp, mode, dir, F, h->K, h->wline_d[dir] + lo, hi - lo, tpb, line_scratch(h, dir),
-                         h->nlines[dir], add_u, h->xw, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+                         h->nlines[dir], add_u, h->xw, h->stream, (h->flags & NPBMZ_PERSIST) != 0, h->sweep_cap);
     CKL(h);
     return 0;
   });
@@ -1733,11 +1737,13 @@ int npbmz_state_check(npbmz_t* h, int* bits, int* zone, int* i, int* j, int* k) 
   return 0;
 }
 
-int npbmz_set_step_priority(npbmz_t* h, int fp64_first) {
+int npbmz_set_step_overlap(npbmz_t* h, int fp64_first, int sweep_ctas_per_sm) {
   if (!h) return fail(nullptr, "null handle");
+  if (sweep_ctas_per_sm < 0 || sweep_ctas_per_sm > 32) return fail(h, "sweep_ctas_per_sm must be 0..32");
   CK(h, cudaStreamSynchronize(h->stream));
   drop_graph(h);
   h->fp64_prio = fp64_first != 0;
+  h->sweep_cap = sweep_ctas_per_sm;
   return 0;
 }
 
@@ -1858,20 +1864,25 @@ int npbmz_autotune(npbmz_t* h) {
     }
   }
   if (!rc && (h->flags & NPBMZ_GRAPH) && !(h->flags & (NPBMZ_EXACT | NPBMZ_PERZONE)) && h->nzones >= 8) {
-    // zone-group branches, each count with and without the priority stream
+    // zone-group branches; with more than one, the priority stream for the
+    // FP64 phases and a cap on the sweeps' resident CTAs per SM
     const int gcand[] = {1, 2, 3, 4, 6, 8};
+    const int ccand[] = {0, 3, 2};
     float best = 1e30f;
-    int best_g = h->ngroups;
+    int best_g = h->ngroups, best_c = h->sweep_cap;
     bool best_p = h->fp64_prio;
     for (int G : gcand)
-      for (int prio = 0; prio < (G > 1 ? 2 : 1) && !rc; ++prio) {
-        if (G > h->nzones || npbmz_set_step_groups(h, G)) continue;
-        h->fp64_prio = prio != 0;
-        const float ms = step_ms();
-        if (ms < 0.f) { rc = -1; break; }
-        if (ms < best) { best = ms; best_g = G; best_p = prio != 0; }
-      }
+      for (int prio = 0; prio < (G > 1 ? 2 : 1) && !rc; ++prio)
+        for (int ci = 0; ci < (G > 1 ? 3 : 1) && !rc; ++ci) {
+          if (G > h->nzones || npbmz_set_step_groups(h, G)) continue;
+          h->fp64_prio = prio != 0;
+          h->sweep_cap = ccand[ci];
+          const float ms = step_ms();
+          if (ms < 0.f) { rc = -1; break; }
+          if (ms < best) { best = ms; best_g = G; best_p = prio != 0; best_c = ccand[ci]; }
+        }
     h->fp64_prio = best_p;
+    h->sweep_cap = best_c;
     if (!rc) rc = npbmz_set_step_groups(h, best_g);
   }
   if (!rc && !(h->flags & (NPBMZ_EXACT | NPBMZ_PERZONE))) {
@@ -1913,11 +1924,11 @@ int npbmz_describe(npbmz_t* h, char* buf, size_t n) {
   }
   tp += "]";
   snprintf(buf, n, "{\"kind\":\"%s\",\"zones\":%d,\"points\":%lld,\"flags\":%d,\"lines_per_cta\":%s,"
-           "\"zone_size_buckets\":%d,\"step_groups\":%d,\"fp64_priority\":%s,\"persistent\":%s,"
-           "\"launches_per_step\":%d,\"device_bytes\":%lld}",
+           "\"zone_size_buckets\":%d,\"step_groups\":%d,\"fp64_priority\":%s,\"sweep_ctas_per_sm\":%d,"
+           "\"persistent\":%s,\"launches_per_step\":%d,\"device_bytes\":%lld}",
            h->kind == NPBMZ_BT ? "BT" : "SP", h->nzones, (long long)h->NP, h->flags, tp.c_str(), h->nbkt, h->ngroups,
-           h->fp64_prio ? "true" : "false", (h->flags & NPBMZ_PERSIST) ? "true" : "false", h->launches_per_step,
-           (long long)h->device_bytes);
+           h->fp64_prio ? "true" : "false", h->sweep_cap, (h->flags & NPBMZ_PERSIST) ? "true" : "false",
+           h->launches_per_step, (long long)h->device_bytes);
   return 0;
 }
 

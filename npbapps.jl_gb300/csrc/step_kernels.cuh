@@ -2404,12 +2404,17 @@ __global__ void __launch_bounds__(128) k_add(Fields F, const Work* __restrict__ 
 // ============================================================================
 // Grid of a work-item kernel: one CTA per item, or (persistent) as many CTAs
 // as fit on the device at once, each looping over items.
-static int item_grid(const void* f, int nwork, int tpb, size_t smem, bool persist) {
-  if (!persist) return nwork;
+// Grid of a work-list kernel: one CTA per item, or (persist) as many CTAs as
+// fit on the SMs looping over the items; ctas_per_sm > 0 makes it persistent
+// with at most that many CTAs per SM, which leaves room on every SM for the
+// CTAs of kernels running beside it on other streams.
+static int item_grid(const void* f, int nwork, int tpb, size_t smem, bool persist, int ctas_per_sm = 0) {
+  if (!persist && ctas_per_sm <= 0) return nwork;
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, tpb, smem) != cudaSuccess || per < 1) per = 1;
+  if (ctas_per_sm > 0 && ctas_per_sm < per) per = ctas_per_sm;
   return nwork < per * sms ? nwork : per * sms;
 }
 
@@ -2475,7 +2480,7 @@ static void launch_solve_t(bool sp, int dir, const Fields& F, const Consts& K, c
 // double-float residual (BT; SP: FP64 residual); 3: FP32 + refinement with
 // an FP64 residual (xw: a [5][NP] buffer for the first solution).
 void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork, int tpb,
-                  void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s, bool persist) {
+                  void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s, bool persist, int ctas_per_sm) {
   if (nwork <= 0) return;
 #if NPBMZ_HAS_FP32
   if (mode == 1) { launch_solve_t<float>(sp, dir, F, K, work, nwork, tpb, scratch, nlt, add_u, F.rhs, 1, s); return; }
@@ -2487,9 +2492,11 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
     const size_t sm_m = pls_mixed_smem(tpb), sm_r = pls_refine_smem(tpb, dir != 2);
 #define NPBMZ_SPL(D, OD)                                                                                          \
   do {                                                                                                            \
-    k_sp_mixed_pl<D><<<item_grid((const void*)k_sp_mixed_pl<D>, nwork, tpb, sm_m, persist), tpb, sm_m, s>>>(       \
+    k_sp_mixed_pl<D><<<item_grid((const void*)k_sp_mixed_pl<D>, nwork, tpb, sm_m, persist, ctas_per_sm), tpb,     \
+                       sm_m, s>>>(                                                                                \
         F, K, work, nwork, scr, nlt, x0);                                                                         \
-    k_sp_refine_pl<D, OD><<<item_grid((const void*)k_sp_refine_pl<D, OD>, nwork, tpb, sm_r, persist), tpb, sm_r,   \
+    k_sp_refine_pl<D, OD><<<item_grid((const void*)k_sp_refine_pl<D, OD>, nwork, tpb, sm_r, persist, ctas_per_sm), \
+                            tpb, sm_r,                                                                            \
                             s>>>(F, K, work, nwork, scr, nlt, add_u, x0);                                         \
   } while (0)
     if (dir == 0) {
@@ -2509,9 +2516,11 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
     const size_t sm_m = pl_mixed_smem(tpb), sm_r = pl_refine_smem(tpb, dir != 2);
 #define NPBMZ_PL(D, OD)                                                                                          \
   do {                                                                                                           \
-    k_bt_mixed_pl<D><<<item_grid((const void*)k_bt_mixed_pl<D>, nwork, tpb, sm_m, persist), tpb, sm_m, s>>>(       \
+    k_bt_mixed_pl<D><<<item_grid((const void*)k_bt_mixed_pl<D>, nwork, tpb, sm_m, persist, ctas_per_sm), tpb,     \
+                       sm_m, s>>>(                                                                                \
         F, K, work, nwork, scr, nlt, x0);                                                                        \
-    k_bt_refine_pl<D, OD><<<item_grid((const void*)k_bt_refine_pl<D, OD>, nwork, tpb, sm_r, persist), tpb, sm_r,   \
+    k_bt_refine_pl<D, OD><<<item_grid((const void*)k_bt_refine_pl<D, OD>, nwork, tpb, sm_r, persist, ctas_per_sm), \
+                            tpb, sm_r,                                                                            \
                             s>>>(F, K, work, nwork, scr, nlt, add_u, x0);                                        \
   } while (0)
     if (dir == 0) {

@@ -16,7 +16,7 @@ namespace npbmz {
                   double* partials, cudaStream_t s, const RhsF64Consts* rc = nullptr, bool persist = false);         \
   void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, const Work* work, int nwork,       \
                     int tpb, void* scratch, int64_t nlt, int add_u, double* xw, cudaStream_t s,                      \
-                    bool persist = false);                                                                           \
+                    bool persist = false, int ctas_per_sm = 0);                                                      \
   void launch_add(const Fields& F, const Work* work, int nwork, cudaStream_t s);                                     \
   }
 NPBMZ_DECLARE_LAUNCHERS(exact)

@@ -44,7 +44,7 @@ EXPORTS = [
     "npbmz_verify", "npbmz_phase", "npbmz_set_stream", "npbmz_synchronize", "npbmz_autotune",
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
     "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
-    "npbmz_step_download", "npbmz_face_plan", "npbmz_pack_faces", "npbmz_unpack_faces", "npbmz_set_step_priority",
+    "npbmz_step_download", "npbmz_face_plan", "npbmz_pack_faces", "npbmz_unpack_faces", "npbmz_set_step_overlap",
     "npbmz_state_check",
 ]
 STATE_DENSITY, STATE_PRESSURE, STATE_NONFINITE = 1, 2, 4
@@ -156,7 +156,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_adjoint.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp]
     L.npbmz_step_profile.argtypes = [vp, ctypes.c_int, dp]
     L.npbmz_set_step_groups.argtypes = [vp, ctypes.c_int]
-    L.npbmz_set_step_priority.argtypes = [vp, ctypes.c_int]
+    L.npbmz_set_step_overlap.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.npbmz_state_check.argtypes = [vp] + [ip] * 5
     i64p = ctypes.POINTER(ctypes.c_int64)
     L.npbmz_face_plan.argtypes = [vp, ctypes.c_int, ip, ctypes.c_int, ip, i64p, i64p]
@@ -352,9 +352,11 @@ class Problem:
         self._check(lib().npbmz_state_check(self._h, *[ctypes.byref(x) for x in v]), "npbmz_state_check")
         return v[0].value, tuple(x.value for x in v[1:])
 
-    def set_step_priority(self, fp64_first: bool):
-        """Zone-group branches: prim + compute_rhs on a high-priority stream."""
-        self._check(lib().npbmz_set_step_priority(self._h, int(bool(fp64_first))), "npbmz_set_step_priority")
+    def set_step_overlap(self, fp64_first: bool, sweep_ctas_per_sm: int = 0):
+        """Zone-group branches: prim + compute_rhs on a high-priority stream,
+        and at most sweep_ctas_per_sm resident sweep CTAs per SM (0: no cap)."""
+        self._check(lib().npbmz_set_step_overlap(self._h, int(bool(fp64_first)), int(sweep_ctas_per_sm)),
+                    "npbmz_set_step_overlap")
 
     def autotune(self):
         self._check(lib().npbmz_autotune(self._h), "npbmz_autotune")

@@ -243,13 +243,14 @@ def test_graph_replay_equals_direct_launches():
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.RHS_DF], ids=["fp64", "mixed", "mixed-dfrhs"])
-@pytest.mark.parametrize("groups,prio", [(2, False), (3, False), (5, False), (2, True), (4, True)])
-def test_zone_group_graph_equals_direct_launches(kind, flags, groups, prio):
+@pytest.mark.parametrize("groups,prio,cap", [(2, False, 0), (3, False, 0), (5, False, 0), (2, True, 0), (4, True, 3),
+                                             (3, False, 2)])
+def test_zone_group_graph_equals_direct_launches(kind, flags, groups, prio, cap):
     """The step graph with zone-group branches (npbmz_set_step_groups), with
-    or without the priority stream for the FP64 phases
-    (npbmz_set_step_priority), runs the same kernels per zone: bit-identical
-    to direct launches of the batched step (class W geometry, 16 zones;
-    uneven for BT)."""
+    or without the priority stream for the FP64 phases and a cap on the
+    sweeps' resident CTAs (npbmz_set_step_overlap), runs the same kernels per
+    zone: bit-identical to direct launches of the batched step (class W
+    geometry, 16 zones; uneven for BT)."""
     geom, dt, _ = geom_class(kind, "W")
     ce = seeded(geom)
     a = npbmz.Problem(geom, dt, flags)
@@ -257,7 +258,7 @@ def test_zone_group_graph_equals_direct_launches(kind, flags, groups, prio):
     a.setup(ce)
     b.setup(ce)
     b.set_step_groups(groups)
-    b.set_step_priority(prio)
+    b.set_step_overlap(prio, cap)
     a.step(6)
     b.step(6)
     b.synchronize()
