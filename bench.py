@@ -638,20 +638,19 @@ def run_gpu(args):
         q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, host.data_ptr(), False)
         ptr = host.data_ptr()
         for _ in range(args.warmup):
-            q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, True, sync=False)
-            q.step_download(1, npbmz.LAYOUT_REF, ptr)
+            q.step_inout(1, npbmz.LAYOUT_REF, ptr, ptr)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            q.transfer_raw(npbmz.U, -1, npbmz.LAYOUT_REF, ptr, True, sync=False)
-            q.step_download(1, npbmz.LAYOUT_REF, ptr)
+            q.step_inout(1, npbmz.LAYOUT_REF, ptr, ptr)
         te = time.perf_counter() - t0
         moved = 5 * 8 * pts
         extra["e2e"] = {"value": pts * world * args.steps / te / 1e6, "unit": "Mgridpt-steps/s",
                         "h2d_bytes_per_step": moved, "d2h_bytes_per_step": moved,
-                        "path": "npbmz_upload_async + npbmz_step_download (zone=-1, NPBMZ_LAYOUT_REF) on page-locked "
-                                "reference-layout u (interior points read/written in place by one kernel each way; "
-                                "each zone group's copy-out starts when its z sweep is done)"}
+                        "path": "npbmz_step_inout(1, NPBMZ_LAYOUT_REF) per step on page-locked reference-layout u, "
+                                "read and written in place (interior points, by kernels over NVLink-C2C): the planes "
+                                "exch_qbc reads first, then each zone group's other points while earlier groups "
+                                "compute; each group copied out when its z sweep is done"}
         if not args.no_cpu_baseline:
             extra["cpu_baseline"] = cpu_baseline(kind, cls, ce)
     if rank == 0:

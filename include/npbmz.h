@@ -218,6 +218,18 @@ int npbmz_state_check(npbmz_t* h, int* bits, int* zone, int* i, int* j, int* k);
  * counterpart in the reference (whose u lives in host memory). */
 int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host);
 
+/* u of every zone from host_in, nsteps steps, u of every zone to host_out
+ * (layout as npbmz_download, zone = -1; host_out may be host_in): the same
+ * result as npbmz_upload + npbmz_step_download, the reference's loop with u
+ * kept in host memory.  For NPBMZ_GRAPH handles with zone-group branches and
+ * page-locked buffers the copies overlap the steps: the planes exch_qbc
+ * reads are uploaded first and exch_qbc runs; the rest of each zone group's
+ * points then arrive while earlier groups already compute, and each group
+ * leaves as soon as its last z sweep is done.  Handles with NPBMZ_REMOTE
+ * faces take the sequential path.  Synchronous; the state check of
+ * npbmz_step applies.  No counterpart in the reference. */
+int npbmz_step_inout(npbmz_t* h, int nsteps, int layout, const double* host_in, double* host_out);
+
 /* The node part of verify (src/BT/verify.jl:411-505): error_norm of u, then
  * compute_rhs without an exchange, rhs_norm; sums over zones.  Synchronous. */
 int npbmz_verify(npbmz_t* h, double* xcr, double* xce);

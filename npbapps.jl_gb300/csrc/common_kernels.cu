@@ -313,10 +313,23 @@ __device__ __forceinline__ int64_t ref_index(int kind, int field, const ZoneDev&
 // page-locked host buffer holding zones from zone_lo (sub = soff[zone_lo]).
 // layout 0: dense [m][k][j][i]; 1: the reference OffsetArray (with halo);
 // 2: compact reference order without halo (BT [k][j][i][m], SP = dense).
+// part (uploads split around exch_qbc): 0 every point; 1 only the interior
+// planes exch_qbc reads (i = 1, nx-2 and j = 1, ny-2, transverse indices
+// 1..n-2); 2 every point but the ghost planes exch_qbc writes (i = 0, nx-1
+// and j = 0, ny-1, transverse indices 1..n-2).
+__device__ __forceinline__ bool exch_point(const ZoneDev& Z, int i, int j, int k, bool ghost) {
+  if (k < 1 || k > Z.nz - 2) return false;
+  const int ilo = ghost ? 0 : 1, ihi = ghost ? Z.nx - 1 : Z.nx - 2;
+  const int jlo = ghost ? 0 : 1, jhi = ghost ? Z.ny - 1 : Z.ny - 2;
+  const bool xface = (i == ilo || i == ihi) && j >= 1 && j <= Z.ny - 2;
+  const bool yface = (j == jlo || j == jhi) && i >= 1 && i <= Z.nx - 2;
+  return xface || yface;
+}
+
 __global__ void __launch_bounds__(256) k_convert(Fields F, double* __restrict__ field_planes,
                                                  double* __restrict__ stage, const int64_t* __restrict__ soff,
                                                  int64_t sub, int zone_lo, int kind, int field, int layout, int dir,
-                                                 const int* __restrict__ zlist) {
+                                                 const int* __restrict__ zlist, int part) {
   const int zone = zlist ? zlist[blockIdx.y] : zone_lo + blockIdx.y;
   const ZoneDev Z = F.zones[zone];
   const int np = Z.nx * Z.ny * Z.nz;
@@ -329,6 +342,8 @@ __global__ void __launch_bounds__(256) k_convert(Fields F, double* __restrict__ 
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 5 * np; t += gridDim.x * blockDim.x) {
     const int m = aos ? t % 5 : t / np, q = aos ? t / 5 : t % np;
     const int i = q % Z.nx, j = (q / Z.nx) % Z.ny, k = q / (Z.nx * Z.ny);
+    if (part == 1 && !exch_point(Z, i, j, k, false)) continue;
+    if (part == 2 && exch_point(Z, i, j, k, true)) continue;
     int64_t s;
     if (layout == 0) s = t;
     else if (layout == 1) s = ref_index(kind, field, Z, m, i, j, k);
@@ -391,12 +406,13 @@ void launch_norm_finish(const ZoneDev* zones, const double* partials, const int*
 }
 
 void launch_convert(const Fields& F, double* planes, double* stage, const int64_t* soff, int64_t sub, int zone_lo,
-                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s, const int* zlist) {
+                    int nzn, int max_np, int kind, int field, int layout, int dir, cudaStream_t s, const int* zlist,
+                    int part) {
   if (nzn <= 0) return;
   int gx = (5 * max_np + 255) / 256;
   if (gx > 512) gx = 512;
   dim3 grid(gx, nzn);
-  k_convert<<<grid, 256, 0, s>>>(F, planes, stage, soff, sub, zone_lo, kind, field, layout, dir, zlist);
+  k_convert<<<grid, 256, 0, s>>>(F, planes, stage, soff, sub, zone_lo, kind, field, layout, dir, zlist, part);
 }
 
 void launch_faces(bool pack, const Fields& F, const FaceDesc* faces, int nfaces, int max_face, double* buf,

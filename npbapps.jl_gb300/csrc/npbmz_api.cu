@@ -286,6 +286,12 @@ struct npbmz_handle {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaGraphExec_t graph_exec = nullptr;
+  // npbmz_step_inout's first step: the grouped graph without exch_qbc, whose
+  // group g waits for the upload of its zones (up_ev[g], recorded on
+  // io_stream before the launch)
+  cudaGraphExec_t graph_inout = nullptr;
+  cudaEvent_t up_ev[8] = {};
+  cudaEvent_t exch_ev = nullptr;
   cudaStream_t graph_stream = nullptr;
   cudaStream_t aux_stream = nullptr;   // graph replay when the handle's stream is the legacy one
   cudaEvent_t fence[2] = {nullptr, nullptr};
@@ -733,7 +739,9 @@ int one_step(npbmz_t* h, bool norm, double* norm_slot) {
 
 void drop_graph(npbmz_t* h) {
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  if (h->graph_inout) cudaGraphExecDestroy(h->graph_inout);
   h->graph_exec = nullptr;
+  h->graph_inout = nullptr;
 }
 
 // One step as zone-group branches (captured into the step graph): after
@@ -741,10 +749,13 @@ void drop_graph(npbmz_t* h) {
 // stream; its primitive kernel waits for group g-1's compute_rhs.  So the
 // FP32 sweeps of group g (FP32 / issue bound) run beside the FP64
 // primitive and compute_rhs kernels of group g+1 (FP64-pipe bound).
-int grouped_step(npbmz_t* h, cudaStream_t cs) {
+// inout: the first step of npbmz_step_inout -- exch_qbc is left out (the
+// caller runs it between the two parts of the upload) and group g's branch
+// first waits for up_ev[g], the upload of its zones.
+int grouped_step(npbmz_t* h, cudaStream_t cs, bool inout) {
   const int G = h->ngroups;
   const bool sp = h->kind == NPBMZ_SP;
-  if (phase_exch(h)) return -1;
+  if (!inout && phase_exch(h)) return -1;
   cudaEvent_t start = h->grp_ev[2 * G];
   CK(h, cudaEventRecord(start, cs));
   int rc = 0;
@@ -754,6 +765,7 @@ int grouped_step(npbmz_t* h, cudaStream_t cs) {
     // or on the group's own stream after group g-1's compute_rhs
     cudaStream_t P = h->fp64_prio ? h->prio_stream : S;
     rc |= cudaStreamWaitEvent(P, start, 0) != cudaSuccess;
+    if (inout) rc |= cudaStreamWaitEvent(P, h->up_ev[g], cudaEventWaitExternal) != cudaSuccess;
     if (g > 0 && P == S) rc |= cudaStreamWaitEvent(S, h->grp_ev[2 * (g - 1)], 0) != cudaSuccess;
     h->stream = P;
     h->cur_group = g;
@@ -778,15 +790,20 @@ bool use_groups(const npbmz_t* h) {
   return h->ngroups > 1 && !use_exact(h) && !(h->flags & NPBMZ_PERZONE);
 }
 
-int capture_step_graph(npbmz_t* h) {
-  drop_graph(h);
+int capture_step_graph(npbmz_t* h, bool inout = false) {
+  cudaGraphExec_t& exec = inout ? h->graph_inout : h->graph_exec;
+  if (exec) cudaGraphExecDestroy(exec);
+  exec = nullptr;
+  if (inout && !use_groups(h)) return fail(h, "the overlapped upload needs zone-group branches");
   if (use_groups(h)) {
     for (int g = 0; g < h->ngroups; ++g)
       if (!h->grp_stream[g]) CK(h, cudaStreamCreateWithFlags(&h->grp_stream[g], cudaStreamNonBlocking));
     for (int e = 0; e < 2 * h->ngroups + 1; ++e)
       if (!h->grp_ev[e]) CK(h, cudaEventCreateWithFlags(&h->grp_ev[e], cudaEventDisableTiming));
-    for (int g = 0; g < h->ngroups; ++g)
+    for (int g = 0; g < h->ngroups; ++g) {
       if (!h->grp_out_ev[g]) CK(h, cudaEventCreateWithFlags(&h->grp_out_ev[g], cudaEventDisableTiming));
+      if (!h->up_ev[g]) CK(h, cudaEventCreateWithFlags(&h->up_ev[g], cudaEventDisableTiming));
+    }
     if (h->fp64_prio && !h->prio_stream) {
       int least = 0, greatest = 0;
       CK(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -809,14 +826,13 @@ int capture_step_graph(npbmz_t* h) {
   cudaStream_t saved = h->stream;
   h->stream = cs;
   CK(h, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-  int rc = use_groups(h) ? grouped_step(h, cs) : one_step(h, false, nullptr);
+  int rc = use_groups(h) ? grouped_step(h, cs, inout) : one_step(h, false, nullptr);
   cudaError_t e = cudaStreamEndCapture(cs, &g);
   h->stream = saved;
   if (rc) { if (g) cudaGraphDestroy(g); return -1; }
   if (e != cudaSuccess) return fail(h, "stream capture failed: %s", cudaGetErrorString(e));
   // kernel nodes keep the priority of the stream they were captured from
-  e = cudaGraphInstantiate(&h->graph_exec, g,
-                           use_groups(h) && h->fp64_prio ? cudaGraphInstantiateFlagUseNodePriority : 0);
+  e = cudaGraphInstantiate(&exec, g, use_groups(h) && h->fp64_prio ? cudaGraphInstantiateFlagUseNodePriority : 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(h, "graph instantiate failed: %s", cudaGetErrorString(e));
   h->graph_stream = h->stream;
@@ -1600,6 +1616,68 @@ int npbmz_step_download(npbmz_t* h, int nsteps, int layout, double* host) {
   return health_verdict(h, "the steps");
 }
 
+int npbmz_step_inout(npbmz_t* h, int nsteps, int layout, const double* host_in, double* host_out) {
+  if (!h) return fail(nullptr, "null handle");
+  if (nsteps < 1) return fail(h, "nsteps must be >= 1");
+  if (!host_in || !host_out) return fail(h, "null host buffer");
+  if (layout != NPBMZ_LAYOUT_DENSE && layout != NPBMZ_LAYOUT_REF) return fail(h, "bad layout %d", layout);
+  auto mapped = [](const void* p) -> double* {
+    cudaPointerAttributes a;
+    std::memset(&a, 0, sizeof(a));
+    const bool ok = cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer;
+    cudaGetLastError();
+    return ok ? reinterpret_cast<double*>(a.devicePointer) : nullptr;
+  };
+  double* din = mapped(host_in);
+  double* dout = mapped(host_out);
+  if (!din || !dout || !(h->flags & NPBMZ_GRAPH) || !use_groups(h) || h->stream == nullptr || h->has_remote) {
+    // the same result in sequence: upload, steps with the copy-out
+    if (transfer(h, -1, NPBMZ_U, layout, const_cast<double*>(host_in), 0, false)) return -1;
+    return npbmz_step_download(h, nsteps, layout, host_out);
+  }
+  if (!h->graph_exec || h->graph_stream != h->stream)
+    if (capture_step_graph(h)) return -1;
+  if (!h->graph_inout || h->graph_stream != h->stream)
+    if (capture_step_graph(h, true)) return -1;
+  if (flush_boundary(h)) return -1;
+  if (!h->io_stream) CK(h, cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
+  if (!h->io_done) CK(h, cudaEventCreateWithFlags(&h->io_done, cudaEventDisableTiming));
+  if (!h->exch_ev) CK(h, cudaEventCreateWithFlags(&h->exch_ev, cudaEventDisableTiming));
+  const Fields F = fields(h);
+  const int64_t* so = h->soff_d[layout][NPBMZ_U];
+  if (health_begin(h)) return -1;
+  // 1. the planes exch_qbc reads, of every zone, then exch_qbc itself
+  launch_convert(F, h->u, din, so, 0, 0, h->nzones, h->max_np, h->kind, NPBMZ_U, layout, 0, h->stream, nullptr, 1);
+  CKL(h);
+  if (phase_exch(h)) return -1;
+  CK(h, cudaEventRecord(h->exch_ev, h->stream));
+  // 2. the rest of each zone group's points on io_stream, group by group; the
+  //    first step's graph starts each group's branch when its part is in
+  CK(h, cudaStreamWaitEvent(h->io_stream, h->exch_ev, 0));
+  for (int g = 0; g < h->ngroups; ++g) {
+    const int z0 = h->grp_zone_off[g], nz = h->grp_zone_off[g + 1] - z0;
+    launch_convert(F, h->u, din, so, 0, 0, nz, h->max_np, h->kind, NPBMZ_U, layout, 0, h->io_stream,
+                   h->grp_zones_d + z0, 2);
+    CKL(h);
+    CK(h, cudaEventRecord(h->up_ev[g], h->io_stream));
+  }
+  CK(h, cudaGraphLaunch(h->graph_inout, h->stream));
+  if (nsteps > 1 && replay_graph(h, nsteps - 1)) return -1;
+  // 3. each group's zones out as soon as the last step's z sweep is done
+  for (int g = 0; g < h->ngroups; ++g) {
+    const int z0 = h->grp_zone_off[g], nz = h->grp_zone_off[g + 1] - z0;
+    CK(h, cudaStreamWaitEvent(h->io_stream, h->grp_out_ev[g], 0));
+    launch_convert(F, h->u, dout, so, 0, 0, nz, h->max_np, h->kind, NPBMZ_U, layout, 1, h->io_stream,
+                   h->grp_zones_d + z0);
+    CKL(h);
+  }
+  CK(h, cudaEventRecord(h->io_done, h->io_stream));
+  if (health_read(h)) return -1;
+  CK(h, cudaStreamWaitEvent(h->stream, h->io_done, 0));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return health_verdict(h, "the steps");
+}
+
 int npbmz_step_profile(npbmz_t* h, int nsteps, double* phase_ms) {
   if (!h) return fail(nullptr, "null handle");
   if (nsteps < 1 || !phase_ms) return fail(h, "nsteps must be >= 1 and phase_ms non-null");
@@ -2014,6 +2092,9 @@ int npbmz_destroy(npbmz_t* h) {
     if (e) cudaEventDestroy(e);
   if (h->io_stream) { cudaStreamSynchronize(h->io_stream); cudaStreamDestroy(h->io_stream); }
   if (h->io_done) cudaEventDestroy(h->io_done);
+  for (cudaEvent_t e : h->up_ev)
+    if (e) cudaEventDestroy(e);
+  if (h->exch_ev) cudaEventDestroy(h->exch_ev);
   if (h->grp_zones_d) cudaFree(h->grp_zones_d);
   if (h->health_d) cudaFree(h->health_d);
   if (h->send_faces_d) cudaFree(h->send_faces_d);

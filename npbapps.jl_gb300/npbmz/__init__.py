@@ -45,7 +45,7 @@ EXPORTS = [
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
     "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
     "npbmz_step_download", "npbmz_face_plan", "npbmz_pack_faces", "npbmz_unpack_faces", "npbmz_set_step_overlap",
-    "npbmz_state_check",
+    "npbmz_state_check", "npbmz_step_inout",
 ]
 STATE_DENSITY, STATE_PRESSURE, STATE_NONFINITE = 1, 2, 4
 REMOTE = -1  # NPBMZ_REMOTE: a face whose neighbour zone lives on another rank
@@ -139,6 +139,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_adi.argtypes = [vp, ctypes.c_int]
     L.npbmz_step.argtypes = [vp, ctypes.c_int, dp]
     L.npbmz_step_download.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    L.npbmz_step_inout.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     L.npbmz_verify.argtypes = [vp, dp, dp]
     L.npbmz_phase.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.npbmz_set_stream.argtypes = [vp, vp]
@@ -303,6 +304,13 @@ class Problem:
         transfer_raw); with a page-locked buffer and zone-group branches the
         copies of each group overlap the other groups' work."""
         self._check(lib().npbmz_step_download(self._h, nsteps, layout, ctypes.c_void_p(ptr)), "npbmz_step_download")
+
+    def step_inout(self, nsteps: int, layout: int, in_ptr: int, out_ptr: int):
+        """u of all zones from the host buffer at in_ptr, nsteps steps, u to
+        out_ptr (layout as transfer_raw); with page-locked buffers and
+        zone-group branches the copies overlap the steps."""
+        self._check(lib().npbmz_step_inout(self._h, nsteps, layout, ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr)),
+                    "npbmz_step_inout")
 
     def step_profile(self, nsteps: int = 1):
         """Mean device milliseconds per step of each phase of the batched step

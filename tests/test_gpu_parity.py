@@ -298,6 +298,60 @@ def test_step_download_equals_step_then_download(kind, flags, groups):
 
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
+@pytest.mark.parametrize("flags,groups,prio,cap,nsteps", [
+    (npbmz.MIXED | npbmz.GRAPH, 3, False, 0, 1), (npbmz.MIXED | npbmz.GRAPH, 2, True, 3, 2),
+    (npbmz.GRAPH, 4, True, 0, 3), (npbmz.MIXED, 1, False, 0, 2)],
+    ids=["mixed-graph-3groups", "mixed-graph-2groups-prio-cap3", "fp64-graph-4groups-prio", "mixed-direct"])
+@pytest.mark.parametrize("layout", [npbmz.LAYOUT_REF, npbmz.LAYOUT_DENSE], ids=["ref", "dense"])
+def test_step_inout_equals_upload_step_download(kind, flags, groups, prio, cap, nsteps, layout):
+    """npbmz_step_inout (exch_qbc's source planes uploaded first, then each
+    zone group's remaining points while earlier groups compute, each group
+    copied out after its last z sweep) leaves the same host array and device
+    state as npbmz_upload + npbmz_step + npbmz_download, from a host array
+    that differs from the device state; in place (host_in == host_out) and
+    into a second buffer."""
+    torch = pytest.importorskip("torch")
+    geom, dt, _ = geom_class(kind, "W")
+    ce = seeded(geom)
+    if layout == npbmz.LAYOUT_REF:
+        total = sum(npbmz.ref_elems(geom.kind, npbmz.U, int(geom.nx[z]), int(geom.ny[z]), int(geom.nz[z]))
+                    for z in range(geom.nzones))
+    else:
+        total = 5 * int(np.sum(geom.nx.astype(np.int64) * geom.ny * geom.nz))
+    a = npbmz.Problem(geom, dt, flags)
+    b = npbmz.Problem(geom, dt, flags)
+    for q in (a, b):
+        q.setup(ce)
+        if flags & npbmz.GRAPH:
+            q.set_step_groups(groups)
+            q.set_step_overlap(prio, cap)
+    # a host u one step ahead of the device state, perturbed, halo untouched
+    src = npbmz.Problem(geom, dt, flags)
+    src.setup(ce)
+    src.step(1)
+    h0 = torch.full((total,), -7.0, dtype=torch.float64, pin_memory=True)
+    src.transfer_raw(npbmz.U, -1, layout, h0.data_ptr(), False)
+    v = h0.numpy()
+    v[v != -7.0] *= 1.0 + 1e-3 * np.sin(np.arange(int(np.sum(v != -7.0))))
+    ha = h0.clone().pin_memory()
+    hb_in = h0.clone().pin_memory()
+    hb_out = torch.full((total,), -7.0, dtype=torch.float64, pin_memory=True)
+    for rep in range(2):
+        a.transfer_raw(npbmz.U, -1, layout, ha.data_ptr(), True)
+        a.step(nsteps)
+        a.transfer_raw(npbmz.U, -1, layout, ha.data_ptr(), False)
+        if rep == 0:
+            b.step_inout(nsteps, layout, hb_in.data_ptr(), hb_out.data_ptr())
+            np.testing.assert_array_equal(ha.numpy(), hb_out.numpy())
+            hb_in.copy_(hb_out)
+        else:
+            b.step_inout(nsteps, layout, hb_in.data_ptr(), hb_in.data_ptr())
+            np.testing.assert_array_equal(ha.numpy(), hb_in.numpy())
+    for z in range(geom.nzones):
+        np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
+
+
+@pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags", [0, npbmz.MIXED, npbmz.MIXED | npbmz.GRAPH, npbmz.MIXED | npbmz.RHS_DF | npbmz.GRAPH],
                          ids=["fp64", "mixed", "mixed-graph", "mixed-dfrhs-graph"])
 def test_persistent_kernels_equal_one_cta_per_item(kind, flags):
