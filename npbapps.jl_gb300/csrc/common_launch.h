@@ -22,6 +22,7 @@ void launch_convert(const Fields& F, double* planes, double* stage, const int64_
                     const int* zlist = nullptr, int part = 0);
 void launch_fill(double* a, int64_t n, double v, cudaStream_t s);
 void launch_state_check(const Fields& F, const Work* work, int nwork, cudaStream_t s);
+void launch_math_check(int which, int n, const double* x, double* y, cudaStream_t s);
 // pack (true) or unpack the listed faces to / from the device buffer buf
 void launch_faces(bool pack, const Fields& F, const FaceDesc* faces, int nfaces, int max_face, double* buf,
                   cudaStream_t s);

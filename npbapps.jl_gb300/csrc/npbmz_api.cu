@@ -1984,6 +1984,20 @@ int npbmz_autotune(npbmz_t* h) {
   return rc ? -1 : 0;
 }
 
+int npbmz_math_check(int which, int n, const double* x, double* y) {
+  if (which < 0 || which > 2 || n < 0 || (n && (!x || !y))) return fail(nullptr, "npbmz_math_check: bad arguments");
+  if (n == 0) return 0;
+  double* d = nullptr;
+  if (cudaMalloc((void**)&d, 2 * (size_t)n * sizeof(double)) != cudaSuccess)
+    return fail(nullptr, "npbmz_math_check: device allocation failed");
+  int rc = 0;
+  if (cudaMemcpy(d, x, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) rc = -1;
+  if (!rc) launch_math_check(which, n, d, d + n, nullptr);
+  if (!rc && cudaMemcpy(y, d + n, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = -1;
+  cudaFree(d);
+  return rc ? fail(nullptr, "npbmz_math_check: %s", cudaGetErrorString(cudaGetLastError())) : 0;
+}
+
 int npbmz_fp64_peak(double* gflops) {
   if (!gflops) return -1;
   return probe_fp64(gflops);

@@ -32,7 +32,11 @@ __device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int
   const int64_t NP = F.NP;
   {
     const double u1 = F.u[p], u2 = F.u[NP + p], u3 = F.u[2 * NP + p], u4 = F.u[3 * NP + p];
+#if NPBMZ_HAS_FP32
+    const double rho_inv = nr_rcp(u1);  // within a few ulps of 1/u1 (FMA build)
+#else
     const double rho_inv = 1.0e0 / u1;
+#endif
     const double square = 0.5e0 * (u2 * u2 + u3 * u3 + u4 * u4) * rho_inv;
     health_check(F, p, u1, F.u[4 * NP + p] - square);
     F.prim[PR_RHOI * NP + p] = rho_inv;
@@ -44,9 +48,15 @@ __device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int
     if (SP) {
       const double u5 = F.u[4 * NP + p];
       double aux = K.c1c2 * rho_inv * (u5 - square);
+#if NPBMZ_HAS_FP32
+      const double ainv = nr_rsqrt(aux);
+      F.prim[PR_SPEED * NP + p] = nr_sqrt_from_rsqrt(aux, ainv);
+      F.prim[PR_AINV * NP + p] = ainv;
+#else
       aux = sqrt(aux);
       F.prim[PR_SPEED * NP + p] = aux;
       F.prim[PR_AINV * NP + p] = 1.0e0 / aux;
+#endif
     }
     if (SP && F.primf) {
       const double v[PS_HI_COUNT] = {rho_inv, u2 * rho_inv, u3 * rho_inv, u4 * rho_inv, F.prim[PR_SPEED * NP + p]};

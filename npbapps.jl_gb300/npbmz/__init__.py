@@ -45,7 +45,7 @@ EXPORTS = [
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
     "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
     "npbmz_step_download", "npbmz_face_plan", "npbmz_pack_faces", "npbmz_unpack_faces", "npbmz_set_step_overlap",
-    "npbmz_state_check", "npbmz_step_inout",
+    "npbmz_state_check", "npbmz_step_inout", "npbmz_math_check",
 ]
 STATE_DENSITY, STATE_PRESSURE, STATE_NONFINITE = 1, 2, 4
 REMOTE = -1  # NPBMZ_REMOTE: a face whose neighbour zone lives on another rank
@@ -140,6 +140,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_step.argtypes = [vp, ctypes.c_int, dp]
     L.npbmz_step_download.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     L.npbmz_step_inout.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.npbmz_math_check.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp]
     L.npbmz_verify.argtypes = [vp, dp, dp]
     L.npbmz_phase.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.npbmz_set_stream.argtypes = [vp, vp]

@@ -524,3 +524,25 @@ def test_bt_class_b_autotuned_launch_shapes_keep_results(oracle_mod, flags):
     a.synchronize()
     for z in range(0, geom.nzones, 7):
         np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
+
+
+@pytest.mark.parametrize("which,ulps", [(0, 2), (1, 3), (2, 2)], ids=["rcp", "rsqrt", "sqrt"])
+def test_fma_build_reciprocal_and_square_root_error_bound(which, ulps):
+    """The FMA build's primitive kernel takes 1/rho and the SP speed of sound
+    and its reciprocal by Newton-Raphson refinement of the FP32 hardware
+    estimates (npbmz_math_check runs the same device functions).  Against
+    numpy's FP64 values (1/x and sqrt correctly rounded, 1/sqrt(x) rounded
+    twice) they stay within 2, 3 and 2 ulps over the range the state takes
+    and far beyond it; outside the FP32 range they fall back to the IEEE
+    operations."""
+    import ctypes
+
+    rng = np.random.default_rng(17)
+    x = np.concatenate([10.0 ** rng.uniform(-30, 30, 200000), rng.uniform(0.01, 100.0, 200000),
+                        np.array([1.0, 2.0, 0.5, 3.0, 1e-37, 1e37, 1e-300, 1e300, 7.0, 1.0 - 2 ** -52])])
+    y = np.zeros_like(x)
+    dp = ctypes.POINTER(ctypes.c_double)
+    assert npbmz.lib().npbmz_math_check(which, len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp)) == 0
+    want = 1.0 / x if which == 0 else 1.0 / np.sqrt(x) if which == 1 else np.sqrt(x)
+    err_ulps = np.abs(y - want) / np.spacing(want)
+    assert np.max(err_ulps) <= ulps, (np.max(err_ulps), x[np.argmax(err_ulps)])
