@@ -292,6 +292,12 @@ struct npbmz_handle {
   cudaGraphExec_t graph_inout = nullptr;
   cudaEvent_t up_ev[8] = {};
   cudaEvent_t exch_ev = nullptr;
+  // its copies of whole zone arrays by the copy engines: a device image of
+  // the caller's buffer, one H2D and one D2H stream, per-group events
+  double* io_image = nullptr;
+  size_t io_image_elems = 0;
+  cudaStream_t io_h2d = nullptr, io_d2h = nullptr;
+  cudaEvent_t dma_ev[8] = {}, conv_ev[8] = {};
   cudaStream_t graph_stream = nullptr;
   cudaStream_t aux_stream = nullptr;   // graph replay when the handle's stream is the legacy one
   cudaEvent_t fence[2] = {nullptr, nullptr};
@@ -387,21 +393,27 @@ int64_t ref_elems(int kind, int field, const ZoneDev& z) {
 
 // Zones into ngroups groups of near-equal point counts (largest zone first
 // into the lightest group).
+// Zone groups are runs of consecutive zones with about equal point counts, so
+// that each group's host arrays are one contiguous range of the caller's
+// buffer (npbmz_step_inout moves a group with one copy each way).  Group g
+// starts at the first zone whose prefix holds g/G of the points, and every
+// group keeps at least one zone.
 void assign_zone_groups(npbmz_t* h) {
   const int nz = h->nzones;
   const int G = std::max(1, std::min(h->ngroups, nz));
   h->ngroups = G;
-  std::vector<int> order(nz);
-  std::iota(order.begin(), order.end(), 0);
-  auto npts = [&](int z) { return (int64_t)h->zh[z].nx * h->zh[z].ny * h->zh[z].nz; };
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return npts(a) > npts(b); });
-  std::vector<int64_t> load(G, 0);
-  h->zone_group.assign(nz, 0);
-  for (int z : order) {
-    const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    h->zone_group[z] = g;
-    load[g] += npts(z);
+  std::vector<int64_t> cum(nz + 1, 0);
+  for (int z = 0; z < nz; ++z) cum[z + 1] = cum[z] + (int64_t)h->zh[z].nx * h->zh[z].ny * h->zh[z].nz;
+  std::vector<int> start(G + 1, 0);
+  start[G] = nz;
+  for (int g = 1; g < G; ++g) {
+    int z = start[g - 1] + 1;
+    while (z < nz - (G - g) && cum[z] * G < cum[nz] * g) ++z;
+    start[g] = z;
   }
+  h->zone_group.assign(nz, 0);
+  for (int g = 0; g < G; ++g)
+    for (int z = start[g]; z < start[g + 1]; ++z) h->zone_group[z] = g;
 }
 
 // Zones group-major, each group's zones by decreasing key (the longest work
@@ -1640,38 +1652,80 @@ int npbmz_step_inout(npbmz_t* h, int nsteps, int layout, const double* host_in, 
   if (!h->graph_inout || h->graph_stream != h->stream)
     if (capture_step_graph(h, true)) return -1;
   if (flush_boundary(h)) return -1;
-  if (!h->io_stream) CK(h, cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
-  if (!h->io_done) CK(h, cudaEventCreateWithFlags(&h->io_done, cudaEventDisableTiming));
-  if (!h->exch_ev) CK(h, cudaEventCreateWithFlags(&h->exch_ev, cudaEventDisableTiming));
+  const std::vector<int64_t>& soh = h->soff_h[layout][NPBMZ_U];
+  const size_t img = (size_t)soh[h->nzones];
+  if (h->io_image_elems < img) {
+    if (h->io_image) { cudaFree(h->io_image); h->device_bytes -= (int64_t)h->io_image_elems * 8; }
+    h->io_image = nullptr;
+    h->io_image_elems = 0;
+    CK(h, cudaMalloc((void**)&h->io_image, img * sizeof(double)));
+    h->io_image_elems = img;
+    h->device_bytes += (int64_t)img * 8;
+  }
+  for (cudaStream_t* st : {&h->io_stream, &h->io_h2d, &h->io_d2h})
+    if (!*st) CK(h, cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&h->io_done, &h->exch_ev})
+    if (!*e) CK(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  for (int g = 0; g < h->ngroups; ++g) {
+    if (!h->dma_ev[g]) CK(h, cudaEventCreateWithFlags(&h->dma_ev[g], cudaEventDisableTiming));
+    if (!h->conv_ev[g]) CK(h, cudaEventCreateWithFlags(&h->conv_ev[g], cudaEventDisableTiming));
+  }
   const Fields F = fields(h);
   const int64_t* so = h->soff_d[layout][NPBMZ_U];
+  // zone groups are runs of consecutive zones: group g's arrays are
+  // [soh[z0], soh[z1]) of the caller's buffer and of the device image
+  auto span = [&](int g, int64_t& off, size_t& bytes) {
+    const int z0 = h->grp_zone_off[g], z1 = h->grp_zone_off[g + 1];
+    off = soh[z0];
+    bytes = (size_t)(soh[z1] - soh[z0]) * sizeof(double);
+  };
   if (health_begin(h)) return -1;
-  // 1. the planes exch_qbc reads, of every zone, then exch_qbc itself
+  // 1. the planes exch_qbc reads, of every zone, straight from host memory,
+  //    then exch_qbc; meanwhile the copy engine brings the zone arrays in
+  for (int g = 0; g < h->ngroups; ++g) {
+    int64_t off;
+    size_t bytes;
+    span(g, off, bytes);
+    CK(h, cudaMemcpyAsync(h->io_image + off, host_in + off, bytes, cudaMemcpyHostToDevice, h->io_h2d));
+    CK(h, cudaEventRecord(h->dma_ev[g], h->io_h2d));
+  }
   launch_convert(F, h->u, din, so, 0, 0, h->nzones, h->max_np, h->kind, NPBMZ_U, layout, 0, h->stream, nullptr, 1);
   CKL(h);
   if (phase_exch(h)) return -1;
   CK(h, cudaEventRecord(h->exch_ev, h->stream));
-  // 2. the rest of each zone group's points on io_stream, group by group; the
-  //    first step's graph starts each group's branch when its part is in
+  // 2. each group's other points from the device image once its copy is in
   CK(h, cudaStreamWaitEvent(h->io_stream, h->exch_ev, 0));
   for (int g = 0; g < h->ngroups; ++g) {
     const int z0 = h->grp_zone_off[g], nz = h->grp_zone_off[g + 1] - z0;
-    launch_convert(F, h->u, din, so, 0, 0, nz, h->max_np, h->kind, NPBMZ_U, layout, 0, h->io_stream,
-                   h->grp_zones_d + z0, 2);
+    CK(h, cudaStreamWaitEvent(h->io_stream, h->dma_ev[g], 0));
+    launch_convert(F, h->u, h->io_image, so, 0, z0, nz, h->max_np, h->kind, NPBMZ_U, layout, 0, h->io_stream,
+                   nullptr, 2);
     CKL(h);
     CK(h, cudaEventRecord(h->up_ev[g], h->io_stream));
   }
   CK(h, cudaGraphLaunch(h->graph_inout, h->stream));
   if (nsteps > 1 && replay_graph(h, nsteps - 1)) return -1;
-  // 3. each group's zones out as soon as the last step's z sweep is done
+  // 3. each group out when its last z sweep is done: interior points into the
+  //    device image (which holds the caller's halo from the copy in), then the
+  //    group's arrays back by the copy engine -- in place only; into another
+  //    buffer the points go straight to host memory (its halo is not ours)
+  const bool in_place = host_out == host_in || layout == NPBMZ_LAYOUT_DENSE;
   for (int g = 0; g < h->ngroups; ++g) {
     const int z0 = h->grp_zone_off[g], nz = h->grp_zone_off[g + 1] - z0;
     CK(h, cudaStreamWaitEvent(h->io_stream, h->grp_out_ev[g], 0));
-    launch_convert(F, h->u, dout, so, 0, 0, nz, h->max_np, h->kind, NPBMZ_U, layout, 1, h->io_stream,
-                   h->grp_zones_d + z0);
+    launch_convert(F, h->u, in_place ? h->io_image : dout, so, 0, z0, nz, h->max_np, h->kind, NPBMZ_U, layout, 1,
+                   h->io_stream);
     CKL(h);
+    if (in_place) {
+      CK(h, cudaEventRecord(h->conv_ev[g], h->io_stream));
+      int64_t off;
+      size_t bytes;
+      span(g, off, bytes);
+      CK(h, cudaStreamWaitEvent(h->io_d2h, h->conv_ev[g], 0));
+      CK(h, cudaMemcpyAsync(host_out + off, h->io_image + off, bytes, cudaMemcpyDeviceToHost, h->io_d2h));
+    }
   }
-  CK(h, cudaEventRecord(h->io_done, h->io_stream));
+  CK(h, cudaEventRecord(h->io_done, in_place ? h->io_d2h : h->io_stream));
   if (health_read(h)) return -1;
   CK(h, cudaStreamWaitEvent(h->stream, h->io_done, 0));
   CK(h, cudaStreamSynchronize(h->stream));
@@ -2109,6 +2163,13 @@ int npbmz_destroy(npbmz_t* h) {
   for (cudaEvent_t e : h->up_ev)
     if (e) cudaEventDestroy(e);
   if (h->exch_ev) cudaEventDestroy(h->exch_ev);
+  for (cudaStream_t st : {h->io_h2d, h->io_d2h})
+    if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+  for (int g = 0; g < 8; ++g) {
+    if (h->dma_ev[g]) cudaEventDestroy(h->dma_ev[g]);
+    if (h->conv_ev[g]) cudaEventDestroy(h->conv_ev[g]);
+  }
+  if (h->io_image) cudaFree(h->io_image);
   if (h->grp_zones_d) cudaFree(h->grp_zones_d);
   if (h->health_d) cudaFree(h->health_d);
   if (h->send_faces_d) cudaFree(h->send_faces_d);
