@@ -109,8 +109,24 @@ int npbmz_lu_ssor(npbmz_lu_t* h, int zone);
 /* niter iterations of the time loop body (src/LU/lu-node.jl:233-270):
  * exch_qbc over all zones, then ssor of every zone.  rsdnm (nullable)
  * receives 5 doubles per iteration: the l2norm of rsd after that
- * iteration, summed over zones (src/LU/l2norm.jl). */
+ * iteration, summed over zones (src/LU/l2norm.jl).  Synchronous.  State
+ * check: every iteration's update tests the points it writes; a density
+ * that is not positive and finite, or a non-finite value, makes the call
+ * return NPBMZ_LU_ERR_STATE after its iterations, with the first bad point
+ * in npbmz_lu_last_error; a non-positive pressure-like quantity
+ * u5 - (u2^2 + u3^2 + u4^2) / (2 u1) is only reported (npbmz_lu_state_check):
+ * LU takes no root of it and the reference carries such a state on. */
+#define NPBMZ_LU_ERR_STATE (-3)
 int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm);
+
+/* What the state check of the last npbmz_lu_iterate found: bits =
+ * NPBMZ_LU_STATE_* (0 when healthy) and the first bad point's zone and
+ * 0-based (i, j, k) of the dense layout (all -1 when none); nullable.  No
+ * counterpart in the reference. */
+#define NPBMZ_LU_STATE_DENSITY 1
+#define NPBMZ_LU_STATE_PRESSURE 2
+#define NPBMZ_LU_STATE_NONFINITE 4
+int npbmz_lu_state_check(npbmz_lu_t* h, int* bits, int* zone, int* i, int* j, int* k);
 
 /* The end-of-run norms of lu-node.jl:306-321, summed over zones: xcr (l2norm
  * of rsd), xce (error against exact), xci (pintgr surface integral).

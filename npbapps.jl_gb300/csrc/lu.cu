@@ -99,6 +99,11 @@ struct npbmz_lu_handle {
   cudaStream_t own = nullptr, stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   CeTable ce{};
+  // state check of npbmz_lu_iterate (LuDev::health) and its page-locked copy
+  unsigned long long* health_d = nullptr;
+  unsigned long long* health_h = nullptr;
+  unsigned health_bits = 0;
+  long long health_point = -1;
   std::string err;
   std::mutex mu;
 };
@@ -126,7 +131,21 @@ int fail(npbmz_lu_t* h, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(h, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
 
-LuDev dev(npbmz_lu_t* h) { return LuDev{h->u, h->rsd, h->frct, h->prim, h->NP, h->zones_d, h->dt, h->omega}; }
+LuDev dev(npbmz_lu_t* h) {
+  return LuDev{h->u, h->rsd, h->frct, h->prim, h->NP, h->zones_d, h->dt, h->omega, h->health_d};
+}
+
+// zone and 0-based (i, j, k) of point index p (LU's interior indexing: pidx)
+void lu_point(const npbmz_lu_t* h, long long p, int* zone, int* i, int* j, int* k) {
+  int z = 0;
+  while (z + 1 < h->nzones && h->zh[z + 1].off <= p) ++z;
+  const LuZone& Z = h->zh[z];
+  const long long q = p - Z.off;
+  *zone = z;
+  *i = (int)(q % Z.nx);
+  *j = (int)((q / Z.nx) % Z.ny);
+  *k = (int)(q / ((long long)Z.nx * Z.ny));
+}
 
 Faces faces(npbmz_lu_t* h) { return Faces{h->stage, h->zoff_d, h->nbr_d, h->klo, h->nkp}; }
 
@@ -345,8 +364,10 @@ void free_all(npbmz_lu_t* h) {
   for (void* p : {(void*)h->zones_d, (void*)h->nbr_d, (void*)h->u, (void*)h->rsd, (void*)h->frct, (void*)h->prim,
                   (void*)h->fac, (void*)h->work_d,
                   (void*)h->zblock_d, (void*)h->partial, (void*)h->norms_d, (void*)h->zone_out_d, (void*)h->stage,
-                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d, (void*)h->ri_d, (void*)h->fb_d})
+                  (void*)h->zoff_d, (void*)h->img, (void*)h->hps_d, (void*)h->ri_d, (void*)h->fb_d,
+                  (void*)h->health_d})
     if (p) cudaFree(p);
+  if (h->health_h) cudaFreeHost(h->health_h);
   if (h->own) cudaStreamDestroy(h->own);
 }
 
@@ -573,7 +594,8 @@ int npbmz_lu_create(int nzones, const int* nx, const int* ny, const int* nz, con
       cudaMalloc(&h->zone_out_d, (6 * (size_t)nzones + 16) * sizeof(double)) ||
       cudaMalloc(&h->stage, so * sizeof(double)) || cudaMalloc(&h->zoff_d, nzones * sizeof(long long)) ||
       cudaMalloc(&h->hps_d, hps.size() * sizeof(int)) || cudaMalloc(&h->ri_d, ri.size() * sizeof(int)) ||
-      cudaMalloc(&h->fb_d, fb.size() * sizeof(int)))
+      cudaMalloc(&h->fb_d, fb.size() * sizeof(int)) || cudaMalloc(&h->health_d, 2 * sizeof(unsigned long long)) ||
+      cudaMallocHost(&h->health_h, 2 * sizeof(unsigned long long)))
     return bail("device allocation failed");
   if (cudaMemcpy(h->zones_d, h->zh.data(), nzones * sizeof(LuZone), cudaMemcpyHostToDevice) ||
       cudaMemcpy(h->nbr_d, h->nbr.data(), 4 * nzones * sizeof(int), cudaMemcpyHostToDevice) ||
@@ -647,6 +669,8 @@ int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
   if (!h) return fail(nullptr, "null handle");
   std::lock_guard<std::mutex> g(h->mu);
   if (niter < 0) return fail(h, "niter < 0");
+  LU_CK(h, cudaMemsetAsync(h->health_d, 0, sizeof(unsigned long long), h->stream));
+  LU_CK(h, cudaMemsetAsync(h->health_d + 1, 0xFF, sizeof(unsigned long long), h->stream));
   if (rsdnm && niter > h->norms_cap) {
     if (h->norms_d) cudaFree(h->norms_d);
     h->norms_d = nullptr;
@@ -677,11 +701,39 @@ int npbmz_lu_iterate(npbmz_lu_t* h, int niter, double* rsdnm) {
     }
     if (rsdnm && launch_rsd_norm(h, h->norms_d + 5 * (size_t)it)) return -1;
   }
-  if (rsdnm && niter > 0) {
+  if (rsdnm && niter > 0)
     LU_CK(h, cudaMemcpyAsync(rsdnm, h->norms_d, (size_t)5 * niter * sizeof(double), cudaMemcpyDeviceToHost,
                              h->stream));
-    LU_CK(h, cudaStreamSynchronize(h->stream));
+  LU_CK(h, cudaMemcpyAsync(h->health_h, h->health_d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           h->stream));
+  LU_CK(h, cudaStreamSynchronize(h->stream));
+  // every iteration's update checks the points it writes; a non-positive or
+  // non-finite density or a non-finite value fails the call (LU takes no
+  // square root of the pressure, so a non-positive one is only reported)
+  h->health_bits = (unsigned)h->health_h[0];
+  h->health_point = h->health_bits ? (long long)h->health_h[1] : -1;
+  if (h->health_bits & (LU_STATE_DENSITY | LU_STATE_NONFINITE)) {
+    int z, i, j, k;
+    lu_point(h, h->health_point, &z, &i, &j, &k);
+    fail(h, "state check failed after the iterations: %s%s%s in u; first bad point zone %d (i, j, k) = (%d, %d, %d)",
+         (h->health_bits & LU_STATE_DENSITY) ? "non-positive or non-finite density" : "",
+         (h->health_bits & LU_STATE_DENSITY) && (h->health_bits & LU_STATE_NONFINITE) ? " and " : "",
+         (h->health_bits & LU_STATE_NONFINITE) ? "a non-finite value" : "", z, i, j, k);
+    return NPBMZ_LU_ERR_STATE;
   }
+  return 0;
+}
+
+int npbmz_lu_state_check(npbmz_lu_t* h, int* bits, int* zone, int* i, int* j, int* k) {
+  if (!h || !bits) return fail(h, "null argument");
+  std::lock_guard<std::mutex> g(h->mu);
+  *bits = (int)h->health_bits;
+  int z = -1, ii = -1, jj = -1, kk = -1;
+  if (h->health_bits) lu_point(h, h->health_point, &z, &ii, &jj, &kk);
+  if (zone) *zone = z;
+  if (i) *i = ii;
+  if (j) *j = jj;
+  if (k) *k = kk;
   return 0;
 }
 

@@ -301,7 +301,24 @@ __global__ void __launch_bounds__(TPB) k_lu_pointwise(LuDev D, const LuWork* __r
       g[m] = D.u[m * D.NP + p] + tmp * D.rsd[m * D.NP + p];
       D.u[m * D.NP + p] = g[m];
     }
-    store_prim(D.prim, D.NP, p, g);
+    double pr[PR_COUNT];
+    prim_point(g, pr);
+#pragma unroll
+    for (int q = 0; q < PR_COUNT; ++q) D.prim[q * D.NP + p] = pr[q];
+    if (D.health) {
+      // on the bit patterns (integer pipe): positive and finite
+      const double pres = g[4] - pr[PR_Q];
+      const unsigned long long br = (unsigned long long)__double_as_longlong(g[0]);
+      const unsigned long long bp = (unsigned long long)__double_as_longlong(pres);
+      const bool rho_ok = br - 1ull < 0x7FEFFFFFFFFFFFFFull, p_ok = bp - 1ull < 0x7FEFFFFFFFFFFFFFull;
+      if (!(rho_ok && p_ok)) {
+        const bool p_finite = (bp & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+        const unsigned bits = (rho_ok ? 0u : LU_STATE_DENSITY) |
+                              (p_ok ? 0u : p_finite ? LU_STATE_PRESSURE : LU_STATE_NONFINITE);
+        atomicOr(D.health, (unsigned long long)bits);
+        atomicMin(D.health + 1, (unsigned long long)p);
+      }
+    }
   } else {
 #pragma unroll
     for (int m = 0; m < 5; ++m) D.rsd[m * D.NP + p] = D.dt * D.rsd[m * D.NP + p];

@@ -34,7 +34,15 @@ struct LuDev {
   long long NP;
   const LuZone* zones;
   double dt, omega;
+  // state check of the update (null: off): word 0 ORs LU_STATE_* bits of every
+  // point found bad, word 1 keeps the smallest such point index
+  unsigned long long* health = nullptr;
 };
+
+// The state check's bits: the density is not positive and finite; the
+// pressure-like quantity u5 - (u2^2 + u3^2 + u4^2) / (2 u1) is finite but not
+// positive; it is not finite (a NaN or an infinity in u).
+constexpr unsigned LU_STATE_DENSITY = 1u, LU_STATE_PRESSURE = 2u, LU_STATE_NONFINITE = 4u;
 
 struct LuWork {  // one block of TPB consecutive points of one zone
   int zone, first;

@@ -17,8 +17,10 @@ LU_EXPORTS = [
     "npbmz_lu_zone_setup", "npbmz_lu_create", "npbmz_lu_setup", "npbmz_lu_upload", "npbmz_lu_download",
     "npbmz_lu_exch_qbc", "npbmz_lu_ssor", "npbmz_lu_iterate", "npbmz_lu_verify", "npbmz_lu_phase",
     "npbmz_lu_set_stream", "npbmz_lu_synchronize", "npbmz_lu_launches_per_iteration", "npbmz_lu_profile",
-    "npbmz_lu_last_error", "npbmz_lu_destroy",
+    "npbmz_lu_last_error", "npbmz_lu_destroy", "npbmz_lu_state_check",
 ]
+ERR_STATE = -3  # NPBMZ_LU_ERR_STATE
+STATE_DENSITY, STATE_PRESSURE, STATE_NONFINITE = 1, 2, 4
 
 # flags, fields and phases (include/npbmz_lu.h)
 FACES_NPB = 0x1
@@ -57,6 +59,7 @@ def lib():
         L.npbmz_lu_last_error.argtypes = [vp]
         L.npbmz_lu_last_error.restype = ctypes.c_char_p
         L.npbmz_lu_destroy.argtypes = [vp]
+        L.npbmz_lu_state_check.argtypes = [vp] + [ip] * 5
         _typed = True
     return L
 
@@ -118,7 +121,13 @@ class LuProblem:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise NpbmzError(f"{what}: " + lib().npbmz_lu_last_error(self._h).decode())
+            raise NpbmzError(f"{what}: " + lib().npbmz_lu_last_error(self._h).decode(), rc)
+
+    def state_check(self):
+        """(bits, (zone, i, j, k)) of the last iterate call's state check."""
+        v = [ctypes.c_int(0) for _ in range(5)]
+        self._check(lib().npbmz_lu_state_check(self._h, *[ctypes.byref(x) for x in v]), "state_check")
+        return v[0].value, tuple(x.value for x in v[1:])
 
     @property
     def points(self):

@@ -306,3 +306,33 @@ def test_page_locked_transfers_match_pageable(layout):
     assert L.npbmz_lu_upload(p._h, -1, lu.U, layout, pinned.data_ptr()) == 0
     for z in range(p.nzones):
         np.testing.assert_array_equal(p.download(z, lu.U), r.get(lu.U, z) * 1.5)
+
+
+@pytest.mark.parametrize("flags", [0, lu.GRAPH, lu.GRAPH | lu.FMA], ids=["direct", "graph", "fma-graph"])
+@pytest.mark.parametrize("m,value,bit,fatal", [(2, float("nan"), lu.STATE_NONFINITE, True),
+                                               (0, -0.5, lu.STATE_DENSITY, True),
+                                               (4, 1e-3, lu.STATE_PRESSURE, False)],
+                         ids=["nan-momentum", "negative-density", "low-energy"])
+def test_state_check_reports_a_planted_point(flags, m, value, bit, fatal):
+    """Each iteration's update tests the points it writes: a non-finite value
+    or a density that is not positive fails npbmz_lu_iterate with
+    NPBMZ_LU_ERR_STATE; a non-positive pressure is only reported by
+    npbmz_lu_state_check (LU never takes its root).  Planted from the host
+    into one interior point of zone 1; a healthy run reports nothing."""
+    g, dt = GEOMS["S"]
+    p, _ = make(g(), dt, flags)
+    p.iterate(2)
+    assert p.state_check() == (0, (-1, -1, -1, -1))
+    u = p.download(1, lu.U)
+    u[m, 2, 3, 3] = value
+    p.upload(1, lu.U, u)
+    if fatal:
+        with pytest.raises(npbmz.NpbmzError) as e:
+            p.iterate(1)
+        assert e.value.code == lu.ERR_STATE and "state check failed" in str(e.value)
+    else:
+        p.iterate(1)
+    bits, (zone, i, j, k) = p.state_check()
+    assert bits & bit and zone == 1
+    if bit == lu.STATE_PRESSURE:
+        assert (i, j, k) == (3, 3, 2)
