@@ -289,12 +289,11 @@ int npbmz_synchronize(npbmz_t* h);
  * Synchronous.  No counterpart in the reference. */
 int npbmz_autotune(npbmz_t* h);
 
-/* The FP64 reciprocal (which = 0), reciprocal square root (1) and square
- * root (2) that the FMA build's primitive kernel uses instead of the IEEE
- * divide and square root (Newton-Raphson refinement of the FP32 hardware
- * estimate), applied on the current device to x[0..n) (host) into y
- * (host).  For the library's tests, which hold them to their error bound.
- * No counterpart in the reference.  Synchronous. */
+/* The FP64 reciprocal (which = 0, the only one) that the FMA build's
+ * primitive kernel uses for 1/rho instead of the IEEE divide (Newton-Raphson
+ * refinement of the FP32 hardware estimate), applied on the current device
+ * to x[0..n) (host) into y (host).  For the library's tests, which hold it to
+ * its error bound.  No counterpart in the reference.  Synchronous. */
 int npbmz_math_check(int which, int n, const double* x, double* y);
 
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (an FMA

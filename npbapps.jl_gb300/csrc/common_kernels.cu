@@ -426,13 +426,12 @@ void launch_faces(bool pack, const Fields& F, const FaceDesc* faces, int nfaces,
   else k_faces<false><<<grid, 256, 0, s>>>(F, faces, buf);
 }
 
-// The FMA build's FP64 reciprocal (which 0), reciprocal square root (1) and
-// square root (2) of npbmz_internal.cuh, for npbmz_math_check.
+// The FMA build's FP64 reciprocal (nr_rcp of npbmz_internal.cuh), for
+// npbmz_math_check.
 __global__ void k_math_check(int which, int n, const double* __restrict__ x, double* __restrict__ y) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const double v = x[t];
-  y[t] = which == 0 ? nr_rcp(v) : which == 1 ? nr_rsqrt(v) : nr_sqrt_from_rsqrt(v, nr_rsqrt(v));
+  if (t >= n || which != 0) return;
+  y[t] = nr_rcp(x[t]);
 }
 
 void launch_math_check(int which, int n, const double* x, double* y, cudaStream_t s) {

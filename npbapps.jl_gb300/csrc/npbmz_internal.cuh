@@ -246,17 +246,17 @@ __device__ __forceinline__ void split_df(double v, float& hi, float& lo) {
   lo = sign ? -mag : mag;
 }
 
-// ---- FP64 reciprocal and reciprocal square root without an FP64 divide ------
+// ---- FP64 reciprocal without an FP64 divide ------------------------------------
 // Newton-Raphson refinement of the FP32 hardware estimate (the method of
 // P. Markstein, "Computation of elementary functions on the IBM RISC
 // System/6000 processor", IBM J. Res. Dev. 34(1), 1990): the estimate is taken
 // of x's leading 24 bits, the operands move between the formats by bit
 // manipulation (integer pipe; a conversion instruction would take the FP64
 // pipe), and each FP64 FMA step squares the relative error -- about 2^-22 for
-// the estimate, 2^-44 after one step, a few ulps after the second.  Used by
-// the FMA build's primitive kernel, where the IEEE divide and square root
-// cost most of its FP64 instructions.  Positive x inside the FP32 normal
-// range only; anything else takes the IEEE operation.
+// the estimate, 2^-44 after one step, within 2 ulps after the second.  Used
+// for 1/rho by the FMA build's primitive kernel, where the IEEE divide cost a
+// large share of its FP64 instructions.  Positive x inside the FP32 normal
+// range only; anything else takes the IEEE divide.
 __device__ __forceinline__ bool f64_to_f32_bits(double x, float& xf) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ffull) - 1023;
@@ -280,23 +280,6 @@ __device__ __forceinline__ double nr_rcp(double x) {
   y = fma(y, e, y);
   e = fma(-x, y, 1.0);
   return fma(y, e, y);
-}
-
-__device__ __forceinline__ double nr_rsqrt(double x) {
-  float xf, yf;
-  if (!f64_to_f32_bits(x, xf)) return 1.0 / sqrt(x);
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
-  double y = f32_to_f64_bits(yf);
-  const double hx = 0.5 * x;
-#pragma unroll
-  for (int it = 0; it < 2; ++it) y = fma(y, fma(-hx, y * y, 0.5), y);  // y (1 + (1 - x y^2) / 2)
-  return y;
-}
-
-// sqrt(x) from y = nr_rsqrt(x): s = x y, corrected once by s + y (x - s^2) / 2.
-__device__ __forceinline__ double nr_sqrt_from_rsqrt(double x, double y) {
-  const double s = x * y;
-  return fma(0.5 * y, fma(-s, s, x), s);
 }
 
 // Lines per sweep direction of a zone (interior transverse indices only).

@@ -549,7 +549,7 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
     } else {  // tzetar in FP64, then add
       double r[5];
 #pragma unroll
-      for (int m = 0; m < 5; ++m) r[m] = (double)*S(slot, 11 + m) + (double)d[m];
+      for (int m = 0; m < 5; ++m) r[m] = f32_to_f64(*S(slot, 11 + m)) + f32_to_f64(d[m]);  // exact, by bits
       const double xvel = *SU(slot, 5), yvel = *SU(slot, 6), zvel = *SU(slot, 7);
       const double ac = *SU(slot, 8), acinv = *SU(slot, 9), qs = *SU(slot, 10);
       const double ac2u = ac * ac;

@@ -47,16 +47,13 @@ __device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int
     F.prim[PR_QS * NP + p] = square * rho_inv;
     if (SP) {
       const double u5 = F.u[4 * NP + p];
+      // IEEE square root and divide in both builds: the speed of sound enters
+      // the SP adjoint's finite-difference checks, which a few-ulp estimate
+      // makes noisy (1/rho above stays on the Newton-Raphson estimate)
       double aux = K.c1c2 * rho_inv * (u5 - square);
-#if NPBMZ_HAS_FP32
-      const double ainv = nr_rsqrt(aux);
-      F.prim[PR_SPEED * NP + p] = nr_sqrt_from_rsqrt(aux, ainv);
-      F.prim[PR_AINV * NP + p] = ainv;
-#else
       aux = sqrt(aux);
       F.prim[PR_SPEED * NP + p] = aux;
       F.prim[PR_AINV * NP + p] = 1.0e0 / aux;
-#endif
     }
     if (SP && F.primf) {
       const double v[PS_HI_COUNT] = {rho_inv, u2 * rho_inv, u3 * rho_inv, u4 * rho_inv, F.prim[PR_SPEED * NP + p]};
@@ -1814,7 +1811,8 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
         o[0] = v.hi;
         o[lo_off] = v.lo;
       } else {
-        const double v = (double)xv + (double)d[m];
+        // exact FP32 -> FP64 by bits (a conversion instruction takes the FP64 pipe)
+        const double v = f32_to_f64(xv) + f32_to_f64(d[m]);
         rhs[m * NP + pt] = v;
         if (add_u) F.u[m * NP + pt] = *SU(slot, m) + v;
       }

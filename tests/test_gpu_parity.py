@@ -526,15 +526,12 @@ def test_bt_class_b_autotuned_launch_shapes_keep_results(oracle_mod, flags):
         np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
 
 
-@pytest.mark.parametrize("which,ulps", [(0, 2), (1, 3), (2, 2)], ids=["rcp", "rsqrt", "sqrt"])
-def test_fma_build_reciprocal_and_square_root_error_bound(which, ulps):
-    """The FMA build's primitive kernel takes 1/rho and the SP speed of sound
-    and its reciprocal by Newton-Raphson refinement of the FP32 hardware
-    estimates (npbmz_math_check runs the same device functions).  Against
-    numpy's FP64 values (1/x and sqrt correctly rounded, 1/sqrt(x) rounded
-    twice) they stay within 2, 3 and 2 ulps over the range the state takes
-    and far beyond it; outside the FP32 range they fall back to the IEEE
-    operations."""
+def test_fma_build_reciprocal_error_bound():
+    """The FMA build's primitive kernel takes 1/rho by Newton-Raphson
+    refinement of the FP32 hardware estimate (npbmz_math_check runs the same
+    device function).  Against numpy's correctly rounded 1/x it stays within
+    2 ulps over the range the state takes and far beyond it; outside the FP32
+    range it falls back to the IEEE divide."""
     import ctypes
 
     rng = np.random.default_rng(17)
@@ -542,7 +539,7 @@ def test_fma_build_reciprocal_and_square_root_error_bound(which, ulps):
                         np.array([1.0, 2.0, 0.5, 3.0, 1e-37, 1e37, 1e-300, 1e300, 7.0, 1.0 - 2 ** -52])])
     y = np.zeros_like(x)
     dp = ctypes.POINTER(ctypes.c_double)
-    assert npbmz.lib().npbmz_math_check(which, len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp)) == 0
-    want = 1.0 / x if which == 0 else 1.0 / np.sqrt(x) if which == 1 else np.sqrt(x)
+    assert npbmz.lib().npbmz_math_check(0, len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp)) == 0
+    want = 1.0 / x
     err_ulps = np.abs(y - want) / np.spacing(want)
-    assert np.max(err_ulps) <= ulps, (np.max(err_ulps), x[np.argmax(err_ulps)])
+    assert np.max(err_ulps) <= 2, (np.max(err_ulps), x[np.argmax(err_ulps)])
