@@ -9,11 +9,11 @@
 //           FP32 pairs of the state, L d = r in FP32, x = x0 + d,
 // so that no FP64 arithmetic runs except in the z sweep's output: add
 // (src/SP/add.jl:14-23) in FP64, after tzetar (src/SP/tzetar.jl:27-52) in
-// double-float, from the FP64 primitives split exactly by bits or from the
-// double-float ones of the double-float compute_rhs (NPBMZ_RHS_DF).  The x
-// and y sweeps hand their transformed results (ninvr, src/SP/ninvr.jl:19-32;
-// pinvr, src/SP/pinvr.jl:20-33, applied in double-float) to the next sweep
-// as double-float planes.  Each thread streams its line's data PIPE points ahead
+// FP64 from the FP64 primitives, or in double-float from the double-float
+// ones of the double-float compute_rhs (NPBMZ_RHS_DF).  The x and y sweeps hand
+// their transformed results (ninvr, src/SP/ninvr.jl:19-32; pinvr,
+// src/SP/pinvr.jl:20-33, applied in double-float) to the next sweep as
+// double-float planes.  Each thread streams its line's data PIPE points ahead
 // with cp.async into a ring in shared memory, in both passes' forward
 // elimination and back substitution; the x sweep reads its x-line-major copies.
 
@@ -522,22 +522,13 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
         dst[0] = o[m].hi;
         dst[lo_off] = o[m].lo;
       }
-    } else {
-      // tzetar (src/SP/tzetar.jl:27-52) in double-float on the FP32 pipe --
-      // from the double-float primitives of the double-float compute_rhs, or
-      // from the FP64 ones split exactly by bits -- then add in FP64
+    } else if (F.xd) {  // tzetar in double-float, then add in FP64
       df64 r[5];
 #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = df_two_sum(*S(slot, 11 + m), d[m]);
-      df64 xvel, yvel, zvel, ac, acinv, qs, uzik1;
-      if (F.xd) {
-        auto w2 = [&](int e) -> df64 { const float* q = reinterpret_cast<const float*>(SU(slot, e)); return {q[0], q[1]}; };
-        xvel = w2(5); yvel = w2(6); zvel = w2(7); ac = w2(8); qs = w2(9); uzik1 = w2(10);
-        acinv = df_rcp(ac);
-      } else {
-        auto sp = [&](int e) -> df64 { df64 v; split_df(*SU(slot, e), v.hi, v.lo); return v; };
-        xvel = sp(5); yvel = sp(6); zvel = sp(7); ac = sp(8); acinv = sp(9); qs = sp(10); uzik1 = sp(0);
-      }
+      auto w2 = [&](int e) -> df64 { const float* q = reinterpret_cast<const float*>(SU(slot, e)); return {q[0], q[1]}; };
+      const df64 xvel = w2(5), yvel = w2(6), zvel = w2(7), ac = w2(8), qs = w2(9), uzik1 = w2(10);
+      const df64 acinv = df_rcp(ac);
       const df64 btuz = df_mul(f2df(K.p_bt), uzik1);
       const df64 t1 = df_mul(df_mul(btuz, acinv), df_add(r[3], r[4]));
       const df64 t2 = df_add(r[2], t1);
@@ -554,6 +545,29 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
         const double v = df_to_double(o[m]);
         F.rhs[m * NP + pt] = v;
         if (add_u) F.u[m * NP + pt] = *SU(slot, m) + v;
+      }
+    } else {  // tzetar in FP64, then add
+      double r[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) r[m] = f32_to_f64(*S(slot, 11 + m)) + f32_to_f64(d[m]);  // exact, by bits
+      const double xvel = *SU(slot, 5), yvel = *SU(slot, 6), zvel = *SU(slot, 7);
+      const double ac = *SU(slot, 8), acinv = *SU(slot, 9), qs = *SU(slot, 10);
+      const double ac2u = ac * ac;
+      const double uzik1 = *SU(slot, 0);
+      const double btuz = K.bt * uzik1;
+      const double t1 = btuz * acinv * (r[3] + r[4]);
+      const double t2 = r[2] + t1;
+      const double t3 = btuz * (r[3] - r[4]);
+      double o[5];
+      o[0] = t2;
+      o[1] = -uzik1 * r[1] + xvel * t2;
+      o[2] = uzik1 * r[0] + yvel * t2;
+      o[3] = zvel * t2 + t3;
+      o[4] = uzik1 * (-xvel * r[1] + yvel * r[0]) + qs * t2 + K.c2iv * ac2u * t1 + zvel * t3;
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        F.rhs[m * NP + pt] = o[m];
+        if (add_u) F.u[m * NP + pt] = *SU(slot, m) + o[m];
       }
     }
   };
