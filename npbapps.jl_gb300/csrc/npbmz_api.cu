@@ -1689,7 +1689,15 @@ int npbmz_step_inout(npbmz_t* h, int nsteps, int layout, const double* host_in, 
   };
   if (health_begin(h)) return -1;
   // 1. the planes exch_qbc reads, of every zone, straight from host memory,
-  //    then exch_qbc; meanwhile the copy engine brings the zone arrays in
+  //    then exch_qbc; the copy engine starts on the zone arrays once those
+  //    planes are in (sharing the link, both would finish late: 0.6 ms for
+  //    the planes instead of 0.18 ms on BT-C)
+  launch_convert(F, h->u, din, so, 0, 0, h->nzones, h->max_np, h->kind, NPBMZ_U, layout, 0, h->stream, nullptr, 1);
+  CKL(h);
+  // (exch_ev is recorded again after exch_qbc below; each wait binds to the
+  // record made before it)
+  CK(h, cudaEventRecord(h->exch_ev, h->stream));
+  CK(h, cudaStreamWaitEvent(h->io_h2d, h->exch_ev, 0));
   for (int g = 0; g < h->ngroups; ++g) {
     int64_t off;
     size_t bytes;
@@ -1697,8 +1705,6 @@ int npbmz_step_inout(npbmz_t* h, int nsteps, int layout, const double* host_in, 
     CK(h, cudaMemcpyAsync(h->io_image + off, host_in + off, bytes, cudaMemcpyHostToDevice, h->io_h2d));
     CK(h, cudaEventRecord(h->dma_ev[g], h->io_h2d));
   }
-  launch_convert(F, h->u, din, so, 0, 0, h->nzones, h->max_np, h->kind, NPBMZ_U, layout, 0, h->stream, nullptr, 1);
-  CKL(h);
   if (phase_exch(h)) return -1;
   CK(h, cudaEventRecord(h->exch_ev, h->stream));
   // 2. each group's other points from the device image once its copy is in
