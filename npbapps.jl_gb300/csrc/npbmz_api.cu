@@ -393,22 +393,27 @@ int64_t ref_elems(int kind, int field, const ZoneDev& z) {
 
 // Zones into ngroups groups of near-equal point counts (largest zone first
 // into the lightest group).
-// Zone groups are runs of consecutive zones with about equal point counts, so
-// that each group's host arrays are one contiguous range of the caller's
-// buffer (npbmz_step_inout moves a group with one copy each way).  Group g
-// starts at the first zone whose prefix holds g/G of the points, and every
-// group keeps at least one zone.
+// Zone groups are runs of consecutive zones, so that each group's host arrays
+// are one contiguous range of the caller's buffer (npbmz_step_inout moves a
+// group with one copy each way).  With 4 or more groups the first and the
+// last hold half the points of the others: the first step of
+// npbmz_step_inout waits for the first group's copy in, and its end for the
+// last group's copy out.  Group g starts at the first zone whose prefix holds
+// its share of the points, and every group keeps at least one zone.
 void assign_zone_groups(npbmz_t* h) {
   const int nz = h->nzones;
   const int G = std::max(1, std::min(h->ngroups, nz));
   h->ngroups = G;
   std::vector<int64_t> cum(nz + 1, 0);
   for (int z = 0; z < nz; ++z) cum[z + 1] = cum[z] + (int64_t)h->zh[z].nx * h->zh[z].ny * h->zh[z].nz;
+  // weights in halves: 1 for the end groups, 2 for the others (G >= 4)
+  std::vector<int64_t> wcum(G + 1, 0);
+  for (int g = 0; g < G; ++g) wcum[g + 1] = wcum[g] + ((G >= 4 && (g == 0 || g == G - 1)) ? 1 : 2);
   std::vector<int> start(G + 1, 0);
   start[G] = nz;
   for (int g = 1; g < G; ++g) {
     int z = start[g - 1] + 1;
-    while (z < nz - (G - g) && cum[z] * G < cum[nz] * g) ++z;
+    while (z < nz - (G - g) && cum[z] * wcum[G] < cum[nz] * wcum[g]) ++z;
     start[g] = z;
   }
   h->zone_group.assign(nz, 0);

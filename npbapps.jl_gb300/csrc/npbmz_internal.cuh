@@ -178,6 +178,21 @@ __device__ __forceinline__ bool finite_bits(float v) { return (__float_as_uint(v
 
 // rho and pressure in FP64, or (the double-float kernels) as the high words
 // of their double-float values
+// The same from the energy e = rho E and k = |rho v|^2 / (2 rho) without
+// forming e - k (an FP64 instruction): for e positive and finite, e - k > 0
+// exactly when e > k, and for k >= 0 that order is the order of the bit
+// patterns; a negative k (negative rho) leaves e - k positive.
+__device__ __forceinline__ void health_check_ek(const Fields& F, int64_t p, double rho, double e, double k) {
+  if (!F.health) return;
+  const long long be = __double_as_longlong(e), bk = __double_as_longlong(k);
+  const bool ok = positive_finite(rho) && positive_finite(e) && finite_bits(k) && (bk < 0 || be > bk);
+  if (__builtin_expect(ok, 1)) return;
+  const bool finite = finite_bits(e) && finite_bits(k);
+  const unsigned bits = (positive_finite(rho) ? 0u : HEALTH_DENSITY) |
+                        (!finite ? HEALTH_NONFINITE : (bk < 0 || (be > bk && be > 0)) ? 0u : HEALTH_PRESSURE);
+  health_report(F, p, bits);
+}
+
 template <typename R>
 __device__ __forceinline__ void health_check(const Fields& F, int64_t p, R rho, R pressure) {
   if (!F.health) return;

@@ -38,7 +38,7 @@ __device__ __forceinline__ void prim_point(const Fields& F, const Consts& K, int
     const double rho_inv = 1.0e0 / u1;
 #endif
     const double square = 0.5e0 * (u2 * u2 + u3 * u3 + u4 * u4) * rho_inv;
-    health_check(F, p, u1, F.u[4 * NP + p] - square);
+    health_check_ek(F, p, u1, F.u[4 * NP + p], square);
     F.prim[PR_RHOI * NP + p] = rho_inv;
     F.prim[PR_US * NP + p] = u2 * rho_inv;
     F.prim[PR_VS * NP + p] = u3 * rho_inv;
