@@ -319,58 +319,51 @@ __global__ void __launch_bounds__(128) k_rhs_df(Fields F, RhsDfConsts C, const W
 // The x sweep gives each thread one x line, so that a warp's lines sit nx
 // points apart in the zone layout; it reads x-line-major copies of the FP32
 // state pairs instead (plane e of point i of line g at [(i * E + e) * nlx +
-// g]).  These kernels move the lines of each x-sweep work item (lpi lines of
-// one zone from `first`) in chunks of 32 lines x XT_W points through a shared
-// tile per plane.  The zone-layout side of a chunk is walked as one flat
-// range of (line, i) pairs -- the interior rows of consecutive lines are
-// adjacent in memory, so those reads or writes are coalesced whatever nx is --
-// and the x-line-major side as 32 consecutive lines per warp access.
-constexpr int XT_W = 64;   // points of a line per tile
-constexpr int XT_PB = 4;   // planes per tile
-
-// zone-layout index of point i of x line l (interior j, k) of zone Z
-__device__ __forceinline__ int64_t xline_point(const ZoneDev& Z, int l, int i) {
-  const int iy = Z.ny - 2;
-  return Z.off + ((int64_t)(1 + l / iy) * Z.ny + 1 + l % iy) * Z.nx + i;
-}
-
+// g]).  This kernel makes them for the lines of each x-sweep work item (lpi
+// lines of one zone from `first`, every point of each line): 32-line x
+// 32-point tiles of PB planes at a time go through shared memory, so that
+// the zone-layout reads (along i) and the x-line-major writes (along g) are
+// both coalesced, with 4 * PB loads in flight per thread.
 template <bool SP>
 __global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __restrict__ work, int nwork, int lpi) {
   constexpr int E = SP ? (int)PS_COUNT : (int)PF_COUNT;
-  __shared__ float tile[XT_PB][32][XT_W + 1];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;  // 8 warps
+  constexpr int PB = E / 2;
+  __shared__ float tile[PB][32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
   const int64_t NP = F.NP;
   for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
     const Work w = work[it];
     const ZoneDev Z = F.zones[w.zone];
     const int l1 = min(w.first + lpi, zone_lines(Z, 0));
-    for (int l0 = w.first; l0 < l1; l0 += 32) {
-      const int nl = min(32, l1 - l0);
-      for (int i0 = 0; i0 < Z.nx; i0 += XT_W) {
-        const int ni = min(XT_W, Z.nx - i0);
+    const int iy = Z.ny - 2;
+    for (int l0 = w.first; l0 < l1; l0 += 32)
+      for (int i0 = 0; i0 < Z.nx; i0 += 32)
 #pragma unroll 1
-        for (int e0 = 0; e0 < E; e0 += XT_PB) {
-          const int pb = min(XT_PB, E - e0);
-          // zone layout -> tile, flat over (line, point) of the chunk
-          for (int f = threadIdx.x; f < nl * ni; f += 256) {
-            const int r = f / ni, c = f - r * ni;
-            const int64_t p = xline_point(Z, l0 + r, i0 + c);
+        for (int e0 = 0; e0 < E; e0 += PB) {
+          float v[PB][4];
 #pragma unroll
-            for (int b = 0; b < XT_PB; ++b)
-              if (b < pb) tile[b][r][c] = F.primf[(int64_t)(e0 + b) * NP + p];
+          for (int r4 = 0; r4 < 4; ++r4) {  // row ty + 8 r4: line l0 + row, column tx: point i0 + tx
+            const int l = l0 + ty + 8 * r4, i = i0 + tx;
+            const bool ok = l < l1 && i < Z.nx;
+            const int64_t p = ok ? Z.off + ((int64_t)(1 + l / iy) * Z.ny + 1 + l % iy) * Z.nx + i : 0;
+#pragma unroll
+            for (int b = 0; b < PB; ++b) v[b][r4] = ok ? F.primf[(int64_t)(e0 + b) * NP + p] : 0.f;
+          }
+#pragma unroll
+          for (int b = 0; b < PB; ++b)
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4) tile[b][ty + 8 * r4][tx] = v[b][r4];
+          __syncthreads();
+#pragma unroll
+          for (int r4 = 0; r4 < 4; ++r4) {  // point i0 + ty + 8 r4 of line l0 + tx
+            const int i = i0 + ty + 8 * r4, l = l0 + tx;
+            if (l < l1 && i < Z.nx)
+#pragma unroll
+              for (int b = 0; b < PB; ++b)
+                F.pfx[((int64_t)i * E + e0 + b) * F.nlx + Z.lineoff[0] + l] = tile[b][tx][ty + 8 * r4];
           }
           __syncthreads();
-          // tile -> x-line-major: warp w takes points w, w + 8, ...; lane = line
-          if (lane < nl)
-            for (int c = wid; c < ni; c += 8)
-#pragma unroll
-              for (int b = 0; b < XT_PB; ++b)
-                if (b < pb)
-                  F.pfx[((int64_t)(i0 + c) * E + e0 + b) * F.nlx + Z.lineoff[0] + l0 + lane] = tile[b][lane][c];
-          __syncthreads();
         }
-      }
-    }
   }
 }
 
@@ -378,41 +371,44 @@ __global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __rest
 // (10 planes, interior points) goes from the x-line-major rdx, where each
 // thread wrote its own line, to the zone-layout rdf that the y sweep reads.
 __global__ void __launch_bounds__(256) k_xline_back(Fields F, const Work* __restrict__ work, int nwork, int lpi) {
-  __shared__ float tile[XT_PB][32][XT_W + 1];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int PB = 5;
+  __shared__ float tile[PB][32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
   const int64_t NP = F.NP;
   for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
     const Work w = work[it];
     const ZoneDev Z = F.zones[w.zone];
     const int l1 = min(w.first + lpi, zone_lines(Z, 0));
-    const int nin = Z.nx - 2;  // interior points 1..nx-2
-    for (int l0 = w.first; l0 < l1; l0 += 32) {
-      const int nl = min(32, l1 - l0);
-      for (int i0 = 0; i0 < nin; i0 += XT_W) {
-        const int ni = min(XT_W, nin - i0);
+    const int iy = Z.ny - 2;
+    for (int l0 = w.first; l0 < l1; l0 += 32)
+      for (int i0 = 1; i0 < Z.nx - 1; i0 += 32)
 #pragma unroll 1
-        for (int e0 = 0; e0 < 10; e0 += XT_PB) {
-          const int pb = min(XT_PB, 10 - e0);
-          // x-line-major -> tile: lane = line, warp w takes points w, w + 8, ...
-          if (lane < nl)
-            for (int c = wid; c < ni; c += 8)
+        for (int e0 = 0; e0 < 10; e0 += PB) {
+          float v[PB][4];
 #pragma unroll
-              for (int b = 0; b < XT_PB; ++b)
-                if (b < pb)
-                  tile[b][lane][c] = F.rdx[((int64_t)(1 + i0 + c) * 10 + e0 + b) * F.nlx + Z.lineoff[0] + l0 + lane];
+          for (int r4 = 0; r4 < 4; ++r4) {  // row ty + 8 r4: point i0 + row, column tx: line l0 + tx
+            const int i = i0 + ty + 8 * r4, l = l0 + tx;
+            const bool ok = l < l1 && i < Z.nx - 1;
+#pragma unroll
+            for (int b = 0; b < PB; ++b)
+              v[b][r4] = ok ? F.rdx[((int64_t)i * 10 + e0 + b) * F.nlx + Z.lineoff[0] + l] : 0.f;
+          }
+#pragma unroll
+          for (int b = 0; b < PB; ++b)
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4) tile[b][ty + 8 * r4][tx] = v[b][r4];
           __syncthreads();
-          // tile -> zone layout, flat over (line, point)
-          for (int f = threadIdx.x; f < nl * ni; f += 256) {
-            const int r = f / ni, c = f - r * ni;
-            const int64_t p = xline_point(Z, l0 + r, 1 + i0 + c);
 #pragma unroll
-            for (int b = 0; b < XT_PB; ++b)
-              if (b < pb) F.rdf[(int64_t)(e0 + b) * NP + p] = tile[b][r][c];
+          for (int r4 = 0; r4 < 4; ++r4) {  // line l0 + ty + 8 r4, point i0 + tx
+            const int l = l0 + ty + 8 * r4, i = i0 + tx;
+            if (l < l1 && i < Z.nx - 1) {
+              const int64_t p = Z.off + ((int64_t)(1 + l / iy) * Z.ny + 1 + l % iy) * Z.nx + i;
+#pragma unroll
+              for (int b = 0; b < PB; ++b) F.rdf[(int64_t)(e0 + b) * NP + p] = tile[b][tx][ty + 8 * r4];
+            }
           }
           __syncthreads();
         }
-      }
-    }
   }
 }
 
