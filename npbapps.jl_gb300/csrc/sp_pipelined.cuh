@@ -235,6 +235,10 @@ __device__ __forceinline__ void sp_mixed_pl_item(const Fields& F, const Consts& 
     }
     cpa_commit();
   };
+  // the ring's first slots go out before the line's first point is read
+  // directly, so that the two memory latencies overlap
+#pragma unroll
+  for (int q = 0; q < PIPE - 1; ++q) issue_fwd(q);
   float gcv[3], grh[3], gsp[3];  // geometry at q-1, q, q+1
   {
     float cv, rh, sp;
@@ -257,8 +261,6 @@ __device__ __forceinline__ void sp_mixed_pl_item(const Fields& F, const Consts& 
     gcv[0] = gcv[1]; grh[0] = grh[1]; gsp[0] = gsp[1];
     gcv[1] = gcv[2]; grh[1] = grh[2]; gsp[1] = gsp[2];
   };
-#pragma unroll
-  for (int q = 0; q < PIPE - 1; ++q) issue_fwd(q);
   SpElim e;
   {
     float L0[3][5], L1[3][5], r0[5], r1[5];
@@ -374,6 +376,10 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
     }
     cpa_commit();
   };
+  // the ring's first slots go out before the line's first points are read
+  // directly, so that the two memory latencies overlap
+#pragma unroll
+  for (int q = 0; q < PIPE - 1; ++q) issue_fwd(q);
   // geometry window (cv, rhon, speed at q-1, q, q+1) and x window (q-2 .. q+2)
   df64 gcv[3], grh[3], gsp[3];
   df64 xw[5][5];
@@ -436,8 +442,6 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
 #pragma unroll
       for (int m = 0; m < 5; ++m) xw[k][m] = xw[k + 1][m];
   };
-#pragma unroll
-  for (int q = 0; q < PIPE - 1; ++q) issue_fwd(q);
   SpElim e;
   {
     float L0[3][5], L1[3][5], r0[5], r1[5];

@@ -1514,7 +1514,10 @@ constexpr int PL_MIXED_W = 30;   // words per slot, first pass
 constexpr int PL_REFINE_W = 35;  // words per slot, refinement pass
 
 // Dynamic shared memory of the pipelined kernels for tpb threads.
-__host__ __device__ constexpr size_t pl_mixed_smem(int tpb) { return (size_t)PIPE * PL_MIXED_W * tpb * sizeof(float); }
+// (the first pass keeps 5 more words per line: b at the line's last point)
+__host__ __device__ constexpr size_t pl_mixed_smem(int tpb) {
+  return (size_t)(PIPE * PL_MIXED_W + 5) * tpb * sizeof(float);
+}
 __host__ __device__ constexpr size_t pl_refine_smem(int tpb, bool out_df) {
   return (size_t)PIPE * 5 * tpb * sizeof(double) * (out_df ? 0 : 1) + (size_t)PIPE * PL_REFINE_W * tpb * sizeof(float);
 }
@@ -1557,6 +1560,13 @@ __device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& 
     }
     cpa_commit();
   };
+  // the ring's first slots (and b at the last point, which the back
+  // substitution starts from) go out before the line's first points are read
+  // directly, so that the memory latencies overlap
+#pragma unroll
+  for (int m = 0; m < 5; ++m) cpa4(S(PIPE, m), b_at(n - 1, m));
+#pragma unroll
+  for (int q = 1; q < PIPE; ++q) issue_fwd(q);
   BtF32Carry<DIR> c;
   {
     float s0[6], s1[6];
@@ -1569,8 +1579,6 @@ __device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& 
     for (int m = 0; m < 5; ++m) c.rp[m] = *b_at(0, m);
     bt_f32_begin<DIR>(K, n, s0, s1, c);
   }
-#pragma unroll
-  for (int q = 1; q < PIPE; ++q) issue_fwd(q);
   for (int p = 1; p <= n - 2; ++p) {
     issue_fwd(p + PIPE - 1);
     cpa_wait<PIPE - 1>();
@@ -1581,12 +1589,24 @@ __device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& 
 #pragma unroll
     for (int m = 0; m < 5; ++m) r[m] = *S(slot, 6 + m);
     bt_f32_step<DIR>(K, p, n, false, r, s, c, scr, nlt, gl);
+    if (p + PIPE > n - 2) {
+      // the ring does not refill this slot: C'_p and r'_p stay here for the
+      // back substitution, which so starts without a trip to memory
+#pragma unroll
+      for (int a = 0; a < 5; ++a)
+#pragma unroll
+        for (int b = 0; b < 5; ++b) *S(slot, a * 5 + b) = c.Cp[a][b];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) *S(slot, 25 + m) = c.rp[m];
+    }
   }
   cpa_wait<0>();
-  // back substitution: step p (n-2 .. 1) consumes C'_p and r'_p
+  // back substitution: step p (n-2 .. 1) consumes C'_p and r'_p from slot
+  // p % PIPE: the last PIPE points as the forward pass left them, the others
+  // loaded PIPE steps ahead into the slot just consumed
   auto issue_bwd = [&](int p) {
     if (p >= 1) {
-      const int slot = (n - 2 - p) % PIPE;
+      const int slot = p % PIPE;
 #pragma unroll
       for (int e = 0; e < 30; ++e) cpa4(S(slot, e), scr + ((int64_t)p * 30 + e) * nlt + gl);
     }
@@ -1594,13 +1614,10 @@ __device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& 
   };
   float rn[5];
 #pragma unroll
-  for (int m = 0; m < 5; ++m) rn[m] = *b_at(n - 1, m);
-#pragma unroll
-  for (int q = 0; q < PIPE - 1; ++q) issue_bwd(n - 2 - q);
+  for (int m = 0; m < 5; ++m) rn[m] = *S(PIPE, m);
   for (int p = n - 2; p >= 1; --p) {
-    issue_bwd(p - (PIPE - 1));
-    cpa_wait<PIPE - 1>();
-    const int slot = (n - 2 - p) % PIPE;
+    if (p + PIPE <= n - 2) cpa_wait<PIPE - 1>();
+    const int slot = p % PIPE;
     float r[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -1614,6 +1631,7 @@ __device__ __forceinline__ void bt_mixed_pl_item(const Fields& F, const Consts& 
       *x0_at(p, m) = r[m];
       rn[m] = r[m];
     }
+    issue_bwd(p - PIPE);
   }
   cpa_wait<0>();
 }
@@ -1709,6 +1727,10 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
     cpa_commit();
   };
 
+  // the ring's first slots go out before the line's first points are read
+  // directly, so that the two memory latencies overlap
+#pragma unroll
+  for (int q = 1; q < PIPE; ++q) issue_fwd(q);
   df64 acc_c[5], acc_n[5], xq[5], sq[6], P[5], Q[5];
   BtF32Carry<DIR> c;
   {
@@ -1734,8 +1756,6 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
     for (int m = 0; m < 5; ++m) c.rp[m] = 0.f;
     bt_f32_begin<DIR>(K, n, s0, s1, c);
   }
-#pragma unroll
-  for (int q = 1; q < PIPE; ++q) issue_fwd(q);
   for (int p = 1; p <= n - 2; ++p) {
     issue_fwd(p + PIPE - 1);
     cpa_wait<PIPE - 1>();
@@ -1765,12 +1785,34 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
 #pragma unroll
     for (int e = 0; e < 6; ++e) s[e] = sq[e].hi;
     bt_f32_step<DIR>(K, p, n, true, r, s, c, scr, nlt, gl);
+    if (p + PIPE > n - 2) {
+      // the ring does not refill this slot: C'_p and r'_p stay here for the
+      // back substitution, x0_p (and u_p) are fetched now, so that it starts
+      // without a trip to memory
+#pragma unroll
+      for (int a = 0; a < 5; ++a)
+#pragma unroll
+        for (int b = 0; b < 5; ++b) *S(slot, a * 5 + b) = c.Cp[a][b];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        *S(slot, 25 + m) = c.rp[m];
+        cpa4(S(slot, 30 + m), x0_at(p, m));
+      }
+      if (!OUT_DF && add_u) {
+        const int64_t pt = base + (int64_t)p * st;
+#pragma unroll
+        for (int m = 0; m < 5; ++m) cpa8(SU(slot, m), F.u + m * NP + pt);
+      }
+      cpa_commit();
+    }
   }
   cpa_wait<0>();
   // back substitution: step p (n-2 .. 1) consumes C'_p, r'_p, x0_p (and u_p)
+  // from slot p % PIPE: the last PIPE points as the forward pass left them,
+  // the others loaded PIPE steps ahead into the slot just consumed
   auto issue_bwd = [&](int p) {
     if (p >= 1) {
-      const int slot = (n - 2 - p) % PIPE;
+      const int slot = p % PIPE;
       const int64_t pt = base + (int64_t)p * st;
 #pragma unroll
       for (int e = 0; e < 30; ++e) cpa4(S(slot, e), scr + ((int64_t)p * 30 + e) * nlt + gl);
@@ -1784,12 +1826,9 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
     cpa_commit();
   };
   float dn[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-  for (int q = 0; q < PIPE - 1; ++q) issue_bwd(n - 2 - q);
   for (int p = n - 2; p >= 1; --p) {
-    issue_bwd(p - (PIPE - 1));
-    cpa_wait<PIPE - 1>();
-    const int slot = (n - 2 - p) % PIPE;
+    if (p + PIPE <= n - 2) cpa_wait<PIPE - 1>();
+    const int slot = p % PIPE;
     const int64_t pt = base + (int64_t)p * st;
     float d[5];
 #pragma unroll
@@ -1818,6 +1857,7 @@ __device__ __forceinline__ void bt_refine_pl_item(const Fields& F, const Consts&
       }
       dn[m] = d[m];
     }
+    issue_bwd(p - PIPE);
   }
   cpa_wait<0>();
 }
@@ -2584,8 +2624,10 @@ void launch_solve(bool sp, int mode, int dir, const Fields& F, const Consts& K, 
 // Opt the pipelined sweeps into their dynamic shared memory (above 48 KB for
 // 128 threads per CTA); called once per handle, outside any stream capture.
 int configure_kernels() {
-  const size_t bt_cap = pl_refine_smem(128, false), sp_cap = pls_refine_smem(128, false);
-  const int cap = (int)(bt_cap > sp_cap ? bt_cap : sp_cap);
+  size_t cap_b = pl_refine_smem(128, false);
+  for (size_t b : {pl_mixed_smem(128), pls_mixed_smem(128), pls_refine_smem(128, false)})
+    if (b > cap_b) cap_b = b;
+  const int cap = (int)cap_b;
   cudaError_t e = cudaSuccess;
   auto set = [&](const void* f) {
     const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
