@@ -107,9 +107,11 @@ struct SpElim {
 };
 
 // Eliminate with row p+2 (bands L2, rhs r2): the loop body of sp_forward_f32.
-// Writes l4, l5 and the eliminated rhs of row p to the line scratch.
+// Writes l4, l5 and the eliminated rhs of row p to the line scratch (and, with
+// sl set, to words 0..10 of this thread's ring slot, word k at sl[k * T]).
 __device__ __forceinline__ void sp_elim_step(SpElim& e, int p, const float L2[3][5], const float r2[5],
-                                             float* __restrict__ scr, int64_t nlt, int64_t gl) {
+                                             float* __restrict__ scr, int64_t nlt, int64_t gl,
+                                             float* sl = nullptr, int T = 0) {
   float rr2[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) rr2[m] = r2[m];
@@ -131,12 +133,17 @@ __device__ __forceinline__ void sp_elim_step(SpElim& e, int p, const float L2[3]
     for (int m = SP_M0(s); m <= SP_M1(s); ++m) rr2[m] -= L2[s][0] * e.rr[0][m];
     scr[((int64_t)p * 11 + 2 * s) * nlt + gl] = e.cur4[s];
     scr[((int64_t)p * 11 + 2 * s + 1) * nlt + gl] = e.cur5[s];
+    if (sl) {
+      sl[(2 * s) * T] = e.cur4[s];
+      sl[(2 * s + 1) * T] = e.cur5[s];
+    }
     e.cur3[s] = e.nx3[s]; e.cur4[s] = e.nx4[s]; e.cur5[s] = e.nx5[s];
     e.nx2[s] = n2; e.nx3[s] = n3; e.nx4[s] = L2[s][3]; e.nx5[s] = L2[s][4];
   }
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
     scr[((int64_t)p * 11 + 6 + m) * nlt + gl] = e.rr[0][m];
+    if (sl) sl[(6 + m) * T] = e.rr[0][m];
     e.rr[0][m] = e.rr[1][m];
     e.rr[1][m] = rr2[m];
   }
@@ -274,22 +281,25 @@ __device__ __forceinline__ void sp_mixed_pl_item(const Fields& F, const Consts& 
     float L2[3][5], r2[5];
     issue_fwd(p + 2 + PIPE - 1);
     row(p + 2, L2, r2);
-    sp_elim_step(e, p, L2, r2, scr, nlt, Ln.gl);
+    // the ring does not refill the slot row p + 2 came in: row p's words stay
+    // there for the back substitution, which so starts without a trip to memory
+    const bool keep = p + 2 + PIPE > n - 1;
+    sp_elim_step(e, p, L2, r2, scr, nlt, Ln.gl, keep ? S((p + 2) % PIPE, 0) : nullptr, T);
   }
   SpF32Tail tail;
   sp_elim_finish(e, tail);
   cpa_wait<0>();
-  // back substitution: row p (n-3 .. 1) consumes l4, l5, r' of row p
+  // back substitution: row p (n-3 .. 1) consumes l4, l5, r' of row p from
+  // slot (p + 2) % PIPE: the last rows as the forward pass left them, the
+  // others loaded PIPE rows ahead into the slot just consumed
   auto issue_bwd = [&](int p) {
     if (p >= 1) {
-      const int slot = (n - 3 - p) % PIPE;
+      const int slot = (p + 2) % PIPE;
 #pragma unroll
       for (int k = 0; k < 11; ++k) cpa4(S(slot, k), scr + ((int64_t)p * 11 + k) * nlt + Ln.gl);
     }
     cpa_commit();
   };
-#pragma unroll
-  for (int q = 0; q < PIPE - 1; ++q) issue_bwd(n - 3 - q);
   float b1[5], b2[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
@@ -299,9 +309,8 @@ __device__ __forceinline__ void sp_mixed_pl_item(const Fields& F, const Consts& 
     *Ln.x0_at(n - 2, m) = b1[m];
   }
   for (int p = n - 3; p >= 1; --p) {
-    issue_bwd(p - (PIPE - 1));
-    cpa_wait<PIPE - 1>();
-    const int slot = (n - 3 - p) % PIPE;
+    if (p + 2 + PIPE <= n - 1) cpa_wait<PIPE - 1>();
+    const int slot = (p + 2) % PIPE;
     float r[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -314,6 +323,7 @@ __device__ __forceinline__ void sp_mixed_pl_item(const Fields& F, const Consts& 
       b1[m] = r[m];
       *Ln.x0_at(p, m) = r[m];
     }
+    issue_bwd(p - PIPE);
   }
   cpa_wait<0>();
 }
@@ -451,27 +461,13 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
     row(1, L1, r1);
     sp_elim_begin(e, L0, r0, L1, r1);
   }
-  for (int p = 0; p <= n - 3; ++p) {
-    float L2[3][5], r2[5];
-    issue_fwd(p + 2 + PIPE - 1);
-    row(p + 2, L2, r2);
-    sp_elim_step(e, p, L2, r2, scr, nlt, Ln.gl);
-  }
-  SpF32Tail tail;
-  sp_elim_finish(e, tail);
-  cpa_wait<0>();
   // back substitution: row p (n-2 .. 1) consumes l4, l5, r' (rows <= n-3), x0
-  // and, in the z sweep, u and the primitives tzetar reads
-  auto issue_bwd = [&](int p) {
-    if (p >= 1) {
-      const int slot = (n - 2 - p) % PIPE;
-      const int64_t pt = Ln.base + (int64_t)p * Ln.st;
-      if (p <= n - 3) {
+  // and, in the z sweep, u and the primitives tzetar reads, from slot
+  // (p + 2) % PIPE.  issue_rest: all but l4, l5, r'
+  auto issue_rest = [&](int p, int slot) {
+    const int64_t pt = Ln.base + (int64_t)p * Ln.st;
 #pragma unroll
-        for (int k = 0; k < 11; ++k) cpa4(S(slot, k), scr + ((int64_t)p * 11 + k) * nlt + Ln.gl);
-      }
-#pragma unroll
-      for (int m = 0; m < 5; ++m) cpa4(S(slot, 11 + m), Ln.x0_at(p, m));
+    for (int m = 0; m < 5; ++m) cpa4(S(slot, 11 + m), Ln.x0_at(p, m));
       if (!OUT_DF) {
         if (add_u) {
 #pragma unroll
@@ -498,6 +494,32 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
           cpa8(SU(slot, 10), F.prim + PR_QS * NP + pt);
         }
       }
+  };
+  for (int p = 0; p <= n - 3; ++p) {
+    float L2[3][5], r2[5];
+    issue_fwd(p + 2 + PIPE - 1);
+    row(p + 2, L2, r2);
+    // rows n-1-PIPE .. n-2 stay in the slots the ring does not refill (row p
+    // in the one row p + 2 came in), so that the back substitution starts
+    // without a trip to memory: l4, l5, r' written here, the rest fetched now
+    const bool keep = p >= n - 1 - PIPE;
+    sp_elim_step(e, p, L2, r2, scr, nlt, Ln.gl, keep ? S((p + 2) % PIPE, 0) : nullptr, T);
+    if (keep) {
+      if (p >= 1) issue_rest(p, (p + 2) % PIPE);
+      if (p == (n - 1 - PIPE > 0 ? n - 1 - PIPE : 0)) issue_rest(n - 2, n % PIPE);
+      cpa_commit();
+    }
+  }
+  SpF32Tail tail;
+  sp_elim_finish(e, tail);
+  cpa_wait<0>();
+  // the other rows PIPE ahead into the slot just consumed
+  auto issue_bwd = [&](int p) {
+    if (p >= 1) {
+      const int slot = (p + 2) % PIPE;
+#pragma unroll
+      for (int k = 0; k < 11; ++k) cpa4(S(slot, k), scr + ((int64_t)p * 11 + k) * nlt + Ln.gl);
+      issue_rest(p, slot);
     }
     cpa_commit();
   };
@@ -575,24 +597,20 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
       }
     }
   };
-#pragma unroll
-  for (int q = 0; q < PIPE - 1; ++q) issue_bwd(n - 2 - q);
   float b1[5], b2[5];
   {
-    issue_bwd(n - 2 - (PIPE - 1));
-    cpa_wait<PIPE - 1>();
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
       const int s = m < 3 ? 0 : m - 2;
       b2[m] = tail.rlast[m];
       b1[m] = tail.r2[m] - tail.cur4[s] * b2[m];
     }
-    emit(n - 2, 0, b1);
+    emit(n - 2, n % PIPE, b1);
+    issue_bwd(n - 2 - PIPE);
   }
   for (int p = n - 3; p >= 1; --p) {
-    issue_bwd(p - (PIPE - 1));
-    cpa_wait<PIPE - 1>();
-    const int slot = (n - 2 - p) % PIPE;
+    if (p <= n - 2 - PIPE) cpa_wait<PIPE - 1>();
+    const int slot = (p + 2) % PIPE;
     float r[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -602,6 +620,7 @@ __device__ __forceinline__ void sp_refine_pl_item(const Fields& F, const Consts&
 #pragma unroll
     for (int m = 0; m < 5; ++m) { b2[m] = b1[m]; b1[m] = r[m]; }
     emit(p, slot, r);
+    issue_bwd(p - PIPE);
   }
   cpa_wait<0>();
 }
