@@ -255,6 +255,10 @@ struct npbmz_handle {
   std::vector<Range> grp_pts, grp_int, grp_line[3];
   int cur_group = -1;              // >= 0 while the phases of one group are issued
   cudaStream_t grp_stream[8] = {};
+  // the zone groups' streams of the npbmz_step_inout graph: priorities fall
+  // with the group number, so that the groups finish in the order their copies
+  // came in and each one's copy out starts while later groups compute
+  cudaStream_t io_grp_stream[8] = {};
   // the zone groups' primitive kernels and compute_rhs (FP64 pipe) on one
   // stream of the device's greatest priority, so that their CTAs go to SMs
   // ahead of the waiting CTAs of the sweeps (FP32 pipe) they run beside
@@ -777,10 +781,11 @@ int grouped_step(npbmz_t* h, cudaStream_t cs, bool inout) {
   CK(h, cudaEventRecord(start, cs));
   int rc = 0;
   for (int g = 0; g < G && !rc; ++g) {
-    cudaStream_t S = h->grp_stream[g];
+    cudaStream_t S = inout ? h->io_grp_stream[g] : h->grp_stream[g];
     // prim + compute_rhs of group g: on the priority stream (in group order),
-    // or on the group's own stream after group g-1's compute_rhs
-    cudaStream_t P = h->fp64_prio ? h->prio_stream : S;
+    // or on the group's own stream after group g-1's compute_rhs (always so
+    // in the npbmz_step_inout graph, whose group streams carry the priorities)
+    cudaStream_t P = h->fp64_prio && !inout ? h->prio_stream : S;
     rc |= cudaStreamWaitEvent(P, start, 0) != cudaSuccess;
     if (inout) rc |= cudaStreamWaitEvent(P, h->up_ev[g], cudaEventWaitExternal) != cudaSuccess;
     if (g > 0 && P == S) rc |= cudaStreamWaitEvent(S, h->grp_ev[2 * (g - 1)], 0) != cudaSuccess;
@@ -826,6 +831,20 @@ int capture_step_graph(npbmz_t* h, bool inout = false) {
       CK(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
       CK(h, cudaStreamCreateWithPriority(&h->prio_stream, cudaStreamNonBlocking, greatest));
     }
+    if (inout) {
+      int least = 0, greatest = 0;
+      CK(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      const int levels = least - greatest + 1;  // greatest is the numerically smaller
+      for (int g = 0; g < h->ngroups; ++g) {
+        if (h->io_grp_stream[g]) {
+          CK(h, cudaStreamSynchronize(h->io_grp_stream[g]));
+          CK(h, cudaStreamDestroy(h->io_grp_stream[g]));
+        }
+        // group 0 at the greatest priority, the last groups at the least
+        const int prio = greatest + g * levels / h->ngroups;
+        CK(h, cudaStreamCreateWithPriority(&h->io_grp_stream[g], cudaStreamNonBlocking, prio));
+      }
+    }
   }
   if (flush_boundary(h)) return -1;  // keep the one-off reset out of the graph
   // Capture is not allowed on the legacy default stream: capture and replay
@@ -849,7 +868,8 @@ int capture_step_graph(npbmz_t* h, bool inout = false) {
   if (rc) { if (g) cudaGraphDestroy(g); return -1; }
   if (e != cudaSuccess) return fail(h, "stream capture failed: %s", cudaGetErrorString(e));
   // kernel nodes keep the priority of the stream they were captured from
-  e = cudaGraphInstantiate(&exec, g, use_groups(h) && h->fp64_prio ? cudaGraphInstantiateFlagUseNodePriority : 0);
+  e = cudaGraphInstantiate(&exec, g,
+                           use_groups(h) && (h->fp64_prio || inout) ? cudaGraphInstantiateFlagUseNodePriority : 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(h, "graph instantiate failed: %s", cudaGetErrorString(e));
   h->graph_stream = h->stream;
@@ -2171,6 +2191,8 @@ int npbmz_destroy(npbmz_t* h) {
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   if (h->aux_stream) { cudaStreamSynchronize(h->aux_stream); cudaStreamDestroy(h->aux_stream); }
   for (cudaStream_t gs : h->grp_stream)
+    if (gs) { cudaStreamSynchronize(gs); cudaStreamDestroy(gs); }
+  for (cudaStream_t gs : h->io_grp_stream)
     if (gs) { cudaStreamSynchronize(gs); cudaStreamDestroy(gs); }
   if (h->prio_stream) { cudaStreamSynchronize(h->prio_stream); cudaStreamDestroy(h->prio_stream); }
   for (cudaEvent_t e : h->grp_ev)
