@@ -672,8 +672,10 @@ def run_gpu(args):
                         "path": "npbmz_step_inout(1, NPBMZ_LAYOUT_REF) per step on one page-locked buffer holding "
                                 "every zone's reference-layout u: the planes exch_qbc reads by a kernel from host "
                                 "memory, then each zone group's arrays by the copy engine while earlier groups "
-                                "compute, and each group back by the copy engine when its last z sweep is done "
-                                "(halo bytes travel unchanged; the counts above are the interior points)"}
+                                "compute (group branches at priorities falling with the group number, so groups "
+                                "finish in arrival order), and each group back by the copy engine when its last z "
+                                "sweep is done (halo bytes travel unchanged; the counts above are the interior "
+                                "points)"}
         if not args.no_cpu_baseline:
             extra["cpu_baseline"] = cpu_baseline(kind, cls, ce)
     if rank == 0:
