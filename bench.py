@@ -532,7 +532,7 @@ def run_gpu(args):
         p.setup(ce)
         d = p.describe()
         tuned = {k: d[k] for k in ("lines_per_cta", "zone_size_buckets", "step_groups", "fp64_priority",
-                                   "sweep_ctas_per_sm", "persistent")}
+                                   "sweep_ctas_per_sm", "persistent", "copy_fusion")}
     with ClockSampler(local) as clk:
         ms = time_steps(p, torch, stream, args.steps, args.warmup, dist)
     ms_max, value = whole_job(ms, pts, args.steps, world, dist)

@@ -255,6 +255,9 @@ struct npbmz_handle {
   std::vector<Range> grp_pts, grp_int, grp_line[3];
   int cur_group = -1;              // >= 0 while the phases of one group are issued
   cudaStream_t grp_stream[8] = {};
+  // the x sweep's x-line-major state copies made by the compute_rhs launch
+  // (k_rhs_flux_xc) instead of a kernel of their own (npbmz_set_copy_fusion)
+  bool copy_fusion = false;
   // the zone groups' streams of the npbmz_step_inout graph: priorities fall
   // with the group number, so that the groups finish in the order their copies
   // came in and each one's copy out starts while later groups compute
@@ -616,6 +619,30 @@ int line_launches(npbmz_t* h, int dir, int zone, Fn fn) {
 }
 
 // ---- phases ---------------------------------------------------------------
+// The x sweep of a fused step reads x-line-major copies of the FP32 state.
+// With copy fusion on and the x-sweep work list of this launch scope one
+// slice (one line shape), the compute_rhs launch makes them (k_rhs_flux_xc),
+// so that their memory traffic runs beside the FP64-bound compute_rhs;
+// otherwise the primitive phase launches k_xline_copy per slice.
+struct XSlices {
+  int n = 0, lo = 0, hi = 0, tpb = 0;
+};
+XSlices x_slices(npbmz_t* h, int zone) {
+  XSlices x;
+  line_launches(h, 0, zone, [&](int lo, int hi, int tpb) {
+    ++x.n;
+    x.lo = lo;
+    x.hi = hi;
+    x.tpb = tpb;
+    return 0;
+  });
+  return x;
+}
+bool copy_in_rhs(npbmz_t* h, int zone, bool fused) {
+  return fused && h->copy_fusion && h->pfx && h->flux && h->fdt && !h->dfrhs && !use_exact(h) &&
+         x_slices(h, zone).n == 1;
+}
+
 // fused: part of a whole step (run_adi): with the double-float primitive
 // kernel, the FP64 prim planes that only single phases read are skipped.
 int phase_prim(npbmz_t* h, int zone, bool fused = false) {
@@ -642,7 +669,7 @@ int phase_prim(npbmz_t* h, int zone, bool fused = false) {
       fast::launch_prim_w(sp, Fp, h->K, h->wpts_d + wlo, whi - wlo, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
     CKL(h);
     // the x sweep of a fused step reads x-line-major copies of the state
-    if (fused && h->pfx &&
+    if (fused && h->pfx && !copy_in_rhs(h, zone, fused) &&
         line_launches(h, 0, zone, [&](int llo, int lhi, int tpb) {
           fast::launch_xline_copy(sp, F, h->wline_d[0] + llo, lhi - llo, tpb, h->stream);
           CKL(h);
@@ -667,8 +694,12 @@ int phase_rhs(npbmz_t* h, int zone, bool tx, bool norm, bool fused = false) {
   else if (h->dfrhs)
     fast::launch_rhs_df(tx, norm, F, h->rdc, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream,
                         (h->flags & NPBMZ_PERSIST) != 0);
-  else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->rc64,
-                        (h->flags & NPBMZ_PERSIST) != 0);
+  else if (copy_in_rhs(h, zone, fused)) {
+    const XSlices x = x_slices(h, zone);
+    fast::launch_rhs_xc(tx, norm, F, h->K, h->rc64, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo,
+                        h->wline_d[0] + x.lo, x.hi - x.lo, x.tpb, h->stream, (h->flags & NPBMZ_PERSIST) != 0);
+  } else fast::launch_rhs(tx, norm, F, h->K, h->wint_d + lo, hi - lo, h->part_rhs + 5 * lo, h->stream, &h->rc64,
+                          (h->flags & NPBMZ_PERSIST) != 0);
   CKL(h);
   return 0;
 }
@@ -940,7 +971,7 @@ int count_launches(npbmz_t* h) {
   const bool refined = (h->flags & NPBMZ_MIXED) && !(h->flags & NPBMZ_FP32_NOREFINE);
   // prim, its x-line-major copy (double-float compute_rhs), compute_rhs,
   // two kernels per refined sweep and the x result's copy back
-  const int adi = 2 + (h->pfx ? 1 : 0) + 3 * (refined ? 2 : 1) + (h->rdx ? 1 : 0);
+  const int adi = 2 + (h->pfx && !h->copy_fusion ? 1 : 0) + 3 * (refined ? 2 : 1) + (h->rdx ? 1 : 0);
   int batches = 1;
   if (h->flags & NPBMZ_PERZONE) batches = h->nzones;
   else if ((h->flags & NPBMZ_GRAPH) && h->ngroups > 1 && !(h->flags & NPBMZ_EXACT)) batches = h->ngroups;
@@ -1918,6 +1949,15 @@ int npbmz_set_step_overlap(npbmz_t* h, int fp64_first, int sweep_ctas_per_sm) {
   return 0;
 }
 
+int npbmz_set_copy_fusion(npbmz_t* h, int on) {
+  if (!h) return fail(nullptr, "null handle");
+  CK(h, cudaStreamSynchronize(h->stream));
+  drop_graph(h);
+  h->copy_fusion = on != 0;
+  h->launches_per_step = count_launches(h);
+  return 0;
+}
+
 int npbmz_set_stream(npbmz_t* h, void* stream) {
   if (!h) return fail(nullptr, "null handle");
   if (h->own_stream && h->stream) {
@@ -1944,8 +1984,9 @@ int npbmz_autotune(npbmz_t* h) {
   //    bucket's candidates are timed on its own launches.  2. For graph
   //    handles, the number of zone-group branches of the step graph, timed on
   //    whole steps.  3. Persistent kernels (NPBMZ_PERSIST) on or off, timed
-  //    on whole steps.  Timed on a snapshot of u and rhs, restored afterwards;
-  //    no choice changes the results.
+  //    on whole steps.  4. The x sweep's state copies in the compute_rhs
+  //    launch or on their own (before 2 and after 3).  Timed on a snapshot of
+  //    u and rhs, restored afterwards; no choice changes the results.
   const int cand[] = {32, 64, 128};
   const size_t bytes = 5 * (size_t)h->NP * sizeof(double);
   double* usave = nullptr;
@@ -2034,6 +2075,21 @@ int npbmz_autotune(npbmz_t* h) {
       if (build_line_lists(h)) rc = -1;
     }
   }
+  // the x-line-major copies in the compute_rhs launch or on their own: timed
+  // before the group stage (whose choices depend on it) and again after the
+  // last stage
+  auto tune_copy_fusion = [&]() -> int {
+    if (!h->pfx || (h->flags & NPBMZ_EXACT)) return 0;
+    drop_graph(h);
+    const float t_now = step_ms();
+    h->copy_fusion = !h->copy_fusion;
+    drop_graph(h);
+    const float t_other = step_ms();
+    if (t_now < 0.f || t_other < 0.f) return -1;
+    if (t_now <= t_other) h->copy_fusion = !h->copy_fusion;  // keep the first
+    return 0;
+  };
+  if (!rc) rc = tune_copy_fusion();
   if (!rc && (h->flags & NPBMZ_GRAPH) && !(h->flags & (NPBMZ_EXACT | NPBMZ_PERZONE)) && h->nzones >= 8) {
     // zone-group branches; with more than one, the priority stream for the
     // FP64 phases and a cap on the sweeps' resident CTAs per SM
@@ -2065,6 +2121,7 @@ int npbmz_autotune(npbmz_t* h) {
     if (t_now < 0.f || t_other < 0.f) rc = -1;
     else if (t_now <= t_other) h->flags ^= NPBMZ_PERSIST;  // keep the first
   }
+  if (!rc) rc = tune_copy_fusion();
   cudaMemcpyAsync(h->u, usave, bytes, cudaMemcpyDeviceToDevice, h->stream);
   cudaMemcpyAsync(h->rhs, rsave, bytes, cudaMemcpyDeviceToDevice, h->stream);
   cudaStreamSynchronize(h->stream);
@@ -2110,10 +2167,10 @@ int npbmz_describe(npbmz_t* h, char* buf, size_t n) {
   tp += "]";
   snprintf(buf, n, "{\"kind\":\"%s\",\"zones\":%d,\"points\":%lld,\"flags\":%d,\"lines_per_cta\":%s,"
            "\"zone_size_buckets\":%d,\"step_groups\":%d,\"fp64_priority\":%s,\"sweep_ctas_per_sm\":%d,"
-           "\"persistent\":%s,\"launches_per_step\":%d,\"device_bytes\":%lld}",
+           "\"persistent\":%s,\"copy_fusion\":%s,\"launches_per_step\":%d,\"device_bytes\":%lld}",
            h->kind == NPBMZ_BT ? "BT" : "SP", h->nzones, (long long)h->NP, h->flags, tp.c_str(), h->nbkt, h->ngroups,
            h->fp64_prio ? "true" : "false", h->sweep_cap, (h->flags & NPBMZ_PERSIST) ? "true" : "false",
-           h->launches_per_step, (long long)h->device_bytes);
+           h->copy_fusion ? "true" : "false", h->launches_per_step, (long long)h->device_bytes);
   return 0;
 }
 

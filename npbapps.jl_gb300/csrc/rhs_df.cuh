@@ -325,45 +325,88 @@ __global__ void __launch_bounds__(128) k_rhs_df(Fields F, RhsDfConsts C, const W
 // the zone-layout reads (along i) and the x-line-major writes (along g) are
 // both coalesced, with 4 * PB loads in flight per thread.
 template <bool SP>
-__global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __restrict__ work, int nwork, int lpi) {
-  constexpr int E = SP ? (int)PS_COUNT : (int)PF_COUNT;
-  constexpr int PB = E / 2;
-  __shared__ float tile[PB][32][33];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
+struct XlineTile {
+  static constexpr int E = SP ? (int)PS_COUNT : (int)PF_COUNT;
+  static constexpr int PB = E / 2;
+  float t[PB][32][33];
+};
+
+// One work item of the copy, by a CTA of NW warps: the 32 rows of a tile in
+// 32 / (4 NW) passes of 4 rows per thread, 4 PB loads in flight per thread.
+template <bool SP, int NW>
+__device__ __forceinline__ void xline_copy_item(const Fields& F, const Work w, int lpi, XlineTile<SP>& T) {
+  constexpr int E = XlineTile<SP>::E, PB = XlineTile<SP>::PB, R = 4, PASSES = 32 / (R * NW);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int64_t NP = F.NP;
-  for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
-    const Work w = work[it];
-    const ZoneDev Z = F.zones[w.zone];
-    const int l1 = min(w.first + lpi, zone_lines(Z, 0));
-    const int iy = Z.ny - 2;
-    for (int l0 = w.first; l0 < l1; l0 += 32)
-      for (int i0 = 0; i0 < Z.nx; i0 += 32)
+  const ZoneDev Z = F.zones[w.zone];
+  const int l1 = min(w.first + lpi, zone_lines(Z, 0));
+  const int iy = Z.ny - 2;
+  for (int l0 = w.first; l0 < l1; l0 += 32)
+    for (int i0 = 0; i0 < Z.nx; i0 += 32)
 #pragma unroll 1
-        for (int e0 = 0; e0 < E; e0 += PB) {
-          float v[PB][4];
+      for (int e0 = 0; e0 < E; e0 += PB) {
+#pragma unroll 1
+        for (int h = 0; h < PASSES; ++h) {
+          float v[PB][R];
 #pragma unroll
-          for (int r4 = 0; r4 < 4; ++r4) {  // row ty + 8 r4: line l0 + row, column tx: point i0 + tx
-            const int l = l0 + ty + 8 * r4, i = i0 + tx;
+          for (int r = 0; r < R; ++r) {  // row ty + NW (R h + r): a line, column tx: point i0 + tx
+            const int l = l0 + ty + NW * (R * h + r), i = i0 + tx;
             const bool ok = l < l1 && i < Z.nx;
             const int64_t p = ok ? Z.off + ((int64_t)(1 + l / iy) * Z.ny + 1 + l % iy) * Z.nx + i : 0;
 #pragma unroll
-            for (int b = 0; b < PB; ++b) v[b][r4] = ok ? F.primf[(int64_t)(e0 + b) * NP + p] : 0.f;
+            for (int b = 0; b < PB; ++b) v[b][r] = ok ? F.primf[(int64_t)(e0 + b) * NP + p] : 0.f;
           }
 #pragma unroll
           for (int b = 0; b < PB; ++b)
 #pragma unroll
-            for (int r4 = 0; r4 < 4; ++r4) tile[b][ty + 8 * r4][tx] = v[b][r4];
-          __syncthreads();
+            for (int r = 0; r < R; ++r) T.t[b][ty + NW * (R * h + r)][tx] = v[b][r];
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int h = 0; h < PASSES; ++h)
 #pragma unroll
-          for (int r4 = 0; r4 < 4; ++r4) {  // point i0 + ty + 8 r4 of line l0 + tx
-            const int i = i0 + ty + 8 * r4, l = l0 + tx;
+          for (int r = 0; r < R; ++r) {  // point i0 + ty + NW (R h + r) of line l0 + tx
+            const int i = i0 + ty + NW * (R * h + r), l = l0 + tx;
             if (l < l1 && i < Z.nx)
 #pragma unroll
               for (int b = 0; b < PB; ++b)
-                F.pfx[((int64_t)i * E + e0 + b) * F.nlx + Z.lineoff[0] + l] = tile[b][tx][ty + 8 * r4];
+                F.pfx[((int64_t)i * E + e0 + b) * F.nlx + Z.lineoff[0] + l] = T.t[b][tx][ty + NW * (R * h + r)];
           }
-          __syncthreads();
-        }
+        __syncthreads();
+      }
+}
+
+template <bool SP>
+__global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __restrict__ work, int nwork, int lpi) {
+  __shared__ XlineTile<SP> tile;
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) xline_copy_item<SP, 8>(F, work[it], lpi, tile);
+}
+
+// compute_rhs (k_rhs_flux) and the x-line-major state copies (k_xline_copy)
+// in one launch: both read what the primitive kernel wrote, and the copy's
+// memory traffic runs beside compute_rhs, which the FP64 pipe binds.  Item b
+// of the nwork + ncopy is a copy item when (b + 1) is a multiple of s = total
+// / ncopy (the copies spread evenly over the launch), otherwise the compute_rhs
+// item b minus the copies before it.
+template <bool TX, bool NORM>
+__global__ void __launch_bounds__(128) k_rhs_flux_xc(Fields F, Consts K, RhsF64Consts RC, const Work* __restrict__ work,
+                                                     int nwork, double* __restrict__ partials,
+                                                     const Work* __restrict__ cwork, int ncopy, int lpi) {
+  __shared__ double red[NORM ? 5 * 128 : 1];
+  __shared__ double wt[3 * 32 * 5];
+  __shared__ XlineTile<TX> tile;
+  for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&RC.w[0][0][0])[e];
+  __syncthreads();
+  const int total = nwork + ncopy;
+  const int s = ncopy > 0 ? total / ncopy : total + 1;
+  for (int b = blockIdx.x; b < total; b += gridDim.x) {
+    const int q = (b + 1) / s;
+    if ((b + 1) % s == 0 && q <= ncopy) {
+      xline_copy_item<TX, 4>(F, cwork[q - 1], lpi, tile);
+    } else {
+      const int it = b - min(ncopy, b / s);
+      rhs_flux_item<TX, NORM>(F, K, RC, work[it], it, partials, wt, red);
+    }
   }
 }
 

@@ -352,15 +352,11 @@ __device__ __forceinline__ void rhs_dir(double r[5], const double* __restrict__ 
   r[4] = fma(dt, (wv[p + st] + wv[p - st]) - 2.0 * wv[p], r[4]);
 }
 
+// One work item (128 interior points of one zone) of compute_rhs; wt: the
+// dissipation weights in shared memory, red: the NORM reduction scratch.
 template <bool TX, bool NORM>
-__global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, RhsF64Consts RC, const Work* __restrict__ work,
-                                                  int nwork, double* __restrict__ partials) {
-  __shared__ double red[NORM ? 5 * 128 : 1];
-  __shared__ double wt[3 * 32 * 5];
-  for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&RC.w[0][0][0])[e];
-  __syncthreads();
-  for (int it = blockIdx.x; it < nwork; it += gridDim.x) {
-  const Work w = work[it];
+__device__ __forceinline__ void rhs_flux_item(const Fields& F, const Consts& K, const RhsF64Consts& RC, const Work w,
+                                              int it, double* __restrict__ partials, const double* wt, double* red) {
   const ZoneDev Z = F.zones[w.zone];
   const int64_t NP = F.NP;
   const int ix = Z.nx - 2, iy = Z.ny - 2;
@@ -444,7 +440,16 @@ __global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, RhsF64Cons
     if (threadIdx.x == 0)
       for (int m = 0; m < 5; ++m) partials[it * 5 + m] = sq[m];
   }
-  }
+}
+
+template <bool TX, bool NORM>
+__global__ void __launch_bounds__(128) k_rhs_flux(Fields F, Consts K, RhsF64Consts RC, const Work* __restrict__ work,
+                                                  int nwork, double* __restrict__ partials) {
+  __shared__ double red[NORM ? 5 * 128 : 1];
+  __shared__ double wt[3 * 32 * 5];
+  for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&RC.w[0][0][0])[e];
+  __syncthreads();
+  for (int it = blockIdx.x; it < nwork; it += gridDim.x) rhs_flux_item<TX, NORM>(F, K, RC, work[it], it, partials, wt, red);
 }
 
 // The two end points of every x line in the x-line-major double-float rhs
@@ -2685,6 +2690,22 @@ void launch_xline_copy(bool sp, const Fields& F, const Work* work, int nwork, in
   if (nwork <= 0) return;
   if (sp) k_xline_copy<true><<<nwork, 256, 0, s>>>(F, work, nwork, lpi);
   else k_xline_copy<false><<<nwork, 256, 0, s>>>(F, work, nwork, lpi);
+}
+
+void launch_rhs_xc(bool tx, bool norm, const Fields& F, const Consts& K, const RhsF64Consts& rc, const Work* work,
+                   int nwork, double* partials, const Work* cwork, int ncopy, int lpi, cudaStream_t s, bool persist) {
+  if (nwork + ncopy <= 0) return;
+#define NPBMZ_RHS_XC(A, B)                                                                                   \
+  k_rhs_flux_xc<A, B><<<item_grid((const void*)k_rhs_flux_xc<A, B>, nwork + ncopy, 128, 0, persist), 128, 0, s>>>( \
+      F, K, rc, work, nwork, partials, cwork, ncopy, lpi)
+  if (tx) {
+    if (norm) NPBMZ_RHS_XC(true, true);
+    else NPBMZ_RHS_XC(true, false);
+  } else {
+    if (norm) NPBMZ_RHS_XC(false, true);
+    else NPBMZ_RHS_XC(false, false);
+  }
+#undef NPBMZ_RHS_XC
 }
 
 void launch_scale(const double* src, double* dst, double a, int64_t n, cudaStream_t s) {

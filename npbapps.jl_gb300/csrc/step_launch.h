@@ -37,6 +37,10 @@ void launch_rhs_df(bool tx, bool norm, const Fields& F, const RhsDfConsts& C, co
 // x-line-major copies of the FP32 state pairs for the x-sweep items
 // work[0..nwork) of lpi lines each
 void launch_xline_copy(bool sp, const Fields& F, const Work* work, int nwork, int lpi, cudaStream_t s);
+// compute_rhs (the FP64 kernel with the point functions) and those copies in
+// one launch: work[0..nwork) compute_rhs items, cwork[0..ncopy) copy items
+void launch_rhs_xc(bool tx, bool norm, const Fields& F, const Consts& K, const RhsF64Consts& rc, const Work* work,
+                   int nwork, double* partials, const Work* cwork, int ncopy, int lpi, cudaStream_t s, bool persist);
 // the forcing at both ends of every x line into Fields::rdx
 void launch_xline_ends(const Fields& F, const Work* work, int nwork, int tpb, cudaStream_t s);
 // dynamic shared memory limits of the pipelined sweeps; 0 on success

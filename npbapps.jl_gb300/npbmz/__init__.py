@@ -45,7 +45,7 @@ EXPORTS = [
     "npbmz_fp64_peak", "npbmz_launches_per_step", "npbmz_device_bytes", "npbmz_describe", "npbmz_last_error", "npbmz_destroy",
     "npbmz_bt_xsolve_noalloc", "npbmz_adjoint", "npbmz_step_profile", "npbmz_set_step_groups",
     "npbmz_step_download", "npbmz_face_plan", "npbmz_pack_faces", "npbmz_unpack_faces", "npbmz_set_step_overlap",
-    "npbmz_state_check", "npbmz_step_inout", "npbmz_math_check",
+    "npbmz_set_copy_fusion", "npbmz_state_check", "npbmz_step_inout", "npbmz_math_check",
 ]
 STATE_DENSITY, STATE_PRESSURE, STATE_NONFINITE = 1, 2, 4
 REMOTE = -1  # NPBMZ_REMOTE: a face whose neighbour zone lives on another rank
@@ -159,6 +159,7 @@ def lib(build_if_missing: bool = True):
     L.npbmz_step_profile.argtypes = [vp, ctypes.c_int, dp]
     L.npbmz_set_step_groups.argtypes = [vp, ctypes.c_int]
     L.npbmz_set_step_overlap.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.npbmz_set_copy_fusion.argtypes = [vp, ctypes.c_int]
     L.npbmz_state_check.argtypes = [vp] + [ip] * 5
     i64p = ctypes.POINTER(ctypes.c_int64)
     L.npbmz_face_plan.argtypes = [vp, ctypes.c_int, ip, ctypes.c_int, ip, i64p, i64p]
@@ -366,6 +367,11 @@ class Problem:
         and at most sweep_ctas_per_sm resident sweep CTAs per SM (0: no cap)."""
         self._check(lib().npbmz_set_step_overlap(self._h, int(bool(fp64_first)), int(sweep_ctas_per_sm)),
                     "npbmz_set_step_overlap")
+
+    def set_copy_fusion(self, on: bool):
+        """The x sweep's x-line-major state copies in the compute_rhs launch
+        (True) or by a kernel of their own (False)."""
+        self._check(lib().npbmz_set_copy_fusion(self._h, int(bool(on))), "npbmz_set_copy_fusion")
 
     def autotune(self):
         self._check(lib().npbmz_autotune(self._h), "npbmz_autotune")

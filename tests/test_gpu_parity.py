@@ -268,6 +268,33 @@ def test_zone_group_graph_equals_direct_launches(kind, flags, groups, prio, cap)
 
 
 @pytest.mark.parametrize("kind", ["BT", "SP"])
+@pytest.mark.parametrize("flags,groups", [(npbmz.MIXED | npbmz.GRAPH, 2), (npbmz.MIXED | npbmz.GRAPH, 1),
+                                          (npbmz.MIXED, 1), (0, 1)],
+                         ids=["mixed-graph-2groups", "mixed-graph", "mixed-direct", "fp64-direct"])
+def test_copy_fusion_changes_no_result(kind, flags, groups):
+    """The x sweep's x-line-major state copies made in the compute_rhs launch
+    (npbmz_set_copy_fusion) leave u, rhs and the norms bit-identical to the
+    separate copy kernel; class W geometry (16 zones, uneven for BT)."""
+    geom, dt, _ = geom_class(kind, "W")
+    ce = seeded(geom)
+    a = npbmz.Problem(geom, dt, flags)
+    b = npbmz.Problem(geom, dt, flags)
+    for q in (a, b):
+        q.setup(ce)
+        if flags & npbmz.GRAPH:
+            q.set_step_groups(groups)
+    b.set_copy_fusion(True)
+    assert b.describe()["copy_fusion"] and not a.describe()["copy_fusion"]
+    a.step(5)
+    b.step(5)
+    b.synchronize()
+    for z in range(geom.nzones):
+        np.testing.assert_array_equal(a.download(npbmz.U, z), b.download(npbmz.U, z))
+        np.testing.assert_array_equal(a.download(npbmz.RHS, z), b.download(npbmz.RHS, z))
+    np.testing.assert_array_equal(np.concatenate(a.verify()), np.concatenate(b.verify()))
+
+
+@pytest.mark.parametrize("kind", ["BT", "SP"])
 @pytest.mark.parametrize("flags,groups", [(npbmz.MIXED | npbmz.GRAPH, 3), (npbmz.GRAPH, 2), (npbmz.MIXED, 1)],
                          ids=["mixed-graph-3groups", "fp64-graph-2groups", "mixed-direct"])
 def test_step_download_equals_step_then_download(kind, flags, groups):
