@@ -324,18 +324,19 @@ __global__ void __launch_bounds__(128) k_rhs_df(Fields F, RhsDfConsts C, const W
 // 32-point tiles of PB planes at a time go through shared memory, so that
 // the zone-layout reads (along i) and the x-line-major writes (along g) are
 // both coalesced, with 4 * PB loads in flight per thread.
-template <bool SP>
+// Shared tile of PB planes (default: half of the E planes per pass).
+template <bool SP, int PBV = 0>
 struct XlineTile {
   static constexpr int E = SP ? (int)PS_COUNT : (int)PF_COUNT;
-  static constexpr int PB = E / 2;
+  static constexpr int PB = PBV ? PBV : E / 2;
   float t[PB][32][33];
 };
 
 // One work item of the copy, by a CTA of NW warps: the 32 rows of a tile in
 // 32 / (4 NW) passes of 4 rows per thread, 4 PB loads in flight per thread.
-template <bool SP, int NW>
-__device__ __forceinline__ void xline_copy_item(const Fields& F, const Work w, int lpi, XlineTile<SP>& T) {
-  constexpr int E = XlineTile<SP>::E, PB = XlineTile<SP>::PB, R = 4, PASSES = 32 / (R * NW);
+template <bool SP, int NW, int PBV = 0>
+__device__ __forceinline__ void xline_copy_item(const Fields& F, const Work w, int lpi, XlineTile<SP, PBV>& T) {
+  constexpr int E = XlineTile<SP, PBV>::E, PB = XlineTile<SP, PBV>::PB, R = 4, PASSES = 32 / (R * NW);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int64_t NP = F.NP;
   const ZoneDev Z = F.zones[w.zone];
@@ -384,7 +385,9 @@ __global__ void __launch_bounds__(256) k_xline_copy(Fields F, const Work* __rest
 
 // compute_rhs (k_rhs_flux) and the x-line-major state copies (k_xline_copy)
 // in one launch: both read what the primitive kernel wrote, and the copy's
-// memory traffic runs beside compute_rhs, which the FP64 pipe binds.  Item b
+// memory traffic runs beside compute_rhs, which the FP64 pipe binds.  The
+// copy's tile holds 2 planes (8.4 KB): with half the planes per pass (25 KB)
+// the BT-C step graph ran 3.22 ms per step against 3.08 ms.  Item b
 // of the nwork + ncopy is a copy item when (b + 1) is a multiple of s = total
 // / ncopy (the copies spread evenly over the launch), otherwise the compute_rhs
 // item b minus the copies before it.
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(128) k_rhs_flux_xc(Fields F, Consts K, RhsF64C
                                                      const Work* __restrict__ cwork, int ncopy, int lpi) {
   __shared__ double red[NORM ? 5 * 128 : 1];
   __shared__ double wt[3 * 32 * 5];
-  __shared__ XlineTile<TX> tile;
+  __shared__ XlineTile<TX, 2> tile;
   for (int e = threadIdx.x; e < 3 * 32 * 5; e += blockDim.x) wt[e] = (&RC.w[0][0][0])[e];
   __syncthreads();
   const int total = nwork + ncopy;
@@ -402,7 +405,7 @@ __global__ void __launch_bounds__(128) k_rhs_flux_xc(Fields F, Consts K, RhsF64C
   for (int b = blockIdx.x; b < total; b += gridDim.x) {
     const int q = (b + 1) / s;
     if ((b + 1) % s == 0 && q <= ncopy) {
-      xline_copy_item<TX, 4>(F, cwork[q - 1], lpi, tile);
+      xline_copy_item<TX, 4, 2>(F, cwork[q - 1], lpi, tile);
     } else {
       const int it = b - min(ncopy, b / s);
       rhs_flux_item<TX, NORM>(F, K, RC, work[it], it, partials, wt, red);
