@@ -277,12 +277,13 @@ int npbmz_set_step_groups(npbmz_t* h, int groups);
 int npbmz_set_step_overlap(npbmz_t* h, int fp64_first, int sweep_ctas_per_sm);
 
 /* Where a step of the FMA build makes the x sweep's x-line-major copies of
- * the FP32 state: on != 0 in the compute_rhs launch (one kernel whose blocks
- * each do either compute_rhs points or copy tiles, the copies spread evenly
- * over the launch), when the x-sweep work list of the launch is one line
- * shape; 0 (the default) by a copy kernel of their own after the primitive
- * kernel.  Launch configuration only: results are unchanged.  npbmz_autotune
- * chooses it on whole steps.  No counterpart in the reference. */
+ * the FP32 state: on != 0 (the default) in the compute_rhs launch (one
+ * kernel whose blocks each do either compute_rhs points or copy tiles, the
+ * copies spread evenly over the launch), when the x-sweep work list of the
+ * launch is one line shape; 0 by a copy kernel of their own after the
+ * primitive kernel.  Launch configuration only: results are unchanged.
+ * npbmz_autotune chooses it on whole steps.  No counterpart in the
+ * reference. */
 int npbmz_set_copy_fusion(npbmz_t* h, int on);
 
 /* Use `stream` (a cudaStream_t, NULL = the legacy default stream) for all

@@ -257,7 +257,7 @@ struct npbmz_handle {
   cudaStream_t grp_stream[8] = {};
   // the x sweep's x-line-major state copies made by the compute_rhs launch
   // (k_rhs_flux_xc) instead of a kernel of their own (npbmz_set_copy_fusion)
-  bool copy_fusion = false;
+  bool copy_fusion = true;
   // the zone groups' streams of the npbmz_step_inout graph: priorities fall
   // with the group number, so that the groups finish in the order their copies
   // came in and each one's copy out starts while later groups compute

@@ -283,6 +283,8 @@ def test_copy_fusion_changes_no_result(kind, flags, groups):
         q.setup(ce)
         if flags & npbmz.GRAPH:
             q.set_step_groups(groups)
+    assert a.describe()["copy_fusion"]  # the default
+    a.set_copy_fusion(False)
     b.set_copy_fusion(True)
     assert b.describe()["copy_fusion"] and not a.describe()["copy_fusion"]
     a.step(5)
